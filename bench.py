@@ -1,0 +1,374 @@
+#!/usr/bin/env python3
+"""Scan-insertion benchmark: rays/s and voxel-updates/s on the dense street workload.
+
+One step = one insertPointCloud of a 262,144-point 128x2048 LiDAR scan
+(pcl::PointXYZ layout) into one resident map at 0.05 m voxels, max range 60 m,
+through the C ABI of libvdb_gb300.so. The scans come from the seeded
+synthetic street of vdb_mapping_gb300.workloads ("dense").
+
+  value  rays/s with the scans already in HBM (device pointers), CUDA events
+         on the map's stream around each insert, L2 flushed between steps.
+  e2e    the same through the public API with pinned HOST buffers: the
+         host-to-device copy of the scan and the device-to-host read of the
+         call's status are inside the timed region (wall clock per call).
+
+`--impl reference` times the reference's CPU path (the C++ oracle restating
+it: VDBMapping::raycastPointCloud + updateMap) on all host cores, as
+independent map replicas, for the same metric.
+
+With --gpus N > 1 (torchrun, one rank per GPU) each rank inserts the same
+scan sequence into its own map: replicas only, no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "rays/s & voxel-updates/s, batched vs plain GPU, bit-exact; p99 insert latency"
+UNIT = "rays/s"
+FALLBACK_HBM_GBS = 6800.0
+L2_FLUSH_BYTES = 256 << 20
+PCL_POINT_BYTES = 16
+STATUS_BYTES = 80  # device status block (DevStatus) read back by every call
+
+# DRAM traffic per launch of the dominant kernel, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum); None until profiled.
+NCU_TRAFFIC_BYTES = None
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="dense")
+    ap.add_argument("--cpu-scans", type=int, default=2, help="scans in the single-thread CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def measured_peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def config_block(wl, args, world):
+    return {
+        "workload": f"{wl.name}: {wl.points_per_scan} pts/scan 128x2048 LiDAR, street 200x200x20 m, "
+                    f"voxel {wl.resolution} m, max_range {wl.max_range} m",
+        "points_per_scan": wl.points_per_scan,
+        "voxel_m": wl.resolution,
+        "max_range_m": wl.max_range,
+        "scans_timed": args.steps,
+        "scans_warmup": args.warmup,
+        "point_layout": "pcl::PointXYZ 16 B",
+        "l2": "flushed between steps (256 MiB write)",
+        "parallelism": f"replicas x{world}" if world > 1 else "single map",
+    }
+
+
+# --------------------------------------------------------------------------
+# Reference arm: the CPU path on all host cores
+# --------------------------------------------------------------------------
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import numpy as np
+    import oracle as O
+
+    from vdb_mapping_gb300 import workloads as W
+
+    wl = W.get(args.workload)
+    threads = os.cpu_count() or 1
+    slice_rays = 32768  # bounded sample per thread and step
+    n_src = max(1, min(args.steps + args.warmup, 4))
+    scans = [wl.scan(k) for k in range(n_src)]
+    times, rays = [], 0
+    for step in range(args.warmup + args.steps):
+        pts, org = scans[step % n_src]
+        off = (step * 7919) % max(1, pts.shape[0] - slice_rays)
+        sample = pts[off:off + slice_rays][None, :, :3]
+        sec, _ = O.bench_replicas(wl.resolution, wl.config, sample, np.asarray([org]), threads)
+        if step >= args.warmup:
+            times.append(sec)
+            rays += threads * slice_rays
+    total = sum(times)
+    value = rays / total
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded street scene, no dataset)",
+        "config": config_block(wl, args, world),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{threads} independent CPU maps (one per thread), each inserting a "
+                                   f"{slice_rays}-ray slice of a {wl.name} scan per step; the C++ oracle "
+                                   f"restating raycastPointCloud+updateMap, -O2, single-threaded per map like "
+                                   f"the reference"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# --------------------------------------------------------------------------
+# Our arm
+# --------------------------------------------------------------------------
+
+def cpu_baseline_single(wl, scans, n):
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle as O
+
+    m = O.OracleMap(wl.resolution)
+    m.setConfig(wl.config)
+    m.addInputSource("lidar", wl.max_range, 0)
+    t0 = time.perf_counter()
+    rays = 0
+    for pts, org in scans[:n]:
+        m.insertPointCloud(pts, org, "lidar")
+        rays += pts.shape[0]
+    sec = time.perf_counter() - t0
+    return {"value": rays / sec, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{wl.name} scans 0-{n - 1} ({rays} rays) into a fresh map, one thread, C++ oracle "
+                      f"restating the reference path (-O2, no FMA contraction)"}
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from vdb_mapping_gb300 import OccupancyVDBMapping
+    from vdb_mapping_gb300 import workloads as W
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    wl = W.get(args.workload)
+    n_scans = args.warmup + args.steps
+    scans = [wl.scan(k % wl.n_scans) for k in range(n_scans)]
+    n_pts = scans[0][0].shape[0]
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    cap = 1 << 22
+
+    def new_map():
+        m = OccupancyVDBMapping(wl.resolution, initial_leaf_capacity=cap, device=local)
+        m.setConfig(wl.config)
+        m.addInputSource("lidar", wl.max_range, 0)
+        return m
+
+    # ---- device-resident run -------------------------------------------------
+    dev_pts = [torch.from_numpy(p).cuda() for p, _ in scans]
+    torch.cuda.synchronize()
+    m = new_map()
+    for k in range(args.warmup):
+        m.insertPointCloud(dev_pts[k], scans[k][1], "lidar", stream=sh)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stats, phases = [], []
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    wall0 = time.perf_counter()
+    for i in range(args.steps):
+        k = args.warmup + i
+        flush.zero_()
+        ev[i][0].record(stream)
+        m.insertPointCloud(dev_pts[k], scans[k][1], "lidar", stream=sh)
+        ev[i][1].record(stream)
+        stats.append(dict(m.last_stats))
+        phases.append(m.timings())
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = sum(step_ms) / 1000.0
+    if dist:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    rays = args.steps * n_pts * world
+    updates = sum(s["updates"] for s in stats) * world
+    value = rays / total_s
+    launches = sum(p["launches"] for p in phases)
+
+    # ---- roofline of the dominant kernel (live event times) -------------------
+    hbm_peak, peak_kind = measured_peaks()
+    dda = statistics.mean(p["dda_ms"] for p in phases)
+    sweep = statistics.mean(p["sweep_ms"] for p in phases)
+    prep = statistics.mean(p["prep_ms"] for p in phases)
+    mean_u = statistics.mean(s["updates"] for s in stats)
+    mean_lt = statistics.mean(s["touched_leaves"] for s in stats)
+    # Algorithmic bytes per launch (SURVEY 8d units): sweep = FP32 read+write per
+    # updated voxel + active bit r/w + visited/hit masks per touched leaf; DDA =
+    # ray record + order index per ray + one mask line per touched leaf; prep =
+    # point read + ray record write.
+    alg = {
+        "k_sweep": (8.25 * mean_u + 128.0 * mean_lt, sweep),
+        "k_dda_mark": (20.0 * n_pts + 128.0 * mean_lt, dda),
+        "prep (k_prep+k_scan+k_scatter)": (36.0 * n_pts, prep),
+    }
+    dom = max(alg, key=lambda k: alg[k][1])
+    dom_bytes, dom_ms = alg[dom]
+    achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
+    window_bytes = 12.0 * n_pts + 8.25 * mean_u + 128.0 * mean_lt
+    mean_total_ms = statistics.mean(p["total_ms"] for p in phases)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 DDA / f32 log-odds",
+        "data": "synthetic (seeded street scene, no dataset)",
+        "config": config_block(wl, args, world),
+        "voxel_updates_per_s": updates / total_s,
+        "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
+                       "max": max(step_ms)},
+        "phases_ms": {"prep": prep, "dda_mark": dda, "sweep": sweep, "kernels_total": mean_total_ms},
+        "per_scan": {"rays": n_pts, "visits": statistics.mean(s["visits"] for s in stats),
+                     "updates": mean_u, "touched_leaves": mean_lt,
+                     "new_leaves": statistics.mean(s["new_leaves"] for s in stats)},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+                     "traffic": NCU_TRAFFIC_BYTES,
+                     "algorithmic_bytes_per_launch": dom_bytes, "launch_ms": dom_ms,
+                     "window_GBps": window_bytes / (mean_total_ms / 1000.0) / 1e9},
+        "gpu_launches": launches,
+        "wall_s_timed_region": wall,
+        "map_leaves": m.leafCount(),
+    }
+    if clk:
+        line["clocks"] = clk
+
+    # ---- end to end through the public API with pinned host buffers ----------
+    if not args.no_e2e:
+        host_pts = [torch.from_numpy(p).pin_memory() for p, _ in scans]
+        del m
+        torch.cuda.synchronize()
+        m2 = new_map()
+        for k in range(args.warmup):
+            m2.insertPointCloud(host_pts[k].numpy(), scans[k][1], "lidar")
+        e2e_t = []
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            k = args.warmup + i
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            m2.insertPointCloud(host_pts[k].numpy(), scans[k][1], "lidar")
+            e2e_t.append(time.perf_counter() - t0)
+        e2e_s = sum(e2e_t)
+        if dist:
+            t = torch.tensor([e2e_s], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        line["e2e"] = {"value": rays / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n_pts * PCL_POINT_BYTES,
+                       "d2h_bytes_per_step": STATUS_BYTES,
+                       "latency_ms": {"p50": 1000 * float(np.percentile(e2e_t, 50)),
+                                      "p99": 1000 * float(np.percentile(e2e_t, 99))}}
+        del m2
+
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_single(wl, scans, min(args.cpu_scans, len(scans)))
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

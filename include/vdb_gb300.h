@@ -1,0 +1,171 @@
+/* vdb_gb300.h — C ABI of the GB300 scan-insertion library (libvdb_gb300.so).
+ *
+ * The reference (vdb_mapping) is a header-only C++ class template with no C
+ * ABI; this interface is the boundary its C++ API (include/vdb_mapping/*.hpp
+ * in this repository) and any FFI binding call into. Plain pointers, sizes
+ * and int status codes only; no exceptions cross it. Every entry point names
+ * the reference member it replaces (paths relative to the vdb_mapping tree).
+ *
+ * Threading: one map may be used from one host thread at a time. All calls
+ * that launch GPU work are synchronous unless stated otherwise: they return
+ * after the work on the map's stream has completed.
+ */
+#ifndef VDB_GB300_H
+#define VDB_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct vdbg_map vdbg_map;
+
+/* Status codes. 1-5 mirror the reference's print-and-return paths. */
+enum vdbg_status
+{
+  VDBG_OK                   = 0,
+  VDBG_ERR_NOT_CONFIGURED   = 1,  /* raycast before setConfig (VDBMapping.hpp:478-482) */
+  VDBG_ERR_UNKNOWN_SOURCE   = 2,  /* source id not registered (VDBMapping.hpp:321-325) */
+  VDBG_ERR_BAD_RANGE        = 3,  /* negative max_range (VDBMapping.hpp:1458-1463) */
+  VDBG_ERR_BAD_PROBABILITY  = 4,  /* prob_miss > 0.5 or prob_hit < 0.5 (OccupancyVDBMapping.hpp:65-76) */
+  VDBG_ERR_DUPLICATE_SOURCE = 5,  /* source id registered twice */
+  VDBG_ERR_INVALID_ARGUMENT = 6,
+  VDBG_ERR_OUT_OF_MEMORY    = 7,  /* device allocation failed or memory budget reached */
+  VDBG_ERR_COORD_RANGE      = 8,  /* a voxel index outside [-2^23, 2^23) on some axis */
+  VDBG_ERR_CUDA             = 9,
+  VDBG_ERR_TIMEOUT          = 10, /* a bounded device wait gave up */
+  VDBG_ERR_BUFFER_TOO_SMALL = 11
+};
+
+/* Input flags. */
+#define VDBG_POINTS_DEVICE 1u /* xyz points to device memory (default: host memory) */
+
+/* vdb_mapping::Config (OccupancyVDBMapping.hpp:38-44) with its BaseConfig
+ * (VDBMapping.hpp:64-71); map_directory_path is not part of the path. */
+typedef struct vdbg_config
+{
+  double max_range;
+  int32_t fast_mode;
+  int32_t reserved0;
+  double accumulation_period;
+  double prob_hit;
+  double prob_miss;
+  double prob_thres_min;
+  double prob_thres_max;
+} vdbg_config;
+
+/* Map creation options (no counterpart in the reference). Zero fields take
+ * defaults. */
+typedef struct vdbg_options
+{
+  int64_t initial_leaf_capacity; /* leaf pool slots to reserve (default 65536) */
+  int64_t max_device_bytes;      /* growth budget for this map (0 = unlimited) */
+  int32_t device;                /* CUDA device ordinal (default current) */
+  int32_t reserved0;
+} vdbg_options;
+
+/* Counters of one call (accumulate, integrate or insert). */
+typedef struct vdbg_scan_stats
+{
+  uint64_t rays;           /* points cast (NaN points are skipped) */
+  uint64_t visits;         /* DDA voxel visits plus endpoint hit marks */
+  uint64_t hits;           /* unclipped endpoints */
+  uint64_t updates;        /* update-grid voxels applied to the map (updateMap iterations) */
+  uint64_t new_leaves;     /* 8^3 map leaves created */
+  uint64_t touched_leaves; /* leaves swept by the integration */
+  uint64_t skipped_nonfinite; /* +-inf points skipped (undefined in the reference) */
+  double device_ms;        /* device time of the call's kernels */
+} vdbg_scan_stats;
+
+/* VDBMapping(double resolution) VDBMapping.hpp:115-134 / OccupancyVDBMapping.hpp:49. */
+int vdbg_create(double resolution, const vdbg_options* options, vdbg_map** out);
+
+/* ~VDBMapping VDBMapping.hpp:139-154. */
+int vdbg_destroy(vdbg_map* map);
+
+/* OccupancyVDBMapping::setConfig OccupancyVDBMapping.hpp:59-89 over
+ * VDBMapping::setConfig VDBMapping.hpp:1456-1469. Returns BAD_RANGE (nothing
+ * changed) or BAD_PROBABILITY (range applied, log-odds kept) like the
+ * reference's early returns. */
+int vdbg_set_config(vdbg_map* map, const vdbg_config* config);
+
+/* Log-odds constants in use: hit, miss, thres_min, thres_max, max, min. */
+int vdbg_get_log_odds(const vdbg_map* map, float out6[6]);
+
+/* VDBMapping::addInputSource VDBMapping.hpp:1352-1375 (max_range 0 selects
+ * the configured max_range; no worker thread is started). */
+int vdbg_add_input_source(vdbg_map* map, const char* source_id, double max_range, double max_rate);
+
+/* VDBMapping::insertPointCloud VDBMapping.hpp:399-406: accumulate this cloud
+ * into the source's update grid, then integrate every source. `xyz` holds n
+ * points of three floats at `stride_bytes` spacing (16 for pcl::PointXYZ).
+ * An unknown source or missing config returns its status after still running
+ * the integration, as the reference does. `stream` is a cudaStream_t or NULL
+ * for the map's own stream. */
+int vdbg_insert_point_cloud(vdbg_map* map, const float* xyz, int64_t n, int64_t stride_bytes,
+                            const double origin[3], const char* source_id, uint32_t flags,
+                            void* stream, vdbg_scan_stats* stats);
+
+/* VDBMapping::accumulateUpdate VDBMapping.hpp:316-346. */
+int vdbg_accumulate_update(vdbg_map* map, const float* xyz, int64_t n, int64_t stride_bytes,
+                           const double origin[3], const char* source_id, uint32_t flags,
+                           void* stream, vdbg_scan_stats* stats);
+
+/* VDBMapping::integrateUpdate VDBMapping.hpp:375-387: every source's update
+ * grid, in source-id order, then fresh update grids. */
+int vdbg_integrate_update(vdbg_map* map, void* stream, vdbg_scan_stats* stats);
+
+/* VDBMapping::raycastPointCloud VDBMapping.hpp:466-539 with fast_mode off,
+ * into the update grid of `source_id` with an explicit raycast range. */
+int vdbg_raycast_point_cloud(vdbg_map* map, const float* xyz, int64_t n, int64_t stride_bytes,
+                             const double origin[3], double raycast_range, const char* source_id,
+                             uint32_t flags, void* stream, vdbg_scan_stats* stats);
+
+/* VDBMapping::updateMap VDBMapping.hpp:731-792 for one source's update grid,
+ * which is then emptied. */
+int vdbg_update_map(vdbg_map* map, const char* source_id, void* stream, vdbg_scan_stats* stats);
+
+/* VDBMapping::resetMap VDBMapping.hpp:174-186. */
+int vdbg_reset_map(vdbg_map* map);
+
+/* Number of 8^3 leaves in the map (VDBMapping::getGrid()->tree().leafCount()). */
+int vdbg_leaf_count(vdbg_map* map, int64_t* out);
+
+/* VDBMapping::getGrid VDBMapping.hpp:799, as an export: the map's leaves
+ * sorted by origin (x, then y, then z). origins: int32[capacity][3] leaf
+ * origins (multiples of 8); values: float[capacity][512] log-odds in OpenVDB
+ * leaf order (offset = (x&7)<<6 | (y&7)<<3 | (z&7)); masks: uint64[capacity][8]
+ * value (active) masks, bit i of word w = voxel offset 64*w+i. Any of the
+ * three may be NULL. Returns BUFFER_TOO_SMALL (and the needed count in
+ * *n_out) if capacity is too small. */
+int vdbg_export_leaves(vdbg_map* map, int64_t capacity, int32_t* origins, float* values,
+                       uint64_t* masks, int64_t* n_out);
+
+/* Device-side timing of the last call (no counterpart in the reference),
+ * from CUDA events recorded on the call's stream between its kernels. */
+typedef struct vdbg_timings
+{
+  double prep_ms;   /* clip + quantise + L1 bucket sort of the rays */
+  double dda_ms;    /* DDA traversal and update-mask marking */
+  double sweep_ms;  /* log-odds sweep over the touched leaves */
+  double total_ms;  /* first to last kernel of the call */
+  uint64_t launches;       /* kernels launched by the call */
+  uint64_t launches_total; /* kernels launched by this map since creation */
+  uint64_t retries;        /* re-marking passes after a pool or hash growth */
+  uint64_t reserved0;
+} vdbg_timings;
+
+int vdbg_get_timings(const vdbg_map* map, vdbg_timings* out);
+
+/* Device bytes held by the map. */
+int vdbg_device_bytes(const vdbg_map* map, int64_t* out);
+
+/* Human-readable text of a status code (static storage). */
+const char* vdbg_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VDB_GB300_H */

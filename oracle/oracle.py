@@ -1,0 +1,179 @@
+"""ctypes face of the CPU oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
+by bench.py's CPU-baseline legs, as the checker. The product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    lib = C.CDLL(LIB)
+    P, D, I64, U64P = C.c_void_p, C.c_double, C.c_int64, C.POINTER(C.c_uint64)
+    sig = {
+        "vo_create": (P, [D, C.c_int, C.c_int]),
+        "vo_destroy": (None, [P]),
+        "vo_set_config": (C.c_int, [P, D, C.c_int, D, D, D, D, D]),
+        "vo_add_source": (C.c_int, [P, C.c_char_p, D, D]),
+        "vo_insert": (C.c_int, [P, P, I64, I64, C.POINTER(D), C.c_char_p, U64P]),
+        "vo_accumulate": (C.c_int, [P, P, I64, I64, C.POINTER(D), C.c_char_p, U64P]),
+        "vo_integrate": (None, [P, U64P]),
+        "vo_reset": (None, [P]),
+        "vo_leaf_count": (I64, [P]),
+        "vo_active_count": (I64, [P]),
+        "vo_export": (None, [P, P, P, P]),
+        "vo_get_value": (C.c_float, [P, C.c_int32, C.c_int32, C.c_int32]),
+        "vo_is_value_on": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32]),
+        "vo_log_odds": (None, [P, C.POINTER(C.c_float)]),
+        "vo_cast_ray": (I64, [P, P, P, I64]),
+        "vo_world_to_index": (None, [D, C.POINTER(D), P, C.c_int]),
+        "vo_clip_quantise": (None, [P, I64, I64, C.POINTER(D), D, D, P]),
+        "vo_bench_replicas": (D, [D, C.POINTER(D), P, I64, I64, I64, C.POINTER(D), C.c_int, U64P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+STAT_KEYS = ("rays", "visits", "hits", "updates", "new_leaves")
+
+
+def _cloud(cloud):
+    arr = np.asarray(cloud, dtype=np.float32)
+    if arr.ndim != 2 or arr.shape[1] < 3:
+        raise ValueError("cloud must be (N, 3+)")
+    arr = np.ascontiguousarray(arr)
+    return arr, arr.shape[0], arr.shape[1]
+
+
+def _d3(v):
+    return (C.c_double * 3)(*[float(x) for x in v])
+
+
+class OracleMap:
+    """OccupancyVDBMapping semantics on the CPU (see vdb_oracle.hpp)."""
+
+    def __init__(self, resolution, w2i_divide=False, unit_reciprocal=False):
+        self._l = load()
+        self._h = self._l.vo_create(float(resolution), int(w2i_divide), int(unit_reciprocal))
+        self.resolution = float(resolution)
+        self.last_stats = None
+
+    def __del__(self):
+        try:
+            self._l.vo_destroy(self._h)
+        except Exception:
+            pass
+
+    def setConfig(self, c) -> int:
+        return self._l.vo_set_config(self._h, c.max_range, int(c.fast_mode), c.accumulation_period,
+                                     c.prob_hit, c.prob_miss, c.prob_thres_min, c.prob_thres_max)
+
+    def addInputSource(self, sid, max_range, max_rate) -> int:
+        return self._l.vo_add_source(self._h, sid.encode(), float(max_range), float(max_rate))
+
+    def _call(self, fn, cloud, origin, sid):
+        arr, n, stride = _cloud(cloud)
+        st = (C.c_uint64 * 5)()
+        r = fn(self._h, arr.ctypes.data, n, stride, _d3(origin), sid.encode(), st)
+        self.last_stats = dict(zip(STAT_KEYS, list(st)))
+        return r
+
+    def insertPointCloud(self, cloud, origin, sid) -> int:
+        return self._call(self._l.vo_insert, cloud, origin, sid)
+
+    def accumulateUpdate(self, cloud, origin, sid) -> int:
+        return self._call(self._l.vo_accumulate, cloud, origin, sid)
+
+    def integrateUpdate(self):
+        st = (C.c_uint64 * 5)()
+        self._l.vo_integrate(self._h, st)
+        self.last_stats = dict(zip(STAT_KEYS, list(st)))
+
+    def resetMap(self):
+        self._l.vo_reset(self._h)
+
+    def leafCount(self) -> int:
+        return self._l.vo_leaf_count(self._h)
+
+    def activeVoxelCount(self) -> int:
+        return self._l.vo_active_count(self._h)
+
+    def exportLeaves(self):
+        n = self.leafCount()
+        origins = np.zeros((n, 3), np.int32)
+        values = np.zeros((n, 512), np.float32)
+        masks = np.zeros((n, 8), np.uint64)
+        self._l.vo_export(self._h, origins.ctypes.data, values.ctypes.data, masks.ctypes.data)
+        return origins, values, masks
+
+    def getValue(self, xyz) -> float:
+        return self._l.vo_get_value(self._h, *[int(c) for c in xyz])
+
+    def isValueOn(self, xyz) -> bool:
+        return bool(self._l.vo_is_value_on(self._h, *[int(c) for c in xyz]))
+
+    def logOdds(self):
+        out = (C.c_float * 2)()
+        self._l.vo_log_odds(self._h, out)
+        return {"hit": out[0], "miss": out[1]}
+
+
+def cast_ray(o, e, cap=1 << 20):
+    """Voxels castRayIntoGrid visits from voxel o to voxel e, in order."""
+    lib = load()
+    oo = np.asarray(o, np.int32)
+    ee = np.asarray(e, np.int32)
+    out = np.zeros((cap, 3), np.int32)
+    n = lib.vo_cast_ray(oo.ctypes.data, ee.ctypes.data, out.ctypes.data, cap)
+    if n > cap:
+        return cast_ray(o, e, cap=int(n))
+    return out[:n].copy()
+
+
+def world_to_index(res, w, divide=False):
+    lib = load()
+    out = np.zeros(3, np.int32)
+    lib.vo_world_to_index(float(res), _d3(w), out.ctypes.data, int(divide))
+    return tuple(int(v) for v in out)
+
+
+def clip_quantise(cloud, origin, max_range, res):
+    """int32 (N,5): valid, clipped, end voxel xyz."""
+    lib = load()
+    arr, n, stride = _cloud(cloud)
+    rec = np.zeros((n, 5), np.int32)
+    lib.vo_clip_quantise(arr.ctypes.data, n, stride, _d3(origin), float(max_range), float(res),
+                         rec.ctypes.data)
+    return rec
+
+
+def bench_replicas(res, cfg, scans, origins, threads):
+    """Wall seconds for `threads` independent CPU maps each inserting all scans."""
+    lib = load()
+    scans = np.ascontiguousarray(np.asarray(scans, np.float32))
+    s, n, k = scans.shape
+    origins = np.ascontiguousarray(np.asarray(origins, np.float64))
+    cfg7 = (C.c_double * 7)(cfg.max_range, float(cfg.fast_mode), cfg.accumulation_period, cfg.prob_hit,
+                            cfg.prob_miss, cfg.prob_thres_min, cfg.prob_thres_max)
+    st = (C.c_uint64 * 5)()
+    sec = lib.vo_bench_replicas(float(res), cfg7, scans.ctypes.data, s, n, k,
+                                origins.ctypes.data_as(C.POINTER(C.c_double)), int(threads), st)
+    return sec, dict(zip(STAT_KEYS, list(st)))

@@ -1,0 +1,210 @@
+// oracle_capi.cpp — extern "C" face of the CPU oracle (vdb_oracle.hpp) for
+// ctypes. TEST INFRASTRUCTURE ONLY: loaded by tests/, by the smoke check and
+// by bench.py's CPU-baseline legs, never by the product library.
+#include "vdb_oracle.hpp"
+
+#include <chrono>
+#include <thread>
+
+using namespace vdb_oracle;
+
+namespace {
+struct Handle
+{
+  OccupancyMap map;
+  explicit Handle(double res, Variant v) : map(res, v) {}
+};
+inline void put_stats(const ScanStats& s, uint64_t* out)
+{
+  if (!out) return;
+  out[0] = s.rays;
+  out[1] = s.visits;
+  out[2] = s.hits;
+  out[3] = s.updates;
+  out[4] = s.new_leaves;
+}
+} // namespace
+
+extern "C" {
+
+void* vo_create(double resolution, int w2i_divide, int unit_reciprocal)
+{
+  Variant v;
+  v.w2i_divide      = w2i_divide != 0;
+  v.unit_reciprocal = unit_reciprocal != 0;
+  return new Handle(resolution, v);
+}
+
+void vo_destroy(void* h) { delete static_cast<Handle*>(h); }
+
+int vo_set_config(void* h, double max_range, int fast_mode, double accumulation_period,
+                  double prob_hit, double prob_miss, double prob_thres_min, double prob_thres_max)
+{
+  Config c;
+  c.max_range           = max_range;
+  c.fast_mode           = fast_mode != 0;
+  c.accumulation_period = accumulation_period;
+  c.prob_hit            = prob_hit;
+  c.prob_miss           = prob_miss;
+  c.prob_thres_min      = prob_thres_min;
+  c.prob_thres_max      = prob_thres_max;
+  return static_cast<Handle*>(h)->map.set_config(c);
+}
+
+int vo_add_source(void* h, const char* id, double max_range, double max_rate)
+{
+  return static_cast<Handle*>(h)->map.add_input_source(id, max_range, max_rate);
+}
+
+int vo_insert(void* h, const float* xyz, int64_t n, int64_t stride_floats, const double* origin,
+              const char* id, uint64_t* stats)
+{
+  ScanStats s;
+  const int r = static_cast<Handle*>(h)->map.insert_point_cloud(
+    xyz, static_cast<size_t>(n), static_cast<size_t>(stride_floats), origin, id, &s);
+  put_stats(s, stats);
+  return r;
+}
+
+int vo_accumulate(void* h, const float* xyz, int64_t n, int64_t stride_floats, const double* origin,
+                  const char* id, uint64_t* stats)
+{
+  ScanStats s;
+  const int r = static_cast<Handle*>(h)->map.accumulate_update(
+    xyz, static_cast<size_t>(n), static_cast<size_t>(stride_floats), origin, id, &s);
+  put_stats(s, stats);
+  return r;
+}
+
+void vo_integrate(void* h, uint64_t* stats)
+{
+  ScanStats s;
+  static_cast<Handle*>(h)->map.integrate_update(&s);
+  put_stats(s, stats);
+}
+
+void vo_reset(void* h) { static_cast<Handle*>(h)->map.reset_map(); }
+
+int64_t vo_leaf_count(void* h)
+{
+  return static_cast<int64_t>(static_cast<Handle*>(h)->map.map().leaf_count());
+}
+
+int64_t vo_active_count(void* h)
+{
+  return static_cast<int64_t>(static_cast<Handle*>(h)->map.map().active_voxel_count());
+}
+
+// Leaves sorted by origin: origins[L][3], values[L][512], masks[L][8].
+void vo_export(void* h, int32_t* origins, float* values, uint64_t* masks)
+{
+  const auto leaves = static_cast<Handle*>(h)->map.map().sorted_leaves();
+  for (size_t i = 0; i < leaves.size(); ++i)
+  {
+    origins[3 * i + 0] = leaves[i]->origin.x;
+    origins[3 * i + 1] = leaves[i]->origin.y;
+    origins[3 * i + 2] = leaves[i]->origin.z;
+    std::memcpy(values + 512 * i, leaves[i]->value, 512 * sizeof(float));
+    std::memcpy(masks + 8 * i, leaves[i]->on, 8 * sizeof(uint64_t));
+  }
+}
+
+float vo_get_value(void* h, int32_t x, int32_t y, int32_t z)
+{
+  return static_cast<Handle*>(h)->map.map().get_value(Coord(x, y, z));
+}
+
+int vo_is_value_on(void* h, int32_t x, int32_t y, int32_t z)
+{
+  return static_cast<Handle*>(h)->map.map().is_value_on(Coord(x, y, z)) ? 1 : 0;
+}
+
+void vo_log_odds(void* h, float* out2)
+{
+  out2[0] = static_cast<Handle*>(h)->map.lo_hit();
+  out2[1] = static_cast<Handle*>(h)->map.lo_miss();
+}
+
+// Voxels visited by castRayIntoGrid from o to e, in visiting order. Returns the
+// count; writes at most `cap` voxels.
+int64_t vo_cast_ray(const int32_t* o, const int32_t* e, int32_t* out, int64_t cap)
+{
+  int64_t n = 0;
+  cast_ray(Coord(o[0], o[1], o[2]), Coord(e[0], e[1], e[2]), [&](const Coord& v) {
+    if (n < cap)
+    {
+      out[3 * n + 0] = v.x;
+      out[3 * n + 1] = v.y;
+      out[3 * n + 2] = v.z;
+    }
+    ++n;
+  });
+  return n;
+}
+
+void vo_world_to_index(double res, const double* w, int32_t* out, int w2i_divide)
+{
+  Variant v;
+  v.w2i_divide  = w2i_divide != 0;
+  const Coord c = world_to_index(w, res, v);
+  out[0]        = c.x;
+  out[1]        = c.y;
+  out[2]        = c.z;
+}
+
+// Per point: valid, clipped, end voxel (x,y,z). rec is int32[n][5].
+void vo_clip_quantise(const float* xyz, int64_t n, int64_t stride_floats, const double* origin,
+                      double range, double res, int32_t* rec)
+{
+  for (int64_t i = 0; i < n; ++i)
+  {
+    const float* p  = xyz + i * stride_floats;
+    const RayEnd re = clip_and_quantise(origin, p[0], p[1], p[2], range, res);
+    rec[5 * i + 0]  = re.valid ? 1 : 0;
+    rec[5 * i + 1]  = re.clipped ? 1 : 0;
+    rec[5 * i + 2]  = re.end.x;
+    rec[5 * i + 3]  = re.end.y;
+    rec[5 * i + 4]  = re.end.z;
+  }
+}
+
+// CPU baseline: `threads` independent maps (one per thread), each inserting
+// the same `n_scans` scans in order through insert_point_cloud. Points are
+// xyz float triplets with `stride_floats` spacing, scan s starting at
+// xyz + s * n_pts * stride_floats, origin at origins + 3 * s. Returns the
+// wall-clock seconds; per-scan stats of thread 0 are summed into `stats`.
+double vo_bench_replicas(double res, const double* cfg7, const float* xyz, int64_t n_scans,
+                         int64_t n_pts, int64_t stride_floats, const double* origins, int threads,
+                         uint64_t* stats)
+{
+  Config c;
+  c.max_range      = cfg7[0];
+  c.fast_mode      = cfg7[1] != 0.0;
+  c.accumulation_period = cfg7[2];
+  c.prob_hit       = cfg7[3];
+  c.prob_miss      = cfg7[4];
+  c.prob_thres_min = cfg7[5];
+  c.prob_thres_max = cfg7[6];
+  if (threads < 1) threads = 1;
+  std::vector<ScanStats> st(static_cast<size_t>(threads));
+  auto work = [&](int t) {
+    OccupancyMap m(res);
+    m.set_config(c);
+    m.add_input_source("bench", c.max_range, 0);
+    for (int64_t s = 0; s < n_scans; ++s)
+    {
+      m.insert_point_cloud(xyz + s * n_pts * stride_floats, static_cast<size_t>(n_pts),
+                           static_cast<size_t>(stride_floats), origins + 3 * s, "bench", &st[t]);
+    }
+  };
+  const auto t0 = std::chrono::steady_clock::now();
+  std::vector<std::thread> pool;
+  for (int t = 1; t < threads; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto& th : pool) th.join();
+  const auto t1 = std::chrono::steady_clock::now();
+  put_stats(st[0], stats);
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
+} // extern "C"

@@ -1,0 +1,697 @@
+// vdb_oracle.hpp — CPU restatement of vdb_mapping's scan-insertion path.
+//
+// TEST INFRASTRUCTURE ONLY. This header is the checker that the CUDA library
+// is compared against. Only tests/, __graft_entry__.smoke() and bench.py's CPU
+// baseline legs may load it; the product library never links it.
+//
+// It restates, in plain single-threaded C++17 compiled with
+// -ffp-contract=off, the following reference code (paths relative to the
+// vdb_mapping project):
+//   include/vdb_mapping/VDBMapping.hpp:466-539    raycastPointCloud
+//   include/vdb_mapping/VDBMapping.hpp:550-566    castRayIntoGrid
+//   include/vdb_mapping/VDBMapping.hpp:612-631    worldToIndex
+//   include/vdb_mapping/VDBMapping.hpp:731-792    updateMap
+//   include/vdb_mapping/VDBMapping.hpp:316-406    accumulate / integrate / insert
+//   include/vdb_mapping/VDBMapping.hpp:1352-1375  addInputSource
+//   include/vdb_mapping/VDBMapping.hpp:1456-1469  VDBMapping::setConfig
+//   include/vdb_mapping/OccupancyVDBMapping.hpp:59-117  log-odds constants and node updates
+// plus the OpenVDB arithmetic those lines call (OpenVDB is a third-party
+// dependency that is not vendored in the reference; README.md:11 asks for
+// OpenVDB >= 8.3, no exact version is pinned):
+//   math::Ray<double>        eye/dir stored as given, invDir = 1/dir per component
+//   math::DDA<Ray<double>,0> init and step(): argmin of the three tMax values,
+//                            ties resolved to the higher axis (z over y over x),
+//                            sequential `tMax += tDelta`, continue while t <= t1
+//   Transform::createLinearTransform(res)  world->index = w * (1/res)
+//   Coord::floor             int(floor(x))
+//   Vec3d::length / unit     sqrt((x*x + y*y) + z*z), component-wise division
+//   Tree4<.,5,4,3> leaves    8^3 voxels, offset = (x&7)<<6 | (y&7)<<3 | (z&7),
+//                            background 0.0f, leaves are never pruned here
+//
+// Parity pins: the reference's own tests/mapping.cpp compiles unmodified
+// against oracle/refshim (this header behind the reference class names) and
+// all of its assertions pass; hand-derived known-answer cases in
+// tests/test_oracle.py pin the parts those tests leave open (DDA ties,
+// off-axis rays, hit-over-miss dedup, clamp and hysteresis).
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace vdb_oracle {
+
+struct Coord
+{
+  int32_t x = 0, y = 0, z = 0;
+  Coord() = default;
+  Coord(int32_t x_, int32_t y_, int32_t z_) : x(x_), y(y_), z(z_) {}
+  int32_t operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+  int32_t& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+  bool operator==(const Coord& o) const { return x == o.x && y == o.y && z == o.z; }
+  bool operator!=(const Coord& o) const { return !(*this == o); }
+  bool operator<(const Coord& o) const
+  {
+    if (x != o.x) return x < o.x;
+    if (y != o.y) return y < o.y;
+    return z < o.z;
+  }
+};
+
+// Arithmetic variants used only for the sensitivity report: how many voxels
+// would change if OpenVDB's linear map divided by the voxel size instead of
+// multiplying by its inverse, or if Vec3d::unit multiplied by 1/length.
+struct Variant
+{
+  bool w2i_divide      = false;
+  bool unit_reciprocal = false;
+};
+
+// Leaf geometry of Tree4<T,5,4,3>: 8^3 voxels per leaf.
+inline Coord leaf_origin(const Coord& v) { return Coord(v.x & ~7, v.y & ~7, v.z & ~7); }
+inline uint32_t leaf_offset(const Coord& v)
+{
+  return (uint32_t(v.x & 7) << 6) | (uint32_t(v.y & 7) << 3) | uint32_t(v.z & 7);
+}
+
+// VDBMapping.hpp:612-631. Per axis: a coordinate that is not an exact multiple
+// of the resolution (std::fmod != 0, NaN counts as non-zero) is shifted by
+// res/2, then mapped to index space by the linear transform (w * (1/res)) and
+// floored.
+inline Coord world_to_index(const double w_in[3], double res, const Variant& var = Variant())
+{
+  const double inv_res = 1.0 / res;
+  Coord out;
+  for (int i = 0; i < 3; ++i)
+  {
+    double w = w_in[i];
+    if (std::fmod(w, res) != 0.0)
+    {
+      w = w + (res / 2.0);
+    }
+    const double idx = var.w2i_divide ? (w / res) : (w * inv_res);
+    out[i]           = static_cast<int32_t>(std::floor(idx));
+  }
+  return out;
+}
+
+// Index of the smallest of three values; equal values resolve to the higher
+// index (OpenVDB math::MinIndex semantics, used by DDA::step).
+inline int argmin3_high_ties(const double v[3])
+{
+  int a = 2;
+  if (v[1] < v[a]) a = 1;
+  if (v[0] < v[a]) a = 0;
+  return a;
+}
+
+// OpenVDB's DDA<Ray<double>,0> over the ray built in VDBMapping.hpp:554-558:
+// eye = origin voxel + 0.5, dir = end - origin (integer valued), t in [0, 1].
+struct DDA
+{
+  int32_t voxel[3];
+  int32_t step[3];
+  double next[3];
+  double delta[3];
+  double t0, t1;
+
+  DDA(const Coord& o, const Coord& e)
+  {
+    double eye[3], dir[3], inv[3];
+    for (int i = 0; i < 3; ++i)
+    {
+      eye[i] = static_cast<double>(o[i]) + 0.5;                             // asVec3d() + 0.5
+      dir[i] = static_cast<double>(e[i]) - static_cast<double>(o[i]);       // Vec3d - Coord
+      inv[i] = 1.0 / dir[i];                                                // Ray: invDir = 1/dir
+    }
+    t0 = 0.0;  // DDAT dda(ray, 0)
+    t1 = 1.0;  // RayT(..., 0, 1)
+    double pos[3];
+    for (int i = 0; i < 3; ++i)
+    {
+      pos[i]   = eye[i] + dir[i] * t0;  // ray(t0)
+      voxel[i] = static_cast<int32_t>(std::floor(pos[i]));
+    }
+    for (int i = 0; i < 3; ++i)
+    {
+      if (dir[i] == 0.0)
+      {
+        step[i]  = 0;
+        next[i]  = std::numeric_limits<double>::max();
+        delta[i] = std::numeric_limits<double>::max();
+      }
+      else if (inv[i] > 0)
+      {
+        step[i]  = 1;
+        next[i]  = t0 + (static_cast<double>(voxel[i] + 1) - pos[i]) * inv[i];
+        delta[i] = static_cast<double>(step[i]) * inv[i];
+      }
+      else
+      {
+        step[i]  = -1;
+        next[i]  = t0 + (static_cast<double>(voxel[i]) - pos[i]) * inv[i];
+        delta[i] = static_cast<double>(step[i]) * inv[i];
+      }
+    }
+  }
+
+  Coord cur() const { return Coord(voxel[0], voxel[1], voxel[2]); }
+
+  bool advance()
+  {
+    const int a = argmin3_high_ties(next);
+    t0          = next[a];
+    next[a] += delta[a];
+    voxel[a] += step[a];
+    return t0 <= t1;
+  }
+};
+
+// VDBMapping.hpp:550-566: mark every voxel the DDA visits, nothing at all when
+// the ray starts and ends in the same voxel.
+template <class F>
+inline void cast_ray(const Coord& o, const Coord& e, F&& mark)
+{
+  if (e == o) return;
+  DDA dda(o, e);
+  do
+  {
+    mark(dda.cur());
+  } while (dda.advance());
+}
+
+// Result of VDBMapping.hpp:499-519 for one point.
+struct RayEnd
+{
+  bool valid     = false;  // false: NaN point or origin (skipped), or non-finite point
+  bool clipped   = false;  // max_range_ray: the endpoint is free space, not a hit
+  bool nonfinite = false;  // +-inf coordinate: undefined in the reference, skipped here
+  Coord end;
+};
+
+// VDBMapping.hpp:501-519 for one point.
+inline RayEnd clip_and_quantise(const double o[3], float px, float py, float pz, double raycast_range,
+                                double res, const Variant& var = Variant())
+{
+  RayEnd r;
+  double e[3] = {static_cast<double>(px), static_cast<double>(py), static_cast<double>(pz)};
+  if (std::isnan(e[0]) || std::isnan(e[1]) || std::isnan(e[2]) || std::isnan(o[0]) ||
+      std::isnan(o[1]) || std::isnan(o[2]))
+  {
+    return r;
+  }
+  if (std::isinf(e[0]) || std::isinf(e[1]) || std::isinf(e[2]))
+  {
+    // The reference would floor a NaN into a Coord (undefined behaviour).
+    r.nonfinite = true;
+    return r;
+  }
+  double d[3]     = {e[0] - o[0], e[1] - o[1], e[2] - o[2]};
+  const double ln = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  if (raycast_range > 0.0 && ln > raycast_range)
+  {
+    for (int i = 0; i < 3; ++i)
+    {
+      const double u = var.unit_reciprocal ? d[i] * (1.0 / ln) : d[i] / ln;
+      e[i]           = o[i] + u * raycast_range;
+    }
+    r.clipped = true;
+  }
+  r.end   = world_to_index(e, res, var);
+  r.valid = true;
+  return r;
+}
+
+// Open-addressing map from leaf origin to a dense index.
+class LeafIndex
+{
+public:
+  LeafIndex() { rehash(1024); }
+  void clear()
+  {
+    m_count = 0;
+    m_keys.assign(1024, Coord());
+    m_vals.assign(1024, kEmpty);
+  }
+  size_t size() const { return m_count; }
+  // Returns the index for `origin`, inserting `next_index` if it is absent.
+  uint32_t find_or_insert(const Coord& origin, uint32_t next_index, bool& inserted)
+  {
+    if ((m_count + 1) * 2 > m_keys.size()) rehash(m_keys.size() * 2);
+    size_t h = hash(origin) & (m_keys.size() - 1);
+    while (true)
+    {
+      if (m_vals[h] == kEmpty)
+      {
+        m_keys[h] = origin;
+        m_vals[h] = next_index;
+        ++m_count;
+        inserted = true;
+        return next_index;
+      }
+      if (m_keys[h] == origin)
+      {
+        inserted = false;
+        return m_vals[h];
+      }
+      h = (h + 1) & (m_keys.size() - 1);
+    }
+  }
+  bool find(const Coord& origin, uint32_t& out) const
+  {
+    size_t h = hash(origin) & (m_keys.size() - 1);
+    while (true)
+    {
+      if (m_vals[h] == kEmpty) return false;
+      if (m_keys[h] == origin)
+      {
+        out = m_vals[h];
+        return true;
+      }
+      h = (h + 1) & (m_keys.size() - 1);
+    }
+  }
+
+private:
+  static constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+  static size_t hash(const Coord& c)
+  {
+    uint64_t k = (uint64_t(uint32_t(c.x)) * 0x9E3779B97F4A7C15ull) ^
+                 (uint64_t(uint32_t(c.y)) * 0xC2B2AE3D27D4EB4Full) ^
+                 (uint64_t(uint32_t(c.z)) * 0x165667B19E3779F9ull);
+    k ^= k >> 29;
+    k *= 0xBF58476D1CE4E5B9ull;
+    k ^= k >> 32;
+    return static_cast<size_t>(k);
+  }
+  void rehash(size_t cap)
+  {
+    std::vector<Coord> ok;
+    std::vector<uint32_t> ov;
+    ok.swap(m_keys);
+    ov.swap(m_vals);
+    m_keys.assign(cap, Coord());
+    m_vals.assign(cap, kEmpty);
+    for (size_t i = 0; i < ov.size(); ++i)
+    {
+      if (ov[i] == kEmpty) continue;
+      size_t h = hash(ok[i]) & (cap - 1);
+      while (m_vals[h] != kEmpty) h = (h + 1) & (cap - 1);
+      m_keys[h] = ok[i];
+      m_vals[h] = ov[i];
+    }
+  }
+  std::vector<Coord> m_keys;
+  std::vector<uint32_t> m_vals;
+  size_t m_count = 0;
+};
+
+// Tree4<bool,1,4,3> update grid (VDBMapping.hpp:89) reduced to what the path
+// uses: per voxel an active bit (touched this window) and a value bit (hit).
+struct UpdateLeaf
+{
+  Coord origin;
+  uint64_t active[8];
+  uint64_t value[8];
+};
+
+class UpdateGrid
+{
+public:
+  void clear()
+  {
+    m_index.clear();
+    m_leaves.clear();
+    m_last = nullptr;
+  }
+  bool empty() const { return m_leaves.empty(); }
+  // setActiveState(v, true): VDBMapping.hpp:563
+  void set_active(const Coord& v)
+  {
+    UpdateLeaf& l = leaf(v);
+    const uint32_t off = leaf_offset(v);
+    l.active[off >> 6] |= 1ull << (off & 63);
+  }
+  // setValueOn(v, true): VDBMapping.hpp:535
+  void set_value_on(const Coord& v)
+  {
+    UpdateLeaf& l = leaf(v);
+    const uint32_t off = leaf_offset(v);
+    l.active[off >> 6] |= 1ull << (off & 63);
+    l.value[off >> 6] |= 1ull << (off & 63);
+  }
+  const std::vector<UpdateLeaf>& leaves() const { return m_leaves; }
+  size_t active_count() const
+  {
+    size_t n = 0;
+    for (const auto& l : m_leaves)
+      for (int w = 0; w < 8; ++w) n += static_cast<size_t>(__builtin_popcountll(l.active[w]));
+    return n;
+  }
+
+private:
+  UpdateLeaf& leaf(const Coord& v)
+  {
+    const Coord o = leaf_origin(v);
+    if (m_last && m_last_origin == o) return *m_last;
+    bool inserted;
+    const uint32_t idx = m_index.find_or_insert(o, static_cast<uint32_t>(m_leaves.size()), inserted);
+    if (inserted)
+    {
+      UpdateLeaf nl;
+      nl.origin = o;
+      std::memset(nl.active, 0, sizeof(nl.active));
+      std::memset(nl.value, 0, sizeof(nl.value));
+      m_leaves.push_back(nl);
+    }
+    m_last        = &m_leaves[idx];
+    m_last_origin = o;
+    return *m_last;
+  }
+  LeafIndex m_index;
+  std::vector<UpdateLeaf> m_leaves;
+  UpdateLeaf* m_last = nullptr;
+  Coord m_last_origin;
+};
+
+// Tree4<float,5,4,3> map leaf: 512 FP32 log-odds plus the 512-bit value mask.
+struct MapLeaf
+{
+  Coord origin;
+  float value[512];
+  uint64_t on[8];
+};
+
+class FloatMap
+{
+public:
+  void clear()
+  {
+    m_index.clear();
+    m_leaves.clear();
+  }
+  bool empty() const { return m_leaves.empty(); }
+  size_t leaf_count() const { return m_leaves.size(); }
+  // Leaf for `v`, created with background 0.0f and all voxels inactive.
+  MapLeaf& touch(const Coord& v)
+  {
+    const Coord o = leaf_origin(v);
+    bool inserted;
+    const uint32_t idx = m_index.find_or_insert(o, static_cast<uint32_t>(m_leaves.size()), inserted);
+    if (inserted)
+    {
+      m_leaves.emplace_back(new MapLeaf);
+      MapLeaf& nl = *m_leaves.back();
+      nl.origin   = o;
+      std::fill(nl.value, nl.value + 512, 0.0f);
+      std::memset(nl.on, 0, sizeof(nl.on));
+    }
+    return *m_leaves[idx];
+  }
+  float get_value(const Coord& v) const
+  {
+    uint32_t idx;
+    if (!m_index.find(leaf_origin(v), idx)) return 0.0f;
+    return m_leaves[idx]->value[leaf_offset(v)];
+  }
+  bool is_value_on(const Coord& v) const
+  {
+    uint32_t idx;
+    if (!m_index.find(leaf_origin(v), idx)) return false;
+    const uint32_t off = leaf_offset(v);
+    return (m_leaves[idx]->on[off >> 6] >> (off & 63)) & 1ull;
+  }
+  size_t active_voxel_count() const
+  {
+    size_t n = 0;
+    for (const auto& l : m_leaves)
+      for (int w = 0; w < 8; ++w) n += static_cast<size_t>(__builtin_popcountll(l->on[w]));
+    return n;
+  }
+  // Leaves sorted by origin (x, then y, then z).
+  std::vector<const MapLeaf*> sorted_leaves() const
+  {
+    std::vector<const MapLeaf*> out;
+    out.reserve(m_leaves.size());
+    for (const auto& l : m_leaves) out.push_back(l.get());
+    std::sort(out.begin(), out.end(),
+              [](const MapLeaf* a, const MapLeaf* b) { return a->origin < b->origin; });
+    return out;
+  }
+
+private:
+  LeafIndex m_index;
+  std::vector<std::unique_ptr<MapLeaf> > m_leaves;
+};
+
+// Config of OccupancyVDBMapping.hpp:38-44 plus BaseConfig VDBMapping.hpp:64-71
+// (map_directory_path is irrelevant to the path and omitted).
+struct Config
+{
+  double max_range           = 0.0;
+  bool fast_mode             = false;
+  double accumulation_period = 0.0;
+  double prob_hit            = 0.0;
+  double prob_miss           = 0.0;
+  double prob_thres_min      = 0.0;
+  double prob_thres_max      = 0.0;
+};
+
+struct ScanStats
+{
+  uint64_t rays      = 0;  // valid (non-NaN) points cast
+  uint64_t visits    = 0;  // DDA voxel marks plus endpoint hit marks
+  uint64_t hits      = 0;  // unclipped endpoints
+  uint64_t updates   = 0;  // updateMap iterations (active update-grid voxels)
+  uint64_t new_leaves = 0; // map leaves created by the integration
+};
+
+enum Status : int
+{
+  kOk                = 0,
+  kNotConfigured     = 1,  // raycastPointCloud before setConfig (VDBMapping.hpp:478-482)
+  kUnknownSource     = 2,  // VDBMapping.hpp:321-325
+  kBadRange          = 3,  // negative max_range (VDBMapping.hpp:1458-1463)
+  kBadProbability    = 4,  // OccupancyVDBMapping.hpp:65-76
+  kDuplicateSource   = 5,
+};
+
+class OccupancyMap
+{
+public:
+  explicit OccupancyMap(double resolution, Variant var = Variant())
+    : m_resolution(resolution), m_var(var)
+  {
+  }
+
+  double resolution() const { return m_resolution; }
+
+  // OccupancyVDBMapping.hpp:59-89 over VDBMapping.hpp:1456-1469. As in the
+  // reference the base part marks the configuration as set before the
+  // probability checks, which may then keep the previous log-odds.
+  int set_config(const Config& c)
+  {
+    if (c.max_range < 0.0) return kBadRange;
+    m_max_range  = c.max_range;
+    m_fast_mode  = c.fast_mode;
+    m_config_set = true;
+    if (c.prob_miss > 0.5) return kBadProbability;
+    if (c.prob_hit < 0.5) return kBadProbability;
+    m_lo_miss      = static_cast<float>(std::log(c.prob_miss) - std::log(1 - c.prob_miss));
+    m_lo_hit       = static_cast<float>(std::log(c.prob_hit) - std::log(1 - c.prob_hit));
+    m_lo_thres_min = static_cast<float>(std::log(c.prob_thres_min) - std::log(1 - c.prob_thres_min));
+    m_lo_thres_max = static_cast<float>(std::log(c.prob_thres_max) - std::log(1 - c.prob_thres_max));
+    m_lo_max       = static_cast<float>(std::log(0.99) - std::log(0.01));
+    m_lo_min       = static_cast<float>(std::log(0.01) - std::log(0.99));
+    m_config_set   = true;
+    return kOk;
+  }
+
+  // VDBMapping.hpp:1352-1375 without the worker thread: a source id with a
+  // private update grid and range (0 selects the configured max_range).
+  int add_input_source(const std::string& id, double max_range, double /*max_rate*/)
+  {
+    if (m_sources.count(id)) return kDuplicateSource;
+    Source s;
+    s.max_range  = (max_range == 0) ? m_max_range : max_range;
+    m_sources[id] = std::move(s);
+    return kOk;
+  }
+
+  // VDBMapping.hpp:466-539 into `grid` (fast_mode is not part of this path).
+  int raycast_point_cloud(const float* xyz, size_t n, size_t stride_floats, const double origin[3],
+                          double raycast_range, UpdateGrid& grid, ScanStats* st = nullptr)
+  {
+    if (!m_config_set) return kNotConfigured;
+    const Coord oi = world_to_index(origin, m_resolution, m_var);
+    for (size_t i = 0; i < n; ++i)
+    {
+      const float* p  = xyz + i * stride_floats;
+      const RayEnd re = clip_and_quantise(origin, p[0], p[1], p[2], raycast_range, m_resolution, m_var);
+      if (!re.valid) continue;
+      if (st) ++st->rays;
+      cast_ray(oi, re.end, [&](const Coord& v) {
+        grid.set_active(v);
+        if (st) ++st->visits;
+      });
+      if (!re.clipped)
+      {
+        grid.set_value_on(re.end);
+        if (st)
+        {
+          ++st->visits;
+          ++st->hits;
+        }
+      }
+    }
+    return kOk;
+  }
+
+  // VDBMapping.hpp:731-792 with OccupancyVDBMapping.hpp:92-117. Returns the
+  // number of update-grid voxels applied. `change` (optional) receives the
+  // change grid: hits whose active state flipped are set on, misses whose
+  // active state flipped are marked active with value false.
+  uint64_t update_map(const UpdateGrid& grid, UpdateGrid* change = nullptr, ScanStats* st = nullptr)
+  {
+    uint64_t n = 0;
+    if (grid.empty()) return 0;
+    for (const UpdateLeaf& ul : grid.leaves())
+    {
+      const size_t before = m_map.leaf_count();
+      MapLeaf& ml         = m_map.touch(ul.origin);
+      if (st && m_map.leaf_count() != before) ++st->new_leaves;
+      for (int w = 0; w < 8; ++w)
+      {
+        uint64_t act = ul.active[w];
+        while (act)
+        {
+          const int b        = __builtin_ctzll(act);
+          act &= act - 1;
+          const uint32_t off = static_cast<uint32_t>(w * 64 + b);
+          const bool is_hit  = (ul.value[w] >> b) & 1ull;
+          float& v           = ml.value[off];
+          const bool last    = (ml.on[w] >> b) & 1ull;
+          bool active        = last;
+          if (is_hit)
+          {
+            v += m_lo_hit;
+            if (v > m_lo_thres_max)
+            {
+              active = true;
+              if (v > m_lo_max) v = m_lo_max;
+            }
+          }
+          else
+          {
+            v += m_lo_miss;
+            if (v < m_lo_thres_min)
+            {
+              active = false;
+              if (v < m_lo_min) v = m_lo_min;
+            }
+          }
+          if (active)
+            ml.on[w] |= (1ull << b);
+          else
+            ml.on[w] &= ~(1ull << b);
+          if (change && active != last)
+          {
+            const Coord c(ul.origin.x + int32_t(off >> 6), ul.origin.y + int32_t((off >> 3) & 7),
+                          ul.origin.z + int32_t(off & 7));
+            if (is_hit)
+              change->set_value_on(c);
+            else
+              change->set_active(c);
+          }
+          ++n;
+        }
+      }
+    }
+    // VDBMapping.hpp:785-789: artificial-area voxels are re-activated.
+    for (const Coord& c : m_artificial)
+    {
+      MapLeaf& ml        = m_map.touch(c);
+      const uint32_t off = leaf_offset(c);
+      ml.on[off >> 6] |= 1ull << (off & 63);
+    }
+    if (st) st->updates += n;
+    return n;
+  }
+
+  // VDBMapping.hpp:316-346.
+  int accumulate_update(const float* xyz, size_t n, size_t stride_floats, const double origin[3],
+                        const std::string& id, ScanStats* st = nullptr)
+  {
+    auto it = m_sources.find(id);
+    if (it == m_sources.end()) return kUnknownSource;
+    if (it->second.max_range > 0)
+    {
+      return raycast_point_cloud(xyz, n, stride_floats, origin, it->second.max_range,
+                                 it->second.grid, st);
+    }
+    return kOk;
+  }
+
+  // VDBMapping.hpp:375-387: every source, in source-id order.
+  void integrate_update(ScanStats* st = nullptr)
+  {
+    for (auto& kv : m_sources)
+    {
+      update_map(kv.second.grid, nullptr, st);
+      kv.second.grid.clear();
+    }
+  }
+
+  // VDBMapping.hpp:399-406: always reports success; an unknown source or a
+  // missing config only skips the accumulation.
+  int insert_point_cloud(const float* xyz, size_t n, size_t stride_floats, const double origin[3],
+                         const std::string& id, ScanStats* st = nullptr)
+  {
+    const int s = accumulate_update(xyz, n, stride_floats, origin, id, st);
+    integrate_update(st);
+    return s;
+  }
+
+  // VDBMapping.hpp:174-186.
+  void reset_map()
+  {
+    m_map.clear();
+    for (auto& kv : m_sources) kv.second.grid.clear();
+  }
+
+  void set_artificial(const std::vector<Coord>& voxels) { m_artificial = voxels; }
+
+  const FloatMap& map() const { return m_map; }
+  float lo_hit() const { return m_lo_hit; }
+  float lo_miss() const { return m_lo_miss; }
+
+private:
+  struct Source
+  {
+    double max_range = 0.0;
+    UpdateGrid grid;
+  };
+  double m_resolution;
+  Variant m_var;
+  double m_max_range   = 0.0;
+  bool m_fast_mode     = false;
+  bool m_config_set    = false;
+  float m_lo_hit       = 0.0f;
+  float m_lo_miss      = 0.0f;
+  float m_lo_thres_min = 0.0f;
+  float m_lo_thres_max = 0.0f;
+  float m_lo_max       = 0.0f;
+  float m_lo_min       = 0.0f;
+  FloatMap m_map;
+  std::map<std::string, Source> m_sources;
+  std::vector<Coord> m_artificial;
+};
+
+} // namespace vdb_oracle

@@ -1,0 +1,75 @@
+"""CPU checks of the C ABI: the library builds for sm_103a, loads, and exports
+every entry point include/vdb_gb300.h declares (no GPU work is launched)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(REPO, "include", "vdb_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(vdbg_\w+)\s*\(", text, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib_path():
+    from vdb_mapping_gb300.build import build_library
+
+    return build_library()
+
+
+def test_header_declares_the_path():
+    fns = declared_functions()
+    for name in ["vdbg_create", "vdbg_destroy", "vdbg_set_config", "vdbg_add_input_source",
+                 "vdbg_insert_point_cloud", "vdbg_accumulate_update", "vdbg_integrate_update",
+                 "vdbg_raycast_point_cloud", "vdbg_update_map", "vdbg_reset_map", "vdbg_export_leaves"]:
+        assert name in fns
+
+
+def test_library_exports_every_declared_symbol(lib_path):
+    out = subprocess.run(["nm", "-D", "--defined-only", lib_path], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (vdbg_\w+)", out))
+    missing = [f for f in declared_functions() if f not in exported]
+    assert not missing, missing
+
+
+def test_library_loads_and_binds(lib_path):
+    from vdb_mapping_gb300 import _lib
+
+    lib = _lib.load()
+    for name, _, _ in _lib.SIGNATURES:
+        assert hasattr(lib, name)
+    # The Python binding covers every entry point of the header.
+    bound = {n for n, _, _ in _lib.SIGNATURES}
+    assert set(declared_functions()) <= bound, set(declared_functions()) - bound
+
+
+def test_status_strings(lib_path):
+    from vdb_mapping_gb300 import _lib
+
+    lib = _lib.load()
+    for code in _lib.STATUS:
+        assert lib.vdbg_status_string(code)
+    assert lib.vdbg_status_string(1).decode().startswith("Map not properly configured")
+
+
+def test_struct_layouts_match_header():
+    from vdb_mapping_gb300 import _lib
+
+    assert C.sizeof(_lib.vdbg_config) == 56
+    assert C.sizeof(_lib.vdbg_options) == 24
+    assert C.sizeof(_lib.vdbg_scan_stats) == 64
+
+
+def test_build_targets_sm_103a_only():
+    from vdb_mapping_gb300 import build
+
+    flags = " ".join(build.NVCC_FLAGS)
+    assert "arch=compute_103a,code=sm_103a" in flags
+    assert flags.count("-gencode") == 1
+    assert "-fmad=false" in flags

@@ -1,0 +1,140 @@
+"""ctypes binding of the C ABI in include/vdb_gb300.h (libvdb_gb300.so).
+
+The library is the only compute path: if it is missing this module raises,
+there is no fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from .build import LIB_PATH
+
+VDBG_POINTS_DEVICE = 1
+
+STATUS = {
+    0: "VDBG_OK",
+    1: "VDBG_ERR_NOT_CONFIGURED",
+    2: "VDBG_ERR_UNKNOWN_SOURCE",
+    3: "VDBG_ERR_BAD_RANGE",
+    4: "VDBG_ERR_BAD_PROBABILITY",
+    5: "VDBG_ERR_DUPLICATE_SOURCE",
+    6: "VDBG_ERR_INVALID_ARGUMENT",
+    7: "VDBG_ERR_OUT_OF_MEMORY",
+    8: "VDBG_ERR_COORD_RANGE",
+    9: "VDBG_ERR_CUDA",
+    10: "VDBG_ERR_TIMEOUT",
+    11: "VDBG_ERR_BUFFER_TOO_SMALL",
+}
+STATUS_CODE = {v: k for k, v in STATUS.items()}
+
+
+class vdbg_config(C.Structure):
+    _fields_ = [
+        ("max_range", C.c_double),
+        ("fast_mode", C.c_int32),
+        ("reserved0", C.c_int32),
+        ("accumulation_period", C.c_double),
+        ("prob_hit", C.c_double),
+        ("prob_miss", C.c_double),
+        ("prob_thres_min", C.c_double),
+        ("prob_thres_max", C.c_double),
+    ]
+
+
+class vdbg_options(C.Structure):
+    _fields_ = [
+        ("initial_leaf_capacity", C.c_int64),
+        ("max_device_bytes", C.c_int64),
+        ("device", C.c_int32),
+        ("reserved0", C.c_int32),
+    ]
+
+
+class vdbg_scan_stats(C.Structure):
+    _fields_ = [
+        ("rays", C.c_uint64),
+        ("visits", C.c_uint64),
+        ("hits", C.c_uint64),
+        ("updates", C.c_uint64),
+        ("new_leaves", C.c_uint64),
+        ("touched_leaves", C.c_uint64),
+        ("skipped_nonfinite", C.c_uint64),
+        ("device_ms", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class vdbg_timings(C.Structure):
+    _fields_ = [
+        ("prep_ms", C.c_double),
+        ("dda_ms", C.c_double),
+        ("sweep_ms", C.c_double),
+        ("total_ms", C.c_double),
+        ("launches", C.c_uint64),
+        ("launches_total", C.c_uint64),
+        ("retries", C.c_uint64),
+        ("reserved0", C.c_uint64),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved0"}
+
+
+# (name, restype, argtypes) of every exported entry point.
+_P = C.c_void_p
+_D3 = C.POINTER(C.c_double)
+SIGNATURES = [
+    ("vdbg_create", C.c_int, [C.c_double, C.POINTER(vdbg_options), C.POINTER(_P)]),
+    ("vdbg_destroy", C.c_int, [_P]),
+    ("vdbg_set_config", C.c_int, [_P, C.POINTER(vdbg_config)]),
+    ("vdbg_get_log_odds", C.c_int, [_P, C.POINTER(C.c_float)]),
+    ("vdbg_add_input_source", C.c_int, [_P, C.c_char_p, C.c_double, C.c_double]),
+    ("vdbg_insert_point_cloud", C.c_int,
+     [_P, _P, C.c_int64, C.c_int64, _D3, C.c_char_p, C.c_uint32, _P, C.POINTER(vdbg_scan_stats)]),
+    ("vdbg_accumulate_update", C.c_int,
+     [_P, _P, C.c_int64, C.c_int64, _D3, C.c_char_p, C.c_uint32, _P, C.POINTER(vdbg_scan_stats)]),
+    ("vdbg_integrate_update", C.c_int, [_P, _P, C.POINTER(vdbg_scan_stats)]),
+    ("vdbg_raycast_point_cloud", C.c_int,
+     [_P, _P, C.c_int64, C.c_int64, _D3, C.c_double, C.c_char_p, C.c_uint32, _P,
+      C.POINTER(vdbg_scan_stats)]),
+    ("vdbg_update_map", C.c_int, [_P, C.c_char_p, _P, C.POINTER(vdbg_scan_stats)]),
+    ("vdbg_reset_map", C.c_int, [_P]),
+    ("vdbg_leaf_count", C.c_int, [_P, C.POINTER(C.c_int64)]),
+    ("vdbg_export_leaves", C.c_int, [_P, C.c_int64, _P, _P, _P, C.POINTER(C.c_int64)]),
+    ("vdbg_device_bytes", C.c_int, [_P, C.POINTER(C.c_int64)]),
+    ("vdbg_get_timings", C.c_int, [_P, C.POINTER(vdbg_timings)]),
+    ("vdbg_status_string", C.c_char_p, [C.c_int]),
+]
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Loads libvdb_gb300.so (building it first if absent) and binds it."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        from .build import build_library
+        build_library()
+    if not os.path.exists(p):
+        raise RuntimeError(f"libvdb_gb300.so not found at {p}; run vdb_mapping_gb300.build")
+    lib = C.CDLL(p)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class VdbgError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        text = load().vdbg_status_string(status).decode()
+        super().__init__(f"{where}: {STATUS.get(status, status)} ({text})")

@@ -1,0 +1,334 @@
+// device_common.cuh — shared device-side pieces of the scan-insertion path:
+// the leaf hash, the per-scan mask marking and the exact arithmetic helpers.
+//
+// Map layout in HBM (one map):
+//   hkeys   u64[H]      packed leaf coordinate (voxel >> 3, 21 bits per axis)
+//   hslots  i32[H]      leaf slot for the key; -1 while being published
+//   origin  int4[P]     leaf origin (voxel coordinates, multiples of 8)
+//   values  f32[P][512] log-odds, OpenVDB leaf order (x&7)<<6 | (y&7)<<3 | (z&7)
+//   active  u64[P][8]   value (active) mask, bit i of word w = offset 64w+i
+//   flags   u32[P]      1 once the leaf belongs to the map (first integration)
+// Per update grid (one per input source):
+//   upd     u64[P][16]  words 0-7 visited, 8-15 hit, same bit order as active
+//   epoch   u32[P]      integration window in which the leaf was last touched
+//   touched i32[P]      leaves touched in the current window, n_touched of them
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace vdbg {
+
+constexpr unsigned long long kEmptyKey = ~0ull;
+constexpr int kSlotPending             = -1;
+constexpr int kSlotFailed              = -2;
+constexpr int kNoSlot                  = -3;
+constexpr uint32_t kMaxProbes          = 4096;
+constexpr uint32_t kSpinLimit          = 1u << 22;
+constexpr int kKeyBits                 = 21;
+constexpr int kLeafCoordMin            = -(1 << (kKeyBits - 1));
+constexpr int kLeafCoordMax            = (1 << (kKeyBits - 1)) - 1;
+constexpr double kVoxelMin             = -8388608.0;  // -2^23
+constexpr double kVoxelMaxExcl         = 8388608.0;   //  2^23
+
+// Device error bits (DevStatus::error).
+constexpr uint32_t kErrPoolFull   = 1u;
+constexpr uint32_t kErrHashFull   = 2u;
+constexpr uint32_t kErrSpin       = 4u;
+constexpr uint32_t kErrCoordRange = 8u;
+constexpr uint32_t kErrStepBound  = 16u;
+
+// Ray record meta word: bits 0-28 L1 length, bit 29 clipped, bit 30 valid.
+constexpr uint32_t kMetaL1Mask   = (1u << 29) - 1;
+constexpr uint32_t kMetaClipped  = 1u << 29;
+constexpr uint32_t kMetaValid    = 1u << 30;
+
+// Counting-sort buckets for rays by L1 length (descending).
+constexpr int kNumBuckets  = 4096;
+constexpr int kBucketShift = 3;
+
+struct DevStatus
+{
+  uint32_t error;
+  uint32_t n_leaves;  // leaf bump allocator (may exceed capacity after a failed allocation)
+  uint32_t n_valid;   // rays in the order array this scan
+  uint32_t touched;   // leaves swept (summed over sweeps)
+  unsigned long long rays;
+  unsigned long long visits;
+  unsigned long long hits;
+  unsigned long long updates;
+  unsigned long long nonfinite;
+  unsigned long long pad[3];
+};
+
+struct LogOdds
+{
+  float hit, miss, thres_min, thres_max, max, min;
+};
+
+// Geometry of one scan: sensor origin in world and index space, the raycast
+// range and the quantiser constants (res/2 and 1/res computed on the host).
+struct ScanGeom
+{
+  double ox, oy, oz;
+  double range;
+  double res, half_res, inv_res;
+  int ovx, ovy, ovz;
+  int pad;
+};
+
+struct MapView
+{
+  unsigned long long* hkeys;
+  int* hslots;
+  uint32_t hmask;
+  uint32_t capacity;
+  int4* origin;
+  DevStatus* st;
+};
+
+struct ChannelView
+{
+  unsigned long long* upd;
+  uint32_t* epoch;
+  int* touched;
+  uint32_t* n_touched;
+  uint32_t cur_epoch;
+};
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p)
+{
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p)
+{
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_acquire_s32(const int* p)
+{
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_s32(int* p, int v)
+{
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Murmur3 64-bit finaliser (published mixing function).
+__device__ __forceinline__ unsigned long long mix64(unsigned long long k)
+{
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ull;
+  k ^= k >> 33;
+  return k;
+}
+
+__device__ __forceinline__ unsigned long long pack_leaf_key(int lx, int ly, int lz)
+{
+  const unsigned long long m = (1ull << kKeyBits) - 1;
+  return ((static_cast<unsigned long long>(lx) & m) << (2 * kKeyBits)) |
+         ((static_cast<unsigned long long>(ly) & m) << kKeyBits) |
+         (static_cast<unsigned long long>(lz) & m);
+}
+
+// Appends `slot` to the channel's touched list the first time it is seen in
+// the current integration window.
+__device__ __forceinline__ void touch_leaf(const ChannelView& c, int slot)
+{
+  uint32_t* e = c.epoch + slot;
+  if (ld_relaxed_u32(e) != c.cur_epoch)
+  {
+    if (atomicExch(e, c.cur_epoch) != c.cur_epoch)
+    {
+      const uint32_t t = atomicAdd(c.n_touched, 1u);
+      c.touched[t]     = slot;
+    }
+  }
+}
+
+// Slot of leaf (lx,ly,lz), allocating it if absent. Lock-free open addressing
+// with linear probing: the thread whose CAS claims an empty key allocates the
+// slot from the bump counter and publishes it; others that find the key wait
+// (bounded) for the publication. Returns kSlotFailed after setting an error
+// bit when the pool or the probe budget is exhausted.
+__device__ __forceinline__ int find_or_insert_leaf(const MapView& m, int lx, int ly, int lz)
+{
+  const unsigned long long key = pack_leaf_key(lx, ly, lz);
+  uint32_t h                   = static_cast<uint32_t>(mix64(key)) & m.hmask;
+  for (uint32_t probe = 0; probe < kMaxProbes; ++probe)
+  {
+    unsigned long long k = ld_relaxed_u64(m.hkeys + h);
+    if (k == kEmptyKey)
+    {
+      const unsigned long long prev = atomicCAS(m.hkeys + h, kEmptyKey, key);
+      if (prev == kEmptyKey)
+      {
+        const uint32_t s = atomicAdd(&m.st->n_leaves, 1u);
+        int slot;
+        if (s >= m.capacity)
+        {
+          atomicOr(&m.st->error, kErrPoolFull);
+          slot = kSlotFailed;
+        }
+        else
+        {
+          m.origin[s] = make_int4(lx * 8, ly * 8, lz * 8, 0);
+          slot        = static_cast<int>(s);
+        }
+        st_release_s32(m.hslots + h, slot);
+        return slot;
+      }
+      k = prev;
+    }
+    if (k == key)
+    {
+      int s          = ld_acquire_s32(m.hslots + h);
+      uint32_t spins = 0;
+      while (s == kSlotPending)
+      {
+        if (++spins > kSpinLimit)
+        {
+          atomicOr(&m.st->error, kErrSpin);
+          return kSlotFailed;
+        }
+        __nanosleep(64);
+        s = ld_acquire_s32(m.hslots + h);
+      }
+      return s < 0 ? kSlotFailed : s;
+    }
+    h = (h + 1) & m.hmask;
+  }
+  atomicOr(&m.st->error, kErrHashFull);
+  return kSlotFailed;
+}
+
+// Per-thread marker: caches the current leaf slot and accumulates the bits of
+// one 64-bit mask word (one x-slab of the leaf) before a single atomicOr.
+struct Marker
+{
+  int lx, ly, lz;
+  int slot;
+  int word;
+  unsigned long long bits;
+};
+
+__device__ __forceinline__ void marker_init(Marker& mk)
+{
+  mk.lx   = 0x7fffffff;
+  mk.ly   = 0x7fffffff;
+  mk.lz   = 0x7fffffff;
+  mk.slot = kNoSlot;
+  mk.word = -1;
+  mk.bits = 0ull;
+}
+
+// OR `bits` into a mask word; bits only ever get set while a scan is being
+// marked, so a relaxed read that already shows them makes the atomic
+// unnecessary (a stale read can only show fewer bits).
+__device__ __forceinline__ void or_bits(unsigned long long* p, unsigned long long bits)
+{
+  const unsigned long long cur = ld_relaxed_u64(p);
+  if ((cur & bits) != bits) atomicOr(p, bits);
+}
+
+__device__ __forceinline__ void marker_flush(Marker& mk, const ChannelView& c)
+{
+  if (mk.bits && mk.slot >= 0)
+  {
+    or_bits(c.upd + static_cast<size_t>(mk.slot) * 16 + mk.word, mk.bits);
+  }
+  mk.bits = 0ull;
+}
+
+__device__ __forceinline__ void marker_enter_leaf(Marker& mk, const MapView& m, const ChannelView& c,
+                                                  int lx, int ly, int lz)
+{
+  marker_flush(mk, c);
+  mk.lx   = lx;
+  mk.ly   = ly;
+  mk.lz   = lz;
+  mk.slot = find_or_insert_leaf(m, lx, ly, lz);
+  if (mk.slot >= 0) touch_leaf(c, mk.slot);
+  mk.word = -1;
+}
+
+// setActiveState(voxel, true) on the update grid (VDBMapping.hpp:563).
+__device__ __forceinline__ void mark_visit(Marker& mk, const MapView& m, const ChannelView& c, int x,
+                                           int y, int z)
+{
+  const int lx = x >> 3, ly = y >> 3, lz = z >> 3;
+  if (lx != mk.lx || ly != mk.ly || lz != mk.lz || mk.slot == kNoSlot)
+  {
+    marker_enter_leaf(mk, m, c, lx, ly, lz);
+  }
+  const int w = x & 7;
+  if (w != mk.word)
+  {
+    marker_flush(mk, c);
+    mk.word = w;
+  }
+  mk.bits |= 1ull << (((y & 7) << 3) | (z & 7));
+}
+
+// setValueOn(end, true) on the update grid (VDBMapping.hpp:535): the hit word.
+__device__ __forceinline__ void mark_hit(Marker& mk, const MapView& m, const ChannelView& c, int x,
+                                         int y, int z)
+{
+  marker_flush(mk, c);
+  const int lx = x >> 3, ly = y >> 3, lz = z >> 3;
+  if (lx != mk.lx || ly != mk.ly || lz != mk.lz || mk.slot == kNoSlot)
+  {
+    marker_enter_leaf(mk, m, c, lx, ly, lz);
+  }
+  if (mk.slot >= 0)
+  {
+    or_bits(c.upd + static_cast<size_t>(mk.slot) * 16 + 8 + (x & 7),
+            1ull << (((y & 7) << 3) | (z & 7)));
+  }
+}
+
+// VDBMapping.hpp:612-631 for one axis: shift non-multiples of the resolution
+// by res/2 (std::fmod is exact, as CUDA's fmod is), scale by 1/res, floor.
+// Returns false when the index leaves [-2^23, 2^23) (or is NaN).
+__device__ __forceinline__ bool world_to_index_axis(double w, const ScanGeom& g, int& out)
+{
+  if (fmod(w, g.res) != 0.0) w = __dadd_rn(w, g.half_res);
+  const double f = floor(__dmul_rn(w, g.inv_res));
+  if (!(f >= kVoxelMin && f < kVoxelMaxExcl)) return false;
+  out = static_cast<int>(f);
+  return true;
+}
+
+// OpenVDB log-odds node updates (OccupancyVDBMapping.hpp:92-117): FP32 add,
+// clamp only inside the threshold branch; a hit never deactivates, a miss
+// never activates.
+__device__ __forceinline__ void apply_update(float& v, bool& on, bool hit, const LogOdds& lo)
+{
+  if (hit)
+  {
+    v = __fadd_rn(v, lo.hit);
+    if (v > lo.thres_max)
+    {
+      on = true;
+      if (v > lo.max) v = lo.max;
+    }
+  }
+  else
+  {
+    v = __fadd_rn(v, lo.miss);
+    if (v < lo.thres_min)
+    {
+      on = false;
+      if (v < lo.min) v = lo.min;
+    }
+  }
+}
+
+} // namespace vdbg

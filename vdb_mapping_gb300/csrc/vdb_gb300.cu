@@ -1,0 +1,910 @@
+// vdb_gb300.cu — host side of the C ABI declared in include/vdb_gb300.h.
+//
+// One vdbg_map owns one occupancy map resident on one GPU (leaf hash, leaf
+// pool, one update grid per input source) plus the per-scan scratch buffers.
+// Every entry point launches its kernels on one stream and waits for them, so
+// the calls have the reference's synchronous semantics.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "vdb_gb300.h"
+
+using namespace vdbg;
+
+namespace {
+
+struct Channel
+{
+  std::string id;
+  double max_range            = 0.0;
+  unsigned long long* upd     = nullptr;  // [P][16]
+  uint32_t* epoch             = nullptr;  // [P]
+  int* touched                = nullptr;  // [P]
+  uint32_t* n_touched         = nullptr;  // device scalar
+  uint32_t cur_epoch          = 1;
+  bool pending                = false;    // marked since its last integration
+};
+
+} // namespace
+
+struct vdbg_map
+{
+  int device            = 0;
+  double resolution     = 0.0;
+  double half_res       = 0.0;
+  double inv_res        = 0.0;
+  bool config_set       = false;
+  double max_range      = 0.0;
+  bool fast_mode        = false;
+  double accumulation_period = 0.0;
+  LogOdds lo{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  int64_t max_bytes     = 0;
+
+  cudaStream_t stream   = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev_prep = nullptr, ev_dda = nullptr;  // after k_scatter, after k_dda_mark
+  bool timed_prep       = false;
+  vdbg_timings timings{};
+
+  // Leaf pool and hash.
+  uint32_t capacity     = 0;
+  uint32_t hash_size    = 0;
+  float* values         = nullptr;
+  unsigned long long* active = nullptr;
+  int4* origin          = nullptr;
+  uint32_t* flags       = nullptr;
+  unsigned long long* hkeys = nullptr;
+  int* hslots           = nullptr;
+  uint32_t n_leaves     = 0;  // host copy after the last call
+
+  DevStatus* d_status   = nullptr;
+  DevStatus* h_status   = nullptr;  // pinned
+
+  std::vector<Channel> channels;  // sorted by id (std::map order of the reference)
+
+  // Per-scan scratch.
+  char* d_pts           = nullptr;
+  size_t pts_cap        = 0;
+  int4* d_rays          = nullptr;
+  int* d_order          = nullptr;
+  size_t ray_cap        = 0;
+  uint32_t* d_hist      = nullptr;
+  uint32_t* d_cursor    = nullptr;
+
+  int64_t bytes         = 0;
+};
+
+namespace {
+
+#define VDBG_CUDA(call)                                                                    \
+  do                                                                                       \
+  {                                                                                        \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+    {                                                                                      \
+      std::fprintf(stderr, "vdb_gb300: %s failed: %s\n", #call, cudaGetErrorString(e_));   \
+      return e_ == cudaErrorMemoryAllocation ? VDBG_ERR_OUT_OF_MEMORY : VDBG_ERR_CUDA;     \
+    }                                                                                      \
+  } while (0)
+
+constexpr uint32_t kDefaultCapacity = 1u << 16;
+constexpr int kSweepBlocks          = 152 * 8;
+constexpr int kSweepThreads         = 256;
+
+uint32_t next_pow2(uint64_t v)
+{
+  uint64_t p = 1;
+  while (p < v) p <<= 1;
+  return static_cast<uint32_t>(p);
+}
+
+int set_device(const vdbg_map* m)
+{
+  VDBG_CUDA(cudaSetDevice(m->device));
+  return VDBG_OK;
+}
+
+template <class T>
+int dev_alloc(vdbg_map* m, T** p, size_t count)
+{
+  *p = nullptr;
+  if (count == 0) return VDBG_OK;
+  const size_t b = count * sizeof(T);
+  if (m->max_bytes > 0 && m->bytes + static_cast<int64_t>(b) > m->max_bytes) return VDBG_ERR_OUT_OF_MEMORY;
+  VDBG_CUDA(cudaMalloc(reinterpret_cast<void**>(p), b));
+  m->bytes += static_cast<int64_t>(b);
+  return VDBG_OK;
+}
+
+template <class T>
+void dev_free(vdbg_map* m, T*& p, size_t count)
+{
+  if (p)
+  {
+    cudaFree(p);
+    m->bytes -= static_cast<int64_t>(count * sizeof(T));
+  }
+  p = nullptr;
+}
+
+#define VDBG_TRY(expr)        \
+  do                          \
+  {                           \
+    const int s_ = (expr);    \
+    if (s_ != VDBG_OK) return s_; \
+  } while (0)
+
+MapView map_view(const vdbg_map* m)
+{
+  MapView v;
+  v.hkeys    = m->hkeys;
+  v.hslots   = m->hslots;
+  v.hmask    = m->hash_size - 1;
+  v.capacity = m->capacity;
+  v.origin   = m->origin;
+  v.st       = m->d_status;
+  return v;
+}
+
+ChannelView channel_view(const Channel& c)
+{
+  ChannelView v;
+  v.upd       = c.upd;
+  v.epoch     = c.epoch;
+  v.touched   = c.touched;
+  v.n_touched = c.n_touched;
+  v.cur_epoch = c.cur_epoch;
+  return v;
+}
+
+int alloc_channel(vdbg_map* m, Channel& c, uint32_t cap)
+{
+  VDBG_TRY(dev_alloc(m, &c.upd, static_cast<size_t>(cap) * 16));
+  VDBG_TRY(dev_alloc(m, &c.epoch, cap));
+  VDBG_TRY(dev_alloc(m, &c.touched, cap));
+  if (!c.n_touched) VDBG_TRY(dev_alloc(m, &c.n_touched, 1));
+  VDBG_CUDA(cudaMemsetAsync(c.upd, 0, static_cast<size_t>(cap) * 16 * sizeof(unsigned long long), m->stream));
+  VDBG_CUDA(cudaMemsetAsync(c.epoch, 0, static_cast<size_t>(cap) * sizeof(uint32_t), m->stream));
+  return VDBG_OK;
+}
+
+void free_channel(vdbg_map* m, Channel& c, uint32_t cap)
+{
+  dev_free(m, c.upd, static_cast<size_t>(cap) * 16);
+  dev_free(m, c.epoch, cap);
+  dev_free(m, c.touched, cap);
+}
+
+// Builds the hash of leaves [0, n) into a fresh table of `hsize` entries.
+int rebuild_hash(vdbg_map* m, uint32_t hsize, uint32_t n)
+{
+  dev_free(m, m->hkeys, m->hash_size);
+  dev_free(m, m->hslots, m->hash_size);
+  m->hash_size = hsize;
+  VDBG_TRY(dev_alloc(m, &m->hkeys, hsize));
+  VDBG_TRY(dev_alloc(m, &m->hslots, hsize));
+  VDBG_CUDA(cudaMemsetAsync(m->hkeys, 0xff, static_cast<size_t>(hsize) * sizeof(unsigned long long), m->stream));
+  VDBG_CUDA(cudaMemsetAsync(m->hslots, 0xff, static_cast<size_t>(hsize) * sizeof(int), m->stream));
+  if (n > 0)
+  {
+    k_rehash<<<(n + 255) / 256, 256, 0, m->stream>>>(map_view(m), n);
+    VDBG_CUDA(cudaGetLastError());
+  }
+  return VDBG_OK;
+}
+
+// Allocates the leaf pool with `cap` slots, keeping leaves [0, keep).
+int resize_pool(vdbg_map* m, uint32_t cap, uint32_t keep)
+{
+  float* values              = nullptr;
+  unsigned long long* active = nullptr;
+  int4* origin               = nullptr;
+  uint32_t* flags            = nullptr;
+  std::vector<Channel> fresh(m->channels.size());
+  int st = dev_alloc(m, &values, static_cast<size_t>(cap) * 512);
+  if (st == VDBG_OK) st = dev_alloc(m, &active, static_cast<size_t>(cap) * 8);
+  if (st == VDBG_OK) st = dev_alloc(m, &origin, cap);
+  if (st == VDBG_OK) st = dev_alloc(m, &flags, cap);
+  for (size_t i = 0; i < fresh.size() && st == VDBG_OK; ++i)
+  {
+    fresh[i].n_touched = m->channels[i].n_touched;
+    st                 = alloc_channel(m, fresh[i], cap);
+  }
+  if (st != VDBG_OK)
+  {
+    // Leave the map as it was.
+    dev_free(m, values, static_cast<size_t>(cap) * 512);
+    dev_free(m, active, static_cast<size_t>(cap) * 8);
+    dev_free(m, origin, cap);
+    dev_free(m, flags, cap);
+    for (Channel& c : fresh) free_channel(m, c, cap);
+    return st;
+  }
+  cudaStream_t s = m->stream;
+  VDBG_CUDA(cudaMemsetAsync(values, 0, static_cast<size_t>(cap) * 512 * sizeof(float), s));
+  VDBG_CUDA(cudaMemsetAsync(active, 0, static_cast<size_t>(cap) * 8 * sizeof(unsigned long long), s));
+  VDBG_CUDA(cudaMemsetAsync(flags, 0, static_cast<size_t>(cap) * sizeof(uint32_t), s));
+  if (keep > 0)
+  {
+    VDBG_CUDA(cudaMemcpyAsync(values, m->values, static_cast<size_t>(keep) * 512 * sizeof(float),
+                              cudaMemcpyDeviceToDevice, s));
+    VDBG_CUDA(cudaMemcpyAsync(active, m->active, static_cast<size_t>(keep) * 8 * sizeof(unsigned long long),
+                              cudaMemcpyDeviceToDevice, s));
+    VDBG_CUDA(cudaMemcpyAsync(origin, m->origin, static_cast<size_t>(keep) * sizeof(int4),
+                              cudaMemcpyDeviceToDevice, s));
+    VDBG_CUDA(cudaMemcpyAsync(flags, m->flags, static_cast<size_t>(keep) * sizeof(uint32_t),
+                              cudaMemcpyDeviceToDevice, s));
+  }
+  for (size_t i = 0; i < m->channels.size(); ++i)
+  {
+    Channel& c  = m->channels[i];
+    Channel& nc = fresh[i];
+    if (keep > 0)
+    {
+      VDBG_CUDA(cudaMemcpyAsync(nc.upd, c.upd, static_cast<size_t>(keep) * 16 * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToDevice, s));
+      VDBG_CUDA(cudaMemcpyAsync(nc.epoch, c.epoch, static_cast<size_t>(keep) * sizeof(uint32_t),
+                                cudaMemcpyDeviceToDevice, s));
+      VDBG_CUDA(cudaMemcpyAsync(nc.touched, c.touched, static_cast<size_t>(keep) * sizeof(int),
+                                cudaMemcpyDeviceToDevice, s));
+    }
+    VDBG_CUDA(cudaStreamSynchronize(s));
+    free_channel(m, c, m->capacity);
+    c.upd     = nc.upd;
+    c.epoch   = nc.epoch;
+    c.touched = nc.touched;
+  }
+  VDBG_CUDA(cudaStreamSynchronize(s));
+  dev_free(m, m->values, static_cast<size_t>(m->capacity) * 512);
+  dev_free(m, m->active, static_cast<size_t>(m->capacity) * 8);
+  dev_free(m, m->origin, m->capacity);
+  dev_free(m, m->flags, m->capacity);
+  m->values   = values;
+  m->active   = active;
+  m->origin   = origin;
+  m->flags    = flags;
+  m->capacity = cap;
+  VDBG_TRY(rebuild_hash(m, next_pow2(static_cast<uint64_t>(cap) * 2), keep));
+  // Work queued by the caller on another stream must see the new tables.
+  VDBG_CUDA(cudaStreamSynchronize(s));
+  return VDBG_OK;
+}
+
+int ensure_scratch(vdbg_map* m, int64_t n, int64_t stride, bool host_input)
+{
+  if (host_input)
+  {
+    const size_t need = static_cast<size_t>(n) * static_cast<size_t>(stride);
+    if (need > m->pts_cap)
+    {
+      dev_free(m, m->d_pts, m->pts_cap);
+      m->pts_cap = 0;
+      const size_t cap = std::max(need, m->pts_cap * 3 / 2);
+      VDBG_TRY(dev_alloc(m, &m->d_pts, cap));
+      m->pts_cap = cap;
+    }
+  }
+  if (static_cast<size_t>(n) > m->ray_cap)
+  {
+    dev_free(m, m->d_rays, m->ray_cap);
+    dev_free(m, m->d_order, m->ray_cap);
+    const size_t cap = std::max(static_cast<size_t>(n), m->ray_cap * 3 / 2);
+    m->ray_cap       = 0;
+    VDBG_TRY(dev_alloc(m, &m->d_rays, cap));
+    VDBG_TRY(dev_alloc(m, &m->d_order, cap));
+    m->ray_cap = cap;
+  }
+  return VDBG_OK;
+}
+
+Channel* find_channel(vdbg_map* m, const char* id)
+{
+  if (!id) return nullptr;
+  for (Channel& c : m->channels)
+    if (c.id == id) return &c;
+  return nullptr;
+}
+
+// Host copy of VDBMapping.hpp:612-631 for the sensor origin (compiled with
+// -ffp-contract=off, the same IEEE operations as the device quantiser).
+bool origin_to_index(const vdbg_map* m, const double o[3], int out[3])
+{
+  for (int a = 0; a < 3; ++a)
+  {
+    double w = o[a];
+    if (std::fmod(w, m->resolution) != 0.0) w = w + m->half_res;
+    const double f = std::floor(w * m->inv_res);
+    if (!(f >= kVoxelMin && f < kVoxelMaxExcl)) return false;
+    out[a] = static_cast<int>(f);
+  }
+  return true;
+}
+
+void clear_status(DevStatus* h) { std::memset(h, 0, sizeof(DevStatus)); }
+
+int begin_call(vdbg_map* m, cudaStream_t s)
+{
+  VDBG_TRY(set_device(m));
+  m->timings.launches_total += m->timings.launches;
+  const uint64_t total = m->timings.launches_total;
+  m->timings           = vdbg_timings{};
+  m->timings.launches_total = total;
+  m->timed_prep        = false;
+  clear_status(m->h_status);
+  m->h_status->n_leaves = m->n_leaves;
+  VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+  VDBG_CUDA(cudaEventRecord(m->ev0, s));
+  return VDBG_OK;
+}
+
+int fetch_status(vdbg_map* m, cudaStream_t s)
+{
+  VDBG_CUDA(cudaEventRecord(m->ev1, s));
+  VDBG_CUDA(cudaMemcpyAsync(m->h_status, m->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+  VDBG_CUDA(cudaStreamSynchronize(s));
+  return VDBG_OK;
+}
+
+void fill_stats(vdbg_map* m, uint32_t leaves_before, vdbg_scan_stats* st)
+{
+  if (!st) return;
+  const DevStatus& h = *m->h_status;
+  st->rays           = h.rays;
+  st->visits         = h.visits;
+  st->hits           = h.hits;
+  st->updates        = h.updates;
+  st->new_leaves     = m->n_leaves - leaves_before;
+  st->touched_leaves = h.touched;
+  st->skipped_nonfinite = h.nonfinite;
+  st->device_ms = m->timings.total_ms;
+}
+
+void record_timings(vdbg_map* m)
+{
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+  m->timings.total_ms = ms;
+  if (m->timed_prep)
+  {
+    float a = 0.f, b = 0.f, c = 0.f;
+    cudaEventElapsedTime(&a, m->ev0, m->ev_prep);
+    cudaEventElapsedTime(&b, m->ev_prep, m->ev_dda);
+    cudaEventElapsedTime(&c, m->ev_dda, m->ev1);
+    m->timings.prep_ms  = a;
+    m->timings.dda_ms   = b;
+    m->timings.sweep_ms = c;
+  }
+  else
+  {
+    m->timings.sweep_ms = ms;
+  }
+}
+
+// Marks one cloud into channel `c` (VDBMapping.hpp:466-539). Kernels are
+// queued on `s`; the caller fetches the status.
+int launch_raycast(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t stride,
+                   const double origin[3], double range, uint32_t flags, cudaStream_t s, bool* queued,
+                   ScanGeom* geom_out)
+{
+  *queued = false;
+  if (n <= 0) return VDBG_OK;
+  if (std::isnan(origin[0]) || std::isnan(origin[1]) || std::isnan(origin[2])) return VDBG_OK;
+  ScanGeom g;
+  g.ox       = origin[0];
+  g.oy       = origin[1];
+  g.oz       = origin[2];
+  g.range    = range;
+  g.res      = m->resolution;
+  g.half_res = m->half_res;
+  g.inv_res  = m->inv_res;
+  int ov[3];
+  if (!origin_to_index(m, origin, ov)) return VDBG_ERR_COORD_RANGE;
+  g.ovx = ov[0];
+  g.ovy = ov[1];
+  g.ovz = ov[2];
+  g.pad = 0;
+
+  const bool host_input = (flags & VDBG_POINTS_DEVICE) == 0;
+  VDBG_TRY(ensure_scratch(m, n, stride, host_input));
+  const char* pts = reinterpret_cast<const char*>(xyz);
+  if (host_input)
+  {
+    VDBG_CUDA(cudaMemcpyAsync(m->d_pts, xyz, static_cast<size_t>(n) * static_cast<size_t>(stride),
+                              cudaMemcpyHostToDevice, s));
+    pts = m->d_pts;
+  }
+  const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
+  k_prep<<<blocks, 256, 0, s>>>(pts, n, stride, g, m->d_rays, m->d_hist, m->d_status);
+  k_scan<<<1, 1024, 0, s>>>(m->d_hist, m->d_cursor, m->d_status);
+  k_scatter<<<blocks, 256, 0, s>>>(m->d_rays, n, m->d_cursor, m->d_order);
+  VDBG_CUDA(cudaEventRecord(m->ev_prep, s));
+  k_dda_mark<<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(m->d_rays, m->d_order, n, g,
+                                                                   map_view(m), channel_view(c));
+  VDBG_CUDA(cudaGetLastError());
+  VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
+  m->timed_prep = true;
+  m->timings.launches += 4;
+  c.pending  = true;
+  *queued    = true;
+  *geom_out  = g;
+  return VDBG_OK;
+}
+
+int launch_sweep(vdbg_map* m, Channel& c, cudaStream_t s)
+{
+  k_sweep<<<kSweepBlocks, kSweepThreads, 0, s>>>(channel_view(c), m->values, m->active, m->flags, m->lo,
+                                                 m->d_status);
+  VDBG_CUDA(cudaGetLastError());
+  m->timings.launches += 1;
+  return VDBG_OK;
+}
+
+// After a sweep: fresh update grid for the channel.
+int finish_sweep(vdbg_map* m, Channel& c, cudaStream_t s)
+{
+  VDBG_CUDA(cudaMemsetAsync(c.n_touched, 0, sizeof(uint32_t), s));
+  c.cur_epoch += 1;
+  if (c.cur_epoch == 0) c.cur_epoch = 1;
+  c.pending = false;
+  return VDBG_OK;
+}
+
+// Grows the pool after an allocation failure (or when it is getting full) and
+// rebuilds the hash. `requested` is the bump counter, which counts every
+// allocation attempt of the failed pass.
+int grow_for(vdbg_map* m, uint64_t requested)
+{
+  const uint32_t keep = std::min<uint32_t>(m->n_leaves, m->capacity);
+  uint64_t want       = std::max<uint64_t>(static_cast<uint64_t>(m->capacity) * 2, requested + requested / 2);
+  if (want > (1ull << 30)) want = 1ull << 30;
+  if (want <= m->capacity) return VDBG_ERR_OUT_OF_MEMORY;
+  return resize_pool(m, static_cast<uint32_t>(want), keep);
+}
+
+int map_error(uint32_t err)
+{
+  if (err & kErrCoordRange) return VDBG_ERR_COORD_RANGE;
+  if (err & kErrSpin) return VDBG_ERR_TIMEOUT;
+  if (err & kErrStepBound) return VDBG_ERR_CUDA;
+  return VDBG_ERR_OUT_OF_MEMORY;
+}
+
+int maybe_grow_ahead(vdbg_map* m)
+{
+  if (static_cast<uint64_t>(m->n_leaves) * 10 > static_cast<uint64_t>(m->capacity) * 7)
+  {
+    return grow_for(m, static_cast<uint64_t>(m->capacity) * 2);
+  }
+  return VDBG_OK;
+}
+
+cudaStream_t pick_stream(vdbg_map* m, void* stream)
+{
+  return stream ? static_cast<cudaStream_t>(stream) : m->stream;
+}
+
+bool bad_points(const float* xyz, int64_t n, int64_t stride)
+{
+  if (n < 0) return true;
+  if (n == 0) return false;
+  if (!xyz || stride < 12 || (stride % 4) != 0) return true;
+  if ((reinterpret_cast<uintptr_t>(xyz) % 4) != 0) return true;
+  if (n > (int64_t(1) << 31) - 1) return true;
+  return false;
+}
+
+// accumulate (optional) + integration of the listed channels, one status
+// fetch at the end in the common case. Pool or hash exhaustion is handled by
+// growing and marking the cloud again: marking is idempotent (bits are only
+// OR-ed in, a leaf already on the touched list is not added twice) and the
+// sweeps are skipped on the device while an error is set. A voxel index out
+// of range skips the whole cloud (nothing of it is marked) and the other
+// pending update grids are still integrated.
+int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t stride,
+                             const double origin[3], Channel* src, double range, uint32_t flags,
+                             cudaStream_t s, bool integrate_all, Channel* only, vdbg_scan_stats* stats)
+{
+  VDBG_TRY(begin_call(m, s));
+  const uint32_t leaves_before = m->n_leaves;
+  bool queued                  = false;
+  ScanGeom g{};
+  if (src)
+  {
+    VDBG_TRY(launch_raycast(m, *src, xyz, n, stride, origin, range, flags, s, &queued, &g));
+  }
+  std::vector<Channel*> todo;
+  if (integrate_all)
+  {
+    for (Channel& c : m->channels)
+      if (c.pending) todo.push_back(&c);
+  }
+  else if (only && only->pending)
+  {
+    todo.push_back(only);
+  }
+  auto sweeps = [&]() -> int {
+    for (Channel* c : todo) VDBG_TRY(launch_sweep(m, *c, s));
+    return VDBG_OK;
+  };
+  VDBG_TRY(sweeps());
+  int call_status = VDBG_OK;
+  bool done       = false;
+  for (int attempt = 0; attempt < 8 && !done; ++attempt)
+  {
+    VDBG_TRY(fetch_status(m, s));
+    const uint32_t err = m->h_status->error;
+    m->n_leaves        = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
+    if (err == 0)
+    {
+      done = true;
+      break;
+    }
+    if (err & (kErrSpin | kErrStepBound)) return map_error(err);
+    if (err & kErrCoordRange)
+    {
+      // The cloud was not marked; integrate what else is pending.
+      call_status        = VDBG_ERR_COORD_RANGE;
+      DevStatus clean;
+      clear_status(&clean);
+      clean.n_leaves     = m->n_leaves;
+      *m->h_status       = clean;
+      VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+      VDBG_TRY(sweeps());
+      continue;
+    }
+    // Pool or hash exhausted: grow, clear the error, mark again, sweep.
+    const uint64_t requested = m->h_status->n_leaves;
+    VDBG_TRY(grow_for(m, requested));
+    DevStatus keep = *m->h_status;
+    keep.error     = 0;
+    keep.n_leaves  = m->n_leaves;
+    *m->h_status   = keep;
+    VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+    if (queued)
+    {
+      k_dda_mark<<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(m->d_rays, m->d_order, n, g,
+                                                                       map_view(m), channel_view(*src));
+      VDBG_CUDA(cudaGetLastError());
+      m->timings.launches += 1;
+      m->timings.retries += 1;
+      m->timed_prep = false;  // phases overlap the growth; only the total is meaningful
+    }
+    VDBG_TRY(sweeps());
+  }
+  if (!done) return VDBG_ERR_OUT_OF_MEMORY;
+  record_timings(m);
+  for (Channel* c : todo) VDBG_TRY(finish_sweep(m, *c, s));
+  if (!todo.empty()) VDBG_CUDA(cudaStreamSynchronize(s));
+  fill_stats(m, leaves_before, stats);
+  VDBG_TRY(maybe_grow_ahead(m));
+  return call_status;
+}
+
+} // namespace
+
+extern "C" {
+
+const char* vdbg_status_string(int s)
+{
+  switch (s)
+  {
+    case VDBG_OK: return "ok";
+    case VDBG_ERR_NOT_CONFIGURED: return "Map not properly configured. Did you call setConfig method?";
+    case VDBG_ERR_UNKNOWN_SOURCE: return "Source not available";
+    case VDBG_ERR_BAD_RANGE: return "Range cannot be negative";
+    case VDBG_ERR_BAD_PROBABILITY: return "Probability for a miss should be below 0.5 and for a hit above 0.5";
+    case VDBG_ERR_DUPLICATE_SOURCE: return "Source already registered";
+    case VDBG_ERR_INVALID_ARGUMENT: return "Invalid argument";
+    case VDBG_ERR_OUT_OF_MEMORY: return "Out of device memory (or over the map's memory budget)";
+    case VDBG_ERR_COORD_RANGE: return "Voxel index outside [-2^23, 2^23)";
+    case VDBG_ERR_CUDA: return "CUDA error";
+    case VDBG_ERR_TIMEOUT: return "Bounded device wait gave up";
+    case VDBG_ERR_BUFFER_TOO_SMALL: return "Buffer too small";
+    default: return "unknown status";
+  }
+}
+
+int vdbg_create(double resolution, const vdbg_options* options, vdbg_map** out)
+{
+  if (!out) return VDBG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (!(resolution > 0.0) || !std::isfinite(resolution)) return VDBG_ERR_INVALID_ARGUMENT;
+  vdbg_map* m  = new vdbg_map();
+  m->resolution = resolution;
+  m->half_res   = resolution / 2.0;
+  m->inv_res    = 1.0 / resolution;
+  uint32_t cap  = kDefaultCapacity;
+  if (options)
+  {
+    if (options->initial_leaf_capacity > 0)
+      cap = static_cast<uint32_t>(std::min<int64_t>(options->initial_leaf_capacity, int64_t(1) << 30));
+    m->max_bytes = options->max_device_bytes;
+    m->device    = options->device;
+  }
+  else
+  {
+    cudaGetDevice(&m->device);
+  }
+  auto fail = [&](int s) {
+    vdbg_destroy(m);
+    return s;
+  };
+  if (cudaSetDevice(m->device) != cudaSuccess) return fail(VDBG_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(VDBG_ERR_CUDA);
+  if (cudaEventCreate(&m->ev0) != cudaSuccess || cudaEventCreate(&m->ev1) != cudaSuccess ||
+      cudaEventCreate(&m->ev_prep) != cudaSuccess || cudaEventCreate(&m->ev_dda) != cudaSuccess)
+    return fail(VDBG_ERR_CUDA);
+  if (cudaMallocHost(reinterpret_cast<void**>(&m->h_status), sizeof(DevStatus)) != cudaSuccess)
+    return fail(VDBG_ERR_OUT_OF_MEMORY);
+  clear_status(m->h_status);
+  int s = dev_alloc(m, &m->d_status, 1);
+  if (s != VDBG_OK) return fail(s);
+  s = dev_alloc(m, &m->d_hist, kNumBuckets);
+  if (s != VDBG_OK) return fail(s);
+  s = dev_alloc(m, &m->d_cursor, kNumBuckets);
+  if (s != VDBG_OK) return fail(s);
+  if (cudaMemsetAsync(m->d_hist, 0, kNumBuckets * sizeof(uint32_t), m->stream) != cudaSuccess)
+    return fail(VDBG_ERR_CUDA);
+  s = resize_pool(m, cap, 0);
+  if (s != VDBG_OK) return fail(s);
+  if (cudaStreamSynchronize(m->stream) != cudaSuccess) return fail(VDBG_ERR_CUDA);
+  *out = m;
+  return VDBG_OK;
+}
+
+int vdbg_destroy(vdbg_map* m)
+{
+  if (!m) return VDBG_OK;
+  cudaSetDevice(m->device);
+  if (m->stream) cudaStreamSynchronize(m->stream);
+  for (Channel& c : m->channels)
+  {
+    free_channel(m, c, m->capacity);
+    dev_free(m, c.n_touched, 1);
+  }
+  dev_free(m, m->values, static_cast<size_t>(m->capacity) * 512);
+  dev_free(m, m->active, static_cast<size_t>(m->capacity) * 8);
+  dev_free(m, m->origin, m->capacity);
+  dev_free(m, m->flags, m->capacity);
+  dev_free(m, m->hkeys, m->hash_size);
+  dev_free(m, m->hslots, m->hash_size);
+  dev_free(m, m->d_status, 1);
+  dev_free(m, m->d_hist, kNumBuckets);
+  dev_free(m, m->d_cursor, kNumBuckets);
+  dev_free(m, m->d_pts, m->pts_cap);
+  dev_free(m, m->d_rays, m->ray_cap);
+  dev_free(m, m->d_order, m->ray_cap);
+  if (m->h_status) cudaFreeHost(m->h_status);
+  if (m->ev0) cudaEventDestroy(m->ev0);
+  if (m->ev1) cudaEventDestroy(m->ev1);
+  if (m->ev_prep) cudaEventDestroy(m->ev_prep);
+  if (m->ev_dda) cudaEventDestroy(m->ev_dda);
+  if (m->stream) cudaStreamDestroy(m->stream);
+  delete m;
+  return VDBG_OK;
+}
+
+int vdbg_set_config(vdbg_map* m, const vdbg_config* c)
+{
+  if (!m || !c) return VDBG_ERR_INVALID_ARGUMENT;
+  if (c->max_range < 0.0) return VDBG_ERR_BAD_RANGE;
+  m->max_range           = c->max_range;
+  m->fast_mode           = c->fast_mode != 0;
+  m->accumulation_period = c->accumulation_period;
+  m->config_set          = true;
+  if (c->prob_miss > 0.5) return VDBG_ERR_BAD_PROBABILITY;
+  if (c->prob_hit < 0.5) return VDBG_ERR_BAD_PROBABILITY;
+  m->lo.miss      = static_cast<float>(std::log(c->prob_miss) - std::log(1 - c->prob_miss));
+  m->lo.hit       = static_cast<float>(std::log(c->prob_hit) - std::log(1 - c->prob_hit));
+  m->lo.thres_min = static_cast<float>(std::log(c->prob_thres_min) - std::log(1 - c->prob_thres_min));
+  m->lo.thres_max = static_cast<float>(std::log(c->prob_thres_max) - std::log(1 - c->prob_thres_max));
+  m->lo.max       = static_cast<float>(std::log(0.99) - std::log(0.01));
+  m->lo.min       = static_cast<float>(std::log(0.01) - std::log(0.99));
+  return VDBG_OK;
+}
+
+int vdbg_get_log_odds(const vdbg_map* m, float out6[6])
+{
+  if (!m || !out6) return VDBG_ERR_INVALID_ARGUMENT;
+  out6[0] = m->lo.hit;
+  out6[1] = m->lo.miss;
+  out6[2] = m->lo.thres_min;
+  out6[3] = m->lo.thres_max;
+  out6[4] = m->lo.max;
+  out6[5] = m->lo.min;
+  return VDBG_OK;
+}
+
+int vdbg_add_input_source(vdbg_map* m, const char* id, double max_range, double max_rate)
+{
+  (void)max_rate;
+  if (!m || !id) return VDBG_ERR_INVALID_ARGUMENT;
+  if (find_channel(m, id)) return VDBG_ERR_DUPLICATE_SOURCE;
+  VDBG_TRY(set_device(m));
+  Channel c;
+  c.id        = id;
+  c.max_range = (max_range == 0) ? m->max_range : max_range;
+  VDBG_TRY(alloc_channel(m, c, m->capacity));
+  VDBG_CUDA(cudaMemsetAsync(c.n_touched, 0, sizeof(uint32_t), m->stream));
+  VDBG_CUDA(cudaStreamSynchronize(m->stream));
+  m->channels.push_back(c);
+  std::sort(m->channels.begin(), m->channels.end(),
+            [](const Channel& a, const Channel& b) { return a.id < b.id; });
+  return VDBG_OK;
+}
+
+int vdbg_accumulate_update(vdbg_map* m, const float* xyz, int64_t n, int64_t stride, const double origin[3],
+                           const char* id, uint32_t flags, void* stream, vdbg_scan_stats* stats)
+{
+  if (!m || !origin || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  Channel* src = find_channel(m, id);
+  if (!src) return VDBG_ERR_UNKNOWN_SOURCE;
+  if (!(src->max_range > 0)) return VDBG_OK;
+  if (!m->config_set) return VDBG_ERR_NOT_CONFIGURED;
+  return accumulate_and_integrate(m, xyz, n, stride, origin, src, src->max_range, flags, pick_stream(m, stream),
+                                  false, nullptr, stats);
+}
+
+int vdbg_integrate_update(vdbg_map* m, void* stream, vdbg_scan_stats* stats)
+{
+  if (!m) return VDBG_ERR_INVALID_ARGUMENT;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  return accumulate_and_integrate(m, nullptr, 0, 16, nullptr, nullptr, 0.0, 0, pick_stream(m, stream), true,
+                                  nullptr, stats);
+}
+
+int vdbg_insert_point_cloud(vdbg_map* m, const float* xyz, int64_t n, int64_t stride, const double origin[3],
+                            const char* id, uint32_t flags, void* stream, vdbg_scan_stats* stats)
+{
+  if (!m || !origin || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  Channel* src  = find_channel(m, id);
+  int pre       = VDBG_OK;
+  if (!src)
+    pre = VDBG_ERR_UNKNOWN_SOURCE;
+  else if (src->max_range > 0 && !m->config_set)
+    pre = VDBG_ERR_NOT_CONFIGURED;
+  const bool cast = src && src->max_range > 0 && m->config_set;
+  const int r     = accumulate_and_integrate(m, xyz, n, stride, origin, cast ? src : nullptr,
+                                             cast ? src->max_range : 0.0, flags, pick_stream(m, stream), true,
+                                             nullptr, stats);
+  return r != VDBG_OK ? r : pre;
+}
+
+int vdbg_raycast_point_cloud(vdbg_map* m, const float* xyz, int64_t n, int64_t stride, const double origin[3],
+                             double range, const char* id, uint32_t flags, void* stream,
+                             vdbg_scan_stats* stats)
+{
+  if (!m || !origin || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  if (!m->config_set) return VDBG_ERR_NOT_CONFIGURED;
+  Channel* src = find_channel(m, id);
+  if (!src) return VDBG_ERR_UNKNOWN_SOURCE;
+  return accumulate_and_integrate(m, xyz, n, stride, origin, src, range, flags, pick_stream(m, stream), false,
+                                  nullptr, stats);
+}
+
+int vdbg_update_map(vdbg_map* m, const char* id, void* stream, vdbg_scan_stats* stats)
+{
+  if (!m) return VDBG_ERR_INVALID_ARGUMENT;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  Channel* src = find_channel(m, id);
+  if (!src) return VDBG_ERR_UNKNOWN_SOURCE;
+  return accumulate_and_integrate(m, nullptr, 0, 16, nullptr, nullptr, 0.0, 0, pick_stream(m, stream), false,
+                                  src, stats);
+}
+
+int vdbg_reset_map(vdbg_map* m)
+{
+  if (!m) return VDBG_ERR_INVALID_ARGUMENT;
+  VDBG_TRY(set_device(m));
+  cudaStream_t s = m->stream;
+  const uint32_t cap = m->capacity;
+  VDBG_CUDA(cudaMemsetAsync(m->values, 0, static_cast<size_t>(cap) * 512 * sizeof(float), s));
+  VDBG_CUDA(cudaMemsetAsync(m->active, 0, static_cast<size_t>(cap) * 8 * sizeof(unsigned long long), s));
+  VDBG_CUDA(cudaMemsetAsync(m->flags, 0, static_cast<size_t>(cap) * sizeof(uint32_t), s));
+  VDBG_CUDA(cudaMemsetAsync(m->hkeys, 0xff, static_cast<size_t>(m->hash_size) * sizeof(unsigned long long), s));
+  VDBG_CUDA(cudaMemsetAsync(m->hslots, 0xff, static_cast<size_t>(m->hash_size) * sizeof(int), s));
+  for (Channel& c : m->channels)
+  {
+    VDBG_CUDA(cudaMemsetAsync(c.upd, 0, static_cast<size_t>(cap) * 16 * sizeof(unsigned long long), s));
+    VDBG_CUDA(cudaMemsetAsync(c.epoch, 0, static_cast<size_t>(cap) * sizeof(uint32_t), s));
+    VDBG_CUDA(cudaMemsetAsync(c.n_touched, 0, sizeof(uint32_t), s));
+    c.cur_epoch = 1;
+    c.pending   = false;
+  }
+  VDBG_CUDA(cudaStreamSynchronize(s));
+  m->n_leaves = 0;
+  return VDBG_OK;
+}
+
+int vdbg_leaf_count(vdbg_map* m, int64_t* out)
+{
+  if (!m || !out) return VDBG_ERR_INVALID_ARGUMENT;
+  VDBG_TRY(set_device(m));
+  const uint32_t n = std::min(m->n_leaves, m->capacity);
+  std::vector<uint32_t> flags(n);
+  if (n) VDBG_CUDA(cudaMemcpy(flags.data(), m->flags, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  int64_t c = 0;
+  for (uint32_t f : flags) c += (f != 0);
+  *out = c;
+  return VDBG_OK;
+}
+
+int vdbg_export_leaves(vdbg_map* m, int64_t capacity, int32_t* origins, float* values, uint64_t* masks,
+                       int64_t* n_out)
+{
+  if (!m || !n_out || capacity < 0) return VDBG_ERR_INVALID_ARGUMENT;
+  VDBG_TRY(set_device(m));
+  VDBG_CUDA(cudaStreamSynchronize(m->stream));
+  const uint32_t n = std::min(m->n_leaves, m->capacity);
+  std::vector<uint32_t> flags(n);
+  std::vector<int4> orig(n);
+  if (n)
+  {
+    VDBG_CUDA(cudaMemcpy(flags.data(), m->flags, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    VDBG_CUDA(cudaMemcpy(orig.data(), m->origin, n * sizeof(int4), cudaMemcpyDeviceToHost));
+  }
+  std::vector<uint32_t> idx;
+  idx.reserve(n);
+  for (uint32_t i = 0; i < n; ++i)
+    if (flags[i]) idx.push_back(i);
+  std::sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) {
+    if (orig[a].x != orig[b].x) return orig[a].x < orig[b].x;
+    if (orig[a].y != orig[b].y) return orig[a].y < orig[b].y;
+    return orig[a].z < orig[b].z;
+  });
+  *n_out = static_cast<int64_t>(idx.size());
+  if (static_cast<int64_t>(idx.size()) > capacity) return VDBG_ERR_BUFFER_TOO_SMALL;
+  if (origins)
+  {
+    for (size_t k = 0; k < idx.size(); ++k)
+    {
+      origins[3 * k + 0] = orig[idx[k]].x;
+      origins[3 * k + 1] = orig[idx[k]].y;
+      origins[3 * k + 2] = orig[idx[k]].z;
+    }
+  }
+  if (values || masks)
+  {
+    std::vector<float> hv(values ? static_cast<size_t>(n) * 512 : 0);
+    std::vector<unsigned long long> hm(masks ? static_cast<size_t>(n) * 8 : 0);
+    if (values && n)
+      VDBG_CUDA(cudaMemcpy(hv.data(), m->values, static_cast<size_t>(n) * 512 * sizeof(float),
+                           cudaMemcpyDeviceToHost));
+    if (masks && n)
+      VDBG_CUDA(cudaMemcpy(hm.data(), m->active, static_cast<size_t>(n) * 8 * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < idx.size(); ++k)
+    {
+      if (values) std::memcpy(values + 512 * k, hv.data() + static_cast<size_t>(idx[k]) * 512, 512 * sizeof(float));
+      if (masks) std::memcpy(masks + 8 * k, hm.data() + static_cast<size_t>(idx[k]) * 8, 8 * sizeof(uint64_t));
+    }
+  }
+  return VDBG_OK;
+}
+
+int vdbg_get_timings(const vdbg_map* m, vdbg_timings* out)
+{
+  if (!m || !out) return VDBG_ERR_INVALID_ARGUMENT;
+  *out = m->timings;
+  out->launches_total += m->timings.launches;
+  return VDBG_OK;
+}
+
+int vdbg_device_bytes(const vdbg_map* m, int64_t* out)
+{
+  if (!m || !out) return VDBG_ERR_INVALID_ARGUMENT;
+  *out = m->bytes;
+  return VDBG_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,325 @@
+"""Python mirror of vdb_mapping's OccupancyVDBMapping over the C ABI.
+
+Names, argument meaning and error behaviour follow the reference
+(include/vdb_mapping/VDBMapping.hpp, include/vdb_mapping/OccupancyVDBMapping.hpp):
+errors that the reference prints and swallows are printed and swallowed here
+too (``insertPointCloud`` always returns True, VDBMapping.hpp:399-406);
+everything else the library reports raises ``VdbgError``.
+
+Point clouds are ``numpy`` arrays of shape (N, 3) or (N, 4) float32 in host
+memory (a pcl::PointXYZ cloud is (N, 4)), or CUDA ``torch`` tensors of the same
+shapes, which are read in place on the device.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import VdbgError
+
+
+@dataclass
+class Config:
+    """vdb_mapping::Config (OccupancyVDBMapping.hpp:38-44) + BaseConfig (VDBMapping.hpp:64-71)."""
+
+    max_range: float = 0.0
+    fast_mode: bool = False
+    accumulation_period: float = 0.0
+    prob_hit: float = 0.0
+    prob_miss: float = 0.0
+    prob_thres_min: float = 0.0
+    prob_thres_max: float = 0.0
+    map_directory_path: str = ""
+
+
+def _cloud_args(cloud):
+    """(pointer, n, stride_bytes, flags, keepalive) for a numpy array or CUDA tensor."""
+    if hasattr(cloud, "is_cuda") and cloud.is_cuda:
+        import torch
+
+        if cloud.dtype != torch.float32 or cloud.dim() != 2 or cloud.shape[1] < 3:
+            raise ValueError("CUDA cloud must be a float32 tensor of shape (N, 3+)")
+        if cloud.stride(1) != 1:
+            cloud = cloud.contiguous()
+        return cloud.data_ptr(), cloud.shape[0], cloud.stride(0) * 4, _lib.VDBG_POINTS_DEVICE, cloud
+    if hasattr(cloud, "numpy") and not isinstance(cloud, np.ndarray):
+        cloud = cloud.numpy()
+    arr = np.asarray(cloud)
+    if arr.dtype != np.float32:
+        arr = arr.astype(np.float32)
+    if arr.ndim != 2 or arr.shape[1] < 3:
+        raise ValueError("cloud must have shape (N, 3) or (N, 4)")
+    if arr.strides[1] != 4 or arr.strides[0] % 4:
+        arr = np.ascontiguousarray(arr)
+    return arr.ctypes.data, arr.shape[0], arr.strides[0], 0, arr
+
+
+def _origin(origin):
+    o = (C.c_double * 3)(*[float(v) for v in origin])
+    return o
+
+
+class Grid:
+    """Export of the map (VDBMapping::getGrid, VDBMapping.hpp:799).
+
+    Holds the leaves sorted by origin: ``origins`` (L,3) int32, ``values``
+    (L,512) float32 log-odds in OpenVDB leaf order, ``masks`` (L,8) uint64
+    active masks. ``getAccessor()`` gives OpenVDB-style point queries. A grid
+    obtained from a mapping re-exports itself when the map has changed since,
+    so an accessor taken before an insertion sees its result (as an OpenVDB
+    accessor on the live grid does).
+    """
+
+    def __init__(self, origins, values, masks, owner=None, version=-1):
+        self._set(origins, values, masks)
+        self._owner = owner
+        self._version = version
+
+    def _set(self, origins, values, masks):
+        self.origins = origins
+        self.values = values
+        self.masks = masks
+        self._index = {tuple(o): i for i, o in enumerate(origins.tolist())}
+
+    def _sync(self):
+        if self._owner is not None and self._owner._version != self._version:
+            o, v, m = self._owner._export()
+            self._set(o, v, m)
+            self._version = self._owner._version
+
+    def leafCount(self) -> int:
+        self._sync()
+        return len(self.origins)
+
+    def activeVoxelCount(self) -> int:
+        self._sync()
+        return int(sum(bin(int(w)).count("1") for w in self.masks.ravel()))
+
+    def getAccessor(self):
+        return _Accessor(self)
+
+    def _lookup(self, xyz):
+        self._sync()
+        x, y, z = (int(c) for c in xyz)
+        i = self._index.get((x & ~7, y & ~7, z & ~7))
+        off = ((x & 7) << 6) | ((y & 7) << 3) | (z & 7)
+        return i, off
+
+    def getValue(self, xyz) -> float:
+        i, off = self._lookup(xyz)
+        return 0.0 if i is None else float(self.values[i, off])
+
+    def isValueOn(self, xyz) -> bool:
+        i, off = self._lookup(xyz)
+        if i is None:
+            return False
+        return bool((int(self.masks[i, off >> 6]) >> (off & 63)) & 1)
+
+
+class _Accessor:
+    def __init__(self, grid: Grid):
+        self._g = grid
+
+    def getValue(self, xyz) -> float:
+        return self._g.getValue(xyz)
+
+    def isValueOn(self, xyz) -> bool:
+        return self._g.isValueOn(xyz)
+
+
+class OccupancyVDBMapping:
+    """vdb_mapping::OccupancyVDBMapping (OccupancyVDBMapping.hpp:46-200) on the GPU."""
+
+    def __init__(self, resolution: float, initial_leaf_capacity: int = 0, max_device_bytes: int = 0,
+                 device: int | None = None):
+        self._lib = _lib.load()
+        opts = _lib.vdbg_options()
+        opts.initial_leaf_capacity = int(initial_leaf_capacity)
+        opts.max_device_bytes = int(max_device_bytes)
+        if device is None:
+            try:
+                import torch
+
+                device = torch.cuda.current_device() if torch.cuda.is_available() else 0
+            except Exception:  # pragma: no cover - torch is plumbing only
+                device = 0
+        opts.device = int(device)
+        h = C.c_void_p()
+        s = self._lib.vdbg_create(float(resolution), C.byref(opts), C.byref(h))
+        if s != 0:
+            raise VdbgError(s, "vdbg_create")
+        self._h = h
+        self.resolution = float(resolution)
+        self._version = 0
+        self._grid = None
+        self.last_stats = None
+
+    # -- lifetime -----------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.vdbg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, s, where, swallow=()):
+        if s == 0:
+            return True
+        if s in swallow:
+            return False
+        raise VdbgError(s, where)
+
+    # -- configuration (OccupancyVDBMapping.hpp:59-89, VDBMapping.hpp:1352-1375) ----
+    def setConfig(self, config: Config) -> None:
+        c = _lib.vdbg_config()
+        c.max_range = config.max_range
+        c.fast_mode = 1 if config.fast_mode else 0
+        c.accumulation_period = config.accumulation_period
+        c.prob_hit = config.prob_hit
+        c.prob_miss = config.prob_miss
+        c.prob_thres_min = config.prob_thres_min
+        c.prob_thres_max = config.prob_thres_max
+        s = self._lib.vdbg_set_config(self._h, C.byref(c))
+        if s == _lib.STATUS_CODE["VDBG_ERR_BAD_RANGE"]:
+            print(f"Max range of {config.max_range} invalid. Range cannot be negative.", file=sys.stderr)
+        elif s == _lib.STATUS_CODE["VDBG_ERR_BAD_PROBABILITY"]:
+            if config.prob_miss > 0.5:
+                print(f"Probability for a miss should be below 0.5 but is {config.prob_miss}", file=sys.stderr)
+            else:
+                print(f"Probability for a hit should be above 0.5 but is {config.prob_hit}", file=sys.stderr)
+        else:
+            self._check(s, "vdbg_set_config")
+
+    def logOdds(self):
+        out = (C.c_float * 6)()
+        self._check(self._lib.vdbg_get_log_odds(self._h, out), "vdbg_get_log_odds")
+        keys = ("hit", "miss", "thres_min", "thres_max", "max", "min")
+        return dict(zip(keys, list(out)))
+
+    def addInputSource(self, source_id: str, max_range: float, max_rate: float) -> None:
+        self._check(self._lib.vdbg_add_input_source(self._h, source_id.encode(), float(max_range),
+                                                    float(max_rate)), "vdbg_add_input_source")
+
+    # -- the hot path -------------------------------------------------------------
+    def _cloud_call(self, fn, cloud, origin, *extra, stream=None):
+        ptr, n, stride, flags, keep = _cloud_args(cloud)
+        st = _lib.vdbg_scan_stats()
+        s = fn(self._h, C.c_void_p(ptr), n, stride, _origin(origin), *extra, flags,
+               C.c_void_p(stream) if stream else None, C.byref(st))
+        del keep
+        self.last_stats = st.as_dict()
+        self._version += 1
+        return s
+
+    def insertPointCloud(self, cloud, origin, source_id: str, stream=None) -> bool:
+        """VDBMapping.hpp:399-406; always True, like the reference."""
+        s = self._cloud_call(self._lib.vdbg_insert_point_cloud, cloud, origin, source_id.encode(),
+                             stream=stream)
+        if s == _lib.STATUS_CODE["VDBG_ERR_UNKNOWN_SOURCE"]:
+            print(f"Tried to accumulate update for {source_id}. Source not available")
+        elif s == _lib.STATUS_CODE["VDBG_ERR_NOT_CONFIGURED"]:
+            print("Map not properly configured. Did you call setConfig method?", file=sys.stderr)
+        else:
+            self._check(s, "vdbg_insert_point_cloud")
+        return True
+
+    def accumulateUpdate(self, cloud, origin, source_id: str, stream=None) -> None:
+        """VDBMapping.hpp:316-346."""
+        s = self._cloud_call(self._lib.vdbg_accumulate_update, cloud, origin, source_id.encode(),
+                             stream=stream)
+        if s == _lib.STATUS_CODE["VDBG_ERR_UNKNOWN_SOURCE"]:
+            print(f"Tried to accumulate update for {source_id}. Source not available")
+        elif s == _lib.STATUS_CODE["VDBG_ERR_NOT_CONFIGURED"]:
+            print("Map not properly configured. Did you call setConfig method?", file=sys.stderr)
+        else:
+            self._check(s, "vdbg_accumulate_update")
+
+    def integrateUpdate(self, stream=None) -> None:
+        """VDBMapping.hpp:375-387."""
+        st = _lib.vdbg_scan_stats()
+        s = self._lib.vdbg_integrate_update(self._h, C.c_void_p(stream) if stream else None, C.byref(st))
+        self.last_stats = st.as_dict()
+        self._version += 1
+        self._check(s, "vdbg_integrate_update")
+
+    def raycastPointCloud(self, cloud, origin, raycast_range: float, source_id: str, stream=None) -> bool:
+        """VDBMapping.hpp:466-539 into the update grid of `source_id`."""
+        s = self._cloud_call(self._lib.vdbg_raycast_point_cloud, cloud, origin, float(raycast_range),
+                             source_id.encode(), stream=stream)
+        if s == _lib.STATUS_CODE["VDBG_ERR_NOT_CONFIGURED"]:
+            print("Map not properly configured. Did you call setConfig method?", file=sys.stderr)
+            return False
+        self._check(s, "vdbg_raycast_point_cloud")
+        return True
+
+    def updateMap(self, source_id: str, stream=None) -> None:
+        """VDBMapping.hpp:731-792 for one source's update grid."""
+        st = _lib.vdbg_scan_stats()
+        s = self._lib.vdbg_update_map(self._h, source_id.encode(), C.c_void_p(stream) if stream else None,
+                                      C.byref(st))
+        self.last_stats = st.as_dict()
+        self._version += 1
+        self._check(s, "vdbg_update_map")
+
+    def resetMap(self) -> None:
+        """VDBMapping.hpp:174-186."""
+        self._check(self._lib.vdbg_reset_map(self._h), "vdbg_reset_map")
+        self._version += 1
+        self._grid = None
+
+    # -- export -------------------------------------------------------------------
+    def leafCount(self) -> int:
+        n = C.c_int64()
+        self._check(self._lib.vdbg_leaf_count(self._h, C.byref(n)), "vdbg_leaf_count")
+        return n.value
+
+    def timings(self) -> dict:
+        """Per-phase device times and launch counts of the last call."""
+        t = _lib.vdbg_timings()
+        self._check(self._lib.vdbg_get_timings(self._h, C.byref(t)), "vdbg_get_timings")
+        return t.as_dict()
+
+    def deviceBytes(self) -> int:
+        n = C.c_int64()
+        self._check(self._lib.vdbg_device_bytes(self._h, C.byref(n)), "vdbg_device_bytes")
+        return n.value
+
+    def _export(self):
+        n = C.c_int64()
+        cap = self.leafCount()
+        while True:
+            origins = np.zeros((cap, 3), np.int32)
+            values = np.zeros((cap, 512), np.float32)
+            masks = np.zeros((cap, 8), np.uint64)
+            s = self._lib.vdbg_export_leaves(self._h, cap, origins.ctypes.data, values.ctypes.data,
+                                             masks.ctypes.data, C.byref(n))
+            if s == _lib.STATUS_CODE["VDBG_ERR_BUFFER_TOO_SMALL"]:
+                cap = n.value
+                continue
+            self._check(s, "vdbg_export_leaves")
+            k = n.value
+            return origins[:k], values[:k], masks[:k]
+
+    def exportLeaves(self):
+        """(origins, values, masks) sorted by leaf origin."""
+        return self._export()
+
+    def getGrid(self) -> Grid:
+        if self._grid is None:
+            self._grid = Grid(np.zeros((0, 3), np.int32), np.zeros((0, 512), np.float32),
+                              np.zeros((0, 8), np.uint64), owner=self, version=-1)
+        return self._grid

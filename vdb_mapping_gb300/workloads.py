@@ -1,0 +1,275 @@
+"""Seeded synthetic scan workloads with the shapes of the benchmark configs.
+
+No public dataset is used: each config is a procedurally generated scene that
+a simulated sensor scans. Points are float32 in the map frame, laid out as
+pcl::PointXYZ (x, y, z, pad) rows of 16 bytes.
+
+  small   seed 1: 40x40x6 m room with 20 random boxes; 64x1024 LiDAR beams
+          (elevation -25..+15 deg, uniform azimuth); 10 scans from (0,0,1.5)
+          stepping 0.2 m along x; range noise sigma 2 cm; 5% no-returns;
+          voxel 0.1 m, max_range 30 m.
+  dense   seed 2: 200x200x20 m street (buildings, cars as boxes, poles and
+          trees as cylinders); 128x2048 beams; 100 scans stepping 1 m along
+          the street; sigma 1 cm; 3% no-returns; voxel 0.05 m, max_range 60 m.
+  stress  seed 3: 20 scans of 65,536 rays with uniform random directions and
+          log-uniform ranges 0.5-200 m from (5000,-3000,40); 1% of endpoints
+          on quantiser boundaries and DDA tie directions; voxel 0.02 m,
+          max_range 250 m.
+
+A no-return beam gets its endpoint at twice the max range along the beam, so
+the reference's strict `length > max_range` clip turns it into free space.
+All configs use prob_hit 0.7, prob_miss 0.4 and the thresholds 0.12/0.97.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .mapping import Config
+
+
+def default_config(max_range: float) -> Config:
+    return Config(max_range=max_range, fast_mode=False, accumulation_period=0.0, prob_hit=0.7,
+                  prob_miss=0.4, prob_thres_min=0.12, prob_thres_max=0.97)
+
+
+# ---------------------------------------------------------------------------
+# Ray-scene intersection (float64, vectorised over rays)
+# ---------------------------------------------------------------------------
+
+def _hit_boxes(o, d, boxes, t_best):
+    """Nearest entry of rays (origin o (3,), dirs d (N,3)) into axis-aligned
+    boxes [(lo(3), hi(3)), ...]; updates t_best in place."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        inv = 1.0 / d
+    for lo, hi in boxes:
+        t1 = (lo - o) * inv
+        t2 = (hi - o) * inv
+        tmin = np.nanmax(np.minimum(t1, t2), axis=1)
+        tmax = np.nanmin(np.maximum(t1, t2), axis=1)
+        ok = (tmax >= tmin) & (tmax > 0) & (tmin > 1e-6)
+        t_best[ok] = np.minimum(t_best[ok], tmin[ok])
+
+
+def _hit_room_inside(o, d, lo, hi, t_best):
+    """Exit distance of rays from inside the box [lo, hi]."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        inv = 1.0 / d
+        t1 = (lo - o) * inv
+        t2 = (hi - o) * inv
+    tmax = np.nanmin(np.where(np.isfinite(np.maximum(t1, t2)), np.maximum(t1, t2), np.inf), axis=1)
+    np.minimum(t_best, tmax, out=t_best)
+
+
+def _hit_cylinders(o, d, cyls, t_best):
+    """Vertical cylinders [(cx, cy, r, z0, z1), ...] (outer surface)."""
+    a = d[:, 0] ** 2 + d[:, 1] ** 2
+    for cx, cy, r, z0, z1 in cyls:
+        ox, oy = o[0] - cx, o[1] - cy
+        b = 2 * (ox * d[:, 0] + oy * d[:, 1])
+        c = ox * ox + oy * oy - r * r
+        disc = b * b - 4 * a * c
+        ok = (disc >= 0) & (a > 1e-12)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            t = (-b - np.sqrt(np.where(ok, disc, 0))) / (2 * a)
+        z = o[2] + t * d[:, 2]
+        ok &= (t > 1e-6) & (z >= z0) & (z <= z1)
+        t_best[ok] = np.minimum(t_best[ok], t[ok])
+
+
+def _hit_ground(o, d, t_best, z=0.0):
+    with np.errstate(divide="ignore", invalid="ignore"):
+        t = (z - o[2]) / d[:, 2]
+    ok = (d[:, 2] < 0) & (t > 0)
+    t_best[ok] = np.minimum(t_best[ok], t[ok])
+
+
+def lidar_directions(rows: int, cols: int, el_min=-25.0, el_max=15.0) -> np.ndarray:
+    el = np.deg2rad(np.linspace(el_min, el_max, rows))
+    az = np.arange(cols) * (2 * np.pi / cols)
+    ce, se = np.cos(el)[:, None], np.sin(el)[:, None]
+    d = np.stack([np.broadcast_to(ce * np.cos(az)[None, :], (rows, cols)),
+                  np.broadcast_to(ce * np.sin(az)[None, :], (rows, cols)),
+                  np.broadcast_to(se, (rows, cols))], axis=-1)
+    return d.reshape(-1, 3)
+
+
+def _to_pcl(o, d, r) -> np.ndarray:
+    pts = np.empty((d.shape[0], 4), np.float32)
+    pts[:, :3] = (o[None, :] + d * r[:, None]).astype(np.float32)
+    pts[:, 3] = 1.0
+    return pts
+
+
+# ---------------------------------------------------------------------------
+# Workloads
+# ---------------------------------------------------------------------------
+
+@dataclass
+class Workload:
+    name: str
+    resolution: float
+    max_range: float
+    n_scans: int
+    points_per_scan: int
+    seed: int
+    config: Config = field(default=None)
+
+    def __post_init__(self):
+        if self.config is None:
+            self.config = default_config(self.max_range)
+
+    def scan(self, k: int):
+        """(points (N,4) float32, origin (3,) float64) of scan k."""
+        raise NotImplementedError
+
+    def describe(self) -> dict:
+        return {"workload": self.name, "points_per_scan": self.points_per_scan, "scans": self.n_scans,
+                "voxel_m": self.resolution, "max_range_m": self.max_range, "seed": self.seed}
+
+
+class RoomWorkload(Workload):
+    def __init__(self, name="small", seed=1, rows=64, cols=1024, n_scans=10, resolution=0.1,
+                 max_range=30.0, sigma=0.02, no_return=0.05, n_boxes=20):
+        super().__init__(name, resolution, max_range, n_scans, rows * cols, seed)
+        rng = np.random.default_rng(seed)
+        self.lo, self.hi = np.array([-20.0, -20.0, 0.0]), np.array([20.0, 20.0, 6.0])
+        self.boxes = []
+        while len(self.boxes) < n_boxes:
+            c = rng.uniform([-18, -18], [18, 18])
+            size = rng.uniform([0.3, 0.3, 0.5], [3.0, 3.0, 3.0])
+            lo = np.array([c[0] - size[0] / 2, c[1] - size[1] / 2, 0.0])
+            hi = np.array([c[0] + size[0] / 2, c[1] + size[1] / 2, size[2]])
+            # keep the sensor path (x in [-1, 3], |y| < 1) clear
+            if hi[0] > -1.5 and lo[0] < 3.5 and hi[1] > -1.5 and lo[1] < 1.5:
+                continue
+            self.boxes.append((lo, hi))
+        self.dirs = lidar_directions(rows, cols)
+        self.sigma, self.no_return, self.seed = sigma, no_return, seed
+
+    def origin(self, k):
+        return np.array([0.2 * k, 0.0, 1.5])
+
+    def scan(self, k):
+        o = self.origin(k)
+        d = self.dirs
+        t = np.full(d.shape[0], np.inf)
+        _hit_room_inside(o, d, self.lo, self.hi, t)
+        _hit_boxes(o, d, self.boxes, t)
+        rng = np.random.default_rng([self.seed, k])
+        r = t + rng.normal(0.0, self.sigma, t.shape)
+        lost = (rng.random(t.shape) < self.no_return) | ~np.isfinite(t)
+        r = np.where(lost, 2.0 * self.max_range, r)
+        return _to_pcl(o, d, r), o
+
+
+class StreetWorkload(Workload):
+    def __init__(self, name="dense", seed=2, rows=128, cols=2048, n_scans=100, resolution=0.05,
+                 max_range=60.0, sigma=0.01, no_return=0.03):
+        super().__init__(name, resolution, max_range, n_scans, rows * cols, seed)
+        rng = np.random.default_rng(seed)
+        boxes, cyls = [], []
+        # Buildings along both sides of a 20 m wide street running along x.
+        for side in (-1, 1):
+            x = -100.0
+            while x < 100.0:
+                w = rng.uniform(8, 25)
+                depth = rng.uniform(10, 30)
+                h = rng.uniform(5, 20)
+                setback = rng.uniform(10, 14)
+                y0 = side * setback
+                y1 = side * (setback + depth)
+                boxes.append((np.array([x, min(y0, y1), 0.0]), np.array([x + w, max(y0, y1), h])))
+                x += w + rng.uniform(1, 6)
+        # Parked cars.
+        for _ in range(60):
+            cx = rng.uniform(-100, 100)
+            cy = rng.choice([-1, 1]) * rng.uniform(5.5, 8.0)
+            boxes.append((np.array([cx - 2.2, cy - 0.9, 0.0]), np.array([cx + 2.2, cy + 0.9, 1.5])))
+        # Poles and trees on the sidewalks.
+        for _ in range(80):
+            cx = rng.uniform(-100, 100)
+            cy = rng.choice([-1, 1]) * rng.uniform(8.5, 9.8)
+            r = rng.uniform(0.08, 0.5)
+            cyls.append((cx, cy, r, 0.0, rng.uniform(3, 9)))
+        self.boxes, self.cyls = boxes, cyls
+        self.dirs = lidar_directions(rows, cols)
+        self.sigma, self.no_return = sigma, no_return
+        self.bounds_lo, self.bounds_hi = np.array([-100.0, -100.0, 0.0]), np.array([100.0, 100.0, 20.0])
+
+    def origin(self, k):
+        return np.array([-50.0 + 1.0 * k, 0.0, 1.8])
+
+    def scan(self, k):
+        o = self.origin(k)
+        d = self.dirs
+        t = np.full(d.shape[0], np.inf)
+        _hit_ground(o, d, t)
+        # Only primitives within reach of this scan.
+        reach = 2.0 * self.max_range
+        near_boxes = [b for b in self.boxes
+                      if (b[0][0] - o[0] < reach) and (o[0] - b[1][0] < reach)]
+        near_cyls = [c for c in self.cyls if abs(c[0] - o[0]) < reach]
+        _hit_boxes(o, d, near_boxes, t)
+        _hit_cylinders(o, d, near_cyls, t)
+        # The scene ends at its 200x200x20 m bounds: no return beyond.
+        exit_t = np.full(d.shape[0], np.inf)
+        _hit_room_inside(o, d, self.bounds_lo, self.bounds_hi, exit_t)
+        t = np.where(t <= exit_t, t, np.inf)
+        rng = np.random.default_rng([self.seed, k])
+        r = t + rng.normal(0.0, self.sigma, t.shape)
+        lost = (rng.random(t.shape) < self.no_return) | ~np.isfinite(t)
+        r = np.where(lost, 2.0 * self.max_range, r)
+        return _to_pcl(o, d, r), o
+
+
+class StressWorkload(Workload):
+    def __init__(self, name="stress", seed=3, n_rays=65536, n_scans=20, resolution=0.02, max_range=250.0,
+                 origin=(5000.0, -3000.0, 40.0), special_frac=0.01):
+        super().__init__(name, resolution, max_range, n_scans, n_rays, seed)
+        self.base_origin = np.array(origin, np.float64)
+        self.special_frac = special_frac
+
+    def origin(self, k):
+        return self.base_origin + np.array([0.37 * k, -0.21 * k, 0.05 * k])
+
+    def scan(self, k):
+        rng = np.random.default_rng([self.seed, k])
+        n = self.points_per_scan
+        o = self.origin(k)
+        v = rng.normal(size=(n, 3))
+        v /= np.linalg.norm(v, axis=1, keepdims=True)
+        r = np.exp(rng.uniform(np.log(0.5), np.log(200.0), n))
+        pts = _to_pcl(o, v, r)
+        res = self.resolution
+        n_sp = int(round(self.special_frac * n))
+        idx = rng.choice(n, size=n_sp, replace=False)
+        half = n_sp // 2
+        # Quantiser boundaries: coordinates at (k - 1/2) * res (float32 nearest).
+        for i in idx[:half]:
+            axes = rng.random(3) < 0.6
+            axes[rng.integers(3)] = True
+            for a in np.nonzero(axes)[0]:
+                kk = np.round(pts[i, a] / res)
+                pts[i, a] = np.float32((kk - 0.5) * res)
+        # DDA tie directions: voxel deltas with equal or small-ratio components.
+        ovox = np.floor(o / res + 0.5)
+        patterns = [(1, 1, 0), (1, 1, 1), (1, 3, 0), (2, 6, 0), (1, 1, 2), (3, 5, 0), (1, 3, 5), (2, 2, 1)]
+        for i in idx[half:]:
+            p = np.array(patterns[rng.integers(len(patterns))], np.float64)
+            p = p[rng.permutation(3)] * rng.choice([-1, 1], 3)
+            scale = rng.integers(1, max(2, int(150.0 / res / max(1.0, np.abs(p).sum()))))
+            vox = ovox + p * scale
+            pts[i, :3] = (vox * res).astype(np.float32)  # voxel centre
+        return pts, o
+
+
+def get(name: str) -> Workload:
+    if name == "small":
+        return RoomWorkload()
+    if name == "dense":
+        return StreetWorkload()
+    if name == "stress":
+        return StressWorkload()
+    raise KeyError(name)
