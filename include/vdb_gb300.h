@@ -1,7 +1,7 @@
 /* vdb_gb300.h — C ABI of the GB300 scan-insertion library (libvdb_gb300.so).
  *
  * The reference (vdb_mapping) is a header-only C++ class template with no C
- * ABI; this interface is the boundary its C++ API (include/vdb_mapping/*.hpp
+ * ABI; this interface is the boundary its C++ API (the vdb_mapping/ headers
  * in this repository) and any FFI binding call into. Plain pointers, sizes
  * and int status codes only; no exceptions cross it. Every entry point names
  * the reference member it replaces (paths relative to the vdb_mapping tree).

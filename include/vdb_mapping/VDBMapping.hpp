@@ -1,0 +1,555 @@
+// vdb_mapping/VDBMapping.hpp — drop-in for the reference's
+// include/vdb_mapping/VDBMapping.hpp, backed by libvdb_gb300.so.
+//
+// Same namespace, class names, typedefs and member signatures as the
+// reference for the scan-insertion path (VDBMapping.hpp:64-103 config and
+// types, :115-186 construction/reset, :316-406 accumulate/integrate/insert,
+// :466-539 raycastPointCloud, :612-631 worldToIndex, :731-792 updateMap,
+// :799 getGrid, :1343 getMapMutex, :1352-1375 addInputSource, :1456-1469
+// setConfig). The map lives on the GPU; calls are synchronous like the
+// reference's. Differences, all on purpose:
+//   * no background threads: addDataToAccumulate accumulates at once and
+//     integrateUpdate is called by the user (or by insertPointCloud);
+//   * getGrid() returns an export of the device map (GridT). Without OpenVDB
+//     it is a leaf table with OpenVDB-style accessors that re-syncs itself
+//     after every map change; with OpenVDB (VDBG_WITH_OPENVDB) it is an
+//     openvdb::FloatGrid refreshed on each getGrid() call;
+//   * only the occupancy data type (float log-odds) is implemented, which is
+//     the only specialisation the reference ships (OccupancyVDBMapping.hpp).
+// Parts of the reference outside the insertion path (sections, morphology,
+// artificial areas, file I/O, ray queries, fast mode) are not provided.
+#ifndef VDB_MAPPING_GB300_VDB_MAPPING_HPP
+#define VDB_MAPPING_GB300_VDB_MAPPING_HPP
+
+#include <cmath>
+#include <cstdint>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <shared_mutex>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../vdb_gb300.h"
+
+#if defined(VDBG_WITH_OPENVDB)
+#include <eigen3/Eigen/Geometry>
+#include <openvdb/openvdb.h>
+#include <pcl/point_cloud.h>
+#include <pcl/point_types.h>
+#else
+// ---- Stand-ins for the third-party types on the path (PCL, Eigen, OpenVDB) --
+namespace pcl {
+struct PointXYZ
+{
+  float x, y, z;
+  float data_pad;  // pcl::PointXYZ is 16 bytes: x, y, z and a padding float
+  PointXYZ() : x(0.f), y(0.f), z(0.f), data_pad(1.f) {}
+  PointXYZ(float x_, float y_, float z_) : x(x_), y(y_), z(z_), data_pad(1.f) {}
+};
+template <typename PointT>
+class PointCloud
+{
+public:
+  using Ptr      = std::shared_ptr<PointCloud<PointT> >;
+  using ConstPtr = std::shared_ptr<const PointCloud<PointT> >;
+  std::vector<PointT> points;
+  uint32_t width = 0, height = 1;
+  size_t size() const { return points.size(); }
+  bool empty() const { return points.empty(); }
+  typename std::vector<PointT>::const_iterator begin() const { return points.begin(); }
+  typename std::vector<PointT>::const_iterator end() const { return points.end(); }
+};
+} // namespace pcl
+
+namespace Eigen {
+template <typename Scalar, int Rows, int Cols>
+class Matrix
+{
+public:
+  Matrix() : m{} {}
+  Matrix(Scalar x, Scalar y, Scalar z) : m{x, y, z} {}
+  Scalar x() const { return m[0]; }
+  Scalar y() const { return m[1]; }
+  Scalar z() const { return m[2]; }
+  Scalar& x() { return m[0]; }
+  Scalar& y() { return m[1]; }
+  Scalar& z() { return m[2]; }
+  Scalar operator()(int i) const { return m[i]; }
+
+private:
+  Scalar m[Rows * Cols];
+};
+} // namespace Eigen
+
+namespace openvdb {
+using Int32 = int32_t;
+class Coord
+{
+public:
+  Coord() : v{0, 0, 0} {}
+  Coord(Int32 x, Int32 y, Int32 z) : v{x, y, z} {}
+  Int32 x() const { return v[0]; }
+  Int32 y() const { return v[1]; }
+  Int32 z() const { return v[2]; }
+  Int32 operator[](int i) const { return v[i]; }
+  bool operator==(const Coord& o) const { return v[0] == o.v[0] && v[1] == o.v[1] && v[2] == o.v[2]; }
+  bool operator!=(const Coord& o) const { return !(*this == o); }
+
+private:
+  Int32 v[3];
+};
+namespace math {
+template <typename T>
+class Vec3
+{
+public:
+  Vec3() : m{0, 0, 0} {}
+  Vec3(T x, T y, T z) : m{x, y, z} {}
+  T x() const { return m[0]; }
+  T y() const { return m[1]; }
+  T z() const { return m[2]; }
+  T& x() { return m[0]; }
+  T& y() { return m[1]; }
+  T& z() { return m[2]; }
+  T operator[](int i) const { return m[i]; }
+
+private:
+  T m[3];
+};
+} // namespace math
+using Vec3d = math::Vec3<double>;
+} // namespace openvdb
+#endif
+
+namespace vdb_mapping {
+
+/*!
+ * \brief Base configuration (VDBMapping.hpp:64-71).
+ */
+struct BaseConfig
+{
+  double max_range           = 0.0;
+  bool fast_mode             = false;
+  double accumulation_period = 0.0;
+  std::string map_directory_path;
+};
+
+namespace detail {
+
+inline void throw_status(int s, const char* where)
+{
+  throw std::runtime_error(std::string(where) + ": " + vdbg_status_string(s));
+}
+
+// Device map handle shared by the mapping object and the grids it exported.
+struct DeviceMap
+{
+  vdbg_map* map   = nullptr;
+  uint64_t version = 0;  // bumped by every call that can change the map
+  explicit DeviceMap(double resolution)
+  {
+    const int s = vdbg_create(resolution, nullptr, &map);
+    if (s != VDBG_OK) throw_status(s, "vdbg_create");
+  }
+  ~DeviceMap() { vdbg_destroy(map); }
+  DeviceMap(const DeviceMap&) = delete;
+  DeviceMap& operator=(const DeviceMap&) = delete;
+};
+
+// Host snapshot of the device map: leaves sorted by origin.
+struct LeafTable
+{
+  std::vector<int32_t> origins;  // [L][3]
+  std::vector<float> values;     // [L][512]
+  std::vector<uint64_t> masks;   // [L][8]
+  std::map<std::tuple<int32_t, int32_t, int32_t>, size_t> index;
+
+  void load(vdbg_map* m)
+  {
+    int64_t n = 0;
+    vdbg_leaf_count(m, &n);
+    for (;;)
+    {
+      origins.assign(static_cast<size_t>(n) * 3, 0);
+      values.assign(static_cast<size_t>(n) * 512, 0.f);
+      masks.assign(static_cast<size_t>(n) * 8, 0);
+      int64_t got = 0;
+      const int s = vdbg_export_leaves(m, n, origins.data(), values.data(), masks.data(), &got);
+      if (s == VDBG_ERR_BUFFER_TOO_SMALL)
+      {
+        n = got;
+        continue;
+      }
+      if (s != VDBG_OK) throw_status(s, "vdbg_export_leaves");
+      n = got;
+      break;
+    }
+    origins.resize(static_cast<size_t>(n) * 3);
+    values.resize(static_cast<size_t>(n) * 512);
+    masks.resize(static_cast<size_t>(n) * 8);
+    index.clear();
+    for (size_t i = 0; i < static_cast<size_t>(n); ++i)
+      index.emplace(std::make_tuple(origins[3 * i], origins[3 * i + 1], origins[3 * i + 2]), i);
+  }
+};
+
+} // namespace detail
+
+#if !defined(VDBG_WITH_OPENVDB)
+/*!
+ * \brief Export of the device map with the OpenVDB grid calls the insertion
+ * path's users make: getAccessor(), Accessor::getValue / isValueOn,
+ * activeVoxelCount, leafCount. Reads re-sync the snapshot when the map has
+ * changed since it was taken, like an accessor on a live OpenVDB grid.
+ */
+template <typename TData>
+class LeafGrid
+{
+public:
+  using Ptr      = std::shared_ptr<LeafGrid>;
+  using ValueType = TData;
+
+  explicit LeafGrid(std::shared_ptr<detail::DeviceMap> dev) : m_dev(std::move(dev)) {}
+
+  class Accessor
+  {
+  public:
+    Accessor() = default;
+    explicit Accessor(const LeafGrid* g) : m_grid(g) {}
+    TData getValue(const openvdb::Coord& c) const { return m_grid->value(c); }
+    bool isValueOn(const openvdb::Coord& c) const { return m_grid->isOn(c); }
+
+  private:
+    const LeafGrid* m_grid = nullptr;
+  };
+  using ConstAccessor = Accessor;
+
+  Accessor getAccessor() const { return Accessor(this); }
+  Accessor getConstAccessor() const { return Accessor(this); }
+
+  TData value(const openvdb::Coord& c) const
+  {
+    size_t i;
+    uint32_t off;
+    if (!find(c, i, off)) return TData(0);
+    return m_table.values[i * 512 + off];
+  }
+  bool isOn(const openvdb::Coord& c) const
+  {
+    size_t i;
+    uint32_t off;
+    if (!find(c, i, off)) return false;
+    return (m_table.masks[i * 8 + (off >> 6)] >> (off & 63)) & 1ull;
+  }
+  size_t leafCount() const
+  {
+    sync();
+    return m_table.origins.size() / 3;
+  }
+  uint64_t activeVoxelCount() const
+  {
+    sync();
+    uint64_t n = 0;
+    for (uint64_t w : m_table.masks) n += static_cast<uint64_t>(__builtin_popcountll(w));
+    return n;
+  }
+  bool empty() const { return leafCount() == 0; }
+  /*! The raw snapshot: origins [L][3], values [L][512], masks [L][8]. */
+  const detail::LeafTable& leaves() const
+  {
+    sync();
+    return m_table;
+  }
+
+private:
+  void sync() const
+  {
+    if (!m_dev || m_version == m_dev->version) return;
+    m_table.load(m_dev->map);
+    m_version = m_dev->version;
+  }
+  bool find(const openvdb::Coord& c, size_t& i, uint32_t& off) const
+  {
+    sync();
+    const auto it = m_table.index.find(std::make_tuple(c.x() & ~7, c.y() & ~7, c.z() & ~7));
+    if (it == m_table.index.end()) return false;
+    i   = it->second;
+    off = (static_cast<uint32_t>(c.x() & 7) << 6) | (static_cast<uint32_t>(c.y() & 7) << 3) |
+          static_cast<uint32_t>(c.z() & 7);
+    return true;
+  }
+  std::shared_ptr<detail::DeviceMap> m_dev;
+  mutable detail::LeafTable m_table;
+  mutable uint64_t m_version = ~0ull;
+};
+#endif
+
+/*!
+ * \brief Update grid handle (VDBMapping.hpp:89): an update grid living on the
+ * device inside the map it is first used with.
+ */
+class DeviceUpdateGrid
+{
+public:
+  using Ptr = std::shared_ptr<DeviceUpdateGrid>;
+  struct Accessor
+  {
+    DeviceUpdateGrid* grid = nullptr;
+  };
+  static Ptr create(bool /*background*/ = false) { return std::make_shared<DeviceUpdateGrid>(); }
+  Accessor getAccessor() { return Accessor{this}; }
+  bool empty() const { return !m_pending; }
+
+  // Internal: the hidden source id of this grid inside `map`.
+  const std::string& bind(vdbg_map* map)
+  {
+    if (m_map != map)
+    {
+      static uint64_t counter = 0;
+      m_id  = "\x01update-grid-" + std::to_string(++counter);
+      m_map = map;
+      const int s = vdbg_add_input_source(map, m_id.c_str(), 0.0, 0.0);
+      if (s != VDBG_OK) detail::throw_status(s, "vdbg_add_input_source");
+    }
+    return m_id;
+  }
+  bool m_pending = false;
+
+private:
+  vdbg_map* m_map = nullptr;
+  std::string m_id;
+};
+
+/*!
+ * \brief Occupancy-map engine on the GPU (VDBMapping.hpp:77-1568, for the
+ * scan-insertion path).
+ */
+template <typename TData, typename TConfig = BaseConfig>
+class VDBMapping
+{
+public:
+  using PointT      = pcl::PointXYZ;
+  using PointCloudT = pcl::PointCloud<PointT>;
+#if defined(VDBG_WITH_OPENVDB)
+  using GridT = openvdb::Grid<typename openvdb::tree::Tree4<TData, 5, 4, 3>::Type>;
+#else
+  using GridT = LeafGrid<TData>;
+#endif
+  using UpdateGridT = DeviceUpdateGrid;
+
+  VDBMapping()                  = delete;
+  VDBMapping(const VDBMapping&) = delete;
+  VDBMapping& operator=(const VDBMapping&) = delete;
+
+  /*! VDBMapping.hpp:115-134 (no integration thread is started). */
+  explicit VDBMapping(const double resolution)
+    : m_resolution(resolution)
+    , m_dev(std::make_shared<detail::DeviceMap>(resolution))
+    , m_map_mutex(std::make_shared<std::shared_mutex>())
+  {
+    m_vdb_grid = makeGrid();
+  }
+
+  virtual ~VDBMapping() = default;
+
+  /*! VDBMapping.hpp:174-186. */
+  void resetMap()
+  {
+    std::unique_lock map_lock(*m_map_mutex);
+    check(vdbg_reset_map(m_dev->map), "vdbg_reset_map");
+    ++m_dev->version;  // grids and accessors handed out re-sync to the empty map
+  }
+
+  /*! VDBMapping.hpp:316-346. */
+  void accumulateUpdate(const typename PointCloudT::ConstPtr& cloud,
+                        const Eigen::Matrix<double, 3, 1>& origin,
+                        const std::string source_id)
+  {
+    std::shared_lock map_lock(*m_map_mutex);
+    const double o[3] = {origin.x(), origin.y(), origin.z()};
+    const int s = vdbg_accumulate_update(m_dev->map, pointsOf(cloud), sizeOf(cloud), sizeof(PointT), o,
+                                         source_id.c_str(), 0, nullptr, nullptr);
+    if (s == VDBG_ERR_UNKNOWN_SOURCE)
+      std::cout << "Tried to accumulate update for " << source_id << ". Source not available" << std::endl;
+    else if (s == VDBG_ERR_NOT_CONFIGURED)
+      std::cerr << "Map not properly configured. Did you call setConfig method?" << std::endl;
+    else
+      check(s, "vdbg_accumulate_update");
+  }
+
+  /*! VDBMapping.hpp:355-370; accumulated at once (there is no worker thread). */
+  void addDataToAccumulate(const typename PointCloudT::ConstPtr& cloud,
+                           const Eigen::Matrix<double, 3, 1>& origin,
+                           const std::string source_id)
+  {
+    accumulateUpdate(cloud, origin, source_id);
+  }
+
+  /*! VDBMapping.hpp:375-387. */
+  void integrateUpdate()
+  {
+    std::unique_lock map_lock(*m_map_mutex);
+    check(vdbg_integrate_update(m_dev->map, nullptr, nullptr), "vdbg_integrate_update");
+    ++m_dev->version;
+  }
+
+  /*! VDBMapping.hpp:399-406: always true. */
+  bool insertPointCloud(const typename PointCloudT::ConstPtr& cloud,
+                        const Eigen::Matrix<double, 3, 1>& origin,
+                        const std::string source_id)
+  {
+    std::unique_lock map_lock(*m_map_mutex);
+    const double o[3] = {origin.x(), origin.y(), origin.z()};
+    vdbg_scan_stats st;
+    const int s = vdbg_insert_point_cloud(m_dev->map, pointsOf(cloud), sizeOf(cloud), sizeof(PointT), o,
+                                          source_id.c_str(), 0, nullptr, &st);
+    ++m_dev->version;
+    if (s == VDBG_ERR_UNKNOWN_SOURCE)
+      std::cout << "Tried to accumulate update for " << source_id << ". Source not available" << std::endl;
+    else if (s == VDBG_ERR_NOT_CONFIGURED)
+      std::cerr << "Map not properly configured. Did you call setConfig method?" << std::endl;
+    else
+      check(s, "vdbg_insert_point_cloud");
+    m_last_stats = st;
+    return true;
+  }
+
+  /*! VDBMapping.hpp:466-539 (fast_mode off) into `update_grid_acc`'s grid. */
+  bool raycastPointCloud(const typename PointCloudT::ConstPtr& cloud,
+                         const Eigen::Matrix<double, 3, 1>& origin,
+                         const double raycast_range,
+                         typename UpdateGridT::Accessor& update_grid_acc)
+  {
+    if (!m_config_set)
+    {
+      std::cerr << "Map not properly configured. Did you call setConfig method?" << std::endl;
+      return false;
+    }
+    const std::string& id = update_grid_acc.grid->bind(m_dev->map);
+    const double o[3]     = {origin.x(), origin.y(), origin.z()};
+    check(vdbg_raycast_point_cloud(m_dev->map, pointsOf(cloud), sizeOf(cloud), sizeof(PointT), o, raycast_range,
+                                   id.c_str(), 0, nullptr, nullptr),
+          "vdbg_raycast_point_cloud");
+    update_grid_acc.grid->m_pending = true;
+    return true;
+  }
+
+  /*! VDBMapping.hpp:731-792. The change grid is not produced (an empty grid
+   * is returned). */
+  typename UpdateGridT::Ptr updateMap(const typename UpdateGridT::Ptr& temp_grid)
+  {
+    typename UpdateGridT::Ptr change = UpdateGridT::create(false);
+    if (!temp_grid || temp_grid->empty()) return change;
+    const std::string& id = temp_grid->bind(m_dev->map);
+    check(vdbg_update_map(m_dev->map, id.c_str(), nullptr, nullptr), "vdbg_update_map");
+    temp_grid->m_pending = false;
+    ++m_dev->version;
+    return change;
+  }
+
+  /*! VDBMapping.hpp:612-631, on the host with the same IEEE operations. */
+  openvdb::Coord worldToIndex(const openvdb::Vec3d& w) const
+  {
+    double a[3] = {w.x(), w.y(), w.z()};
+    int32_t out[3];
+    const double inv = 1.0 / m_resolution;
+    for (int i = 0; i < 3; ++i)
+    {
+      if (std::fmod(a[i], m_resolution) != 0.0) a[i] = a[i] + (m_resolution / 2.0);
+      out[i] = static_cast<int32_t>(std::floor(a[i] * inv));
+    }
+    return openvdb::Coord(out[0], out[1], out[2]);
+  }
+
+  /*! VDBMapping.hpp:799. */
+  typename GridT::Ptr getGrid() const
+  {
+#if defined(VDBG_WITH_OPENVDB)
+    refreshOpenVDB();
+#endif
+    return m_vdb_grid;
+  }
+
+  /*! VDBMapping.hpp:1343. */
+  std::shared_ptr<std::shared_mutex> getMapMutex() { return m_map_mutex; }
+
+  /*! VDBMapping.hpp:1352-1375 (no worker thread). */
+  void addInputSource(std::string source_id, double max_range, double max_rate)
+  {
+    check(vdbg_add_input_source(m_dev->map, source_id.c_str(), max_range, max_rate), "vdbg_add_input_source");
+  }
+
+  /*! VDBMapping.hpp:1456-1469. */
+  virtual void setConfig(const TConfig& config) = 0;
+
+  /*! Counters of the last insertPointCloud (no counterpart in the reference). */
+  const vdbg_scan_stats& lastStats() const { return m_last_stats; }
+
+  /*! The C ABI handle, for callers that drive the device map directly. */
+  vdbg_map* deviceMap() const { return m_dev->map; }
+
+protected:
+  static void check(int s, const char* where)
+  {
+    if (s != VDBG_OK) detail::throw_status(s, where);
+  }
+  static const float* pointsOf(const typename PointCloudT::ConstPtr& cloud)
+  {
+    return (cloud && !cloud->points.empty()) ? &cloud->points[0].x : nullptr;
+  }
+  static int64_t sizeOf(const typename PointCloudT::ConstPtr& cloud)
+  {
+    return cloud ? static_cast<int64_t>(cloud->points.size()) : 0;
+  }
+  typename GridT::Ptr makeGrid() const
+  {
+#if defined(VDBG_WITH_OPENVDB)
+    auto g = GridT::create(TData());
+    g->setTransform(openvdb::math::Transform::createLinearTransform(m_resolution));
+    g->setGridClass(openvdb::GRID_LEVEL_SET);
+    return g;
+#else
+    return std::make_shared<GridT>(m_dev);
+#endif
+  }
+#if defined(VDBG_WITH_OPENVDB)
+  // Rebuilds the OpenVDB grid from the device export when the map changed.
+  void refreshOpenVDB() const
+  {
+    if (m_grid_version == m_dev->version) return;
+    detail::LeafTable t;
+    t.load(m_dev->map);
+    m_vdb_grid->clear();
+    auto acc = m_vdb_grid->getAccessor();
+    const size_t n = t.origins.size() / 3;
+    for (size_t i = 0; i < n; ++i)
+    {
+      const openvdb::Coord o(t.origins[3 * i], t.origins[3 * i + 1], t.origins[3 * i + 2]);
+      auto* leaf = acc.touchLeaf(o);
+      for (uint32_t off = 0; off < 512; ++off)
+      {
+        const bool on = (t.masks[i * 8 + (off >> 6)] >> (off & 63)) & 1ull;
+        leaf->setValueOnly(off, t.values[i * 512 + off]);
+        leaf->setActiveState(off, on);
+      }
+    }
+    m_grid_version = m_dev->version;
+  }
+  mutable uint64_t m_grid_version = ~0ull;
+#endif
+
+  double m_resolution;
+  std::shared_ptr<detail::DeviceMap> m_dev;
+  mutable typename GridT::Ptr m_vdb_grid;
+  mutable std::shared_ptr<std::shared_mutex> m_map_mutex;
+  bool m_config_set = false;
+  vdbg_scan_stats m_last_stats{};
+};
+
+} // namespace vdb_mapping
+
+#endif

@@ -1,0 +1,130 @@
+// Drop-in check: the reference-style C++ API (include/vdb_mapping/*.hpp) on
+// the GPU library. Mirrors the known answers of the reference's unit tests
+// (unconfigured insert, positive and negative axis points, the max-range
+// clip, reset) plus an accumulate/integrate round with two sources. Uses the
+// minimal test macros in oracle/refshim/gtest/gtest.h.
+#include "gtest/gtest.h"
+#include <vdb_mapping/OccupancyVDBMapping.hpp>
+
+#include <cmath>
+
+using vdb_mapping::Config;
+using vdb_mapping::OccupancyVDBMapping;
+
+namespace {
+
+float logodds(double p) { return static_cast<float>(std::log(p) - std::log(1 - p)); }
+
+Config test_config(double max_range)
+{
+  Config c;
+  c.max_range      = max_range;
+  c.fast_mode      = false;
+  c.prob_hit       = 0.9;
+  c.prob_miss      = 0.1;
+  c.prob_thres_max = 0.51;
+  c.prob_thres_min = 0.49;
+  return c;
+}
+
+OccupancyVDBMapping::PointCloudT::Ptr cloud_of(std::initializer_list<std::array<float, 3> > pts)
+{
+  OccupancyVDBMapping::PointCloudT::Ptr c(new OccupancyVDBMapping::PointCloudT);
+  for (const auto& p : pts) c->points.emplace_back(p[0], p[1], p[2]);
+  return c;
+}
+
+} // namespace
+
+TEST(DropIn, UnconfiguredThenConfigured)
+{
+  OccupancyVDBMapping map(1.0);
+  auto cloud = cloud_of({{0.f, 0.f, 1.f}});
+  Eigen::Matrix<double, 3, 1> origin(0, 0, 0);
+  EXPECT_TRUE(map.insertPointCloud(cloud, origin, "lidar"));
+  auto acc = map.getGrid()->getAccessor();
+  EXPECT_EQ(acc.getValue(openvdb::Coord(0, 0, 1)), 0.0f);
+  map.setConfig(test_config(10));
+  map.addInputSource("lidar", 10, 0);
+  map.insertPointCloud(cloud, origin, "lidar");
+  EXPECT_EQ(acc.getValue(openvdb::Coord(0, 0, 0)), logodds(0.1));
+  EXPECT_EQ(acc.getValue(openvdb::Coord(0, 0, 1)), logodds(0.9));
+}
+
+TEST(DropIn, AxisPointsBothSigns)
+{
+  for (int sign : {1, -1})
+  {
+    const double res = 0.1;
+    OccupancyVDBMapping map(res);
+    map.setConfig(test_config(10));
+    map.addInputSource("lidar", 10, 0);
+    auto cloud = cloud_of({{0.f, 0.f, static_cast<float>(sign * 5 * res)}});
+    map.insertPointCloud(cloud, Eigen::Matrix<double, 3, 1>(0, 0, 0), "lidar");
+    auto acc = map.getGrid()->getAccessor();
+    for (int i = (sign > 0 ? 0 : 1); i < 5; ++i)
+    {
+      EXPECT_EQ(acc.getValue(openvdb::Coord(0, 0, sign * i)), logodds(0.1));
+      EXPECT_FALSE(acc.isValueOn(openvdb::Coord(0, 0, sign * i)));
+    }
+    EXPECT_EQ(acc.getValue(openvdb::Coord(0, 0, sign * 5)), logodds(0.9));
+    EXPECT_TRUE(acc.isValueOn(openvdb::Coord(0, 0, sign * 5)));
+  }
+}
+
+TEST(DropIn, ClippedEndpointIsFree)
+{
+  const double res = 0.1;
+  OccupancyVDBMapping map(res);
+  map.setConfig(test_config(0.5));
+  map.addInputSource("lidar", 0.5, 0);
+  map.insertPointCloud(cloud_of({{0.f, 0.f, 0.7f}}), Eigen::Matrix<double, 3, 1>(0, 0, 0), "lidar");
+  auto acc = map.getGrid()->getAccessor();
+  for (int i = 0; i <= 5; ++i) EXPECT_EQ(acc.getValue(openvdb::Coord(0, 0, i)), logodds(0.1));
+  EXPECT_EQ(acc.getValue(openvdb::Coord(0, 0, 6)), 0.0f);
+}
+
+TEST(DropIn, ResetClears)
+{
+  OccupancyVDBMapping map(1.0);
+  map.setConfig(test_config(10));
+  map.addInputSource("lidar", 10, 0);
+  map.insertPointCloud(cloud_of({{0.f, 0.f, 1.f}}), Eigen::Matrix<double, 3, 1>(0, 0, 0), "lidar");
+  EXPECT_EQ(map.getGrid()->getAccessor().getValue(openvdb::Coord(0, 0, 1)), logodds(0.9));
+  map.resetMap();
+  EXPECT_EQ(map.getGrid()->getAccessor().getValue(openvdb::Coord(0, 0, 1)), 0.0f);
+  EXPECT_EQ(map.getGrid()->leafCount(), static_cast<size_t>(0));
+}
+
+TEST(DropIn, AccumulateThenIntegrate)
+{
+  OccupancyVDBMapping map(1.0);
+  map.setConfig(test_config(10));
+  map.addInputSource("a", 10, 0);
+  map.addInputSource("b", 10, 0);
+  auto cloud = cloud_of({{3.f, 0.f, 0.f}});
+  Eigen::Matrix<double, 3, 1> origin(0, 0, 0);
+  map.accumulateUpdate(cloud, origin, "a");
+  map.accumulateUpdate(cloud, origin, "a");  // same window: once
+  map.accumulateUpdate(cloud, origin, "b");
+  EXPECT_EQ(map.getGrid()->leafCount(), static_cast<size_t>(0));
+  map.integrateUpdate();
+  // two sources -> two hit updates on (3,0,0); one miss each on (0..2,0,0)
+  const float h  = logodds(0.9);
+  float two_hits = h + h;
+  const float mx = static_cast<float>(std::log(0.99) - std::log(0.01));
+  if (two_hits > mx) two_hits = mx;
+  EXPECT_EQ(map.getGrid()->getAccessor().getValue(openvdb::Coord(3, 0, 0)), two_hits);
+  // raycastPointCloud + updateMap on a private update grid
+  auto grid = OccupancyVDBMapping::UpdateGridT::create(false);
+  auto gacc = grid->getAccessor();
+  EXPECT_TRUE(map.raycastPointCloud(cloud, origin, 10.0, gacc));
+  map.updateMap(grid);
+  EXPECT_TRUE(map.getGrid()->getAccessor().isValueOn(openvdb::Coord(3, 0, 0)));
+}
+
+int main(int argc, char** argv)
+{
+  ::testing::InitGoogleTest(&argc, argv);
+  return RUN_ALL_TESTS();
+}
