@@ -55,6 +55,8 @@ def parse_args():
     ap.add_argument("--cpu-scans", type=int, default=2, help="scans in the single-thread CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--leaf-capacity", type=int, default=0,
+                    help="leaf pool slots reserved up front (default: sized for the workload)")
     return ap.parse_args()
 
 
@@ -125,9 +127,17 @@ def dist_env():
     return world, rank, local
 
 
+DESCRIPTIONS = {
+    "dense": "128x2048 LiDAR scans of a seeded 200x200x20 m street",
+    "small": "64x1024 LiDAR scans of a seeded 40x40x6 m room with 20 boxes",
+    "stress": "65,536 random rays of 0.5-200 m from (5000,-3000,40) m",
+}
+DEFAULT_CAPACITY = {"dense": 1 << 23, "small": 1 << 18, "stress": 1 << 25}
+
+
 def config_block(wl, args, world):
     return {
-        "workload": f"{wl.name}: {wl.points_per_scan} pts/scan 128x2048 LiDAR, street 200x200x20 m, "
+        "workload": f"{wl.name}: {wl.points_per_scan} pts/scan, {DESCRIPTIONS.get(wl.name, wl.name)}, "
                     f"voxel {wl.resolution} m, max_range {wl.max_range} m",
         "points_per_scan": wl.points_per_scan,
         "voxel_m": wl.resolution,
@@ -137,6 +147,7 @@ def config_block(wl, args, world):
         "point_layout": "pcl::PointXYZ 16 B",
         "l2": "flushed between steps (256 MiB write)",
         "parallelism": f"replicas x{world}" if world > 1 else "single map",
+        "leaf_pool_slots": args.leaf_capacity or DEFAULT_CAPACITY.get(wl.name, 1 << 20),
     }
 
 
@@ -231,7 +242,7 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
-    cap = 1 << 22
+    cap = args.leaf_capacity or DEFAULT_CAPACITY.get(wl.name, 1 << 20)
 
     def new_map():
         m = OccupancyVDBMapping(wl.resolution, initial_leaf_capacity=cap, device=local)

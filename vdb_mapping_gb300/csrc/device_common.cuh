@@ -58,7 +58,9 @@ struct DevStatus
   unsigned long long hits;
   unsigned long long updates;
   unsigned long long nonfinite;
-  unsigned long long pad[3];
+  uint32_t ray_cursor;  // next position in the ray order handed to a DDA warp
+  uint32_t pad32;
+  unsigned long long pad[2];
 };
 
 struct LogOdds
@@ -108,6 +110,27 @@ __device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p)
   asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+// L1-cached loads for data that only ever moves one way during a kernel
+// (hash keys: empty -> key; slots: pending -> slot; epochs: old -> current):
+// a stale value is always the earlier state, which the callers handle.
+__device__ __forceinline__ unsigned long long ld_ca_u64(const unsigned long long* p)
+{
+  unsigned long long v;
+  asm volatile("ld.global.ca.u64 %0, [%1];" : "=l"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ int ld_ca_s32(const int* p)
+{
+  int v;
+  asm volatile("ld.global.ca.s32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ uint32_t ld_ca_u32(const uint32_t* p)
+{
+  uint32_t v;
+  asm volatile("ld.global.ca.u32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
 __device__ __forceinline__ int ld_acquire_s32(const int* p)
 {
   int v;
@@ -130,6 +153,14 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long k)
   return k;
 }
 
+__device__ __forceinline__ int unpack_leaf_coord(unsigned long long key, int field)
+{
+  // field 0 = x (bits 42-62), 1 = y (21-41), 2 = z (0-20); sign-extend 21 bits
+  const int shift = (2 - field) * kKeyBits;
+  const int v     = static_cast<int>((key >> shift) & ((1ull << kKeyBits) - 1));
+  return (v << (32 - kKeyBits)) >> (32 - kKeyBits);
+}
+
 __device__ __forceinline__ unsigned long long pack_leaf_key(int lx, int ly, int lz)
 {
   const unsigned long long m = (1ull << kKeyBits) - 1;
@@ -143,7 +174,7 @@ __device__ __forceinline__ unsigned long long pack_leaf_key(int lx, int ly, int 
 __device__ __forceinline__ void touch_leaf(const ChannelView& c, int slot)
 {
   uint32_t* e = c.epoch + slot;
-  if (ld_relaxed_u32(e) != c.cur_epoch)
+  if (ld_ca_u32(e) != c.cur_epoch)
   {
     if (atomicExch(e, c.cur_epoch) != c.cur_epoch)
     {
@@ -164,7 +195,7 @@ __device__ __forceinline__ int find_or_insert_leaf(const MapView& m, int lx, int
   uint32_t h                   = static_cast<uint32_t>(mix64(key)) & m.hmask;
   for (uint32_t probe = 0; probe < kMaxProbes; ++probe)
   {
-    unsigned long long k = ld_relaxed_u64(m.hkeys + h);
+    unsigned long long k = ld_ca_u64(m.hkeys + h);
     if (k == kEmptyKey)
     {
       const unsigned long long prev = atomicCAS(m.hkeys + h, kEmptyKey, key);
@@ -189,7 +220,8 @@ __device__ __forceinline__ int find_or_insert_leaf(const MapView& m, int lx, int
     }
     if (k == key)
     {
-      int s          = ld_acquire_s32(m.hslots + h);
+      int s          = ld_ca_s32(m.hslots + h);
+      if (s == kSlotPending) s = ld_acquire_s32(m.hslots + h);
       uint32_t spins = 0;
       while (s == kSlotPending)
       {

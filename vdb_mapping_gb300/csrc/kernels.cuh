@@ -174,107 +174,321 @@ __global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, 
   order[base + rank] = static_cast<int>(i);
 }
 
-// One thread per ray (long rays first). FP64 DDA restating OpenVDB's
-// DDA<Ray<double>,0> as driven by castRayIntoGrid: eye = origin voxel + 0.5,
-// dir = end - origin, t in [0,1]. The positive tMax values are compared as
-// int64 bit patterns (same order as the doubles), so the only FP64 operation
-// per step is the sequential tMax += tDelta of the stepped axis.
-__global__ void __launch_bounds__(128, 8) k_dda_mark(const int4* __restrict__ rays,
-                                                  const int* __restrict__ order, int64_t n,
-                                                  ScanGeom g, MapView m, ChannelView c)
-{
-  if (ld_relaxed_u32(&m.st->error) != 0u) return;
-  const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (j >= n || j >= static_cast<int64_t>(m.st->n_valid)) return;
-  const int4 r       = rays[order[j]];
-  const uint32_t meta = static_cast<uint32_t>(r.w);
-  const uint32_t l1   = meta & kMetaL1Mask;
+// ---------------------------------------------------------------------------
+// k_dda_mark: warp-cooperative traversal.
+//
+// Each lane walks one ray at a time with the FP64 DDA of OpenVDB's
+// DDA<Ray<double>,0> as driven by castRayIntoGrid (eye = origin voxel + 0.5,
+// dir = end - origin, t in [0,1]). The positive tMax values are compared as
+// int64 bit patterns, which order like the doubles, so the only FP64 operation
+// per step is the sequential tMax += tDelta of the stepped axis; the step is
+// branch-free so the 32 lanes stay converged.
+//
+// Visits are collected per 8^3 leaf: the bits of the current x-slab of the
+// leaf (64 voxels) live in a register; a slab change ORs them into the lane's
+// current leaf record in shared memory. A leaf change closes the record into
+// the lane's private ring (kDdaRing records). Every kDdaSteps steps the warp
+// flushes all closed records together, one record per lane per round:
+// duplicate leaves in a round are merged, one lane per distinct leaf resolves
+// the slot in the device hash (all lookups of the round in flight at once) and
+// ORs the words into the update masks with fire-and-forget reductions.
+// Rays come from the L1-sorted order (long rays first), handed to idle lanes
+// at each round, so lanes rarely idle while rays remain.
+// ---------------------------------------------------------------------------
+constexpr int kDdaWarps = 2;   // warps per block
+constexpr int kDdaRing  = 4;   // leaf records per lane (3 closed + the open one)
+constexpr int kDdaSteps = 24;  // DDA steps between flushes
+// Record meta word: bits 0-7 non-zero word mask, bit 8 hit, bits 9-17 hit voxel offset.
+constexpr uint32_t kRecHit = 1u << 8;
 
-  Marker mk;
-  marker_init(mk);
-  if (l1 > 0)
-  {
-    const int o[3] = {g.ovx, g.ovy, g.ovz};
-    const int e[3] = {r.x, r.y, r.z};
-    int vox[3], stp[3];
-    long long nxt[3];
-    double dlt[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-    {
-      const double eye = __dadd_rn(static_cast<double>(o[a]), 0.5);
-      const double dir = __dsub_rn(static_cast<double>(e[a]), static_cast<double>(o[a]));
-      const double pos = __dadd_rn(eye, __dmul_rn(dir, 0.0));
-      vox[a]           = static_cast<int>(floor(pos));
-      if (dir == 0.0)
-      {
-        stp[a] = 0;
-        nxt[a] = __double_as_longlong(1.7976931348623157e308);
-        dlt[a] = 1.7976931348623157e308;
-      }
-      else
-      {
-        const double inv = __ddiv_rn(1.0, dir);
-        if (inv > 0.0)
-        {
-          stp[a] = 1;
-          nxt[a] = __double_as_longlong(
-            __dadd_rn(0.0, __dmul_rn(__dsub_rn(static_cast<double>(vox[a] + 1), pos), inv)));
-        }
-        else
-        {
-          stp[a] = -1;
-          nxt[a] = __double_as_longlong(
-            __dadd_rn(0.0, __dmul_rn(__dsub_rn(static_cast<double>(vox[a]), pos), inv)));
-        }
-        dlt[a] = __dmul_rn(static_cast<double>(stp[a]), inv);
-      }
-    }
-    const long long kOne = __double_as_longlong(1.0);
-    int x = vox[0], y = vox[1], z = vox[2];
-    long long nx = nxt[0], ny = nxt[1], nz = nxt[2];
-    mark_visit(mk, m, c, x, y, z);
-    // L1 + 1 steps: the first L1 land inside [0,1], the next one leaves it.
-    for (uint32_t s = 0; s <= l1; ++s)
-    {
-      long long t0;
-      if (nx < ny && nx < nz)
-      {
-        t0 = nx;
-        nx = __double_as_longlong(__dadd_rn(__longlong_as_double(nx), dlt[0]));
-        x += stp[0];
-      }
-      else if (ny < nz)
-      {
-        t0 = ny;
-        ny = __double_as_longlong(__dadd_rn(__longlong_as_double(ny), dlt[1]));
-        y += stp[1];
-      }
-      else
-      {
-        t0 = nz;
-        nz = __double_as_longlong(__dadd_rn(__longlong_as_double(nz), dlt[2]));
-        z += stp[2];
-      }
-      if (t0 > kOne) break;
-      if (s == l1)
-      {
-        // More than L1 steps inside the ray: cannot happen for integer rays.
-        atomicOr(&m.st->error, kErrStepBound);
-        break;
-      }
-      mark_visit(mk, m, c, x, y, z);
-    }
-  }
-  if (!(meta & kMetaClipped))
-  {
-    mark_hit(mk, m, c, r.x, r.y, r.z);
-  }
-  marker_flush(mk, c);
+struct DdaWarpSmem
+{
+  unsigned long long words[kDdaRing][8][32];
+  unsigned long long keys[kDdaRing][32];
+  uint32_t meta[kDdaRing][32];
+};
+
+__device__ __forceinline__ uint32_t lanemask_lt()
+{
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
 }
 
-// Persistent sweep over the touched leaves: one warp per leaf, 16 voxels per
-// lane (four float4 loads, only where the lane has update bits).
+// ORs the register slab into the open record.
+__device__ __forceinline__ void dda_put_slab(DdaWarpSmem& q, int lane, int rec, int w, unsigned long long bits,
+                                             uint32_t& nz)
+{
+  if (w < 0 || bits == 0ull) return;
+  if (nz & (1u << w))
+    q.words[rec][w][lane] |= bits;
+  else
+    q.words[rec][w][lane] = bits;
+  nz |= 1u << w;
+}
+
+// Flushes the closed records [0, n_done) of every lane, round by round.
+__device__ __forceinline__ void dda_flush(DdaWarpSmem& q, int lane, int n_done, const MapView& m,
+                                          const ChannelView& c)
+{
+  __syncwarp();
+  const int rounds = __reduce_max_sync(0xffffffffu, static_cast<unsigned>(n_done));
+  for (int r = 0; r < rounds; ++r)
+  {
+    const bool mine              = r < n_done;
+    const unsigned long long key = mine ? q.keys[r][lane] : kEmptyKey;
+    const uint32_t meta          = mine ? q.meta[r][lane] : 0u;
+    const unsigned peers         = __match_any_sync(0xffffffffu, key);
+    const int leader             = __ffs(peers) - 1;
+    const uint32_t nz            = meta & 0xffu;
+    // Words any record of the group has; the leader clears the ones it lacks
+    // (they hold stale data), then the others OR theirs in.
+    const uint32_t group_nz = __reduce_or_sync(peers, nz);
+    if (mine && leader == lane)
+    {
+      for (uint32_t z = group_nz & ~nz; z; z &= z - 1) q.words[r][__ffs(z) - 1][lane] = 0ull;
+    }
+    __syncwarp();
+    if (mine && leader != lane)
+    {
+      for (uint32_t z = nz; z; z &= z - 1)
+      {
+        const int w = __ffs(z) - 1;
+        atomicOr(&q.words[r][w][leader], q.words[r][w][lane]);
+      }
+    }
+    __syncwarp();
+    int slot = kSlotFailed;
+    if (mine && leader == lane)
+    {
+      slot = find_or_insert_leaf(m, unpack_leaf_coord(key, 0), unpack_leaf_coord(key, 1),
+                                 unpack_leaf_coord(key, 2));
+      if (slot >= 0)
+      {
+        touch_leaf(c, slot);
+        unsigned long long* u = c.upd + static_cast<size_t>(slot) * 16;
+        for (uint32_t z = group_nz; z; z &= z - 1)
+        {
+          const int w = __ffs(z) - 1;
+          atomicOr(u + w, q.words[r][w][lane]);
+        }
+      }
+    }
+    slot = __shfl_sync(0xffffffffu, slot, leader);
+    if (mine && slot >= 0 && (meta & kRecHit))
+    {
+      const uint32_t off = (meta >> 9) & 511u;
+      atomicOr(c.upd + static_cast<size_t>(slot) * 16 + 8 + (off >> 6), 1ull << (off & 63));
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __restrict__ rays,
+                                                               const int* __restrict__ order, ScanGeom g,
+                                                               MapView m, ChannelView c)
+{
+  __shared__ DdaWarpSmem smem[kDdaWarps];
+  const int lane = static_cast<int>(threadIdx.x & 31);
+  // Warp-uniform early exit: other warps may set the error word meanwhile.
+  if (__shfl_sync(0xffffffffu, ld_relaxed_u32(&m.st->error), 0) != 0u) return;
+  DdaWarpSmem& q    = smem[threadIdx.x >> 5];
+  const uint32_t nv = m.st->n_valid;
+
+  bool drained = false;
+  // Per-lane ray state.
+  bool has_ray = false, cur_valid = false, clipped = false;
+  int vx = 0, vy = 0, vz = 0, sx = 0, sy = 0, sz = 0;
+  long long nx = 0, ny = 0, nz = 0;
+  double dx = 0.0, dy = 0.0, dz = 0.0;
+  int clx = 0, cly = 0, clz = 0;
+  int cur_w = -1;
+  unsigned long long slab = 0ull;
+  uint32_t rec_nz = 0;  // non-zero words of the open record
+  int n_done = 0;       // closed records in the ring; the open one is at index n_done
+  uint32_t hit_off = 0, budget = 0;
+  const long long kOne = __double_as_longlong(1.0);
+  const long long kMax = __double_as_longlong(1.7976931348623157e308);
+
+  for (;;)
+  {
+    // ---- hand out rays to idle lanes ------------------------------------------
+    if (!drained && __shfl_sync(0xffffffffu, ld_relaxed_u32(&m.st->error), 0) != 0u)
+    {
+      drained = true;  // a pool or hash overflow forces a second pass; stop early
+    }
+    if (!drained)
+    {
+      const unsigned need = __ballot_sync(0xffffffffu, !has_ray);
+      if (need)
+      {
+        const int leader = __ffs(need) - 1;
+        uint32_t base    = 0;
+        if (lane == leader) base = atomicAdd(&m.st->ray_cursor, static_cast<uint32_t>(__popc(need)));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (base + static_cast<uint32_t>(__popc(need)) >= nv) drained = true;
+        if (!has_ray)
+        {
+          const uint32_t idx = base + static_cast<uint32_t>(__popc(need & lanemask_lt()));
+          if (idx < nv)
+          {
+            const int4 r        = rays[order[idx]];
+            const uint32_t meta = static_cast<uint32_t>(r.w);
+            const uint32_t l1   = meta & kMetaL1Mask;
+            clipped             = (meta & kMetaClipped) != 0;
+            hit_off = (static_cast<uint32_t>(r.x & 7) << 6) | (static_cast<uint32_t>(r.y & 7) << 3) |
+                      static_cast<uint32_t>(r.z & 7);
+            if (l1 == 0)
+            {
+              // castRayIntoGrid marks nothing; an unclipped endpoint is still a hit.
+              if (!clipped)
+              {
+                q.keys[n_done][lane] = pack_leaf_key(r.x >> 3, r.y >> 3, r.z >> 3);
+                q.meta[n_done][lane] = kRecHit | (hit_off << 9);
+                ++n_done;
+              }
+            }
+            else
+            {
+              const int o[3] = {g.ovx, g.ovy, g.ovz};
+              const int e[3] = {r.x, r.y, r.z};
+              int vox[3], stp[3];
+              long long nxt[3];
+              double dlt[3];
+#pragma unroll
+              for (int a = 0; a < 3; ++a)
+              {
+                const double eye = __dadd_rn(static_cast<double>(o[a]), 0.5);
+                const double dir = __dsub_rn(static_cast<double>(e[a]), static_cast<double>(o[a]));
+                const double pos = __dadd_rn(eye, __dmul_rn(dir, 0.0));
+                vox[a]           = static_cast<int>(floor(pos));
+                if (dir == 0.0)
+                {
+                  stp[a] = 0;
+                  nxt[a] = kMax;
+                  dlt[a] = 1.7976931348623157e308;
+                }
+                else
+                {
+                  const double inv = __ddiv_rn(1.0, dir);
+                  if (inv > 0.0)
+                  {
+                    stp[a] = 1;
+                    nxt[a] = __double_as_longlong(
+                      __dadd_rn(0.0, __dmul_rn(__dsub_rn(static_cast<double>(vox[a] + 1), pos), inv)));
+                  }
+                  else
+                  {
+                    stp[a] = -1;
+                    nxt[a] = __double_as_longlong(
+                      __dadd_rn(0.0, __dmul_rn(__dsub_rn(static_cast<double>(vox[a]), pos), inv)));
+                  }
+                  dlt[a] = __dmul_rn(static_cast<double>(stp[a]), inv);
+                }
+              }
+              vx = vox[0]; vy = vox[1]; vz = vox[2];
+              sx = stp[0]; sy = stp[1]; sz = stp[2];
+              nx = nxt[0]; ny = nxt[1]; nz = nxt[2];
+              dx = dlt[0]; dy = dlt[1]; dz = dlt[2];
+              budget    = l1 + 1;
+              has_ray   = true;
+              cur_valid = false;
+            }
+          }
+        }
+      }
+    }
+    const bool any_ray = __ballot_sync(0xffffffffu, has_ray) != 0u;
+    if (!any_ray && drained && __ballot_sync(0xffffffffu, n_done > 0) == 0u) break;
+
+    // ---- DDA steps (no warp votes inside) --------------------------------------
+    if (any_ray)
+    {
+#pragma unroll 2
+      for (int s = 0; s < kDdaSteps; ++s)
+      {
+        if (!has_ray) continue;
+        // setActiveState(voxel) on the update grid, leaf by leaf.
+        const int lx = vx >> 3, ly = vy >> 3, lz = vz >> 3;
+        if (!cur_valid || lx != clx || ly != cly || lz != clz)
+        {
+          if (cur_valid)
+          {
+            if (n_done == kDdaRing - 1) continue;  // ring full: wait for the flush
+            dda_put_slab(q, lane, n_done, cur_w, slab, rec_nz);
+            q.meta[n_done][lane] = rec_nz;
+            ++n_done;
+          }
+          clx                  = lx;
+          cly                  = ly;
+          clz                  = lz;
+          q.keys[n_done][lane] = pack_leaf_key(lx, ly, lz);
+          cur_valid            = true;
+          rec_nz               = 0u;
+          cur_w                = -1;
+          slab                 = 0ull;
+        }
+        const int w = vx & 7;
+        if (w != cur_w)
+        {
+          dda_put_slab(q, lane, n_done, cur_w, slab, rec_nz);
+          cur_w = w;
+          slab  = 0ull;
+        }
+        slab |= 1ull << (((vy & 7) << 3) | (vz & 7));
+        // DDA::step(): argmin of tMax (ties to the higher axis), branch-free.
+        const bool ax      = (nx < ny) && (nx < nz);
+        const bool ay      = !ax && (ny < nz);
+        const long long t0 = ax ? nx : (ay ? ny : nz);
+        const double d     = ax ? dx : (ay ? dy : dz);
+        const long long tn = __double_as_longlong(__dadd_rn(__longlong_as_double(t0), d));
+        nx                 = ax ? tn : nx;
+        ny                 = ay ? tn : ny;
+        nz                 = (!ax && !ay) ? tn : nz;
+        vx += ax ? sx : 0;
+        vy += ay ? sy : 0;
+        vz += (!ax && !ay) ? sz : 0;
+        budget -= 1;
+        bool fin = t0 > kOne;
+        if (!fin && budget == 0)
+        {
+          // More than L1 + 1 visits: cannot happen for integer rays.
+          atomicOr(&m.st->error, kErrStepBound);
+          fin = true;
+        }
+        if (fin)
+        {
+          // The last marked voxel is the endpoint: its record carries the hit.
+          dda_put_slab(q, lane, n_done, cur_w, slab, rec_nz);
+          q.meta[n_done][lane] = rec_nz | (clipped ? 0u : (kRecHit | (hit_off << 9)));
+          ++n_done;
+          has_ray   = false;
+          cur_valid = false;
+        }
+      }
+    }
+
+    // ---- flush the closed records; the open one moves to the ring start -------
+    dda_flush(q, lane, n_done, m, c);
+    if (n_done > 0 && cur_valid)
+    {
+      q.keys[0][lane] = q.keys[n_done][lane];
+      for (uint32_t z = rec_nz; z; z &= z - 1)
+      {
+        const int w      = __ffs(z) - 1;
+        q.words[0][w][lane] = q.words[n_done][w][lane];
+      }
+    }
+    n_done = 0;
+    __syncwarp();
+  }
+}
+
+// Persistent sweep over the touched leaves: 8 lanes per leaf, lane w owning
+// the x-slab w (voxel offsets 64w..64w+63, one word of each mask), so a warp
+// sweeps four leaves at once. A lane loads the float4 groups of its slab that
+// hold update bits (all loads issued before any use), applies the log-odds
+// rules, stores them back and clears its update words.
 __global__ void __launch_bounds__(256) k_sweep(ChannelView c, float* __restrict__ values,
                                                unsigned long long* __restrict__ active,
                                                uint32_t* __restrict__ flags, LogOdds lo, DevStatus* st)
@@ -282,53 +496,63 @@ __global__ void __launch_bounds__(256) k_sweep(ChannelView c, float* __restrict_
   if (ld_relaxed_u32(&st->error) != 0u) return;
   const uint32_t nt   = *c.n_touched;
   const int lane      = static_cast<int>(threadIdx.x & 31);
+  const int w         = lane & 7;
+  const uint32_t grp  = static_cast<uint32_t>(lane >> 3);
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nw   = (gridDim.x * blockDim.x) >> 5;
-  const int w         = lane >> 2;
-  const int sh        = (lane & 3) * 16;
   unsigned long long n_upd = 0;
-  for (uint32_t i = warp; i < nt; i += nw)
+  for (uint32_t base = warp * 4; base < nt; base += nw * 4)
   {
-    const int slot           = c.touched[i];
-    unsigned long long* u    = c.upd + static_cast<size_t>(slot) * 16;
-    const unsigned long long vis = u[w];
-    const unsigned long long hw  = u[8 + w];
-    const uint32_t hb        = static_cast<uint32_t>(hw >> sh) & 0xffffu;
-    const uint32_t ab        = (static_cast<uint32_t>(vis >> sh) & 0xffffu) | hb;
-    unsigned long long* aw   = active + static_cast<size_t>(slot) * 8 + w;
-    uint32_t ob              = static_cast<uint32_t>(*aw >> sh) & 0xffffu;
-    if (ab)
+    const uint32_t i = base + grp;
+    if (i >= nt) continue;
+    const int slot                 = c.touched[i];
+    // Mark the leaf as part of the map the first time it is swept (every
+    // touched leaf carries at least one update bit).
+    if (w == 0 && ld_ca_u32(flags + slot) == 0u) flags[slot] = 1u;
+    unsigned long long* u          = c.upd + static_cast<size_t>(slot) * 16;
+    const unsigned long long hitw  = u[8 + w];
+    const unsigned long long actw  = u[w] | hitw;
+    if (actw == 0ull) continue;
+    unsigned long long* aw         = active + static_cast<size_t>(slot) * 8 + w;
+    const unsigned long long on_in = *aw;
+    unsigned long long on          = on_in;
+    float4* vp = reinterpret_cast<float4*>(values + static_cast<size_t>(slot) * 512 + w * 64);
+#pragma unroll
+    for (int half = 0; half < 2; ++half)
     {
-      float4* vp = reinterpret_cast<float4*>(values + static_cast<size_t>(slot) * 512 + lane * 16);
+      float4 v[8];
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
+      for (int k = 0; k < 8; ++k)
       {
-        const uint32_t a4 = (ab >> (4 * q)) & 0xfu;
-        if (!a4) continue;
-        float4 v4   = vp[q];
-        float vv[4] = {v4.x, v4.y, v4.z, v4.w};
+        const int qd = half * 8 + k;
+        if ((actw >> (4 * qd)) & 0xfull) v[k] = vp[qd];
+      }
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
+      for (int k = 0; k < 8; ++k)
+      {
+        const int qd           = half * 8 + k;
+        const uint32_t a4      = static_cast<uint32_t>(actw >> (4 * qd)) & 0xfu;
+        if (!a4) continue;
+        const uint32_t h4      = static_cast<uint32_t>(hitw >> (4 * qd)) & 0xfu;
+        float vv[4]            = {v[k].x, v[k].y, v[k].z, v[k].w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
         {
-          const int bit = 4 * q + k;
-          if ((a4 >> k) & 1u)
+          if ((a4 >> j) & 1u)
           {
-            bool on = (ob >> bit) & 1u;
-            apply_update(vv[k], on, (hb >> bit) & 1u, lo);
-            ob = on ? (ob | (1u << bit)) : (ob & ~(1u << bit));
+            const int bit = 4 * qd + j;
+            bool o        = (on >> bit) & 1ull;
+            apply_update(vv[j], o, (h4 >> j) & 1u, lo);
+            on = o ? (on | (1ull << bit)) : (on & ~(1ull << bit));
           }
         }
-        vp[q] = make_float4(vv[0], vv[1], vv[2], vv[3]);
+        vp[qd] = make_float4(vv[0], vv[1], vv[2], vv[3]);
       }
-      n_upd += static_cast<unsigned long long>(__popc(ab));
     }
-    unsigned long long part = static_cast<unsigned long long>(ob) << sh;
-    part |= __shfl_xor_sync(0xffffffffu, part, 1);
-    part |= __shfl_xor_sync(0xffffffffu, part, 2);
-    if ((lane & 3) == 0) *aw = part;
-    __syncwarp();
-    if (lane < 16) u[lane] = 0ull;
-    if (lane == 0) flags[slot] = 1u;
+    if (on != on_in) *aw = on;
+    u[w] = 0ull;
+    if (hitw) u[8 + w] = 0ull;
+    n_upd += static_cast<unsigned long long>(__popcll(actw));
   }
   for (int off = 16; off > 0; off >>= 1) n_upd += __shfl_xor_sync(0xffffffffu, n_upd, off);
   if (lane == 0 && n_upd) atomicAdd(&st->updates, n_upd);

@@ -79,6 +79,7 @@ struct vdbg_map
   uint32_t* d_cursor    = nullptr;
 
   int64_t bytes         = 0;
+  int num_sms           = 152;
 };
 
 namespace {
@@ -389,6 +390,16 @@ void record_timings(vdbg_map* m)
 
 // Marks one cloud into channel `c` (VDBMapping.hpp:466-539). Kernels are
 // queued on `s`; the caller fetches the status.
+void launch_dda(vdbg_map* m, int64_t n, const ScanGeom& g, const Channel& c, cudaStream_t s)
+{
+  // Persistent warps; every warp pulls rays until the order is drained.
+  const int64_t warps_needed = (n + 31) / 32;
+  int64_t blocks             = (warps_needed + kDdaWarps - 1) / kDdaWarps;
+  blocks                     = std::min<int64_t>(blocks, static_cast<int64_t>(m->num_sms) * 10);
+  k_dda_mark<<<static_cast<unsigned>(std::max<int64_t>(blocks, 1)), kDdaWarps * 32, 0, s>>>(
+    m->d_rays, m->d_order, g, map_view(m), channel_view(c));
+}
+
 int launch_raycast(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t stride,
                    const double origin[3], double range, uint32_t flags, cudaStream_t s, bool* queued,
                    ScanGeom* geom_out)
@@ -425,8 +436,7 @@ int launch_raycast(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t
   k_scan<<<1, 1024, 0, s>>>(m->d_hist, m->d_cursor, m->d_status);
   k_scatter<<<blocks, 256, 0, s>>>(m->d_rays, n, m->d_cursor, m->d_order);
   VDBG_CUDA(cudaEventRecord(m->ev_prep, s));
-  k_dda_mark<<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(m->d_rays, m->d_order, n, g,
-                                                                   map_view(m), channel_view(c));
+  launch_dda(m, n, g, c, s);
   VDBG_CUDA(cudaGetLastError());
   VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
   m->timed_prep = true;
@@ -562,15 +572,15 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
     // Pool or hash exhausted: grow, clear the error, mark again, sweep.
     const uint64_t requested = m->h_status->n_leaves;
     VDBG_TRY(grow_for(m, requested));
-    DevStatus keep = *m->h_status;
-    keep.error     = 0;
-    keep.n_leaves  = m->n_leaves;
+    DevStatus keep  = *m->h_status;
+    keep.error      = 0;
+    keep.n_leaves   = m->n_leaves;
+    keep.ray_cursor = 0;  // the re-marking pass walks all rays again
     *m->h_status   = keep;
     VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
     if (queued)
     {
-      k_dda_mark<<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(m->d_rays, m->d_order, n, g,
-                                                                       map_view(m), channel_view(*src));
+      launch_dda(m, n, g, *src, s);
       VDBG_CUDA(cudaGetLastError());
       m->timings.launches += 1;
       m->timings.retries += 1;
@@ -637,6 +647,8 @@ int vdbg_create(double resolution, const vdbg_options* options, vdbg_map** out)
     return s;
   };
   if (cudaSetDevice(m->device) != cudaSuccess) return fail(VDBG_ERR_CUDA);
+  if (cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, m->device) != cudaSuccess)
+    return fail(VDBG_ERR_CUDA);
   if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(VDBG_ERR_CUDA);
   if (cudaEventCreate(&m->ev0) != cudaSuccess || cudaEventCreate(&m->ev1) != cudaSuccess ||
       cudaEventCreate(&m->ev_prep) != cudaSuccess || cudaEventCreate(&m->ev_dda) != cudaSuccess)
