@@ -35,7 +35,8 @@ enum vdbg_status
   VDBG_ERR_COORD_RANGE      = 8,  /* a voxel index outside [-2^23, 2^23) on some axis */
   VDBG_ERR_CUDA             = 9,
   VDBG_ERR_TIMEOUT          = 10, /* a bounded device wait gave up */
-  VDBG_ERR_BUFFER_TOO_SMALL = 11
+  VDBG_ERR_BUFFER_TOO_SMALL = 11,
+  VDBG_ERR_SIZE_LIMIT       = 12  /* input larger than a fixed-size entry point accepts */
 };
 
 /* Input flags. */
@@ -160,6 +161,29 @@ int vdbg_get_timings(const vdbg_map* map, vdbg_timings* out);
 
 /* Device bytes held by the map. */
 int vdbg_device_bytes(const vdbg_map* map, int64_t* out);
+
+/* Insertion that allocates no device memory during the call. No counterpart
+ * in the reference: it exists for callers that must not allocate while they
+ * run, such as real-time mapping loops where cudaMalloc's unbounded latency
+ * and implicit device synchronisation break the cycle budget, or hosts that
+ * own all device memory through their own pool. Same semantics and results as
+ * vdbg_insert_point_cloud, but the per-scan scratch lives in one fixed
+ * VDBG_NOALLOC_SCRATCH_BYTES device array inside the library (held by every
+ * GPU that loads it, until the process exits) instead of buffers the map
+ * grows on demand. Limits: n <= VDBG_NOALLOC_MAX_POINTS and, for host input,
+ * stride_bytes <= 16; larger inputs return VDBG_ERR_SIZE_LIMIT. The map's leaf
+ * pool is not grown: when it is full the call returns VDBG_ERR_OUT_OF_MEMORY,
+ * applies nothing and discards the source's pending update grid, so create
+ * the map with an initial_leaf_capacity that covers its extent. The first
+ * call on a device looks up the array's device address (a one-time set-up);
+ * make that first call before any stream capture. All calls share the array,
+ * so calls that overlap on the GPU (other threads, other streams, other maps)
+ * race: serialise them. */
+#define VDBG_NOALLOC_MAX_POINTS 262144
+#define VDBG_NOALLOC_SCRATCH_BYTES (262144 * (16 + 16 + 4) + 2 * 4096 * 4)
+int vdbg_insert_point_cloud_noalloc(vdbg_map* map, const float* xyz, int64_t n, int64_t stride_bytes,
+                                    const double origin[3], const char* source_id, uint32_t flags,
+                                    void* stream, vdbg_scan_stats* stats);
 
 /* Human-readable text of a status code (static storage). */
 const char* vdbg_status_string(int status);

@@ -11,6 +11,7 @@ import os
 from .build import LIB_PATH
 
 VDBG_POINTS_DEVICE = 1
+VDBG_NOALLOC_MAX_POINTS = 262144
 
 STATUS = {
     0: "VDBG_OK",
@@ -25,6 +26,7 @@ STATUS = {
     9: "VDBG_ERR_CUDA",
     10: "VDBG_ERR_TIMEOUT",
     11: "VDBG_ERR_BUFFER_TOO_SMALL",
+    12: "VDBG_ERR_SIZE_LIMIT",
 }
 STATUS_CODE = {v: k for k, v in STATUS.items()}
 
@@ -106,6 +108,8 @@ SIGNATURES = [
     ("vdbg_export_leaves", C.c_int, [_P, C.c_int64, _P, _P, _P, C.POINTER(C.c_int64)]),
     ("vdbg_device_bytes", C.c_int, [_P, C.POINTER(C.c_int64)]),
     ("vdbg_get_timings", C.c_int, [_P, C.POINTER(vdbg_timings)]),
+    ("vdbg_insert_point_cloud_noalloc", C.c_int,
+     [_P, _P, C.c_int64, C.c_int64, _D3, C.c_char_p, C.c_uint32, _P, C.POINTER(vdbg_scan_stats)]),
     ("vdbg_status_string", C.c_char_p, [C.c_int]),
 ]
 

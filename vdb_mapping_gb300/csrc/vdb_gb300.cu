@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -617,6 +618,9 @@ const char* vdbg_status_string(int s)
     case VDBG_ERR_CUDA: return "CUDA error";
     case VDBG_ERR_TIMEOUT: return "Bounded device wait gave up";
     case VDBG_ERR_BUFFER_TOO_SMALL: return "Buffer too small";
+    case VDBG_ERR_SIZE_LIMIT:
+      return "Input too large for vdbg_insert_point_cloud_noalloc (more than VDBG_NOALLOC_MAX_POINTS points, "
+             "or a host stride above 16 bytes)";
     default: return "unknown status";
   }
 }
@@ -920,3 +924,186 @@ int vdbg_device_bytes(const vdbg_map* m, int64_t* out)
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// Insertion without device allocation (vdbg_insert_point_cloud_noalloc).
+//
+// The per-scan scratch of the regular path (host points staged on the device,
+// ray records, the L1 order and the bucket histogram/cursor) is carved out of
+// one file-scope device array instead of map-owned buffers that grow on
+// demand; the map's leaf pool and hash are used as created and never grown.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int64_t kNoAllocMaxPoints = VDBG_NOALLOC_MAX_POINTS;
+constexpr size_t kNoAllocPtsBytes   = static_cast<size_t>(kNoAllocMaxPoints) * 16;
+constexpr size_t kNoAllocRaysBytes  = static_cast<size_t>(kNoAllocMaxPoints) * sizeof(int4);
+constexpr size_t kNoAllocOrderBytes = static_cast<size_t>(kNoAllocMaxPoints) * sizeof(int);
+constexpr size_t kNoAllocHistBytes  = static_cast<size_t>(kNumBuckets) * sizeof(uint32_t);
+constexpr size_t kNoAllocBytes      = kNoAllocPtsBytes + kNoAllocRaysBytes + kNoAllocOrderBytes + 2 * kNoAllocHistBytes;
+static_assert(kNoAllocBytes == static_cast<size_t>(VDBG_NOALLOC_SCRATCH_BYTES), "scratch size and header disagree");
+
+constexpr int kNoAllocMaxDevices = 64;
+
+} // namespace
+
+// One copy per GPU that loads the library, zero-initialised at load.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+
+std::mutex g_noalloc_mutex;
+char* g_noalloc_base[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on `device`, looked up once per device
+// with that device current (in host code the symbol names a host-side
+// stand-in, not device memory).
+int noalloc_scratch(int device, char** out)
+{
+  if (device < 0 || device >= kNoAllocMaxDevices) return VDBG_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_base[device])
+  {
+    void* p           = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+    {
+      std::fprintf(stderr, "vdb_gb300: cudaGetSymbolAddress(g_noalloc_scratch) failed: %s\n",
+                   cudaGetErrorString(e));
+      return VDBG_ERR_CUDA;
+    }
+    g_noalloc_base[device] = static_cast<char*>(p);
+  }
+  *out = g_noalloc_base[device];
+  return VDBG_OK;
+}
+
+// Zeroes the update words of the leaves on a channel's touched list (used
+// when a no-allocation insertion has to give up after a partial marking).
+__global__ void k_clear_touched(ChannelView c)
+{
+  const size_t words = static_cast<size_t>(*c.n_touched) * 16;
+  for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < words;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+  {
+    c.upd[static_cast<size_t>(c.touched[i >> 4]) * 16 + (i & 15u)] = 0ull;
+  }
+}
+
+} // namespace
+
+extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, int64_t n, int64_t stride,
+                                               const double origin[3], const char* id, uint32_t flags,
+                                               void* stream, vdbg_scan_stats* stats)
+{
+  if (!m || !origin || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  const bool host_input = (flags & VDBG_POINTS_DEVICE) == 0;
+  if (n > kNoAllocMaxPoints || (host_input && stride > 16)) return VDBG_ERR_SIZE_LIMIT;
+  VDBG_TRY(set_device(m));
+  char* base = nullptr;
+  VDBG_TRY(noalloc_scratch(m->device, &base));
+  char* d_pts       = base;
+  int4* d_rays      = reinterpret_cast<int4*>(base + kNoAllocPtsBytes);
+  int* d_order      = reinterpret_cast<int*>(base + kNoAllocPtsBytes + kNoAllocRaysBytes);
+  uint32_t* d_hist  = reinterpret_cast<uint32_t*>(base + kNoAllocPtsBytes + kNoAllocRaysBytes + kNoAllocOrderBytes);
+  uint32_t* d_cursor = d_hist + kNumBuckets;
+  cudaStream_t s     = pick_stream(m, stream);
+
+  Channel* src = find_channel(m, id);
+  int pre      = VDBG_OK;
+  if (!src)
+    pre = VDBG_ERR_UNKNOWN_SOURCE;
+  else if (src->max_range > 0 && !m->config_set)
+    pre = VDBG_ERR_NOT_CONFIGURED;
+  const bool cast = src && src->max_range > 0 && m->config_set && n > 0 &&
+                    !(std::isnan(origin[0]) || std::isnan(origin[1]) || std::isnan(origin[2]));
+
+  VDBG_TRY(begin_call(m, s));
+  const uint32_t leaves_before = m->n_leaves;
+  if (cast)
+  {
+    ScanGeom g;
+    g.ox       = origin[0];
+    g.oy       = origin[1];
+    g.oz       = origin[2];
+    g.range    = src->max_range;
+    g.res      = m->resolution;
+    g.half_res = m->half_res;
+    g.inv_res  = m->inv_res;
+    int ov[3];
+    if (!origin_to_index(m, origin, ov)) return VDBG_ERR_COORD_RANGE;
+    g.ovx = ov[0];
+    g.ovy = ov[1];
+    g.ovz = ov[2];
+    g.pad = 0;
+    // The histogram must start at zero; the previous call's contents remain.
+    VDBG_CUDA(cudaMemsetAsync(d_hist, 0, kNoAllocHistBytes, s));
+    const char* pts = reinterpret_cast<const char*>(xyz);
+    if (host_input)
+    {
+      VDBG_CUDA(cudaMemcpyAsync(d_pts, xyz, static_cast<size_t>(n) * static_cast<size_t>(stride),
+                                cudaMemcpyHostToDevice, s));
+      pts = d_pts;
+    }
+    const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
+    k_prep<<<blocks, 256, 0, s>>>(pts, n, stride, g, d_rays, d_hist, m->d_status);
+    k_scan<<<1, 1024, 0, s>>>(d_hist, d_cursor, m->d_status);
+    k_scatter<<<blocks, 256, 0, s>>>(d_rays, n, d_cursor, d_order);
+    VDBG_CUDA(cudaEventRecord(m->ev_prep, s));
+    const int64_t warps_needed = (n + 31) / 32;
+    int64_t dblocks            = (warps_needed + kDdaWarps - 1) / kDdaWarps;
+    dblocks                    = std::min<int64_t>(dblocks, static_cast<int64_t>(m->num_sms) * 10);
+    k_dda_mark<<<static_cast<unsigned>(std::max<int64_t>(dblocks, 1)), kDdaWarps * 32, 0, s>>>(
+      d_rays, d_order, g, map_view(m), channel_view(*src));
+    VDBG_CUDA(cudaGetLastError());
+    VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
+    m->timed_prep = true;
+    m->timings.launches += 4;
+    src->pending = true;
+  }
+  std::vector<Channel*> todo;
+  for (Channel& c : m->channels)
+    if (c.pending) todo.push_back(&c);
+  for (Channel* c : todo) VDBG_TRY(launch_sweep(m, *c, s));
+  VDBG_TRY(fetch_status(m, s));
+  uint32_t err = m->h_status->error;
+  m->n_leaves  = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
+  int result   = pre;
+  if (err & kErrCoordRange)
+  {
+    // Nothing of the cloud was marked; integrate what else is pending.
+    result = VDBG_ERR_COORD_RANGE;
+    DevStatus clean;
+    clear_status(&clean);
+    clean.n_leaves = m->n_leaves;
+    *m->h_status   = clean;
+    VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+    for (Channel* c : todo) VDBG_TRY(launch_sweep(m, *c, s));
+    VDBG_TRY(fetch_status(m, s));
+    err = m->h_status->error;
+  }
+  if (err != 0)
+  {
+    // The pool may not grow here: drop the partial marking of this source,
+    // apply nothing and report.
+    if (src && cast)
+    {
+      k_clear_touched<<<m->num_sms * 4, 256, 0, s>>>(channel_view(*src));
+      VDBG_CUDA(cudaGetLastError());
+      VDBG_TRY(finish_sweep(m, *src, s));
+    }
+    DevStatus clean;
+    clear_status(&clean);
+    clean.n_leaves = m->n_leaves;
+    *m->h_status   = clean;
+    VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+    VDBG_CUDA(cudaStreamSynchronize(s));
+    return (err & (kErrPoolFull | kErrHashFull)) ? VDBG_ERR_OUT_OF_MEMORY : map_error(err);
+  }
+  record_timings(m);
+  for (Channel* c : todo) VDBG_TRY(finish_sweep(m, *c, s));
+  if (!todo.empty()) VDBG_CUDA(cudaStreamSynchronize(s));
+  fill_stats(m, leaves_before, stats);
+  return result;
+}
