@@ -63,7 +63,7 @@ typedef struct vdbg_options
   int64_t initial_leaf_capacity; /* leaf pool slots to reserve (default 65536) */
   int64_t max_device_bytes;      /* growth budget for this map (0 = unlimited) */
   int32_t device;                /* CUDA device ordinal (default current) */
-  int32_t reserved0;
+  int32_t initial_block_capacity; /* 64^3-voxel blocks to reserve (default: leaf capacity / 32, >= 1024) */
 } vdbg_options;
 
 /* Counters of one call (accumulate, integrate or insert). */

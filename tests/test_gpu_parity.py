@@ -182,6 +182,23 @@ def test_pool_growth_retry_is_exact(vdbg, oracle):
     assert_same_map(g.exportLeaves(), o.exportLeaves(), "growth")
 
 
+def test_block_pool_growth_retry_is_exact(vdbg, oracle):
+    """Tiny leaf and block pools force both to grow mid-scan, several times,
+    with the block hash rebuilt and failed leaf cells retried."""
+    rng = np.random.default_rng(9)
+    cfg = Config(max_range=12.0, prob_hit=0.7, prob_miss=0.4, prob_thres_min=0.12, prob_thres_max=0.97)
+    g, o = pair(vdbg, oracle, 0.05, cfg, initial_leaf_capacity=16, initial_block_capacity=2)
+    scans = []
+    for k in range(3):
+        org = rng.uniform(-30, 30, 3)
+        d = rng.normal(size=(6000, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        pts = (org + d * rng.uniform(0.5, 15.0, (6000, 1))).astype(np.float32)
+        scans.append((pts, org))
+    run_both(g, o, scans)
+    assert_same_map(g.exportLeaves(), o.exportLeaves(), "block growth")
+
+
 def test_device_pointer_input_matches_host(vdbg, oracle):
     import torch
 

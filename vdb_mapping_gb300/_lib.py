@@ -49,7 +49,7 @@ class vdbg_options(C.Structure):
         ("initial_leaf_capacity", C.c_int64),
         ("max_device_bytes", C.c_int64),
         ("device", C.c_int32),
-        ("reserved0", C.c_int32),
+        ("initial_block_capacity", C.c_int32),
     ]
 
 

@@ -1,17 +1,25 @@
 // device_common.cuh — shared device-side pieces of the scan-insertion path:
-// the leaf hash, the per-scan mask marking and the exact arithmetic helpers.
+// the two-level leaf index, the first-touch bookkeeping and the exact
+// arithmetic helpers.
 //
-// Map layout in HBM (one map):
-//   hkeys   u64[H]      packed leaf coordinate (voxel >> 3, 21 bits per axis)
-//   hslots  i32[H]      leaf slot for the key; -1 while being published
-//   origin  int4[P]     leaf origin (voxel coordinates, multiples of 8)
-//   values  f32[P][512] log-odds, OpenVDB leaf order (x&7)<<6 | (y&7)<<3 | (z&7)
-//   active  u64[P][8]   value (active) mask, bit i of word w = offset 64w+i
-//   flags   u32[P]      1 once the leaf belongs to the map (first integration)
+// Map layout in HBM (one map). Like OpenVDB's Tree4<float,5,4,3>, leaves are
+// 8^3 voxels; above them, instead of OpenVDB's 16^3/32^3 internal nodes, a
+// hash of 8^3-leaf blocks (64^3 voxels) each holding a dense table of leaf
+// slots, so finding a leaf is one load from a small, L2-resident table:
+//   bkeys   u64[HB]      packed block coordinate (voxel >> 6, 21 bits per axis)
+//   bslots  i32[HB]      block index for the key; -1 while being published
+//   borigin int4[PB]     block coordinate (voxel >> 6)
+//   bleaf   i32[PB][512] leaf slot of each leaf cell of the block, -1 none
+//   origin  int4[P]      leaf origin (voxel coordinates, multiples of 8)
+//   values  f32[P][512]  log-odds, OpenVDB leaf order (x&7)<<6 | (y&7)<<3 | (z&7)
+//   active  u64[P][8]    value (active) mask, bit i of word w = offset 64w+i
+//   flags   u32[P]       1 once the leaf belongs to the map (first integration)
 // Per update grid (one per input source):
-//   upd     u64[P][16]  words 0-7 visited, 8-15 hit, same bit order as active
-//   epoch   u32[P]      integration window in which the leaf was last touched
-//   touched i32[P]      leaves touched in the current window, n_touched of them
+//   upd      u64[P][16]  words 0-7 visited, 8-15 hit, same bit order as active
+//   btouched u64[PB][8]  leaf cells of the block touched in the current window
+//   bepoch   u32[PB]     window in which the block was last touched
+//   blist    i32[PB]     blocks touched in the current window (n_blist)
+//   touched  i32[P]      leaves touched in the window, compacted before the sweep
 #pragma once
 
 #include <cstdint>
@@ -20,9 +28,12 @@
 namespace vdbg {
 
 constexpr unsigned long long kEmptyKey = ~0ull;
-constexpr int kSlotPending             = -1;
+constexpr int kSlotPending             = -1;  // block hash: being published
 constexpr int kSlotFailed              = -2;
 constexpr int kNoSlot                  = -3;
+constexpr int kLeafEmpty               = -1;  // bleaf cell states
+constexpr int kLeafPending             = -2;
+constexpr int kLeafFailed              = -3;
 constexpr uint32_t kMaxProbes          = 4096;
 constexpr uint32_t kSpinLimit          = 1u << 22;
 constexpr int kKeyBits                 = 21;
@@ -37,6 +48,7 @@ constexpr uint32_t kErrHashFull   = 2u;
 constexpr uint32_t kErrSpin       = 4u;
 constexpr uint32_t kErrCoordRange = 8u;
 constexpr uint32_t kErrStepBound  = 16u;
+constexpr uint32_t kErrBlockFull  = 32u;
 
 // Ray record meta word: bits 0-28 L1 length, bit 29 clipped, bit 30 valid.
 constexpr uint32_t kMetaL1Mask   = (1u << 29) - 1;
@@ -59,7 +71,7 @@ struct DevStatus
   unsigned long long updates;
   unsigned long long nonfinite;
   uint32_t ray_cursor;  // next position in the ray order handed to a DDA warp
-  uint32_t pad32;
+  uint32_t n_blocks;    // block bump allocator
   unsigned long long pad[2];
 };
 
@@ -81,18 +93,24 @@ struct ScanGeom
 
 struct MapView
 {
-  unsigned long long* hkeys;
-  int* hslots;
-  uint32_t hmask;
-  uint32_t capacity;
+  unsigned long long* bkeys;
+  int* bslots;
+  uint32_t bhmask;
+  uint32_t bcapacity;
+  int* bleaf;
+  int4* borigin;
   int4* origin;
+  uint32_t capacity;
   DevStatus* st;
 };
 
 struct ChannelView
 {
   unsigned long long* upd;
-  uint32_t* epoch;
+  unsigned long long* btouched;
+  uint32_t* bepoch;
+  int* blist;
+  uint32_t* n_blist;
   int* touched;
   uint32_t* n_touched;
   uint32_t cur_epoch;
@@ -169,59 +187,61 @@ __device__ __forceinline__ unsigned long long pack_leaf_key(int lx, int ly, int 
          (static_cast<unsigned long long>(lz) & m);
 }
 
-// Appends `slot` to the channel's touched list the first time it is seen in
-// the current integration window.
-__device__ __forceinline__ void touch_leaf(const ChannelView& c, int slot)
+// Appends block `b` to the channel's touched-block list the first time it is
+// seen in the current integration window.
+__device__ __forceinline__ void touch_block(const ChannelView& c, int b)
 {
-  uint32_t* e = c.epoch + slot;
+  uint32_t* e = c.bepoch + b;
   if (ld_ca_u32(e) != c.cur_epoch)
   {
     if (atomicExch(e, c.cur_epoch) != c.cur_epoch)
     {
-      const uint32_t t = atomicAdd(c.n_touched, 1u);
-      c.touched[t]     = slot;
+      const uint32_t t = atomicAdd(c.n_blist, 1u);
+      c.blist[t]       = b;
     }
   }
 }
 
-// Slot of leaf (lx,ly,lz), allocating it if absent. Lock-free open addressing
-// with linear probing: the thread whose CAS claims an empty key allocates the
-// slot from the bump counter and publishes it; others that find the key wait
-// (bounded) for the publication. Returns kSlotFailed after setting an error
-// bit when the pool or the probe budget is exhausted.
-__device__ __forceinline__ int find_or_insert_leaf(const MapView& m, int lx, int ly, int lz)
+// Index of block (bx,by,bz), allocating it if absent. Lock-free open
+// addressing with linear probing: the thread whose CAS claims an empty key
+// allocates the block from the bump counter and publishes it; others that
+// find the key wait (bounded) for the publication. New blocks come with all
+// leaf cells empty (the block pool is filled with -1 when allocated). Returns
+// kSlotFailed after setting an error bit when the block pool or the probe
+// budget is exhausted.
+__device__ __forceinline__ int find_or_insert_block(const MapView& m, int bx, int by, int bz)
 {
-  const unsigned long long key = pack_leaf_key(lx, ly, lz);
-  uint32_t h                   = static_cast<uint32_t>(mix64(key)) & m.hmask;
+  const unsigned long long key = pack_leaf_key(bx, by, bz);
+  uint32_t h                   = static_cast<uint32_t>(mix64(key)) & m.bhmask;
   for (uint32_t probe = 0; probe < kMaxProbes; ++probe)
   {
-    unsigned long long k = ld_ca_u64(m.hkeys + h);
+    unsigned long long k = ld_ca_u64(m.bkeys + h);
     if (k == kEmptyKey)
     {
-      const unsigned long long prev = atomicCAS(m.hkeys + h, kEmptyKey, key);
+      const unsigned long long prev = atomicCAS(m.bkeys + h, kEmptyKey, key);
       if (prev == kEmptyKey)
       {
-        const uint32_t s = atomicAdd(&m.st->n_leaves, 1u);
+        const uint32_t s = atomicAdd(&m.st->n_blocks, 1u);
         int slot;
-        if (s >= m.capacity)
+        if (s >= m.bcapacity)
         {
-          atomicOr(&m.st->error, kErrPoolFull);
+          atomicOr(&m.st->error, kErrBlockFull);
           slot = kSlotFailed;
         }
         else
         {
-          m.origin[s] = make_int4(lx * 8, ly * 8, lz * 8, 0);
-          slot        = static_cast<int>(s);
+          m.borigin[s] = make_int4(bx, by, bz, 0);
+          slot         = static_cast<int>(s);
         }
-        st_release_s32(m.hslots + h, slot);
+        st_release_s32(m.bslots + h, slot);
         return slot;
       }
       k = prev;
     }
     if (k == key)
     {
-      int s          = ld_ca_s32(m.hslots + h);
-      if (s == kSlotPending) s = ld_acquire_s32(m.hslots + h);
+      int s = ld_ca_s32(m.bslots + h);
+      if (s == kSlotPending) s = ld_acquire_s32(m.bslots + h);
       uint32_t spins = 0;
       while (s == kSlotPending)
       {
@@ -231,99 +251,66 @@ __device__ __forceinline__ int find_or_insert_leaf(const MapView& m, int lx, int
           return kSlotFailed;
         }
         __nanosleep(64);
-        s = ld_acquire_s32(m.hslots + h);
+        s = ld_acquire_s32(m.bslots + h);
       }
-      return s < 0 ? kSlotFailed : s;
+      if (s < 0)
+      {
+        // An allocation that failed earlier: the host has to grow and retry.
+        atomicOr(&m.st->error, kErrBlockFull);
+        return kSlotFailed;
+      }
+      return s;
     }
-    h = (h + 1) & m.hmask;
+    h = (h + 1) & m.bhmask;
   }
   atomicOr(&m.st->error, kErrHashFull);
   return kSlotFailed;
 }
 
-// Per-thread marker: caches the current leaf slot and accumulates the bits of
-// one 64-bit mask word (one x-slab of the leaf) before a single atomicOr.
-struct Marker
+// Slot of the leaf in cell `cell` of block `b` (leaf coordinate lx,ly,lz),
+// allocating it from the leaf pool if the cell is empty: a CAS moves the cell
+// from empty to pending, the winner takes a slot and publishes it.
+__device__ __forceinline__ int find_or_insert_leaf(const MapView& m, int b, int cell, int lx, int ly, int lz)
 {
-  int lx, ly, lz;
-  int slot;
-  int word;
-  unsigned long long bits;
-};
-
-__device__ __forceinline__ void marker_init(Marker& mk)
-{
-  mk.lx   = 0x7fffffff;
-  mk.ly   = 0x7fffffff;
-  mk.lz   = 0x7fffffff;
-  mk.slot = kNoSlot;
-  mk.word = -1;
-  mk.bits = 0ull;
-}
-
-// OR `bits` into a mask word; bits only ever get set while a scan is being
-// marked, so a relaxed read that already shows them makes the atomic
-// unnecessary (a stale read can only show fewer bits).
-__device__ __forceinline__ void or_bits(unsigned long long* p, unsigned long long bits)
-{
-  const unsigned long long cur = ld_relaxed_u64(p);
-  if ((cur & bits) != bits) atomicOr(p, bits);
-}
-
-__device__ __forceinline__ void marker_flush(Marker& mk, const ChannelView& c)
-{
-  if (mk.bits && mk.slot >= 0)
+  int* e = m.bleaf + static_cast<size_t>(b) * 512 + cell;
+  int s  = ld_ca_s32(e);
+  if (s >= 0) return s;
+  if (s == kLeafEmpty)
   {
-    or_bits(c.upd + static_cast<size_t>(mk.slot) * 16 + mk.word, mk.bits);
+    const int prev = atomicCAS(e, kLeafEmpty, kLeafPending);
+    if (prev == kLeafEmpty)
+    {
+      const uint32_t t = atomicAdd(&m.st->n_leaves, 1u);
+      if (t >= m.capacity)
+      {
+        atomicOr(&m.st->error, kErrPoolFull);
+        st_release_s32(e, kLeafFailed);
+        return kSlotFailed;
+      }
+      m.origin[t] = make_int4(lx * 8, ly * 8, lz * 8, 0);
+      st_release_s32(e, static_cast<int>(t));
+      return static_cast<int>(t);
+    }
+    s = prev;
   }
-  mk.bits = 0ull;
-}
-
-__device__ __forceinline__ void marker_enter_leaf(Marker& mk, const MapView& m, const ChannelView& c,
-                                                  int lx, int ly, int lz)
-{
-  marker_flush(mk, c);
-  mk.lx   = lx;
-  mk.ly   = ly;
-  mk.lz   = lz;
-  mk.slot = find_or_insert_leaf(m, lx, ly, lz);
-  if (mk.slot >= 0) touch_leaf(c, mk.slot);
-  mk.word = -1;
-}
-
-// setActiveState(voxel, true) on the update grid (VDBMapping.hpp:563).
-__device__ __forceinline__ void mark_visit(Marker& mk, const MapView& m, const ChannelView& c, int x,
-                                           int y, int z)
-{
-  const int lx = x >> 3, ly = y >> 3, lz = z >> 3;
-  if (lx != mk.lx || ly != mk.ly || lz != mk.lz || mk.slot == kNoSlot)
+  uint32_t spins = 0;
+  while (s == kLeafPending)
   {
-    marker_enter_leaf(mk, m, c, lx, ly, lz);
+    if (++spins > kSpinLimit)
+    {
+      atomicOr(&m.st->error, kErrSpin);
+      return kSlotFailed;
+    }
+    __nanosleep(64);
+    s = ld_acquire_s32(e);
   }
-  const int w = x & 7;
-  if (w != mk.word)
+  if (s < 0)
   {
-    marker_flush(mk, c);
-    mk.word = w;
+    // An allocation that failed earlier: the host has to grow and retry.
+    atomicOr(&m.st->error, kErrPoolFull);
+    return kSlotFailed;
   }
-  mk.bits |= 1ull << (((y & 7) << 3) | (z & 7));
-}
-
-// setValueOn(end, true) on the update grid (VDBMapping.hpp:535): the hit word.
-__device__ __forceinline__ void mark_hit(Marker& mk, const MapView& m, const ChannelView& c, int x,
-                                         int y, int z)
-{
-  marker_flush(mk, c);
-  const int lx = x >> 3, ly = y >> 3, lz = z >> 3;
-  if (lx != mk.lx || ly != mk.ly || lz != mk.lz || mk.slot == kNoSlot)
-  {
-    marker_enter_leaf(mk, m, c, lx, ly, lz);
-  }
-  if (mk.slot >= 0)
-  {
-    or_bits(c.upd + static_cast<size_t>(mk.slot) * 16 + 8 + (x & 7),
-            1ull << (((y & 7) << 3) | (z & 7)));
-  }
+  return s;
 }
 
 // VDBMapping.hpp:612-631 for one axis: shift non-multiples of the resolution

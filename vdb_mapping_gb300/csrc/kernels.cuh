@@ -8,10 +8,11 @@
 //   k_dda_mark VDBMapping.hpp:550-566,   FP64 DDA from the sensor voxel to the
 //              :533-536                 endpoint voxel; marks visited and hit
 //                                       bits of the per-leaf update masks
+//   k_compact  (none)                   touched blocks -> flat touched-leaf list
 //   k_sweep    VDBMapping.hpp:731-792 + per touched leaf: FP32 log-odds update,
 //              OccupancyVDBMapping.hpp:92-117  thresholds, clamp, active mask;
 //                                       clears the update masks
-//   k_rehash   (none)                   rebuilds the leaf hash after pool growth
+//   k_rehash   (none)                   rebuilds the block hash after growth
 #pragma once
 
 #include "device_common.cuh"
@@ -228,8 +229,9 @@ __device__ __forceinline__ void dda_put_slab(DdaWarpSmem& q, int lane, int rec, 
 }
 
 // Flushes the closed records [0, n_done) of every lane, round by round.
+// `cbkey`/`cblock` cache the lane's last resolved block across rounds.
 __device__ __forceinline__ void dda_flush(DdaWarpSmem& q, int lane, int n_done, const MapView& m,
-                                          const ChannelView& c)
+                                          const ChannelView& c, unsigned long long& cbkey, int& cblock)
 {
   __syncwarp();
   const int rounds = __reduce_max_sync(0xffffffffu, static_cast<unsigned>(n_done));
@@ -261,16 +263,27 @@ __device__ __forceinline__ void dda_flush(DdaWarpSmem& q, int lane, int n_done, 
     int slot = kSlotFailed;
     if (mine && leader == lane)
     {
-      slot = find_or_insert_leaf(m, unpack_leaf_coord(key, 0), unpack_leaf_coord(key, 1),
-                                 unpack_leaf_coord(key, 2));
-      if (slot >= 0)
+      const int lx = unpack_leaf_coord(key, 0), ly = unpack_leaf_coord(key, 1), lz = unpack_leaf_coord(key, 2);
+      const unsigned long long bkey = pack_leaf_key(lx >> 3, ly >> 3, lz >> 3);
+      if (bkey != cbkey)
       {
-        touch_leaf(c, slot);
-        unsigned long long* u = c.upd + static_cast<size_t>(slot) * 16;
-        for (uint32_t z = group_nz; z; z &= z - 1)
+        cbkey  = bkey;
+        cblock = find_or_insert_block(m, lx >> 3, ly >> 3, lz >> 3);
+        if (cblock >= 0) touch_block(c, cblock);
+      }
+      if (cblock >= 0)
+      {
+        const int cell = ((lx & 7) << 6) | ((ly & 7) << 3) | (lz & 7);
+        slot           = find_or_insert_leaf(m, cblock, cell, lx, ly, lz);
+        if (slot >= 0)
         {
-          const int w = __ffs(z) - 1;
-          atomicOr(u + w, q.words[r][w][lane]);
+          atomicOr(c.btouched + static_cast<size_t>(cblock) * 8 + (cell >> 6), 1ull << (cell & 63));
+          unsigned long long* u = c.upd + static_cast<size_t>(slot) * 16;
+          for (uint32_t z = group_nz; z; z &= z - 1)
+          {
+            const int w = __ffs(z) - 1;
+            atomicOr(u + w, q.words[r][w][lane]);
+          }
         }
       }
     }
@@ -307,6 +320,8 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
   uint32_t rec_nz = 0;  // non-zero words of the open record
   int n_done = 0;       // closed records in the ring; the open one is at index n_done
   uint32_t hit_off = 0, budget = 0;
+  unsigned long long cbkey = kEmptyKey;  // last block resolved by this lane
+  int cblock               = kSlotFailed;
   const long long kOne = __double_as_longlong(1.0);
   const long long kMax = __double_as_longlong(1.7976931348623157e308);
 
@@ -469,7 +484,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
     }
 
     // ---- flush the closed records; the open one moves to the ring start -------
-    dda_flush(q, lane, n_done, m, c);
+    dda_flush(q, lane, n_done, m, c, cbkey, cblock);
     if (n_done > 0 && cur_valid)
     {
       q.keys[0][lane] = q.keys[n_done][lane];
@@ -559,24 +574,70 @@ __global__ void __launch_bounds__(256) k_sweep(ChannelView c, float* __restrict_
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&st->touched, nt);
 }
 
-// Inserts leaves [0, n) of the pool into an empty hash table.
+// Turns the touched-block list of a window into the flat list of touched
+// leaves the sweep walks, clearing the blocks' touched bits. One warp per
+// block, one lane per 64-cell word. `force` runs it while an error is set
+// (to undo a partial marking).
+__global__ void __launch_bounds__(256) k_compact(MapView m, ChannelView c, DevStatus* st, int force)
+{
+  if (!force && ld_relaxed_u32(&st->error) != 0u) return;
+  const uint32_t nb   = *c.n_blist;
+  const int lane      = static_cast<int>(threadIdx.x & 31);
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nw   = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = warp; i < nb; i += nw)
+  {
+    const int b                 = c.blist[i];
+    unsigned long long* tw      = c.btouched + static_cast<size_t>(b) * 8;
+    const unsigned long long w  = lane < 8 ? tw[lane] : 0ull;
+    const uint32_t cnt          = static_cast<uint32_t>(__popcll(w));
+    uint32_t incl               = cnt;
+    for (int off = 1; off < 8; off <<= 1)
+    {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += y;
+    }
+    uint32_t base = 0;
+    if (lane == 7) base = atomicAdd(c.n_touched, incl);
+    base = __shfl_sync(0xffffffffu, base, 7) + incl - cnt;
+    if (lane < 8 && w)
+    {
+      const int* cells = m.bleaf + static_cast<size_t>(b) * 512 + lane * 64;
+      uint32_t k       = 0;
+      for (unsigned long long z = w; z; z &= z - 1) c.touched[base + k++] = cells[__ffsll(z) - 1];
+      tw[lane] = 0ull;
+    }
+  }
+}
+
+// Inserts blocks [0, n) of the block pool into an empty block hash.
 __global__ void k_rehash(MapView m, uint32_t n)
 {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const int4 o                 = m.origin[s];
-  const unsigned long long key = pack_leaf_key(o.x >> 3, o.y >> 3, o.z >> 3);
-  uint32_t h                   = static_cast<uint32_t>(mix64(key)) & m.hmask;
-  for (uint32_t probe = 0; probe <= m.hmask; ++probe)
+  const int4 o                 = m.borigin[s];
+  const unsigned long long key = pack_leaf_key(o.x, o.y, o.z);
+  uint32_t h                   = static_cast<uint32_t>(mix64(key)) & m.bhmask;
+  for (uint32_t probe = 0; probe <= m.bhmask; ++probe)
   {
-    if (atomicCAS(m.hkeys + h, kEmptyKey, key) == kEmptyKey)
+    if (atomicCAS(m.bkeys + h, kEmptyKey, key) == kEmptyKey)
     {
-      m.hslots[h] = static_cast<int>(s);
+      m.bslots[h] = static_cast<int>(s);
       return;
     }
-    h = (h + 1) & m.hmask;
+    h = (h + 1) & m.bhmask;
   }
   atomicOr(&m.st->error, kErrHashFull);
+}
+
+// After a pool growth: leaf cells whose allocation failed become empty again.
+__global__ void k_reset_failed_leaves(int* __restrict__ bleaf, size_t cells)
+{
+  for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < cells;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+  {
+    if (bleaf[i] == kLeafFailed) bleaf[i] = kLeafEmpty;
+  }
 }
 
 } // namespace vdbg

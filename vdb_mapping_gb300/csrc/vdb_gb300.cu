@@ -24,13 +24,16 @@ namespace {
 struct Channel
 {
   std::string id;
-  double max_range            = 0.0;
-  unsigned long long* upd     = nullptr;  // [P][16]
-  uint32_t* epoch             = nullptr;  // [P]
-  int* touched                = nullptr;  // [P]
-  uint32_t* n_touched         = nullptr;  // device scalar
-  uint32_t cur_epoch          = 1;
-  bool pending                = false;    // marked since its last integration
+  double max_range                  = 0.0;
+  unsigned long long* upd           = nullptr;  // [P][16]
+  int* touched                      = nullptr;  // [P] compacted touched leaves
+  uint32_t* n_touched               = nullptr;  // device scalar
+  unsigned long long* btouched      = nullptr;  // [PB][8]
+  uint32_t* bepoch                  = nullptr;  // [PB]
+  int* blist                        = nullptr;  // [PB]
+  uint32_t* n_blist                 = nullptr;  // device scalar
+  uint32_t cur_epoch                = 1;
+  bool pending                      = false;    // marked since its last integration
 };
 
 } // namespace
@@ -54,16 +57,21 @@ struct vdbg_map
   bool timed_prep       = false;
   vdbg_timings timings{};
 
-  // Leaf pool and hash.
+  // Leaf pool.
   uint32_t capacity     = 0;
-  uint32_t hash_size    = 0;
   float* values         = nullptr;
   unsigned long long* active = nullptr;
   int4* origin          = nullptr;
   uint32_t* flags       = nullptr;
-  unsigned long long* hkeys = nullptr;
-  int* hslots           = nullptr;
   uint32_t n_leaves     = 0;  // host copy after the last call
+  // Block pool and block hash.
+  uint32_t bcapacity    = 0;
+  uint32_t bhash_size   = 0;
+  int* bleaf            = nullptr;
+  int4* borigin         = nullptr;
+  unsigned long long* bkeys = nullptr;
+  int* bslots           = nullptr;
+  uint32_t n_blocks     = 0;  // host copy after the last call
 
   DevStatus* d_status   = nullptr;
   DevStatus* h_status   = nullptr;  // pinned
@@ -97,6 +105,7 @@ namespace {
   } while (0)
 
 constexpr uint32_t kDefaultCapacity = 1u << 16;
+constexpr uint32_t kMinBlocks       = 1u << 10;
 constexpr int kSweepBlocks          = 152 * 8;
 constexpr int kSweepThreads         = 256;
 
@@ -146,12 +155,15 @@ void dev_free(vdbg_map* m, T*& p, size_t count)
 MapView map_view(const vdbg_map* m)
 {
   MapView v;
-  v.hkeys    = m->hkeys;
-  v.hslots   = m->hslots;
-  v.hmask    = m->hash_size - 1;
-  v.capacity = m->capacity;
-  v.origin   = m->origin;
-  v.st       = m->d_status;
+  v.bkeys     = m->bkeys;
+  v.bslots    = m->bslots;
+  v.bhmask    = m->bhash_size - 1;
+  v.bcapacity = m->bcapacity;
+  v.bleaf     = m->bleaf;
+  v.borigin   = m->borigin;
+  v.origin    = m->origin;
+  v.capacity  = m->capacity;
+  v.st        = m->d_status;
   return v;
 }
 
@@ -159,41 +171,69 @@ ChannelView channel_view(const Channel& c)
 {
   ChannelView v;
   v.upd       = c.upd;
-  v.epoch     = c.epoch;
+  v.btouched  = c.btouched;
+  v.bepoch    = c.bepoch;
+  v.blist     = c.blist;
+  v.n_blist   = c.n_blist;
   v.touched   = c.touched;
   v.n_touched = c.n_touched;
   v.cur_epoch = c.cur_epoch;
   return v;
 }
 
-int alloc_channel(vdbg_map* m, Channel& c, uint32_t cap)
+// Leaf-indexed arrays of an update grid.
+int alloc_channel_leaves(vdbg_map* m, Channel& c, uint32_t cap)
 {
   VDBG_TRY(dev_alloc(m, &c.upd, static_cast<size_t>(cap) * 16));
-  VDBG_TRY(dev_alloc(m, &c.epoch, cap));
   VDBG_TRY(dev_alloc(m, &c.touched, cap));
-  if (!c.n_touched) VDBG_TRY(dev_alloc(m, &c.n_touched, 1));
   VDBG_CUDA(cudaMemsetAsync(c.upd, 0, static_cast<size_t>(cap) * 16 * sizeof(unsigned long long), m->stream));
-  VDBG_CUDA(cudaMemsetAsync(c.epoch, 0, static_cast<size_t>(cap) * sizeof(uint32_t), m->stream));
   return VDBG_OK;
 }
 
-void free_channel(vdbg_map* m, Channel& c, uint32_t cap)
+void free_channel_leaves(vdbg_map* m, Channel& c, uint32_t cap)
 {
   dev_free(m, c.upd, static_cast<size_t>(cap) * 16);
-  dev_free(m, c.epoch, cap);
   dev_free(m, c.touched, cap);
 }
 
-// Builds the hash of leaves [0, n) into a fresh table of `hsize` entries.
+// Block-indexed arrays of an update grid.
+int alloc_channel_blocks(vdbg_map* m, Channel& c, uint32_t bcap)
+{
+  VDBG_TRY(dev_alloc(m, &c.btouched, static_cast<size_t>(bcap) * 8));
+  VDBG_TRY(dev_alloc(m, &c.bepoch, bcap));
+  VDBG_TRY(dev_alloc(m, &c.blist, bcap));
+  VDBG_CUDA(cudaMemsetAsync(c.btouched, 0, static_cast<size_t>(bcap) * 8 * sizeof(unsigned long long), m->stream));
+  VDBG_CUDA(cudaMemsetAsync(c.bepoch, 0, static_cast<size_t>(bcap) * sizeof(uint32_t), m->stream));
+  return VDBG_OK;
+}
+
+void free_channel_blocks(vdbg_map* m, Channel& c, uint32_t bcap)
+{
+  dev_free(m, c.btouched, static_cast<size_t>(bcap) * 8);
+  dev_free(m, c.bepoch, bcap);
+  dev_free(m, c.blist, bcap);
+}
+
+// Builds the block hash of blocks [0, n) into a fresh table of `hsize` entries.
 int rebuild_hash(vdbg_map* m, uint32_t hsize, uint32_t n)
 {
-  dev_free(m, m->hkeys, m->hash_size);
-  dev_free(m, m->hslots, m->hash_size);
-  m->hash_size = hsize;
-  VDBG_TRY(dev_alloc(m, &m->hkeys, hsize));
-  VDBG_TRY(dev_alloc(m, &m->hslots, hsize));
-  VDBG_CUDA(cudaMemsetAsync(m->hkeys, 0xff, static_cast<size_t>(hsize) * sizeof(unsigned long long), m->stream));
-  VDBG_CUDA(cudaMemsetAsync(m->hslots, 0xff, static_cast<size_t>(hsize) * sizeof(int), m->stream));
+  unsigned long long* keys = nullptr;
+  int* slots               = nullptr;
+  int st                   = dev_alloc(m, &keys, hsize);
+  if (st == VDBG_OK) st = dev_alloc(m, &slots, hsize);
+  if (st != VDBG_OK)
+  {
+    dev_free(m, keys, hsize);
+    dev_free(m, slots, hsize);
+    return st;
+  }
+  dev_free(m, m->bkeys, m->bhash_size);
+  dev_free(m, m->bslots, m->bhash_size);
+  m->bkeys      = keys;
+  m->bslots     = slots;
+  m->bhash_size = hsize;
+  VDBG_CUDA(cudaMemsetAsync(m->bkeys, 0xff, static_cast<size_t>(hsize) * sizeof(unsigned long long), m->stream));
+  VDBG_CUDA(cudaMemsetAsync(m->bslots, 0xff, static_cast<size_t>(hsize) * sizeof(int), m->stream));
   if (n > 0)
   {
     k_rehash<<<(n + 255) / 256, 256, 0, m->stream>>>(map_view(m), n);
@@ -202,7 +242,8 @@ int rebuild_hash(vdbg_map* m, uint32_t hsize, uint32_t n)
   return VDBG_OK;
 }
 
-// Allocates the leaf pool with `cap` slots, keeping leaves [0, keep).
+// Allocates the leaf pool with `cap` slots, keeping leaves [0, keep). The
+// block tables keep their slot numbers, so nothing else moves.
 int resize_pool(vdbg_map* m, uint32_t cap, uint32_t keep)
 {
   float* values              = nullptr;
@@ -214,11 +255,7 @@ int resize_pool(vdbg_map* m, uint32_t cap, uint32_t keep)
   if (st == VDBG_OK) st = dev_alloc(m, &active, static_cast<size_t>(cap) * 8);
   if (st == VDBG_OK) st = dev_alloc(m, &origin, cap);
   if (st == VDBG_OK) st = dev_alloc(m, &flags, cap);
-  for (size_t i = 0; i < fresh.size() && st == VDBG_OK; ++i)
-  {
-    fresh[i].n_touched = m->channels[i].n_touched;
-    st                 = alloc_channel(m, fresh[i], cap);
-  }
+  for (size_t i = 0; i < fresh.size() && st == VDBG_OK; ++i) st = alloc_channel_leaves(m, fresh[i], cap);
   if (st != VDBG_OK)
   {
     // Leave the map as it was.
@@ -226,7 +263,7 @@ int resize_pool(vdbg_map* m, uint32_t cap, uint32_t keep)
     dev_free(m, active, static_cast<size_t>(cap) * 8);
     dev_free(m, origin, cap);
     dev_free(m, flags, cap);
-    for (Channel& c : fresh) free_channel(m, c, cap);
+    for (Channel& c : fresh) free_channel_leaves(m, c, cap);
     return st;
   }
   cudaStream_t s = m->stream;
@@ -252,15 +289,10 @@ int resize_pool(vdbg_map* m, uint32_t cap, uint32_t keep)
     {
       VDBG_CUDA(cudaMemcpyAsync(nc.upd, c.upd, static_cast<size_t>(keep) * 16 * sizeof(unsigned long long),
                                 cudaMemcpyDeviceToDevice, s));
-      VDBG_CUDA(cudaMemcpyAsync(nc.epoch, c.epoch, static_cast<size_t>(keep) * sizeof(uint32_t),
-                                cudaMemcpyDeviceToDevice, s));
-      VDBG_CUDA(cudaMemcpyAsync(nc.touched, c.touched, static_cast<size_t>(keep) * sizeof(int),
-                                cudaMemcpyDeviceToDevice, s));
     }
     VDBG_CUDA(cudaStreamSynchronize(s));
-    free_channel(m, c, m->capacity);
+    free_channel_leaves(m, c, m->capacity);
     c.upd     = nc.upd;
-    c.epoch   = nc.epoch;
     c.touched = nc.touched;
   }
   VDBG_CUDA(cudaStreamSynchronize(s));
@@ -273,7 +305,61 @@ int resize_pool(vdbg_map* m, uint32_t cap, uint32_t keep)
   m->origin   = origin;
   m->flags    = flags;
   m->capacity = cap;
-  VDBG_TRY(rebuild_hash(m, next_pow2(static_cast<uint64_t>(cap) * 2), keep));
+  return VDBG_OK;
+}
+
+// Allocates the block pool with `bcap` blocks, keeping blocks [0, keep), and
+// rebuilds the block hash.
+int resize_blocks(vdbg_map* m, uint32_t bcap, uint32_t keep)
+{
+  int* bleaf    = nullptr;
+  int4* borigin = nullptr;
+  std::vector<Channel> fresh(m->channels.size());
+  int st = dev_alloc(m, &bleaf, static_cast<size_t>(bcap) * 512);
+  if (st == VDBG_OK) st = dev_alloc(m, &borigin, bcap);
+  for (size_t i = 0; i < fresh.size() && st == VDBG_OK; ++i) st = alloc_channel_blocks(m, fresh[i], bcap);
+  if (st != VDBG_OK)
+  {
+    dev_free(m, bleaf, static_cast<size_t>(bcap) * 512);
+    dev_free(m, borigin, bcap);
+    for (Channel& c : fresh) free_channel_blocks(m, c, bcap);
+    return st;
+  }
+  cudaStream_t s = m->stream;
+  VDBG_CUDA(cudaMemsetAsync(bleaf, 0xff, static_cast<size_t>(bcap) * 512 * sizeof(int), s));
+  if (keep > 0)
+  {
+    VDBG_CUDA(cudaMemcpyAsync(bleaf, m->bleaf, static_cast<size_t>(keep) * 512 * sizeof(int),
+                              cudaMemcpyDeviceToDevice, s));
+    VDBG_CUDA(cudaMemcpyAsync(borigin, m->borigin, static_cast<size_t>(keep) * sizeof(int4),
+                              cudaMemcpyDeviceToDevice, s));
+  }
+  for (size_t i = 0; i < m->channels.size(); ++i)
+  {
+    Channel& c  = m->channels[i];
+    Channel& nc = fresh[i];
+    if (keep > 0)
+    {
+      VDBG_CUDA(cudaMemcpyAsync(nc.btouched, c.btouched, static_cast<size_t>(keep) * 8 * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToDevice, s));
+      VDBG_CUDA(cudaMemcpyAsync(nc.bepoch, c.bepoch, static_cast<size_t>(keep) * sizeof(uint32_t),
+                                cudaMemcpyDeviceToDevice, s));
+      VDBG_CUDA(cudaMemcpyAsync(nc.blist, c.blist, static_cast<size_t>(keep) * sizeof(int),
+                                cudaMemcpyDeviceToDevice, s));
+    }
+    VDBG_CUDA(cudaStreamSynchronize(s));
+    free_channel_blocks(m, c, m->bcapacity);
+    c.btouched = nc.btouched;
+    c.bepoch   = nc.bepoch;
+    c.blist    = nc.blist;
+  }
+  VDBG_CUDA(cudaStreamSynchronize(s));
+  dev_free(m, m->bleaf, static_cast<size_t>(m->bcapacity) * 512);
+  dev_free(m, m->borigin, m->bcapacity);
+  m->bleaf     = bleaf;
+  m->borigin   = borigin;
+  m->bcapacity = bcap;
+  VDBG_TRY(rebuild_hash(m, next_pow2(static_cast<uint64_t>(bcap) * 2), keep));
   // Work queued by the caller on another stream must see the new tables.
   VDBG_CUDA(cudaStreamSynchronize(s));
   return VDBG_OK;
@@ -341,6 +427,7 @@ int begin_call(vdbg_map* m, cudaStream_t s)
   m->timed_prep        = false;
   clear_status(m->h_status);
   m->h_status->n_leaves = m->n_leaves;
+  m->h_status->n_blocks = m->n_blocks;
   VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
   VDBG_CUDA(cudaEventRecord(m->ev0, s));
   return VDBG_OK;
@@ -448,12 +535,15 @@ int launch_raycast(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t
   return VDBG_OK;
 }
 
+// Integration of one update grid: compact its touched blocks into the list
+// of touched leaves, then sweep them.
 int launch_sweep(vdbg_map* m, Channel& c, cudaStream_t s)
 {
+  k_compact<<<kSweepBlocks, kSweepThreads, 0, s>>>(map_view(m), channel_view(c), m->d_status, 0);
   k_sweep<<<kSweepBlocks, kSweepThreads, 0, s>>>(channel_view(c), m->values, m->active, m->flags, m->lo,
                                                  m->d_status);
   VDBG_CUDA(cudaGetLastError());
-  m->timings.launches += 1;
+  m->timings.launches += 2;
   return VDBG_OK;
 }
 
@@ -461,15 +551,16 @@ int launch_sweep(vdbg_map* m, Channel& c, cudaStream_t s)
 int finish_sweep(vdbg_map* m, Channel& c, cudaStream_t s)
 {
   VDBG_CUDA(cudaMemsetAsync(c.n_touched, 0, sizeof(uint32_t), s));
+  VDBG_CUDA(cudaMemsetAsync(c.n_blist, 0, sizeof(uint32_t), s));
   c.cur_epoch += 1;
   if (c.cur_epoch == 0) c.cur_epoch = 1;
   c.pending = false;
   return VDBG_OK;
 }
 
-// Grows the pool after an allocation failure (or when it is getting full) and
-// rebuilds the hash. `requested` is the bump counter, which counts every
-// allocation attempt of the failed pass.
+// Grows the leaf pool after an allocation failure (or when it is getting
+// full). `requested` is the bump counter, which counts every allocation
+// attempt of the failed pass.
 int grow_for(vdbg_map* m, uint64_t requested)
 {
   const uint32_t keep = std::min<uint32_t>(m->n_leaves, m->capacity);
@@ -477,6 +568,16 @@ int grow_for(vdbg_map* m, uint64_t requested)
   if (want > (1ull << 30)) want = 1ull << 30;
   if (want <= m->capacity) return VDBG_ERR_OUT_OF_MEMORY;
   return resize_pool(m, static_cast<uint32_t>(want), keep);
+}
+
+// Same for the block pool (which also rebuilds the block hash).
+int grow_blocks_for(vdbg_map* m, uint64_t requested)
+{
+  const uint32_t keep = std::min<uint32_t>(m->n_blocks, m->bcapacity);
+  uint64_t want       = std::max<uint64_t>(static_cast<uint64_t>(m->bcapacity) * 2, requested + requested / 2);
+  if (want > (1ull << 28)) want = 1ull << 28;
+  if (want <= m->bcapacity) return VDBG_ERR_OUT_OF_MEMORY;
+  return resize_blocks(m, static_cast<uint32_t>(want), keep);
 }
 
 int map_error(uint32_t err)
@@ -491,7 +592,11 @@ int maybe_grow_ahead(vdbg_map* m)
 {
   if (static_cast<uint64_t>(m->n_leaves) * 10 > static_cast<uint64_t>(m->capacity) * 7)
   {
-    return grow_for(m, static_cast<uint64_t>(m->capacity) * 2);
+    VDBG_TRY(grow_for(m, static_cast<uint64_t>(m->capacity) * 2));
+  }
+  if (static_cast<uint64_t>(m->n_blocks) * 10 > static_cast<uint64_t>(m->bcapacity) * 7)
+  {
+    VDBG_TRY(grow_blocks_for(m, static_cast<uint64_t>(m->bcapacity) * 2));
   }
   return VDBG_OK;
 }
@@ -547,11 +652,14 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
   VDBG_TRY(sweeps());
   int call_status = VDBG_OK;
   bool done       = false;
-  for (int attempt = 0; attempt < 8 && !done; ++attempt)
+  // Every growth at least doubles what ran out, so this converges long before
+  // the pools reach their size limits.
+  for (int attempt = 0; attempt < 40 && !done; ++attempt)
   {
     VDBG_TRY(fetch_status(m, s));
     const uint32_t err = m->h_status->error;
     m->n_leaves        = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
+    m->n_blocks        = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
     if (err == 0)
     {
       done = true;
@@ -565,17 +673,28 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
       DevStatus clean;
       clear_status(&clean);
       clean.n_leaves     = m->n_leaves;
+      clean.n_blocks     = m->n_blocks;
       *m->h_status       = clean;
       VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
       VDBG_TRY(sweeps());
       continue;
     }
-    // Pool or hash exhausted: grow, clear the error, mark again, sweep.
-    const uint64_t requested = m->h_status->n_leaves;
-    VDBG_TRY(grow_for(m, requested));
+    // A pool or the block hash is exhausted: grow what ran out, let the
+    // failed leaf cells be allocated again, clear the error, mark again, sweep.
+    if (err & kErrPoolFull) VDBG_TRY(grow_for(m, m->h_status->n_leaves));
+    if (err & kErrBlockFull) VDBG_TRY(grow_blocks_for(m, m->h_status->n_blocks));
+    if ((err & kErrHashFull) && !(err & kErrBlockFull))
+      VDBG_TRY(rebuild_hash(m, m->bhash_size * 2, m->n_blocks));
+    if (m->n_blocks > 0)
+    {
+      k_reset_failed_leaves<<<m->num_sms * 4, 256, 0, m->stream>>>(m->bleaf, static_cast<size_t>(m->n_blocks) * 512);
+      VDBG_CUDA(cudaGetLastError());
+    }
+    VDBG_CUDA(cudaStreamSynchronize(m->stream));
     DevStatus keep  = *m->h_status;
     keep.error      = 0;
     keep.n_leaves   = m->n_leaves;
+    keep.n_blocks   = m->n_blocks;
     keep.ray_cursor = 0;  // the re-marking pass walks all rays again
     *m->h_status   = keep;
     VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
@@ -635,10 +754,12 @@ int vdbg_create(double resolution, const vdbg_options* options, vdbg_map** out)
   m->half_res   = resolution / 2.0;
   m->inv_res    = 1.0 / resolution;
   uint32_t cap  = kDefaultCapacity;
+  uint32_t bcap = 0;
   if (options)
   {
     if (options->initial_leaf_capacity > 0)
       cap = static_cast<uint32_t>(std::min<int64_t>(options->initial_leaf_capacity, int64_t(1) << 30));
+    if (options->initial_block_capacity > 0) bcap = static_cast<uint32_t>(options->initial_block_capacity);
     m->max_bytes = options->max_device_bytes;
     m->device    = options->device;
   }
@@ -670,6 +791,10 @@ int vdbg_create(double resolution, const vdbg_options* options, vdbg_map** out)
     return fail(VDBG_ERR_CUDA);
   s = resize_pool(m, cap, 0);
   if (s != VDBG_OK) return fail(s);
+  // A block holds up to 512 leaves; maps fill blocks partly, so reserve one
+  // block per 32 leaf slots and grow on demand.
+  s = resize_blocks(m, bcap ? bcap : std::max<uint32_t>(kMinBlocks, cap / 32), 0);
+  if (s != VDBG_OK) return fail(s);
   if (cudaStreamSynchronize(m->stream) != cudaSuccess) return fail(VDBG_ERR_CUDA);
   *out = m;
   return VDBG_OK;
@@ -682,15 +807,19 @@ int vdbg_destroy(vdbg_map* m)
   if (m->stream) cudaStreamSynchronize(m->stream);
   for (Channel& c : m->channels)
   {
-    free_channel(m, c, m->capacity);
+    free_channel_leaves(m, c, m->capacity);
+    free_channel_blocks(m, c, m->bcapacity);
     dev_free(m, c.n_touched, 1);
+    dev_free(m, c.n_blist, 1);
   }
   dev_free(m, m->values, static_cast<size_t>(m->capacity) * 512);
   dev_free(m, m->active, static_cast<size_t>(m->capacity) * 8);
   dev_free(m, m->origin, m->capacity);
   dev_free(m, m->flags, m->capacity);
-  dev_free(m, m->hkeys, m->hash_size);
-  dev_free(m, m->hslots, m->hash_size);
+  dev_free(m, m->bleaf, static_cast<size_t>(m->bcapacity) * 512);
+  dev_free(m, m->borigin, m->bcapacity);
+  dev_free(m, m->bkeys, m->bhash_size);
+  dev_free(m, m->bslots, m->bhash_size);
   dev_free(m, m->d_status, 1);
   dev_free(m, m->d_hist, kNumBuckets);
   dev_free(m, m->d_cursor, kNumBuckets);
@@ -747,8 +876,20 @@ int vdbg_add_input_source(vdbg_map* m, const char* id, double max_range, double 
   Channel c;
   c.id        = id;
   c.max_range = (max_range == 0) ? m->max_range : max_range;
-  VDBG_TRY(alloc_channel(m, c, m->capacity));
+  int st      = alloc_channel_leaves(m, c, m->capacity);
+  if (st == VDBG_OK) st = alloc_channel_blocks(m, c, m->bcapacity);
+  if (st == VDBG_OK) st = dev_alloc(m, &c.n_touched, 1);
+  if (st == VDBG_OK) st = dev_alloc(m, &c.n_blist, 1);
+  if (st != VDBG_OK)
+  {
+    free_channel_leaves(m, c, m->capacity);
+    free_channel_blocks(m, c, m->bcapacity);
+    dev_free(m, c.n_touched, 1);
+    dev_free(m, c.n_blist, 1);
+    return st;
+  }
   VDBG_CUDA(cudaMemsetAsync(c.n_touched, 0, sizeof(uint32_t), m->stream));
+  VDBG_CUDA(cudaMemsetAsync(c.n_blist, 0, sizeof(uint32_t), m->stream));
   VDBG_CUDA(cudaStreamSynchronize(m->stream));
   m->channels.push_back(c);
   std::sort(m->channels.begin(), m->channels.end(),
@@ -822,23 +963,28 @@ int vdbg_reset_map(vdbg_map* m)
 {
   if (!m) return VDBG_ERR_INVALID_ARGUMENT;
   VDBG_TRY(set_device(m));
-  cudaStream_t s = m->stream;
-  const uint32_t cap = m->capacity;
+  cudaStream_t s      = m->stream;
+  const uint32_t cap  = m->capacity;
+  const uint32_t bcap = m->bcapacity;
   VDBG_CUDA(cudaMemsetAsync(m->values, 0, static_cast<size_t>(cap) * 512 * sizeof(float), s));
   VDBG_CUDA(cudaMemsetAsync(m->active, 0, static_cast<size_t>(cap) * 8 * sizeof(unsigned long long), s));
   VDBG_CUDA(cudaMemsetAsync(m->flags, 0, static_cast<size_t>(cap) * sizeof(uint32_t), s));
-  VDBG_CUDA(cudaMemsetAsync(m->hkeys, 0xff, static_cast<size_t>(m->hash_size) * sizeof(unsigned long long), s));
-  VDBG_CUDA(cudaMemsetAsync(m->hslots, 0xff, static_cast<size_t>(m->hash_size) * sizeof(int), s));
+  VDBG_CUDA(cudaMemsetAsync(m->bleaf, 0xff, static_cast<size_t>(bcap) * 512 * sizeof(int), s));
+  VDBG_CUDA(cudaMemsetAsync(m->bkeys, 0xff, static_cast<size_t>(m->bhash_size) * sizeof(unsigned long long), s));
+  VDBG_CUDA(cudaMemsetAsync(m->bslots, 0xff, static_cast<size_t>(m->bhash_size) * sizeof(int), s));
   for (Channel& c : m->channels)
   {
     VDBG_CUDA(cudaMemsetAsync(c.upd, 0, static_cast<size_t>(cap) * 16 * sizeof(unsigned long long), s));
-    VDBG_CUDA(cudaMemsetAsync(c.epoch, 0, static_cast<size_t>(cap) * sizeof(uint32_t), s));
+    VDBG_CUDA(cudaMemsetAsync(c.btouched, 0, static_cast<size_t>(bcap) * 8 * sizeof(unsigned long long), s));
+    VDBG_CUDA(cudaMemsetAsync(c.bepoch, 0, static_cast<size_t>(bcap) * sizeof(uint32_t), s));
     VDBG_CUDA(cudaMemsetAsync(c.n_touched, 0, sizeof(uint32_t), s));
+    VDBG_CUDA(cudaMemsetAsync(c.n_blist, 0, sizeof(uint32_t), s));
     c.cur_epoch = 1;
     c.pending   = false;
   }
   VDBG_CUDA(cudaStreamSynchronize(s));
   m->n_leaves = 0;
+  m->n_blocks = 0;
   return VDBG_OK;
 }
 
@@ -1069,6 +1215,7 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
   VDBG_TRY(fetch_status(m, s));
   uint32_t err = m->h_status->error;
   m->n_leaves  = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
+  m->n_blocks  = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
   int result   = pre;
   if (err & kErrCoordRange)
   {
@@ -1077,6 +1224,7 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
     DevStatus clean;
     clear_status(&clean);
     clean.n_leaves = m->n_leaves;
+    clean.n_blocks = m->n_blocks;
     *m->h_status   = clean;
     VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
     for (Channel* c : todo) VDBG_TRY(launch_sweep(m, *c, s));
@@ -1089,13 +1237,29 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
     // apply nothing and report.
     if (src && cast)
     {
+      k_compact<<<m->num_sms * 4, 256, 0, s>>>(map_view(m), channel_view(*src), m->d_status, 1);
       k_clear_touched<<<m->num_sms * 4, 256, 0, s>>>(channel_view(*src));
       VDBG_CUDA(cudaGetLastError());
       VDBG_TRY(finish_sweep(m, *src, s));
     }
+    // Failed leaf cells become empty again and the block hash is rebuilt in
+    // place from the allocated blocks, so later calls see a consistent index.
+    if (m->n_blocks > 0)
+    {
+      k_reset_failed_leaves<<<m->num_sms * 4, 256, 0, s>>>(m->bleaf, static_cast<size_t>(m->n_blocks) * 512);
+      VDBG_CUDA(cudaGetLastError());
+    }
+    VDBG_CUDA(cudaMemsetAsync(m->bkeys, 0xff, static_cast<size_t>(m->bhash_size) * sizeof(unsigned long long), s));
+    VDBG_CUDA(cudaMemsetAsync(m->bslots, 0xff, static_cast<size_t>(m->bhash_size) * sizeof(int), s));
+    if (m->n_blocks > 0)
+    {
+      k_rehash<<<(m->n_blocks + 255) / 256, 256, 0, s>>>(map_view(m), m->n_blocks);
+      VDBG_CUDA(cudaGetLastError());
+    }
     DevStatus clean;
     clear_status(&clean);
     clean.n_leaves = m->n_leaves;
+    clean.n_blocks = m->n_blocks;
     *m->h_status   = clean;
     VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
     VDBG_CUDA(cudaStreamSynchronize(s));

@@ -135,10 +135,11 @@ class OccupancyVDBMapping:
     """vdb_mapping::OccupancyVDBMapping (OccupancyVDBMapping.hpp:46-200) on the GPU."""
 
     def __init__(self, resolution: float, initial_leaf_capacity: int = 0, max_device_bytes: int = 0,
-                 device: int | None = None):
+                 device: int | None = None, initial_block_capacity: int = 0):
         self._lib = _lib.load()
         opts = _lib.vdbg_options()
         opts.initial_leaf_capacity = int(initial_leaf_capacity)
+        opts.initial_block_capacity = int(initial_block_capacity)
         opts.max_device_bytes = int(max_device_bytes)
         if device is None:
             try:
