@@ -2,9 +2,10 @@
 //
 //   k_prep     VDBMapping.hpp:499-519   NaN skip, FP64 length + max-range clip,
 //                                       worldToIndex of the endpoint, L1 length,
-//                                       bucket histogram (rays sorted long-first)
-//   k_scan     (none)                   exclusive scan of the bucket histogram
-//   k_scatter  (none)                   counting-sort scatter of ray ids
+//                                       direction-bin histogram
+//   k_scan     (none)                   exclusive scan of the bin histogram
+//   k_scatter  (none)                   counting-sort scatter of ray ids (rays
+//                                       grouped by direction)
 //   k_dda_mark VDBMapping.hpp:550-566,   FP64 DDA from the sensor voxel to the
 //              :533-536                 endpoint voxel; marks visited and hit
 //                                       bits of the per-leaf update masks
@@ -19,11 +20,45 @@
 
 namespace vdbg {
 
-__device__ __forceinline__ int ray_bucket(uint32_t l1)
+// Sort bin of a ray (voxel offset d from the sensor voxel, L1 length l1):
+// four length classes, longest first, so long rays start early and do not
+// extend the tail; within a class, the cube-map face of the dominant axis and
+// a 13 x 13 cell on it (6 * 169 = 1014 direction cells). Rays of one bin are
+// angular neighbours of similar length; the DDA hands warps short runs of
+// this order so their lanes walk through the same leaves and their leaf
+// records merge. Order only; the map does not depend on it.
+__device__ __forceinline__ int ray_bin(int dx, int dy, int dz, uint32_t l1)
 {
-  const uint32_t b = l1 >> kBucketShift;
-  return kNumBuckets - 1 - static_cast<int>(b < static_cast<uint32_t>(kNumBuckets - 1) ? b : kNumBuckets - 1);
+  const int ax = abs(dx), ay = abs(dy), az = abs(dz);
+  int face, u, v, mx;
+  if (ax >= ay && ax >= az)
+  {
+    face = dx >= 0 ? 0 : 1;
+    u    = dy;
+    v    = dz;
+    mx   = ax;
+  }
+  else if (ay >= az)
+  {
+    face = dy >= 0 ? 2 : 3;
+    u    = dx;
+    v    = dz;
+    mx   = ay;
+  }
+  else
+  {
+    face = dz >= 0 ? 4 : 5;
+    u    = dx;
+    v    = dy;
+    mx   = az;
+  }
+  const int cls = l1 >= 1024u ? 0 : (l1 >= 512u ? 1 : (l1 >= 256u ? 2 : 3));
+  if (mx == 0) return cls * 1014;
+  const int iu = static_cast<int>((static_cast<long long>(u + mx) * 13) / (2 * mx + 1));
+  const int iv = static_cast<int>((static_cast<long long>(v + mx) * 13) / (2 * mx + 1));
+  return cls * 1014 + face * 169 + iv * 13 + iu;
 }
+static_assert(4 * 1014 <= kNumBuckets, "sort bins exceed the histogram");
 
 // One thread per point. rays[i] = (end voxel xyz, meta). Every lane of a
 // warp stays to the end so the warp-wide reductions see a full mask.
@@ -101,7 +136,7 @@ __global__ void __launch_bounds__(256) k_prep(const char* __restrict__ pts, int6
     if (sr) atomicAdd(&st->rays, sr);
     if (sn) atomicAdd(&st->nonfinite, sn);
   }
-  const int b          = valid ? ray_bucket(meta & kMetaL1Mask) : -1;
+  const int b          = valid ? ray_bin(ex - g.ovx, ey - g.ovy, ez - g.ovz, meta & kMetaL1Mask) : -1;
   const unsigned peers = __match_any_sync(0xffffffffu, b);
   if (valid && (__ffs(peers) - 1) == static_cast<int>(threadIdx.x & 31))
   {
@@ -157,13 +192,14 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ hist, uint
   if (t == 1023) st->n_valid = base;
 }
 
-__global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, int64_t n,
+__global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, int64_t n, ScanGeom g,
                                                  uint32_t* __restrict__ cursor, int* __restrict__ order)
 {
   const int64_t i      = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const uint32_t meta  = i < n ? static_cast<uint32_t>(rays[i].w) : 0u;
+  const int4 r         = i < n ? rays[i] : make_int4(0, 0, 0, 0);
+  const uint32_t meta  = static_cast<uint32_t>(r.w);
   const bool valid     = (meta & kMetaValid) != 0;
-  const int b          = valid ? ray_bucket(meta & kMetaL1Mask) : -1;
+  const int b          = valid ? ray_bin(r.x - g.ovx, r.y - g.ovy, r.z - g.ovz, meta & kMetaL1Mask) : -1;
   const unsigned peers = __match_any_sync(0xffffffffu, b);
   const int lane       = static_cast<int>(threadIdx.x & 31);
   const int leader     = __ffs(peers) - 1;
@@ -199,6 +235,7 @@ __global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, 
 constexpr int kDdaWarps = 2;   // warps per block
 constexpr int kDdaRing  = 4;   // leaf records per lane (3 closed + the open one)
 constexpr int kDdaSteps = 24;  // DDA steps between flushes
+constexpr uint32_t kDdaChunk = 16;  // rays a warp takes from the binned order at a time
 // Record meta word: bits 0-7 non-zero word mask, bit 8 hit, bits 9-17 hit voxel offset.
 constexpr uint32_t kRecHit = 1u << 8;
 
@@ -309,6 +346,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
   const uint32_t nv = m.st->n_valid;
 
   bool drained = false;
+  uint32_t chunk_next = 0, chunk_end = 0;  // the warp's current run of rays
   // Per-lane ray state.
   bool has_ray = false, cur_valid = false, clipped = false;
   int vx = 0, vy = 0, vz = 0, sx = 0, sy = 0, sz = 0;
@@ -332,20 +370,33 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
     {
       drained = true;  // a pool or hash overflow forces a second pass; stop early
     }
-    if (!drained)
+    unsigned need = drained ? 0u : __ballot_sync(0xffffffffu, !has_ray);
+    while (need)
     {
-      const unsigned need = __ballot_sync(0xffffffffu, !has_ray);
-      if (need)
+      // Idle lanes take the next rays of the warp's run of the binned order.
+      if (chunk_next >= chunk_end)
       {
-        const int leader = __ffs(need) - 1;
-        uint32_t base    = 0;
-        if (lane == leader) base = atomicAdd(&m.st->ray_cursor, static_cast<uint32_t>(__popc(need)));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (base + static_cast<uint32_t>(__popc(need)) >= nv) drained = true;
-        if (!has_ray)
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&m.st->ray_cursor, kDdaChunk);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= nv)
         {
-          const uint32_t idx = base + static_cast<uint32_t>(__popc(need & lanemask_lt()));
-          if (idx < nv)
+          drained = true;
+          break;
+        }
+        chunk_next = base;
+        chunk_end  = min(base + kDdaChunk, nv);
+      }
+      const uint32_t avail = chunk_end - chunk_next;
+      const uint32_t rank  = static_cast<uint32_t>(__popc(need & lanemask_lt()));
+      const bool take      = ((need >> lane) & 1u) && rank < avail;
+      const uint32_t idx   = chunk_next + rank;
+      const unsigned took  = __ballot_sync(0xffffffffu, take);
+      chunk_next += static_cast<uint32_t>(__popc(took));
+      need &= ~took;
+      {
+        if (take)
+        {
           {
             const int4 r        = rays[order[idx]];
             const uint32_t meta = static_cast<uint32_t>(r.w);

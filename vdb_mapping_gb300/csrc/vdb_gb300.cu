@@ -522,7 +522,7 @@ int launch_raycast(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t
   const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
   k_prep<<<blocks, 256, 0, s>>>(pts, n, stride, g, m->d_rays, m->d_hist, m->d_status);
   k_scan<<<1, 1024, 0, s>>>(m->d_hist, m->d_cursor, m->d_status);
-  k_scatter<<<blocks, 256, 0, s>>>(m->d_rays, n, m->d_cursor, m->d_order);
+  k_scatter<<<blocks, 256, 0, s>>>(m->d_rays, n, g, m->d_cursor, m->d_order);
   VDBG_CUDA(cudaEventRecord(m->ev_prep, s));
   launch_dda(m, n, g, c, s);
   VDBG_CUDA(cudaGetLastError());
@@ -1195,7 +1195,7 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
     const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
     k_prep<<<blocks, 256, 0, s>>>(pts, n, stride, g, d_rays, d_hist, m->d_status);
     k_scan<<<1, 1024, 0, s>>>(d_hist, d_cursor, m->d_status);
-    k_scatter<<<blocks, 256, 0, s>>>(d_rays, n, d_cursor, d_order);
+    k_scatter<<<blocks, 256, 0, s>>>(d_rays, n, g, d_cursor, d_order);
     VDBG_CUDA(cudaEventRecord(m->ev_prep, s));
     const int64_t warps_needed = (n + 31) / 32;
     int64_t dblocks            = (warps_needed + kDdaWarps - 1) / kDdaWarps;
