@@ -56,7 +56,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--points", type=int, default=0,
-                    help="use only the first N points of each scan (small profiling cases)")
+                    help="use an evenly strided subset of N points of each scan (small profiling cases)")
     ap.add_argument("--leaf-capacity", type=int, default=0,
                     help="leaf pool slots reserved up front (default: sized for the workload)")
     return ap.parse_args()
@@ -241,7 +241,8 @@ def run_ours(args):
     n_scans = args.warmup + args.steps
     scans = [wl.scan(k % wl.n_scans) for k in range(n_scans)]
     if args.points:
-        scans = [(p[:args.points].copy(), o) for p, o in scans]
+        # an evenly strided subset keeps the scan's geometry (all elevations)
+        scans = [(np.ascontiguousarray(p[::max(1, p.shape[0] // args.points)][:args.points]), o) for p, o in scans]
     n_pts = scans[0][0].shape[0]
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream

@@ -170,7 +170,9 @@ int vdbg_device_bytes(const vdbg_map* map, int64_t* out);
  * vdbg_insert_point_cloud, but the per-scan scratch lives in one fixed
  * VDBG_NOALLOC_SCRATCH_BYTES device array inside the library (held by every
  * GPU that loads it, until the process exits) instead of buffers the map
- * grows on demand. Limits: n <= VDBG_NOALLOC_MAX_POINTS and, for host input,
+ * grows on demand. It also runs its ray traversal on fewer warps, in as many
+ * passes as the scan needs, so it is slower than the regular call. Limits:
+ * n <= VDBG_NOALLOC_MAX_POINTS and, for host input,
  * stride_bytes <= 16; larger inputs return VDBG_ERR_SIZE_LIMIT. The map's leaf
  * pool is not grown: when it is full the call returns VDBG_ERR_OUT_OF_MEMORY,
  * applies nothing and discards the source's pending update grid, so create
@@ -180,7 +182,9 @@ int vdbg_device_bytes(const vdbg_map* map, int64_t* out);
  * so calls that overlap on the GPU (other threads, other streams, other maps)
  * race: serialise them. */
 #define VDBG_NOALLOC_MAX_POINTS 262144
-#define VDBG_NOALLOC_SCRATCH_BYTES (262144 * (16 + 16 + 4) + 2 * 4096 * 4)
+#define VDBG_NOALLOC_DDA_WARPS 256
+#define VDBG_NOALLOC_RUN_SEGMENT 4096
+#define VDBG_NOALLOC_SCRATCH_BYTES (28u << 20)
 int vdbg_insert_point_cloud_noalloc(vdbg_map* map, const float* xyz, int64_t n, int64_t stride_bytes,
                                     const double origin[3], const char* source_id, uint32_t flags,
                                     void* stream, vdbg_scan_stats* stats);

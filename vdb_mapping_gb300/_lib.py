@@ -12,6 +12,7 @@ from .build import LIB_PATH
 
 VDBG_POINTS_DEVICE = 1
 VDBG_NOALLOC_MAX_POINTS = 262144
+VDBG_NOALLOC_SCRATCH_BYTES = 28 << 20
 
 STATUS = {
     0: "VDBG_OK",

@@ -49,6 +49,7 @@ constexpr uint32_t kErrSpin       = 4u;
 constexpr uint32_t kErrCoordRange = 8u;
 constexpr uint32_t kErrStepBound  = 16u;
 constexpr uint32_t kErrBlockFull  = 32u;
+constexpr uint32_t kErrRunsFull   = 64u;
 
 // Ray record meta word: bits 0-28 L1 length, bit 29 clipped, bit 30 valid.
 constexpr uint32_t kMetaL1Mask   = (1u << 29) - 1;
@@ -72,7 +73,9 @@ struct DevStatus
   unsigned long long nonfinite;
   uint32_t ray_cursor;  // next position in the ray order handed to a DDA warp
   uint32_t n_blocks;    // block bump allocator
-  unsigned long long pad[2];
+  uint32_t inflight;    // lanes that ended a DDA pass with a ray in flight
+  uint32_t pad32;
+  unsigned long long pad[1];
 };
 
 struct LogOdds
@@ -102,6 +105,39 @@ struct MapView
   int4* origin;
   uint32_t capacity;
   DevStatus* st;
+};
+
+// Slab runs of one DDA pass: a run is the set of voxels one ray visits in one
+// x-slab (64 voxels) of one leaf. Warp w of the pass writes its runs to its
+// own segment [w * seg, w * seg + count[w]).
+struct RunBuffer
+{
+  unsigned long long* key;   // leaf key
+  unsigned long long* bits;  // visited voxels of the slab
+  unsigned char* slab;       // x & 7
+  uint32_t* count;           // runs per warp segment
+  uint32_t seg;              // segment capacity (runs)
+  uint32_t warps;            // segments
+};
+
+// DDA state of a lane whose ray was still in flight when its warp's segment
+// filled; the next pass resumes from it.
+struct LaneState
+{
+  long long nx, ny, nz;
+  double dx, dy, dz;
+  unsigned long long run;
+  int vx, vy, vz;
+  int rx, ry, rz;
+  int sx, sy, sz;
+  uint32_t budget;
+  uint32_t flags;  // bit 0: has_ray, bit 1: run_open
+  uint32_t pad;
+};
+
+struct WarpState
+{
+  uint32_t chunk_next, chunk_end, drained, pad;
 };
 
 struct ChannelView

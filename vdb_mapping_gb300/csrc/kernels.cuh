@@ -6,9 +6,12 @@
 //   k_scan     (none)                   exclusive scan of the bin histogram
 //   k_scatter  (none)                   counting-sort scatter of ray ids (rays
 //                                       grouped by direction)
-//   k_dda_mark VDBMapping.hpp:550-566,   FP64 DDA from the sensor voxel to the
-//              :533-536                 endpoint voxel; marks visited and hit
-//                                       bits of the per-leaf update masks
+//   k_dda_mark VDBMapping.hpp:550-566    FP64 DDA from the sensor voxel to the
+//                                       endpoint voxel; writes the visited
+//                                       voxels as slab runs
+//   k_apply_runs VDBMapping.hpp:563     merges the runs, ORs them into the
+//                                       per-leaf update masks
+//   k_mark_hits VDBMapping.hpp:533-536  hit bits of unclipped endpoints
 //   k_compact  (none)                   touched blocks -> flat touched-leaf list
 //   k_sweep    VDBMapping.hpp:731-792 + per touched leaf: FP32 log-odds update,
 //              OccupancyVDBMapping.hpp:92-117  thresholds, clamp, active mask;
@@ -212,7 +215,7 @@ __global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, 
 }
 
 // ---------------------------------------------------------------------------
-// k_dda_mark: warp-cooperative traversal.
+// k_dda_mark: warp-cooperative traversal, writing slab runs.
 //
 // Each lane walks one ray at a time with the FP64 DDA of OpenVDB's
 // DDA<Ray<double>,0> as driven by castRayIntoGrid (eye = origin voxel + 0.5,
@@ -221,29 +224,30 @@ __global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, 
 // per step is the sequential tMax += tDelta of the stepped axis; the step is
 // branch-free so the 32 lanes stay converged.
 //
-// Visits are collected per 8^3 leaf: the bits of the current x-slab of the
-// leaf (64 voxels) live in a register; a slab change ORs them into the lane's
-// current leaf record in shared memory. A leaf change closes the record into
-// the lane's private ring (kDdaRing records). Every kDdaSteps steps the warp
-// flushes all closed records together, one record per lane per round:
-// duplicate leaves in a round are merged, one lane per distinct leaf resolves
-// the slot in the device hash (all lookups of the round in flight at once) and
-// ORs the words into the update masks with fire-and-forget reductions.
-// Rays come from the L1-sorted order (long rays first), handed to idle lanes
-// at each round, so lanes rarely idle while rays remain.
+// A ray is monotone in every axis, so it visits each x-slab of each 8^3 leaf
+// (64 voxels, one mask word) in a single contiguous run. The lane keeps the
+// bits of the current run in a register and appends each finished run to its
+// private ring in shared memory. Every kDdaSteps steps the warp copies all
+// rings to its segment of the run buffer in one coalesced pass; k_apply_runs
+// merges and applies them. Rays come from the length-then-direction order in
+// short runs per warp (ray_bin), so a segment holds runs of neighbouring rays.
+//
+// A pass ends for a warp when its segment cannot take another round: the
+// lanes' DDA state and the warp's ray run are saved and the next pass
+// (resume != 0) continues from them, after k_apply_runs emptied the buffer.
 // ---------------------------------------------------------------------------
-constexpr int kDdaWarps = 2;   // warps per block
-constexpr int kDdaRing  = 4;   // leaf records per lane (3 closed + the open one)
-constexpr int kDdaSteps = 24;  // DDA steps between flushes
-constexpr uint32_t kDdaChunk = 16;  // rays a warp takes from the binned order at a time
-// Record meta word: bits 0-7 non-zero word mask, bit 8 hit, bits 9-17 hit voxel offset.
-constexpr uint32_t kRecHit = 1u << 8;
+constexpr int kDdaWarps      = 2;                // warps per block
+constexpr int kDdaSteps      = 16;               // DDA steps between ring copies
+constexpr int kDdaRing       = kDdaSteps + 1;    // a step closes at most one run, the last one two
+constexpr uint32_t kDdaRound = 32u * kDdaRing;   // most runs a warp writes per round
+constexpr uint32_t kDdaChunk = 16;               // rays a warp takes from the binned order at a time
 
 struct DdaWarpSmem
 {
-  unsigned long long words[kDdaRing][8][32];
-  unsigned long long keys[kDdaRing][32];
-  uint32_t meta[kDdaRing][32];
+  unsigned long long keys[kDdaRing][32];  // leaf key of the run
+  unsigned long long bits[kDdaRing][32];  // visited voxels of the slab
+  unsigned char slab[kDdaRing][32];       // x & 7 of the slab
+  uint32_t incl[32];                      // inclusive prefix of the lanes' run counts
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt()
@@ -253,123 +257,92 @@ __device__ __forceinline__ uint32_t lanemask_lt()
   return m;
 }
 
-// ORs the register slab into the open record.
-__device__ __forceinline__ void dda_put_slab(DdaWarpSmem& q, int lane, int rec, int w, unsigned long long bits,
-                                             uint32_t& nz)
+// Copies the lanes' rings to positions [pos, pos + total) of the run buffer,
+// coalesced (record j of the warp goes to pos + j). Returns total.
+__device__ __forceinline__ uint32_t dda_write_runs(DdaWarpSmem& q, int lane, int n_rec, const RunBuffer& rb,
+                                                   size_t pos)
 {
-  if (w < 0 || bits == 0ull) return;
-  if (nz & (1u << w))
-    q.words[rec][w][lane] |= bits;
-  else
-    q.words[rec][w][lane] = bits;
-  nz |= 1u << w;
-}
-
-// Flushes the closed records [0, n_done) of every lane, round by round.
-// `cbkey`/`cblock` cache the lane's last resolved block across rounds.
-__device__ __forceinline__ void dda_flush(DdaWarpSmem& q, int lane, int n_done, const MapView& m,
-                                          const ChannelView& c, unsigned long long& cbkey, int& cblock)
-{
-  __syncwarp();
-  const int rounds = __reduce_max_sync(0xffffffffu, static_cast<unsigned>(n_done));
-  for (int r = 0; r < rounds; ++r)
+  uint32_t incl = static_cast<uint32_t>(n_rec);
+  for (int off = 1; off < 32; off <<= 1)
   {
-    const bool mine              = r < n_done;
-    const unsigned long long key = mine ? q.keys[r][lane] : kEmptyKey;
-    const uint32_t meta          = mine ? q.meta[r][lane] : 0u;
-    const unsigned peers         = __match_any_sync(0xffffffffu, key);
-    const int leader             = __ffs(peers) - 1;
-    const uint32_t nz            = meta & 0xffu;
-    // Words any record of the group has; the leader clears the ones it lacks
-    // (they hold stale data), then the others OR theirs in.
-    const uint32_t group_nz = __reduce_or_sync(peers, nz);
-    if (mine && leader == lane)
-    {
-      for (uint32_t z = group_nz & ~nz; z; z &= z - 1) q.words[r][__ffs(z) - 1][lane] = 0ull;
-    }
-    __syncwarp();
-    if (mine && leader != lane)
-    {
-      for (uint32_t z = nz; z; z &= z - 1)
-      {
-        const int w = __ffs(z) - 1;
-        atomicOr(&q.words[r][w][leader], q.words[r][w][lane]);
-      }
-    }
-    __syncwarp();
-    int slot = kSlotFailed;
-    if (mine && leader == lane)
-    {
-      const int lx = unpack_leaf_coord(key, 0), ly = unpack_leaf_coord(key, 1), lz = unpack_leaf_coord(key, 2);
-      const unsigned long long bkey = pack_leaf_key(lx >> 3, ly >> 3, lz >> 3);
-      if (bkey != cbkey)
-      {
-        cbkey  = bkey;
-        cblock = find_or_insert_block(m, lx >> 3, ly >> 3, lz >> 3);
-        if (cblock >= 0) touch_block(c, cblock);
-      }
-      if (cblock >= 0)
-      {
-        const int cell = ((lx & 7) << 6) | ((ly & 7) << 3) | (lz & 7);
-        slot           = find_or_insert_leaf(m, cblock, cell, lx, ly, lz);
-        if (slot >= 0)
-        {
-          atomicOr(c.btouched + static_cast<size_t>(cblock) * 8 + (cell >> 6), 1ull << (cell & 63));
-          unsigned long long* u = c.upd + static_cast<size_t>(slot) * 16;
-          for (uint32_t z = group_nz; z; z &= z - 1)
-          {
-            const int w = __ffs(z) - 1;
-            atomicOr(u + w, q.words[r][w][lane]);
-          }
-        }
-      }
-    }
-    slot = __shfl_sync(0xffffffffu, slot, leader);
-    if (mine && slot >= 0 && (meta & kRecHit))
-    {
-      const uint32_t off = (meta >> 9) & 511u;
-      atomicOr(c.upd + static_cast<size_t>(slot) * 16 + 8 + (off >> 6), 1ull << (off & 63));
-    }
-    __syncwarp();
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += y;
   }
+  q.incl[lane]         = incl;
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  __syncwarp();
+  for (uint32_t j = static_cast<uint32_t>(lane); j < total; j += 32)
+  {
+    // Owner lane of record j: the first lane whose inclusive prefix exceeds j.
+    int lo = 0, hi = 31;
+    while (lo < hi)
+    {
+      const int mid = (lo + hi) >> 1;
+      if (q.incl[mid] > j)
+        hi = mid;
+      else
+        lo = mid + 1;
+    }
+    const uint32_t r    = j - (lo > 0 ? q.incl[lo - 1] : 0u);
+    rb.key[pos + j]     = q.keys[r][lo];
+    rb.bits[pos + j]    = q.bits[r][lo];
+    rb.slab[pos + j]    = q.slab[r][lo];
+  }
+  __syncwarp();
+  return total;
 }
 
 __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __restrict__ rays,
                                                                const int* __restrict__ order, ScanGeom g,
-                                                               MapView m, ChannelView c)
+                                                               MapView m, RunBuffer rb,
+                                                               LaneState* __restrict__ lstate,
+                                                               WarpState* __restrict__ wstate, int resume)
 {
   __shared__ DdaWarpSmem smem[kDdaWarps];
-  const int lane = static_cast<int>(threadIdx.x & 31);
-  // Warp-uniform early exit: other warps may set the error word meanwhile.
-  if (__shfl_sync(0xffffffffu, ld_relaxed_u32(&m.st->error), 0) != 0u) return;
+  const int lane    = static_cast<int>(threadIdx.x & 31);
+  const uint32_t gw = blockIdx.x * kDdaWarps + (threadIdx.x >> 5);
   DdaWarpSmem& q    = smem[threadIdx.x >> 5];
   const uint32_t nv = m.st->n_valid;
+  const size_t seg0 = static_cast<size_t>(gw) * rb.seg;
+  uint32_t count    = 0;  // runs this warp wrote in this pass
 
-  bool drained = false;
+  bool drained        = false;
   uint32_t chunk_next = 0, chunk_end = 0;  // the warp's current run of rays
   // Per-lane ray state.
-  bool has_ray = false, cur_valid = false, clipped = false;
+  bool has_ray = false, run_open = false;
   int vx = 0, vy = 0, vz = 0, sx = 0, sy = 0, sz = 0;
   long long nx = 0, ny = 0, nz = 0;
   double dx = 0.0, dy = 0.0, dz = 0.0;
-  int clx = 0, cly = 0, clz = 0;
-  int cur_w = -1;
-  unsigned long long slab = 0ull;
-  uint32_t rec_nz = 0;  // non-zero words of the open record
-  int n_done = 0;       // closed records in the ring; the open one is at index n_done
-  uint32_t hit_off = 0, budget = 0;
-  unsigned long long cbkey = kEmptyKey;  // last block resolved by this lane
-  int cblock               = kSlotFailed;
+  int rx = 0, ry = 0, rz = 0;  // current run: exact x, leaf y, leaf z
+  unsigned long long run = 0ull;
+  int n_rec       = 0;
+  uint32_t budget = 0;
+  if (resume)
+  {
+    const WarpState w = wstate[gw];
+    chunk_next        = w.chunk_next;
+    chunk_end         = w.chunk_end;
+    drained           = w.drained != 0u;
+    const LaneState l = lstate[gw * 32 + lane];
+    has_ray           = (l.flags & 1u) != 0u;
+    run_open          = (l.flags & 2u) != 0u;
+    nx = l.nx; ny = l.ny; nz = l.nz;
+    dx = l.dx; dy = l.dy; dz = l.dz;
+    run = l.run;
+    vx = l.vx; vy = l.vy; vz = l.vz;
+    rx = l.rx; ry = l.ry; rz = l.rz;
+    sx = l.sx; sy = l.sy; sz = l.sz;
+    budget = l.budget;
+  }
   const long long kOne = __double_as_longlong(1.0);
   const long long kMax = __double_as_longlong(1.7976931348623157e308);
+  bool paused          = false;
 
   for (;;)
   {
     // ---- hand out rays to idle lanes ------------------------------------------
-    if (!drained && __shfl_sync(0xffffffffu, ld_relaxed_u32(&m.st->error), 0) != 0u)
-    {
-      drained = true;  // a pool or hash overflow forces a second pass; stop early
-    }
+    // (The traversal allocates nothing, so it ignores the error word: pool
+    // overflows come from k_apply_runs and k_mark_hits, which the host re-runs.)
     unsigned need = drained ? 0u : __ballot_sync(0xffffffffu, !has_ray);
     while (need)
     {
@@ -394,114 +367,87 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
       const unsigned took  = __ballot_sync(0xffffffffu, take);
       chunk_next += static_cast<uint32_t>(__popc(took));
       need &= ~took;
+      if (take)
       {
-        if (take)
+        const int4 r      = rays[order[idx]];
+        const uint32_t l1 = static_cast<uint32_t>(r.w) & kMetaL1Mask;
+        if (l1 > 0)
         {
+          // (An endpoint in the sensor voxel is only a hit; k_mark_hits does it.)
+          const int o[3] = {g.ovx, g.ovy, g.ovz};
+          const int e[3] = {r.x, r.y, r.z};
+          int vox[3], stp[3];
+          long long nxt[3];
+          double dlt[3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
           {
-            const int4 r        = rays[order[idx]];
-            const uint32_t meta = static_cast<uint32_t>(r.w);
-            const uint32_t l1   = meta & kMetaL1Mask;
-            clipped             = (meta & kMetaClipped) != 0;
-            hit_off = (static_cast<uint32_t>(r.x & 7) << 6) | (static_cast<uint32_t>(r.y & 7) << 3) |
-                      static_cast<uint32_t>(r.z & 7);
-            if (l1 == 0)
+            const double eye = __dadd_rn(static_cast<double>(o[a]), 0.5);
+            const double dir = __dsub_rn(static_cast<double>(e[a]), static_cast<double>(o[a]));
+            const double pos = __dadd_rn(eye, __dmul_rn(dir, 0.0));
+            vox[a]           = static_cast<int>(floor(pos));
+            if (dir == 0.0)
             {
-              // castRayIntoGrid marks nothing; an unclipped endpoint is still a hit.
-              if (!clipped)
-              {
-                q.keys[n_done][lane] = pack_leaf_key(r.x >> 3, r.y >> 3, r.z >> 3);
-                q.meta[n_done][lane] = kRecHit | (hit_off << 9);
-                ++n_done;
-              }
+              stp[a] = 0;
+              nxt[a] = kMax;
+              dlt[a] = 1.7976931348623157e308;
             }
             else
             {
-              const int o[3] = {g.ovx, g.ovy, g.ovz};
-              const int e[3] = {r.x, r.y, r.z};
-              int vox[3], stp[3];
-              long long nxt[3];
-              double dlt[3];
-#pragma unroll
-              for (int a = 0; a < 3; ++a)
+              const double inv = __ddiv_rn(1.0, dir);
+              if (inv > 0.0)
               {
-                const double eye = __dadd_rn(static_cast<double>(o[a]), 0.5);
-                const double dir = __dsub_rn(static_cast<double>(e[a]), static_cast<double>(o[a]));
-                const double pos = __dadd_rn(eye, __dmul_rn(dir, 0.0));
-                vox[a]           = static_cast<int>(floor(pos));
-                if (dir == 0.0)
-                {
-                  stp[a] = 0;
-                  nxt[a] = kMax;
-                  dlt[a] = 1.7976931348623157e308;
-                }
-                else
-                {
-                  const double inv = __ddiv_rn(1.0, dir);
-                  if (inv > 0.0)
-                  {
-                    stp[a] = 1;
-                    nxt[a] = __double_as_longlong(
-                      __dadd_rn(0.0, __dmul_rn(__dsub_rn(static_cast<double>(vox[a] + 1), pos), inv)));
-                  }
-                  else
-                  {
-                    stp[a] = -1;
-                    nxt[a] = __double_as_longlong(
-                      __dadd_rn(0.0, __dmul_rn(__dsub_rn(static_cast<double>(vox[a]), pos), inv)));
-                  }
-                  dlt[a] = __dmul_rn(static_cast<double>(stp[a]), inv);
-                }
+                stp[a] = 1;
+                nxt[a] = __double_as_longlong(
+                  __dadd_rn(0.0, __dmul_rn(__dsub_rn(static_cast<double>(vox[a] + 1), pos), inv)));
               }
-              vx = vox[0]; vy = vox[1]; vz = vox[2];
-              sx = stp[0]; sy = stp[1]; sz = stp[2];
-              nx = nxt[0]; ny = nxt[1]; nz = nxt[2];
-              dx = dlt[0]; dy = dlt[1]; dz = dlt[2];
-              budget    = l1 + 1;
-              has_ray   = true;
-              cur_valid = false;
+              else
+              {
+                stp[a] = -1;
+                nxt[a] = __double_as_longlong(
+                  __dadd_rn(0.0, __dmul_rn(__dsub_rn(static_cast<double>(vox[a]), pos), inv)));
+              }
+              dlt[a] = __dmul_rn(static_cast<double>(stp[a]), inv);
             }
           }
+          vx = vox[0]; vy = vox[1]; vz = vox[2];
+          sx = stp[0]; sy = stp[1]; sz = stp[2];
+          nx = nxt[0]; ny = nxt[1]; nz = nxt[2];
+          dx = dlt[0]; dy = dlt[1]; dz = dlt[2];
+          budget   = l1 + 1;
+          has_ray  = true;
+          run_open = false;
         }
       }
     }
-    const bool any_ray = __ballot_sync(0xffffffffu, has_ray) != 0u;
-    if (!any_ray && drained && __ballot_sync(0xffffffffu, n_done > 0) == 0u) break;
+    if (__ballot_sync(0xffffffffu, has_ray) == 0u && drained) break;
+    if (count + kDdaRound > rb.seg)
+    {
+      paused = true;  // the segment cannot take another round
+      break;
+    }
 
     // ---- DDA steps (no warp votes inside) --------------------------------------
-    if (any_ray)
+#pragma unroll 4
+    for (int s = 0; s < kDdaSteps; ++s)
     {
-#pragma unroll 2
-      for (int s = 0; s < kDdaSteps; ++s)
+      if (has_ray)
       {
-        if (!has_ray) continue;
-        // setActiveState(voxel) on the update grid, leaf by leaf.
-        const int lx = vx >> 3, ly = vy >> 3, lz = vz >> 3;
-        if (!cur_valid || lx != clx || ly != cly || lz != clz)
+        // setActiveState(voxel) on the update grid, one slab run at a time.
+        const int ly = vy >> 3, lz = vz >> 3;
+        if (run_open && (vx != rx || ly != ry || lz != rz))
         {
-          if (cur_valid)
-          {
-            if (n_done == kDdaRing - 1) continue;  // ring full: wait for the flush
-            dda_put_slab(q, lane, n_done, cur_w, slab, rec_nz);
-            q.meta[n_done][lane] = rec_nz;
-            ++n_done;
-          }
-          clx                  = lx;
-          cly                  = ly;
-          clz                  = lz;
-          q.keys[n_done][lane] = pack_leaf_key(lx, ly, lz);
-          cur_valid            = true;
-          rec_nz               = 0u;
-          cur_w                = -1;
-          slab                 = 0ull;
+          q.keys[n_rec][lane] = pack_leaf_key(rx >> 3, ry, rz);
+          q.bits[n_rec][lane] = run;
+          q.slab[n_rec][lane] = static_cast<unsigned char>(rx & 7);
+          ++n_rec;
+          run = 0ull;
         }
-        const int w = vx & 7;
-        if (w != cur_w)
-        {
-          dda_put_slab(q, lane, n_done, cur_w, slab, rec_nz);
-          cur_w = w;
-          slab  = 0ull;
-        }
-        slab |= 1ull << (((vy & 7) << 3) | (vz & 7));
+        rx       = vx;
+        ry       = ly;
+        rz       = lz;
+        run_open = true;
+        run |= 1ull << (((vy & 7) << 3) | (vz & 7));
         // DDA::step(): argmin of tMax (ties to the higher axis), branch-free.
         const bool ax      = (nx < ny) && (nx < nz);
         const bool ay      = !ax && (ny < nz);
@@ -524,30 +470,197 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
         }
         if (fin)
         {
-          // The last marked voxel is the endpoint: its record carries the hit.
-          dda_put_slab(q, lane, n_done, cur_w, slab, rec_nz);
-          q.meta[n_done][lane] = rec_nz | (clipped ? 0u : (kRecHit | (hit_off << 9)));
-          ++n_done;
-          has_ray   = false;
-          cur_valid = false;
+          q.keys[n_rec][lane] = pack_leaf_key(rx >> 3, ry, rz);
+          q.bits[n_rec][lane] = run;
+          q.slab[n_rec][lane] = static_cast<unsigned char>(rx & 7);
+          ++n_rec;
+          run      = 0ull;
+          run_open = false;
+          has_ray  = false;
         }
       }
     }
 
-    // ---- flush the closed records; the open one moves to the ring start -------
-    dda_flush(q, lane, n_done, m, c, cbkey, cblock);
-    if (n_done > 0 && cur_valid)
+    // ---- copy the rings to the warp's segment ------------------------------------
+    __syncwarp();
+    count += dda_write_runs(q, lane, n_rec, rb, seg0 + count);
+    n_rec = 0;
+  }
+
+  // ---- end of the pass: record the segment and what is left in flight ------------
+  if (lane == 0)
+  {
+    rb.count[gw] = count;
+    WarpState w;
+    w.chunk_next = chunk_next;
+    w.chunk_end  = chunk_end;
+    w.drained    = drained ? 1u : 0u;
+    w.pad        = 0u;
+    wstate[gw]   = w;
+  }
+  const unsigned live = __ballot_sync(0xffffffffu, has_ray);
+  if (lane == 0 && paused)
+  {
+    const uint32_t left = static_cast<uint32_t>(__popc(live)) + (chunk_end > chunk_next ? chunk_end - chunk_next : 0u);
+    if (left) atomicAdd(&m.st->inflight, left);
+  }
+  LaneState l;
+  l.nx = nx; l.ny = ny; l.nz = nz;
+  l.dx = dx; l.dy = dy; l.dz = dz;
+  l.run = run;
+  l.vx = vx; l.vy = vy; l.vz = vz;
+  l.rx = rx; l.ry = ry; l.rz = rz;
+  l.sx = sx; l.sy = sy; l.sz = sz;
+  l.budget = budget;
+  l.flags  = (has_ray ? 1u : 0u) | (run_open ? 2u : 0u);
+  l.pad    = 0u;
+  lstate[gw * 32 + lane] = l;
+}
+
+// ---------------------------------------------------------------------------
+// k_apply_runs: merges the scan's slab runs and ORs them into the update masks.
+//
+// Persistent blocks take chunks of kApplyChunk runs (written together by
+// warps walking neighbouring rays, so a chunk repeats few leaves). Each thread
+// ORs its runs into the block's leaf table in shared memory; the block then
+// drains the table: one thread per distinct leaf resolves its slot through the
+// block index (allocating leaves and blocks as needed), marks it touched and
+// ORs the non-zero words into the update masks. A run that finds the table
+// full is applied directly.
+// ---------------------------------------------------------------------------
+constexpr int kApplyThreads = 256;
+constexpr int kApplyChunk   = 1024;
+constexpr int kApplyTable   = 512;  // 2^9 entries, see apply_hash
+
+struct ApplySmem
+{
+  unsigned long long key[kApplyTable];
+  unsigned int words[kApplyTable][16];  // 8 mask words as lo/hi halves
+  unsigned int count;
+};
+
+__device__ __forceinline__ uint32_t apply_hash(unsigned long long key)
+{
+  return static_cast<uint32_t>((key * 0x9E3779B97F4A7C15ull) >> 55);
+}
+
+// Slab of leaf `key` in the update masks: resolves (and allocates) the leaf
+// and marks it touched in its block. Returns the leaf slot or kSlotFailed.
+__device__ __forceinline__ int apply_resolve(const MapView& m, const ChannelView& c, unsigned long long key)
+{
+  const int lx = unpack_leaf_coord(key, 0), ly = unpack_leaf_coord(key, 1), lz = unpack_leaf_coord(key, 2);
+  const int b  = find_or_insert_block(m, lx >> 3, ly >> 3, lz >> 3);
+  if (b < 0) return kSlotFailed;
+  touch_block(c, b);
+  const int cell = ((lx & 7) << 6) | ((ly & 7) << 3) | (lz & 7);
+  const int slot = find_or_insert_leaf(m, b, cell, lx, ly, lz);
+  if (slot >= 0) atomicOr(c.btouched + static_cast<size_t>(b) * 8 + (cell >> 6), 1ull << (cell & 63));
+  return slot;
+}
+
+__global__ void __launch_bounds__(kApplyThreads, 4) k_apply_runs(RunBuffer rb, MapView m, ChannelView c)
+{
+  __shared__ ApplySmem t;
+  if (ld_relaxed_u32(&m.st->error) != 0u) return;
+  for (int e = threadIdx.x; e < kApplyTable; e += kApplyThreads)
+  {
+    t.key[e] = kEmptyKey;
+#pragma unroll
+    for (int w = 0; w < 16; ++w) t.words[e][w] = 0u;
+  }
+  __syncthreads();
+  // Work items: (segment, chunk of kApplyChunk runs), segment-major.
+  const uint32_t chunks_per_seg = (rb.seg + kApplyChunk - 1) / kApplyChunk;
+  const uint32_t items          = rb.warps * chunks_per_seg;
+  for (uint32_t item = blockIdx.x; item < items; item += gridDim.x)
+  {
+    const uint32_t sg    = item / chunks_per_seg;
+    const uint32_t start = (item % chunks_per_seg) * kApplyChunk;
+    const uint32_t cnt   = rb.count[sg];
+    if (start >= cnt) continue;  // uniform across the block
+    const size_t base  = static_cast<size_t>(sg) * rb.seg;
+    const uint32_t end = min(start + kApplyChunk, cnt);
+    for (uint32_t i = start + threadIdx.x; i < end; i += kApplyThreads)
     {
-      q.keys[0][lane] = q.keys[n_done][lane];
-      for (uint32_t z = rec_nz; z; z &= z - 1)
+      const unsigned long long key  = rb.key[base + i];
+      const unsigned long long bits = rb.bits[base + i];
+      const int w                   = rb.slab[base + i];
+      uint32_t h                    = apply_hash(key);
+      bool done                     = false;
+      for (int probe = 0; probe < 16 && !done; ++probe)
       {
-        const int w      = __ffs(z) - 1;
-        q.words[0][w][lane] = q.words[n_done][w][lane];
+        unsigned long long k = t.key[h];
+        if (k == kEmptyKey)
+        {
+          const unsigned long long prev = atomicCAS(&t.key[h], kEmptyKey, key);
+          k                             = (prev == kEmptyKey) ? key : prev;
+        }
+        if (k == key)
+        {
+          const unsigned int lo = static_cast<unsigned int>(bits), hi = static_cast<unsigned int>(bits >> 32);
+          if (lo) atomicOr(&t.words[h][2 * w], lo);
+          if (hi) atomicOr(&t.words[h][2 * w + 1], hi);
+          done = true;
+        }
+        h = (h + 1) & (kApplyTable - 1);
+      }
+      if (!done)
+      {
+        // Table crowded: apply this run directly.
+        const int slot = apply_resolve(m, c, key);
+        if (slot >= 0) atomicOr(c.upd + static_cast<size_t>(slot) * 16 + w, bits);
       }
     }
-    n_done = 0;
-    __syncwarp();
+    __syncthreads();
+    for (int e = threadIdx.x; e < kApplyTable; e += kApplyThreads)
+    {
+      const unsigned long long key = t.key[e];
+      if (key == kEmptyKey) continue;
+      const int slot = apply_resolve(m, c, key);
+      if (slot >= 0)
+      {
+        unsigned long long* u = c.upd + static_cast<size_t>(slot) * 16;
+#pragma unroll
+        for (int w = 0; w < 8; ++w)
+        {
+          const unsigned long long b =
+            (static_cast<unsigned long long>(t.words[e][2 * w + 1]) << 32) | t.words[e][2 * w];
+          if (b) atomicOr(u + w, b);
+        }
+      }
+      t.key[e] = kEmptyKey;
+#pragma unroll
+      for (int w = 0; w < 16; ++w) t.words[e][w] = 0u;
+    }
+    __syncthreads();
   }
+}
+
+// Endpoint hits (setValueOn(end, true), VDBMapping.hpp:533-536): one thread
+// per unclipped ray ORs the hit bit of its end voxel, creating the leaf when
+// the DDA did not visit it (an endpoint in the sensor voxel).
+__global__ void __launch_bounds__(256) k_mark_hits(const int4* __restrict__ rays, const int* __restrict__ order,
+                                                   MapView m, ChannelView c)
+{
+  if (ld_relaxed_u32(&m.st->error) != 0u) return;
+  const uint32_t nv = m.st->n_valid;
+  const uint32_t j  = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nv) return;
+  const int4 r        = rays[order[j]];
+  const uint32_t meta = static_cast<uint32_t>(r.w);
+  if (meta & kMetaClipped) return;
+  const int lx = r.x >> 3, ly = r.y >> 3, lz = r.z >> 3;
+  const int b  = find_or_insert_block(m, lx >> 3, ly >> 3, lz >> 3);
+  if (b < 0) return;
+  touch_block(c, b);
+  const int cell = ((lx & 7) << 6) | ((ly & 7) << 3) | (lz & 7);
+  const int slot = find_or_insert_leaf(m, b, cell, lx, ly, lz);
+  if (slot < 0) return;
+  unsigned long long* bt = c.btouched + static_cast<size_t>(b) * 8 + (cell >> 6);
+  if (!((*bt >> (cell & 63)) & 1ull)) atomicOr(bt, 1ull << (cell & 63));
+  const uint32_t off = (static_cast<uint32_t>(r.x & 7) << 6) | (static_cast<uint32_t>(r.y & 7) << 3) |
+                       static_cast<uint32_t>(r.z & 7);
+  atomicOr(c.upd + static_cast<size_t>(slot) * 16 + 8 + (off >> 6), 1ull << (off & 63));
 }
 
 // Persistent sweep over the touched leaves: 8 lanes per leaf, lane w owning

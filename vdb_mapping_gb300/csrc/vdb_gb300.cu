@@ -86,6 +86,16 @@ struct vdbg_map
   size_t ray_cap        = 0;
   uint32_t* d_hist      = nullptr;
   uint32_t* d_cursor    = nullptr;
+  // DDA run buffer (one segment per DDA warp) and resumable lane/warp state.
+  uint32_t dda_warps    = 0;
+  uint32_t run_seg      = 0;
+  unsigned long long* run_key  = nullptr;
+  unsigned long long* run_bits = nullptr;
+  unsigned char* run_slab      = nullptr;
+  uint32_t* run_count   = nullptr;
+  LaneState* lstate     = nullptr;
+  WarpState* wstate     = nullptr;
+  uint32_t passes_last  = 0;
 
   int64_t bytes         = 0;
   int num_sms           = 152;
@@ -108,6 +118,8 @@ constexpr uint32_t kDefaultCapacity = 1u << 16;
 constexpr uint32_t kMinBlocks       = 1u << 10;
 constexpr int kSweepBlocks          = 152 * 8;
 constexpr int kSweepThreads         = 256;
+constexpr uint32_t kMinRunSeg       = 2048;   // runs per DDA warp segment, at least
+constexpr uint32_t kMaxRunBytes     = 2u << 30;  // run buffer growth budget
 
 uint32_t next_pow2(uint64_t v)
 {
@@ -478,19 +490,12 @@ void record_timings(vdbg_map* m)
 
 // Marks one cloud into channel `c` (VDBMapping.hpp:466-539). Kernels are
 // queued on `s`; the caller fetches the status.
-void launch_dda(vdbg_map* m, int64_t n, const ScanGeom& g, const Channel& c, cudaStream_t s)
-{
-  // Persistent warps; every warp pulls rays until the order is drained.
-  const int64_t warps_needed = (n + 31) / 32;
-  int64_t blocks             = (warps_needed + kDdaWarps - 1) / kDdaWarps;
-  blocks                     = std::min<int64_t>(blocks, static_cast<int64_t>(m->num_sms) * 10);
-  k_dda_mark<<<static_cast<unsigned>(std::max<int64_t>(blocks, 1)), kDdaWarps * 32, 0, s>>>(
-    m->d_rays, m->d_order, g, map_view(m), channel_view(c));
-}
-
-int launch_raycast(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t stride,
-                   const double origin[3], double range, uint32_t flags, cudaStream_t s, bool* queued,
-                   ScanGeom* geom_out)
+// Queues the per-point stage of raycastPointCloud (VDBMapping.hpp:499-519):
+// clip, quantise, sort rays into the DDA order. `queued` is false when there
+// is nothing to cast (empty cloud, NaN origin).
+int launch_prep(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t stride, const double origin[3],
+                double range, uint32_t flags, cudaStream_t s, char* pts_scratch, int4* rays, int* order,
+                uint32_t* hist, uint32_t* cursor, bool* queued, ScanGeom* geom_out)
 {
   *queued = false;
   if (n <= 0) return VDBG_OK;
@@ -509,29 +514,144 @@ int launch_raycast(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t
   g.ovy = ov[1];
   g.ovz = ov[2];
   g.pad = 0;
-
-  const bool host_input = (flags & VDBG_POINTS_DEVICE) == 0;
-  VDBG_TRY(ensure_scratch(m, n, stride, host_input));
   const char* pts = reinterpret_cast<const char*>(xyz);
-  if (host_input)
+  if ((flags & VDBG_POINTS_DEVICE) == 0)
   {
-    VDBG_CUDA(cudaMemcpyAsync(m->d_pts, xyz, static_cast<size_t>(n) * static_cast<size_t>(stride),
+    VDBG_CUDA(cudaMemcpyAsync(pts_scratch, xyz, static_cast<size_t>(n) * static_cast<size_t>(stride),
                               cudaMemcpyHostToDevice, s));
-    pts = m->d_pts;
+    pts = pts_scratch;
   }
   const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
-  k_prep<<<blocks, 256, 0, s>>>(pts, n, stride, g, m->d_rays, m->d_hist, m->d_status);
-  k_scan<<<1, 1024, 0, s>>>(m->d_hist, m->d_cursor, m->d_status);
-  k_scatter<<<blocks, 256, 0, s>>>(m->d_rays, n, g, m->d_cursor, m->d_order);
-  VDBG_CUDA(cudaEventRecord(m->ev_prep, s));
-  launch_dda(m, n, g, c, s);
+  k_prep<<<blocks, 256, 0, s>>>(pts, n, stride, g, rays, hist, m->d_status);
+  k_scan<<<1, 1024, 0, s>>>(hist, cursor, m->d_status);
+  k_scatter<<<blocks, 256, 0, s>>>(rays, n, g, cursor, order);
   VDBG_CUDA(cudaGetLastError());
-  VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
+  VDBG_CUDA(cudaEventRecord(m->ev_prep, s));
   m->timed_prep = true;
-  m->timings.launches += 4;
-  c.pending  = true;
-  *queued    = true;
-  *geom_out  = g;
+  m->timings.launches += 3;
+  c.pending = true;
+  *queued   = true;
+  *geom_out = g;
+  return VDBG_OK;
+}
+
+// Allocates (or grows) the DDA run buffer: dda_warps segments of `seg` runs,
+// plus the per-lane and per-warp resume state.
+int ensure_runs(vdbg_map* m, uint32_t seg)
+{
+  if (m->run_key && seg <= m->run_seg) return VDBG_OK;
+  const size_t W = m->dda_warps;
+  dev_free(m, m->run_key, W * m->run_seg);
+  dev_free(m, m->run_bits, W * m->run_seg);
+  dev_free(m, m->run_slab, W * m->run_seg);
+  m->run_seg = 0;
+  VDBG_TRY(dev_alloc(m, &m->run_key, W * seg));
+  VDBG_TRY(dev_alloc(m, &m->run_bits, W * seg));
+  VDBG_TRY(dev_alloc(m, &m->run_slab, W * seg));
+  if (!m->run_count) VDBG_TRY(dev_alloc(m, &m->run_count, W));
+  if (!m->lstate) VDBG_TRY(dev_alloc(m, &m->lstate, W * 32));
+  if (!m->wstate) VDBG_TRY(dev_alloc(m, &m->wstate, W));
+  m->run_seg = seg;
+  return VDBG_OK;
+}
+
+RunBuffer run_buffer(unsigned long long* key, unsigned long long* bits, unsigned char* slab, uint32_t* count,
+                     uint32_t seg, uint32_t warps)
+{
+  RunBuffer rb;
+  rb.key   = key;
+  rb.bits  = bits;
+  rb.slab  = slab;
+  rb.count = count;
+  rb.seg   = seg;
+  rb.warps = warps;
+  return rb;
+}
+
+void clear_error_keep_counters(vdbg_map* m)
+{
+  m->h_status->error    = 0;
+  m->h_status->n_leaves = m->n_leaves;
+  m->h_status->n_blocks = m->n_blocks;
+}
+
+int map_error(uint32_t err);
+int grow_for(vdbg_map* m, uint64_t requested);
+int grow_blocks_for(vdbg_map* m, uint64_t requested);
+int rebuild_hash(vdbg_map* m, uint32_t hsize, uint32_t n);
+
+// castRayIntoGrid for every ray (VDBMapping.hpp:550-566) and the endpoint
+// hits (VDBMapping.hpp:533-536), into channel `c`: endpoint hits once, then
+// DDA passes, each followed by k_apply_runs, until no ray is left in flight.
+// One status fetch per pass. When the leaf or block pool runs out the pools
+// grow (if `may_grow`) and the hits and the pass's runs are applied again
+// (both idempotent); otherwise the call fails with OUT_OF_MEMORY.
+int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, int64_t n, const ScanGeom& g,
+                   const RunBuffer& rb, LaneState* ls, WarpState* ws, bool may_grow, cudaStream_t s)
+{
+  const unsigned hit_blocks   = static_cast<unsigned>((n + 255) / 256);
+  const unsigned apply_blocks = static_cast<unsigned>(m->num_sms) * 8;
+  k_mark_hits<<<hit_blocks, 256, 0, s>>>(rays, order, map_view(m), channel_view(c));
+  m->timings.launches += 1;
+  uint32_t passes = 0;
+  for (;;)
+  {
+    VDBG_CUDA(cudaMemsetAsync(&m->d_status->inflight, 0, sizeof(uint32_t), s));
+    k_dda_mark<<<rb.warps / kDdaWarps, kDdaWarps * 32, 0, s>>>(rays, order, g, map_view(m), rb, ls, ws,
+                                                              passes > 0 ? 1 : 0);
+    k_apply_runs<<<apply_blocks, kApplyThreads, 0, s>>>(rb, map_view(m), channel_view(c));
+    VDBG_CUDA(cudaGetLastError());
+    m->timings.launches += 2;
+    ++passes;
+    VDBG_TRY(fetch_status(m, s));
+    for (int attempt = 0; m->h_status->error != 0u; ++attempt)
+    {
+      const uint32_t err = m->h_status->error;
+      m->n_leaves        = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
+      m->n_blocks        = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
+      if (err & kErrCoordRange)
+      {
+        // Nothing of the cloud was cast (the prep stage flagged it).
+        clear_error_keep_counters(m);
+        VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+        VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
+        VDBG_CUDA(cudaStreamSynchronize(s));
+        m->passes_last = passes;
+        return VDBG_ERR_COORD_RANGE;
+      }
+      if (err & (kErrSpin | kErrStepBound)) return map_error(err);
+      if (!may_grow || attempt >= 40) return VDBG_ERR_OUT_OF_MEMORY;
+      // A pool or the block hash ran out: grow what ran out, let the failed
+      // leaf cells be allocated again, apply the hits and this pass's runs again.
+      if (err & kErrPoolFull) VDBG_TRY(grow_for(m, m->h_status->n_leaves));
+      if (err & kErrBlockFull) VDBG_TRY(grow_blocks_for(m, m->h_status->n_blocks));
+      if ((err & kErrHashFull) && !(err & kErrBlockFull))
+        VDBG_TRY(rebuild_hash(m, m->bhash_size * 2, m->n_blocks));
+      if (m->n_blocks > 0)
+      {
+        k_reset_failed_leaves<<<m->num_sms * 4, 256, 0, m->stream>>>(m->bleaf,
+                                                                     static_cast<size_t>(m->n_blocks) * 512);
+        VDBG_CUDA(cudaGetLastError());
+      }
+      VDBG_CUDA(cudaStreamSynchronize(m->stream));
+      clear_error_keep_counters(m);
+      VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+      k_mark_hits<<<hit_blocks, 256, 0, s>>>(rays, order, map_view(m), channel_view(c));
+      k_apply_runs<<<apply_blocks, kApplyThreads, 0, s>>>(rb, map_view(m), channel_view(c));
+      VDBG_CUDA(cudaGetLastError());
+      m->timings.launches += 2;
+      m->timings.retries += 1;
+      VDBG_TRY(fetch_status(m, s));
+    }
+    m->n_leaves = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
+    m->n_blocks = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
+    if (m->h_status->inflight == 0u && m->h_status->ray_cursor >= m->h_status->n_valid) break;
+    // Every pass completes at least one round per warp, so this bound is
+    // never reached by a working device; it turns a logic error into a status.
+    if (passes > (1u << 20)) return VDBG_ERR_TIMEOUT;
+  }
+  VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
+  m->passes_last = passes;
   return VDBG_OK;
 }
 
@@ -616,24 +736,49 @@ bool bad_points(const float* xyz, int64_t n, int64_t stride)
   return false;
 }
 
-// accumulate (optional) + integration of the listed channels, one status
-// fetch at the end in the common case. Pool or hash exhaustion is handled by
-// growing and marking the cloud again: marking is idempotent (bits are only
-// OR-ed in, a leaf already on the touched list is not added twice) and the
-// sweeps are skipped on the device while an error is set. A voxel index out
-// of range skips the whole cloud (nothing of it is marked) and the other
-// pending update grids are still integrated.
+// accumulate (optional) + integration of the listed channels. The marking
+// fetches the status once per DDA pass (normally one); pool and hash
+// exhaustion are handled inside run_dda_passes. A voxel index out of range
+// skips the whole cloud (nothing of it is marked) and the other pending
+// update grids are still integrated.
 int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t stride,
                              const double origin[3], Channel* src, double range, uint32_t flags,
                              cudaStream_t s, bool integrate_all, Channel* only, vdbg_scan_stats* stats)
 {
   VDBG_TRY(begin_call(m, s));
   const uint32_t leaves_before = m->n_leaves;
-  bool queued                  = false;
-  ScanGeom g{};
-  if (src)
+  int call_status              = VDBG_OK;
+  if (src && n > 0)
   {
-    VDBG_TRY(launch_raycast(m, *src, xyz, n, stride, origin, range, flags, s, &queued, &g));
+    const bool host_input = (flags & VDBG_POINTS_DEVICE) == 0;
+    VDBG_TRY(ensure_scratch(m, n, stride, host_input));
+    // One pass for a scan like the last one: segments sized from the previous
+    // call's pass count (bounded by the run-buffer budget).
+    uint32_t seg = std::max<uint32_t>(m->run_seg, kMinRunSeg);
+    if (m->passes_last > 1)
+    {
+      const uint64_t want  = static_cast<uint64_t>(m->run_seg) * m->passes_last * 5 / 4;
+      const uint64_t limit = kMaxRunBytes / (17ull * m->dda_warps);
+      seg                  = static_cast<uint32_t>(std::min<uint64_t>(want, limit));
+    }
+    VDBG_TRY(ensure_runs(m, seg));
+    bool queued = false;
+    ScanGeom g{};
+    const int r = launch_prep(m, *src, xyz, n, stride, origin, range, flags, s, m->d_pts, m->d_rays, m->d_order,
+                              m->d_hist, m->d_cursor, &queued, &g);
+    if (r == VDBG_ERR_COORD_RANGE)
+      call_status = r;
+    else if (r != VDBG_OK)
+      return r;
+    if (queued)
+    {
+      const RunBuffer rb = run_buffer(m->run_key, m->run_bits, m->run_slab, m->run_count, m->run_seg, m->dda_warps);
+      const int d        = run_dda_passes(m, *src, m->d_rays, m->d_order, n, g, rb, m->lstate, m->wstate, true, s);
+      if (d == VDBG_ERR_COORD_RANGE)
+        call_status = d;
+      else if (d != VDBG_OK)
+        return d;
+    }
   }
   std::vector<Channel*> todo;
   if (integrate_all)
@@ -645,70 +790,9 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
   {
     todo.push_back(only);
   }
-  auto sweeps = [&]() -> int {
-    for (Channel* c : todo) VDBG_TRY(launch_sweep(m, *c, s));
-    return VDBG_OK;
-  };
-  VDBG_TRY(sweeps());
-  int call_status = VDBG_OK;
-  bool done       = false;
-  // Every growth at least doubles what ran out, so this converges long before
-  // the pools reach their size limits.
-  for (int attempt = 0; attempt < 40 && !done; ++attempt)
-  {
-    VDBG_TRY(fetch_status(m, s));
-    const uint32_t err = m->h_status->error;
-    m->n_leaves        = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
-    m->n_blocks        = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
-    if (err == 0)
-    {
-      done = true;
-      break;
-    }
-    if (err & (kErrSpin | kErrStepBound)) return map_error(err);
-    if (err & kErrCoordRange)
-    {
-      // The cloud was not marked; integrate what else is pending.
-      call_status        = VDBG_ERR_COORD_RANGE;
-      DevStatus clean;
-      clear_status(&clean);
-      clean.n_leaves     = m->n_leaves;
-      clean.n_blocks     = m->n_blocks;
-      *m->h_status       = clean;
-      VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
-      VDBG_TRY(sweeps());
-      continue;
-    }
-    // A pool or the block hash is exhausted: grow what ran out, let the
-    // failed leaf cells be allocated again, clear the error, mark again, sweep.
-    if (err & kErrPoolFull) VDBG_TRY(grow_for(m, m->h_status->n_leaves));
-    if (err & kErrBlockFull) VDBG_TRY(grow_blocks_for(m, m->h_status->n_blocks));
-    if ((err & kErrHashFull) && !(err & kErrBlockFull))
-      VDBG_TRY(rebuild_hash(m, m->bhash_size * 2, m->n_blocks));
-    if (m->n_blocks > 0)
-    {
-      k_reset_failed_leaves<<<m->num_sms * 4, 256, 0, m->stream>>>(m->bleaf, static_cast<size_t>(m->n_blocks) * 512);
-      VDBG_CUDA(cudaGetLastError());
-    }
-    VDBG_CUDA(cudaStreamSynchronize(m->stream));
-    DevStatus keep  = *m->h_status;
-    keep.error      = 0;
-    keep.n_leaves   = m->n_leaves;
-    keep.n_blocks   = m->n_blocks;
-    keep.ray_cursor = 0;  // the re-marking pass walks all rays again
-    *m->h_status   = keep;
-    VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
-    if (queued)
-    {
-      launch_dda(m, n, g, *src, s);
-      VDBG_CUDA(cudaGetLastError());
-      m->timings.launches += 1;
-      m->timings.retries += 1;
-      m->timed_prep = false;  // phases overlap the growth; only the total is meaningful
-    }
-    VDBG_TRY(sweeps());
-  }
-  if (!done) return VDBG_ERR_OUT_OF_MEMORY;
+  for (Channel* c : todo) VDBG_TRY(launch_sweep(m, *c, s));
+  VDBG_TRY(fetch_status(m, s));
+  if (m->h_status->error != 0u) return map_error(m->h_status->error);
   record_timings(m);
   for (Channel* c : todo) VDBG_TRY(finish_sweep(m, *c, s));
   if (!todo.empty()) VDBG_CUDA(cudaStreamSynchronize(s));
@@ -774,6 +858,7 @@ int vdbg_create(double resolution, const vdbg_options* options, vdbg_map** out)
   if (cudaSetDevice(m->device) != cudaSuccess) return fail(VDBG_ERR_CUDA);
   if (cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, m->device) != cudaSuccess)
     return fail(VDBG_ERR_CUDA);
+  m->dda_warps = static_cast<uint32_t>(m->num_sms) * 10u * kDdaWarps;  // k_dda_mark's resident warps
   if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(VDBG_ERR_CUDA);
   if (cudaEventCreate(&m->ev0) != cudaSuccess || cudaEventCreate(&m->ev1) != cudaSuccess ||
       cudaEventCreate(&m->ev_prep) != cudaSuccess || cudaEventCreate(&m->ev_dda) != cudaSuccess)
@@ -826,6 +911,12 @@ int vdbg_destroy(vdbg_map* m)
   dev_free(m, m->d_pts, m->pts_cap);
   dev_free(m, m->d_rays, m->ray_cap);
   dev_free(m, m->d_order, m->ray_cap);
+  dev_free(m, m->run_key, static_cast<size_t>(m->dda_warps) * m->run_seg);
+  dev_free(m, m->run_bits, static_cast<size_t>(m->dda_warps) * m->run_seg);
+  dev_free(m, m->run_slab, static_cast<size_t>(m->dda_warps) * m->run_seg);
+  dev_free(m, m->run_count, m->dda_warps);
+  dev_free(m, m->lstate, static_cast<size_t>(m->dda_warps) * 32);
+  dev_free(m, m->wstate, m->dda_warps);
   if (m->h_status) cudaFreeHost(m->h_status);
   if (m->ev0) cudaEventDestroy(m->ev0);
   if (m->ev1) cudaEventDestroy(m->ev1);
@@ -1075,26 +1166,41 @@ int vdbg_device_bytes(const vdbg_map* m, int64_t* out)
 // Insertion without device allocation (vdbg_insert_point_cloud_noalloc).
 //
 // The per-scan scratch of the regular path (host points staged on the device,
-// ray records, the L1 order and the bucket histogram/cursor) is carved out of
-// one file-scope device array instead of map-owned buffers that grow on
-// demand; the map's leaf pool and hash are used as created and never grown.
+// ray records, the DDA order, the bucket histogram/cursor, the DDA run buffer
+// and the DDA resume state) is carved out of one file-scope device array
+// instead of map-owned buffers that grow on demand; the DDA runs on a fixed
+// number of warps with small run segments, in as many passes as the scan
+// needs. The map's leaf pool and block index are used as created and never
+// grown.
 // ---------------------------------------------------------------------------
 namespace {
 
 constexpr int64_t kNoAllocMaxPoints = VDBG_NOALLOC_MAX_POINTS;
-constexpr size_t kNoAllocPtsBytes   = static_cast<size_t>(kNoAllocMaxPoints) * 16;
-constexpr size_t kNoAllocRaysBytes  = static_cast<size_t>(kNoAllocMaxPoints) * sizeof(int4);
-constexpr size_t kNoAllocOrderBytes = static_cast<size_t>(kNoAllocMaxPoints) * sizeof(int);
-constexpr size_t kNoAllocHistBytes  = static_cast<size_t>(kNumBuckets) * sizeof(uint32_t);
-constexpr size_t kNoAllocBytes      = kNoAllocPtsBytes + kNoAllocRaysBytes + kNoAllocOrderBytes + 2 * kNoAllocHistBytes;
-static_assert(kNoAllocBytes == static_cast<size_t>(VDBG_NOALLOC_SCRATCH_BYTES), "scratch size and header disagree");
+constexpr uint32_t kNoAllocWarps    = VDBG_NOALLOC_DDA_WARPS;
+constexpr uint32_t kNoAllocSeg      = VDBG_NOALLOC_RUN_SEGMENT;
+constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+constexpr size_t kNoAllocPtsBytes   = align256(static_cast<size_t>(kNoAllocMaxPoints) * 16);
+constexpr size_t kNoAllocRaysBytes  = align256(static_cast<size_t>(kNoAllocMaxPoints) * sizeof(int4));
+constexpr size_t kNoAllocOrderBytes = align256(static_cast<size_t>(kNoAllocMaxPoints) * sizeof(int));
+constexpr size_t kNoAllocHistBytes  = align256(static_cast<size_t>(kNumBuckets) * sizeof(uint32_t));
+constexpr size_t kNoAllocRunN       = static_cast<size_t>(kNoAllocWarps) * kNoAllocSeg;
+constexpr size_t kNoAllocKeyBytes   = align256(kNoAllocRunN * sizeof(unsigned long long));
+constexpr size_t kNoAllocSlabBytes  = align256(kNoAllocRunN);
+constexpr size_t kNoAllocCountBytes = align256(static_cast<size_t>(kNoAllocWarps) * sizeof(uint32_t));
+constexpr size_t kNoAllocLaneBytes  = align256(static_cast<size_t>(kNoAllocWarps) * 32 * sizeof(LaneState));
+constexpr size_t kNoAllocWarpBytes  = align256(static_cast<size_t>(kNoAllocWarps) * sizeof(WarpState));
+constexpr size_t kNoAllocBytes = kNoAllocPtsBytes + kNoAllocRaysBytes + kNoAllocOrderBytes + 2 * kNoAllocHistBytes +
+                                 2 * kNoAllocKeyBytes + kNoAllocSlabBytes + kNoAllocCountBytes + kNoAllocLaneBytes +
+                                 kNoAllocWarpBytes;
+static_assert(kNoAllocBytes <= static_cast<size_t>(VDBG_NOALLOC_SCRATCH_BYTES), "scratch size and header disagree");
+static_assert(kNoAllocWarps % kDdaWarps == 0, "DDA warps per block");
 
 constexpr int kNoAllocMaxDevices = 64;
 
 } // namespace
 
 // One copy per GPU that loads the library, zero-initialised at load.
-static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+static __device__ __align__(256) unsigned char g_noalloc_scratch[VDBG_NOALLOC_SCRATCH_BYTES];
 
 namespace {
 
@@ -1110,7 +1216,7 @@ int noalloc_scratch(int device, char** out)
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
   if (!g_noalloc_base[device])
   {
-    void* p           = nullptr;
+    void* p             = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p)
     {
@@ -1149,12 +1255,29 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
   VDBG_TRY(set_device(m));
   char* base = nullptr;
   VDBG_TRY(noalloc_scratch(m->device, &base));
-  char* d_pts       = base;
-  int4* d_rays      = reinterpret_cast<int4*>(base + kNoAllocPtsBytes);
-  int* d_order      = reinterpret_cast<int*>(base + kNoAllocPtsBytes + kNoAllocRaysBytes);
-  uint32_t* d_hist  = reinterpret_cast<uint32_t*>(base + kNoAllocPtsBytes + kNoAllocRaysBytes + kNoAllocOrderBytes);
-  uint32_t* d_cursor = d_hist + kNumBuckets;
-  cudaStream_t s     = pick_stream(m, stream);
+  char* p            = base;
+  char* d_pts        = p;
+  p += kNoAllocPtsBytes;
+  int4* d_rays       = reinterpret_cast<int4*>(p);
+  p += kNoAllocRaysBytes;
+  int* d_order       = reinterpret_cast<int*>(p);
+  p += kNoAllocOrderBytes;
+  uint32_t* d_hist   = reinterpret_cast<uint32_t*>(p);
+  p += kNoAllocHistBytes;
+  uint32_t* d_cursor = reinterpret_cast<uint32_t*>(p);
+  p += kNoAllocHistBytes;
+  unsigned long long* r_key  = reinterpret_cast<unsigned long long*>(p);
+  p += kNoAllocKeyBytes;
+  unsigned long long* r_bits = reinterpret_cast<unsigned long long*>(p);
+  p += kNoAllocKeyBytes;
+  unsigned char* r_slab      = reinterpret_cast<unsigned char*>(p);
+  p += kNoAllocSlabBytes;
+  uint32_t* r_count          = reinterpret_cast<uint32_t*>(p);
+  p += kNoAllocCountBytes;
+  LaneState* ls              = reinterpret_cast<LaneState*>(p);
+  p += kNoAllocLaneBytes;
+  WarpState* ws              = reinterpret_cast<WarpState*>(p);
+  cudaStream_t s             = pick_stream(m, stream);
 
   Channel* src = find_channel(m, id);
   int pre      = VDBG_OK;
@@ -1162,86 +1285,42 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
     pre = VDBG_ERR_UNKNOWN_SOURCE;
   else if (src->max_range > 0 && !m->config_set)
     pre = VDBG_ERR_NOT_CONFIGURED;
-  const bool cast = src && src->max_range > 0 && m->config_set && n > 0 &&
-                    !(std::isnan(origin[0]) || std::isnan(origin[1]) || std::isnan(origin[2]));
+  const bool cast = src && src->max_range > 0 && m->config_set;
 
   VDBG_TRY(begin_call(m, s));
   const uint32_t leaves_before = m->n_leaves;
+  int result                   = pre;
+  int dda                      = VDBG_OK;
   if (cast)
   {
-    ScanGeom g;
-    g.ox       = origin[0];
-    g.oy       = origin[1];
-    g.oz       = origin[2];
-    g.range    = src->max_range;
-    g.res      = m->resolution;
-    g.half_res = m->half_res;
-    g.inv_res  = m->inv_res;
-    int ov[3];
-    if (!origin_to_index(m, origin, ov)) return VDBG_ERR_COORD_RANGE;
-    g.ovx = ov[0];
-    g.ovy = ov[1];
-    g.ovz = ov[2];
-    g.pad = 0;
     // The histogram must start at zero; the previous call's contents remain.
     VDBG_CUDA(cudaMemsetAsync(d_hist, 0, kNoAllocHistBytes, s));
-    const char* pts = reinterpret_cast<const char*>(xyz);
-    if (host_input)
+    bool queued = false;
+    ScanGeom g{};
+    const int r = launch_prep(m, *src, xyz, n, stride, origin, src->max_range, flags, s, d_pts, d_rays, d_order,
+                              d_hist, d_cursor, &queued, &g);
+    if (r != VDBG_OK) return r;
+    if (queued)
     {
-      VDBG_CUDA(cudaMemcpyAsync(d_pts, xyz, static_cast<size_t>(n) * static_cast<size_t>(stride),
-                                cudaMemcpyHostToDevice, s));
-      pts = d_pts;
+      const RunBuffer rb = run_buffer(r_key, r_bits, r_slab, r_count, kNoAllocSeg, kNoAllocWarps);
+      dda                = run_dda_passes(m, *src, d_rays, d_order, n, g, rb, ls, ws, false, s);
+      if (dda == VDBG_ERR_COORD_RANGE)
+      {
+        result = dda;
+        dda    = VDBG_OK;
+      }
     }
-    const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
-    k_prep<<<blocks, 256, 0, s>>>(pts, n, stride, g, d_rays, d_hist, m->d_status);
-    k_scan<<<1, 1024, 0, s>>>(d_hist, d_cursor, m->d_status);
-    k_scatter<<<blocks, 256, 0, s>>>(d_rays, n, g, d_cursor, d_order);
-    VDBG_CUDA(cudaEventRecord(m->ev_prep, s));
-    const int64_t warps_needed = (n + 31) / 32;
-    int64_t dblocks            = (warps_needed + kDdaWarps - 1) / kDdaWarps;
-    dblocks                    = std::min<int64_t>(dblocks, static_cast<int64_t>(m->num_sms) * 10);
-    k_dda_mark<<<static_cast<unsigned>(std::max<int64_t>(dblocks, 1)), kDdaWarps * 32, 0, s>>>(
-      d_rays, d_order, g, map_view(m), channel_view(*src));
-    VDBG_CUDA(cudaGetLastError());
-    VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
-    m->timed_prep = true;
-    m->timings.launches += 4;
-    src->pending = true;
   }
-  std::vector<Channel*> todo;
-  for (Channel& c : m->channels)
-    if (c.pending) todo.push_back(&c);
-  for (Channel* c : todo) VDBG_TRY(launch_sweep(m, *c, s));
-  VDBG_TRY(fetch_status(m, s));
-  uint32_t err = m->h_status->error;
-  m->n_leaves  = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
-  m->n_blocks  = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
-  int result   = pre;
-  if (err & kErrCoordRange)
-  {
-    // Nothing of the cloud was marked; integrate what else is pending.
-    result = VDBG_ERR_COORD_RANGE;
-    DevStatus clean;
-    clear_status(&clean);
-    clean.n_leaves = m->n_leaves;
-    clean.n_blocks = m->n_blocks;
-    *m->h_status   = clean;
-    VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
-    for (Channel* c : todo) VDBG_TRY(launch_sweep(m, *c, s));
-    VDBG_TRY(fetch_status(m, s));
-    err = m->h_status->error;
-  }
-  if (err != 0)
+  if (dda != VDBG_OK)
   {
     // The pool may not grow here: drop the partial marking of this source,
     // apply nothing and report.
-    if (src && cast)
-    {
-      k_compact<<<m->num_sms * 4, 256, 0, s>>>(map_view(m), channel_view(*src), m->d_status, 1);
-      k_clear_touched<<<m->num_sms * 4, 256, 0, s>>>(channel_view(*src));
-      VDBG_CUDA(cudaGetLastError());
-      VDBG_TRY(finish_sweep(m, *src, s));
-    }
+    m->n_leaves = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
+    m->n_blocks = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
+    k_compact<<<m->num_sms * 4, 256, 0, s>>>(map_view(m), channel_view(*src), m->d_status, 1);
+    k_clear_touched<<<m->num_sms * 4, 256, 0, s>>>(channel_view(*src));
+    VDBG_CUDA(cudaGetLastError());
+    VDBG_TRY(finish_sweep(m, *src, s));
     // Failed leaf cells become empty again and the block hash is rebuilt in
     // place from the allocated blocks, so later calls see a consistent index.
     if (m->n_blocks > 0)
@@ -1263,8 +1342,14 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
     *m->h_status   = clean;
     VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
     VDBG_CUDA(cudaStreamSynchronize(s));
-    return (err & (kErrPoolFull | kErrHashFull)) ? VDBG_ERR_OUT_OF_MEMORY : map_error(err);
+    return dda;
   }
+  std::vector<Channel*> todo;
+  for (Channel& c : m->channels)
+    if (c.pending) todo.push_back(&c);
+  for (Channel* c : todo) VDBG_TRY(launch_sweep(m, *c, s));
+  VDBG_TRY(fetch_status(m, s));
+  if (m->h_status->error != 0u) return map_error(m->h_status->error);
   record_timings(m);
   for (Channel* c : todo) VDBG_TRY(finish_sweep(m, *c, s));
   if (!todo.empty()) VDBG_CUDA(cudaStreamSynchronize(s));
