@@ -32,7 +32,7 @@ enum vdbg_status
   VDBG_ERR_DUPLICATE_SOURCE = 5,  /* source id registered twice */
   VDBG_ERR_INVALID_ARGUMENT = 6,
   VDBG_ERR_OUT_OF_MEMORY    = 7,  /* device allocation failed or memory budget reached */
-  VDBG_ERR_COORD_RANGE      = 8,  /* a voxel index outside [-2^23, 2^23) on some axis */
+  VDBG_ERR_COORD_RANGE      = 8,  /* a voxel index outside [-2^21, 2^21) on some axis */
   VDBG_ERR_CUDA             = 9,
   VDBG_ERR_TIMEOUT          = 10, /* a bounded device wait gave up */
   VDBG_ERR_BUFFER_TOO_SMALL = 11,
@@ -188,6 +188,34 @@ int vdbg_device_bytes(const vdbg_map* map, int64_t* out);
 int vdbg_insert_point_cloud_noalloc(vdbg_map* map, const float* xyz, int64_t n, int64_t stride_bytes,
                                     const double origin[3], const char* source_id, uint32_t flags,
                                     void* stream, vdbg_scan_stats* stats);
+
+/* Batches of independent maps. No counterpart in the reference, which runs
+ * one OccupancyVDBMapping per map: here up to 126 maps with their own
+ * resolutions and configs share one device pool, and one call inserts one
+ * scan into each map (insertPointCloud, VDBMapping.hpp:399-406, for every map
+ * at once) through a single pass of the kernels. Each map's result equals
+ * what inserting its scan alone into its own map would give. The single-map
+ * entry points reject batch handles; vdbg_destroy, vdbg_reset_map,
+ * vdbg_leaf_count (all maps), vdbg_get_timings and vdbg_device_bytes accept
+ * them. */
+int vdbg_create_batch(int n_maps, const double* resolutions, const vdbg_options* options, vdbg_map** out);
+
+/* setConfig (OccupancyVDBMapping.hpp:59-89) of map `map` of a batch; a map's
+ * scans are cast to its max_range (0: that map's scans are not cast). */
+int vdbg_batch_set_config(vdbg_map* batch, int map, const vdbg_config* config);
+
+/* One scan per map: counts[i] points of map i, concatenated in map order in
+ * xyz (stride_bytes apart), origins[3*i..3*i+2] its sensor origin. Maps with
+ * no points, a zero max_range or a NaN origin are skipped. A voxel index out
+ * of range in any scan leaves every map of the batch unchanged and returns
+ * VDBG_ERR_COORD_RANGE. stats receives the totals over the batch. */
+int vdbg_batch_insert(vdbg_map* batch, const float* xyz, const int64_t* counts, int64_t stride_bytes,
+                      const double* origins, uint32_t flags, void* stream, vdbg_scan_stats* stats);
+
+/* Leaf count and export (as vdbg_leaf_count / vdbg_export_leaves) of one map. */
+int vdbg_batch_leaf_count(vdbg_map* batch, int map, int64_t* out);
+int vdbg_batch_export_leaves(vdbg_map* batch, int map, int64_t capacity, int32_t* origins, float* values,
+                             uint64_t* masks, int64_t* n_out);
 
 /* Human-readable text of a status code (static storage). */
 const char* vdbg_status_string(int status);

@@ -111,6 +111,13 @@ SIGNATURES = [
     ("vdbg_get_timings", C.c_int, [_P, C.POINTER(vdbg_timings)]),
     ("vdbg_insert_point_cloud_noalloc", C.c_int,
      [_P, _P, C.c_int64, C.c_int64, _D3, C.c_char_p, C.c_uint32, _P, C.POINTER(vdbg_scan_stats)]),
+    ("vdbg_create_batch", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(vdbg_options), C.POINTER(_P)]),
+    ("vdbg_batch_set_config", C.c_int, [_P, C.c_int, C.POINTER(vdbg_config)]),
+    ("vdbg_batch_insert", C.c_int,
+     [_P, _P, C.POINTER(C.c_int64), C.c_int64, C.POINTER(C.c_double), C.c_uint32, _P,
+      C.POINTER(vdbg_scan_stats)]),
+    ("vdbg_batch_leaf_count", C.c_int, [_P, C.c_int, C.POINTER(C.c_int64)]),
+    ("vdbg_batch_export_leaves", C.c_int, [_P, C.c_int, C.c_int64, _P, _P, _P, C.POINTER(C.c_int64)]),
     ("vdbg_status_string", C.c_char_p, [C.c_int]),
 ]
 

@@ -2,15 +2,16 @@
 // the two-level leaf index, the first-touch bookkeeping and the exact
 // arithmetic helpers.
 //
-// Map layout in HBM (one map). Like OpenVDB's Tree4<float,5,4,3>, leaves are
-// 8^3 voxels; above them, instead of OpenVDB's 16^3/32^3 internal nodes, a
-// hash of 8^3-leaf blocks (64^3 voxels) each holding a dense table of leaf
-// slots, so finding a leaf is one load from a small, L2-resident table:
-//   bkeys   u64[HB]      packed block coordinate (voxel >> 6, 21 bits per axis)
+// Map layout in HBM. One pool holds one map or a batch of independent maps
+// (map id 0..126, part of every key). Like OpenVDB's Tree4<float,5,4,3>,
+// leaves are 8^3 voxels; above them, instead of OpenVDB's 16^3/32^3 internal
+// nodes, a hash of 8^3-leaf blocks (64^3 voxels) each holding a dense table
+// of leaf slots, so finding a leaf is one load from a small, L2-resident table:
+//   bkeys   u64[HB]      packed (map, block coordinate = voxel >> 6)
 //   bslots  i32[HB]      block index for the key; -1 while being published
-//   borigin int4[PB]     block coordinate (voxel >> 6)
+//   borigin int4[PB]     block coordinate (voxel >> 6), .w = map
 //   bleaf   i32[PB][512] leaf slot of each leaf cell of the block, -1 none
-//   origin  int4[P]      leaf origin (voxel coordinates, multiples of 8)
+//   origin  int4[P]      leaf origin (voxel coordinates, multiples of 8), .w = map
 //   values  f32[P][512]  log-odds, OpenVDB leaf order (x&7)<<6 | (y&7)<<3 | (z&7)
 //   active  u64[P][8]    value (active) mask, bit i of word w = offset 64w+i
 //   flags   u32[P]       1 once the leaf belongs to the map (first integration)
@@ -36,11 +37,15 @@ constexpr int kLeafPending             = -2;
 constexpr int kLeafFailed              = -3;
 constexpr uint32_t kMaxProbes          = 4096;
 constexpr uint32_t kSpinLimit          = 1u << 22;
-constexpr int kKeyBits                 = 21;
-constexpr int kLeafCoordMin            = -(1 << (kKeyBits - 1));
-constexpr int kLeafCoordMax            = (1 << (kKeyBits - 1)) - 1;
-constexpr double kVoxelMin             = -8388608.0;  // -2^23
-constexpr double kVoxelMaxExcl         = 8388608.0;   //  2^23
+// Keys: map id in bits 57-63, then x, y, z as 19-bit two's complement
+// (leaf or block coordinates). Voxel indices are limited to [-2^21, 2^21) per
+// axis so that leaf coordinates fit; map 127 is reserved (its key with all
+// coordinates -1 would be kEmptyKey).
+constexpr int kKeyBits                 = 19;
+constexpr int kMapShift                = 3 * kKeyBits;
+constexpr int kMaxMaps                 = 127;
+constexpr double kVoxelMin             = -2097152.0;  // -2^21
+constexpr double kVoxelMaxExcl         = 2097152.0;   //  2^21
 
 // Device error bits (DevStatus::error).
 constexpr uint32_t kErrPoolFull   = 1u;
@@ -56,9 +61,11 @@ constexpr uint32_t kMetaL1Mask   = (1u << 29) - 1;
 constexpr uint32_t kMetaClipped  = 1u << 29;
 constexpr uint32_t kMetaValid    = 1u << 30;
 
-// Counting-sort buckets for rays by L1 length (descending).
-constexpr int kNumBuckets  = 4096;
-constexpr int kBucketShift = 3;
+// Counting-sort buckets of the DDA order: 4 length classes x scans x 1014
+// direction cells (see ray_bin).
+constexpr int kDirCells    = 1014;
+constexpr int kLenClasses  = 4;
+constexpr int kBucketsPerScan = kLenClasses * kDirCells;
 
 struct DevStatus
 {
@@ -83,16 +90,62 @@ struct LogOdds
   float hit, miss, thres_min, thres_max, max, min;
 };
 
+// Log-odds constants of the maps in the pool: `table[map]` when there are
+// several maps, else `lo0`.
+struct LogOddsTable
+{
+  LogOdds lo0;
+  const LogOdds* table;
+};
+
 // Geometry of one scan: sensor origin in world and index space, the raycast
-// range and the quantiser constants (res/2 and 1/res computed on the host).
+// range, the quantiser constants (res/2 and 1/res computed on the host) and
+// the map the scan goes into.
 struct ScanGeom
 {
   double ox, oy, oz;
   double range;
   double res, half_res, inv_res;
   int ovx, ovy, ovz;
-  int pad;
+  int map;
 };
+
+// The scans of one call. Points (and rays) of scan s are [first[s],
+// first[s+1]). With one scan the geometry travels in the kernel parameters
+// and the arrays are not used.
+struct ScanTable
+{
+  ScanGeom g0;
+  const ScanGeom* geom;     // [n] (n > 1)
+  const uint32_t* first;    // [n + 1] (n > 1)
+  const uint16_t* ray_scan; // [rays] scan of each ray (n > 1)
+  int n;
+};
+
+__device__ __forceinline__ int scan_of_point(const ScanTable& t, uint32_t i)
+{
+  if (t.n <= 1) return 0;
+  int lo = 0, hi = t.n - 1;  // last s with first[s] <= i
+  while (lo < hi)
+  {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(t.first + mid) <= i)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int scan_of_ray(const ScanTable& t, uint32_t i)
+{
+  return t.n <= 1 ? 0 : static_cast<int>(__ldg(t.ray_scan + i));
+}
+
+__device__ __forceinline__ const ScanGeom& scan_geom(const ScanTable& t, int s)
+{
+  return t.n <= 1 ? t.g0 : t.geom[s];
+}
 
 struct MapView
 {
@@ -132,7 +185,7 @@ struct LaneState
   int sx, sy, sz;
   uint32_t budget;
   uint32_t flags;  // bit 0: has_ray, bit 1: run_open
-  uint32_t pad;
+  uint32_t map;
 };
 
 struct WarpState
@@ -209,16 +262,19 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long k)
 
 __device__ __forceinline__ int unpack_leaf_coord(unsigned long long key, int field)
 {
-  // field 0 = x (bits 42-62), 1 = y (21-41), 2 = z (0-20); sign-extend 21 bits
+  // field 0 = x (bits 38-56), 1 = y (19-37), 2 = z (0-18); sign-extend 19 bits
   const int shift = (2 - field) * kKeyBits;
   const int v     = static_cast<int>((key >> shift) & ((1ull << kKeyBits) - 1));
   return (v << (32 - kKeyBits)) >> (32 - kKeyBits);
 }
 
-__device__ __forceinline__ unsigned long long pack_leaf_key(int lx, int ly, int lz)
+__device__ __forceinline__ int unpack_map(unsigned long long key) { return static_cast<int>(key >> kMapShift); }
+
+__device__ __forceinline__ unsigned long long pack_leaf_key(int map, int lx, int ly, int lz)
 {
   const unsigned long long m = (1ull << kKeyBits) - 1;
-  return ((static_cast<unsigned long long>(lx) & m) << (2 * kKeyBits)) |
+  return (static_cast<unsigned long long>(map) << kMapShift) |
+         ((static_cast<unsigned long long>(lx) & m) << (2 * kKeyBits)) |
          ((static_cast<unsigned long long>(ly) & m) << kKeyBits) |
          (static_cast<unsigned long long>(lz) & m);
 }
@@ -245,9 +301,9 @@ __device__ __forceinline__ void touch_block(const ChannelView& c, int b)
 // leaf cells empty (the block pool is filled with -1 when allocated). Returns
 // kSlotFailed after setting an error bit when the block pool or the probe
 // budget is exhausted.
-__device__ __forceinline__ int find_or_insert_block(const MapView& m, int bx, int by, int bz)
+__device__ __forceinline__ int find_or_insert_block(const MapView& m, int map, int bx, int by, int bz)
 {
-  const unsigned long long key = pack_leaf_key(bx, by, bz);
+  const unsigned long long key = pack_leaf_key(map, bx, by, bz);
   uint32_t h                   = static_cast<uint32_t>(mix64(key)) & m.bhmask;
   for (uint32_t probe = 0; probe < kMaxProbes; ++probe)
   {
@@ -266,7 +322,7 @@ __device__ __forceinline__ int find_or_insert_block(const MapView& m, int bx, in
         }
         else
         {
-          m.borigin[s] = make_int4(bx, by, bz, 0);
+          m.borigin[s] = make_int4(bx, by, bz, map);
           slot         = static_cast<int>(s);
         }
         st_release_s32(m.bslots + h, slot);
@@ -306,7 +362,8 @@ __device__ __forceinline__ int find_or_insert_block(const MapView& m, int bx, in
 // Slot of the leaf in cell `cell` of block `b` (leaf coordinate lx,ly,lz),
 // allocating it from the leaf pool if the cell is empty: a CAS moves the cell
 // from empty to pending, the winner takes a slot and publishes it.
-__device__ __forceinline__ int find_or_insert_leaf(const MapView& m, int b, int cell, int lx, int ly, int lz)
+__device__ __forceinline__ int find_or_insert_leaf(const MapView& m, int b, int cell, int map, int lx, int ly,
+                                                   int lz)
 {
   int* e = m.bleaf + static_cast<size_t>(b) * 512 + cell;
   int s  = ld_ca_s32(e);
@@ -323,7 +380,7 @@ __device__ __forceinline__ int find_or_insert_leaf(const MapView& m, int b, int 
         st_release_s32(e, kLeafFailed);
         return kSlotFailed;
       }
-      m.origin[t] = make_int4(lx * 8, ly * 8, lz * 8, 0);
+      m.origin[t] = make_int4(lx * 8, ly * 8, lz * 8, map);
       st_release_s32(e, static_cast<int>(t));
       return static_cast<int>(t);
     }
@@ -351,7 +408,7 @@ __device__ __forceinline__ int find_or_insert_leaf(const MapView& m, int b, int 
 
 // VDBMapping.hpp:612-631 for one axis: shift non-multiples of the resolution
 // by res/2 (std::fmod is exact, as CUDA's fmod is), scale by 1/res, floor.
-// Returns false when the index leaves [-2^23, 2^23) (or is NaN).
+// Returns false when the index leaves [-2^21, 2^21) (or is NaN).
 __device__ __forceinline__ bool world_to_index_axis(double w, const ScanGeom& g, int& out)
 {
   if (fmod(w, g.res) != 0.0) w = __dadd_rn(w, g.half_res);

@@ -23,14 +23,15 @@
 
 namespace vdbg {
 
-// Sort bin of a ray (voxel offset d from the sensor voxel, L1 length l1):
-// four length classes, longest first, so long rays start early and do not
-// extend the tail; within a class, the cube-map face of the dominant axis and
-// a 13 x 13 cell on it (6 * 169 = 1014 direction cells). Rays of one bin are
-// angular neighbours of similar length; the DDA hands warps short runs of
-// this order so their lanes walk through the same leaves and their leaf
-// records merge. Order only; the map does not depend on it.
-__device__ __forceinline__ int ray_bin(int dx, int dy, int dz, uint32_t l1)
+// Sort bucket of a ray of scan s (voxel offset d from the sensor voxel, L1
+// length l1): four length classes, longest first, so long rays start early
+// and do not extend the tail; within a class the scan, then the cube-map face
+// of the dominant axis and a 13 x 13 cell on it (6 * 169 = 1014 direction
+// cells). Rays of one bucket are angular neighbours of similar length in one
+// map; the DDA hands warps short runs of this order so their lanes walk
+// through the same leaves and their leaf records merge. Order only; the map
+// does not depend on it.
+__device__ __forceinline__ int ray_bucket(int dx, int dy, int dz, uint32_t l1, int s, int n_scans)
 {
   const int ax = abs(dx), ay = abs(dy), az = abs(dz);
   int face, u, v, mx;
@@ -55,30 +56,39 @@ __device__ __forceinline__ int ray_bin(int dx, int dy, int dz, uint32_t l1)
     v    = dy;
     mx   = az;
   }
-  const int cls = l1 >= 1024u ? 0 : (l1 >= 512u ? 1 : (l1 >= 256u ? 2 : 3));
-  if (mx == 0) return cls * 1014;
+  const int cls  = l1 >= 1024u ? 0 : (l1 >= 512u ? 1 : (l1 >= 256u ? 2 : 3));
+  const int base = (cls * n_scans + s) * kDirCells;
+  if (mx == 0) return base;
   const int iu = static_cast<int>((static_cast<long long>(u + mx) * 13) / (2 * mx + 1));
   const int iv = static_cast<int>((static_cast<long long>(v + mx) * 13) / (2 * mx + 1));
-  return cls * 1014 + face * 169 + iv * 13 + iu;
+  return base + face * 169 + iv * 13 + iu;
 }
-static_assert(4 * 1014 <= kNumBuckets, "sort bins exceed the histogram");
+static_assert(6 * 169 == kDirCells, "direction cells");
 
 // One thread per point. rays[i] = (end voxel xyz, meta). Every lane of a
 // warp stays to the end so the warp-wide reductions see a full mask.
 __global__ void __launch_bounds__(256) k_prep(const char* __restrict__ pts, int64_t n, int64_t stride,
-                                              ScanGeom g, int4* __restrict__ rays,
-                                              uint32_t* __restrict__ hist, DevStatus* st)
+                                              ScanTable t, int4* __restrict__ rays,
+                                              uint16_t* __restrict__ ray_scan, uint32_t* __restrict__ hist,
+                                              DevStatus* st)
 {
   const int64_t i     = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const bool in_range = i < n;
   uint32_t meta       = 0;
   int ex = 0, ey = 0, ez = 0;
   unsigned long long visits = 0, hit = 0, valid = 0, nonfinite = 0;
+  const int sc       = in_range ? scan_of_point(t, static_cast<uint32_t>(i)) : 0;
+  const ScanGeom& g  = scan_geom(t, sc);
   if (in_range)
   {
+    if (t.n > 1) ray_scan[i] = static_cast<uint16_t>(sc);
     const float* p = reinterpret_cast<const float*>(pts + i * stride);
     const float px = p[0], py = p[1], pz = p[2];
-    if (isnan(px) || isnan(py) || isnan(pz))
+    if (g.map < 0)
+    {
+      // A scan of the batch that is not cast (no points to cast, NaN origin).
+    }
+    else if (isnan(px) || isnan(py) || isnan(pz))
     {
       // VDBMapping.hpp:505-510: skipped.
     }
@@ -139,7 +149,8 @@ __global__ void __launch_bounds__(256) k_prep(const char* __restrict__ pts, int6
     if (sr) atomicAdd(&st->rays, sr);
     if (sn) atomicAdd(&st->nonfinite, sn);
   }
-  const int b          = valid ? ray_bin(ex - g.ovx, ey - g.ovy, ez - g.ovz, meta & kMetaL1Mask) : -1;
+  const int b =
+    valid ? ray_bucket(ex - g.ovx, ey - g.ovy, ez - g.ovz, meta & kMetaL1Mask, sc, t.n) : -1;
   const unsigned peers = __match_any_sync(0xffffffffu, b);
   if (valid && (__ffs(peers) - 1) == static_cast<int>(threadIdx.x & 31))
   {
@@ -147,62 +158,79 @@ __global__ void __launch_bounds__(256) k_prep(const char* __restrict__ pts, int6
   }
 }
 
-// Single block of 1024 threads: exclusive scan of kNumBuckets counts into
-// cursor[], total into st->n_valid; clears the histogram for the next scan.
+// Single block of 1024 threads: exclusive scan of the nb bucket counts into
+// cursor[], total into st->n_valid; clears the histogram for the next call.
+// The buckets go in tiles of 4096 (4 per thread) with a running carry.
 __global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ hist, uint32_t* __restrict__ cursor,
-                                               DevStatus* st)
+                                               uint32_t nb, DevStatus* st)
 {
-  constexpr int kPer = kNumBuckets / 1024;
+  constexpr int kPer = 4;
   __shared__ uint32_t warp_sums[32];
-  const int t = threadIdx.x;
-  uint32_t v[kPer];
-  uint32_t local = 0;
-#pragma unroll
-  for (int k = 0; k < kPer; ++k)
-  {
-    v[k] = hist[t * kPer + k];
-    local += v[k];
-  }
-  // inclusive warp scan of `local`
+  __shared__ uint32_t carry_s;
+  const int t    = threadIdx.x;
   const int lane = t & 31, warp = t >> 5;
-  uint32_t inc = local;
-  for (int off = 1; off < 32; off <<= 1)
+  uint32_t carry = 0;
+  for (uint32_t tile = 0; tile < nb; tile += 1024 * kPer)
   {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
-    if (lane >= off) inc += y;
-  }
-  if (lane == 31) warp_sums[warp] = inc;
-  __syncthreads();
-  if (warp == 0)
-  {
-    uint32_t ws = warp_sums[lane];
+    uint32_t v[kPer];
+    uint32_t local = 0;
+#pragma unroll
+    for (int k = 0; k < kPer; ++k)
+    {
+      const uint32_t idx = tile + t * kPer + k;
+      v[k]               = idx < nb ? hist[idx] : 0u;
+      local += v[k];
+    }
+    // inclusive warp scan of `local`
+    uint32_t inc = local;
     for (int off = 1; off < 32; off <<= 1)
     {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, ws, off);
-      if (lane >= off) ws += y;
+      const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+      if (lane >= off) inc += y;
     }
-    warp_sums[lane] = ws;  // inclusive
-  }
-  __syncthreads();
-  uint32_t base = (warp > 0 ? warp_sums[warp - 1] : 0u) + inc - local;
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    if (warp == 0)
+    {
+      uint32_t ws = warp_sums[lane];
+      for (int off = 1; off < 32; off <<= 1)
+      {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, ws, off);
+        if (lane >= off) ws += y;
+      }
+      warp_sums[lane] = ws;  // inclusive
+      if (lane == 31) carry_s = carry + ws;
+    }
+    __syncthreads();
+    uint32_t base = carry + (warp > 0 ? warp_sums[warp - 1] : 0u) + inc - local;
 #pragma unroll
-  for (int k = 0; k < kPer; ++k)
-  {
-    cursor[t * kPer + k] = base;
-    base += v[k];
-    hist[t * kPer + k] = 0u;
+    for (int k = 0; k < kPer; ++k)
+    {
+      const uint32_t idx = tile + t * kPer + k;
+      if (idx < nb)
+      {
+        cursor[idx] = base;
+        hist[idx]   = 0u;
+      }
+      base += v[k];
+    }
+    carry = carry_s;
+    __syncthreads();
   }
-  if (t == 1023) st->n_valid = base;
+  if (t == 0) st->n_valid = carry;
 }
 
-__global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, int64_t n, ScanGeom g,
+__global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, int64_t n, ScanTable t,
                                                  uint32_t* __restrict__ cursor, int* __restrict__ order)
 {
   const int64_t i      = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const int4 r         = i < n ? rays[i] : make_int4(0, 0, 0, 0);
   const uint32_t meta  = static_cast<uint32_t>(r.w);
   const bool valid     = (meta & kMetaValid) != 0;
-  const int b          = valid ? ray_bin(r.x - g.ovx, r.y - g.ovy, r.z - g.ovz, meta & kMetaL1Mask) : -1;
+  const int sc         = valid ? scan_of_ray(t, static_cast<uint32_t>(i)) : 0;
+  const ScanGeom& g    = scan_geom(t, sc);
+  const int b =
+    valid ? ray_bucket(r.x - g.ovx, r.y - g.ovy, r.z - g.ovz, meta & kMetaL1Mask, sc, t.n) : -1;
   const unsigned peers = __match_any_sync(0xffffffffu, b);
   const int lane       = static_cast<int>(threadIdx.x & 31);
   const int leader     = __ffs(peers) - 1;
@@ -293,7 +321,7 @@ __device__ __forceinline__ uint32_t dda_write_runs(DdaWarpSmem& q, int lane, int
 }
 
 __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __restrict__ rays,
-                                                               const int* __restrict__ order, ScanGeom g,
+                                                               const int* __restrict__ order, ScanTable t,
                                                                MapView m, RunBuffer rb,
                                                                LaneState* __restrict__ lstate,
                                                                WarpState* __restrict__ wstate, int resume)
@@ -314,6 +342,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
   long long nx = 0, ny = 0, nz = 0;
   double dx = 0.0, dy = 0.0, dz = 0.0;
   int rx = 0, ry = 0, rz = 0;  // current run: exact x, leaf y, leaf z
+  int map = 0;                 // map of the lane's ray
   unsigned long long run = 0ull;
   int n_rec       = 0;
   uint32_t budget = 0;
@@ -333,6 +362,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
     rx = l.rx; ry = l.ry; rz = l.rz;
     sx = l.sx; sy = l.sy; sz = l.sz;
     budget = l.budget;
+    map    = static_cast<int>(l.map);
   }
   const long long kOne = __double_as_longlong(1.0);
   const long long kMax = __double_as_longlong(1.7976931348623157e308);
@@ -369,12 +399,15 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
       need &= ~took;
       if (take)
       {
-        const int4 r      = rays[order[idx]];
+        const int ri      = order[idx];
+        const int4 r      = rays[ri];
         const uint32_t l1 = static_cast<uint32_t>(r.w) & kMetaL1Mask;
         if (l1 > 0)
         {
           // (An endpoint in the sensor voxel is only a hit; k_mark_hits does it.)
-          const int o[3] = {g.ovx, g.ovy, g.ovz};
+          const ScanGeom& g = scan_geom(t, scan_of_ray(t, static_cast<uint32_t>(ri)));
+          map               = g.map;
+          const int o[3]    = {g.ovx, g.ovy, g.ovz};
           const int e[3] = {r.x, r.y, r.z};
           int vox[3], stp[3];
           long long nxt[3];
@@ -437,7 +470,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
         const int ly = vy >> 3, lz = vz >> 3;
         if (run_open && (vx != rx || ly != ry || lz != rz))
         {
-          q.keys[n_rec][lane] = pack_leaf_key(rx >> 3, ry, rz);
+          q.keys[n_rec][lane] = pack_leaf_key(map, rx >> 3, ry, rz);
           q.bits[n_rec][lane] = run;
           q.slab[n_rec][lane] = static_cast<unsigned char>(rx & 7);
           ++n_rec;
@@ -470,7 +503,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
         }
         if (fin)
         {
-          q.keys[n_rec][lane] = pack_leaf_key(rx >> 3, ry, rz);
+          q.keys[n_rec][lane] = pack_leaf_key(map, rx >> 3, ry, rz);
           q.bits[n_rec][lane] = run;
           q.slab[n_rec][lane] = static_cast<unsigned char>(rx & 7);
           ++n_rec;
@@ -513,7 +546,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
   l.sx = sx; l.sy = sy; l.sz = sz;
   l.budget = budget;
   l.flags  = (has_ray ? 1u : 0u) | (run_open ? 2u : 0u);
-  l.pad    = 0u;
+  l.map    = static_cast<uint32_t>(map);
   lstate[gw * 32 + lane] = l;
 }
 
@@ -529,7 +562,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
 // full is applied directly.
 // ---------------------------------------------------------------------------
 constexpr int kApplyThreads = 256;
-constexpr int kApplyChunk   = 1024;
+constexpr int kApplyChunk   = 4096;
 constexpr int kApplyTable   = 512;  // 2^9 entries, see apply_hash
 
 struct ApplySmem
@@ -549,11 +582,12 @@ __device__ __forceinline__ uint32_t apply_hash(unsigned long long key)
 __device__ __forceinline__ int apply_resolve(const MapView& m, const ChannelView& c, unsigned long long key)
 {
   const int lx = unpack_leaf_coord(key, 0), ly = unpack_leaf_coord(key, 1), lz = unpack_leaf_coord(key, 2);
-  const int b  = find_or_insert_block(m, lx >> 3, ly >> 3, lz >> 3);
+  const int mp = unpack_map(key);
+  const int b  = find_or_insert_block(m, mp, lx >> 3, ly >> 3, lz >> 3);
   if (b < 0) return kSlotFailed;
   touch_block(c, b);
   const int cell = ((lx & 7) << 6) | ((ly & 7) << 3) | (lz & 7);
-  const int slot = find_or_insert_leaf(m, b, cell, lx, ly, lz);
+  const int slot = find_or_insert_leaf(m, b, cell, mp, lx, ly, lz);
   if (slot >= 0) atomicOr(c.btouched + static_cast<size_t>(b) * 8 + (cell >> 6), 1ull << (cell & 63));
   return slot;
 }
@@ -640,21 +674,23 @@ __global__ void __launch_bounds__(kApplyThreads, 4) k_apply_runs(RunBuffer rb, M
 // per unclipped ray ORs the hit bit of its end voxel, creating the leaf when
 // the DDA did not visit it (an endpoint in the sensor voxel).
 __global__ void __launch_bounds__(256) k_mark_hits(const int4* __restrict__ rays, const int* __restrict__ order,
-                                                   MapView m, ChannelView c)
+                                                   ScanTable t, MapView m, ChannelView c)
 {
   if (ld_relaxed_u32(&m.st->error) != 0u) return;
   const uint32_t nv = m.st->n_valid;
   const uint32_t j  = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nv) return;
-  const int4 r        = rays[order[j]];
+  const int ri        = order[j];
+  const int4 r        = rays[ri];
   const uint32_t meta = static_cast<uint32_t>(r.w);
   if (meta & kMetaClipped) return;
+  const int mp = scan_geom(t, scan_of_ray(t, static_cast<uint32_t>(ri))).map;
   const int lx = r.x >> 3, ly = r.y >> 3, lz = r.z >> 3;
-  const int b  = find_or_insert_block(m, lx >> 3, ly >> 3, lz >> 3);
+  const int b  = find_or_insert_block(m, mp, lx >> 3, ly >> 3, lz >> 3);
   if (b < 0) return;
   touch_block(c, b);
   const int cell = ((lx & 7) << 6) | ((ly & 7) << 3) | (lz & 7);
-  const int slot = find_or_insert_leaf(m, b, cell, lx, ly, lz);
+  const int slot = find_or_insert_leaf(m, b, cell, mp, lx, ly, lz);
   if (slot < 0) return;
   unsigned long long* bt = c.btouched + static_cast<size_t>(b) * 8 + (cell >> 6);
   if (!((*bt >> (cell & 63)) & 1ull)) atomicOr(bt, 1ull << (cell & 63));
@@ -670,7 +706,8 @@ __global__ void __launch_bounds__(256) k_mark_hits(const int4* __restrict__ rays
 // rules, stores them back and clears its update words.
 __global__ void __launch_bounds__(256) k_sweep(ChannelView c, float* __restrict__ values,
                                                unsigned long long* __restrict__ active,
-                                               uint32_t* __restrict__ flags, LogOdds lo, DevStatus* st)
+                                               uint32_t* __restrict__ flags, const int4* __restrict__ origin,
+                                               LogOddsTable lt, DevStatus* st)
 {
   if (ld_relaxed_u32(&st->error) != 0u) return;
   const uint32_t nt   = *c.n_touched;
@@ -692,6 +729,7 @@ __global__ void __launch_bounds__(256) k_sweep(ChannelView c, float* __restrict_
     const unsigned long long hitw  = u[8 + w];
     const unsigned long long actw  = u[w] | hitw;
     if (actw == 0ull) continue;
+    const LogOdds lo               = lt.table ? lt.table[origin[slot].w] : lt.lo0;
     unsigned long long* aw         = active + static_cast<size_t>(slot) * 8 + w;
     const unsigned long long on_in = *aw;
     unsigned long long on          = on_in;
@@ -780,7 +818,7 @@ __global__ void k_rehash(MapView m, uint32_t n)
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const int4 o                 = m.borigin[s];
-  const unsigned long long key = pack_leaf_key(o.x, o.y, o.z);
+  const unsigned long long key = pack_leaf_key(o.w, o.x, o.y, o.z);
   uint32_t h                   = static_cast<uint32_t>(mix64(key)) & m.bhmask;
   for (uint32_t probe = 0; probe <= m.bhmask; ++probe)
   {

@@ -1,7 +1,9 @@
 // vdb_gb300.cu — host side of the C ABI declared in include/vdb_gb300.h.
 //
 // One vdbg_map owns one occupancy map resident on one GPU (leaf hash, leaf
-// pool, one update grid per input source) plus the per-scan scratch buffers.
+// pool, one update grid per input source) plus the per-scan scratch buffers,
+// or (vdbg_create_batch) a batch of independent maps sharing one pool, each
+// with its own resolution and log-odds, integrated one scan per map per call.
 // Every entry point launches its kernels on one stream and waits for them, so
 // the calls have the reference's synchronous semantics.
 #include <algorithm>
@@ -36,19 +38,32 @@ struct Channel
   bool pending                      = false;    // marked since its last integration
 };
 
+// Configuration of one map (OccupancyVDBMapping::setConfig).
+struct MapConf
+{
+  double resolution          = 0.0;
+  double half_res            = 0.0;
+  double inv_res             = 0.0;
+  bool config_set            = false;
+  double max_range           = 0.0;
+  bool fast_mode             = false;
+  double accumulation_period = 0.0;
+  LogOdds lo{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+};
+
 } // namespace
 
 struct vdbg_map
 {
   int device            = 0;
-  double resolution     = 0.0;
-  double half_res       = 0.0;
-  double inv_res        = 0.0;
-  bool config_set       = false;
-  double max_range      = 0.0;
-  bool fast_mode        = false;
-  double accumulation_period = 0.0;
-  LogOdds lo{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  std::vector<MapConf> conf;  // one entry, or one per map of a batch
+  bool batch            = false;
+  LogOdds* d_lo         = nullptr;  // [maps] (batch)
+  ScanGeom* d_geom      = nullptr;  // [maps] (batch)
+  uint32_t* d_first     = nullptr;  // [maps + 1] (batch)
+  ScanGeom* h_geom      = nullptr;  // pinned staging of d_geom and d_first (batch)
+  uint32_t* h_first     = nullptr;
+  uint16_t* d_ray_scan  = nullptr;  // [ray_cap] (batch)
   int64_t max_bytes     = 0;
 
   cudaStream_t stream   = nullptr;
@@ -84,8 +99,9 @@ struct vdbg_map
   int4* d_rays          = nullptr;
   int* d_order          = nullptr;
   size_t ray_cap        = 0;
-  uint32_t* d_hist      = nullptr;
+  uint32_t* d_hist      = nullptr;  // [buckets]
   uint32_t* d_cursor    = nullptr;
+  uint32_t buckets      = 0;
   // DDA run buffer (one segment per DDA warp) and resumable lane/warp state.
   uint32_t dda_warps    = 0;
   uint32_t run_seg      = 0;
@@ -396,9 +412,11 @@ int ensure_scratch(vdbg_map* m, int64_t n, int64_t stride, bool host_input)
     dev_free(m, m->d_rays, m->ray_cap);
     dev_free(m, m->d_order, m->ray_cap);
     const size_t cap = std::max(static_cast<size_t>(n), m->ray_cap * 3 / 2);
+    dev_free(m, m->d_ray_scan, m->ray_cap);
     m->ray_cap       = 0;
     VDBG_TRY(dev_alloc(m, &m->d_rays, cap));
     VDBG_TRY(dev_alloc(m, &m->d_order, cap));
+    if (m->batch) VDBG_TRY(dev_alloc(m, &m->d_ray_scan, cap));
     m->ray_cap = cap;
   }
   return VDBG_OK;
@@ -414,13 +432,13 @@ Channel* find_channel(vdbg_map* m, const char* id)
 
 // Host copy of VDBMapping.hpp:612-631 for the sensor origin (compiled with
 // -ffp-contract=off, the same IEEE operations as the device quantiser).
-bool origin_to_index(const vdbg_map* m, const double o[3], int out[3])
+bool origin_to_index(const MapConf& mc, const double o[3], int out[3])
 {
   for (int a = 0; a < 3; ++a)
   {
     double w = o[a];
-    if (std::fmod(w, m->resolution) != 0.0) w = w + m->half_res;
-    const double f = std::floor(w * m->inv_res);
+    if (std::fmod(w, mc.resolution) != 0.0) w = w + mc.half_res;
+    const double f = std::floor(w * mc.inv_res);
     if (!(f >= kVoxelMin && f < kVoxelMaxExcl)) return false;
     out[a] = static_cast<int>(f);
   }
@@ -488,32 +506,53 @@ void record_timings(vdbg_map* m)
   }
 }
 
-// Marks one cloud into channel `c` (VDBMapping.hpp:466-539). Kernels are
-// queued on `s`; the caller fetches the status.
-// Queues the per-point stage of raycastPointCloud (VDBMapping.hpp:499-519):
-// clip, quantise, sort rays into the DDA order. `queued` is false when there
-// is nothing to cast (empty cloud, NaN origin).
-int launch_prep(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t stride, const double origin[3],
-                double range, uint32_t flags, cudaStream_t s, char* pts_scratch, int4* rays, int* order,
-                uint32_t* hist, uint32_t* cursor, bool* queued, ScanGeom* geom_out)
+// Geometry of a scan of map `map` from `origin` with raycast range `range`.
+// Returns false (nothing to cast) for a NaN origin (VDBMapping.hpp:505-510);
+// sets *coord_range when the origin's voxel is outside the index range.
+bool scan_geom_for(const vdbg_map* m, int map, const double origin[3], double range, ScanGeom* g,
+                   bool* coord_range)
 {
-  *queued = false;
-  if (n <= 0) return VDBG_OK;
-  if (std::isnan(origin[0]) || std::isnan(origin[1]) || std::isnan(origin[2])) return VDBG_OK;
-  ScanGeom g;
-  g.ox       = origin[0];
-  g.oy       = origin[1];
-  g.oz       = origin[2];
-  g.range    = range;
-  g.res      = m->resolution;
-  g.half_res = m->half_res;
-  g.inv_res  = m->inv_res;
+  *coord_range = false;
+  if (std::isnan(origin[0]) || std::isnan(origin[1]) || std::isnan(origin[2])) return false;
+  const MapConf& mc = m->conf[map];
   int ov[3];
-  if (!origin_to_index(m, origin, ov)) return VDBG_ERR_COORD_RANGE;
-  g.ovx = ov[0];
-  g.ovy = ov[1];
-  g.ovz = ov[2];
-  g.pad = 0;
+  if (!origin_to_index(mc, origin, ov))
+  {
+    *coord_range = true;
+    return false;
+  }
+  g->ox       = origin[0];
+  g->oy       = origin[1];
+  g->oz       = origin[2];
+  g->range    = range;
+  g->res      = mc.resolution;
+  g->half_res = mc.half_res;
+  g->inv_res  = mc.inv_res;
+  g->ovx      = ov[0];
+  g->ovy      = ov[1];
+  g->ovz      = ov[2];
+  g->map      = map;
+  return true;
+}
+
+ScanTable single_table(const ScanGeom& g)
+{
+  ScanTable t{};
+  t.g0       = g;
+  t.geom     = nullptr;
+  t.first    = nullptr;
+  t.ray_scan = nullptr;
+  t.n        = 1;
+  return t;
+}
+
+// Queues the per-point stage of raycastPointCloud (VDBMapping.hpp:499-519)
+// for the scans of table `t` (n points in all, in scan order): clip,
+// quantise, sort rays into the DDA order.
+int launch_prep(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t stride, const ScanTable& t,
+                uint32_t flags, cudaStream_t s, char* pts_scratch, int4* rays, uint16_t* ray_scan, int* order,
+                uint32_t* hist, uint32_t* cursor)
+{
   const char* pts = reinterpret_cast<const char*>(xyz);
   if ((flags & VDBG_POINTS_DEVICE) == 0)
   {
@@ -522,16 +561,14 @@ int launch_prep(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t st
     pts = pts_scratch;
   }
   const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
-  k_prep<<<blocks, 256, 0, s>>>(pts, n, stride, g, rays, hist, m->d_status);
-  k_scan<<<1, 1024, 0, s>>>(hist, cursor, m->d_status);
-  k_scatter<<<blocks, 256, 0, s>>>(rays, n, g, cursor, order);
+  k_prep<<<blocks, 256, 0, s>>>(pts, n, stride, t, rays, ray_scan, hist, m->d_status);
+  k_scan<<<1, 1024, 0, s>>>(hist, cursor, static_cast<uint32_t>(kBucketsPerScan * t.n), m->d_status);
+  k_scatter<<<blocks, 256, 0, s>>>(rays, n, t, cursor, order);
   VDBG_CUDA(cudaGetLastError());
   VDBG_CUDA(cudaEventRecord(m->ev_prep, s));
   m->timed_prep = true;
   m->timings.launches += 3;
   c.pending = true;
-  *queued   = true;
-  *geom_out = g;
   return VDBG_OK;
 }
 
@@ -586,18 +623,18 @@ int rebuild_hash(vdbg_map* m, uint32_t hsize, uint32_t n);
 // One status fetch per pass. When the leaf or block pool runs out the pools
 // grow (if `may_grow`) and the hits and the pass's runs are applied again
 // (both idempotent); otherwise the call fails with OUT_OF_MEMORY.
-int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, int64_t n, const ScanGeom& g,
+int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, int64_t n, const ScanTable& t,
                    const RunBuffer& rb, LaneState* ls, WarpState* ws, bool may_grow, cudaStream_t s)
 {
   const unsigned hit_blocks   = static_cast<unsigned>((n + 255) / 256);
   const unsigned apply_blocks = static_cast<unsigned>(m->num_sms) * 8;
-  k_mark_hits<<<hit_blocks, 256, 0, s>>>(rays, order, map_view(m), channel_view(c));
+  k_mark_hits<<<hit_blocks, 256, 0, s>>>(rays, order, t, map_view(m), channel_view(c));
   m->timings.launches += 1;
   uint32_t passes = 0;
   for (;;)
   {
     VDBG_CUDA(cudaMemsetAsync(&m->d_status->inflight, 0, sizeof(uint32_t), s));
-    k_dda_mark<<<rb.warps / kDdaWarps, kDdaWarps * 32, 0, s>>>(rays, order, g, map_view(m), rb, ls, ws,
+    k_dda_mark<<<rb.warps / kDdaWarps, kDdaWarps * 32, 0, s>>>(rays, order, t, map_view(m), rb, ls, ws,
                                                               passes > 0 ? 1 : 0);
     k_apply_runs<<<apply_blocks, kApplyThreads, 0, s>>>(rb, map_view(m), channel_view(c));
     VDBG_CUDA(cudaGetLastError());
@@ -636,7 +673,7 @@ int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, 
       VDBG_CUDA(cudaStreamSynchronize(m->stream));
       clear_error_keep_counters(m);
       VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
-      k_mark_hits<<<hit_blocks, 256, 0, s>>>(rays, order, map_view(m), channel_view(c));
+      k_mark_hits<<<hit_blocks, 256, 0, s>>>(rays, order, t, map_view(m), channel_view(c));
       k_apply_runs<<<apply_blocks, kApplyThreads, 0, s>>>(rb, map_view(m), channel_view(c));
       VDBG_CUDA(cudaGetLastError());
       m->timings.launches += 2;
@@ -660,7 +697,10 @@ int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, 
 int launch_sweep(vdbg_map* m, Channel& c, cudaStream_t s)
 {
   k_compact<<<kSweepBlocks, kSweepThreads, 0, s>>>(map_view(m), channel_view(c), m->d_status, 0);
-  k_sweep<<<kSweepBlocks, kSweepThreads, 0, s>>>(channel_view(c), m->values, m->active, m->flags, m->lo,
+  LogOddsTable lt;
+  lt.lo0   = m->conf[0].lo;
+  lt.table = m->batch ? m->d_lo : nullptr;
+  k_sweep<<<kSweepBlocks, kSweepThreads, 0, s>>>(channel_view(c), m->values, m->active, m->flags, m->origin, lt,
                                                  m->d_status);
   VDBG_CUDA(cudaGetLastError());
   m->timings.launches += 2;
@@ -741,14 +781,42 @@ bool bad_points(const float* xyz, int64_t n, int64_t stride)
 // exhaustion are handled inside run_dda_passes. A voxel index out of range
 // skips the whole cloud (nothing of it is marked) and the other pending
 // update grids are still integrated.
-int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t stride,
-                             const double origin[3], Channel* src, double range, uint32_t flags,
-                             cudaStream_t s, bool integrate_all, Channel* only, vdbg_scan_stats* stats)
+// The scans to cast in one call: the table and the status to report when a
+// scan could not be cast at all (an origin outside the index range).
+struct CastPlan
+{
+  ScanTable table{};
+  bool any       = false;
+  int status     = VDBG_OK;
+};
+
+// Plan for one cloud of the single map from `origin`.
+CastPlan plan_single(const vdbg_map* m, int64_t n, const double origin[3], double range)
+{
+  CastPlan p;
+  if (n <= 0 || !origin) return p;
+  ScanGeom g{};
+  bool coord_range = false;
+  if (scan_geom_for(m, 0, origin, range, &g, &coord_range))
+  {
+    p.table = single_table(g);
+    p.any   = true;
+  }
+  else if (coord_range)
+  {
+    p.status = VDBG_ERR_COORD_RANGE;
+  }
+  return p;
+}
+
+int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t stride, const CastPlan& plan,
+                             Channel* src, uint32_t flags, cudaStream_t s, bool integrate_all, Channel* only,
+                             vdbg_scan_stats* stats)
 {
   VDBG_TRY(begin_call(m, s));
   const uint32_t leaves_before = m->n_leaves;
-  int call_status              = VDBG_OK;
-  if (src && n > 0)
+  int call_status              = plan.status;
+  if (src && n > 0 && plan.any)
   {
     const bool host_input = (flags & VDBG_POINTS_DEVICE) == 0;
     VDBG_TRY(ensure_scratch(m, n, stride, host_input));
@@ -762,23 +830,26 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
       seg                  = static_cast<uint32_t>(std::min<uint64_t>(want, limit));
     }
     VDBG_TRY(ensure_runs(m, seg));
-    bool queued = false;
-    ScanGeom g{};
-    const int r = launch_prep(m, *src, xyz, n, stride, origin, range, flags, s, m->d_pts, m->d_rays, m->d_order,
-                              m->d_hist, m->d_cursor, &queued, &g);
-    if (r == VDBG_ERR_COORD_RANGE)
-      call_status = r;
-    else if (r != VDBG_OK)
-      return r;
-    if (queued)
+    ScanTable t = plan.table;
+    if (t.n > 1)
     {
-      const RunBuffer rb = run_buffer(m->run_key, m->run_bits, m->run_slab, m->run_count, m->run_seg, m->dda_warps);
-      const int d        = run_dda_passes(m, *src, m->d_rays, m->d_order, n, g, rb, m->lstate, m->wstate, true, s);
-      if (d == VDBG_ERR_COORD_RANGE)
-        call_status = d;
-      else if (d != VDBG_OK)
-        return d;
+      // Scan table to the device (from pinned staging, so the copy is async).
+      VDBG_CUDA(cudaMemcpyAsync(m->d_geom, m->h_geom, static_cast<size_t>(t.n) * sizeof(ScanGeom),
+                                cudaMemcpyHostToDevice, s));
+      VDBG_CUDA(cudaMemcpyAsync(m->d_first, m->h_first, static_cast<size_t>(t.n + 1) * sizeof(uint32_t),
+                                cudaMemcpyHostToDevice, s));
+      t.geom     = m->d_geom;
+      t.first    = m->d_first;
+      t.ray_scan = m->d_ray_scan;
     }
+    VDBG_TRY(launch_prep(m, *src, xyz, n, stride, t, flags, s, m->d_pts, m->d_rays, m->d_ray_scan, m->d_order,
+                         m->d_hist, m->d_cursor));
+    const RunBuffer rb = run_buffer(m->run_key, m->run_bits, m->run_slab, m->run_count, m->run_seg, m->dda_warps);
+    const int d        = run_dda_passes(m, *src, m->d_rays, m->d_order, n, t, rb, m->lstate, m->wstate, true, s);
+    if (d == VDBG_ERR_COORD_RANGE)
+      call_status = d;
+    else if (d != VDBG_OK)
+      return d;
   }
   std::vector<Channel*> todo;
   if (integrate_all)
@@ -817,7 +888,7 @@ const char* vdbg_status_string(int s)
     case VDBG_ERR_DUPLICATE_SOURCE: return "Source already registered";
     case VDBG_ERR_INVALID_ARGUMENT: return "Invalid argument";
     case VDBG_ERR_OUT_OF_MEMORY: return "Out of device memory (or over the map's memory budget)";
-    case VDBG_ERR_COORD_RANGE: return "Voxel index outside [-2^23, 2^23)";
+    case VDBG_ERR_COORD_RANGE: return "Voxel index outside [-2^21, 2^21)";
     case VDBG_ERR_CUDA: return "CUDA error";
     case VDBG_ERR_TIMEOUT: return "Bounded device wait gave up";
     case VDBG_ERR_BUFFER_TOO_SMALL: return "Buffer too small";
@@ -828,15 +899,25 @@ const char* vdbg_status_string(int s)
   }
 }
 
-int vdbg_create(double resolution, const vdbg_options* options, vdbg_map** out)
+} // extern "C"
+
+namespace {
+
+int create_impl(int n_maps, const double* resolutions, const vdbg_options* options, bool batch, vdbg_map** out)
 {
   if (!out) return VDBG_ERR_INVALID_ARGUMENT;
   *out = nullptr;
-  if (!(resolution > 0.0) || !std::isfinite(resolution)) return VDBG_ERR_INVALID_ARGUMENT;
-  vdbg_map* m  = new vdbg_map();
-  m->resolution = resolution;
-  m->half_res   = resolution / 2.0;
-  m->inv_res    = 1.0 / resolution;
+  if (n_maps < 1 || n_maps > kMaxMaps || !resolutions) return VDBG_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < n_maps; ++i)
+    if (!(resolutions[i] > 0.0) || !std::isfinite(resolutions[i])) return VDBG_ERR_INVALID_ARGUMENT;
+  vdbg_map* m = new vdbg_map();
+  m->conf.resize(static_cast<size_t>(n_maps));
+  for (int i = 0; i < n_maps; ++i)
+  {
+    m->conf[i].resolution = resolutions[i];
+    m->conf[i].half_res   = resolutions[i] / 2.0;
+    m->conf[i].inv_res    = 1.0 / resolutions[i];
+  }
   uint32_t cap  = kDefaultCapacity;
   uint32_t bcap = 0;
   if (options)
@@ -868,12 +949,25 @@ int vdbg_create(double resolution, const vdbg_options* options, vdbg_map** out)
   clear_status(m->h_status);
   int s = dev_alloc(m, &m->d_status, 1);
   if (s != VDBG_OK) return fail(s);
-  s = dev_alloc(m, &m->d_hist, kNumBuckets);
+  m->buckets = static_cast<uint32_t>(kBucketsPerScan) * static_cast<uint32_t>(n_maps);
+  s          = dev_alloc(m, &m->d_hist, m->buckets);
   if (s != VDBG_OK) return fail(s);
-  s = dev_alloc(m, &m->d_cursor, kNumBuckets);
+  s = dev_alloc(m, &m->d_cursor, m->buckets);
   if (s != VDBG_OK) return fail(s);
-  if (cudaMemsetAsync(m->d_hist, 0, kNumBuckets * sizeof(uint32_t), m->stream) != cudaSuccess)
+  if (cudaMemsetAsync(m->d_hist, 0, m->buckets * sizeof(uint32_t), m->stream) != cudaSuccess)
     return fail(VDBG_ERR_CUDA);
+  if (batch)
+  {
+    m->batch = true;
+    s        = dev_alloc(m, &m->d_lo, static_cast<size_t>(n_maps));
+    if (s == VDBG_OK) s = dev_alloc(m, &m->d_geom, static_cast<size_t>(n_maps));
+    if (s == VDBG_OK) s = dev_alloc(m, &m->d_first, static_cast<size_t>(n_maps) + 1);
+    if (s != VDBG_OK) return fail(s);
+    if (cudaMallocHost(reinterpret_cast<void**>(&m->h_geom), sizeof(ScanGeom) * n_maps) != cudaSuccess ||
+        cudaMallocHost(reinterpret_cast<void**>(&m->h_first), sizeof(uint32_t) * (n_maps + 1)) != cudaSuccess)
+      return fail(VDBG_ERR_OUT_OF_MEMORY);
+    if (cudaMemsetAsync(m->d_lo, 0, sizeof(LogOdds) * n_maps, m->stream) != cudaSuccess) return fail(VDBG_ERR_CUDA);
+  }
   s = resize_pool(m, cap, 0);
   if (s != VDBG_OK) return fail(s);
   // A block holds up to 512 leaves; maps fill blocks partly, so reserve one
@@ -883,6 +977,94 @@ int vdbg_create(double resolution, const vdbg_options* options, vdbg_map** out)
   if (cudaStreamSynchronize(m->stream) != cudaSuccess) return fail(VDBG_ERR_CUDA);
   *out = m;
   return VDBG_OK;
+}
+
+// setConfig of OccupancyVDBMapping.hpp:59-89 / VDBMapping.hpp:1456-1469 for map `i`.
+int set_config_impl(vdbg_map* m, int i, const vdbg_config* c)
+{
+  MapConf& mc = m->conf[i];
+  if (c->max_range < 0.0) return VDBG_ERR_BAD_RANGE;
+  mc.max_range           = c->max_range;
+  mc.fast_mode           = c->fast_mode != 0;
+  mc.accumulation_period = c->accumulation_period;
+  mc.config_set          = true;
+  if (c->prob_miss > 0.5) return VDBG_ERR_BAD_PROBABILITY;
+  if (c->prob_hit < 0.5) return VDBG_ERR_BAD_PROBABILITY;
+  mc.lo.miss      = static_cast<float>(std::log(c->prob_miss) - std::log(1 - c->prob_miss));
+  mc.lo.hit       = static_cast<float>(std::log(c->prob_hit) - std::log(1 - c->prob_hit));
+  mc.lo.thres_min = static_cast<float>(std::log(c->prob_thres_min) - std::log(1 - c->prob_thres_min));
+  mc.lo.thres_max = static_cast<float>(std::log(c->prob_thres_max) - std::log(1 - c->prob_thres_max));
+  mc.lo.max       = static_cast<float>(std::log(0.99) - std::log(0.01));
+  mc.lo.min       = static_cast<float>(std::log(0.01) - std::log(0.99));
+  if (m->batch)
+  {
+    VDBG_TRY(set_device(m));
+    VDBG_CUDA(cudaMemcpy(m->d_lo + i, &mc.lo, sizeof(LogOdds), cudaMemcpyHostToDevice));
+  }
+  return VDBG_OK;
+}
+
+// Leaves of map `map` (-1: all) that belong to the map, sorted by origin.
+int export_impl(vdbg_map* m, int map, int64_t capacity, int32_t* origins, float* values, uint64_t* masks,
+                int64_t* n_out, bool count_only)
+{
+  VDBG_TRY(set_device(m));
+  VDBG_CUDA(cudaStreamSynchronize(m->stream));
+  const uint32_t n = std::min(m->n_leaves, m->capacity);
+  std::vector<uint32_t> flags(n);
+  std::vector<int4> orig(n);
+  if (n)
+  {
+    VDBG_CUDA(cudaMemcpy(flags.data(), m->flags, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    VDBG_CUDA(cudaMemcpy(orig.data(), m->origin, n * sizeof(int4), cudaMemcpyDeviceToHost));
+  }
+  std::vector<uint32_t> idx;
+  idx.reserve(n);
+  for (uint32_t i = 0; i < n; ++i)
+    if (flags[i] && (map < 0 || orig[i].w == map)) idx.push_back(i);
+  *n_out = static_cast<int64_t>(idx.size());
+  if (count_only) return VDBG_OK;
+  std::sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) {
+    if (orig[a].x != orig[b].x) return orig[a].x < orig[b].x;
+    if (orig[a].y != orig[b].y) return orig[a].y < orig[b].y;
+    return orig[a].z < orig[b].z;
+  });
+  if (static_cast<int64_t>(idx.size()) > capacity) return VDBG_ERR_BUFFER_TOO_SMALL;
+  if (origins)
+  {
+    for (size_t k = 0; k < idx.size(); ++k)
+    {
+      origins[3 * k + 0] = orig[idx[k]].x;
+      origins[3 * k + 1] = orig[idx[k]].y;
+      origins[3 * k + 2] = orig[idx[k]].z;
+    }
+  }
+  if (values || masks)
+  {
+    std::vector<float> hv(values ? static_cast<size_t>(n) * 512 : 0);
+    std::vector<unsigned long long> hm(masks ? static_cast<size_t>(n) * 8 : 0);
+    if (values && n)
+      VDBG_CUDA(cudaMemcpy(hv.data(), m->values, static_cast<size_t>(n) * 512 * sizeof(float),
+                           cudaMemcpyDeviceToHost));
+    if (masks && n)
+      VDBG_CUDA(cudaMemcpy(hm.data(), m->active, static_cast<size_t>(n) * 8 * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < idx.size(); ++k)
+    {
+      if (values) std::memcpy(values + 512 * k, hv.data() + static_cast<size_t>(idx[k]) * 512, 512 * sizeof(float));
+      if (masks) std::memcpy(masks + 8 * k, hm.data() + static_cast<size_t>(idx[k]) * 8, 8 * sizeof(uint64_t));
+    }
+  }
+  return VDBG_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int vdbg_create(double resolution, const vdbg_options* options, vdbg_map** out)
+{
+  return create_impl(1, &resolution, options, false, out);
 }
 
 int vdbg_destroy(vdbg_map* m)
@@ -906,8 +1088,14 @@ int vdbg_destroy(vdbg_map* m)
   dev_free(m, m->bkeys, m->bhash_size);
   dev_free(m, m->bslots, m->bhash_size);
   dev_free(m, m->d_status, 1);
-  dev_free(m, m->d_hist, kNumBuckets);
-  dev_free(m, m->d_cursor, kNumBuckets);
+  dev_free(m, m->d_hist, m->buckets);
+  dev_free(m, m->d_cursor, m->buckets);
+  dev_free(m, m->d_lo, m->conf.size());
+  dev_free(m, m->d_geom, m->conf.size());
+  dev_free(m, m->d_first, m->conf.size() + 1);
+  dev_free(m, m->d_ray_scan, m->ray_cap);
+  if (m->h_geom) cudaFreeHost(m->h_geom);
+  if (m->h_first) cudaFreeHost(m->h_first);
   dev_free(m, m->d_pts, m->pts_cap);
   dev_free(m, m->d_rays, m->ray_cap);
   dev_free(m, m->d_order, m->ray_cap);
@@ -929,44 +1117,32 @@ int vdbg_destroy(vdbg_map* m)
 
 int vdbg_set_config(vdbg_map* m, const vdbg_config* c)
 {
-  if (!m || !c) return VDBG_ERR_INVALID_ARGUMENT;
-  if (c->max_range < 0.0) return VDBG_ERR_BAD_RANGE;
-  m->max_range           = c->max_range;
-  m->fast_mode           = c->fast_mode != 0;
-  m->accumulation_period = c->accumulation_period;
-  m->config_set          = true;
-  if (c->prob_miss > 0.5) return VDBG_ERR_BAD_PROBABILITY;
-  if (c->prob_hit < 0.5) return VDBG_ERR_BAD_PROBABILITY;
-  m->lo.miss      = static_cast<float>(std::log(c->prob_miss) - std::log(1 - c->prob_miss));
-  m->lo.hit       = static_cast<float>(std::log(c->prob_hit) - std::log(1 - c->prob_hit));
-  m->lo.thres_min = static_cast<float>(std::log(c->prob_thres_min) - std::log(1 - c->prob_thres_min));
-  m->lo.thres_max = static_cast<float>(std::log(c->prob_thres_max) - std::log(1 - c->prob_thres_max));
-  m->lo.max       = static_cast<float>(std::log(0.99) - std::log(0.01));
-  m->lo.min       = static_cast<float>(std::log(0.01) - std::log(0.99));
-  return VDBG_OK;
+  if (!m || !c || m->batch) return VDBG_ERR_INVALID_ARGUMENT;
+  return set_config_impl(m, 0, c);
 }
 
 int vdbg_get_log_odds(const vdbg_map* m, float out6[6])
 {
   if (!m || !out6) return VDBG_ERR_INVALID_ARGUMENT;
-  out6[0] = m->lo.hit;
-  out6[1] = m->lo.miss;
-  out6[2] = m->lo.thres_min;
-  out6[3] = m->lo.thres_max;
-  out6[4] = m->lo.max;
-  out6[5] = m->lo.min;
+  const LogOdds& lo = m->conf[0].lo;
+  out6[0] = lo.hit;
+  out6[1] = lo.miss;
+  out6[2] = lo.thres_min;
+  out6[3] = lo.thres_max;
+  out6[4] = lo.max;
+  out6[5] = lo.min;
   return VDBG_OK;
 }
 
 int vdbg_add_input_source(vdbg_map* m, const char* id, double max_range, double max_rate)
 {
   (void)max_rate;
-  if (!m || !id) return VDBG_ERR_INVALID_ARGUMENT;
+  if (!m || !id || m->batch) return VDBG_ERR_INVALID_ARGUMENT;
   if (find_channel(m, id)) return VDBG_ERR_DUPLICATE_SOURCE;
   VDBG_TRY(set_device(m));
   Channel c;
   c.id        = id;
-  c.max_range = (max_range == 0) ? m->max_range : max_range;
+  c.max_range = (max_range == 0) ? m->conf[0].max_range : max_range;
   int st      = alloc_channel_leaves(m, c, m->capacity);
   if (st == VDBG_OK) st = alloc_channel_blocks(m, c, m->bcapacity);
   if (st == VDBG_OK) st = dev_alloc(m, &c.n_touched, 1);
@@ -991,39 +1167,39 @@ int vdbg_add_input_source(vdbg_map* m, const char* id, double max_range, double 
 int vdbg_accumulate_update(vdbg_map* m, const float* xyz, int64_t n, int64_t stride, const double origin[3],
                            const char* id, uint32_t flags, void* stream, vdbg_scan_stats* stats)
 {
-  if (!m || !origin || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
+  if (!m || m->batch || !origin || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
   if (stats) std::memset(stats, 0, sizeof(*stats));
   Channel* src = find_channel(m, id);
   if (!src) return VDBG_ERR_UNKNOWN_SOURCE;
   if (!(src->max_range > 0)) return VDBG_OK;
-  if (!m->config_set) return VDBG_ERR_NOT_CONFIGURED;
-  return accumulate_and_integrate(m, xyz, n, stride, origin, src, src->max_range, flags, pick_stream(m, stream),
-                                  false, nullptr, stats);
+  if (!m->conf[0].config_set) return VDBG_ERR_NOT_CONFIGURED;
+  return accumulate_and_integrate(m, xyz, n, stride, plan_single(m, n, origin, src->max_range), src, flags,
+                                  pick_stream(m, stream), false, nullptr, stats);
 }
 
 int vdbg_integrate_update(vdbg_map* m, void* stream, vdbg_scan_stats* stats)
 {
-  if (!m) return VDBG_ERR_INVALID_ARGUMENT;
+  if (!m || m->batch) return VDBG_ERR_INVALID_ARGUMENT;
   if (stats) std::memset(stats, 0, sizeof(*stats));
-  return accumulate_and_integrate(m, nullptr, 0, 16, nullptr, nullptr, 0.0, 0, pick_stream(m, stream), true,
+  return accumulate_and_integrate(m, nullptr, 0, 16, CastPlan{}, nullptr, 0, pick_stream(m, stream), true,
                                   nullptr, stats);
 }
 
 int vdbg_insert_point_cloud(vdbg_map* m, const float* xyz, int64_t n, int64_t stride, const double origin[3],
                             const char* id, uint32_t flags, void* stream, vdbg_scan_stats* stats)
 {
-  if (!m || !origin || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
+  if (!m || m->batch || !origin || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
   if (stats) std::memset(stats, 0, sizeof(*stats));
   Channel* src  = find_channel(m, id);
   int pre       = VDBG_OK;
   if (!src)
     pre = VDBG_ERR_UNKNOWN_SOURCE;
-  else if (src->max_range > 0 && !m->config_set)
+  else if (src->max_range > 0 && !m->conf[0].config_set)
     pre = VDBG_ERR_NOT_CONFIGURED;
-  const bool cast = src && src->max_range > 0 && m->config_set;
-  const int r     = accumulate_and_integrate(m, xyz, n, stride, origin, cast ? src : nullptr,
-                                             cast ? src->max_range : 0.0, flags, pick_stream(m, stream), true,
-                                             nullptr, stats);
+  const bool cast     = src && src->max_range > 0 && m->conf[0].config_set;
+  const CastPlan plan = cast ? plan_single(m, n, origin, src->max_range) : CastPlan{};
+  const int r         = accumulate_and_integrate(m, xyz, n, stride, plan, cast ? src : nullptr, flags,
+                                                 pick_stream(m, stream), true, nullptr, stats);
   return r != VDBG_OK ? r : pre;
 }
 
@@ -1031,23 +1207,23 @@ int vdbg_raycast_point_cloud(vdbg_map* m, const float* xyz, int64_t n, int64_t s
                              double range, const char* id, uint32_t flags, void* stream,
                              vdbg_scan_stats* stats)
 {
-  if (!m || !origin || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
+  if (!m || m->batch || !origin || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
   if (stats) std::memset(stats, 0, sizeof(*stats));
-  if (!m->config_set) return VDBG_ERR_NOT_CONFIGURED;
+  if (!m->conf[0].config_set) return VDBG_ERR_NOT_CONFIGURED;
   Channel* src = find_channel(m, id);
   if (!src) return VDBG_ERR_UNKNOWN_SOURCE;
-  return accumulate_and_integrate(m, xyz, n, stride, origin, src, range, flags, pick_stream(m, stream), false,
-                                  nullptr, stats);
+  return accumulate_and_integrate(m, xyz, n, stride, plan_single(m, n, origin, range), src, flags,
+                                  pick_stream(m, stream), false, nullptr, stats);
 }
 
 int vdbg_update_map(vdbg_map* m, const char* id, void* stream, vdbg_scan_stats* stats)
 {
-  if (!m) return VDBG_ERR_INVALID_ARGUMENT;
+  if (!m || m->batch) return VDBG_ERR_INVALID_ARGUMENT;
   if (stats) std::memset(stats, 0, sizeof(*stats));
   Channel* src = find_channel(m, id);
   if (!src) return VDBG_ERR_UNKNOWN_SOURCE;
-  return accumulate_and_integrate(m, nullptr, 0, 16, nullptr, nullptr, 0.0, 0, pick_stream(m, stream), false,
-                                  src, stats);
+  return accumulate_and_integrate(m, nullptr, 0, 16, CastPlan{}, nullptr, 0, pick_stream(m, stream), false, src,
+                                  stats);
 }
 
 int vdbg_reset_map(vdbg_map* m)
@@ -1082,67 +1258,14 @@ int vdbg_reset_map(vdbg_map* m)
 int vdbg_leaf_count(vdbg_map* m, int64_t* out)
 {
   if (!m || !out) return VDBG_ERR_INVALID_ARGUMENT;
-  VDBG_TRY(set_device(m));
-  const uint32_t n = std::min(m->n_leaves, m->capacity);
-  std::vector<uint32_t> flags(n);
-  if (n) VDBG_CUDA(cudaMemcpy(flags.data(), m->flags, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-  int64_t c = 0;
-  for (uint32_t f : flags) c += (f != 0);
-  *out = c;
-  return VDBG_OK;
+  return export_impl(m, -1, 0, nullptr, nullptr, nullptr, out, true);
 }
 
 int vdbg_export_leaves(vdbg_map* m, int64_t capacity, int32_t* origins, float* values, uint64_t* masks,
                        int64_t* n_out)
 {
   if (!m || !n_out || capacity < 0) return VDBG_ERR_INVALID_ARGUMENT;
-  VDBG_TRY(set_device(m));
-  VDBG_CUDA(cudaStreamSynchronize(m->stream));
-  const uint32_t n = std::min(m->n_leaves, m->capacity);
-  std::vector<uint32_t> flags(n);
-  std::vector<int4> orig(n);
-  if (n)
-  {
-    VDBG_CUDA(cudaMemcpy(flags.data(), m->flags, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-    VDBG_CUDA(cudaMemcpy(orig.data(), m->origin, n * sizeof(int4), cudaMemcpyDeviceToHost));
-  }
-  std::vector<uint32_t> idx;
-  idx.reserve(n);
-  for (uint32_t i = 0; i < n; ++i)
-    if (flags[i]) idx.push_back(i);
-  std::sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) {
-    if (orig[a].x != orig[b].x) return orig[a].x < orig[b].x;
-    if (orig[a].y != orig[b].y) return orig[a].y < orig[b].y;
-    return orig[a].z < orig[b].z;
-  });
-  *n_out = static_cast<int64_t>(idx.size());
-  if (static_cast<int64_t>(idx.size()) > capacity) return VDBG_ERR_BUFFER_TOO_SMALL;
-  if (origins)
-  {
-    for (size_t k = 0; k < idx.size(); ++k)
-    {
-      origins[3 * k + 0] = orig[idx[k]].x;
-      origins[3 * k + 1] = orig[idx[k]].y;
-      origins[3 * k + 2] = orig[idx[k]].z;
-    }
-  }
-  if (values || masks)
-  {
-    std::vector<float> hv(values ? static_cast<size_t>(n) * 512 : 0);
-    std::vector<unsigned long long> hm(masks ? static_cast<size_t>(n) * 8 : 0);
-    if (values && n)
-      VDBG_CUDA(cudaMemcpy(hv.data(), m->values, static_cast<size_t>(n) * 512 * sizeof(float),
-                           cudaMemcpyDeviceToHost));
-    if (masks && n)
-      VDBG_CUDA(cudaMemcpy(hm.data(), m->active, static_cast<size_t>(n) * 8 * sizeof(unsigned long long),
-                           cudaMemcpyDeviceToHost));
-    for (size_t k = 0; k < idx.size(); ++k)
-    {
-      if (values) std::memcpy(values + 512 * k, hv.data() + static_cast<size_t>(idx[k]) * 512, 512 * sizeof(float));
-      if (masks) std::memcpy(masks + 8 * k, hm.data() + static_cast<size_t>(idx[k]) * 8, 8 * sizeof(uint64_t));
-    }
-  }
-  return VDBG_OK;
+  return export_impl(m, -1, capacity, origins, values, masks, n_out, false);
 }
 
 int vdbg_get_timings(const vdbg_map* m, vdbg_timings* out)
@@ -1158,6 +1281,97 @@ int vdbg_device_bytes(const vdbg_map* m, int64_t* out)
   if (!m || !out) return VDBG_ERR_INVALID_ARGUMENT;
   *out = m->bytes;
   return VDBG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batches of independent maps.
+// ---------------------------------------------------------------------------
+int vdbg_create_batch(int n_maps, const double* resolutions, const vdbg_options* options, vdbg_map** out)
+{
+  VDBG_TRY(create_impl(n_maps, resolutions, options, true, out));
+  vdbg_map* m = *out;
+  Channel c;
+  c.id   = "";
+  int st = alloc_channel_leaves(m, c, m->capacity);
+  if (st == VDBG_OK) st = alloc_channel_blocks(m, c, m->bcapacity);
+  if (st == VDBG_OK) st = dev_alloc(m, &c.n_touched, 1);
+  if (st == VDBG_OK) st = dev_alloc(m, &c.n_blist, 1);
+  if (st == VDBG_OK && (cudaMemsetAsync(c.n_touched, 0, sizeof(uint32_t), m->stream) != cudaSuccess ||
+                        cudaMemsetAsync(c.n_blist, 0, sizeof(uint32_t), m->stream) != cudaSuccess ||
+                        cudaStreamSynchronize(m->stream) != cudaSuccess))
+    st = VDBG_ERR_CUDA;
+  m->channels.push_back(c);  // freed by vdbg_destroy on failure too
+  if (st != VDBG_OK)
+  {
+    vdbg_destroy(m);
+    *out = nullptr;
+  }
+  return st;
+}
+
+int vdbg_batch_set_config(vdbg_map* m, int map, const vdbg_config* c)
+{
+  if (!m || !c || !m->batch || map < 0 || map >= static_cast<int>(m->conf.size())) return VDBG_ERR_INVALID_ARGUMENT;
+  return set_config_impl(m, map, c);
+}
+
+int vdbg_batch_insert(vdbg_map* m, const float* xyz, const int64_t* counts, int64_t stride, const double* origins,
+                      uint32_t flags, void* stream, vdbg_scan_stats* stats)
+{
+  if (!m || !m->batch || !counts || !origins) return VDBG_ERR_INVALID_ARGUMENT;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  const int nm  = static_cast<int>(m->conf.size());
+  int64_t total = 0;
+  for (int i = 0; i < nm; ++i)
+  {
+    if (counts[i] < 0) return VDBG_ERR_INVALID_ARGUMENT;
+    total += counts[i];
+  }
+  if (bad_points(xyz, total, stride)) return VDBG_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < nm; ++i)
+    if (counts[i] > 0 && !m->conf[i].config_set) return VDBG_ERR_NOT_CONFIGURED;
+  CastPlan plan;
+  m->h_first[0] = 0;
+  for (int i = 0; i < nm; ++i)
+  {
+    m->h_first[i + 1] = m->h_first[i] + static_cast<uint32_t>(counts[i]);
+    ScanGeom g{};
+    bool coord_range = false;
+    const double range = m->conf[i].max_range;
+    if (counts[i] > 0 && range > 0 && scan_geom_for(m, i, origins + 3 * i, range, &g, &coord_range))
+    {
+      plan.any = true;
+    }
+    else
+    {
+      // An origin outside the index range fails the whole batch unmarked, as
+      // an endpoint outside it does (k_prep).
+      if (coord_range) return VDBG_ERR_COORD_RANGE;
+      g     = ScanGeom{};
+      g.map = -1;
+    }
+    m->h_geom[i] = g;
+  }
+  if (nm == 1)
+    plan.table = single_table(m->h_geom[0]);
+  else
+    plan.table.n = nm;
+  return accumulate_and_integrate(m, xyz, total, stride, plan, &m->channels[0], flags, pick_stream(m, stream), true,
+                                  nullptr, stats);
+}
+
+int vdbg_batch_leaf_count(vdbg_map* m, int map, int64_t* out)
+{
+  if (!m || !out || map < 0 || map >= static_cast<int>(m->conf.size())) return VDBG_ERR_INVALID_ARGUMENT;
+  return export_impl(m, map, 0, nullptr, nullptr, nullptr, out, true);
+}
+
+int vdbg_batch_export_leaves(vdbg_map* m, int map, int64_t capacity, int32_t* origins, float* values,
+                             uint64_t* masks, int64_t* n_out)
+{
+  if (!m || !n_out || capacity < 0 || map < 0 || map >= static_cast<int>(m->conf.size()))
+    return VDBG_ERR_INVALID_ARGUMENT;
+  return export_impl(m, map, capacity, origins, values, masks, n_out, false);
 }
 
 } // extern "C"
@@ -1182,7 +1396,7 @@ constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 constexpr size_t kNoAllocPtsBytes   = align256(static_cast<size_t>(kNoAllocMaxPoints) * 16);
 constexpr size_t kNoAllocRaysBytes  = align256(static_cast<size_t>(kNoAllocMaxPoints) * sizeof(int4));
 constexpr size_t kNoAllocOrderBytes = align256(static_cast<size_t>(kNoAllocMaxPoints) * sizeof(int));
-constexpr size_t kNoAllocHistBytes  = align256(static_cast<size_t>(kNumBuckets) * sizeof(uint32_t));
+constexpr size_t kNoAllocHistBytes  = align256(static_cast<size_t>(kBucketsPerScan) * sizeof(uint32_t));
 constexpr size_t kNoAllocRunN       = static_cast<size_t>(kNoAllocWarps) * kNoAllocSeg;
 constexpr size_t kNoAllocKeyBytes   = align256(kNoAllocRunN * sizeof(unsigned long long));
 constexpr size_t kNoAllocSlabBytes  = align256(kNoAllocRunN);
@@ -1248,7 +1462,7 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
                                                const double origin[3], const char* id, uint32_t flags,
                                                void* stream, vdbg_scan_stats* stats)
 {
-  if (!m || !origin || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
+  if (!m || m->batch || !origin || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
   if (stats) std::memset(stats, 0, sizeof(*stats));
   const bool host_input = (flags & VDBG_POINTS_DEVICE) == 0;
   if (n > kNoAllocMaxPoints || (host_input && stride > 16)) return VDBG_ERR_SIZE_LIMIT;
@@ -1283,9 +1497,9 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
   int pre      = VDBG_OK;
   if (!src)
     pre = VDBG_ERR_UNKNOWN_SOURCE;
-  else if (src->max_range > 0 && !m->config_set)
+  else if (src->max_range > 0 && !m->conf[0].config_set)
     pre = VDBG_ERR_NOT_CONFIGURED;
-  const bool cast = src && src->max_range > 0 && m->config_set;
+  const bool cast = src && src->max_range > 0 && m->conf[0].config_set;
 
   VDBG_TRY(begin_call(m, s));
   const uint32_t leaves_before = m->n_leaves;
@@ -1295,15 +1509,14 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
   {
     // The histogram must start at zero; the previous call's contents remain.
     VDBG_CUDA(cudaMemsetAsync(d_hist, 0, kNoAllocHistBytes, s));
-    bool queued = false;
-    ScanGeom g{};
-    const int r = launch_prep(m, *src, xyz, n, stride, origin, src->max_range, flags, s, d_pts, d_rays, d_order,
-                              d_hist, d_cursor, &queued, &g);
-    if (r != VDBG_OK) return r;
-    if (queued)
+    const CastPlan plan = plan_single(m, n, origin, src->max_range);
+    if (plan.status != VDBG_OK) result = plan.status;
+    if (plan.any)
     {
+      VDBG_TRY(launch_prep(m, *src, xyz, n, stride, plan.table, flags, s, d_pts, d_rays, nullptr, d_order, d_hist,
+                           d_cursor));
       const RunBuffer rb = run_buffer(r_key, r_bits, r_slab, r_count, kNoAllocSeg, kNoAllocWarps);
-      dda                = run_dda_passes(m, *src, d_rays, d_order, n, g, rb, ls, ws, false, s);
+      dda                = run_dda_passes(m, *src, d_rays, d_order, n, plan.table, rb, ls, ws, false, s);
       if (dda == VDBG_ERR_COORD_RANGE)
       {
         result = dda;

@@ -324,3 +324,147 @@ class OccupancyVDBMapping:
             self._grid = Grid(np.zeros((0, 3), np.int32), np.zeros((0, 512), np.float32),
                               np.zeros((0, 8), np.uint64), owner=self, version=-1)
         return self._grid
+
+
+def _config_struct(config: Config):
+    c = _lib.vdbg_config()
+    c.max_range = config.max_range
+    c.fast_mode = 1 if config.fast_mode else 0
+    c.accumulation_period = config.accumulation_period
+    c.prob_hit = config.prob_hit
+    c.prob_miss = config.prob_miss
+    c.prob_thres_min = config.prob_thres_min
+    c.prob_thres_max = config.prob_thres_max
+    return c
+
+
+class MapBatch:
+    """Independent occupancy maps in one device pool, one scan per map per call.
+
+    No counterpart in the reference, which holds one OccupancyVDBMapping per
+    map: ``insert`` is ``insertPointCloud`` (VDBMapping.hpp:399-406) for every
+    map at once, with each map's own resolution and setConfig
+    (OccupancyVDBMapping.hpp:59-89). Each map's result equals inserting its
+    scan alone into its own map.
+    """
+
+    def __init__(self, resolutions, initial_leaf_capacity: int = 0, max_device_bytes: int = 0,
+                 device: int | None = None, initial_block_capacity: int = 0):
+        self._lib = _lib.load()
+        self.resolutions = [float(r) for r in resolutions]
+        opts = _lib.vdbg_options()
+        opts.initial_leaf_capacity = int(initial_leaf_capacity)
+        opts.initial_block_capacity = int(initial_block_capacity)
+        opts.max_device_bytes = int(max_device_bytes)
+        if device is None:
+            try:
+                import torch
+
+                device = torch.cuda.current_device() if torch.cuda.is_available() else 0
+            except Exception:  # pragma: no cover - torch is plumbing only
+                device = 0
+        opts.device = int(device)
+        res = (C.c_double * len(self.resolutions))(*self.resolutions)
+        h = C.c_void_p()
+        s = self._lib.vdbg_create_batch(len(self.resolutions), res, C.byref(opts), C.byref(h))
+        if s != 0:
+            raise VdbgError(s, "vdbg_create_batch")
+        self._h = h
+        self.last_stats = None
+
+    def __len__(self):
+        return len(self.resolutions)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.vdbg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, s, where):
+        if s != 0:
+            raise VdbgError(s, where)
+
+    def setConfig(self, map_index: int, config: Config) -> None:
+        c = _config_struct(config)
+        self._check(self._lib.vdbg_batch_set_config(self._h, int(map_index), C.byref(c)), "vdbg_batch_set_config")
+
+    def insert(self, clouds, origins, stream=None) -> dict:
+        """One scan per map: ``clouds[i]`` ((N,3)/(N,4) float32 host array, or None)
+        from ``origins[i]``. Returns the summed scan statistics."""
+        n_maps = len(self.resolutions)
+        if len(clouds) != n_maps or len(origins) != n_maps:
+            raise ValueError("one cloud and one origin per map")
+        parts, counts = [], []
+        for c in clouds:
+            if c is None:
+                counts.append(0)
+                continue
+            a = np.asarray(c, dtype=np.float32)
+            if a.ndim != 2 or a.shape[1] < 3:
+                raise ValueError("cloud must have shape (N, 3) or (N, 4)")
+            if a.shape[1] != 4:
+                a = np.concatenate([a[:, :3], np.zeros((a.shape[0], 1), np.float32)], axis=1)
+            parts.append(np.ascontiguousarray(a))
+            counts.append(a.shape[0])
+        pts = np.concatenate(parts) if parts else np.zeros((0, 4), np.float32)
+        return self.insert_packed(pts, counts, origins, stream=stream)
+
+    def insert_packed(self, pts, counts, origins, stream=None) -> dict:
+        """``pts``: (sum(counts), 4) float32 host array (or CUDA tensor) holding
+        the maps' scans back to back in map order."""
+        ptr, n, stride, flags, keep = _cloud_args(pts)
+        cnt = (C.c_int64 * len(counts))(*[int(c) for c in counts])
+        if n != sum(int(c) for c in counts):
+            raise ValueError("counts do not add up to the number of points")
+        org = (C.c_double * (3 * len(origins)))(*[float(v) for o in origins for v in o])
+        st = _lib.vdbg_scan_stats()
+        s = self._lib.vdbg_batch_insert(self._h, C.c_void_p(ptr), cnt, stride, org, flags,
+                                        C.c_void_p(stream) if stream else None, C.byref(st))
+        del keep
+        self.last_stats = st.as_dict()
+        self._check(s, "vdbg_batch_insert")
+        return self.last_stats
+
+    def leafCount(self, map_index: int) -> int:
+        n = C.c_int64()
+        self._check(self._lib.vdbg_batch_leaf_count(self._h, int(map_index), C.byref(n)), "vdbg_batch_leaf_count")
+        return n.value
+
+    def exportLeaves(self, map_index: int):
+        """(origins, values, masks) of one map, sorted by leaf origin."""
+        n = C.c_int64()
+        cap = self.leafCount(map_index)
+        while True:
+            origins = np.zeros((cap, 3), np.int32)
+            values = np.zeros((cap, 512), np.float32)
+            masks = np.zeros((cap, 8), np.uint64)
+            s = self._lib.vdbg_batch_export_leaves(self._h, int(map_index), cap, origins.ctypes.data,
+                                                   values.ctypes.data, masks.ctypes.data, C.byref(n))
+            if s == _lib.STATUS_CODE["VDBG_ERR_BUFFER_TOO_SMALL"]:
+                cap = n.value
+                continue
+            self._check(s, "vdbg_batch_export_leaves")
+            k = n.value
+            return origins[:k], values[:k], masks[:k]
+
+    def timings(self) -> dict:
+        t = _lib.vdbg_timings()
+        self._check(self._lib.vdbg_get_timings(self._h, C.byref(t)), "vdbg_get_timings")
+        return t.as_dict()
+
+    def deviceBytes(self) -> int:
+        n = C.c_int64()
+        self._check(self._lib.vdbg_device_bytes(self._h, C.byref(n)), "vdbg_device_bytes")
+        return n.value

@@ -15,6 +15,12 @@ pcl::PointXYZ (x, y, z, pad) rows of 16 bytes.
           log-uniform ranges 0.5-200 m from (5000,-3000,40); 1% of endpoints
           on quantiser boundaries and DDA tie directions; voxel 0.02 m,
           max_range 250 m.
+  batched seed 4: 32 independent maps, one scan each per step, 50 steps.
+          Points per scan log-uniform over 2,000-307,200 (mean about 60.6k).
+          A map is a depth camera (640x480 pixels, 90x60 deg field of view,
+          subsampled to its point count, max_range 5 m) or a spinning LiDAR
+          (rows x cols beams, max_range 30-60 m), in its own seeded room of
+          boxes; voxel size drawn from {0.02, 0.05, 0.1, 0.2} m.
 
 A no-return beam gets its endpoint at twice the max range along the beam, so
 the reference's strict `length > max_range` clip turns it into free space.
@@ -265,6 +271,83 @@ class StressWorkload(Workload):
         return pts, o
 
 
+def depth_directions(n: int, fov_h=90.0, fov_v=60.0, yaw=0.0, pitch=0.0) -> np.ndarray:
+    """Unit rays of a pinhole depth camera subsampled to about n pixels of a
+    640x480 image (4:3 grid), looking along yaw/pitch (degrees)."""
+    w = max(4, min(640, int(round(np.sqrt(n * 4.0 / 3.0)))))
+    h = max(3, min(480, int(np.ceil(n / w))))
+    tx = np.tan(np.deg2rad(fov_h / 2)) * np.linspace(-1, 1, w)
+    ty = np.tan(np.deg2rad(fov_v / 2)) * np.linspace(-1, 1, h)
+    gx, gy = np.meshgrid(tx, ty)
+    d = np.stack([np.ones_like(gx), gx, gy], axis=-1).reshape(-1, 3)[:n]
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    cy, sy, cp, sp = np.cos(np.deg2rad(yaw)), np.sin(np.deg2rad(yaw)), np.cos(np.deg2rad(pitch)), np.sin(np.deg2rad(pitch))
+    rot = np.array([[cy * cp, -sy, -cy * sp], [sy * cp, cy, -sy * sp], [sp, 0.0, cp]])
+    return d @ rot.T
+
+
+class BatchedWorkload:
+    """Independent maps of mixed sensors, one scan per map per step."""
+
+    VOXELS = (0.02, 0.05, 0.1, 0.2)
+
+    def __init__(self, name="batched", seed=4, n_maps=32, n_steps=50, n_min=2000, n_max=307200):
+        self.name, self.seed, self.n_maps, self.n_steps = name, seed, n_maps, n_steps
+        rng = np.random.default_rng(seed)
+        self.maps = []
+        for i in range(n_maps):
+            n = int(round(np.exp(rng.uniform(np.log(n_min), np.log(n_max)))))
+            depth = bool(rng.random() < 0.5)
+            res = float(rng.choice(self.VOXELS))
+            if depth:
+                max_range = 5.0
+                room = RoomWorkload(seed=1000 + i, n_boxes=20)
+                dirs = depth_directions(n, yaw=rng.uniform(0, 360), pitch=rng.uniform(-20, 5))
+            else:
+                max_range = float(rng.uniform(30.0, 60.0))
+                room = RoomWorkload(seed=1000 + i, n_boxes=30)
+                room.lo, room.hi = np.array([-45.0, -45.0, 0.0]), np.array([45.0, 45.0, 12.0])
+                rows = int(rng.choice([16, 32, 64, 128]))
+                cols = max(8, n // rows)
+                dirs = lidar_directions(rows, cols)[:n]
+            self.maps.append(dict(n=dirs.shape[0], depth=depth, resolution=res, max_range=max_range, room=room,
+                                  dirs=dirs, sigma=0.01, no_return=0.03, speed=rng.uniform(0.02, 0.2),
+                                  heading=rng.uniform(0, 2 * np.pi)))
+        self.resolutions = [m["resolution"] for m in self.maps]
+        self.configs = [default_config(m["max_range"]) for m in self.maps]
+        self.points_per_step = sum(m["n"] for m in self.maps)
+
+    def origin(self, i, k):
+        m = self.maps[i]
+        step = m["speed"] * k
+        return np.array([step * np.cos(m["heading"]), step * np.sin(m["heading"]), 1.2 + 0.01 * (i % 7)])
+
+    def scan(self, i, k):
+        """(points (N,4) float32, origin (3,) float64) of map i at step k."""
+        m = self.maps[i]
+        o = self.origin(i, k)
+        d = m["dirs"]
+        room = m["room"]
+        t = np.full(d.shape[0], np.inf)
+        _hit_room_inside(o, d, room.lo, room.hi, t)
+        _hit_boxes(o, d, room.boxes, t)
+        rng = np.random.default_rng([self.seed, i, k])
+        r = t + rng.normal(0.0, m["sigma"], t.shape)
+        lost = (rng.random(t.shape) < m["no_return"]) | ~np.isfinite(t)
+        r = np.where(lost, 2.0 * m["max_range"], r)
+        return _to_pcl(o, d, r), o
+
+    def step(self, k):
+        """[(points, origin)] of every map at step k."""
+        return [self.scan(i, k) for i in range(self.n_maps)]
+
+    def describe(self) -> dict:
+        return {"workload": self.name, "maps": self.n_maps, "steps": self.n_steps,
+                "points_per_step": self.points_per_step, "seed": self.seed,
+                "depth_maps": sum(m["depth"] for m in self.maps),
+                "voxels_m": sorted(set(self.resolutions))}
+
+
 def get(name: str) -> Workload:
     if name == "small":
         return RoomWorkload()
@@ -272,4 +355,6 @@ def get(name: str) -> Workload:
         return StreetWorkload()
     if name == "stress":
         return StressWorkload()
+    if name == "batched":
+        return BatchedWorkload()
     raise KeyError(name)
