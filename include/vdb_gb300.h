@@ -36,7 +36,8 @@ enum vdbg_status
   VDBG_ERR_CUDA             = 9,
   VDBG_ERR_TIMEOUT          = 10, /* a bounded device wait gave up */
   VDBG_ERR_BUFFER_TOO_SMALL = 11,
-  VDBG_ERR_SIZE_LIMIT       = 12  /* input larger than a fixed-size entry point accepts */
+  VDBG_ERR_SIZE_LIMIT       = 12, /* input larger than a fixed-size entry point accepts */
+  VDBG_ERR_BUSY             = 13  /* a serving queue is full; submit again later */
 };
 
 /* Input flags. */
@@ -216,6 +217,68 @@ int vdbg_batch_insert(vdbg_map* batch, const float* xyz, const int64_t* counts, 
 int vdbg_batch_leaf_count(vdbg_map* batch, int map, int64_t* out);
 int vdbg_batch_export_leaves(vdbg_map* batch, int map, int64_t capacity, int32_t* origins, float* values,
                              uint64_t* masks, int64_t* n_out);
+
+/* Serving loop over a batch (continuous batching). No counterpart in the
+ * reference, whose per-source worker threads (VDBMapping.hpp:1383-1430) each
+ * feed one map. One worker thread serves every sensor stream of a batch:
+ * vdbg_server_submit copies a scan into pinned staging and queues it on its
+ * map's FIFO without waiting for the GPU; the worker forms every step from
+ * the oldest queued scan of each map (so a map's scans apply in submission
+ * order), admits them against memory_budget_bytes (a scan whose map would
+ * need the pool to grow past the budget waits for a step of its own, and is
+ * completed with VDBG_ERR_OUT_OF_MEMORY if even then it does not fit), and
+ * inserts them with one batched call; scans arriving meanwhile join the next
+ * step. A scan's result is the same whatever it shares a step with. While a
+ * server runs, only the server calls may touch its batch; destroy the server
+ * before using the batch directly again. */
+typedef struct vdbg_server vdbg_server;
+
+typedef struct vdbg_server_options
+{
+  int64_t memory_budget_bytes; /* device bytes the batch may hold (0: no budget) */
+  int32_t max_batch_maps;      /* most maps per step (0: all) */
+  int32_t queue_capacity;      /* most queued scans before submit returns VDBG_ERR_BUSY (0: 4096) */
+} vdbg_server_options;
+
+typedef struct vdbg_server_result
+{
+  uint64_t tag;        /* the caller's tag of the request */
+  int32_t map;
+  int32_t status;      /* VDBG_OK or the batched call's status */
+  int64_t points;
+  int64_t submit_ns;   /* steady-clock times: queued, step started, step done */
+  int64_t start_ns;
+  int64_t done_ns;
+  int32_t batch_maps;  /* scans in the step that served it */
+  int32_t reserved0;
+} vdbg_server_result;
+
+typedef struct vdbg_server_stats
+{
+  int64_t requests_submitted;
+  int64_t requests_done;
+  int64_t rejected;      /* completed with VDBG_ERR_OUT_OF_MEMORY by admission */
+  int64_t steps;
+  int64_t max_step_maps;
+  int64_t queued;
+  int64_t max_queued;
+  uint64_t rays;
+  uint64_t updates;
+  int64_t busy_ns;       /* time spent in batched calls */
+  int64_t device_bytes;
+} vdbg_server_stats;
+
+int vdbg_server_create(vdbg_map* batch, const vdbg_server_options* options, vdbg_server** out);
+/* Queues one scan of map `map` (n points stride_bytes apart, host memory). */
+int vdbg_server_submit(vdbg_server* server, int map, const float* xyz, int64_t n, int64_t stride_bytes,
+                       const double origin[3], uint64_t tag);
+/* Up to `capacity` completed requests, waiting up to wait_ms for the first. */
+int vdbg_server_poll(vdbg_server* server, vdbg_server_result* out, int capacity, int wait_ms, int* n_out);
+/* Waits (up to wait_ms) until every submitted scan has completed. */
+int vdbg_server_drain(vdbg_server* server, int wait_ms);
+int vdbg_server_get_stats(vdbg_server* server, vdbg_server_stats* out);
+/* Completes the queued scans, stops the worker and frees the server (not the batch). */
+int vdbg_server_destroy(vdbg_server* server);
 
 /* Human-readable text of a status code (static storage). */
 const char* vdbg_status_string(int status);

@@ -28,6 +28,7 @@ STATUS = {
     10: "VDBG_ERR_TIMEOUT",
     11: "VDBG_ERR_BUFFER_TOO_SMALL",
     12: "VDBG_ERR_SIZE_LIMIT",
+    13: "VDBG_ERR_BUSY",
 }
 STATUS_CODE = {v: k for k, v in STATUS.items()}
 
@@ -86,6 +87,50 @@ class vdbg_timings(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved0"}
 
 
+class vdbg_server_options(C.Structure):
+    _fields_ = [
+        ("memory_budget_bytes", C.c_int64),
+        ("max_batch_maps", C.c_int32),
+        ("queue_capacity", C.c_int32),
+    ]
+
+
+class vdbg_server_result(C.Structure):
+    _fields_ = [
+        ("tag", C.c_uint64),
+        ("map", C.c_int32),
+        ("status", C.c_int32),
+        ("points", C.c_int64),
+        ("submit_ns", C.c_int64),
+        ("start_ns", C.c_int64),
+        ("done_ns", C.c_int64),
+        ("batch_maps", C.c_int32),
+        ("reserved0", C.c_int32),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved0"}
+
+
+class vdbg_server_stats(C.Structure):
+    _fields_ = [
+        ("requests_submitted", C.c_int64),
+        ("requests_done", C.c_int64),
+        ("rejected", C.c_int64),
+        ("steps", C.c_int64),
+        ("max_step_maps", C.c_int64),
+        ("queued", C.c_int64),
+        ("max_queued", C.c_int64),
+        ("rays", C.c_uint64),
+        ("updates", C.c_uint64),
+        ("busy_ns", C.c_int64),
+        ("device_bytes", C.c_int64),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 # (name, restype, argtypes) of every exported entry point.
 _P = C.c_void_p
 _D3 = C.POINTER(C.c_double)
@@ -118,6 +163,12 @@ SIGNATURES = [
       C.POINTER(vdbg_scan_stats)]),
     ("vdbg_batch_leaf_count", C.c_int, [_P, C.c_int, C.POINTER(C.c_int64)]),
     ("vdbg_batch_export_leaves", C.c_int, [_P, C.c_int, C.c_int64, _P, _P, _P, C.POINTER(C.c_int64)]),
+    ("vdbg_server_create", C.c_int, [_P, C.POINTER(vdbg_server_options), C.POINTER(_P)]),
+    ("vdbg_server_submit", C.c_int, [_P, C.c_int, _P, C.c_int64, C.c_int64, C.POINTER(C.c_double), C.c_uint64]),
+    ("vdbg_server_poll", C.c_int, [_P, C.POINTER(vdbg_server_result), C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    ("vdbg_server_drain", C.c_int, [_P, C.c_int]),
+    ("vdbg_server_get_stats", C.c_int, [_P, C.POINTER(vdbg_server_stats)]),
+    ("vdbg_server_destroy", C.c_int, [_P]),
     ("vdbg_status_string", C.c_char_p, [C.c_int]),
 ]
 

@@ -254,11 +254,14 @@ __global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, 
 //
 // A ray is monotone in every axis, so it visits each x-slab of each 8^3 leaf
 // (64 voxels, one mask word) in a single contiguous run. The lane keeps the
-// bits of the current run in a register and appends each finished run to its
-// private ring in shared memory. Every kDdaSteps steps the warp copies all
-// rings to its segment of the run buffer in one coalesced pass; k_apply_runs
-// merges and applies them. Rays come from the length-then-direction order in
-// short runs per warp (ray_bin), so a segment holds runs of neighbouring rays.
+// bits of the current run in a register; a run is emitted at the first step
+// that leaves it (or after the ray's last voxel). Each step the warp ranks
+// its emitting lanes with one ballot and appends their runs to the warp's
+// record list in shared memory, packed in step order; every kDdaSteps steps
+// the list is copied to the warp's segment of the run buffer with plain
+// coalesced stores, and k_apply_runs merges and applies the segments. Rays
+// come from the length-then-direction order in short runs per warp
+// (ray_bucket), so a segment holds runs of neighbouring rays.
 //
 // A pass ends for a warp when its segment cannot take another round: the
 // lanes' DDA state and the warp's ray run are saved and the next pass
@@ -266,16 +269,15 @@ __global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, 
 // ---------------------------------------------------------------------------
 constexpr int kDdaWarps      = 2;                // warps per block
 constexpr int kDdaSteps      = 16;               // DDA steps between ring copies
-constexpr int kDdaRing       = kDdaSteps + 1;    // a step closes at most one run, the last one two
+constexpr int kDdaRing       = kDdaSteps + 1;    // emissions per lane per round: one per step + the flush
 constexpr uint32_t kDdaRound = 32u * kDdaRing;   // most runs a warp writes per round
 constexpr uint32_t kDdaChunk = 16;               // rays a warp takes from the binned order at a time
 
 struct DdaWarpSmem
 {
-  unsigned long long keys[kDdaRing][32];  // leaf key of the run
-  unsigned long long bits[kDdaRing][32];  // visited voxels of the slab
-  unsigned char slab[kDdaRing][32];       // x & 7 of the slab
-  uint32_t incl[32];                      // inclusive prefix of the lanes' run counts
+  unsigned long long keys[kDdaRound];  // leaf key of the run
+  unsigned long long bits[kDdaRound];  // visited voxels of the slab
+  unsigned char slab[kDdaRound];       // x & 7 of the slab
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt()
@@ -285,39 +287,22 @@ __device__ __forceinline__ uint32_t lanemask_lt()
   return m;
 }
 
-// Copies the lanes' rings to positions [pos, pos + total) of the run buffer,
-// coalesced (record j of the warp goes to pos + j). Returns total.
-__device__ __forceinline__ uint32_t dda_write_runs(DdaWarpSmem& q, int lane, int n_rec, const RunBuffer& rb,
-                                                   size_t pos)
+// Emits the lane's open run when `close` (ranked among the warp's emitting
+// lanes by one ballot) at position *n of the warp's record list.
+__device__ __forceinline__ void dda_emit(DdaWarpSmem& q, bool close, int map, int rx, int ry, int rz,
+                                         unsigned long long& run, bool& run_open, uint32_t& n)
 {
-  uint32_t incl = static_cast<uint32_t>(n_rec);
-  for (int off = 1; off < 32; off <<= 1)
+  const unsigned em = __ballot_sync(0xffffffffu, close);
+  if (close)
   {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, off);
-    if (lane >= off) incl += y;
+    const uint32_t p = n + static_cast<uint32_t>(__popc(em & lanemask_lt()));
+    q.keys[p]        = pack_leaf_key(map, rx >> 3, ry, rz);
+    q.bits[p]        = run;
+    q.slab[p]        = static_cast<unsigned char>(rx & 7);
+    run              = 0ull;
+    run_open         = false;
   }
-  q.incl[lane]         = incl;
-  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-  __syncwarp();
-  for (uint32_t j = static_cast<uint32_t>(lane); j < total; j += 32)
-  {
-    // Owner lane of record j: the first lane whose inclusive prefix exceeds j.
-    int lo = 0, hi = 31;
-    while (lo < hi)
-    {
-      const int mid = (lo + hi) >> 1;
-      if (q.incl[mid] > j)
-        hi = mid;
-      else
-        lo = mid + 1;
-    }
-    const uint32_t r    = j - (lo > 0 ? q.incl[lo - 1] : 0u);
-    rb.key[pos + j]     = q.keys[r][lo];
-    rb.bits[pos + j]    = q.bits[r][lo];
-    rb.slab[pos + j]    = q.slab[r][lo];
-  }
-  __syncwarp();
-  return total;
+  n += static_cast<uint32_t>(__popc(em));
 }
 
 __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __restrict__ rays,
@@ -344,7 +329,6 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
   int rx = 0, ry = 0, rz = 0;  // current run: exact x, leaf y, leaf z
   int map = 0;                 // map of the lane's ray
   unsigned long long run = 0ull;
-  int n_rec       = 0;
   uint32_t budget = 0;
   if (resume)
   {
@@ -460,22 +444,18 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
       break;
     }
 
-    // ---- DDA steps (no warp votes inside) --------------------------------------
+    // ---- DDA steps ----------------------------------------------------------------
+    uint32_t n_rec = 0;  // records of this round in the warp's list
 #pragma unroll 4
     for (int s = 0; s < kDdaSteps; ++s)
     {
+      // setActiveState(voxel) on the update grid, one slab run at a time: the
+      // run of the previous step ends when the voxel leaves it or the ray ended.
+      const int ly = vy >> 3, lz = vz >> 3;
+      dda_emit(q, run_open && (!has_ray || vx != rx || ly != ry || lz != rz), map, rx, ry, rz, run, run_open,
+               n_rec);
       if (has_ray)
       {
-        // setActiveState(voxel) on the update grid, one slab run at a time.
-        const int ly = vy >> 3, lz = vz >> 3;
-        if (run_open && (vx != rx || ly != ry || lz != rz))
-        {
-          q.keys[n_rec][lane] = pack_leaf_key(map, rx >> 3, ry, rz);
-          q.bits[n_rec][lane] = run;
-          q.slab[n_rec][lane] = static_cast<unsigned char>(rx & 7);
-          ++n_rec;
-          run = 0ull;
-        }
         rx       = vx;
         ry       = ly;
         rz       = lz;
@@ -501,23 +481,23 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
           atomicOr(&m.st->error, kErrStepBound);
           fin = true;
         }
-        if (fin)
-        {
-          q.keys[n_rec][lane] = pack_leaf_key(map, rx >> 3, ry, rz);
-          q.bits[n_rec][lane] = run;
-          q.slab[n_rec][lane] = static_cast<unsigned char>(rx & 7);
-          ++n_rec;
-          run      = 0ull;
-          run_open = false;
-          has_ray  = false;
-        }
+        if (fin) has_ray = false;  // its last run is emitted next step
       }
     }
+    // Runs of rays that ended in the last step (a refill must not find them open).
+    dda_emit(q, run_open && !has_ray, map, rx, ry, rz, run, run_open, n_rec);
 
-    // ---- copy the rings to the warp's segment ------------------------------------
+    // ---- copy the list to the warp's segment -------------------------------------
     __syncwarp();
-    count += dda_write_runs(q, lane, n_rec, rb, seg0 + count);
-    n_rec = 0;
+    const size_t pos = seg0 + count;
+    for (uint32_t j = static_cast<uint32_t>(lane); j < n_rec; j += 32)
+    {
+      rb.key[pos + j]  = q.keys[j];
+      rb.bits[pos + j] = q.bits[j];
+      rb.slab[pos + j] = q.slab[j];
+    }
+    __syncwarp();
+    count += n_rec;
   }
 
   // ---- end of the pass: record the segment and what is left in flight ------------
@@ -555,11 +535,14 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
 //
 // Persistent blocks take chunks of kApplyChunk runs (written together by
 // warps walking neighbouring rays, so a chunk repeats few leaves). Each thread
-// ORs its runs into the block's leaf table in shared memory; the block then
-// drains the table: one thread per distinct leaf resolves its slot through the
-// block index (allocating leaves and blocks as needed), marks it touched and
-// ORs the non-zero words into the update masks. A run that finds the table
-// full is applied directly.
+// ORs its runs into the block's leaf table in shared memory (the lanes of a
+// warp holding the same leaf probe it once, through their leader); the first
+// insertion of a leaf appends it to the table's list. The block then drains
+// the list in two steps: one thread per listed leaf resolves its slot through
+// the block index (allocating leaves and blocks as needed) and marks it
+// touched, then eight threads per leaf OR its eight mask words into the update
+// masks, so the words of one leaf go out as one coalesced atomic request. A
+// run that finds the table full is applied directly.
 // ---------------------------------------------------------------------------
 constexpr int kApplyThreads = 256;
 constexpr int kApplyChunk   = 4096;
@@ -569,6 +552,8 @@ struct ApplySmem
 {
   unsigned long long key[kApplyTable];
   unsigned int words[kApplyTable][16];  // 8 mask words as lo/hi halves
+  int slot[kApplyTable];                // resolved leaf slot of a listed entry
+  unsigned short list[kApplyTable];     // entries in use
   unsigned int count;
 };
 
@@ -595,14 +580,22 @@ __device__ __forceinline__ int apply_resolve(const MapView& m, const ChannelView
 __global__ void __launch_bounds__(kApplyThreads, 4) k_apply_runs(RunBuffer rb, MapView m, ChannelView c)
 {
   __shared__ ApplySmem t;
-  if (ld_relaxed_u32(&m.st->error) != 0u) return;
+  __shared__ uint32_t failed;
+  // The error word can be set by other blocks while this one starts: read it
+  // once for the whole block, so that either every thread returns or none
+  // does (the barriers below need all of them).
+  if (threadIdx.x == 0) failed = ld_relaxed_u32(&m.st->error);
+  __syncthreads();
+  if (failed != 0u) return;
   for (int e = threadIdx.x; e < kApplyTable; e += kApplyThreads)
   {
     t.key[e] = kEmptyKey;
 #pragma unroll
     for (int w = 0; w < 16; ++w) t.words[e][w] = 0u;
   }
+  if (threadIdx.x == 0) t.count = 0u;
   __syncthreads();
+  const int lane = static_cast<int>(threadIdx.x & 31);
   // Work items: (segment, chunk of kApplyChunk runs), segment-major.
   const uint32_t chunks_per_seg = (rb.seg + kApplyChunk - 1) / kApplyChunk;
   const uint32_t items          = rb.warps * chunks_per_seg;
@@ -614,31 +607,53 @@ __global__ void __launch_bounds__(kApplyThreads, 4) k_apply_runs(RunBuffer rb, M
     if (start >= cnt) continue;  // uniform across the block
     const size_t base  = static_cast<size_t>(sg) * rb.seg;
     const uint32_t end = min(start + kApplyChunk, cnt);
-    for (uint32_t i = start + threadIdx.x; i < end; i += kApplyThreads)
+    // Whole warps walk the chunk (tail lanes idle) so the match below sees full warps.
+    for (uint32_t i0 = start + (threadIdx.x & ~31u); i0 < end; i0 += kApplyThreads)
     {
-      const unsigned long long key  = rb.key[base + i];
-      const unsigned long long bits = rb.bits[base + i];
-      const int w                   = rb.slab[base + i];
-      uint32_t h                    = apply_hash(key);
-      bool done                     = false;
-      for (int probe = 0; probe < 16 && !done; ++probe)
+      const uint32_t i              = i0 + static_cast<uint32_t>(lane);
+      const bool have               = i < end;
+      const unsigned long long key  = have ? rb.key[base + i] : kEmptyKey;
+      const unsigned long long bits = have ? rb.bits[base + i] : 0ull;
+      const int w                   = have ? rb.slab[base + i] : 0;
+      const unsigned peers          = __match_any_sync(0xffffffffu, key);
+      const int leader              = __ffs(peers) - 1;
+      int h                         = -1;
+      if (have && lane == leader)
       {
-        unsigned long long k = t.key[h];
-        if (k == kEmptyKey)
+        uint32_t p = apply_hash(key);
+        for (int probe = 0; probe < 16; ++probe)
         {
-          const unsigned long long prev = atomicCAS(&t.key[h], kEmptyKey, key);
-          k                             = (prev == kEmptyKey) ? key : prev;
+          unsigned long long k = t.key[p];
+          if (k == kEmptyKey)
+          {
+            const unsigned long long prev = atomicCAS(&t.key[p], kEmptyKey, key);
+            if (prev == kEmptyKey)
+            {
+              t.list[atomicAdd(&t.count, 1u)] = static_cast<unsigned short>(p);
+              k                                = key;
+            }
+            else
+            {
+              k = prev;
+            }
+          }
+          if (k == key)
+          {
+            h = static_cast<int>(p);
+            break;
+          }
+          p = (p + 1) & (kApplyTable - 1);
         }
-        if (k == key)
-        {
-          const unsigned int lo = static_cast<unsigned int>(bits), hi = static_cast<unsigned int>(bits >> 32);
-          if (lo) atomicOr(&t.words[h][2 * w], lo);
-          if (hi) atomicOr(&t.words[h][2 * w + 1], hi);
-          done = true;
-        }
-        h = (h + 1) & (kApplyTable - 1);
       }
-      if (!done)
+      h = __shfl_sync(0xffffffffu, h, leader);
+      if (!have) continue;
+      if (h >= 0)
+      {
+        const unsigned int lo = static_cast<unsigned int>(bits), hi = static_cast<unsigned int>(bits >> 32);
+        if (lo) atomicOr(&t.words[h][2 * w], lo);
+        if (hi) atomicOr(&t.words[h][2 * w + 1], hi);
+      }
+      else
       {
         // Table crowded: apply this run directly.
         const int slot = apply_resolve(m, c, key);
@@ -646,26 +661,27 @@ __global__ void __launch_bounds__(kApplyThreads, 4) k_apply_runs(RunBuffer rb, M
       }
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < kApplyTable; e += kApplyThreads)
+    const uint32_t n_used = t.count;
+    for (uint32_t k = threadIdx.x; k < n_used; k += kApplyThreads)
     {
-      const unsigned long long key = t.key[e];
-      if (key == kEmptyKey) continue;
-      const int slot = apply_resolve(m, c, key);
-      if (slot >= 0)
-      {
-        unsigned long long* u = c.upd + static_cast<size_t>(slot) * 16;
-#pragma unroll
-        for (int w = 0; w < 8; ++w)
-        {
-          const unsigned long long b =
-            (static_cast<unsigned long long>(t.words[e][2 * w + 1]) << 32) | t.words[e][2 * w];
-          if (b) atomicOr(u + w, b);
-        }
-      }
-      t.key[e] = kEmptyKey;
-#pragma unroll
-      for (int w = 0; w < 16; ++w) t.words[e][w] = 0u;
+      const int e = t.list[k];
+      t.slot[e]   = apply_resolve(m, c, t.key[e]);
     }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < n_used * 8u; k += kApplyThreads)
+    {
+      const int e    = t.list[k >> 3];
+      const int w    = static_cast<int>(k & 7u);
+      const int slot = t.slot[e];
+      const unsigned long long b =
+        (static_cast<unsigned long long>(t.words[e][2 * w + 1]) << 32) | t.words[e][2 * w];
+      if (slot >= 0 && b) atomicOr(c.upd + static_cast<size_t>(slot) * 16 + w, b);
+      t.words[e][2 * w]     = 0u;
+      t.words[e][2 * w + 1] = 0u;
+      if (w == 0) t.key[e] = kEmptyKey;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) t.count = 0u;
     __syncthreads();
   }
 }
@@ -704,10 +720,13 @@ __global__ void __launch_bounds__(256) k_mark_hits(const int4* __restrict__ rays
 // sweeps four leaves at once. A lane loads the float4 groups of its slab that
 // hold update bits (all loads issued before any use), applies the log-odds
 // rules, stores them back and clears its update words.
-__global__ void __launch_bounds__(256) k_sweep(ChannelView c, float* __restrict__ values,
-                                               unsigned long long* __restrict__ active,
-                                               uint32_t* __restrict__ flags, const int4* __restrict__ origin,
-                                               LogOddsTable lt, DevStatus* st)
+// kPerMap: the pool holds a batch of maps, each leaf takes its map's log-odds
+// constants (else the one map's, kept in registers).
+template <bool kPerMap>
+__global__ void __launch_bounds__(256, 4) k_sweep(ChannelView c, float* __restrict__ values,
+                                                  unsigned long long* __restrict__ active,
+                                                  uint32_t* __restrict__ flags, const int4* __restrict__ origin,
+                                                  LogOddsTable lt, DevStatus* st)
 {
   if (ld_relaxed_u32(&st->error) != 0u) return;
   const uint32_t nt   = *c.n_touched;
@@ -729,7 +748,7 @@ __global__ void __launch_bounds__(256) k_sweep(ChannelView c, float* __restrict_
     const unsigned long long hitw  = u[8 + w];
     const unsigned long long actw  = u[w] | hitw;
     if (actw == 0ull) continue;
-    const LogOdds lo               = lt.table ? lt.table[origin[slot].w] : lt.lo0;
+    const LogOdds lo               = kPerMap ? lt.table[origin[slot].w] : lt.lo0;
     unsigned long long* aw         = active + static_cast<size_t>(slot) * 8 + w;
     const unsigned long long on_in = *aw;
     unsigned long long on          = on_in;
@@ -830,6 +849,49 @@ __global__ void k_rehash(MapView m, uint32_t n)
     h = (h + 1) & m.bhmask;
   }
   atomicOr(&m.st->error, kErrHashFull);
+}
+
+// Zeroes the update words of the leaves on a channel's touched list (when a
+// marking has to give up and its partial update grid is dropped).
+__global__ void k_clear_touched(ChannelView c)
+{
+  const size_t words = static_cast<size_t>(*c.n_touched) * 16;
+  for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < words;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+  {
+    c.upd[static_cast<size_t>(c.touched[i >> 4]) * 16 + (i & 15u)] = 0ull;
+  }
+}
+
+// Releases leaf slots [from, to) (allocated by a call whose marking was
+// dropped): their cells in blocks below `keep_blocks` become empty again (the
+// tables of younger blocks are cleared whole by the host). Their values,
+// masks and flags were never written. The block hash must still hold the
+// blocks (it is rebuilt afterwards).
+__global__ void k_release_leaves(MapView m, uint32_t from, uint32_t to, uint32_t keep_blocks)
+{
+  const uint32_t slot = from + blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= to || slot >= m.capacity) return;
+  const int4 o = m.origin[slot];
+  const int lx = o.x >> 3, ly = o.y >> 3, lz = o.z >> 3;
+  const unsigned long long key = pack_leaf_key(o.w, lx >> 3, ly >> 3, lz >> 3);
+  uint32_t h = static_cast<uint32_t>(mix64(key)) & m.bhmask;
+  for (uint32_t probe = 0; probe <= m.bhmask; ++probe)
+  {
+    const unsigned long long k = m.bkeys[h];
+    if (k == kEmptyKey) return;
+    if (k == key)
+    {
+      const int b = m.bslots[h];
+      if (b >= 0 && static_cast<uint32_t>(b) < keep_blocks)
+      {
+        int* e = m.bleaf + static_cast<size_t>(b) * 512 + (((lx & 7) << 6) | ((ly & 7) << 3) | (lz & 7));
+        if (*e == static_cast<int>(slot)) *e = kLeafEmpty;
+      }
+      return;
+    }
+    h = (h + 1) & m.bhmask;
+  }
 }
 
 // After a pool growth: leaf cells whose allocation failed become empty again.

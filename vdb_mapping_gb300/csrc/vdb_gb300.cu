@@ -87,6 +87,8 @@ struct vdbg_map
   unsigned long long* bkeys = nullptr;
   int* bslots           = nullptr;
   uint32_t n_blocks     = 0;  // host copy after the last call
+  uint32_t call_leaves  = 0;  // n_leaves / n_blocks when the current call began
+  uint32_t call_blocks  = 0;
 
   DevStatus* d_status   = nullptr;
   DevStatus* h_status   = nullptr;  // pinned
@@ -455,6 +457,8 @@ int begin_call(vdbg_map* m, cudaStream_t s)
   m->timings           = vdbg_timings{};
   m->timings.launches_total = total;
   m->timed_prep        = false;
+  m->call_leaves       = m->n_leaves;
+  m->call_blocks       = m->n_blocks;
   clear_status(m->h_status);
   m->h_status->n_leaves = m->n_leaves;
   m->h_status->n_blocks = m->n_blocks;
@@ -700,8 +704,12 @@ int launch_sweep(vdbg_map* m, Channel& c, cudaStream_t s)
   LogOddsTable lt;
   lt.lo0   = m->conf[0].lo;
   lt.table = m->batch ? m->d_lo : nullptr;
-  k_sweep<<<kSweepBlocks, kSweepThreads, 0, s>>>(channel_view(c), m->values, m->active, m->flags, m->origin, lt,
-                                                 m->d_status);
+  if (m->batch)
+    k_sweep<true><<<kSweepBlocks, kSweepThreads, 0, s>>>(channel_view(c), m->values, m->active, m->flags,
+                                                         m->origin, lt, m->d_status);
+  else
+    k_sweep<false><<<kSweepBlocks, kSweepThreads, 0, s>>>(channel_view(c), m->values, m->active, m->flags,
+                                                          m->origin, lt, m->d_status);
   VDBG_CUDA(cudaGetLastError());
   m->timings.launches += 2;
   return VDBG_OK;
@@ -781,6 +789,56 @@ bool bad_points(const float* xyz, int64_t n, int64_t stride)
 // exhaustion are handled inside run_dda_passes. A voxel index out of range
 // skips the whole cloud (nothing of it is marked) and the other pending
 // update grids are still integrated.
+// After a marking that had to give up (a pool that may not grow, a bounded
+// wait that ran out): drops the source's partial update grid so that nothing
+// of it is integrated later, releases the leaves and blocks the current call
+// allocated (so the pool is as the call found it), lets failed leaf cells be
+// allocated again and rebuilds the block hash in place.
+int discard_marking(vdbg_map* m, Channel& c, cudaStream_t s)
+{
+  m->n_leaves = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
+  m->n_blocks = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
+  k_compact<<<m->num_sms * 4, 256, 0, s>>>(map_view(m), channel_view(c), m->d_status, 1);
+  k_clear_touched<<<m->num_sms * 4, 256, 0, s>>>(channel_view(c));
+  VDBG_CUDA(cudaGetLastError());
+  VDBG_TRY(finish_sweep(m, c, s));
+  const uint32_t keep_leaves = std::min(m->call_leaves, m->n_leaves);
+  const uint32_t keep_blocks = std::min(m->call_blocks, m->n_blocks);
+  if (m->n_leaves > keep_leaves)
+  {
+    const uint32_t n = m->n_leaves - keep_leaves;
+    k_release_leaves<<<(n + 255) / 256, 256, 0, s>>>(map_view(m), keep_leaves, m->n_leaves, keep_blocks);
+    VDBG_CUDA(cudaGetLastError());
+  }
+  if (m->n_blocks > keep_blocks)
+  {
+    VDBG_CUDA(cudaMemsetAsync(m->bleaf + static_cast<size_t>(keep_blocks) * 512, 0xff,
+                              static_cast<size_t>(m->n_blocks - keep_blocks) * 512 * sizeof(int), s));
+  }
+  m->n_leaves = keep_leaves;
+  m->n_blocks = keep_blocks;
+  if (m->n_blocks > 0)
+  {
+    k_reset_failed_leaves<<<m->num_sms * 4, 256, 0, s>>>(m->bleaf, static_cast<size_t>(m->n_blocks) * 512);
+    VDBG_CUDA(cudaGetLastError());
+  }
+  VDBG_CUDA(cudaMemsetAsync(m->bkeys, 0xff, static_cast<size_t>(m->bhash_size) * sizeof(unsigned long long), s));
+  VDBG_CUDA(cudaMemsetAsync(m->bslots, 0xff, static_cast<size_t>(m->bhash_size) * sizeof(int), s));
+  if (m->n_blocks > 0)
+  {
+    k_rehash<<<(m->n_blocks + 255) / 256, 256, 0, s>>>(map_view(m), m->n_blocks);
+    VDBG_CUDA(cudaGetLastError());
+  }
+  DevStatus clean;
+  clear_status(&clean);
+  clean.n_leaves = m->n_leaves;
+  clean.n_blocks = m->n_blocks;
+  *m->h_status   = clean;
+  VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+  VDBG_CUDA(cudaStreamSynchronize(s));
+  return VDBG_OK;
+}
+
 // The scans to cast in one call: the table and the status to report when a
 // scan could not be cast at all (an origin outside the index range).
 struct CastPlan
@@ -847,9 +905,15 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
     const RunBuffer rb = run_buffer(m->run_key, m->run_bits, m->run_slab, m->run_count, m->run_seg, m->dda_warps);
     const int d        = run_dda_passes(m, *src, m->d_rays, m->d_order, n, t, rb, m->lstate, m->wstate, true, s);
     if (d == VDBG_ERR_COORD_RANGE)
+    {
       call_status = d;
+    }
     else if (d != VDBG_OK)
+    {
+      // Nothing of this source's window survives a failed marking.
+      if (d != VDBG_ERR_CUDA) discard_marking(m, *src, s);
       return d;
+    }
   }
   std::vector<Channel*> todo;
   if (integrate_all)
@@ -892,6 +956,7 @@ const char* vdbg_status_string(int s)
     case VDBG_ERR_CUDA: return "CUDA error";
     case VDBG_ERR_TIMEOUT: return "Bounded device wait gave up";
     case VDBG_ERR_BUFFER_TOO_SMALL: return "Buffer too small";
+    case VDBG_ERR_BUSY: return "Serving queue full";
     case VDBG_ERR_SIZE_LIMIT:
       return "Input too large for vdbg_insert_point_cloud_noalloc (more than VDBG_NOALLOC_MAX_POINTS points, "
              "or a host stride above 16 bytes)";
@@ -902,6 +967,69 @@ const char* vdbg_status_string(int s)
 } // extern "C"
 
 namespace {
+
+// insertPointCloud for one scan per map of a batch. The points are either one
+// buffer `xyz` (maps back to back) or, with `parts`, one host buffer per map,
+// copied to the device scratch one map at a time.
+int batch_insert_impl(vdbg_map* m, const float* xyz, const float* const* parts, const int64_t* counts,
+                      int64_t stride, const double* origins, uint32_t flags, cudaStream_t s, vdbg_scan_stats* stats)
+{
+  if (!m || !m->batch || !counts || !origins) return VDBG_ERR_INVALID_ARGUMENT;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  const int nm  = static_cast<int>(m->conf.size());
+  int64_t total = 0;
+  for (int i = 0; i < nm; ++i)
+  {
+    if (counts[i] < 0) return VDBG_ERR_INVALID_ARGUMENT;
+    if (parts && counts[i] > 0 && bad_points(parts[i], counts[i], stride)) return VDBG_ERR_INVALID_ARGUMENT;
+    total += counts[i];
+  }
+  if (!parts && bad_points(xyz, total, stride)) return VDBG_ERR_INVALID_ARGUMENT;
+  if (total > (int64_t(1) << 31) - 1) return VDBG_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < nm; ++i)
+    if (counts[i] > 0 && !m->conf[i].config_set) return VDBG_ERR_NOT_CONFIGURED;
+  CastPlan plan;
+  m->h_first[0] = 0;
+  for (int i = 0; i < nm; ++i)
+  {
+    m->h_first[i + 1] = m->h_first[i] + static_cast<uint32_t>(counts[i]);
+    ScanGeom g{};
+    bool coord_range = false;
+    const double range = m->conf[i].max_range;
+    if (counts[i] > 0 && range > 0 && scan_geom_for(m, i, origins + 3 * i, range, &g, &coord_range))
+    {
+      plan.any = true;
+    }
+    else
+    {
+      // An origin outside the index range fails the whole batch unmarked, as
+      // an endpoint outside it does (k_prep).
+      if (coord_range) return VDBG_ERR_COORD_RANGE;
+      g     = ScanGeom{};
+      g.map = -1;
+    }
+    m->h_geom[i] = g;
+  }
+  if (nm == 1)
+    plan.table = single_table(m->h_geom[0]);
+  else
+    plan.table.n = nm;
+  if (parts && total > 0)
+  {
+    VDBG_TRY(set_device(m));
+    VDBG_TRY(ensure_scratch(m, total, stride, true));
+    for (int i = 0; i < nm; ++i)
+    {
+      if (counts[i] == 0) continue;
+      VDBG_CUDA(cudaMemcpyAsync(m->d_pts + static_cast<size_t>(m->h_first[i]) * static_cast<size_t>(stride),
+                                parts[i], static_cast<size_t>(counts[i]) * static_cast<size_t>(stride),
+                                cudaMemcpyHostToDevice, s));
+    }
+    xyz   = reinterpret_cast<const float*>(m->d_pts);
+    flags = flags | VDBG_POINTS_DEVICE;
+  }
+  return accumulate_and_integrate(m, xyz, total, stride, plan, &m->channels[0], flags, s, true, nullptr, stats);
+}
 
 int create_impl(int n_maps, const double* resolutions, const vdbg_options* options, bool batch, vdbg_map** out)
 {
@@ -1318,46 +1446,7 @@ int vdbg_batch_set_config(vdbg_map* m, int map, const vdbg_config* c)
 int vdbg_batch_insert(vdbg_map* m, const float* xyz, const int64_t* counts, int64_t stride, const double* origins,
                       uint32_t flags, void* stream, vdbg_scan_stats* stats)
 {
-  if (!m || !m->batch || !counts || !origins) return VDBG_ERR_INVALID_ARGUMENT;
-  if (stats) std::memset(stats, 0, sizeof(*stats));
-  const int nm  = static_cast<int>(m->conf.size());
-  int64_t total = 0;
-  for (int i = 0; i < nm; ++i)
-  {
-    if (counts[i] < 0) return VDBG_ERR_INVALID_ARGUMENT;
-    total += counts[i];
-  }
-  if (bad_points(xyz, total, stride)) return VDBG_ERR_INVALID_ARGUMENT;
-  for (int i = 0; i < nm; ++i)
-    if (counts[i] > 0 && !m->conf[i].config_set) return VDBG_ERR_NOT_CONFIGURED;
-  CastPlan plan;
-  m->h_first[0] = 0;
-  for (int i = 0; i < nm; ++i)
-  {
-    m->h_first[i + 1] = m->h_first[i] + static_cast<uint32_t>(counts[i]);
-    ScanGeom g{};
-    bool coord_range = false;
-    const double range = m->conf[i].max_range;
-    if (counts[i] > 0 && range > 0 && scan_geom_for(m, i, origins + 3 * i, range, &g, &coord_range))
-    {
-      plan.any = true;
-    }
-    else
-    {
-      // An origin outside the index range fails the whole batch unmarked, as
-      // an endpoint outside it does (k_prep).
-      if (coord_range) return VDBG_ERR_COORD_RANGE;
-      g     = ScanGeom{};
-      g.map = -1;
-    }
-    m->h_geom[i] = g;
-  }
-  if (nm == 1)
-    plan.table = single_table(m->h_geom[0]);
-  else
-    plan.table.n = nm;
-  return accumulate_and_integrate(m, xyz, total, stride, plan, &m->channels[0], flags, pick_stream(m, stream), true,
-                                  nullptr, stats);
+  return batch_insert_impl(m, xyz, nullptr, counts, stride, origins, flags, pick_stream(m, stream), stats);
 }
 
 int vdbg_batch_leaf_count(vdbg_map* m, int map, int64_t* out)
@@ -1444,17 +1533,6 @@ int noalloc_scratch(int device, char** out)
   return VDBG_OK;
 }
 
-// Zeroes the update words of the leaves on a channel's touched list (used
-// when a no-allocation insertion has to give up after a partial marking).
-__global__ void k_clear_touched(ChannelView c)
-{
-  const size_t words = static_cast<size_t>(*c.n_touched) * 16;
-  for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < words;
-       i += static_cast<size_t>(gridDim.x) * blockDim.x)
-  {
-    c.upd[static_cast<size_t>(c.touched[i >> 4]) * 16 + (i & 15u)] = 0ull;
-  }
-}
 
 } // namespace
 
@@ -1528,33 +1606,7 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
   {
     // The pool may not grow here: drop the partial marking of this source,
     // apply nothing and report.
-    m->n_leaves = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
-    m->n_blocks = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
-    k_compact<<<m->num_sms * 4, 256, 0, s>>>(map_view(m), channel_view(*src), m->d_status, 1);
-    k_clear_touched<<<m->num_sms * 4, 256, 0, s>>>(channel_view(*src));
-    VDBG_CUDA(cudaGetLastError());
-    VDBG_TRY(finish_sweep(m, *src, s));
-    // Failed leaf cells become empty again and the block hash is rebuilt in
-    // place from the allocated blocks, so later calls see a consistent index.
-    if (m->n_blocks > 0)
-    {
-      k_reset_failed_leaves<<<m->num_sms * 4, 256, 0, s>>>(m->bleaf, static_cast<size_t>(m->n_blocks) * 512);
-      VDBG_CUDA(cudaGetLastError());
-    }
-    VDBG_CUDA(cudaMemsetAsync(m->bkeys, 0xff, static_cast<size_t>(m->bhash_size) * sizeof(unsigned long long), s));
-    VDBG_CUDA(cudaMemsetAsync(m->bslots, 0xff, static_cast<size_t>(m->bhash_size) * sizeof(int), s));
-    if (m->n_blocks > 0)
-    {
-      k_rehash<<<(m->n_blocks + 255) / 256, 256, 0, s>>>(map_view(m), m->n_blocks);
-      VDBG_CUDA(cudaGetLastError());
-    }
-    DevStatus clean;
-    clear_status(&clean);
-    clean.n_leaves = m->n_leaves;
-    clean.n_blocks = m->n_blocks;
-    *m->h_status   = clean;
-    VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
-    VDBG_CUDA(cudaStreamSynchronize(s));
+    VDBG_TRY(discard_marking(m, *src, s));
     return dda;
   }
   std::vector<Channel*> todo;
@@ -1569,3 +1621,6 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
   fill_stats(m, leaves_before, stats);
   return result;
 }
+
+// The serving loop over a batch (vdbg_server_*).
+#include "server.inl"

@@ -468,3 +468,78 @@ class MapBatch:
         n = C.c_int64()
         self._check(self._lib.vdbg_device_bytes(self._h, C.byref(n)), "vdbg_device_bytes")
         return n.value
+
+
+class MapServer:
+    """Continuous-batching request loop over a ``MapBatch`` (vdbg_server_*).
+
+    ``submit`` queues one scan for one map and returns at once; a native
+    worker thread inserts the oldest queued scan of every map in one batched
+    call per step, admitting scans against ``memory_budget_bytes``; ``poll``
+    returns completed requests with their steady-clock submit/start/done
+    times in ns. While the server runs only it may use the batch.
+    """
+
+    def __init__(self, batch: "MapBatch", memory_budget_bytes: int = 0, max_batch_maps: int = 0,
+                 queue_capacity: int = 0):
+        self._lib = _lib.load()
+        self.batch = batch
+        opts = _lib.vdbg_server_options()
+        opts.memory_budget_bytes = int(memory_budget_bytes)
+        opts.max_batch_maps = int(max_batch_maps)
+        opts.queue_capacity = int(queue_capacity)
+        h = C.c_void_p()
+        s = self._lib.vdbg_server_create(batch._h, C.byref(opts), C.byref(h))
+        if s != 0:
+            raise VdbgError(s, "vdbg_server_create")
+        self._h = h
+
+    def submit(self, map_index: int, cloud, origin, tag: int = 0) -> int:
+        """Queues a host cloud ((N,3)/(N,4) float32); returns the status
+        (VDBG_ERR_BUSY when the queue is full)."""
+        ptr, n, stride, flags, keep = _cloud_args(cloud)
+        if flags:
+            raise ValueError("the server stages host clouds")
+        s = self._lib.vdbg_server_submit(self._h, int(map_index), C.c_void_p(ptr), n, stride, _origin(origin),
+                                         int(tag))
+        del keep
+        if s not in (0, _lib.STATUS_CODE["VDBG_ERR_BUSY"]):
+            raise VdbgError(s, "vdbg_server_submit")
+        return s
+
+    def poll(self, capacity: int = 256, wait_ms: int = 0):
+        buf = (_lib.vdbg_server_result * capacity)()
+        n = C.c_int()
+        s = self._lib.vdbg_server_poll(self._h, buf, capacity, int(wait_ms), C.byref(n))
+        if s != 0:
+            raise VdbgError(s, "vdbg_server_poll")
+        return [buf[i].as_dict() for i in range(n.value)]
+
+    def drain(self, wait_ms: int = 60000) -> None:
+        s = self._lib.vdbg_server_drain(self._h, int(wait_ms))
+        if s != 0:
+            raise VdbgError(s, "vdbg_server_drain")
+
+    def stats(self) -> dict:
+        st = _lib.vdbg_server_stats()
+        s = self._lib.vdbg_server_get_stats(self._h, C.byref(st))
+        if s != 0:
+            raise VdbgError(s, "vdbg_server_get_stats")
+        return st.as_dict()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.vdbg_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
