@@ -57,6 +57,8 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--points", type=int, default=0,
                     help="use an evenly strided subset of N points of each scan (small profiling cases)")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="simulated traffic for --workload serving")
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="device-memory admission budget")
     ap.add_argument("--batch-steps", type=int, default=4,
                     help="distinct steps generated for --workload batched (cycled)")
     ap.add_argument("--leaf-capacity", type=int, default=0,
@@ -431,10 +433,13 @@ def run_batched(args):
                 upd += g.last_stats["updates"]
         return {"updates": upd, "rays": int(sum(counts))}
 
+    phase = []
+
     def timed(fn):
         for k in range(args.warmup):
             fn(k)
         torch.cuda.synchronize()
+        phase.clear()
         ms, upd, rays = [], 0, 0
         for i in range(args.steps):
             k = args.warmup + i
@@ -447,11 +452,14 @@ def run_batched(args):
             ms.append(e0.elapsed_time(e1))
             upd += st["updates"]
             rays += st["rays"]
+            if fn is batched_step:
+                phase.append(b.timings())
         return ms, upd, rays
 
     clocks = ClockSampler(local)
     clocks.start()
     b_ms, b_upd, b_rays = timed(batched_step)
+    b_phase = {k: float(np.mean([p[k] for p in phase])) for k in ("prep_ms", "dda_ms", "sweep_ms", "total_ms")}
     p_ms, p_upd, p_rays = timed(plain_step)
     clk = clocks.stop()
     same = all(all(np.array_equal(x, y) for x, y in zip(b.exportLeaves(i), plain[i].exportLeaves()))
@@ -464,7 +472,8 @@ def run_batched(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 DDA / f32 log-odds",
         "data": f"synthetic (seeded batched workload, {n_distinct} distinct steps cycled)",
         "config": {**wl.describe(), "l2": "flushed between steps (256 MiB write)"},
-        "batched": {"voxel_updates_per_s": b_upd / b_s, "rays_per_s": b_rays / b_s,
+        "batched": {"voxel_updates_per_s": b_upd / b_s, "rays_per_s": b_rays / b_s, "phases_ms": b_phase,
+                    "updates_per_step": b_upd / args.steps,
                     "ms_per_step": {"p50": float(np.percentile(b_ms, 50)), "p99": float(np.percentile(b_ms, 99))}},
         "plain_per_map": {"voxel_updates_per_s": p_upd / p_s, "rays_per_s": p_rays / p_s,
                           "ms_per_step": {"p50": float(np.percentile(p_ms, 50)),
@@ -480,12 +489,106 @@ def run_batched(args):
     return 0
 
 
+# --------------------------------------------------------------------------
+# Serving: Poisson sensor streams through the continuous-batching loop
+# --------------------------------------------------------------------------
+
+def run_serving(args):
+    """16 sensor streams with Poisson arrivals in real time for --serve-seconds
+    through MapServer; reports p50/p99 latency (submit to done) per sensor
+    class next to rays/s and voxel-updates/s."""
+    import threading
+
+    import numpy as np
+    import torch
+
+    from vdb_mapping_gb300 import MapBatch, MapServer
+    from vdb_mapping_gb300 import workloads as W
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    wl = W.get("serving")
+    K = wl.distinct_scans
+    scans = {(i, k): wl.scan(i, k) for i in range(len(wl.streams)) for k in range(K)}
+    batch = MapBatch(wl.resolutions, initial_leaf_capacity=1 << 23, device=local)
+    for i, c in enumerate(wl.configs):
+        batch.setConfig(i, c)
+    # Warm the scratch and run buffers with one scan per map (not timed).
+    batch.insert([scans[(i, 0)][0] for i in range(len(wl.streams))],
+                 [scans[(i, 0)][1] for i in range(len(wl.streams))])
+    budget = int(args.serve_budget_gb * (1 << 30))
+    server = MapServer(batch, memory_budget_bytes=budget)
+    arrivals = wl.arrivals(args.serve_seconds)
+    results, busy = [], 0
+    counter = [0] * len(wl.streams)
+    t_start = time.perf_counter()
+
+    def producer():
+        nonlocal busy
+        for j, (t, i) in enumerate(arrivals):
+            delay = t_start + t - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            k = counter[i]
+            counter[i] += 1
+            pts, org = scans[(i, k % K)]
+            while server.submit(i, pts, org, tag=j) != 0:
+                busy += 1
+                time.sleep(0.0005)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    th = threading.Thread(target=producer)
+    th.start()
+    while th.is_alive() or len(results) < len(arrivals):
+        results += server.poll(512, wait_ms=50)
+        if not th.is_alive() and len(results) >= len(arrivals):
+            break
+    th.join()
+    server.drain()
+    results += server.poll(4096)
+    clk = clocks.stop()
+    st = server.stats()
+    server.close()
+    lat = {"lidar": [], "depth": []}
+    for r in results:
+        lat["depth" if wl.streams[r["map"]]["depth"] else "lidar"].append((r["done_ns"] - r["submit_ns"]) / 1e6)
+    span_s = (max(r["done_ns"] for r in results) - min(r["submit_ns"] for r in results)) / 1e9
+    allv = lat["lidar"] + lat["depth"]
+    line = {
+        "metric": "serving: insert latency p50/p99 (submit to map updated) and rays/s, 16 Poisson sensor streams",
+        "value": float(np.percentile(allv, 99)), "unit": "ms (p99 latency)", "n_gpus": 1,
+        "steps": st["steps"], "warmup": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 DDA / f32 log-odds",
+        "data": f"synthetic (seeded rooms; {K} distinct scans per stream cycled, sensor moving)",
+        "config": {**wl.describe(), "seconds": args.serve_seconds, "memory_budget_gb": args.serve_budget_gb},
+        "latency_ms": {c: {"p50": float(np.percentile(v, 50)), "p99": float(np.percentile(v, 99)),
+                           "max": float(max(v)), "n": len(v),
+                           "sensor_period_ms": 1000.0 / (wl.streams[-1]["hz"] if c == "depth" else wl.streams[0]["hz"])}
+                       for c, v in lat.items() if v},
+        "rays_per_s": st["rays"] / span_s, "voxel_updates_per_s": st["updates"] / span_s,
+        "offered_points_per_s": sum(s["n"] * s["hz"] for s in wl.streams),
+        "steps": st["steps"], "mean_scans_per_step": st["requests_done"] / max(1, st["steps"]),
+        "max_scans_per_step": st["max_step_maps"], "gpu_busy_frac": st["busy_ns"] / 1e9 / span_s,
+        "rejected": st["rejected"], "max_queued": st["max_queued"], "submit_retries_busy": busy,
+        "device_bytes": st["device_bytes"],
+        "statuses": sorted({r["status"] for r in results}),
+    }
+    if clk:
+        line["clocks"] = clk
+    print(json.dumps(line))
+    batch.close()
+    return 0
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "serving":
+        return run_serving(args)
     return run_ours(args)
 
 

@@ -163,6 +163,22 @@ int vdbg_get_timings(const vdbg_map* map, vdbg_timings* out);
 /* Device bytes held by the map. */
 int vdbg_device_bytes(const vdbg_map* map, int64_t* out);
 
+/* Launch and layout parameters of the insertion kernels (no counterpart in
+ * the reference). They change speed only, never results; the package's
+ * autotuner (vdb_mapping_gb300/autotune.py) picks them by timing candidates
+ * on a sample of the caller's scans. */
+typedef struct vdbg_tuning
+{
+  int32_t rays_per_take;     /* rays a DDA warp takes from the sorted order at a time (1-1024; 16) */
+  int32_t apply_chunk_runs;  /* DDA runs an apply block merges in shared memory at a time (256-2^20; 4096) */
+  int32_t length_edges[3];   /* L1 lengths (voxels) starting the sort's length classes, descending (1024, 512, 256) */
+  float hash_load;           /* block-hash load factor (0.05-0.9; 0.5); a change rebuilds the hash */
+  int32_t reserved0;
+} vdbg_tuning;
+
+int vdbg_set_tuning(vdbg_map* map, const vdbg_tuning* tuning);
+int vdbg_get_tuning(const vdbg_map* map, vdbg_tuning* out);
+
 /* Insertion that allocates no device memory during the call. No counterpart
  * in the reference: it exists for callers that must not allocate while they
  * run, such as real-time mapping loops where cudaMalloc's unbounded latency

@@ -87,6 +87,30 @@ class vdbg_timings(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved0"}
 
 
+class vdbg_tuning(C.Structure):
+    _fields_ = [
+        ("rays_per_take", C.c_int32),
+        ("apply_chunk_runs", C.c_int32),
+        ("length_edges", C.c_int32 * 3),
+        ("hash_load", C.c_float),
+        ("reserved0", C.c_int32),
+    ]
+
+    def as_dict(self):
+        return {"rays_per_take": self.rays_per_take, "apply_chunk_runs": self.apply_chunk_runs,
+                "length_edges": tuple(self.length_edges), "hash_load": round(float(self.hash_load), 4)}
+
+    @classmethod
+    def from_dict(cls, d):
+        t = cls()
+        t.rays_per_take = int(d["rays_per_take"])
+        t.apply_chunk_runs = int(d["apply_chunk_runs"])
+        for k in range(3):
+            t.length_edges[k] = int(d["length_edges"][k])
+        t.hash_load = float(d["hash_load"])
+        return t
+
+
 class vdbg_server_options(C.Structure):
     _fields_ = [
         ("memory_budget_bytes", C.c_int64),
@@ -156,6 +180,8 @@ SIGNATURES = [
     ("vdbg_get_timings", C.c_int, [_P, C.POINTER(vdbg_timings)]),
     ("vdbg_insert_point_cloud_noalloc", C.c_int,
      [_P, _P, C.c_int64, C.c_int64, _D3, C.c_char_p, C.c_uint32, _P, C.POINTER(vdbg_scan_stats)]),
+    ("vdbg_set_tuning", C.c_int, [_P, C.POINTER(vdbg_tuning)]),
+    ("vdbg_get_tuning", C.c_int, [_P, C.POINTER(vdbg_tuning)]),
     ("vdbg_create_batch", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(vdbg_options), C.POINTER(_P)]),
     ("vdbg_batch_set_config", C.c_int, [_P, C.c_int, C.POINTER(vdbg_config)]),
     ("vdbg_batch_insert", C.c_int,

@@ -120,6 +120,7 @@ struct ScanTable
   const uint32_t* first;    // [n + 1] (n > 1)
   const uint16_t* ray_scan; // [rays] scan of each ray (n > 1)
   int n;
+  uint32_t edge[3];         // L1 lengths that start the length classes 0, 1, 2 (descending)
 };
 
 __device__ __forceinline__ int scan_of_point(const ScanTable& t, uint32_t i)
@@ -171,6 +172,8 @@ struct RunBuffer
   uint32_t* count;           // runs per warp segment
   uint32_t seg;              // segment capacity (runs)
   uint32_t warps;            // segments
+  uint32_t take;             // rays a DDA warp takes from the order at a time
+  uint32_t apply_chunk;      // runs an apply block merges at a time
 };
 
 // DDA state of a lane whose ray was still in flight when its warp's segment

@@ -31,8 +31,9 @@ namespace vdbg {
 // map; the DDA hands warps short runs of this order so their lanes walk
 // through the same leaves and their leaf records merge. Order only; the map
 // does not depend on it.
-__device__ __forceinline__ int ray_bucket(int dx, int dy, int dz, uint32_t l1, int s, int n_scans)
+__device__ __forceinline__ int ray_bucket(int dx, int dy, int dz, uint32_t l1, int s, const ScanTable& t)
 {
+  const int n_scans = t.n;
   const int ax = abs(dx), ay = abs(dy), az = abs(dz);
   int face, u, v, mx;
   if (ax >= ay && ax >= az)
@@ -56,7 +57,7 @@ __device__ __forceinline__ int ray_bucket(int dx, int dy, int dz, uint32_t l1, i
     v    = dy;
     mx   = az;
   }
-  const int cls  = l1 >= 1024u ? 0 : (l1 >= 512u ? 1 : (l1 >= 256u ? 2 : 3));
+  const int cls  = l1 >= t.edge[0] ? 0 : (l1 >= t.edge[1] ? 1 : (l1 >= t.edge[2] ? 2 : 3));
   const int base = (cls * n_scans + s) * kDirCells;
   if (mx == 0) return base;
   const int iu = static_cast<int>((static_cast<long long>(u + mx) * 13) / (2 * mx + 1));
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(256) k_prep(const char* __restrict__ pts, int6
     if (sn) atomicAdd(&st->nonfinite, sn);
   }
   const int b =
-    valid ? ray_bucket(ex - g.ovx, ey - g.ovy, ez - g.ovz, meta & kMetaL1Mask, sc, t.n) : -1;
+    valid ? ray_bucket(ex - g.ovx, ey - g.ovy, ez - g.ovz, meta & kMetaL1Mask, sc, t) : -1;
   const unsigned peers = __match_any_sync(0xffffffffu, b);
   if (valid && (__ffs(peers) - 1) == static_cast<int>(threadIdx.x & 31))
   {
@@ -230,7 +231,7 @@ __global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, 
   const int sc         = valid ? scan_of_ray(t, static_cast<uint32_t>(i)) : 0;
   const ScanGeom& g    = scan_geom(t, sc);
   const int b =
-    valid ? ray_bucket(r.x - g.ovx, r.y - g.ovy, r.z - g.ovz, meta & kMetaL1Mask, sc, t.n) : -1;
+    valid ? ray_bucket(r.x - g.ovx, r.y - g.ovy, r.z - g.ovz, meta & kMetaL1Mask, sc, t) : -1;
   const unsigned peers = __match_any_sync(0xffffffffu, b);
   const int lane       = static_cast<int>(threadIdx.x & 31);
   const int leader     = __ffs(peers) - 1;
@@ -271,7 +272,6 @@ constexpr int kDdaWarps      = 2;                // warps per block
 constexpr int kDdaSteps      = 16;               // DDA steps between ring copies
 constexpr int kDdaRing       = kDdaSteps + 1;    // emissions per lane per round: one per step + the flush
 constexpr uint32_t kDdaRound = 32u * kDdaRing;   // most runs a warp writes per round
-constexpr uint32_t kDdaChunk = 16;               // rays a warp takes from the binned order at a time
 
 struct DdaWarpSmem
 {
@@ -289,13 +289,13 @@ __device__ __forceinline__ uint32_t lanemask_lt()
 
 // Emits the lane's open run when `close` (ranked among the warp's emitting
 // lanes by one ballot) at position *n of the warp's record list.
-__device__ __forceinline__ void dda_emit(DdaWarpSmem& q, bool close, int map, int rx, int ry, int rz,
+__device__ __forceinline__ void dda_emit(DdaWarpSmem& q, bool close, uint32_t lt, int map, int rx, int ry, int rz,
                                          unsigned long long& run, bool& run_open, uint32_t& n)
 {
   const unsigned em = __ballot_sync(0xffffffffu, close);
   if (close)
   {
-    const uint32_t p = n + static_cast<uint32_t>(__popc(em & lanemask_lt()));
+    const uint32_t p = n + static_cast<uint32_t>(__popc(em & lt));
     q.keys[p]        = pack_leaf_key(map, rx >> 3, ry, rz);
     q.bits[p]        = run;
     q.slab[p]        = static_cast<unsigned char>(rx & 7);
@@ -313,6 +313,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
 {
   __shared__ DdaWarpSmem smem[kDdaWarps];
   const int lane    = static_cast<int>(threadIdx.x & 31);
+  const uint32_t lt = lanemask_lt();
   const uint32_t gw = blockIdx.x * kDdaWarps + (threadIdx.x >> 5);
   DdaWarpSmem& q    = smem[threadIdx.x >> 5];
   const uint32_t nv = m.st->n_valid;
@@ -364,7 +365,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
       if (chunk_next >= chunk_end)
       {
         uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&m.st->ray_cursor, kDdaChunk);
+        if (lane == 0) base = atomicAdd(&m.st->ray_cursor, rb.take);
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= nv)
         {
@@ -372,10 +373,10 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
           break;
         }
         chunk_next = base;
-        chunk_end  = min(base + kDdaChunk, nv);
+        chunk_end  = min(base + rb.take, nv);
       }
       const uint32_t avail = chunk_end - chunk_next;
-      const uint32_t rank  = static_cast<uint32_t>(__popc(need & lanemask_lt()));
+      const uint32_t rank  = static_cast<uint32_t>(__popc(need & lt));
       const bool take      = ((need >> lane) & 1u) && rank < avail;
       const uint32_t idx   = chunk_next + rank;
       const unsigned took  = __ballot_sync(0xffffffffu, take);
@@ -452,7 +453,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
       // setActiveState(voxel) on the update grid, one slab run at a time: the
       // run of the previous step ends when the voxel leaves it or the ray ended.
       const int ly = vy >> 3, lz = vz >> 3;
-      dda_emit(q, run_open && (!has_ray || vx != rx || ly != ry || lz != rz), map, rx, ry, rz, run, run_open,
+      dda_emit(q, run_open && (!has_ray || vx != rx || ly != ry || lz != rz), lt, map, rx, ry, rz, run, run_open,
                n_rec);
       if (has_ray)
       {
@@ -485,7 +486,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
       }
     }
     // Runs of rays that ended in the last step (a refill must not find them open).
-    dda_emit(q, run_open && !has_ray, map, rx, ry, rz, run, run_open, n_rec);
+    dda_emit(q, run_open && !has_ray, lt, map, rx, ry, rz, run, run_open, n_rec);
 
     // ---- copy the list to the warp's segment -------------------------------------
     __syncwarp();
@@ -533,7 +534,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
 // ---------------------------------------------------------------------------
 // k_apply_runs: merges the scan's slab runs and ORs them into the update masks.
 //
-// Persistent blocks take chunks of kApplyChunk runs (written together by
+// Persistent blocks take chunks of rb.apply_chunk runs (written together by
 // warps walking neighbouring rays, so a chunk repeats few leaves). Each thread
 // ORs its runs into the block's leaf table in shared memory (the lanes of a
 // warp holding the same leaf probe it once, through their leader); the first
@@ -545,7 +546,6 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
 // run that finds the table full is applied directly.
 // ---------------------------------------------------------------------------
 constexpr int kApplyThreads = 256;
-constexpr int kApplyChunk   = 4096;
 constexpr int kApplyTable   = 512;  // 2^9 entries, see apply_hash
 
 struct ApplySmem
@@ -564,15 +564,24 @@ __device__ __forceinline__ uint32_t apply_hash(unsigned long long key)
 
 // Slab of leaf `key` in the update masks: resolves (and allocates) the leaf
 // and marks it touched in its block. Returns the leaf slot or kSlotFailed.
+// The common case (block and leaf exist) costs two dependent load pairs: the
+// hash key with its slot, then the leaf cell with the block's epoch; anything
+// else takes the general find-or-insert paths.
 __device__ __forceinline__ int apply_resolve(const MapView& m, const ChannelView& c, unsigned long long key)
 {
   const int lx = unpack_leaf_coord(key, 0), ly = unpack_leaf_coord(key, 1), lz = unpack_leaf_coord(key, 2);
   const int mp = unpack_map(key);
-  const int b  = find_or_insert_block(m, mp, lx >> 3, ly >> 3, lz >> 3);
+  const unsigned long long bkey = pack_leaf_key(mp, lx >> 3, ly >> 3, lz >> 3);
+  const uint32_t h0             = static_cast<uint32_t>(mix64(bkey)) & m.bhmask;
+  const unsigned long long k0   = ld_ca_u64(m.bkeys + h0);
+  const int s0                  = ld_ca_s32(m.bslots + h0);
+  const int b = (k0 == bkey && s0 >= 0) ? s0 : find_or_insert_block(m, mp, lx >> 3, ly >> 3, lz >> 3);
   if (b < 0) return kSlotFailed;
-  touch_block(c, b);
   const int cell = ((lx & 7) << 6) | ((ly & 7) << 3) | (lz & 7);
-  const int slot = find_or_insert_leaf(m, b, cell, mp, lx, ly, lz);
+  const int c0   = ld_ca_s32(m.bleaf + static_cast<size_t>(b) * 512 + cell);
+  const uint32_t ep = ld_ca_u32(c.bepoch + b);
+  if (ep != c.cur_epoch) touch_block(c, b);
+  const int slot = c0 >= 0 ? c0 : find_or_insert_leaf(m, b, cell, mp, lx, ly, lz);
   if (slot >= 0) atomicOr(c.btouched + static_cast<size_t>(b) * 8 + (cell >> 6), 1ull << (cell & 63));
   return slot;
 }
@@ -596,17 +605,17 @@ __global__ void __launch_bounds__(kApplyThreads, 4) k_apply_runs(RunBuffer rb, M
   if (threadIdx.x == 0) t.count = 0u;
   __syncthreads();
   const int lane = static_cast<int>(threadIdx.x & 31);
-  // Work items: (segment, chunk of kApplyChunk runs), segment-major.
-  const uint32_t chunks_per_seg = (rb.seg + kApplyChunk - 1) / kApplyChunk;
+  // Work items: (segment, chunk of rb.apply_chunk runs), segment-major.
+  const uint32_t chunks_per_seg = (rb.seg + rb.apply_chunk - 1) / rb.apply_chunk;
   const uint32_t items          = rb.warps * chunks_per_seg;
   for (uint32_t item = blockIdx.x; item < items; item += gridDim.x)
   {
     const uint32_t sg    = item / chunks_per_seg;
-    const uint32_t start = (item % chunks_per_seg) * kApplyChunk;
+    const uint32_t start = (item % chunks_per_seg) * rb.apply_chunk;
     const uint32_t cnt   = rb.count[sg];
     if (start >= cnt) continue;  // uniform across the block
     const size_t base  = static_cast<size_t>(sg) * rb.seg;
-    const uint32_t end = min(start + kApplyChunk, cnt);
+    const uint32_t end = min(start + rb.apply_chunk, cnt);
     // Whole warps walk the chunk (tail lanes idle) so the match below sees full warps.
     for (uint32_t i0 = start + (threadIdx.x & ~31u); i0 < end; i0 += kApplyThreads)
     {
@@ -745,10 +754,11 @@ __global__ void __launch_bounds__(256, 4) k_sweep(ChannelView c, float* __restri
     // touched leaf carries at least one update bit).
     if (w == 0 && ld_ca_u32(flags + slot) == 0u) flags[slot] = 1u;
     unsigned long long* u          = c.upd + static_cast<size_t>(slot) * 16;
+    const int mp                   = kPerMap ? origin[slot].w : 0;  // loaded beside the masks
     const unsigned long long hitw  = u[8 + w];
     const unsigned long long actw  = u[w] | hitw;
     if (actw == 0ull) continue;
-    const LogOdds lo               = kPerMap ? lt.table[origin[slot].w] : lt.lo0;
+    const LogOdds lo               = kPerMap ? lt.table[mp] : lt.lo0;
     unsigned long long* aw         = active + static_cast<size_t>(slot) * 8 + w;
     const unsigned long long on_in = *aw;
     unsigned long long on          = on_in;

@@ -117,6 +117,7 @@ struct vdbg_map
 
   int64_t bytes         = 0;
   int num_sms           = 152;
+  vdbg_tuning tuning{16, 4096, {1024, 512, 256}, 0.5f, 0};
 };
 
 namespace {
@@ -338,6 +339,13 @@ int resize_pool(vdbg_map* m, uint32_t cap, uint32_t keep)
   return VDBG_OK;
 }
 
+// Block hash entries for `bcap` blocks at the tuned load factor (power of two).
+uint32_t hash_size_for(const vdbg_map* m, uint32_t bcap)
+{
+  const double load = m->tuning.hash_load > 0.f ? m->tuning.hash_load : 0.5;
+  return next_pow2(static_cast<uint64_t>(std::ceil(static_cast<double>(bcap) / load)));
+}
+
 // Allocates the block pool with `bcap` blocks, keeping blocks [0, keep), and
 // rebuilds the block hash.
 int resize_blocks(vdbg_map* m, uint32_t bcap, uint32_t keep)
@@ -389,7 +397,7 @@ int resize_blocks(vdbg_map* m, uint32_t bcap, uint32_t keep)
   m->bleaf     = bleaf;
   m->borigin   = borigin;
   m->bcapacity = bcap;
-  VDBG_TRY(rebuild_hash(m, next_pow2(static_cast<uint64_t>(bcap) * 2), keep));
+  VDBG_TRY(rebuild_hash(m, hash_size_for(m, bcap), keep));
   // Work queued by the caller on another stream must see the new tables.
   VDBG_CUDA(cudaStreamSynchronize(s));
   return VDBG_OK;
@@ -539,6 +547,11 @@ bool scan_geom_for(const vdbg_map* m, int map, const double origin[3], double ra
   return true;
 }
 
+void set_edges(const vdbg_map* m, ScanTable& t)
+{
+  for (int k = 0; k < 3; ++k) t.edge[k] = static_cast<uint32_t>(m->tuning.length_edges[k]);
+}
+
 ScanTable single_table(const ScanGeom& g)
 {
   ScanTable t{};
@@ -596,10 +609,12 @@ int ensure_runs(vdbg_map* m, uint32_t seg)
   return VDBG_OK;
 }
 
-RunBuffer run_buffer(unsigned long long* key, unsigned long long* bits, unsigned char* slab, uint32_t* count,
-                     uint32_t seg, uint32_t warps)
+RunBuffer run_buffer(const vdbg_map* m, unsigned long long* key, unsigned long long* bits, unsigned char* slab,
+                     uint32_t* count, uint32_t seg, uint32_t warps)
 {
   RunBuffer rb;
+  rb.take        = static_cast<uint32_t>(m->tuning.rays_per_take);
+  rb.apply_chunk = static_cast<uint32_t>(m->tuning.apply_chunk_runs);
   rb.key   = key;
   rb.bits  = bits;
   rb.slab  = slab;
@@ -889,6 +904,7 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
     }
     VDBG_TRY(ensure_runs(m, seg));
     ScanTable t = plan.table;
+    set_edges(m, t);
     if (t.n > 1)
     {
       // Scan table to the device (from pinned staging, so the copy is async).
@@ -902,7 +918,8 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
     }
     VDBG_TRY(launch_prep(m, *src, xyz, n, stride, t, flags, s, m->d_pts, m->d_rays, m->d_ray_scan, m->d_order,
                          m->d_hist, m->d_cursor));
-    const RunBuffer rb = run_buffer(m->run_key, m->run_bits, m->run_slab, m->run_count, m->run_seg, m->dda_warps);
+    const RunBuffer rb =
+      run_buffer(m, m->run_key, m->run_bits, m->run_slab, m->run_count, m->run_seg, m->dda_warps);
     const int d        = run_dda_passes(m, *src, m->d_rays, m->d_order, n, t, rb, m->lstate, m->wstate, true, s);
     if (d == VDBG_ERR_COORD_RANGE)
     {
@@ -1411,6 +1428,33 @@ int vdbg_device_bytes(const vdbg_map* m, int64_t* out)
   return VDBG_OK;
 }
 
+int vdbg_set_tuning(vdbg_map* m, const vdbg_tuning* t)
+{
+  if (!m || !t) return VDBG_ERR_INVALID_ARGUMENT;
+  if (t->rays_per_take < 1 || t->rays_per_take > 1024) return VDBG_ERR_INVALID_ARGUMENT;
+  if (t->apply_chunk_runs < 256 || t->apply_chunk_runs > (1 << 20)) return VDBG_ERR_INVALID_ARGUMENT;
+  if (!(t->length_edges[0] > t->length_edges[1] && t->length_edges[1] > t->length_edges[2] &&
+        t->length_edges[2] > 0))
+    return VDBG_ERR_INVALID_ARGUMENT;
+  if (!(t->hash_load > 0.05f && t->hash_load <= 0.9f)) return VDBG_ERR_INVALID_ARGUMENT;
+  VDBG_TRY(set_device(m));
+  const bool rehash = t->hash_load != m->tuning.hash_load;
+  m->tuning         = *t;
+  if (rehash)
+  {
+    VDBG_TRY(rebuild_hash(m, hash_size_for(m, m->bcapacity), m->n_blocks));
+    VDBG_CUDA(cudaStreamSynchronize(m->stream));
+  }
+  return VDBG_OK;
+}
+
+int vdbg_get_tuning(const vdbg_map* m, vdbg_tuning* out)
+{
+  if (!m || !out) return VDBG_ERR_INVALID_ARGUMENT;
+  *out = m->tuning;
+  return VDBG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Batches of independent maps.
 // ---------------------------------------------------------------------------
@@ -1587,13 +1631,14 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
   {
     // The histogram must start at zero; the previous call's contents remain.
     VDBG_CUDA(cudaMemsetAsync(d_hist, 0, kNoAllocHistBytes, s));
-    const CastPlan plan = plan_single(m, n, origin, src->max_range);
+    CastPlan plan = plan_single(m, n, origin, src->max_range);
+    set_edges(m, plan.table);
     if (plan.status != VDBG_OK) result = plan.status;
     if (plan.any)
     {
       VDBG_TRY(launch_prep(m, *src, xyz, n, stride, plan.table, flags, s, d_pts, d_rays, nullptr, d_order, d_hist,
                            d_cursor));
-      const RunBuffer rb = run_buffer(r_key, r_bits, r_slab, r_count, kNoAllocSeg, kNoAllocWarps);
+      const RunBuffer rb = run_buffer(m, r_key, r_bits, r_slab, r_count, kNoAllocSeg, kNoAllocWarps);
       dda                = run_dda_passes(m, *src, d_rays, d_order, n, plan.table, rb, ls, ws, false, s);
       if (dda == VDBG_ERR_COORD_RANGE)
       {

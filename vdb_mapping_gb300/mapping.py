@@ -299,6 +299,16 @@ class OccupancyVDBMapping:
         self._check(self._lib.vdbg_device_bytes(self._h, C.byref(n)), "vdbg_device_bytes")
         return n.value
 
+    def setTuning(self, tuning: dict) -> None:
+        """Kernel launch/layout parameters (speed only; results never change)."""
+        t = _lib.vdbg_tuning.from_dict(tuning)
+        self._check(self._lib.vdbg_set_tuning(self._h, C.byref(t)), "vdbg_set_tuning")
+
+    def tuning(self) -> dict:
+        t = _lib.vdbg_tuning()
+        self._check(self._lib.vdbg_get_tuning(self._h, C.byref(t)), "vdbg_get_tuning")
+        return t.as_dict()
+
     def _export(self):
         n = C.c_int64()
         cap = self.leafCount()
@@ -441,6 +451,16 @@ class MapBatch:
         n = C.c_int64()
         self._check(self._lib.vdbg_batch_leaf_count(self._h, int(map_index), C.byref(n)), "vdbg_batch_leaf_count")
         return n.value
+
+    def setTuning(self, tuning: dict) -> None:
+        """Kernel launch/layout parameters (speed only; results never change)."""
+        t = _lib.vdbg_tuning.from_dict(tuning)
+        self._check(self._lib.vdbg_set_tuning(self._h, C.byref(t)), "vdbg_set_tuning")
+
+    def tuning(self) -> dict:
+        t = _lib.vdbg_tuning()
+        self._check(self._lib.vdbg_get_tuning(self._h, C.byref(t)), "vdbg_get_tuning")
+        return t.as_dict()
 
     def exportLeaves(self, map_index: int):
         """(origins, values, masks) of one map, sorted by leaf origin."""

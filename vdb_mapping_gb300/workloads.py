@@ -348,6 +348,75 @@ class BatchedWorkload:
                 "voxels_m": sorted(set(self.resolutions))}
 
 
+class ServingWorkload:
+    """Sensor streams for the serving loop: 8 LiDARs at 10 Hz (65k-262k
+    points, 0.05 m voxels, max_range 30-60 m) and 8 depth cameras at 30 Hz
+    (640x480 = 307,200 points, 0.02 m voxels, max_range 5 m), each in its own
+    seeded room, moving along a heading. Arrivals are Poisson per stream."""
+
+    def __init__(self, name="serving", seed=5, n_lidar=8, n_depth=8, lidar_hz=10.0, depth_hz=30.0,
+                 distinct_scans=2):
+        self.name, self.seed = name, seed
+        rng = np.random.default_rng(seed)
+        self.streams = []
+        for i in range(n_lidar + n_depth):
+            depth = i >= n_lidar
+            if depth:
+                n, res, max_range, hz = 307200, 0.02, 5.0, depth_hz
+                room = RoomWorkload(seed=2000 + i, n_boxes=20)
+                dirs = depth_directions(n, yaw=rng.uniform(0, 360), pitch=rng.uniform(-20, 5))
+            else:
+                rows = int(rng.choice([32, 64, 128]))
+                n = int(rng.integers(65536, 262144 + 1)) // rows * rows
+                res, max_range, hz = 0.05, float(rng.uniform(30.0, 60.0)), lidar_hz
+                room = RoomWorkload(seed=2000 + i, n_boxes=30)
+                room.lo, room.hi = np.array([-45.0, -45.0, 0.0]), np.array([45.0, 45.0, 12.0])
+                dirs = lidar_directions(rows, n // rows)
+            self.streams.append(dict(depth=depth, n=dirs.shape[0], resolution=res, max_range=max_range, hz=hz,
+                                     room=room, dirs=dirs, speed=rng.uniform(0.02, 0.1),
+                                     heading=rng.uniform(0, 2 * np.pi)))
+        self.resolutions = [s["resolution"] for s in self.streams]
+        self.configs = [default_config(s["max_range"]) for s in self.streams]
+        self.distinct_scans = distinct_scans
+
+    def origin(self, i, k):
+        s = self.streams[i]
+        step = s["speed"] * k
+        return np.array([step * np.cos(s["heading"]), step * np.sin(s["heading"]), 1.3])
+
+    def scan(self, i, k):
+        s = self.streams[i]
+        o = self.origin(i, k)
+        d, room = s["dirs"], s["room"]
+        t = np.full(d.shape[0], np.inf)
+        _hit_room_inside(o, d, room.lo, room.hi, t)
+        _hit_boxes(o, d, room.boxes, t)
+        rng = np.random.default_rng([self.seed, i, k])
+        r = t + rng.normal(0.0, 0.01, t.shape)
+        lost = (rng.random(t.shape) < 0.03) | ~np.isfinite(t)
+        r = np.where(lost, 2.0 * s["max_range"], r)
+        return _to_pcl(o, d, r), o
+
+    def arrivals(self, duration_s, seed=None):
+        """Sorted [(time_s, stream)] of Poisson arrivals over duration_s."""
+        rng = np.random.default_rng(self.seed if seed is None else seed)
+        out = []
+        for i, s in enumerate(self.streams):
+            t = rng.exponential(1.0 / s["hz"])
+            while t < duration_s:
+                out.append((t, i))
+                t += rng.exponential(1.0 / s["hz"])
+        return sorted(out)
+
+    def describe(self) -> dict:
+        return {"workload": self.name, "streams": len(self.streams),
+                "lidar": {"count": sum(not s["depth"] for s in self.streams), "hz": self.streams[0]["hz"],
+                          "points": [s["n"] for s in self.streams if not s["depth"]], "voxel_m": 0.05},
+                "depth": {"count": sum(s["depth"] for s in self.streams), "hz": self.streams[-1]["hz"],
+                          "points": 307200, "voxel_m": 0.02, "max_range_m": 5.0},
+                "seed": self.seed}
+
+
 def get(name: str) -> Workload:
     if name == "small":
         return RoomWorkload()
@@ -357,4 +426,6 @@ def get(name: str) -> Workload:
         return StressWorkload()
     if name == "batched":
         return BatchedWorkload()
+    if name == "serving":
+        return ServingWorkload()
     raise KeyError(name)
