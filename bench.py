@@ -40,9 +40,10 @@ L2_FLUSH_BYTES = 256 << 20
 PCL_POINT_BYTES = 16
 STATUS_BYTES = 80  # device status block (DevStatus) read back by every call
 
-# DRAM traffic per launch of the dominant kernel, from one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum); None until profiled.
-NCU_TRAFFIC_BYTES = None
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
+# each kernel on a steady-state dense scan, from one ncu capture of the
+# default workload; see profiles/. None for kernels not captured.
+NCU_TRAFFIC_BYTES = {}
 
 
 def parse_args():
@@ -59,6 +60,7 @@ def parse_args():
                     help="use an evenly strided subset of N points of each scan (small profiling cases)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="simulated traffic for --workload serving")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="device-memory admission budget")
+    ap.add_argument("--no-autotune", action="store_true", help="batched mode: keep the library's default tuning")
     ap.add_argument("--batch-steps", type=int, default=4,
                     help="distinct steps generated for --workload batched (cycled)")
     ap.add_argument("--leaf-capacity", type=int, default=0,
@@ -298,25 +300,30 @@ def run_ours(args):
 
     # ---- roofline of the dominant kernel (live event times) -------------------
     hbm_peak, peak_kind = measured_peaks()
-    dda = statistics.mean(p["dda_ms"] for p in phases)
-    sweep = statistics.mean(p["sweep_ms"] for p in phases)
-    prep = statistics.mean(p["prep_ms"] for p in phases)
+    mean = lambda key: statistics.mean(p[key] for p in phases)  # noqa: E731
+    dda = mean("dda_ms")
+    apply_ms = mean("apply_ms")
+    sweep = mean("sweep_ms")
+    prep = mean("prep_ms")
     mean_u = statistics.mean(s["updates"] for s in stats)
     mean_lt = statistics.mean(s["touched_leaves"] for s in stats)
-    # Algorithmic bytes per launch (SURVEY 8d units): sweep = FP32 read+write per
-    # updated voxel + active bit r/w + visited/hit masks per touched leaf; DDA =
-    # ray record + order index per ray + one mask line per touched leaf; prep =
-    # point read + ray record write.
+    mean_runs = mean("runs")
+    # Algorithmic bytes per launch: sweep = FP32 read+write per updated voxel
+    # + active bit r/w + visited/hit masks per touched leaf; apply = the slab
+    # runs it reads (17 B) + one 64 B visited-mask line per touched leaf;
+    # traversal = ray record + order index per ray + the runs it writes;
+    # prep = point read + ray record write.
     alg = {
         "k_sweep": (8.25 * mean_u + 128.0 * mean_lt, sweep),
-        "k_dda_mark": (20.0 * n_pts + 128.0 * mean_lt, dda),
+        "k_apply_runs": (17.0 * mean_runs + 64.0 * mean_lt, apply_ms),
+        "k_dda_mark": (20.0 * n_pts + 17.0 * mean_runs, dda - apply_ms),
         "prep (k_prep+k_scan+k_scatter)": (36.0 * n_pts, prep),
     }
     dom = max(alg, key=lambda k: alg[k][1])
     dom_bytes, dom_ms = alg[dom]
     achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
     window_bytes = 12.0 * n_pts + 8.25 * mean_u + 128.0 * mean_lt
-    mean_total_ms = statistics.mean(p["total_ms"] for p in phases)
+    mean_total_ms = mean("total_ms")
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -327,14 +334,18 @@ def run_ours(args):
         "voxel_updates_per_s": updates / total_s,
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
                        "max": max(step_ms)},
-        "phases_ms": {"prep": prep, "dda_mark": dda, "sweep": sweep, "kernels_total": mean_total_ms},
+        "phases_ms": {"prep": prep, "traversal (k_mark_hits+k_dda_mark)": dda - apply_ms, "k_apply_runs": apply_ms,
+                      "sweep (k_compact+k_sweep)": sweep, "kernels_total": mean_total_ms},
         "per_scan": {"rays": n_pts, "visits": statistics.mean(s["visits"] for s in stats),
-                     "updates": mean_u, "touched_leaves": mean_lt,
+                     "runs": mean_runs, "updates": mean_u, "touched_leaves": mean_lt,
                      "new_leaves": statistics.mean(s["new_leaves"] for s in stats)},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_kind": peak_kind,
-                     "traffic": NCU_TRAFFIC_BYTES,
+                     "traffic": NCU_TRAFFIC_BYTES.get(dom),
                      "algorithmic_bytes_per_launch": dom_bytes, "launch_ms": dom_ms,
+                     "per_kernel": {k: {"GBps": b_ / (t_ / 1000.0) / 1e9 if t_ > 0 else None, "ms": t_,
+                                        "algorithmic_bytes": b_, "traffic": NCU_TRAFFIC_BYTES.get(k)}
+                                    for k, (b_, t_) in alg.items()},
                      "window_GBps": window_bytes / (mean_total_ms / 1000.0) / 1e9},
         "gpu_launches": launches,
         "wall_s_timed_region": wall,
@@ -411,12 +422,23 @@ def run_batched(args):
     sh = stream.cuda_stream
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
+    tuned = None
+    if not args.no_autotune:
+        # Autotuned launch parameters on the first sample steps (speed only;
+        # both arms use them).
+        from vdb_mapping_gb300 import autotune
+
+        tuned, _ = autotune.tune_batch(wl.resolutions, wl.configs, steps[:min(3, n_distinct)], warmup=1)
     b = MapBatch(wl.resolutions, initial_leaf_capacity=1 << 22, device=local)
+    if tuned:
+        b.setTuning(tuned)
     for i, c in enumerate(wl.configs):
         b.setConfig(i, c)
     plain = []
     for i, c in enumerate(wl.configs):
         g = OccupancyVDBMapping(wl.resolutions[i], initial_leaf_capacity=1 << 17, device=local)
+        if tuned:
+            g.setTuning(tuned)
         g.setConfig(c)
         g.addInputSource("s", c.max_range, 0)
         plain.append(g)
@@ -480,6 +502,7 @@ def run_batched(args):
                                           "p99": float(np.percentile(p_ms, 99))}},
         "batched_over_plain": (b_upd / b_s) / (p_upd / p_s),
         "maps_bit_identical": bool(same),
+        "tuning": tuned or "library defaults",
         "gpu_launches_per_step": {"batched": b.timings()["launches"],
                                   "plain": sum(g.timings()["launches"] for g in plain)},
     }

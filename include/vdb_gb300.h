@@ -155,7 +155,8 @@ typedef struct vdbg_timings
   uint64_t launches;       /* kernels launched by the call */
   uint64_t launches_total; /* kernels launched by this map since creation */
   uint64_t retries;        /* re-marking passes after a pool or hash growth */
-  uint64_t reserved0;
+  double apply_ms;         /* the run-merging kernel (k_apply_runs) alone, all passes (part of dda_ms) */
+  uint64_t runs;           /* slab runs the traversal wrote (the merging kernel's input) */
 } vdbg_timings;
 
 int vdbg_get_timings(const vdbg_map* map, vdbg_timings* out);
@@ -170,10 +171,10 @@ int vdbg_device_bytes(const vdbg_map* map, int64_t* out);
 typedef struct vdbg_tuning
 {
   int32_t rays_per_take;     /* rays a DDA warp takes from the sorted order at a time (1-1024; 16) */
-  int32_t apply_chunk_runs;  /* DDA runs an apply block merges in shared memory at a time (256-2^20; 4096) */
-  int32_t length_edges[3];   /* L1 lengths (voxels) starting the sort's length classes, descending (1024, 512, 256) */
+  int32_t apply_chunk_runs;  /* DDA runs an apply block stages and merges at a time (256-4096, a multiple of 256; 2048) */
+  int32_t length_edges[3];   /* L1 lengths (voxels) starting the sort's length classes, descending (2048, 1024, 512) */
   float hash_load;           /* block-hash load factor (0.05-0.9; 0.5); a change rebuilds the hash */
-  int32_t reserved0;
+  int32_t dda_warps_per_sm;  /* resident DDA warps per SM (2-20, even; 16) */
 } vdbg_tuning;
 
 int vdbg_set_tuning(vdbg_map* map, const vdbg_tuning* tuning);

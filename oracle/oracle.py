@@ -42,6 +42,7 @@ def load():
         "vo_cast_ray": (I64, [P, P, P, I64]),
         "vo_world_to_index": (None, [D, C.POINTER(D), P, C.c_int]),
         "vo_clip_quantise": (None, [P, I64, I64, C.POINTER(D), D, D, P]),
+        "vo_clip_quantise_variant": (None, [P, I64, I64, C.POINTER(D), D, D, C.c_int, C.c_int, P]),
         "vo_bench_replicas": (D, [D, C.POINTER(D), P, I64, I64, I64, C.POINTER(D), C.c_int, U64P]),
     }
     for name, (res, args) in sig.items():
@@ -162,6 +163,16 @@ def clip_quantise(cloud, origin, max_range, res):
     rec = np.zeros((n, 5), np.int32)
     lib.vo_clip_quantise(arr.ctypes.data, n, stride, _d3(origin), float(max_range), float(res),
                          rec.ctypes.data)
+    return rec
+
+
+def clip_quantise_variant(cloud, origin, max_range, res, w2i_divide=False, unit_reciprocal=False):
+    """As clip_quantise, under an arithmetic variant of the OpenVDB facts."""
+    lib = load()
+    arr, n, stride = _cloud(cloud)
+    rec = np.zeros((n, 5), np.int32)
+    lib.vo_clip_quantise_variant(arr.ctypes.data, n, stride, _d3(origin), float(max_range), float(res),
+                                 int(w2i_divide), int(unit_reciprocal), rec.ctypes.data)
     return rec
 
 

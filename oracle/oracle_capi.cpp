@@ -168,6 +168,27 @@ void vo_clip_quantise(const float* xyz, int64_t n, int64_t stride_floats, const 
   }
 }
 
+// The same under an arithmetic variant of the unpinned OpenVDB facts
+// (world-to-index by divide, unit() by reciprocal multiply), for the
+// sensitivity count on the stress workload.
+void vo_clip_quantise_variant(const float* xyz, int64_t n, int64_t stride_floats, const double* origin,
+                              double range, double res, int w2i_divide, int unit_reciprocal, int32_t* rec)
+{
+  Variant v;
+  v.w2i_divide      = w2i_divide != 0;
+  v.unit_reciprocal = unit_reciprocal != 0;
+  for (int64_t i = 0; i < n; ++i)
+  {
+    const float* p  = xyz + i * stride_floats;
+    const RayEnd re = clip_and_quantise(origin, p[0], p[1], p[2], range, res, v);
+    rec[5 * i + 0]  = re.valid ? 1 : 0;
+    rec[5 * i + 1]  = re.clipped ? 1 : 0;
+    rec[5 * i + 2]  = re.end.x;
+    rec[5 * i + 3]  = re.end.y;
+    rec[5 * i + 4]  = re.end.z;
+  }
+}
+
 // CPU baseline: `threads` independent maps (one per thread), each inserting
 // the same `n_scans` scans in order through insert_point_cloud. Points are
 // xyz float triplets with `stride_floats` spacing, scan s starting at

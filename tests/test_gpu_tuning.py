@@ -13,8 +13,10 @@ pytestmark = pytest.mark.gpu
 
 TUNINGS = [
     autotune.DEFAULT,
-    {"rays_per_take": 1, "apply_chunk_runs": 256, "length_edges": (3, 2, 1), "hash_load": 0.9},
-    {"rays_per_take": 32, "apply_chunk_runs": 65536, "length_edges": (4096, 64, 8), "hash_load": 0.1},
+    {"rays_per_take": 1, "apply_chunk_runs": 256, "length_edges": (3, 2, 1), "hash_load": 0.9,
+     "dda_warps_per_sm": 2},
+    {"rays_per_take": 32, "apply_chunk_runs": 4096, "length_edges": (4096, 64, 8), "hash_load": 0.1,
+     "dda_warps_per_sm": 8},
 ]
 
 
@@ -57,7 +59,9 @@ def test_invalid_tunings_rejected(vdbg):
 
     m = vdbg.OccupancyVDBMapping(0.1)
     bad = [dict(autotune.DEFAULT, rays_per_take=0), dict(autotune.DEFAULT, rays_per_take=1025),
-           dict(autotune.DEFAULT, apply_chunk_runs=100),
+           dict(autotune.DEFAULT, apply_chunk_runs=100), dict(autotune.DEFAULT, apply_chunk_runs=8192),
+           dict(autotune.DEFAULT, apply_chunk_runs=1000), dict(autotune.DEFAULT, dda_warps_per_sm=7),
+           dict(autotune.DEFAULT, dda_warps_per_sm=22),
            dict(autotune.DEFAULT, length_edges=(256, 512, 1024)), dict(autotune.DEFAULT, hash_load=0.95)]
     for t in bad:
         with pytest.raises(VdbgError):
@@ -68,8 +72,8 @@ def test_invalid_tunings_rejected(vdbg):
 def test_autotune_returns_a_candidate(vdbg):
     w = W.get("small")
     scans = [w.scan(k) for k in range(2)]
-    small = {"rays_per_take": (8, 16), "apply_chunk_runs": (4096,), "length_edges": ((1024, 512, 256),),
-             "hash_load": (0.5,)}
+    small = {"rays_per_take": (8, 16), "apply_chunk_runs": (2048,), "length_edges": ((2048, 1024, 512),),
+             "hash_load": (0.5,), "dda_warps_per_sm": (16,)}
     best, table = autotune.tune_map(w.resolution, w.config, scans, candidates=small,
                                     initial_leaf_capacity=1 << 18)
     assert best["rays_per_take"] in (8, 16)

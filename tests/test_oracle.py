@@ -343,3 +343,35 @@ def test_oracle_reproduces_golden(oracle, name):
     assert np.array_equal(origins, case["origins"])
     assert np.array_equal(values.view(np.uint32), case["values"].view(np.uint32))
     assert np.array_equal(masks, case["masks"])
+
+
+def variant_sensitivity(oracle, n_scans):
+    """Rays of the stress workload whose quantised endpoint (or clip flag)
+    changes under each arithmetic variant of the unpinned OpenVDB facts; a ray
+    whose origin and end voxels agree walks the same DDA path, so these rays
+    bound every voxel the variants could change."""
+    from vdb_mapping_gb300 import workloads as W
+
+    w = W.get("stress")
+    out = {"rays": 0, "origin_voxels_differ": {}, "w2i_divide": 0, "unit_reciprocal": 0}
+    for k in range(n_scans):
+        pts, org = w.scan(k)
+        base = oracle.clip_quantise(pts, org, w.max_range, w.resolution)
+        out["rays"] += int(base[:, 0].sum())
+        for name, kw in (("w2i_divide", {"w2i_divide": True}), ("unit_reciprocal", {"unit_reciprocal": True})):
+            rec = oracle.clip_quantise_variant(pts, org, w.max_range, w.resolution, **kw)
+            out[name] += int(np.count_nonzero(np.any(rec != base, axis=1)))
+            o1 = oracle.world_to_index(w.resolution, org)
+            o2 = oracle.world_to_index(w.resolution, org, divide=True)
+            out["origin_voxels_differ"][k] = o1 != o2
+    return out
+
+
+def test_variant_sensitivity_on_stress_workload(oracle):
+    # The default reading (multiply by 1/res, unit() by division) is the one
+    # the reference's own tests pin and the GPU path implements; the counts
+    # say how many stress-config rays the two unpinned readings would move.
+    s = variant_sensitivity(oracle, 20)
+    assert s["rays"] > 1_000_000
+    assert s["w2i_divide"] >= 0 and s["unit_reciprocal"] >= 0
+    print("stress variant sensitivity:", s)

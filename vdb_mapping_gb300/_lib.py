@@ -80,11 +80,12 @@ class vdbg_timings(C.Structure):
         ("launches", C.c_uint64),
         ("launches_total", C.c_uint64),
         ("retries", C.c_uint64),
-        ("reserved0", C.c_uint64),
+        ("apply_ms", C.c_double),
+        ("runs", C.c_uint64),
     ]
 
     def as_dict(self):
-        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved0"}
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 class vdbg_tuning(C.Structure):
@@ -93,12 +94,13 @@ class vdbg_tuning(C.Structure):
         ("apply_chunk_runs", C.c_int32),
         ("length_edges", C.c_int32 * 3),
         ("hash_load", C.c_float),
-        ("reserved0", C.c_int32),
+        ("dda_warps_per_sm", C.c_int32),
     ]
 
     def as_dict(self):
         return {"rays_per_take": self.rays_per_take, "apply_chunk_runs": self.apply_chunk_runs,
-                "length_edges": tuple(self.length_edges), "hash_load": round(float(self.hash_load), 4)}
+                "length_edges": tuple(self.length_edges), "hash_load": round(float(self.hash_load), 4),
+                "dda_warps_per_sm": self.dda_warps_per_sm}
 
     @classmethod
     def from_dict(cls, d):
@@ -108,6 +110,7 @@ class vdbg_tuning(C.Structure):
         for k in range(3):
             t.length_edges[k] = int(d["length_edges"][k])
         t.hash_load = float(d["hash_load"])
+        t.dda_warps_per_sm = int(d.get("dda_warps_per_sm", 16))
         return t
 
 

@@ -1,8 +1,9 @@
 """Autotuner of the insertion kernels' launch and layout parameters.
 
-The parameters (``vdbg_tuning``: rays a DDA warp takes from the sorted order
-at a time, runs an apply block merges at a time, the L1 edges of the sort's
-length classes, the block-hash load factor) change speed only, never the map.
+The parameters (``vdbg_tuning``: resident DDA warps per SM, rays a DDA warp
+takes from the sorted order at a time, runs an apply block merges at a time,
+the L1 edges of the sort's length classes, the block-hash load factor) change
+speed only, never the map.
 ``tune`` times candidates on a sample of the caller's own scans, each on a
 fresh map (or batch) so the timed inserts see the same map states, and keeps
 the fastest by coordinate descent: one parameter at a time, starting from the
@@ -12,13 +13,15 @@ from __future__ import annotations
 
 import statistics
 
-DEFAULT = {"rays_per_take": 16, "apply_chunk_runs": 4096, "length_edges": (1024, 512, 256), "hash_load": 0.5}
+DEFAULT = {"rays_per_take": 16, "apply_chunk_runs": 2048, "length_edges": (2048, 1024, 512), "hash_load": 0.5,
+           "dda_warps_per_sm": 16}
 
 CANDIDATES = {
     "rays_per_take": (8, 16, 32),
-    "apply_chunk_runs": (2048, 4096, 8192),
+    "apply_chunk_runs": (1024, 2048, 4096),
     "length_edges": ((512, 256, 128), (1024, 512, 256), (2048, 1024, 512), (2048, 768, 256)),
     "hash_load": (0.25, 0.5),
+    "dda_warps_per_sm": (6, 8, 12, 16, 20),
 }
 
 
@@ -50,7 +53,7 @@ def tune(make, insert, steps, warmup=1, repeats=1, candidates=None, log=None):
     table = []
     best_ms = _measure(make, insert, steps, best, warmup, repeats)
     table.append((dict(best), best_ms))
-    for name in ("length_edges", "rays_per_take", "apply_chunk_runs", "hash_load"):
+    for name in ("dda_warps_per_sm", "length_edges", "rays_per_take", "apply_chunk_runs", "hash_load"):
         for value in cand[name]:
             if value == best[name]:
                 continue

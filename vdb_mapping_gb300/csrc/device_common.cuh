@@ -82,7 +82,7 @@ struct DevStatus
   uint32_t n_blocks;    // block bump allocator
   uint32_t inflight;    // lanes that ended a DDA pass with a ray in flight
   uint32_t pad32;
-  unsigned long long pad[1];
+  unsigned long long runs;  // slab runs written by the traversal (all passes)
 };
 
 struct LogOdds
@@ -250,6 +250,56 @@ __device__ __forceinline__ int ld_acquire_s32(const int* p)
 __device__ __forceinline__ void st_release_s32(int* p, int v)
 {
   asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// ---- bulk asynchronous copies (global -> shared) completed on an mbarrier ----
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+// Orders this thread's earlier shared-memory accesses (and an mbarrier
+// initialisation) before later asynchronous-proxy accesses to shared memory.
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+// `bytes` from global `src` to shared `dst`; both 16-byte aligned, bytes a
+// multiple of 16. Completion is counted on `bar`.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, unsigned long long* bar)
+{
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                 smem_u32(dst)),
+               "l"(__cvta_generic_to_global(src)), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity)
+{
+  uint32_t ok;
+  asm volatile(
+    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+    : "=r"(ok)
+    : "r"(smem_u32(bar)), "r"(parity)
+    : "memory");
+  return ok != 0u;
+}
+// Bounded wait for phase `parity` of `bar`; false when it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, uint32_t parity)
+{
+  for (uint32_t i = 0; i < kSpinLimit; ++i)
+  {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (i > 64) __nanosleep(128);
+  }
+  return false;
 }
 
 // Murmur3 64-bit finaliser (published mixing function).

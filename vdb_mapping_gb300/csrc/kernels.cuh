@@ -505,6 +505,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
   if (lane == 0)
   {
     rb.count[gw] = count;
+    if (count) atomicAdd(&m.st->runs, static_cast<unsigned long long>(count));
     WarpState w;
     w.chunk_next = chunk_next;
     w.chunk_end  = chunk_end;
@@ -534,19 +535,24 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
 // ---------------------------------------------------------------------------
 // k_apply_runs: merges the scan's slab runs and ORs them into the update masks.
 //
-// Persistent blocks take chunks of rb.apply_chunk runs (written together by
-// warps walking neighbouring rays, so a chunk repeats few leaves). Each thread
-// ORs its runs into the block's leaf table in shared memory (the lanes of a
-// warp holding the same leaf probe it once, through their leader); the first
-// insertion of a leaf appends it to the table's list. The block then drains
-// the list in two steps: one thread per listed leaf resolves its slot through
-// the block index (allocating leaves and blocks as needed) and marks it
-// touched, then eight threads per leaf OR its eight mask words into the update
-// masks, so the words of one leaf go out as one coalesced atomic request. A
-// run that finds the table full is applied directly.
+// Persistent blocks take chunks of rb.apply_chunk runs of one warp segment
+// (written together by a warp walking neighbouring rays, so a chunk repeats
+// few leaves). A chunk is staged in shared memory by bulk asynchronous copies
+// (three: keys, bits, slab indices) completed on an mbarrier; the copy of a
+// block's next chunk is issued as soon as the current one has been read, so
+// it overlaps the drain. Each thread ORs its runs into the block's leaf table
+// in shared memory (lanes of a warp holding the same leaf probe it once,
+// through their leader); the first insertion of a leaf appends it to the
+// table's list. The block then drains the list in two steps: one thread per
+// listed leaf resolves its slot through the block index (allocating leaves
+// and blocks as needed) and marks it touched, then eight threads per leaf OR
+// its eight mask words into the update masks, so the words of one leaf go
+// out as one coalesced atomic request. A run that finds the table full is
+// applied directly.
 // ---------------------------------------------------------------------------
-constexpr int kApplyThreads = 256;
-constexpr int kApplyTable   = 512;  // 2^9 entries, see apply_hash
+constexpr int kApplyThreads      = 256;
+constexpr int kApplyTable        = 512;   // 2^9 entries, see apply_hash
+constexpr uint32_t kApplyMaxChunk = 4096;  // runs staged at a time, at most
 
 struct ApplySmem
 {
@@ -554,8 +560,17 @@ struct ApplySmem
   unsigned int words[kApplyTable][16];  // 8 mask words as lo/hi halves
   int slot[kApplyTable];                // resolved leaf slot of a listed entry
   unsigned short list[kApplyTable];     // entries in use
+  unsigned long long bar;               // completion of the staged chunk's copies
   unsigned int count;
+  unsigned int next;                    // the block's next chunk
+  unsigned int failed;
 };
+
+// Dynamic shared memory of k_apply_runs for chunks of `chunk` runs.
+__host__ __device__ constexpr size_t apply_stage_bytes(uint32_t chunk)
+{
+  return static_cast<size_t>(chunk) * 17 + 16;
+}
 
 __device__ __forceinline__ uint32_t apply_hash(unsigned long long key)
 {
@@ -586,44 +601,111 @@ __device__ __forceinline__ int apply_resolve(const MapView& m, const ChannelView
   return slot;
 }
 
-__global__ void __launch_bounds__(kApplyThreads, 4) k_apply_runs(RunBuffer rb, MapView m, ChannelView c)
+// Runs [start, end) of work item `item` (segment-major chunks), end <= start
+// when the item is empty.
+__device__ __forceinline__ void apply_item_range(const RunBuffer& rb, uint32_t cps, uint32_t item, uint32_t& sg,
+                                                 uint32_t& start, uint32_t& end)
+{
+  sg              = item / cps;
+  start           = (item % cps) * rb.apply_chunk;
+  const uint32_t c = rb.count[sg];
+  end             = min(start + rb.apply_chunk, c);
+}
+
+// First non-empty item at or after `item` in this block's stride (items when none).
+__device__ __forceinline__ uint32_t apply_next_item(const RunBuffer& rb, uint32_t cps, uint32_t items, uint32_t item)
+{
+  for (; item < items; item += gridDim.x)
+  {
+    uint32_t sg, start, end;
+    apply_item_range(rb, cps, item, sg, start, end);
+    if (start < end) return item;
+  }
+  return items;
+}
+
+// Stages the runs of `item` (thread 0 only). Segments start on 16-run
+// boundaries and chunks are multiples of 256 runs, so every copy starts
+// 16-byte aligned; lengths are rounded up to 16 bytes, which stays inside the
+// segment.
+__device__ __forceinline__ void apply_stage(const RunBuffer& rb, uint32_t cps, uint32_t item, ApplySmem& t,
+                                            unsigned long long* s_key, unsigned long long* s_bits,
+                                            unsigned char* s_slab)
+{
+  uint32_t sg, start, end;
+  apply_item_range(rb, cps, item, sg, start, end);
+  const size_t base  = static_cast<size_t>(sg) * rb.seg + start;
+  const uint32_t n   = end - start;
+  const uint32_t b8  = (n * 8u + 15u) & ~15u;
+  const uint32_t b1  = (n + 15u) & ~15u;
+  mbar_arrive_expect_tx(&t.bar, 2u * b8 + b1);
+  bulk_copy_g2s(s_key, rb.key + base, b8, &t.bar);
+  bulk_copy_g2s(s_bits, rb.bits + base, b8, &t.bar);
+  bulk_copy_g2s(s_slab, rb.slab + base, b1, &t.bar);
+}
+
+__global__ void __launch_bounds__(kApplyThreads, 3) k_apply_runs(RunBuffer rb, MapView m, ChannelView c)
 {
   __shared__ ApplySmem t;
-  __shared__ uint32_t failed;
+  extern __shared__ __align__(16) unsigned char stage[];
+  unsigned long long* s_key  = reinterpret_cast<unsigned long long*>(stage);
+  unsigned long long* s_bits = s_key + rb.apply_chunk;
+  unsigned char* s_slab      = reinterpret_cast<unsigned char*>(s_bits + rb.apply_chunk);
+  const uint32_t cps         = (rb.seg + rb.apply_chunk - 1) / rb.apply_chunk;
+  const uint32_t items       = rb.warps * cps;
   // The error word can be set by other blocks while this one starts: read it
   // once for the whole block, so that either every thread returns or none
   // does (the barriers below need all of them).
-  if (threadIdx.x == 0) failed = ld_relaxed_u32(&m.st->error);
-  __syncthreads();
-  if (failed != 0u) return;
+  if (threadIdx.x == 0)
+  {
+    t.failed = ld_relaxed_u32(&m.st->error);
+    t.count  = 0u;
+    t.next   = items;
+    if (t.failed == 0u)
+    {
+      mbar_init(&t.bar, 1);
+      fence_proxy_async_smem();
+      t.next = apply_next_item(rb, cps, items, blockIdx.x);
+      if (t.next < items) apply_stage(rb, cps, t.next, t, s_key, s_bits, s_slab);
+    }
+  }
   for (int e = threadIdx.x; e < kApplyTable; e += kApplyThreads)
   {
     t.key[e] = kEmptyKey;
 #pragma unroll
     for (int w = 0; w < 16; ++w) t.words[e][w] = 0u;
   }
-  if (threadIdx.x == 0) t.count = 0u;
   __syncthreads();
-  const int lane = static_cast<int>(threadIdx.x & 31);
-  // Work items: (segment, chunk of rb.apply_chunk runs), segment-major.
-  const uint32_t chunks_per_seg = (rb.seg + rb.apply_chunk - 1) / rb.apply_chunk;
-  const uint32_t items          = rb.warps * chunks_per_seg;
-  for (uint32_t item = blockIdx.x; item < items; item += gridDim.x)
+  if (t.failed != 0u) return;
+  const int lane  = static_cast<int>(threadIdx.x & 31);
+  uint32_t parity = 0;
+  for (uint32_t item = t.next; item < items;)
   {
-    const uint32_t sg    = item / chunks_per_seg;
-    const uint32_t start = (item % chunks_per_seg) * rb.apply_chunk;
-    const uint32_t cnt   = rb.count[sg];
-    if (start >= cnt) continue;  // uniform across the block
-    const size_t base  = static_cast<size_t>(sg) * rb.seg;
-    const uint32_t end = min(start + rb.apply_chunk, cnt);
+    uint32_t sg, start, end;
+    apply_item_range(rb, cps, item, sg, start, end);
+    const bool staged = mbar_wait_bounded(&t.bar, parity);
+    parity ^= 1u;
+    if (__syncthreads_or(!staged))
+    {
+      // The copy did not complete in time: report, and wait (bounded) once
+      // more so no copy is left writing into this block's shared memory.
+      if (threadIdx.x == 0)
+      {
+        atomicOr(&m.st->error, kErrSpin);
+        mbar_wait_bounded(&t.bar, parity ^ 1u);
+      }
+      __syncthreads();
+      return;
+    }
     // Whole warps walk the chunk (tail lanes idle) so the match below sees full warps.
     for (uint32_t i0 = start + (threadIdx.x & ~31u); i0 < end; i0 += kApplyThreads)
     {
       const uint32_t i              = i0 + static_cast<uint32_t>(lane);
       const bool have               = i < end;
-      const unsigned long long key  = have ? rb.key[base + i] : kEmptyKey;
-      const unsigned long long bits = have ? rb.bits[base + i] : 0ull;
-      const int w                   = have ? rb.slab[base + i] : 0;
+      const uint32_t k              = i - start;
+      const unsigned long long key  = have ? s_key[k] : kEmptyKey;
+      const unsigned long long bits = have ? s_bits[k] : 0ull;
+      const int w                   = have ? s_slab[k] : 0;
       const unsigned peers          = __match_any_sync(0xffffffffu, key);
       const int leader              = __ffs(peers) - 1;
       int h                         = -1;
@@ -632,21 +714,21 @@ __global__ void __launch_bounds__(kApplyThreads, 4) k_apply_runs(RunBuffer rb, M
         uint32_t p = apply_hash(key);
         for (int probe = 0; probe < 16; ++probe)
         {
-          unsigned long long k = t.key[p];
-          if (k == kEmptyKey)
+          unsigned long long kk = t.key[p];
+          if (kk == kEmptyKey)
           {
             const unsigned long long prev = atomicCAS(&t.key[p], kEmptyKey, key);
             if (prev == kEmptyKey)
             {
               t.list[atomicAdd(&t.count, 1u)] = static_cast<unsigned short>(p);
-              k                                = key;
+              kk                               = key;
             }
             else
             {
-              k = prev;
+              kk = prev;
             }
           }
-          if (k == key)
+          if (kk == key)
           {
             h = static_cast<int>(p);
             break;
@@ -670,6 +752,16 @@ __global__ void __launch_bounds__(kApplyThreads, 4) k_apply_runs(RunBuffer rb, M
       }
     }
     __syncthreads();
+    // The staging buffer is free: start copying the block's next chunk.
+    if (threadIdx.x == 0)
+    {
+      t.next = apply_next_item(rb, cps, items, item + gridDim.x);
+      if (t.next < items)
+      {
+        fence_proxy_async_smem();
+        apply_stage(rb, cps, t.next, t, s_key, s_bits, s_slab);
+      }
+    }
     const uint32_t n_used = t.count;
     for (uint32_t k = threadIdx.x; k < n_used; k += kApplyThreads)
     {
@@ -690,6 +782,7 @@ __global__ void __launch_bounds__(kApplyThreads, 4) k_apply_runs(RunBuffer rb, M
       if (w == 0) t.key[e] = kEmptyKey;
     }
     __syncthreads();
+    item = t.next;
     if (threadIdx.x == 0) t.count = 0u;
     __syncthreads();
   }

@@ -69,6 +69,7 @@ struct vdbg_map
   cudaStream_t stream   = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t ev_prep = nullptr, ev_dda = nullptr;  // after k_scatter, after k_dda_mark
+  cudaEvent_t ev_a0 = nullptr, ev_a1 = nullptr;     // around each k_apply_runs launch
   bool timed_prep       = false;
   vdbg_timings timings{};
 
@@ -117,7 +118,9 @@ struct vdbg_map
 
   int64_t bytes         = 0;
   int num_sms           = 152;
-  vdbg_tuning tuning{16, 4096, {1024, 512, 256}, 0.5f, 0};
+  vdbg_tuning tuning{16, 2048, {2048, 1024, 512}, 0.5f, 16};
+  uint32_t apply_grid_chunk = 0;   // apply_chunk the cached grid size is for
+  unsigned apply_grid_blocks = 0;
 };
 
 namespace {
@@ -499,6 +502,7 @@ void fill_stats(vdbg_map* m, uint32_t leaves_before, vdbg_scan_stats* st)
 
 void record_timings(vdbg_map* m)
 {
+  m->timings.runs = m->h_status->runs;
   float ms = 0.f;
   cudaEventElapsedTime(&ms, m->ev0, m->ev1);
   m->timings.total_ms = ms;
@@ -591,8 +595,26 @@ int launch_prep(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t st
 
 // Allocates (or grows) the DDA run buffer: dda_warps segments of `seg` runs,
 // plus the per-lane and per-warp resume state.
+// Persistent grid of k_apply_runs: as many blocks as fit on the device with
+// the staging buffer of `chunk` runs.
+unsigned apply_grid(vdbg_map* m, uint32_t chunk)
+{
+  if (m->apply_grid_chunk != chunk)
+  {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_runs, kApplyThreads,
+                                                      apply_stage_bytes(chunk)) != cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+    m->apply_grid_chunk  = chunk;
+    m->apply_grid_blocks = static_cast<unsigned>(m->num_sms * per_sm);
+  }
+  return m->apply_grid_blocks;
+}
+
 int ensure_runs(vdbg_map* m, uint32_t seg)
 {
+  seg = (seg + 15u) & ~15u;  // segments start on 16-run boundaries (bulk copies)
   if (m->run_key && seg <= m->run_seg) return VDBG_OK;
   const size_t W = m->dda_warps;
   dev_free(m, m->run_key, W * m->run_seg);
@@ -636,6 +658,14 @@ int grow_for(vdbg_map* m, uint64_t requested);
 int grow_blocks_for(vdbg_map* m, uint64_t requested);
 int rebuild_hash(vdbg_map* m, uint32_t hsize, uint32_t n);
 
+// Adds the last k_apply_runs launch's duration (its events are complete after
+// a status fetch).
+void add_apply_time(vdbg_map* m)
+{
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, m->ev_a0, m->ev_a1) == cudaSuccess) m->timings.apply_ms += ms;
+}
+
 // castRayIntoGrid for every ray (VDBMapping.hpp:550-566) and the endpoint
 // hits (VDBMapping.hpp:533-536), into channel `c`: endpoint hits once, then
 // DDA passes, each followed by k_apply_runs, until no ray is left in flight.
@@ -646,7 +676,8 @@ int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, 
                    const RunBuffer& rb, LaneState* ls, WarpState* ws, bool may_grow, cudaStream_t s)
 {
   const unsigned hit_blocks   = static_cast<unsigned>((n + 255) / 256);
-  const unsigned apply_blocks = static_cast<unsigned>(m->num_sms) * 8;
+  const unsigned apply_blocks = apply_grid(m, rb.apply_chunk);
+  const size_t apply_smem     = apply_stage_bytes(rb.apply_chunk);
   k_mark_hits<<<hit_blocks, 256, 0, s>>>(rays, order, t, map_view(m), channel_view(c));
   m->timings.launches += 1;
   uint32_t passes = 0;
@@ -655,11 +686,14 @@ int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, 
     VDBG_CUDA(cudaMemsetAsync(&m->d_status->inflight, 0, sizeof(uint32_t), s));
     k_dda_mark<<<rb.warps / kDdaWarps, kDdaWarps * 32, 0, s>>>(rays, order, t, map_view(m), rb, ls, ws,
                                                               passes > 0 ? 1 : 0);
-    k_apply_runs<<<apply_blocks, kApplyThreads, 0, s>>>(rb, map_view(m), channel_view(c));
+    VDBG_CUDA(cudaEventRecord(m->ev_a0, s));
+    k_apply_runs<<<apply_blocks, kApplyThreads, apply_smem, s>>>(rb, map_view(m), channel_view(c));
+    VDBG_CUDA(cudaEventRecord(m->ev_a1, s));
     VDBG_CUDA(cudaGetLastError());
     m->timings.launches += 2;
     ++passes;
     VDBG_TRY(fetch_status(m, s));
+    add_apply_time(m);
     for (int attempt = 0; m->h_status->error != 0u; ++attempt)
     {
       const uint32_t err = m->h_status->error;
@@ -693,11 +727,14 @@ int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, 
       clear_error_keep_counters(m);
       VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
       k_mark_hits<<<hit_blocks, 256, 0, s>>>(rays, order, t, map_view(m), channel_view(c));
-      k_apply_runs<<<apply_blocks, kApplyThreads, 0, s>>>(rb, map_view(m), channel_view(c));
+      VDBG_CUDA(cudaEventRecord(m->ev_a0, s));
+      k_apply_runs<<<apply_blocks, kApplyThreads, apply_smem, s>>>(rb, map_view(m), channel_view(c));
+      VDBG_CUDA(cudaEventRecord(m->ev_a1, s));
       VDBG_CUDA(cudaGetLastError());
       m->timings.launches += 2;
       m->timings.retries += 1;
       VDBG_TRY(fetch_status(m, s));
+      add_apply_time(m);
     }
     m->n_leaves = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
     m->n_blocks = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
@@ -1084,10 +1121,14 @@ int create_impl(int n_maps, const double* resolutions, const vdbg_options* optio
   if (cudaSetDevice(m->device) != cudaSuccess) return fail(VDBG_ERR_CUDA);
   if (cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, m->device) != cudaSuccess)
     return fail(VDBG_ERR_CUDA);
-  m->dda_warps = static_cast<uint32_t>(m->num_sms) * 10u * kDdaWarps;  // k_dda_mark's resident warps
+  m->dda_warps = static_cast<uint32_t>(m->num_sms) * static_cast<uint32_t>(m->tuning.dda_warps_per_sm);
+  if (cudaFuncSetAttribute(k_apply_runs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(apply_stage_bytes(kApplyMaxChunk))) != cudaSuccess)
+    return fail(VDBG_ERR_CUDA);
   if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(VDBG_ERR_CUDA);
   if (cudaEventCreate(&m->ev0) != cudaSuccess || cudaEventCreate(&m->ev1) != cudaSuccess ||
-      cudaEventCreate(&m->ev_prep) != cudaSuccess || cudaEventCreate(&m->ev_dda) != cudaSuccess)
+      cudaEventCreate(&m->ev_prep) != cudaSuccess || cudaEventCreate(&m->ev_dda) != cudaSuccess ||
+      cudaEventCreate(&m->ev_a0) != cudaSuccess || cudaEventCreate(&m->ev_a1) != cudaSuccess)
     return fail(VDBG_ERR_CUDA);
   if (cudaMallocHost(reinterpret_cast<void**>(&m->h_status), sizeof(DevStatus)) != cudaSuccess)
     return fail(VDBG_ERR_OUT_OF_MEMORY);
@@ -1255,6 +1296,8 @@ int vdbg_destroy(vdbg_map* m)
   if (m->ev1) cudaEventDestroy(m->ev1);
   if (m->ev_prep) cudaEventDestroy(m->ev_prep);
   if (m->ev_dda) cudaEventDestroy(m->ev_dda);
+  if (m->ev_a0) cudaEventDestroy(m->ev_a0);
+  if (m->ev_a1) cudaEventDestroy(m->ev_a1);
   if (m->stream) cudaStreamDestroy(m->stream);
   delete m;
   return VDBG_OK;
@@ -1432,14 +1475,34 @@ int vdbg_set_tuning(vdbg_map* m, const vdbg_tuning* t)
 {
   if (!m || !t) return VDBG_ERR_INVALID_ARGUMENT;
   if (t->rays_per_take < 1 || t->rays_per_take > 1024) return VDBG_ERR_INVALID_ARGUMENT;
-  if (t->apply_chunk_runs < 256 || t->apply_chunk_runs > (1 << 20)) return VDBG_ERR_INVALID_ARGUMENT;
+  if (t->apply_chunk_runs < 256 || t->apply_chunk_runs > static_cast<int32_t>(kApplyMaxChunk) ||
+      (t->apply_chunk_runs % 256) != 0)
+    return VDBG_ERR_INVALID_ARGUMENT;
   if (!(t->length_edges[0] > t->length_edges[1] && t->length_edges[1] > t->length_edges[2] &&
         t->length_edges[2] > 0))
     return VDBG_ERR_INVALID_ARGUMENT;
   if (!(t->hash_load > 0.05f && t->hash_load <= 0.9f)) return VDBG_ERR_INVALID_ARGUMENT;
+  if (t->dda_warps_per_sm < kDdaWarps || t->dda_warps_per_sm > 10 * kDdaWarps || (t->dda_warps_per_sm % kDdaWarps))
+    return VDBG_ERR_INVALID_ARGUMENT;
   VDBG_TRY(set_device(m));
+  VDBG_CUDA(cudaStreamSynchronize(m->stream));
   const bool rehash = t->hash_load != m->tuning.hash_load;
-  m->tuning         = *t;
+  if (t->dda_warps_per_sm != m->tuning.dda_warps_per_sm)
+  {
+    // The run buffer and the DDA resume state are per warp: drop them, the
+    // next insertion sizes them for the new warp count.
+    const size_t W = m->dda_warps;
+    dev_free(m, m->run_key, W * m->run_seg);
+    dev_free(m, m->run_bits, W * m->run_seg);
+    dev_free(m, m->run_slab, W * m->run_seg);
+    dev_free(m, m->run_count, W);
+    dev_free(m, m->lstate, W * 32);
+    dev_free(m, m->wstate, W);
+    m->run_seg     = 0;
+    m->passes_last = 0;
+    m->dda_warps   = static_cast<uint32_t>(m->num_sms) * static_cast<uint32_t>(t->dda_warps_per_sm);
+  }
+  m->tuning = *t;
   if (rehash)
   {
     VDBG_TRY(rebuild_hash(m, hash_size_for(m, m->bcapacity), m->n_blocks));
