@@ -42,8 +42,10 @@ STATUS_BYTES = 80  # device status block (DevStatus) read back by every call
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
 # each kernel on a steady-state dense scan, from one ncu capture of the
-# default workload; see profiles/. None for kernels not captured.
-NCU_TRAFFIC_BYTES = {}
+# default workload (profiles/dram_traffic_dense_street.md). Only meaningful
+# for the dense workload; other workloads report None.
+NCU_TRAFFIC_BYTES = {"k_dda_mark": 1235.5e6, "k_apply_runs": 1722.0e6, "k_sweep": 3278.5e6,
+                     "prep (k_prep+k_scan+k_scatter)": 4.2e6}
 
 
 def parse_args():
@@ -321,6 +323,7 @@ def run_ours(args):
     }
     dom = max(alg, key=lambda k: alg[k][1])
     dom_bytes, dom_ms = alg[dom]
+    traffic = NCU_TRAFFIC_BYTES if (wl.name == "dense" and not args.points) else {}
     achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
     window_bytes = 12.0 * n_pts + 8.25 * mean_u + 128.0 * mean_lt
     mean_total_ms = mean("total_ms")
@@ -341,10 +344,10 @@ def run_ours(args):
                      "new_leaves": statistics.mean(s["new_leaves"] for s in stats)},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_kind": peak_kind,
-                     "traffic": NCU_TRAFFIC_BYTES.get(dom),
+                     "traffic": traffic.get(dom),
                      "algorithmic_bytes_per_launch": dom_bytes, "launch_ms": dom_ms,
                      "per_kernel": {k: {"GBps": b_ / (t_ / 1000.0) / 1e9 if t_ > 0 else None, "ms": t_,
-                                        "algorithmic_bytes": b_, "traffic": NCU_TRAFFIC_BYTES.get(k)}
+                                        "algorithmic_bytes": b_, "traffic": traffic.get(k)}
                                     for k, (b_, t_) in alg.items()},
                      "window_GBps": window_bytes / (mean_total_ms / 1000.0) / 1e9},
         "gpu_launches": launches,

@@ -164,6 +164,21 @@ int vdbg_get_timings(const vdbg_map* map, vdbg_timings* out);
 /* Device bytes held by the map. */
 int vdbg_device_bytes(const vdbg_map* map, int64_t* out);
 
+/* Change set (the grid updateMap returns, VDBMapping.hpp:731-792): with
+ * tracking on, every call that integrates (insert, integrate_update,
+ * update_map, batch insert) replaces the change set with the voxels whose
+ * active state its update grid flipped: `active` holds the flipped voxels,
+ * `value` those flipped on (by a hit); a miss only turns voxels off. When a
+ * call integrates several sources' update grids the set is that of the last
+ * one (sources integrate in id order). vdbg_export_changes returns the leaves
+ * with a flip, sorted by origin: origins int32[n][3], active and value
+ * uint64[n][8] (bit i of word w = leaf offset 64w+i), of map `map` of a batch
+ * (-1: every map). Tracking costs 136 bytes per leaf slot and a little sweep
+ * time; off by default. */
+int vdbg_track_changes(vdbg_map* map, int enable);
+int vdbg_export_changes(vdbg_map* map, int map_index, int64_t capacity, int32_t* origins, uint64_t* active,
+                        uint64_t* value, int64_t* n_out);
+
 /* Launch and layout parameters of the insertion kernels (no counterpart in
  * the reference). They change speed only, never results; the package's
  * autotuner (vdb_mapping_gb300/autotune.py) picks them by timing candidates

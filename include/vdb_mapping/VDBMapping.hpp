@@ -25,6 +25,7 @@
 #include <cstdint>
 #include <iostream>
 #include <map>
+#include <tuple>
 #include <memory>
 #include <mutex>
 #include <shared_mutex>
@@ -296,13 +297,46 @@ class DeviceUpdateGrid
 {
 public:
   using Ptr = std::shared_ptr<DeviceUpdateGrid>;
+  /*! Binds the grid to raycastPointCloud; on a change grid returned by
+   * updateMap it reads the change set like the reference's bool accessor. */
   struct Accessor
   {
     DeviceUpdateGrid* grid = nullptr;
+    bool isValueOn(const openvdb::Coord& c) const { return grid && grid->changeBit(c, 0); }
+    bool getValue(const openvdb::Coord& c) const { return grid && grid->changeBit(c, 8); }
   };
   static Ptr create(bool /*background*/ = false) { return std::make_shared<DeviceUpdateGrid>(); }
   Accessor getAccessor() { return Accessor{this}; }
-  bool empty() const { return !m_pending; }
+  bool empty() const { return !m_pending && m_change_origins.empty(); }
+  /*! Active voxels of a change grid (voxels whose occupancy flipped). */
+  uint64_t activeVoxelCount() const
+  {
+    uint64_t n = 0;
+    for (size_t i = 0; i < m_change_origins.size() / 3; ++i)
+      for (int w = 0; w < 8; ++w) n += static_cast<uint64_t>(__builtin_popcountll(m_change_words[i * 16 + w]));
+    return n;
+  }
+
+  // Internal: fills this grid with a change set (origins [n][3], active and
+  // value masks [n][8]).
+  void setChanges(std::vector<int32_t> origins, const std::vector<uint64_t>& active,
+                  const std::vector<uint64_t>& value)
+  {
+    const size_t n   = origins.size() / 3;
+    m_change_origins = std::move(origins);
+    m_change_words.assign(n * 16, 0);
+    m_change_index.clear();
+    for (size_t i = 0; i < n; ++i)
+    {
+      for (int w = 0; w < 8; ++w)
+      {
+        m_change_words[i * 16 + w]     = active[i * 8 + w];
+        m_change_words[i * 16 + 8 + w] = value[i * 8 + w];
+      }
+      m_change_index[std::make_tuple(m_change_origins[3 * i], m_change_origins[3 * i + 1],
+                                     m_change_origins[3 * i + 2])] = i;
+    }
+  }
 
   // Internal: the hidden source id of this grid inside `map`.
   const std::string& bind(vdbg_map* map)
@@ -320,8 +354,19 @@ public:
   bool m_pending = false;
 
 private:
+  bool changeBit(const openvdb::Coord& c, int half) const
+  {
+    const auto it = m_change_index.find(std::make_tuple(c.x() & ~7, c.y() & ~7, c.z() & ~7));
+    if (it == m_change_index.end()) return false;
+    const uint32_t off = (static_cast<uint32_t>(c.x() & 7) << 6) | (static_cast<uint32_t>(c.y() & 7) << 3) |
+                         static_cast<uint32_t>(c.z() & 7);
+    return (m_change_words[it->second * 16 + half + (off >> 6)] >> (off & 63)) & 1ull;
+  }
   vdbg_map* m_map = nullptr;
   std::string m_id;
+  std::vector<int32_t> m_change_origins;
+  std::vector<uint64_t> m_change_words;
+  std::map<std::tuple<int32_t, int32_t, int32_t>, size_t> m_change_index;
 };
 
 /*!
@@ -438,16 +483,31 @@ public:
     return true;
   }
 
-  /*! VDBMapping.hpp:731-792. The change grid is not produced (an empty grid
-   * is returned). */
+  /*! VDBMapping.hpp:731-792. Returns the change grid: voxels whose
+   * occupancy flipped are active, with value true where a hit turned them on
+   * (the map tracks changes from the first call on). */
   typename UpdateGridT::Ptr updateMap(const typename UpdateGridT::Ptr& temp_grid)
   {
     typename UpdateGridT::Ptr change = UpdateGridT::create(false);
     if (!temp_grid || temp_grid->empty()) return change;
+    if (!m_tracking)
+    {
+      check(vdbg_track_changes(m_dev->map, 1), "vdbg_track_changes");
+      m_tracking = true;
+    }
     const std::string& id = temp_grid->bind(m_dev->map);
     check(vdbg_update_map(m_dev->map, id.c_str(), nullptr, nullptr), "vdbg_update_map");
     temp_grid->m_pending = false;
     ++m_dev->version;
+    int64_t n = 0;
+    int s     = vdbg_export_changes(m_dev->map, -1, 0, nullptr, nullptr, nullptr, &n);
+    if (s != VDBG_OK && s != VDBG_ERR_BUFFER_TOO_SMALL) check(s, "vdbg_export_changes");
+    std::vector<int32_t> origins(static_cast<size_t>(n) * 3);
+    std::vector<uint64_t> active(static_cast<size_t>(n) * 8), value(static_cast<size_t>(n) * 8);
+    if (n > 0)
+      check(vdbg_export_changes(m_dev->map, -1, n, origins.data(), active.data(), value.data(), &n),
+            "vdbg_export_changes");
+    change->setChanges(std::move(origins), active, value);
     return change;
   }
 
@@ -547,6 +607,7 @@ protected:
   mutable typename GridT::Ptr m_vdb_grid;
   mutable std::shared_ptr<std::shared_mutex> m_map_mutex;
   bool m_config_set = false;
+  bool m_tracking   = false;  // change sets requested (updateMap)
   vdbg_scan_stats m_last_stats{};
 };
 

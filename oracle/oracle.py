@@ -36,6 +36,8 @@ def load():
         "vo_leaf_count": (I64, [P]),
         "vo_active_count": (I64, [P]),
         "vo_export": (None, [P, P, P, P]),
+        "vo_change_count": (I64, [P]),
+        "vo_export_changes": (None, [P, P, P, P]),
         "vo_get_value": (C.c_float, [P, C.c_int32, C.c_int32, C.c_int32]),
         "vo_is_value_on": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32]),
         "vo_log_odds": (None, [P, C.POINTER(C.c_float)]),
@@ -124,6 +126,15 @@ class OracleMap:
         masks = np.zeros((n, 8), np.uint64)
         self._l.vo_export(self._h, origins.ctypes.data, values.ctypes.data, masks.ctypes.data)
         return origins, values, masks
+
+    def exportChanges(self):
+        """Change grid of the last integration: (origins (L,3), active (L,8), value (L,8))."""
+        n = self._l.vo_change_count(self._h)
+        origins = np.zeros((n, 3), np.int32)
+        active = np.zeros((n, 8), np.uint64)
+        value = np.zeros((n, 8), np.uint64)
+        self._l.vo_export_changes(self._h, origins.ctypes.data, active.ctypes.data, value.ctypes.data)
+        return origins, active, value
 
     def getValue(self, xyz) -> float:
         return self._l.vo_get_value(self._h, *[int(c) for c in xyz])

@@ -3,6 +3,8 @@
 // by bench.py's CPU-baseline legs, never by the product library.
 #include "vdb_oracle.hpp"
 
+#include <algorithm>
+
 #include <chrono>
 #include <thread>
 
@@ -93,6 +95,28 @@ int64_t vo_leaf_count(void* h)
 int64_t vo_active_count(void* h)
 {
   return static_cast<int64_t>(static_cast<Handle*>(h)->map.map().active_voxel_count());
+}
+
+// Change grid of the last integration: leaf count, then leaves sorted by
+// origin with their active (flipped) and value (flipped on by a hit) masks.
+int64_t vo_change_count(void* h)
+{
+  return static_cast<int64_t>(static_cast<Handle*>(h)->map.last_change().leaves().size());
+}
+
+void vo_export_changes(void* h, int32_t* origins, uint64_t* active, uint64_t* value)
+{
+  std::vector<const UpdateLeaf*> ls;
+  for (const auto& l : static_cast<Handle*>(h)->map.last_change().leaves()) ls.push_back(&l);
+  std::sort(ls.begin(), ls.end(), [](const UpdateLeaf* a, const UpdateLeaf* b) { return a->origin < b->origin; });
+  for (size_t i = 0; i < ls.size(); ++i)
+  {
+    origins[3 * i + 0] = ls[i]->origin.x;
+    origins[3 * i + 1] = ls[i]->origin.y;
+    origins[3 * i + 2] = ls[i]->origin.z;
+    std::memcpy(active + 8 * i, ls[i]->active, 8 * sizeof(uint64_t));
+    std::memcpy(value + 8 * i, ls[i]->value, 8 * sizeof(uint64_t));
+  }
 }
 
 // Leaves sorted by origin: origins[L][3], values[L][512], masks[L][8].

@@ -639,15 +639,25 @@ public:
     return kOk;
   }
 
-  // VDBMapping.hpp:375-387: every source, in source-id order.
+  // VDBMapping.hpp:375-387: every source, in source-id order. The change grid
+  // of updateMap (VDBMapping.hpp:733-781), which the reference's
+  // integrateUpdate drops, is kept for the last non-empty update grid of the
+  // call (empty when the call integrated nothing).
   void integrate_update(ScanStats* st = nullptr)
   {
+    m_last_change.clear();
     for (auto& kv : m_sources)
     {
-      update_map(kv.second.grid, nullptr, st);
+      if (!kv.second.grid.empty())
+      {
+        m_last_change.clear();
+        update_map(kv.second.grid, &m_last_change, st);
+      }
       kv.second.grid.clear();
     }
   }
+
+  const UpdateGrid& last_change() const { return m_last_change; }
 
   // VDBMapping.hpp:399-406: always reports success; an unknown source or a
   // missing config only skips the accumulation.
@@ -690,6 +700,7 @@ private:
   float m_lo_max       = 0.0f;
   float m_lo_min       = 0.0f;
   FloatMap m_map;
+  UpdateGrid m_last_change;
   std::map<std::string, Source> m_sources;
   std::vector<Coord> m_artificial;
 };

@@ -123,6 +123,35 @@ TEST(DropIn, AccumulateThenIntegrate)
   EXPECT_TRUE(map.getGrid()->getAccessor().isValueOn(openvdb::Coord(3, 0, 0)));
 }
 
+TEST(DropIn, UpdateMapReturnsTheChangeGrid)
+{
+  // VDBMapping.hpp:768-779: a hit that turns a voxel on is set on in the
+  // change grid; misses on voxels that were never on change nothing.
+  OccupancyVDBMapping map(1.0);
+  map.setConfig(test_config(10));
+  Eigen::Matrix<double, 3, 1> origin(0, 0, 0);
+  auto grid = OccupancyVDBMapping::UpdateGridT::create(false);
+  auto gacc = grid->getAccessor();
+  EXPECT_TRUE(map.raycastPointCloud(cloud_of({{5.f, 0.f, 0.f}}), origin, 10.0, gacc));
+  auto change = map.updateMap(grid);
+  auto cacc   = change->getAccessor();
+  EXPECT_TRUE(cacc.isValueOn(openvdb::Coord(5, 0, 0)));
+  EXPECT_TRUE(cacc.getValue(openvdb::Coord(5, 0, 0)));
+  EXPECT_FALSE(cacc.isValueOn(openvdb::Coord(2, 0, 0)));
+  EXPECT_EQ(change->activeVoxelCount(), static_cast<uint64_t>(1));
+  // two misses on (5,0,0) turn it off: active in the change grid, value false
+  auto grid2 = OccupancyVDBMapping::UpdateGridT::create(false);
+  auto g2acc = grid2->getAccessor();
+  map.raycastPointCloud(cloud_of({{8.f, 0.f, 0.f}}), origin, 10.0, g2acc);
+  map.updateMap(grid2);
+  auto grid3 = OccupancyVDBMapping::UpdateGridT::create(false);
+  auto g3acc = grid3->getAccessor();
+  map.raycastPointCloud(cloud_of({{8.f, 0.f, 0.f}}), origin, 10.0, g3acc);
+  auto change3 = map.updateMap(grid3);
+  EXPECT_TRUE(change3->getAccessor().isValueOn(openvdb::Coord(5, 0, 0)));
+  EXPECT_FALSE(change3->getAccessor().getValue(openvdb::Coord(5, 0, 0)));
+}
+
 int main(int argc, char** argv)
 {
   ::testing::InitGoogleTest(&argc, argv);

@@ -183,6 +183,8 @@ SIGNATURES = [
     ("vdbg_get_timings", C.c_int, [_P, C.POINTER(vdbg_timings)]),
     ("vdbg_insert_point_cloud_noalloc", C.c_int,
      [_P, _P, C.c_int64, C.c_int64, _D3, C.c_char_p, C.c_uint32, _P, C.POINTER(vdbg_scan_stats)]),
+    ("vdbg_track_changes", C.c_int, [_P, C.c_int]),
+    ("vdbg_export_changes", C.c_int, [_P, C.c_int, C.c_int64, _P, _P, _P, C.POINTER(C.c_int64)]),
     ("vdbg_set_tuning", C.c_int, [_P, C.POINTER(vdbg_tuning)]),
     ("vdbg_get_tuning", C.c_int, [_P, C.POINTER(vdbg_tuning)]),
     ("vdbg_create_batch", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(vdbg_options), C.POINTER(_P)]),

@@ -208,6 +208,19 @@ struct ChannelView
   uint32_t cur_epoch;
 };
 
+// Change set of an integration (updateMap's change grid, VDBMapping.hpp:733-781):
+// per leaf slot 16 words (0-7: voxels whose active state flipped, 8-15: those
+// flipped on), written for every leaf the sweep touches, and the list of
+// leaves with a flip. `words` null: not tracked.
+struct ChangeView
+{
+  unsigned long long* words;  // [P][16]
+  int* list;                  // [P]
+  uint32_t* count;            // device scalar
+  uint32_t* epoch;            // [P] integration that last listed the leaf
+  uint32_t cur;               // this integration (never 0)
+};
+
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p)
 {
   unsigned long long v;

@@ -823,12 +823,13 @@ __global__ void __launch_bounds__(256) k_mark_hits(const int4* __restrict__ rays
 // hold update bits (all loads issued before any use), applies the log-odds
 // rules, stores them back and clears its update words.
 // kPerMap: the pool holds a batch of maps, each leaf takes its map's log-odds
-// constants (else the one map's, kept in registers).
-template <bool kPerMap>
+// constants (else the one map's, kept in registers). kChanges: record the
+// change set (every touched word, and the leaves with a flip).
+template <bool kPerMap, bool kChanges>
 __global__ void __launch_bounds__(256, 4) k_sweep(ChannelView c, float* __restrict__ values,
                                                   unsigned long long* __restrict__ active,
                                                   uint32_t* __restrict__ flags, const int4* __restrict__ origin,
-                                                  LogOddsTable lt, DevStatus* st)
+                                                  LogOddsTable lt, ChangeView ch, DevStatus* st)
 {
   if (ld_relaxed_u32(&st->error) != 0u) return;
   const uint32_t nt   = *c.n_touched;
@@ -850,7 +851,15 @@ __global__ void __launch_bounds__(256, 4) k_sweep(ChannelView c, float* __restri
     const int mp                   = kPerMap ? origin[slot].w : 0;  // loaded beside the masks
     const unsigned long long hitw  = u[8 + w];
     const unsigned long long actw  = u[w] | hitw;
-    if (actw == 0ull) continue;
+    if (actw == 0ull)
+    {
+      if (kChanges)
+      {
+        ch.words[static_cast<size_t>(slot) * 16 + w]     = 0ull;
+        ch.words[static_cast<size_t>(slot) * 16 + 8 + w] = 0ull;
+      }
+      continue;
+    }
     const LogOdds lo               = kPerMap ? lt.table[mp] : lt.lo0;
     unsigned long long* aw         = active + static_cast<size_t>(slot) * 8 + w;
     const unsigned long long on_in = *aw;
@@ -892,10 +901,35 @@ __global__ void __launch_bounds__(256, 4) k_sweep(ChannelView c, float* __restri
     u[w] = 0ull;
     if (hitw) u[8 + w] = 0ull;
     n_upd += static_cast<unsigned long long>(__popcll(actw));
+    if (kChanges)
+    {
+      // A hit only turns voxels on and a miss only off, so the flipped bits
+      // that are now on are the hits of VDBMapping.hpp:768-772.
+      const unsigned long long flip                   = on ^ on_in;
+      ch.words[static_cast<size_t>(slot) * 16 + w]     = flip;
+      ch.words[static_cast<size_t>(slot) * 16 + 8 + w] = flip & on;
+      if (flip && atomicExch(ch.epoch + slot, ch.cur) != ch.cur) ch.list[atomicAdd(ch.count, 1u)] = slot;
+    }
   }
   for (int off = 16; off > 0; off >>= 1) n_upd += __shfl_xor_sync(0xffffffffu, n_upd, off);
   if (lane == 0 && n_upd) atomicAdd(&st->updates, n_upd);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&st->touched, nt);
+}
+
+// Gathers the listed change leaves of map `map` (-1: all): origin and the 16
+// change words per leaf, one thread per word; out_n counts what was kept.
+__global__ void k_gather_changes(ChangeView ch, const int4* __restrict__ origin, int map, int4* __restrict__ out_o,
+                                 unsigned long long* __restrict__ out_w, uint32_t* __restrict__ out_n)
+{
+  const uint32_t n = *ch.count;
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int slot = ch.list[k];
+  const int4 o   = origin[slot];
+  if (map >= 0 && o.w != map) return;
+  const uint32_t j = atomicAdd(out_n, 1u);
+  out_o[j]         = o;
+  for (int w = 0; w < 16; ++w) out_w[static_cast<size_t>(j) * 16 + w] = ch.words[static_cast<size_t>(slot) * 16 + w];
 }
 
 // Turns the touched-block list of a window into the flat list of touched

@@ -121,6 +121,14 @@ struct vdbg_map
   vdbg_tuning tuning{16, 2048, {2048, 1024, 512}, 0.5f, 16};
   uint32_t apply_grid_chunk = 0;   // apply_chunk the cached grid size is for
   unsigned apply_grid_blocks = 0;
+  // Change set of the last integration (vdbg_track_changes).
+  bool track_changes               = false;
+  uint32_t chg_cap                 = 0;  // leaf slots the arrays cover
+  unsigned long long* chg_words    = nullptr;
+  int* chg_list                    = nullptr;
+  uint32_t* chg_epoch              = nullptr;
+  uint32_t* chg_count              = nullptr;
+  uint32_t chg_cur                 = 0;
 };
 
 namespace {
@@ -750,18 +758,73 @@ int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, 
 
 // Integration of one update grid: compact its touched blocks into the list
 // of touched leaves, then sweep them.
+void free_changes(vdbg_map* m)
+{
+  dev_free(m, m->chg_words, static_cast<size_t>(m->chg_cap) * 16);
+  dev_free(m, m->chg_list, m->chg_cap);
+  dev_free(m, m->chg_epoch, m->chg_cap);
+  dev_free(m, m->chg_count, 1);
+  m->chg_cap = 0;
+}
+
+// Change-set arrays for the current leaf capacity (their contents only live
+// for one integration, so a resize starts them empty).
+int ensure_changes(vdbg_map* m, cudaStream_t s)
+{
+  if (m->chg_cap == m->capacity && m->chg_words) return VDBG_OK;
+  free_changes(m);
+  const uint32_t cap = m->capacity;
+  VDBG_TRY(dev_alloc(m, &m->chg_words, static_cast<size_t>(cap) * 16));
+  VDBG_TRY(dev_alloc(m, &m->chg_list, cap));
+  VDBG_TRY(dev_alloc(m, &m->chg_epoch, cap));
+  VDBG_TRY(dev_alloc(m, &m->chg_count, 1));
+  VDBG_CUDA(cudaMemsetAsync(m->chg_epoch, 0, static_cast<size_t>(cap) * sizeof(uint32_t), s));
+  VDBG_CUDA(cudaMemsetAsync(m->chg_count, 0, sizeof(uint32_t), s));
+  m->chg_cap = cap;
+  return VDBG_OK;
+}
+
+// Empties the change set (the start of an integrating call, and each sweep:
+// the set keeps the last update grid integrated).
+int reset_changes(vdbg_map* m, cudaStream_t s)
+{
+  if (!m->track_changes) return VDBG_OK;
+  VDBG_TRY(ensure_changes(m, s));
+  VDBG_CUDA(cudaMemsetAsync(m->chg_count, 0, sizeof(uint32_t), s));
+  return VDBG_OK;
+}
+
 int launch_sweep(vdbg_map* m, Channel& c, cudaStream_t s)
 {
   k_compact<<<kSweepBlocks, kSweepThreads, 0, s>>>(map_view(m), channel_view(c), m->d_status, 0);
   LogOddsTable lt;
   lt.lo0   = m->conf[0].lo;
   lt.table = m->batch ? m->d_lo : nullptr;
-  if (m->batch)
-    k_sweep<true><<<kSweepBlocks, kSweepThreads, 0, s>>>(channel_view(c), m->values, m->active, m->flags,
-                                                         m->origin, lt, m->d_status);
+  ChangeView ch{};
+  if (m->track_changes)
+  {
+    VDBG_TRY(reset_changes(m, s));
+    m->chg_cur += 1;
+    if (m->chg_cur == 0) m->chg_cur = 1;  // (epochs of 0 mean never listed)
+    ch.words = m->chg_words;
+    ch.list  = m->chg_list;
+    ch.count = m->chg_count;
+    ch.epoch = m->chg_epoch;
+    ch.cur   = m->chg_cur;
+  }
+  const ChannelView cv = channel_view(c);
+  if (m->batch && m->track_changes)
+    k_sweep<true, true><<<kSweepBlocks, kSweepThreads, 0, s>>>(cv, m->values, m->active, m->flags, m->origin, lt, ch,
+                                                               m->d_status);
+  else if (m->batch)
+    k_sweep<true, false><<<kSweepBlocks, kSweepThreads, 0, s>>>(cv, m->values, m->active, m->flags, m->origin, lt,
+                                                                ch, m->d_status);
+  else if (m->track_changes)
+    k_sweep<false, true><<<kSweepBlocks, kSweepThreads, 0, s>>>(cv, m->values, m->active, m->flags, m->origin, lt,
+                                                                ch, m->d_status);
   else
-    k_sweep<false><<<kSweepBlocks, kSweepThreads, 0, s>>>(channel_view(c), m->values, m->active, m->flags,
-                                                          m->origin, lt, m->d_status);
+    k_sweep<false, false><<<kSweepBlocks, kSweepThreads, 0, s>>>(cv, m->values, m->active, m->flags, m->origin, lt,
+                                                                 ch, m->d_status);
   VDBG_CUDA(cudaGetLastError());
   m->timings.launches += 2;
   return VDBG_OK;
@@ -979,6 +1042,7 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
   {
     todo.push_back(only);
   }
+  if (integrate_all || only) VDBG_TRY(reset_changes(m, s));
   for (Channel* c : todo) VDBG_TRY(launch_sweep(m, *c, s));
   VDBG_TRY(fetch_status(m, s));
   if (m->h_status->error != 0u) return map_error(m->h_status->error);
@@ -1273,6 +1337,7 @@ int vdbg_destroy(vdbg_map* m)
   dev_free(m, m->borigin, m->bcapacity);
   dev_free(m, m->bkeys, m->bhash_size);
   dev_free(m, m->bslots, m->bhash_size);
+  free_changes(m);
   dev_free(m, m->d_status, 1);
   dev_free(m, m->d_hist, m->buckets);
   dev_free(m, m->d_cursor, m->buckets);
@@ -1437,6 +1502,7 @@ int vdbg_reset_map(vdbg_map* m)
     c.cur_epoch = 1;
     c.pending   = false;
   }
+  if (m->chg_count) VDBG_CUDA(cudaMemsetAsync(m->chg_count, 0, sizeof(uint32_t), s));
   VDBG_CUDA(cudaStreamSynchronize(s));
   m->n_leaves = 0;
   m->n_blocks = 0;
@@ -1515,6 +1581,100 @@ int vdbg_get_tuning(const vdbg_map* m, vdbg_tuning* out)
 {
   if (!m || !out) return VDBG_ERR_INVALID_ARGUMENT;
   *out = m->tuning;
+  return VDBG_OK;
+}
+
+int vdbg_track_changes(vdbg_map* m, int enable)
+{
+  if (!m) return VDBG_ERR_INVALID_ARGUMENT;
+  VDBG_TRY(set_device(m));
+  VDBG_CUDA(cudaStreamSynchronize(m->stream));
+  m->track_changes = enable != 0;
+  if (m->track_changes)
+  {
+    VDBG_TRY(ensure_changes(m, m->stream));
+    VDBG_CUDA(cudaMemsetAsync(m->chg_count, 0, sizeof(uint32_t), m->stream));
+    VDBG_CUDA(cudaStreamSynchronize(m->stream));
+  }
+  else
+  {
+    free_changes(m);
+  }
+  return VDBG_OK;
+}
+
+int vdbg_export_changes(vdbg_map* m, int map, int64_t capacity, int32_t* origins, uint64_t* active, uint64_t* value,
+                        int64_t* n_out)
+{
+  if (!m || !n_out || capacity < 0 || map < -1 || map >= static_cast<int>(m->conf.size()))
+    return VDBG_ERR_INVALID_ARGUMENT;
+  *n_out = 0;
+  if (!m->track_changes || !m->chg_count) return VDBG_ERR_INVALID_ARGUMENT;
+  VDBG_TRY(set_device(m));
+  cudaStream_t s = m->stream;
+  uint32_t n     = 0;
+  VDBG_CUDA(cudaMemcpyAsync(&n, m->chg_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  VDBG_CUDA(cudaStreamSynchronize(s));
+  std::vector<int4> o;
+  std::vector<unsigned long long> w;
+  uint32_t kept = 0;
+  if (n > 0)
+  {
+    int4* d_o                = nullptr;
+    unsigned long long* d_w  = nullptr;
+    uint32_t* d_n            = nullptr;
+    int st                   = dev_alloc(m, &d_o, n);
+    if (st == VDBG_OK) st = dev_alloc(m, &d_w, static_cast<size_t>(n) * 16);
+    if (st == VDBG_OK) st = dev_alloc(m, &d_n, 1);
+    if (st == VDBG_OK && cudaMemsetAsync(d_n, 0, sizeof(uint32_t), s) != cudaSuccess) st = VDBG_ERR_CUDA;
+    if (st == VDBG_OK)
+    {
+      ChangeView ch{};
+      ch.words = m->chg_words;
+      ch.list  = m->chg_list;
+      ch.count = m->chg_count;
+      k_gather_changes<<<(n + 255) / 256, 256, 0, s>>>(ch, m->origin, map, d_o, d_w, d_n);
+      if (cudaGetLastError() != cudaSuccess ||
+          cudaMemcpyAsync(&kept, d_n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaStreamSynchronize(s) != cudaSuccess)
+        st = VDBG_ERR_CUDA;
+    }
+    if (st == VDBG_OK && kept > 0)
+    {
+      o.resize(kept);
+      w.resize(static_cast<size_t>(kept) * 16);
+      if (cudaMemcpy(o.data(), d_o, kept * sizeof(int4), cudaMemcpyDeviceToHost) != cudaSuccess ||
+          cudaMemcpy(w.data(), d_w, static_cast<size_t>(kept) * 16 * sizeof(unsigned long long),
+                     cudaMemcpyDeviceToHost) != cudaSuccess)
+        st = VDBG_ERR_CUDA;
+    }
+    dev_free(m, d_o, n);
+    dev_free(m, d_w, static_cast<size_t>(n) * 16);
+    dev_free(m, d_n, 1);
+    if (st != VDBG_OK) return st;
+  }
+  std::vector<uint32_t> idx(kept);
+  std::iota(idx.begin(), idx.end(), 0u);
+  std::sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) {
+    if (o[a].x != o[b].x) return o[a].x < o[b].x;
+    if (o[a].y != o[b].y) return o[a].y < o[b].y;
+    return o[a].z < o[b].z;
+  });
+  *n_out = kept;
+  if (static_cast<int64_t>(kept) > capacity) return VDBG_ERR_BUFFER_TOO_SMALL;
+  for (uint32_t k = 0; k < kept; ++k)
+  {
+    const uint32_t i = idx[k];
+    if (origins)
+    {
+      origins[3 * k + 0] = o[i].x;
+      origins[3 * k + 1] = o[i].y;
+      origins[3 * k + 2] = o[i].z;
+    }
+    if (active) std::memcpy(active + 8 * static_cast<size_t>(k), &w[16 * static_cast<size_t>(i)], 8 * sizeof(uint64_t));
+    if (value)
+      std::memcpy(value + 8 * static_cast<size_t>(k), &w[16 * static_cast<size_t>(i) + 8], 8 * sizeof(uint64_t));
+  }
   return VDBG_OK;
 }
 
@@ -1720,6 +1880,8 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
   std::vector<Channel*> todo;
   for (Channel& c : m->channels)
     if (c.pending) todo.push_back(&c);
+  if (m->track_changes && !m->chg_words) return VDBG_ERR_SIZE_LIMIT;  // would allocate
+  if (m->track_changes) VDBG_CUDA(cudaMemsetAsync(m->chg_count, 0, sizeof(uint32_t), s));
   for (Channel* c : todo) VDBG_TRY(launch_sweep(m, *c, s));
   VDBG_TRY(fetch_status(m, s));
   if (m->h_status->error != 0u) return map_error(m->h_status->error);

@@ -63,6 +63,25 @@ def _origin(origin):
     return o
 
 
+def _export_changes(lib, h, map_index, check):
+    """(origins (L,3) int32, active (L,8) uint64, value (L,8) uint64) of the
+    last integration's change set."""
+    n = C.c_int64()
+    cap = 1024
+    while True:
+        origins = np.zeros((cap, 3), np.int32)
+        active = np.zeros((cap, 8), np.uint64)
+        value = np.zeros((cap, 8), np.uint64)
+        s = lib.vdbg_export_changes(h, int(map_index), cap, origins.ctypes.data, active.ctypes.data,
+                                    value.ctypes.data, C.byref(n))
+        if s == _lib.STATUS_CODE["VDBG_ERR_BUFFER_TOO_SMALL"]:
+            cap = n.value
+            continue
+        check(s, "vdbg_export_changes")
+        k = n.value
+        return origins[:k], active[:k], value[:k]
+
+
 class Grid:
     """Export of the map (VDBMapping::getGrid, VDBMapping.hpp:799).
 
@@ -309,6 +328,16 @@ class OccupancyVDBMapping:
         self._check(self._lib.vdbg_get_tuning(self._h, C.byref(t)), "vdbg_get_tuning")
         return t.as_dict()
 
+    def trackChanges(self, enable: bool = True) -> None:
+        """Keep the change set of each integration (updateMap's change grid,
+        VDBMapping.hpp:731-792)."""
+        self._check(self._lib.vdbg_track_changes(self._h, 1 if enable else 0), "vdbg_track_changes")
+
+    def exportChanges(self):
+        """Change set of the last integration: (origins, active, value) per leaf
+        with a flip, sorted by origin; `value` marks voxels flipped on by a hit."""
+        return _export_changes(self._lib, self._h, -1, self._check)
+
     def _export(self):
         n = C.c_int64()
         cap = self.leafCount()
@@ -461,6 +490,13 @@ class MapBatch:
         t = _lib.vdbg_tuning()
         self._check(self._lib.vdbg_get_tuning(self._h, C.byref(t)), "vdbg_get_tuning")
         return t.as_dict()
+
+    def trackChanges(self, enable: bool = True) -> None:
+        self._check(self._lib.vdbg_track_changes(self._h, 1 if enable else 0), "vdbg_track_changes")
+
+    def exportChanges(self, map_index: int):
+        """Change set of the last batched insert for one map."""
+        return _export_changes(self._lib, self._h, map_index, self._check)
 
     def exportLeaves(self, map_index: int):
         """(origins, values, masks) of one map, sorted by leaf origin."""
