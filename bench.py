@@ -130,6 +130,19 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def max_over_ranks(seconds, dist):
+    """The slowest rank's time (the job's time), on any backend (NCCL on GPU
+    tensors, gloo on CPU tensors); `dist` None for one rank."""
+    if dist is None:
+        return seconds
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -291,10 +304,7 @@ def run_ours(args):
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_s = sum(step_ms) / 1000.0
-    if dist:
-        t = torch.tensor([total_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
+    total_s = max_over_ranks(total_s, dist)
     rays = args.steps * n_pts * world
     updates = sum(s["updates"] for s in stats) * world
     value = rays / total_s
@@ -377,10 +387,7 @@ def run_ours(args):
             m2.insertPointCloud(host_pts[k].numpy(), scans[k][1], "lidar")
             e2e_t.append(time.perf_counter() - t0)
         e2e_s = sum(e2e_t)
-        if dist:
-            t = torch.tensor([e2e_s], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s, dist)
         line["e2e"] = {"value": rays / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n_pts * PCL_POINT_BYTES,
                        "d2h_bytes_per_step": STATUS_BYTES,
                        "latency_ms": {"p50": 1000 * float(np.percentile(e2e_t, 50)),
