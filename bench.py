@@ -63,6 +63,8 @@ def parse_args():
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="simulated traffic for --workload serving")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="device-memory admission budget")
     ap.add_argument("--no-autotune", action="store_true", help="batched mode: keep the library's default tuning")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="batched and serving modes: separate launches instead of the captured step")
     ap.add_argument("--batch-steps", type=int, default=4,
                     help="distinct steps generated for --workload batched (cycled)")
     ap.add_argument("--leaf-capacity", type=int, default=0,
@@ -442,6 +444,7 @@ def run_batched(args):
     b = MapBatch(wl.resolutions, initial_leaf_capacity=1 << 22, device=local)
     if tuned:
         b.setTuning(tuned)
+    b.useGraph(not args.no_graph)
     for i, c in enumerate(wl.configs):
         b.setConfig(i, c)
     plain = []
@@ -515,6 +518,8 @@ def run_batched(args):
         "tuning": tuned or "library defaults",
         "gpu_launches_per_step": {"batched": b.timings()["launches"],
                                   "plain": sum(g.timings()["launches"] for g in plain)},
+        "cuda_graph": {**b.graphStats(), "enabled": not args.no_graph,
+                       "steps": args.warmup + args.steps},
     }
     if clk:
         line["clocks"] = clk
@@ -544,6 +549,7 @@ def run_serving(args):
     K = wl.distinct_scans
     scans = {(i, k): wl.scan(i, k) for i in range(len(wl.streams)) for k in range(K)}
     batch = MapBatch(wl.resolutions, initial_leaf_capacity=1 << 23, device=local)
+    batch.useGraph(not args.no_graph)
     for i, c in enumerate(wl.configs):
         batch.setConfig(i, c)
     # Warm the scratch and run buffers with one scan per map (not timed).
@@ -606,6 +612,7 @@ def run_serving(args):
         "rejected": st["rejected"], "max_queued": st["max_queued"], "submit_retries_busy": busy,
         "device_bytes": st["device_bytes"],
         "statuses": sorted({r["status"] for r in results}),
+        "cuda_graph": {**batch.graphStats(), "enabled": not args.no_graph},
     }
     if clk:
         line["clocks"] = clk

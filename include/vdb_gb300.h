@@ -245,6 +245,19 @@ int vdbg_batch_set_config(vdbg_map* batch, int map, const vdbg_config* config);
 int vdbg_batch_insert(vdbg_map* batch, const float* xyz, const int64_t* counts, int64_t stride_bytes,
                       const double* origins, uint32_t flags, void* stream, vdbg_scan_stats* stats);
 
+/* CUDA-graph replay of vdbg_batch_insert (batches of two or more maps; on by
+ * default). The step is captured once per buffer layout and replayed as one
+ * graph launch: prep, endpoint hits, the first DDA pass with its apply,
+ * compact, sweep. It is captured again after a pool, scratch or run-buffer
+ * reallocation, a tuning change or a new device input pointer. When a step
+ * needs a second DDA pass or a pool to grow, the graph's compact and sweep
+ * skip themselves on the device and the call finishes the step with separate
+ * launches. Off, or with change tracking on, every step uses separate
+ * launches; the results are the same either way. vdbg_graph_stats reports
+ * the captures and replays so far. */
+int vdbg_batch_use_graph(vdbg_map* batch, int enable);
+int vdbg_graph_stats(const vdbg_map* batch, uint64_t* captures, uint64_t* replays);
+
 /* Leaf count and export (as vdbg_leaf_count / vdbg_export_leaves) of one map. */
 int vdbg_batch_leaf_count(vdbg_map* batch, int map, int64_t* out);
 int vdbg_batch_export_leaves(vdbg_map* batch, int map, int64_t capacity, int32_t* origins, float* values,

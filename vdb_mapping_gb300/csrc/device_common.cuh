@@ -81,7 +81,7 @@ struct DevStatus
   uint32_t ray_cursor;  // next position in the ray order handed to a DDA warp
   uint32_t n_blocks;    // block bump allocator
   uint32_t inflight;    // lanes that ended a DDA pass with a ray in flight
-  uint32_t pad32;
+  uint32_t windows;     // update-grid windows closed by k_finish_window
   unsigned long long runs;  // slab runs written by the traversal (all passes)
 };
 
@@ -204,8 +204,9 @@ struct ChannelView
   int* blist;
   uint32_t* n_blist;
   int* touched;
-  uint32_t* n_touched;
-  uint32_t cur_epoch;
+  uint32_t* n_touched;      // [0] leaves on the touched list, [2] the window's epoch
+  const uint32_t* epoch;    // n_touched + 2
+  uint32_t cur_epoch;       // *epoch, loaded by each kernel at its start
 };
 
 // Change set of an integration (updateMap's change grid, VDBMapping.hpp:733-781):
@@ -347,6 +348,14 @@ __device__ __forceinline__ unsigned long long pack_leaf_key(int map, int lx, int
 
 // Appends block `b` to the channel's touched-block list the first time it is
 // seen in the current integration window.
+// True when this call's marking is complete and free of errors (every ray
+// cast, none left in flight), so its update grids may be integrated.
+__device__ __forceinline__ bool marking_complete(const DevStatus* st)
+{
+  return ld_relaxed_u32(&st->error) == 0u && ld_relaxed_u32(&st->inflight) == 0u &&
+         ld_relaxed_u32(&st->ray_cursor) >= ld_relaxed_u32(&st->n_valid);
+}
+
 __device__ __forceinline__ void touch_block(const ChannelView& c, int b)
 {
   uint32_t* e = c.bepoch + b;

@@ -66,6 +66,13 @@ __device__ __forceinline__ int ray_bucket(int dx, int dy, int dz, uint32_t l1, i
 }
 static_assert(6 * 169 == kDirCells, "direction cells");
 
+// Points of the call: a table of several scans holds its total in
+// first[n] (so a captured step may launch for the scratch capacity `n`).
+__device__ __forceinline__ int64_t points_of(const ScanTable& t, int64_t n)
+{
+  return t.n > 1 ? min(n, static_cast<int64_t>(__ldg(t.first + t.n))) : n;
+}
+
 // One thread per point. rays[i] = (end voxel xyz, meta). Every lane of a
 // warp stays to the end so the warp-wide reductions see a full mask.
 __global__ void __launch_bounds__(256) k_prep(const char* __restrict__ pts, int64_t n, int64_t stride,
@@ -74,7 +81,7 @@ __global__ void __launch_bounds__(256) k_prep(const char* __restrict__ pts, int6
                                               DevStatus* st)
 {
   const int64_t i     = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const bool in_range = i < n;
+  const bool in_range = i < points_of(t, n);
   uint32_t meta       = 0;
   int ex = 0, ey = 0, ez = 0;
   unsigned long long visits = 0, hit = 0, valid = 0, nonfinite = 0;
@@ -225,7 +232,7 @@ __global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, 
                                                  uint32_t* __restrict__ cursor, int* __restrict__ order)
 {
   const int64_t i      = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const int4 r         = i < n ? rays[i] : make_int4(0, 0, 0, 0);
+  const int4 r         = i < points_of(t, n) ? rays[i] : make_int4(0, 0, 0, 0);
   const uint32_t meta  = static_cast<uint32_t>(r.w);
   const bool valid     = (meta & kMetaValid) != 0;
   const int sc         = valid ? scan_of_ray(t, static_cast<uint32_t>(i)) : 0;
@@ -646,6 +653,7 @@ __device__ __forceinline__ void apply_stage(const RunBuffer& rb, uint32_t cps, u
 
 __global__ void __launch_bounds__(kApplyThreads, 3) k_apply_runs(RunBuffer rb, MapView m, ChannelView c)
 {
+  c.cur_epoch = *c.epoch;
   __shared__ ApplySmem t;
   extern __shared__ __align__(16) unsigned char stage[];
   unsigned long long* s_key  = reinterpret_cast<unsigned long long*>(stage);
@@ -795,6 +803,7 @@ __global__ void __launch_bounds__(256) k_mark_hits(const int4* __restrict__ rays
                                                    ScanTable t, MapView m, ChannelView c)
 {
   if (ld_relaxed_u32(&m.st->error) != 0u) return;
+  c.cur_epoch = *c.epoch;
   const uint32_t nv = m.st->n_valid;
   const uint32_t j  = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nv) return;
@@ -829,9 +838,9 @@ template <bool kPerMap, bool kChanges>
 __global__ void __launch_bounds__(256, 4) k_sweep(ChannelView c, float* __restrict__ values,
                                                   unsigned long long* __restrict__ active,
                                                   uint32_t* __restrict__ flags, const int4* __restrict__ origin,
-                                                  LogOddsTable lt, ChangeView ch, DevStatus* st)
+                                                  LogOddsTable lt, ChangeView ch, DevStatus* st, int gated)
 {
-  if (ld_relaxed_u32(&st->error) != 0u) return;
+  if (gated ? !marking_complete(st) : ld_relaxed_u32(&st->error) != 0u) return;
   const uint32_t nt   = *c.n_touched;
   const int lane      = static_cast<int>(threadIdx.x & 31);
   const int w         = lane & 7;
@@ -936,9 +945,12 @@ __global__ void k_gather_changes(ChangeView ch, const int4* __restrict__ origin,
 // leaves the sweep walks, clearing the blocks' touched bits. One warp per
 // block, one lane per 64-cell word. `force` runs it while an error is set
 // (to undo a partial marking).
-__global__ void __launch_bounds__(256) k_compact(MapView m, ChannelView c, DevStatus* st, int force)
+// `mode`: 0 skips on an error, 1 (a dropped marking) always runs, 2 (a
+// captured step) skips unless the marking is complete.
+__global__ void __launch_bounds__(256) k_compact(MapView m, ChannelView c, DevStatus* st, int mode)
 {
-  if (!force && ld_relaxed_u32(&st->error) != 0u) return;
+  if (mode == 0 && ld_relaxed_u32(&st->error) != 0u) return;
+  if (mode == 2 && !marking_complete(st)) return;
   const uint32_t nb   = *c.n_blist;
   const int lane      = static_cast<int>(threadIdx.x & 31);
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -966,6 +978,27 @@ __global__ void __launch_bounds__(256) k_compact(MapView m, ChannelView c, DevSt
       tw[lane] = 0ull;
     }
   }
+}
+
+// Starts a channel's first window: empty lists, epoch 1.
+__global__ void k_window_init(ChannelView c)
+{
+  c.n_touched[0] = 0u;
+  c.n_touched[2] = 1u;
+  *c.n_blist     = 0u;
+}
+
+// After a sweep (or a dropped marking): a fresh window for the channel.
+// `gated` (a captured step) skips it when the marking did not complete, so
+// the window is left to the host's continuation of the step.
+__global__ void k_finish_window(ChannelView c, DevStatus* st, int gated)
+{
+  if (gated && !marking_complete(st)) return;
+  st->windows += 1u;
+  c.n_touched[0]     = 0u;
+  *c.n_blist         = 0u;
+  const uint32_t e   = c.n_touched[2] + 1u;
+  c.n_touched[2]     = e == 0u ? 1u : e;  // 0 marks blocks never touched
 }
 
 // Inserts blocks [0, n) of the block pool into an empty block hash.

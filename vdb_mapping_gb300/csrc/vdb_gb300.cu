@@ -34,7 +34,6 @@ struct Channel
   uint32_t* bepoch                  = nullptr;  // [PB]
   int* blist                        = nullptr;  // [PB]
   uint32_t* n_blist                 = nullptr;  // device scalar
-  uint32_t cur_epoch                = 1;
   bool pending                      = false;    // marked since its last integration
 };
 
@@ -129,6 +128,16 @@ struct vdbg_map
   uint32_t* chg_epoch              = nullptr;
   uint32_t* chg_count              = nullptr;
   uint32_t chg_cur                 = 0;
+  // Captured batched step: prep, endpoint hits, one DDA pass and its apply,
+  // compact, sweep, window end. Replayed while nothing it names has moved.
+  uint64_t layout                  = 0;  // bumped by every device (re)allocation and tuning change
+  bool use_graph                   = true;
+  cudaGraphExec_t graph            = nullptr;
+  uint64_t graph_layout            = 0;
+  const void* graph_pts            = nullptr;
+  int64_t graph_stride             = 0;
+  uint64_t graph_captures          = 0;
+  uint64_t graph_replays           = 0;
 };
 
 namespace {
@@ -173,6 +182,7 @@ int dev_alloc(vdbg_map* m, T** p, size_t count)
   if (m->max_bytes > 0 && m->bytes + static_cast<int64_t>(b) > m->max_bytes) return VDBG_ERR_OUT_OF_MEMORY;
   VDBG_CUDA(cudaMalloc(reinterpret_cast<void**>(p), b));
   m->bytes += static_cast<int64_t>(b);
+  m->layout += 1;
   return VDBG_OK;
 }
 
@@ -183,6 +193,7 @@ void dev_free(vdbg_map* m, T*& p, size_t count)
   {
     cudaFree(p);
     m->bytes -= static_cast<int64_t>(count * sizeof(T));
+    m->layout += 1;
   }
   p = nullptr;
 }
@@ -219,7 +230,8 @@ ChannelView channel_view(const Channel& c)
   v.n_blist   = c.n_blist;
   v.touched   = c.touched;
   v.n_touched = c.n_touched;
-  v.cur_epoch = c.cur_epoch;
+  v.epoch     = c.n_touched + 2;
+  v.cur_epoch = 0;  // each kernel loads *epoch
   return v;
 }
 
@@ -674,34 +686,36 @@ void add_apply_time(vdbg_map* m)
   if (cudaEventElapsedTime(&ms, m->ev_a0, m->ev_a1) == cudaSuccess) m->timings.apply_ms += ms;
 }
 
-// castRayIntoGrid for every ray (VDBMapping.hpp:550-566) and the endpoint
-// hits (VDBMapping.hpp:533-536), into channel `c`: endpoint hits once, then
-// DDA passes, each followed by k_apply_runs, until no ray is left in flight.
-// One status fetch per pass. When the leaf or block pool runs out the pools
-// grow (if `may_grow`) and the hits and the pass's runs are applied again
-// (both idempotent); otherwise the call fails with OUT_OF_MEMORY.
-int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, int64_t n, const ScanTable& t,
-                   const RunBuffer& rb, LaneState* ls, WarpState* ws, bool may_grow, cudaStream_t s)
+// Queues one DDA pass (a fresh one, or `resume` of the rays left in flight)
+// and its k_apply_runs.
+int launch_dda_pass(vdbg_map* m, Channel& c, const int4* rays, const int* order, const ScanTable& t,
+                    const RunBuffer& rb, LaneState* ls, WarpState* ws, bool resume, cudaStream_t s,
+                    unsigned event_flags = cudaEventRecordDefault)
 {
-  const unsigned hit_blocks   = static_cast<unsigned>((n + 255) / 256);
-  const unsigned apply_blocks = apply_grid(m, rb.apply_chunk);
-  const size_t apply_smem     = apply_stage_bytes(rb.apply_chunk);
-  k_mark_hits<<<hit_blocks, 256, 0, s>>>(rays, order, t, map_view(m), channel_view(c));
-  m->timings.launches += 1;
-  uint32_t passes = 0;
+  VDBG_CUDA(cudaMemsetAsync(&m->d_status->inflight, 0, sizeof(uint32_t), s));
+  k_dda_mark<<<rb.warps / kDdaWarps, kDdaWarps * 32, 0, s>>>(rays, order, t, map_view(m), rb, ls, ws,
+                                                            resume ? 1 : 0);
+  VDBG_CUDA(cudaEventRecordWithFlags(m->ev_a0, s, event_flags));
+  k_apply_runs<<<apply_grid(m, rb.apply_chunk), kApplyThreads, apply_stage_bytes(rb.apply_chunk), s>>>(
+    rb, map_view(m), channel_view(c));
+  VDBG_CUDA(cudaEventRecordWithFlags(m->ev_a1, s, event_flags));
+  VDBG_CUDA(cudaGetLastError());
+  m->timings.launches += 2;
+  return VDBG_OK;
+}
+
+// After `passes` DDA passes whose status has been fetched: handles a pool or
+// hash that ran out (grow what ran out, let the failed leaf cells be
+// allocated again, apply the hits and the pass's runs again, both
+// idempotent; OUT_OF_MEMORY when the pools may not grow) and queues resume
+// passes, one status fetch each, until no ray is left in flight.
+int settle_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, int64_t n, const ScanTable& t,
+                      const RunBuffer& rb, LaneState* ls, WarpState* ws, bool may_grow, cudaStream_t s,
+                      uint32_t passes)
+{
+  const unsigned hit_blocks = static_cast<unsigned>((n + 255) / 256);
   for (;;)
   {
-    VDBG_CUDA(cudaMemsetAsync(&m->d_status->inflight, 0, sizeof(uint32_t), s));
-    k_dda_mark<<<rb.warps / kDdaWarps, kDdaWarps * 32, 0, s>>>(rays, order, t, map_view(m), rb, ls, ws,
-                                                              passes > 0 ? 1 : 0);
-    VDBG_CUDA(cudaEventRecord(m->ev_a0, s));
-    k_apply_runs<<<apply_blocks, kApplyThreads, apply_smem, s>>>(rb, map_view(m), channel_view(c));
-    VDBG_CUDA(cudaEventRecord(m->ev_a1, s));
-    VDBG_CUDA(cudaGetLastError());
-    m->timings.launches += 2;
-    ++passes;
-    VDBG_TRY(fetch_status(m, s));
-    add_apply_time(m);
     for (int attempt = 0; m->h_status->error != 0u; ++attempt)
     {
       const uint32_t err = m->h_status->error;
@@ -719,8 +733,6 @@ int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, 
       }
       if (err & (kErrSpin | kErrStepBound)) return map_error(err);
       if (!may_grow || attempt >= 40) return VDBG_ERR_OUT_OF_MEMORY;
-      // A pool or the block hash ran out: grow what ran out, let the failed
-      // leaf cells be allocated again, apply the hits and this pass's runs again.
       if (err & kErrPoolFull) VDBG_TRY(grow_for(m, m->h_status->n_leaves));
       if (err & kErrBlockFull) VDBG_TRY(grow_blocks_for(m, m->h_status->n_blocks));
       if ((err & kErrHashFull) && !(err & kErrBlockFull))
@@ -736,7 +748,8 @@ int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, 
       VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
       k_mark_hits<<<hit_blocks, 256, 0, s>>>(rays, order, t, map_view(m), channel_view(c));
       VDBG_CUDA(cudaEventRecord(m->ev_a0, s));
-      k_apply_runs<<<apply_blocks, kApplyThreads, apply_smem, s>>>(rb, map_view(m), channel_view(c));
+      k_apply_runs<<<apply_grid(m, rb.apply_chunk), kApplyThreads, apply_stage_bytes(rb.apply_chunk), s>>>(
+        rb, map_view(m), channel_view(c));
       VDBG_CUDA(cudaEventRecord(m->ev_a1, s));
       VDBG_CUDA(cudaGetLastError());
       m->timings.launches += 2;
@@ -750,10 +763,30 @@ int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, 
     // Every pass completes at least one round per warp, so this bound is
     // never reached by a working device; it turns a logic error into a status.
     if (passes > (1u << 20)) return VDBG_ERR_TIMEOUT;
+    VDBG_TRY(launch_dda_pass(m, c, rays, order, t, rb, ls, ws, true, s));
+    ++passes;
+    VDBG_TRY(fetch_status(m, s));
+    add_apply_time(m);
   }
   VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
   m->passes_last = passes;
   return VDBG_OK;
+}
+
+// castRayIntoGrid for every ray (VDBMapping.hpp:550-566) and the endpoint
+// hits (VDBMapping.hpp:533-536), into channel `c`: endpoint hits once, then
+// DDA passes, each followed by k_apply_runs, until no ray is left in flight.
+// One status fetch per pass.
+int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, int64_t n, const ScanTable& t,
+                   const RunBuffer& rb, LaneState* ls, WarpState* ws, bool may_grow, cudaStream_t s)
+{
+  k_mark_hits<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(rays, order, t, map_view(m),
+                                                                     channel_view(c));
+  m->timings.launches += 1;
+  VDBG_TRY(launch_dda_pass(m, c, rays, order, t, rb, ls, ws, false, s));
+  VDBG_TRY(fetch_status(m, s));
+  add_apply_time(m);
+  return settle_dda_passes(m, c, rays, order, n, t, rb, ls, ws, may_grow, s, 1);
 }
 
 // Integration of one update grid: compact its touched blocks into the list
@@ -794,9 +827,12 @@ int reset_changes(vdbg_map* m, cudaStream_t s)
   return VDBG_OK;
 }
 
-int launch_sweep(vdbg_map* m, Channel& c, cudaStream_t s)
+// `gated`: a captured step, in which the sweep skips itself on the device
+// unless the marking completed.
+int launch_sweep(vdbg_map* m, Channel& c, cudaStream_t s, bool gated = false)
 {
-  k_compact<<<kSweepBlocks, kSweepThreads, 0, s>>>(map_view(m), channel_view(c), m->d_status, 0);
+  const int g = gated ? 1 : 0;
+  k_compact<<<kSweepBlocks, kSweepThreads, 0, s>>>(map_view(m), channel_view(c), m->d_status, gated ? 2 : 0);
   LogOddsTable lt;
   lt.lo0   = m->conf[0].lo;
   lt.table = m->batch ? m->d_lo : nullptr;
@@ -815,28 +851,26 @@ int launch_sweep(vdbg_map* m, Channel& c, cudaStream_t s)
   const ChannelView cv = channel_view(c);
   if (m->batch && m->track_changes)
     k_sweep<true, true><<<kSweepBlocks, kSweepThreads, 0, s>>>(cv, m->values, m->active, m->flags, m->origin, lt, ch,
-                                                               m->d_status);
+                                                               m->d_status, g);
   else if (m->batch)
     k_sweep<true, false><<<kSweepBlocks, kSweepThreads, 0, s>>>(cv, m->values, m->active, m->flags, m->origin, lt,
-                                                                ch, m->d_status);
+                                                                ch, m->d_status, g);
   else if (m->track_changes)
     k_sweep<false, true><<<kSweepBlocks, kSweepThreads, 0, s>>>(cv, m->values, m->active, m->flags, m->origin, lt,
-                                                                ch, m->d_status);
+                                                                ch, m->d_status, g);
   else
     k_sweep<false, false><<<kSweepBlocks, kSweepThreads, 0, s>>>(cv, m->values, m->active, m->flags, m->origin, lt,
-                                                                 ch, m->d_status);
+                                                                 ch, m->d_status, g);
   VDBG_CUDA(cudaGetLastError());
   m->timings.launches += 2;
   return VDBG_OK;
 }
 
-// After a sweep: fresh update grid for the channel.
-int finish_sweep(vdbg_map* m, Channel& c, cudaStream_t s)
+// After a sweep (or a dropped marking): fresh update grid for the channel.
+int finish_sweep(vdbg_map* m, Channel& c, cudaStream_t s, bool gated = false)
 {
-  VDBG_CUDA(cudaMemsetAsync(c.n_touched, 0, sizeof(uint32_t), s));
-  VDBG_CUDA(cudaMemsetAsync(c.n_blist, 0, sizeof(uint32_t), s));
-  c.cur_epoch += 1;
-  if (c.cur_epoch == 0) c.cur_epoch = 1;
+  k_finish_window<<<1, 1, 0, s>>>(channel_view(c), m->d_status, gated ? 1 : 0);
+  VDBG_CUDA(cudaGetLastError());
   c.pending = false;
   return VDBG_OK;
 }
@@ -982,6 +1016,109 @@ CastPlan plan_single(const vdbg_map* m, int64_t n, const double origin[3], doubl
   return p;
 }
 
+// Kernel launches of one captured step (memsets excluded).
+constexpr uint32_t kGraphKernels = 9;
+
+// Queues one batched step for capture: the point count is read on the device
+// from t.first[t.n], the grids cover the scratch capacity `cap`, and every
+// kernel after the DDA pass skips itself unless the marking completed.
+int queue_step(vdbg_map* m, Channel& c, const char* pts, int64_t cap, int64_t stride, const ScanTable& t,
+               const RunBuffer& rb, cudaStream_t s)
+{
+  const unsigned blocks = static_cast<unsigned>((cap + 255) / 256);
+  k_prep<<<blocks, 256, 0, s>>>(pts, cap, stride, t, m->d_rays, m->d_ray_scan, m->d_hist, m->d_status);
+  k_scan<<<1, 1024, 0, s>>>(m->d_hist, m->d_cursor, static_cast<uint32_t>(kBucketsPerScan * t.n), m->d_status);
+  k_scatter<<<blocks, 256, 0, s>>>(m->d_rays, cap, t, m->d_cursor, m->d_order);
+  VDBG_CUDA(cudaEventRecordWithFlags(m->ev_prep, s, cudaEventRecordExternal));
+  k_mark_hits<<<blocks, 256, 0, s>>>(m->d_rays, m->d_order, t, map_view(m), channel_view(c));
+  VDBG_TRY(launch_dda_pass(m, c, m->d_rays, m->d_order, t, rb, m->lstate, m->wstate, false, s,
+                           cudaEventRecordExternal));
+  VDBG_CUDA(cudaEventRecordWithFlags(m->ev_dda, s, cudaEventRecordExternal));
+  VDBG_TRY(launch_sweep(m, c, s, true));
+  k_finish_window<<<1, 1, 0, s>>>(channel_view(c), m->d_status, 1);
+  VDBG_CUDA(cudaGetLastError());
+  return VDBG_OK;
+}
+
+// Captures the step for the current layout into m->graph (updating the
+// executable graph in place when its topology allows).
+int capture_step(vdbg_map* m, Channel& c, const char* pts, int64_t stride, const ScanTable& t, const RunBuffer& rb,
+                 cudaStream_t s)
+{
+  apply_grid(m, rb.apply_chunk);  // (an occupancy query: not inside the capture)
+  const uint32_t launches = m->timings.launches;
+  cudaGraph_t g           = nullptr;
+  VDBG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  const int q          = queue_step(m, c, pts, static_cast<int64_t>(m->ray_cap), stride, t, rb, s);
+  const cudaError_t ec = cudaStreamEndCapture(s, &g);
+  m->timings.launches  = launches;
+  if (q != VDBG_OK || ec != cudaSuccess)
+  {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return q != VDBG_OK ? q : VDBG_ERR_CUDA;
+  }
+  if (m->graph)
+  {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(m->graph, g, &info) != cudaSuccess)
+    {
+      cudaGetLastError();
+      cudaGraphExecDestroy(m->graph);
+      m->graph = nullptr;
+    }
+  }
+  cudaError_t ei = cudaSuccess;
+  if (!m->graph) ei = cudaGraphInstantiate(&m->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ei != cudaSuccess)
+  {
+    m->graph = nullptr;
+    return ei == cudaErrorMemoryAllocation ? VDBG_ERR_OUT_OF_MEMORY : VDBG_ERR_CUDA;
+  }
+  m->graph_layout = m->layout;
+  m->graph_pts    = pts;
+  m->graph_stride = stride;
+  m->graph_captures += 1;
+  return VDBG_OK;
+}
+
+// One batched step through the captured graph: the points' copy, the graph,
+// one status fetch. *swept when the graph integrated the window (the marking
+// completed in its one DDA pass); otherwise the step goes on as the launch
+// loop does (pool growth, resume passes) and the caller sweeps.
+int graph_step(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t stride, const ScanTable& t,
+               uint32_t flags, const RunBuffer& rb, cudaStream_t s, bool* swept)
+{
+  *swept          = false;
+  const char* pts = reinterpret_cast<const char*>(xyz);
+  if ((flags & VDBG_POINTS_DEVICE) == 0)
+  {
+    VDBG_CUDA(cudaMemcpyAsync(m->d_pts, xyz, static_cast<size_t>(n) * static_cast<size_t>(stride),
+                              cudaMemcpyHostToDevice, s));
+    pts = m->d_pts;
+  }
+  c.pending = true;
+  if (!m->graph || m->graph_layout != m->layout || m->graph_pts != pts || m->graph_stride != stride)
+    VDBG_TRY(capture_step(m, c, pts, stride, t, rb, s));
+  VDBG_CUDA(cudaGraphLaunch(m->graph, s));
+  m->graph_replays += 1;
+  m->timed_prep = true;
+  m->timings.launches += kGraphKernels;
+  VDBG_TRY(fetch_status(m, s));
+  add_apply_time(m);
+  if (m->h_status->windows > 0u)
+  {
+    m->n_leaves    = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
+    m->n_blocks    = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
+    m->passes_last = 1;
+    c.pending      = false;
+    *swept         = true;
+    return VDBG_OK;
+  }
+  return settle_dda_passes(m, c, m->d_rays, m->d_order, n, t, rb, m->lstate, m->wstate, true, s, 1);
+}
+
 int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t stride, const CastPlan& plan,
                              Channel* src, uint32_t flags, cudaStream_t s, bool integrate_all, Channel* only,
                              vdbg_scan_stats* stats)
@@ -1016,11 +1153,29 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
       t.first    = m->d_first;
       t.ray_scan = m->d_ray_scan;
     }
-    VDBG_TRY(launch_prep(m, *src, xyz, n, stride, t, flags, s, m->d_pts, m->d_rays, m->d_ray_scan, m->d_order,
-                         m->d_hist, m->d_cursor));
     const RunBuffer rb =
       run_buffer(m, m->run_key, m->run_bits, m->run_slab, m->run_count, m->run_seg, m->dda_warps);
-    const int d        = run_dda_passes(m, *src, m->d_rays, m->d_order, n, t, rb, m->lstate, m->wstate, true, s);
+    const bool graphed = m->use_graph && m->batch && t.n > 1 && !m->track_changes && integrate_all &&
+                         m->channels.size() == 1 && src == &m->channels[0];
+    int d = VDBG_OK;
+    if (graphed)
+    {
+      bool swept = false;
+      d          = graph_step(m, *src, xyz, n, stride, t, flags, rb, s, &swept);
+      if (d == VDBG_OK && swept)
+      {
+        record_timings(m);
+        fill_stats(m, leaves_before, stats);
+        VDBG_TRY(maybe_grow_ahead(m));
+        return call_status;
+      }
+    }
+    else
+    {
+      VDBG_TRY(launch_prep(m, *src, xyz, n, stride, t, flags, s, m->d_pts, m->d_rays, m->d_ray_scan, m->d_order,
+                           m->d_hist, m->d_cursor));
+      d = run_dda_passes(m, *src, m->d_rays, m->d_order, n, t, rb, m->lstate, m->wstate, true, s);
+    }
     if (d == VDBG_ERR_COORD_RANGE)
     {
       call_status = d;
@@ -1322,11 +1477,13 @@ int vdbg_destroy(vdbg_map* m)
   if (!m) return VDBG_OK;
   cudaSetDevice(m->device);
   if (m->stream) cudaStreamSynchronize(m->stream);
+  if (m->graph) cudaGraphExecDestroy(m->graph);
+  m->graph = nullptr;
   for (Channel& c : m->channels)
   {
     free_channel_leaves(m, c, m->capacity);
     free_channel_blocks(m, c, m->bcapacity);
-    dev_free(m, c.n_touched, 1);
+    dev_free(m, c.n_touched, 4);
     dev_free(m, c.n_blist, 1);
   }
   dev_free(m, m->values, static_cast<size_t>(m->capacity) * 512);
@@ -1398,18 +1555,18 @@ int vdbg_add_input_source(vdbg_map* m, const char* id, double max_range, double 
   c.max_range = (max_range == 0) ? m->conf[0].max_range : max_range;
   int st      = alloc_channel_leaves(m, c, m->capacity);
   if (st == VDBG_OK) st = alloc_channel_blocks(m, c, m->bcapacity);
-  if (st == VDBG_OK) st = dev_alloc(m, &c.n_touched, 1);
+  if (st == VDBG_OK) st = dev_alloc(m, &c.n_touched, 4);
   if (st == VDBG_OK) st = dev_alloc(m, &c.n_blist, 1);
   if (st != VDBG_OK)
   {
     free_channel_leaves(m, c, m->capacity);
     free_channel_blocks(m, c, m->bcapacity);
-    dev_free(m, c.n_touched, 1);
+    dev_free(m, c.n_touched, 4);
     dev_free(m, c.n_blist, 1);
     return st;
   }
-  VDBG_CUDA(cudaMemsetAsync(c.n_touched, 0, sizeof(uint32_t), m->stream));
-  VDBG_CUDA(cudaMemsetAsync(c.n_blist, 0, sizeof(uint32_t), m->stream));
+  k_window_init<<<1, 1, 0, m->stream>>>(channel_view(c));
+  VDBG_CUDA(cudaGetLastError());
   VDBG_CUDA(cudaStreamSynchronize(m->stream));
   m->channels.push_back(c);
   std::sort(m->channels.begin(), m->channels.end(),
@@ -1497,10 +1654,9 @@ int vdbg_reset_map(vdbg_map* m)
     VDBG_CUDA(cudaMemsetAsync(c.upd, 0, static_cast<size_t>(cap) * 16 * sizeof(unsigned long long), s));
     VDBG_CUDA(cudaMemsetAsync(c.btouched, 0, static_cast<size_t>(bcap) * 8 * sizeof(unsigned long long), s));
     VDBG_CUDA(cudaMemsetAsync(c.bepoch, 0, static_cast<size_t>(bcap) * sizeof(uint32_t), s));
-    VDBG_CUDA(cudaMemsetAsync(c.n_touched, 0, sizeof(uint32_t), s));
-    VDBG_CUDA(cudaMemsetAsync(c.n_blist, 0, sizeof(uint32_t), s));
-    c.cur_epoch = 1;
-    c.pending   = false;
+    k_window_init<<<1, 1, 0, s>>>(channel_view(c));
+    VDBG_CUDA(cudaGetLastError());
+    c.pending = false;
   }
   if (m->chg_count) VDBG_CUDA(cudaMemsetAsync(m->chg_count, 0, sizeof(uint32_t), s));
   VDBG_CUDA(cudaStreamSynchronize(s));
@@ -1569,6 +1725,7 @@ int vdbg_set_tuning(vdbg_map* m, const vdbg_tuning* t)
     m->dda_warps   = static_cast<uint32_t>(m->num_sms) * static_cast<uint32_t>(t->dda_warps_per_sm);
   }
   m->tuning = *t;
+  m->layout += 1;  // kernel parameters of a captured step change
   if (rehash)
   {
     VDBG_TRY(rebuild_hash(m, hash_size_for(m, m->bcapacity), m->n_blocks));
@@ -1581,6 +1738,28 @@ int vdbg_get_tuning(const vdbg_map* m, vdbg_tuning* out)
 {
   if (!m || !out) return VDBG_ERR_INVALID_ARGUMENT;
   *out = m->tuning;
+  return VDBG_OK;
+}
+
+int vdbg_batch_use_graph(vdbg_map* m, int enable)
+{
+  if (!m || !m->batch) return VDBG_ERR_INVALID_ARGUMENT;
+  VDBG_TRY(set_device(m));
+  m->use_graph = enable != 0;
+  if (!m->use_graph && m->graph)
+  {
+    VDBG_CUDA(cudaStreamSynchronize(m->stream));
+    cudaGraphExecDestroy(m->graph);
+    m->graph = nullptr;
+  }
+  return VDBG_OK;
+}
+
+int vdbg_graph_stats(const vdbg_map* m, uint64_t* captures, uint64_t* replays)
+{
+  if (!m) return VDBG_ERR_INVALID_ARGUMENT;
+  if (captures) *captures = m->graph_captures;
+  if (replays) *replays = m->graph_replays;
   return VDBG_OK;
 }
 
@@ -1689,12 +1868,13 @@ int vdbg_create_batch(int n_maps, const double* resolutions, const vdbg_options*
   c.id   = "";
   int st = alloc_channel_leaves(m, c, m->capacity);
   if (st == VDBG_OK) st = alloc_channel_blocks(m, c, m->bcapacity);
-  if (st == VDBG_OK) st = dev_alloc(m, &c.n_touched, 1);
+  if (st == VDBG_OK) st = dev_alloc(m, &c.n_touched, 4);
   if (st == VDBG_OK) st = dev_alloc(m, &c.n_blist, 1);
-  if (st == VDBG_OK && (cudaMemsetAsync(c.n_touched, 0, sizeof(uint32_t), m->stream) != cudaSuccess ||
-                        cudaMemsetAsync(c.n_blist, 0, sizeof(uint32_t), m->stream) != cudaSuccess ||
-                        cudaStreamSynchronize(m->stream) != cudaSuccess))
-    st = VDBG_ERR_CUDA;
+  if (st == VDBG_OK)
+  {
+    k_window_init<<<1, 1, 0, m->stream>>>(channel_view(c));
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(m->stream) != cudaSuccess) st = VDBG_ERR_CUDA;
+  }
   m->channels.push_back(c);  // freed by vdbg_destroy on failure too
   if (st != VDBG_OK)
   {

@@ -494,6 +494,16 @@ class MapBatch:
     def trackChanges(self, enable: bool = True) -> None:
         self._check(self._lib.vdbg_track_changes(self._h, 1 if enable else 0), "vdbg_track_changes")
 
+    def useGraph(self, enable: bool = True) -> None:
+        """Replay each batched step as one captured CUDA graph (default on;
+        results are the same either way)."""
+        self._check(self._lib.vdbg_batch_use_graph(self._h, 1 if enable else 0), "vdbg_batch_use_graph")
+
+    def graphStats(self) -> dict:
+        c, r = C.c_uint64(), C.c_uint64()
+        self._check(self._lib.vdbg_graph_stats(self._h, C.byref(c), C.byref(r)), "vdbg_graph_stats")
+        return {"captures": c.value, "replays": r.value}
+
     def exportChanges(self, map_index: int):
         """Change set of the last batched insert for one map."""
         return _export_changes(self._lib, self._h, map_index, self._check)
