@@ -282,8 +282,10 @@ def run_ours(args):
     dev_pts = [torch.from_numpy(p).cuda() for p, _ in scans]
     torch.cuda.synchronize()
     m = new_map()
+    warmup_passes = []
     for k in range(args.warmup):
         m.insertPointCloud(dev_pts[k], scans[k][1], "lidar", stream=sh)
+        warmup_passes.append(m.timings()["passes"])
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     stats, phases = [], []
@@ -353,7 +355,8 @@ def run_ours(args):
                       "sweep (k_compact+k_sweep)": sweep, "kernels_total": mean_total_ms},
         "per_scan": {"rays": n_pts, "visits": statistics.mean(s["visits"] for s in stats),
                      "runs": mean_runs, "updates": mean_u, "touched_leaves": mean_lt,
-                     "new_leaves": statistics.mean(s["new_leaves"] for s in stats)},
+                     "new_leaves": statistics.mean(s["new_leaves"] for s in stats),
+                     "dda_passes": [p["passes"] for p in phases], "warmup_dda_passes": warmup_passes},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                      "traffic": traffic.get(dom),

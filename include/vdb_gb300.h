@@ -157,6 +157,7 @@ typedef struct vdbg_timings
   uint64_t retries;        /* re-marking passes after a pool or hash growth */
   double apply_ms;         /* the run-merging kernel (k_apply_runs) alone, all passes (part of dda_ms) */
   uint64_t runs;           /* slab runs the traversal wrote (the merging kernel's input) */
+  uint64_t passes;         /* DDA passes of the call (more than one when the run buffer filled) */
 } vdbg_timings;
 
 int vdbg_get_timings(const vdbg_map* map, vdbg_timings* out);
@@ -249,7 +250,8 @@ int vdbg_batch_insert(vdbg_map* batch, const float* xyz, const int64_t* counts, 
  * default). The step is captured once per buffer layout and replayed as one
  * graph launch: prep, endpoint hits, the first DDA pass with its apply,
  * compact, sweep. It is captured again after a pool, scratch or run-buffer
- * reallocation, a tuning change or a new device input pointer. When a step
+ * reallocation or a tuning change (the input's address and point counts
+ * reach the graph through device memory). When a step
  * needs a second DDA pass or a pool to grow, the graph's compact and sweep
  * skip themselves on the device and the call finishes the step with separate
  * launches. Off, or with change tracking on, every step uses separate

@@ -72,17 +72,21 @@ def test_graph_device_inputs_at_new_addresses(vdbg):
     torch = pytest.importorskip("torch")
     wl = W.BatchedWorkload(seed=65, n_maps=3, n_steps=3, n_min=1000, n_max=8000)
     pair = make_pair(vdbg, wl)
-    for k in range(3):
+    keep = []
+    for k in (0, 1, 2, 1, 0):
         scans = wl.step(k)
         pts = np.concatenate([np.concatenate([p[:, :3], np.zeros((len(p), 1), np.float32)], 1) for p, _ in scans])
         counts = [len(p) for p, _ in scans]
-        dev = torch.from_numpy(pts).cuda()
+        keep.append(torch.from_numpy(pts).cuda())  # every step at a new address
         torch.cuda.synchronize()
+        if k == 1 and len(keep) == 4:
+            before = pair[0].graphStats()["captures"]
         for b in pair:
-            b.insert_packed(dev, counts, [o for _, o in scans])
-        del dev
+            b.insert_packed(keep[-1], counts, [o for _, o in scans])
     assert_pair_equal(pair, wl.n_maps)
-    assert pair[0].graphStats()["replays"] == 3
+    gs = pair[0].graphStats()
+    assert gs["replays"] == 5
+    assert gs["captures"] == before  # new input addresses replay the same graph
 
 
 def test_graph_coord_range_leaves_maps_unchanged(vdbg):

@@ -82,6 +82,7 @@ class vdbg_timings(C.Structure):
         ("retries", C.c_uint64),
         ("apply_ms", C.c_double),
         ("runs", C.c_uint64),
+        ("passes", C.c_uint64),
     ]
 
     def as_dict(self):

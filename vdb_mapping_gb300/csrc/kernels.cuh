@@ -75,11 +75,13 @@ __device__ __forceinline__ int64_t points_of(const ScanTable& t, int64_t n)
 
 // One thread per point. rays[i] = (end voxel xyz, meta). Every lane of a
 // warp stays to the end so the warp-wide reductions see a full mask.
-__global__ void __launch_bounds__(256) k_prep(const char* __restrict__ pts, int64_t n, int64_t stride,
-                                              ScanTable t, int4* __restrict__ rays,
+// `pts_ref` (a captured step): the points' address is read there instead.
+__global__ void __launch_bounds__(256) k_prep(const char* __restrict__ pts, const char* const* pts_ref, int64_t n,
+                                              int64_t stride, ScanTable t, int4* __restrict__ rays,
                                               uint16_t* __restrict__ ray_scan, uint32_t* __restrict__ hist,
                                               DevStatus* st)
 {
+  if (pts_ref) pts = *pts_ref;
   const int64_t i     = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const bool in_range = i < points_of(t, n);
   uint32_t meta       = 0;

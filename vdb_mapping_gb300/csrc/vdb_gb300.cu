@@ -116,6 +116,7 @@ struct vdbg_map
   uint32_t passes_last  = 0;
 
   int64_t bytes         = 0;
+  uint64_t run_budget   = 2ull << 30;  // run buffer bytes the map may grow to
   int num_sms           = 152;
   vdbg_tuning tuning{16, 2048, {2048, 1024, 512}, 0.5f, 16};
   uint32_t apply_grid_chunk = 0;   // apply_chunk the cached grid size is for
@@ -134,7 +135,8 @@ struct vdbg_map
   bool use_graph                   = true;
   cudaGraphExec_t graph            = nullptr;
   uint64_t graph_layout            = 0;
-  const void* graph_pts            = nullptr;
+  const char** d_pts_ref           = nullptr;  // the step's points address (batch), read by k_prep
+  const char** h_pts_ref           = nullptr;  // pinned staging
   int64_t graph_stride             = 0;
   uint64_t graph_captures          = 0;
   uint64_t graph_replays           = 0;
@@ -158,7 +160,7 @@ constexpr uint32_t kMinBlocks       = 1u << 10;
 constexpr int kSweepBlocks          = 152 * 8;
 constexpr int kSweepThreads         = 256;
 constexpr uint32_t kMinRunSeg       = 2048;   // runs per DDA warp segment, at least
-constexpr uint32_t kMaxRunBytes     = 2u << 30;  // run buffer growth budget
+constexpr uint64_t kMaxRunBytes     = 8ull << 30;  // run buffer growth budget, at most 1/32 of the device
 
 uint32_t next_pow2(uint64_t v)
 {
@@ -602,7 +604,7 @@ int launch_prep(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t st
     pts = pts_scratch;
   }
   const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
-  k_prep<<<blocks, 256, 0, s>>>(pts, n, stride, t, rays, ray_scan, hist, m->d_status);
+  k_prep<<<blocks, 256, 0, s>>>(pts, nullptr, n, stride, t, rays, ray_scan, hist, m->d_status);
   k_scan<<<1, 1024, 0, s>>>(hist, cursor, static_cast<uint32_t>(kBucketsPerScan * t.n), m->d_status);
   k_scatter<<<blocks, 256, 0, s>>>(rays, n, t, cursor, order);
   VDBG_CUDA(cudaGetLastError());
@@ -728,7 +730,8 @@ int settle_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* orde
         VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
         VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
         VDBG_CUDA(cudaStreamSynchronize(s));
-        m->passes_last = passes;
+        m->passes_last    = passes;
+        m->timings.passes = passes;
         return VDBG_ERR_COORD_RANGE;
       }
       if (err & (kErrSpin | kErrStepBound)) return map_error(err);
@@ -769,7 +772,8 @@ int settle_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* orde
     add_apply_time(m);
   }
   VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
-  m->passes_last = passes;
+  m->passes_last    = passes;
+  m->timings.passes = passes;
   return VDBG_OK;
 }
 
@@ -1022,11 +1026,12 @@ constexpr uint32_t kGraphKernels = 9;
 // Queues one batched step for capture: the point count is read on the device
 // from t.first[t.n], the grids cover the scratch capacity `cap`, and every
 // kernel after the DDA pass skips itself unless the marking completed.
-int queue_step(vdbg_map* m, Channel& c, const char* pts, int64_t cap, int64_t stride, const ScanTable& t,
-               const RunBuffer& rb, cudaStream_t s)
+int queue_step(vdbg_map* m, Channel& c, int64_t cap, int64_t stride, const ScanTable& t, const RunBuffer& rb,
+               cudaStream_t s)
 {
   const unsigned blocks = static_cast<unsigned>((cap + 255) / 256);
-  k_prep<<<blocks, 256, 0, s>>>(pts, cap, stride, t, m->d_rays, m->d_ray_scan, m->d_hist, m->d_status);
+  k_prep<<<blocks, 256, 0, s>>>(nullptr, m->d_pts_ref, cap, stride, t, m->d_rays, m->d_ray_scan, m->d_hist,
+                                m->d_status);
   k_scan<<<1, 1024, 0, s>>>(m->d_hist, m->d_cursor, static_cast<uint32_t>(kBucketsPerScan * t.n), m->d_status);
   k_scatter<<<blocks, 256, 0, s>>>(m->d_rays, cap, t, m->d_cursor, m->d_order);
   VDBG_CUDA(cudaEventRecordWithFlags(m->ev_prep, s, cudaEventRecordExternal));
@@ -1042,14 +1047,13 @@ int queue_step(vdbg_map* m, Channel& c, const char* pts, int64_t cap, int64_t st
 
 // Captures the step for the current layout into m->graph (updating the
 // executable graph in place when its topology allows).
-int capture_step(vdbg_map* m, Channel& c, const char* pts, int64_t stride, const ScanTable& t, const RunBuffer& rb,
-                 cudaStream_t s)
+int capture_step(vdbg_map* m, Channel& c, int64_t stride, const ScanTable& t, const RunBuffer& rb, cudaStream_t s)
 {
   apply_grid(m, rb.apply_chunk);  // (an occupancy query: not inside the capture)
   const uint32_t launches = m->timings.launches;
   cudaGraph_t g           = nullptr;
   VDBG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  const int q          = queue_step(m, c, pts, static_cast<int64_t>(m->ray_cap), stride, t, rb, s);
+  const int q          = queue_step(m, c, static_cast<int64_t>(m->ray_cap), stride, t, rb, s);
   const cudaError_t ec = cudaStreamEndCapture(s, &g);
   m->timings.launches  = launches;
   if (q != VDBG_OK || ec != cudaSuccess)
@@ -1077,7 +1081,6 @@ int capture_step(vdbg_map* m, Channel& c, const char* pts, int64_t stride, const
     return ei == cudaErrorMemoryAllocation ? VDBG_ERR_OUT_OF_MEMORY : VDBG_ERR_CUDA;
   }
   m->graph_layout = m->layout;
-  m->graph_pts    = pts;
   m->graph_stride = stride;
   m->graph_captures += 1;
   return VDBG_OK;
@@ -1098,9 +1101,13 @@ int graph_step(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t str
                               cudaMemcpyHostToDevice, s));
     pts = m->d_pts;
   }
+  // The points' address goes to the device with the step (the copy reads
+  // the pinned word when it runs; the previous step has completed).
+  *m->h_pts_ref = pts;
+  VDBG_CUDA(cudaMemcpyAsync(m->d_pts_ref, m->h_pts_ref, sizeof(const char*), cudaMemcpyHostToDevice, s));
   c.pending = true;
-  if (!m->graph || m->graph_layout != m->layout || m->graph_pts != pts || m->graph_stride != stride)
-    VDBG_TRY(capture_step(m, c, pts, stride, t, rb, s));
+  if (!m->graph || m->graph_layout != m->layout || m->graph_stride != stride)
+    VDBG_TRY(capture_step(m, c, stride, t, rb, s));
   VDBG_CUDA(cudaGraphLaunch(m->graph, s));
   m->graph_replays += 1;
   m->timed_prep = true;
@@ -1111,8 +1118,9 @@ int graph_step(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t str
   {
     m->n_leaves    = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
     m->n_blocks    = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
-    m->passes_last = 1;
-    c.pending      = false;
+    m->passes_last    = 1;
+    m->timings.passes = 1;
+    c.pending         = false;
     *swept         = true;
     return VDBG_OK;
   }
@@ -1136,7 +1144,7 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
     if (m->passes_last > 1)
     {
       const uint64_t want  = static_cast<uint64_t>(m->run_seg) * m->passes_last * 5 / 4;
-      const uint64_t limit = kMaxRunBytes / (17ull * m->dda_warps);
+      const uint64_t limit = m->run_budget / (17ull * m->dda_warps);
       seg                  = static_cast<uint32_t>(std::min<uint64_t>(want, limit));
     }
     VDBG_TRY(ensure_runs(m, seg));
@@ -1340,6 +1348,11 @@ int create_impl(int n_maps, const double* resolutions, const vdbg_options* optio
   if (cudaSetDevice(m->device) != cudaSuccess) return fail(VDBG_ERR_CUDA);
   if (cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, m->device) != cudaSuccess)
     return fail(VDBG_ERR_CUDA);
+  {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return fail(VDBG_ERR_CUDA);
+    m->run_budget = std::min<uint64_t>(kMaxRunBytes, total_b / 32);
+  }
   m->dda_warps = static_cast<uint32_t>(m->num_sms) * static_cast<uint32_t>(m->tuning.dda_warps_per_sm);
   if (cudaFuncSetAttribute(k_apply_runs, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            static_cast<int>(apply_stage_bytes(kApplyMaxChunk))) != cudaSuccess)
@@ -1367,9 +1380,11 @@ int create_impl(int n_maps, const double* resolutions, const vdbg_options* optio
     s        = dev_alloc(m, &m->d_lo, static_cast<size_t>(n_maps));
     if (s == VDBG_OK) s = dev_alloc(m, &m->d_geom, static_cast<size_t>(n_maps));
     if (s == VDBG_OK) s = dev_alloc(m, &m->d_first, static_cast<size_t>(n_maps) + 1);
+    if (s == VDBG_OK) s = dev_alloc(m, &m->d_pts_ref, 1);
     if (s != VDBG_OK) return fail(s);
     if (cudaMallocHost(reinterpret_cast<void**>(&m->h_geom), sizeof(ScanGeom) * n_maps) != cudaSuccess ||
-        cudaMallocHost(reinterpret_cast<void**>(&m->h_first), sizeof(uint32_t) * (n_maps + 1)) != cudaSuccess)
+        cudaMallocHost(reinterpret_cast<void**>(&m->h_first), sizeof(uint32_t) * (n_maps + 1)) != cudaSuccess ||
+        cudaMallocHost(reinterpret_cast<void**>(&m->h_pts_ref), sizeof(const char*)) != cudaSuccess)
       return fail(VDBG_ERR_OUT_OF_MEMORY);
     if (cudaMemsetAsync(m->d_lo, 0, sizeof(LogOdds) * n_maps, m->stream) != cudaSuccess) return fail(VDBG_ERR_CUDA);
   }
@@ -1504,6 +1519,8 @@ int vdbg_destroy(vdbg_map* m)
   dev_free(m, m->d_ray_scan, m->ray_cap);
   if (m->h_geom) cudaFreeHost(m->h_geom);
   if (m->h_first) cudaFreeHost(m->h_first);
+  dev_free(m, m->d_pts_ref, 1);
+  if (m->h_pts_ref) cudaFreeHost(m->h_pts_ref);
   dev_free(m, m->d_pts, m->pts_cap);
   dev_free(m, m->d_rays, m->ray_cap);
   dev_free(m, m->d_order, m->ray_cap);
