@@ -63,6 +63,8 @@ def parse_args():
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="simulated traffic for --workload serving")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="device-memory admission budget")
     ap.add_argument("--no-autotune", action="store_true", help="batched mode: keep the library's default tuning")
+    ap.add_argument("--tuning", default=None,
+                    help='dense mode: kernel tuning as JSON, e.g. \'{"apply_chunk_runs": 1024}\' (speed only)')
     ap.add_argument("--no-graph", action="store_true",
                     help="batched and serving modes: separate launches instead of the captured step")
     ap.add_argument("--batch-steps", type=int, default=4,
@@ -173,6 +175,7 @@ def config_block(wl, args, world):
         "l2": "flushed between steps (256 MiB write)",
         "parallelism": f"replicas x{world}" if world > 1 else "single map",
         "leaf_pool_slots": args.leaf_capacity or DEFAULT_CAPACITY.get(wl.name, 1 << 20),
+        "tuning": json.loads(args.tuning) if getattr(args, "tuning", None) else "library defaults",
     }
 
 
@@ -274,6 +277,8 @@ def run_ours(args):
 
     def new_map():
         m = OccupancyVDBMapping(wl.resolution, initial_leaf_capacity=cap, device=local)
+        if args.tuning:
+            m.setTuning({**m.tuning(), **json.loads(args.tuning)})
         m.setConfig(wl.config)
         m.addInputSource("lidar", wl.max_range, 0)
         return m

@@ -12,7 +12,10 @@
 //   borigin int4[PB]     block coordinate (voxel >> 6), .w = map
 //   bleaf   i32[PB][512] leaf slot of each leaf cell of the block, -1 none
 //   origin  int4[P]      leaf origin (voxel coordinates, multiples of 8), .w = map
-//   values  f32[P][512]  log-odds, OpenVDB leaf order (x&7)<<6 | (y&7)<<3 | (z&7)
+//   values  f32[P][512]  log-odds, z-major leaf order (z&7)<<6 | (y&7)<<3 | (x&7)
+//                        (OpenVDB's order with x and z swapped: a mask word is
+//                        one z-plane, which a near-horizontal ray crosses in
+//                        one run; the export swaps them back)
 //   active  u64[P][8]    value (active) mask, bit i of word w = offset 64w+i
 //   flags   u32[P]       1 once the leaf belongs to the map (first integration)
 // Per update grid (one per input source):
@@ -82,7 +85,7 @@ struct DevStatus
   uint32_t n_blocks;    // block bump allocator
   uint32_t inflight;    // lanes that ended a DDA pass with a ray in flight
   uint32_t windows;     // update-grid windows closed by k_finish_window
-  unsigned long long runs;  // slab runs written by the traversal (all passes)
+  unsigned long long runs;  // plane runs written by the traversal (all passes)
 };
 
 struct LogOdds
@@ -161,14 +164,14 @@ struct MapView
   DevStatus* st;
 };
 
-// Slab runs of one DDA pass: a run is the set of voxels one ray visits in one
-// x-slab (64 voxels) of one leaf. Warp w of the pass writes its runs to its
-// own segment [w * seg, w * seg + count[w]).
+// Plane runs of one DDA pass: a run is the set of voxels one ray visits in one
+// z-plane (64 voxels, one mask word) of one leaf. Warp w of the pass writes its
+// runs to its own segment [w * seg, w * seg + count[w]).
 struct RunBuffer
 {
   unsigned long long* key;   // leaf key
-  unsigned long long* bits;  // visited voxels of the slab
-  unsigned char* slab;       // x & 7
+  unsigned long long* bits;  // visited voxels of the plane, bit (y & 7) << 3 | (x & 7)
+  unsigned char* slab;       // z & 7 (the mask word)
   uint32_t* count;           // runs per warp segment
   uint32_t seg;              // segment capacity (runs)
   uint32_t warps;            // segments

@@ -8,7 +8,7 @@
 //                                       grouped by direction)
 //   k_dda_mark VDBMapping.hpp:550-566    FP64 DDA from the sensor voxel to the
 //                                       endpoint voxel; writes the visited
-//                                       voxels as slab runs
+//                                       voxels as z-plane runs
 //   k_apply_runs VDBMapping.hpp:563     merges the runs, ORs them into the
 //                                       per-leaf update masks
 //   k_mark_hits VDBMapping.hpp:533-536  hit bits of unclipped endpoints
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, 
 }
 
 // ---------------------------------------------------------------------------
-// k_dda_mark: warp-cooperative traversal, writing slab runs.
+// k_dda_mark: warp-cooperative traversal, writing plane runs.
 //
 // Each lane walks one ray at a time with the FP64 DDA of OpenVDB's
 // DDA<Ray<double>,0> as driven by castRayIntoGrid (eye = origin voxel + 0.5,
@@ -262,8 +262,10 @@ __global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, 
 // per step is the sequential tMax += tDelta of the stepped axis; the step is
 // branch-free so the 32 lanes stay converged.
 //
-// A ray is monotone in every axis, so it visits each x-slab of each 8^3 leaf
-// (64 voxels, one mask word) in a single contiguous run. The lane keeps the
+// A ray is monotone in every axis, so it visits each z-plane of each 8^3 leaf
+// (64 voxels, one mask word) in a single contiguous run; a near-horizontal
+// ray (LiDAR, depth cameras) stays in one plane for its whole crossing of a
+// leaf. The lane keeps the
 // bits of the current run in a register; a run is emitted at the first step
 // that leaves it (or after the ray's last voxel). Each step the warp ranks
 // its emitting lanes with one ballot and appends their runs to the warp's
@@ -285,8 +287,8 @@ constexpr uint32_t kDdaRound = 32u * kDdaRing;   // most runs a warp writes per 
 struct DdaWarpSmem
 {
   unsigned long long keys[kDdaRound];  // leaf key of the run
-  unsigned long long bits[kDdaRound];  // visited voxels of the slab
-  unsigned char slab[kDdaRound];       // x & 7 of the slab
+  unsigned long long bits[kDdaRound];  // visited voxels of the plane
+  unsigned char slab[kDdaRound];       // z & 7 of the plane (its mask word)
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt()
@@ -305,9 +307,9 @@ __device__ __forceinline__ void dda_emit(DdaWarpSmem& q, bool close, uint32_t lt
   if (close)
   {
     const uint32_t p = n + static_cast<uint32_t>(__popc(em & lt));
-    q.keys[p]        = pack_leaf_key(map, rx >> 3, ry, rz);
+    q.keys[p]        = pack_leaf_key(map, rx, ry, rz >> 3);
     q.bits[p]        = run;
-    q.slab[p]        = static_cast<unsigned char>(rx & 7);
+    q.slab[p]        = static_cast<unsigned char>(rz & 7);
     run              = 0ull;
     run_open         = false;
   }
@@ -336,7 +338,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
   int vx = 0, vy = 0, vz = 0, sx = 0, sy = 0, sz = 0;
   long long nx = 0, ny = 0, nz = 0;
   double dx = 0.0, dy = 0.0, dz = 0.0;
-  int rx = 0, ry = 0, rz = 0;  // current run: exact x, leaf y, leaf z
+  int rx = 0, ry = 0, rz = 0;  // current run: leaf x, leaf y, exact z
   int map = 0;                 // map of the lane's ray
   unsigned long long run = 0ull;
   uint32_t budget = 0;
@@ -459,18 +461,19 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
 #pragma unroll 4
     for (int s = 0; s < kDdaSteps; ++s)
     {
-      // setActiveState(voxel) on the update grid, one slab run at a time: the
-      // run of the previous step ends when the voxel leaves it or the ray ended.
-      const int ly = vy >> 3, lz = vz >> 3;
-      dda_emit(q, run_open && (!has_ray || vx != rx || ly != ry || lz != rz), lt, map, rx, ry, rz, run, run_open,
+      // setActiveState(voxel) on the update grid, one z-plane run at a time:
+      // the run of the previous step ends when the voxel leaves it or the ray
+      // ended.
+      const int lx = vx >> 3, ly = vy >> 3;
+      dda_emit(q, run_open && (!has_ray || vz != rz || lx != rx || ly != ry), lt, map, rx, ry, rz, run, run_open,
                n_rec);
       if (has_ray)
       {
-        rx       = vx;
+        rx       = lx;
         ry       = ly;
-        rz       = lz;
+        rz       = vz;
         run_open = true;
-        run |= 1ull << (((vy & 7) << 3) | (vz & 7));
+        run |= 1ull << (((vy & 7) << 3) | (vx & 7));
         // DDA::step(): argmin of tMax (ties to the higher axis), branch-free.
         const bool ax      = (nx < ny) && (nx < nz);
         const bool ay      = !ax && (ny < nz);
@@ -542,7 +545,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
 }
 
 // ---------------------------------------------------------------------------
-// k_apply_runs: merges the scan's slab runs and ORs them into the update masks.
+// k_apply_runs: merges the scan's plane runs and ORs them into the update masks.
 //
 // Persistent blocks take chunks of rb.apply_chunk runs of one warp segment
 // (written together by a warp walking neighbouring rays, so a chunk repeats
@@ -559,19 +562,23 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
 // out as one coalesced atomic request. A run that finds the table full is
 // applied directly.
 // ---------------------------------------------------------------------------
-constexpr int kApplyThreads      = 256;
-constexpr int kApplyTable        = 512;   // 2^9 entries, see apply_hash
-constexpr uint32_t kApplyMaxChunk = 4096;  // runs staged at a time, at most
+// Two block shapes: 256 threads with a 512-entry table for chunks of 1280
+// runs and more (3 blocks per SM at 2048), 128 threads with a 256-entry table
+// for chunks of up to 1024 (6 blocks per SM): fewer threads wait at each
+// barrier and more chunks are in flight per SM.
+constexpr uint32_t kApplyMaxChunk   = 4096;  // runs staged at a time, at most
+constexpr uint32_t kApplySmallChunk = 1024;  // largest chunk of the small shape
 
+template <int kTable>
 struct ApplySmem
 {
-  unsigned long long key[kApplyTable];
-  unsigned int words[kApplyTable][16];  // 8 mask words as lo/hi halves
-  int slot[kApplyTable];                // resolved leaf slot of a listed entry
-  unsigned short list[kApplyTable];     // entries in use
-  unsigned long long bar;               // completion of the staged chunk's copies
+  unsigned long long key[kTable];
+  unsigned int words[kTable][16];  // 8 mask words as lo/hi halves
+  int slot[kTable];                // resolved leaf slot of a listed entry
+  unsigned short list[kTable];     // entries in use
+  unsigned long long bar;          // completion of the staged chunk's copies
   unsigned int count;
-  unsigned int next;                    // the block's next chunk
+  unsigned int next;               // the block's next chunk
   unsigned int failed;
 };
 
@@ -581,9 +588,13 @@ __host__ __device__ constexpr size_t apply_stage_bytes(uint32_t chunk)
   return static_cast<size_t>(chunk) * 17 + 16;
 }
 
+// Table slot of `key` (Fibonacci hashing to log2(kTable) bits).
+template <int kTable>
 __device__ __forceinline__ uint32_t apply_hash(unsigned long long key)
 {
-  return static_cast<uint32_t>((key * 0x9E3779B97F4A7C15ull) >> 55);
+  constexpr int kBits = kTable == 512 ? 9 : 8;
+  static_assert((1 << kBits) == kTable, "table of 256 or 512 entries");
+  return static_cast<uint32_t>((key * 0x9E3779B97F4A7C15ull) >> (64 - kBits));
 }
 
 // Slab of leaf `key` in the update masks: resolves (and allocates) the leaf
@@ -637,7 +648,8 @@ __device__ __forceinline__ uint32_t apply_next_item(const RunBuffer& rb, uint32_
 // boundaries and chunks are multiples of 256 runs, so every copy starts
 // 16-byte aligned; lengths are rounded up to 16 bytes, which stays inside the
 // segment.
-__device__ __forceinline__ void apply_stage(const RunBuffer& rb, uint32_t cps, uint32_t item, ApplySmem& t,
+template <int kTable>
+__device__ __forceinline__ void apply_stage(const RunBuffer& rb, uint32_t cps, uint32_t item, ApplySmem<kTable>& t,
                                             unsigned long long* s_key, unsigned long long* s_bits,
                                             unsigned char* s_slab)
 {
@@ -653,10 +665,11 @@ __device__ __forceinline__ void apply_stage(const RunBuffer& rb, uint32_t cps, u
   bulk_copy_g2s(s_slab, rb.slab + base, b1, &t.bar);
 }
 
-__global__ void __launch_bounds__(kApplyThreads, 3) k_apply_runs(RunBuffer rb, MapView m, ChannelView c)
+template <int kApplyThreads, int kApplyTable>
+__global__ void __launch_bounds__(kApplyThreads) k_apply_runs(RunBuffer rb, MapView m, ChannelView c)
 {
   c.cur_epoch = *c.epoch;
-  __shared__ ApplySmem t;
+  __shared__ ApplySmem<kApplyTable> t;
   extern __shared__ __align__(16) unsigned char stage[];
   unsigned long long* s_key  = reinterpret_cast<unsigned long long*>(stage);
   unsigned long long* s_bits = s_key + rb.apply_chunk;
@@ -721,7 +734,7 @@ __global__ void __launch_bounds__(kApplyThreads, 3) k_apply_runs(RunBuffer rb, M
       int h                         = -1;
       if (have && lane == leader)
       {
-        uint32_t p = apply_hash(key);
+        uint32_t p = apply_hash<kApplyTable>(key);
         for (int probe = 0; probe < 16; ++probe)
         {
           unsigned long long kk = t.key[p];
@@ -823,13 +836,13 @@ __global__ void __launch_bounds__(256) k_mark_hits(const int4* __restrict__ rays
   if (slot < 0) return;
   unsigned long long* bt = c.btouched + static_cast<size_t>(b) * 8 + (cell >> 6);
   if (!((*bt >> (cell & 63)) & 1ull)) atomicOr(bt, 1ull << (cell & 63));
-  const uint32_t off = (static_cast<uint32_t>(r.x & 7) << 6) | (static_cast<uint32_t>(r.y & 7) << 3) |
-                       static_cast<uint32_t>(r.z & 7);
+  const uint32_t off = (static_cast<uint32_t>(r.z & 7) << 6) | (static_cast<uint32_t>(r.y & 7) << 3) |
+                       static_cast<uint32_t>(r.x & 7);
   atomicOr(c.upd + static_cast<size_t>(slot) * 16 + 8 + (off >> 6), 1ull << (off & 63));
 }
 
 // Persistent sweep over the touched leaves: 8 lanes per leaf, lane w owning
-// the x-slab w (voxel offsets 64w..64w+63, one word of each mask), so a warp
+// the z-plane w (voxel offsets 64w..64w+63, one word of each mask), so a warp
 // sweeps four leaves at once. A lane loads the float4 groups of its slab that
 // hold update bits (all loads issued before any use), applies the log-odds
 // rules, stores them back and clears its update words.

@@ -624,8 +624,11 @@ unsigned apply_grid(vdbg_map* m, uint32_t chunk)
   if (m->apply_grid_chunk != chunk)
   {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_runs, kApplyThreads,
-                                                      apply_stage_bytes(chunk)) != cudaSuccess ||
+    const bool small = chunk <= kApplySmallChunk;
+    const cudaError_t e =
+      small ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_runs<128, 256>, 128, apply_stage_bytes(chunk))
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply_runs<256, 512>, 256, apply_stage_bytes(chunk));
+    if (e != cudaSuccess ||
         per_sm < 1)
       per_sm = 1;
     m->apply_grid_chunk  = chunk;
@@ -688,6 +691,17 @@ void add_apply_time(vdbg_map* m)
   if (cudaEventElapsedTime(&ms, m->ev_a0, m->ev_a1) == cudaSuccess) m->timings.apply_ms += ms;
 }
 
+// Queues k_apply_runs in the block shape of the run chunk.
+void launch_apply(vdbg_map* m, Channel& c, const RunBuffer& rb, cudaStream_t s)
+{
+  const unsigned grid = apply_grid(m, rb.apply_chunk);
+  const size_t smem   = apply_stage_bytes(rb.apply_chunk);
+  if (rb.apply_chunk <= kApplySmallChunk)
+    k_apply_runs<128, 256><<<grid, 128, smem, s>>>(rb, map_view(m), channel_view(c));
+  else
+    k_apply_runs<256, 512><<<grid, 256, smem, s>>>(rb, map_view(m), channel_view(c));
+}
+
 // Queues one DDA pass (a fresh one, or `resume` of the rays left in flight)
 // and its k_apply_runs.
 int launch_dda_pass(vdbg_map* m, Channel& c, const int4* rays, const int* order, const ScanTable& t,
@@ -698,8 +712,7 @@ int launch_dda_pass(vdbg_map* m, Channel& c, const int4* rays, const int* order,
   k_dda_mark<<<rb.warps / kDdaWarps, kDdaWarps * 32, 0, s>>>(rays, order, t, map_view(m), rb, ls, ws,
                                                             resume ? 1 : 0);
   VDBG_CUDA(cudaEventRecordWithFlags(m->ev_a0, s, event_flags));
-  k_apply_runs<<<apply_grid(m, rb.apply_chunk), kApplyThreads, apply_stage_bytes(rb.apply_chunk), s>>>(
-    rb, map_view(m), channel_view(c));
+  launch_apply(m, c, rb, s);
   VDBG_CUDA(cudaEventRecordWithFlags(m->ev_a1, s, event_flags));
   VDBG_CUDA(cudaGetLastError());
   m->timings.launches += 2;
@@ -751,8 +764,7 @@ int settle_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* orde
       VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
       k_mark_hits<<<hit_blocks, 256, 0, s>>>(rays, order, t, map_view(m), channel_view(c));
       VDBG_CUDA(cudaEventRecord(m->ev_a0, s));
-      k_apply_runs<<<apply_grid(m, rb.apply_chunk), kApplyThreads, apply_stage_bytes(rb.apply_chunk), s>>>(
-        rb, map_view(m), channel_view(c));
+      launch_apply(m, c, rb, s);
       VDBG_CUDA(cudaEventRecord(m->ev_a1, s));
       VDBG_CUDA(cudaGetLastError());
       m->timings.launches += 2;
@@ -1354,8 +1366,10 @@ int create_impl(int n_maps, const double* resolutions, const vdbg_options* optio
     m->run_budget = std::min<uint64_t>(kMaxRunBytes, total_b / 32);
   }
   m->dda_warps = static_cast<uint32_t>(m->num_sms) * static_cast<uint32_t>(m->tuning.dda_warps_per_sm);
-  if (cudaFuncSetAttribute(k_apply_runs, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           static_cast<int>(apply_stage_bytes(kApplyMaxChunk))) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_apply_runs<256, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(apply_stage_bytes(kApplyMaxChunk))) != cudaSuccess ||
+      cudaFuncSetAttribute(k_apply_runs<128, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(apply_stage_bytes(kApplySmallChunk))) != cudaSuccess)
     return fail(VDBG_ERR_CUDA);
   if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(VDBG_ERR_CUDA);
   if (cudaEventCreate(&m->ev0) != cudaSuccess || cudaEventCreate(&m->ev1) != cudaSuccess ||
@@ -1425,6 +1439,31 @@ int set_config_impl(vdbg_map* m, int i, const vdbg_config* c)
 }
 
 // Leaves of map `map` (-1: all) that belong to the map, sorted by origin.
+// A leaf's voxels are held z-major (offset z << 6 | y << 3 | x); OpenVDB's
+// order is x-major (x << 6 | y << 3 | z). Swapping x and z maps either order
+// to the other.
+inline int swap_xz(int o) { return ((o & 7) << 6) | (o & 0x38) | (o >> 6); }
+
+// One leaf's 512 values into OpenVDB's order.
+void values_to_vdb(const float* in, float* out)
+{
+  for (int o = 0; o < 512; ++o) out[swap_xz(o)] = in[o];
+}
+
+// One leaf's 8-word voxel mask into OpenVDB's order.
+void mask_to_vdb(const unsigned long long* in, uint64_t* out)
+{
+  for (int w = 0; w < 8; ++w) out[w] = 0;
+  for (int w = 0; w < 8; ++w)
+  {
+    for (unsigned long long b = in[w]; b; b &= b - 1)
+    {
+      const int o = swap_xz(w * 64 + __builtin_ctzll(b));
+      out[o >> 6] |= 1ull << (o & 63);
+    }
+  }
+}
+
 int export_impl(vdbg_map* m, int map, int64_t capacity, int32_t* origins, float* values, uint64_t* masks,
                 int64_t* n_out, bool count_only)
 {
@@ -1471,8 +1510,8 @@ int export_impl(vdbg_map* m, int map, int64_t capacity, int32_t* origins, float*
                            cudaMemcpyDeviceToHost));
     for (size_t k = 0; k < idx.size(); ++k)
     {
-      if (values) std::memcpy(values + 512 * k, hv.data() + static_cast<size_t>(idx[k]) * 512, 512 * sizeof(float));
-      if (masks) std::memcpy(masks + 8 * k, hm.data() + static_cast<size_t>(idx[k]) * 8, 8 * sizeof(uint64_t));
+      if (values) values_to_vdb(hv.data() + static_cast<size_t>(idx[k]) * 512, values + 512 * k);
+      if (masks) mask_to_vdb(hm.data() + static_cast<size_t>(idx[k]) * 8, masks + 8 * k);
     }
   }
   return VDBG_OK;
@@ -1867,9 +1906,8 @@ int vdbg_export_changes(vdbg_map* m, int map, int64_t capacity, int32_t* origins
       origins[3 * k + 1] = o[i].y;
       origins[3 * k + 2] = o[i].z;
     }
-    if (active) std::memcpy(active + 8 * static_cast<size_t>(k), &w[16 * static_cast<size_t>(i)], 8 * sizeof(uint64_t));
-    if (value)
-      std::memcpy(value + 8 * static_cast<size_t>(k), &w[16 * static_cast<size_t>(i) + 8], 8 * sizeof(uint64_t));
+    if (active) mask_to_vdb(&w[16 * static_cast<size_t>(i)], active + 8 * static_cast<size_t>(k));
+    if (value) mask_to_vdb(&w[16 * static_cast<size_t>(i) + 8], value + 8 * static_cast<size_t>(k));
   }
   return VDBG_OK;
 }
