@@ -44,7 +44,7 @@ STATUS_BYTES = 80  # device status block (DevStatus) read back by every call
 # each kernel on a steady-state dense scan, from one ncu capture of the
 # default workload (profiles/dram_traffic_dense_street.md). Only meaningful
 # for the dense workload; other workloads report None.
-NCU_TRAFFIC_BYTES = {"k_dda_mark": 1235.5e6, "k_apply_runs": 1722.0e6, "k_sweep": 3278.5e6,
+NCU_TRAFFIC_BYTES = {"k_dda_mark": 429.6e6, "k_apply_runs": 801.2e6, "k_sweep": 2040.1e6,
                      "prep (k_prep+k_scan+k_scatter)": 4.2e6}
 
 

@@ -64,10 +64,10 @@ constexpr uint32_t kMetaL1Mask   = (1u << 29) - 1;
 constexpr uint32_t kMetaClipped  = 1u << 29;
 constexpr uint32_t kMetaValid    = 1u << 30;
 
-// Counting-sort buckets of the DDA order: 4 length classes x scans x 1014
-// direction cells (see ray_bin).
+// Counting-sort buckets of the DDA order: 8 length classes x scans x 1014
+// direction cells (see ray_bucket).
 constexpr int kDirCells    = 1014;
-constexpr int kLenClasses  = 4;
+constexpr int kLenClasses  = 8;
 constexpr int kBucketsPerScan = kLenClasses * kDirCells;
 
 struct DevStatus

@@ -24,7 +24,7 @@
 namespace vdbg {
 
 // Sort bucket of a ray of scan s (voxel offset d from the sensor voxel, L1
-// length l1): four length classes, longest first, so long rays start early
+// length l1): eight length classes, longest first, so long rays start early
 // and do not extend the tail; within a class the scan, then the cube-map face
 // of the dominant axis and a 13 x 13 cell on it (6 * 169 = 1014 direction
 // cells). Rays of one bucket are angular neighbours of similar length in one
@@ -57,7 +57,20 @@ __device__ __forceinline__ int ray_bucket(int dx, int dy, int dz, uint32_t l1, i
     v    = dy;
     mx   = az;
   }
-  const int cls  = l1 >= t.edge[0] ? 0 : (l1 >= t.edge[1] ? 1 : (l1 >= t.edge[2] ? 2 : 3));
+  // Three tuned edges, then halvings of the last edge (four at most), so the
+  // shortest rays come last and the end of a pass waits on short rays only.
+  int cls;
+  if (l1 >= t.edge[0])
+    cls = 0;
+  else if (l1 >= t.edge[1])
+    cls = 1;
+  else if (l1 >= t.edge[2])
+    cls = 2;
+  else
+  {
+    const int halvings = (31 - __clz(static_cast<int>(t.edge[2]))) - (31 - __clz(static_cast<int>(max(l1, 1u)))) - 1;
+    cls                = 3 + min(max(halvings, 0), kLenClasses - 4);
+  }
   const int base = (cls * n_scans + s) * kDirCells;
   if (mx == 0) return base;
   const int iu = static_cast<int>((static_cast<long long>(u + mx) * 13) / (2 * mx + 1));
@@ -228,6 +241,91 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ hist, uint
     __syncthreads();
   }
   if (t == 0) st->n_valid = carry;
+}
+
+// Multi-block form of k_scan for large bucket counts (batches of many
+// maps): per-tile sums, a scan of the tile sums, then each tile's own scan
+// from its offset. A tile is kScanTile buckets of a 1024-thread block.
+constexpr uint32_t kScanTile     = 4096;
+constexpr uint32_t kScanMaxTiles = 1024;
+
+// Exclusive scan of one value per thread over a 1024-thread block; *total
+// receives the block's sum.
+__device__ __forceinline__ uint32_t block_scan_exclusive(uint32_t v, uint32_t* total)
+{
+  __shared__ uint32_t ws[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t inc   = v;
+  for (int off = 1; off < 32; off <<= 1)
+  {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+    if (lane >= off) inc += y;
+  }
+  if (lane == 31) ws[warp] = inc;
+  __syncthreads();
+  if (warp == 0)
+  {
+    uint32_t w = ws[lane];
+    for (int off = 1; off < 32; off <<= 1)
+    {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+      if (lane >= off) w += y;
+    }
+    ws[lane] = w;
+  }
+  __syncthreads();
+  const uint32_t excl = (warp > 0 ? ws[warp - 1] : 0u) + inc - v;
+  *total              = ws[31];
+  __syncthreads();
+  return excl;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_sums(const uint32_t* __restrict__ hist, uint32_t nb,
+                                                    uint32_t* __restrict__ sums)
+{
+  const uint32_t i0 = blockIdx.x * kScanTile + threadIdx.x * 4u;
+  uint32_t v        = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k) v += (i0 + k < nb) ? hist[i0 + k] : 0u;
+  uint32_t total = 0;
+  block_scan_exclusive(v, &total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// Tile sums -> tile offsets (one block, at most kScanMaxTiles tiles); the
+// grand total is the number of rays in the order.
+__global__ void __launch_bounds__(1024) k_scan_tops(uint32_t* __restrict__ sums, uint32_t tiles, DevStatus* st)
+{
+  const uint32_t v = threadIdx.x < tiles ? sums[threadIdx.x] : 0u;
+  uint32_t total   = 0;
+  const uint32_t e = block_scan_exclusive(v, &total);
+  if (threadIdx.x < tiles) sums[threadIdx.x] = e;
+  if (threadIdx.x == 0) st->n_valid = total;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_tiles(uint32_t* __restrict__ hist, uint32_t* __restrict__ cursor,
+                                                     uint32_t nb, const uint32_t* __restrict__ sums)
+{
+  const uint32_t i0 = blockIdx.x * kScanTile + threadIdx.x * 4u;
+  uint32_t v[4], local = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k)
+  {
+    v[k] = (i0 + k < nb) ? hist[i0 + k] : 0u;
+    local += v[k];
+  }
+  uint32_t total = 0;
+  uint32_t base  = sums[blockIdx.x] + block_scan_exclusive(local, &total);
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k)
+  {
+    if (i0 + k < nb)
+    {
+      cursor[i0 + k] = base;
+      hist[i0 + k]   = 0u;
+    }
+    base += v[k];
+  }
 }
 
 __global__ void __launch_bounds__(256) k_scatter(const int4* __restrict__ rays, int64_t n, ScanTable t,

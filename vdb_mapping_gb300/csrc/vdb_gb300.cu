@@ -589,6 +589,22 @@ ScanTable single_table(const ScanGeom& g)
   return t;
 }
 
+// Exclusive scan of nb bucket counts into cursor (total to the status):
+// one block for up to four tiles, else the multi-block form with its tile
+// sums in cursor[nb, nb + tiles).
+void launch_scan(uint32_t* hist, uint32_t* cursor, uint32_t nb, DevStatus* st, cudaStream_t s)
+{
+  if (nb <= 4 * kScanTile)
+  {
+    k_scan<<<1, 1024, 0, s>>>(hist, cursor, nb, st);
+    return;
+  }
+  const uint32_t tiles = (nb + kScanTile - 1) / kScanTile;
+  k_scan_sums<<<tiles, 1024, 0, s>>>(hist, nb, cursor + nb);
+  k_scan_tops<<<1, 1024, 0, s>>>(cursor + nb, tiles, st);
+  k_scan_tiles<<<tiles, 1024, 0, s>>>(hist, cursor, nb, cursor + nb);
+}
+
 // Queues the per-point stage of raycastPointCloud (VDBMapping.hpp:499-519)
 // for the scans of table `t` (n points in all, in scan order): clip,
 // quantise, sort rays into the DDA order.
@@ -605,7 +621,7 @@ int launch_prep(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t st
   }
   const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
   k_prep<<<blocks, 256, 0, s>>>(pts, nullptr, n, stride, t, rays, ray_scan, hist, m->d_status);
-  k_scan<<<1, 1024, 0, s>>>(hist, cursor, static_cast<uint32_t>(kBucketsPerScan * t.n), m->d_status);
+  launch_scan(hist, cursor, static_cast<uint32_t>(kBucketsPerScan * t.n), m->d_status, s);
   k_scatter<<<blocks, 256, 0, s>>>(rays, n, t, cursor, order);
   VDBG_CUDA(cudaGetLastError());
   VDBG_CUDA(cudaEventRecord(m->ev_prep, s));
@@ -1044,7 +1060,7 @@ int queue_step(vdbg_map* m, Channel& c, int64_t cap, int64_t stride, const ScanT
   const unsigned blocks = static_cast<unsigned>((cap + 255) / 256);
   k_prep<<<blocks, 256, 0, s>>>(nullptr, m->d_pts_ref, cap, stride, t, m->d_rays, m->d_ray_scan, m->d_hist,
                                 m->d_status);
-  k_scan<<<1, 1024, 0, s>>>(m->d_hist, m->d_cursor, static_cast<uint32_t>(kBucketsPerScan * t.n), m->d_status);
+  launch_scan(m->d_hist, m->d_cursor, static_cast<uint32_t>(kBucketsPerScan * t.n), m->d_status, s);
   k_scatter<<<blocks, 256, 0, s>>>(m->d_rays, cap, t, m->d_cursor, m->d_order);
   VDBG_CUDA(cudaEventRecordWithFlags(m->ev_prep, s, cudaEventRecordExternal));
   k_mark_hits<<<blocks, 256, 0, s>>>(m->d_rays, m->d_order, t, map_view(m), channel_view(c));
@@ -1384,7 +1400,10 @@ int create_impl(int n_maps, const double* resolutions, const vdbg_options* optio
   m->buckets = static_cast<uint32_t>(kBucketsPerScan) * static_cast<uint32_t>(n_maps);
   s          = dev_alloc(m, &m->d_hist, m->buckets);
   if (s != VDBG_OK) return fail(s);
-  s = dev_alloc(m, &m->d_cursor, m->buckets);
+  // (the multi-block scan keeps its tile sums after the cursors)
+  static_assert(static_cast<uint64_t>(kMaxMaps) * kBucketsPerScan <= static_cast<uint64_t>(kScanMaxTiles) * kScanTile,
+                "bucket scan tiles");
+  s = dev_alloc(m, &m->d_cursor, m->buckets + kScanMaxTiles);
   if (s != VDBG_OK) return fail(s);
   if (cudaMemsetAsync(m->d_hist, 0, m->buckets * sizeof(uint32_t), m->stream) != cudaSuccess)
     return fail(VDBG_ERR_CUDA);
@@ -1551,7 +1570,7 @@ int vdbg_destroy(vdbg_map* m)
   free_changes(m);
   dev_free(m, m->d_status, 1);
   dev_free(m, m->d_hist, m->buckets);
-  dev_free(m, m->d_cursor, m->buckets);
+  dev_free(m, m->d_cursor, m->buckets + kScanMaxTiles);
   dev_free(m, m->d_lo, m->conf.size());
   dev_free(m, m->d_geom, m->conf.size());
   dev_free(m, m->d_first, m->conf.size() + 1);
