@@ -939,14 +939,85 @@ __global__ void __launch_bounds__(256) k_mark_hits(const int4* __restrict__ rays
   atomicOr(c.upd + static_cast<size_t>(slot) * 16 + 8 + (off >> 6), 1ull << (off & 63));
 }
 
-// Persistent sweep over the touched leaves: 8 lanes per leaf, lane w owning
-// the z-plane w (voxel offsets 64w..64w+63, one word of each mask), so a warp
-// sweeps four leaves at once. A lane loads the float4 groups of its slab that
-// hold update bits (all loads issued before any use), applies the log-odds
-// rules, stores them back and clears its update words.
+// Persistent sweep over the touched leaves, in two stages per warp. Finding:
+// 8 lanes per leaf, lane w reading the update words of the z-plane w (voxel
+// offsets 64w..64w+63, one word of each mask) of four leaves at once; the
+// planes holding update bits go to the warp's queue in shared memory (most
+// planes of a touched leaf hold none). Applying: once 32 planes are queued,
+// each lane takes one, loads the float4 groups with update bits (all loads
+// issued before any use), applies the log-odds rules, stores them back and
+// clears the plane's update words; so every lane of the warp has a plane.
 // kPerMap: the pool holds a batch of maps, each leaf takes its map's log-odds
 // constants (else the one map's, kept in registers). kChanges: record the
 // change set (every touched word, and the leaves with a flip).
+struct SweepTask
+{
+  unsigned long long actw, hitw;  // visited-or-hit and hit bits of the plane
+  int slot;                       // leaf slot
+  int w;                          // plane
+};
+constexpr int kSweepQueue = 64;  // per-warp ring: up to 31 left over + 32 found
+
+template <bool kPerMap, bool kChanges>
+__device__ __forceinline__ unsigned long long sweep_plane(const SweepTask& k, ChannelView& c, float* values,
+                                                          unsigned long long* active, const int4* origin,
+                                                          const LogOddsTable& lt, const ChangeView& ch)
+{
+  const unsigned long long actw = k.actw, hitw = k.hitw;
+  const int slot = k.slot, w = k.w;
+  const LogOdds lo               = kPerMap ? lt.table[origin[slot].w] : lt.lo0;
+  unsigned long long* aw         = active + static_cast<size_t>(slot) * 8 + w;
+  const unsigned long long on_in = *aw;
+  unsigned long long on          = on_in;
+  float4* vp = reinterpret_cast<float4*>(values + static_cast<size_t>(slot) * 512 + w * 64);
+#pragma unroll
+  for (int half = 0; half < 2; ++half)
+  {
+    float4 v[8];
+#pragma unroll
+    for (int k4 = 0; k4 < 8; ++k4)
+    {
+      const int qd = half * 8 + k4;
+      if ((actw >> (4 * qd)) & 0xfull) v[k4] = vp[qd];
+    }
+#pragma unroll
+    for (int k4 = 0; k4 < 8; ++k4)
+    {
+      const int qd      = half * 8 + k4;
+      const uint32_t a4 = static_cast<uint32_t>(actw >> (4 * qd)) & 0xfu;
+      if (!a4) continue;
+      const uint32_t h4 = static_cast<uint32_t>(hitw >> (4 * qd)) & 0xfu;
+      float vv[4]       = {v[k4].x, v[k4].y, v[k4].z, v[k4].w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+      {
+        if ((a4 >> j) & 1u)
+        {
+          const int bit = 4 * qd + j;
+          bool o        = (on >> bit) & 1ull;
+          apply_update(vv[j], o, (h4 >> j) & 1u, lo);
+          on = o ? (on | (1ull << bit)) : (on & ~(1ull << bit));
+        }
+      }
+      vp[qd] = make_float4(vv[0], vv[1], vv[2], vv[3]);
+    }
+  }
+  if (on != on_in) *aw = on;
+  unsigned long long* u = c.upd + static_cast<size_t>(slot) * 16;
+  u[w]                  = 0ull;
+  if (hitw) u[8 + w] = 0ull;
+  if (kChanges)
+  {
+    // A hit only turns voxels on and a miss only off, so the flipped bits
+    // that are now on are the hits of VDBMapping.hpp:768-772.
+    const unsigned long long flip                   = on ^ on_in;
+    ch.words[static_cast<size_t>(slot) * 16 + w]     = flip;
+    ch.words[static_cast<size_t>(slot) * 16 + 8 + w] = flip & on;
+    if (flip && atomicExch(ch.epoch + slot, ch.cur) != ch.cur) ch.list[atomicAdd(ch.count, 1u)] = slot;
+  }
+  return static_cast<unsigned long long>(__popcll(actw));
+}
+
 template <bool kPerMap, bool kChanges>
 __global__ void __launch_bounds__(256, 4) k_sweep(ChannelView c, float* __restrict__ values,
                                                   unsigned long long* __restrict__ active,
@@ -954,84 +1025,65 @@ __global__ void __launch_bounds__(256, 4) k_sweep(ChannelView c, float* __restri
                                                   LogOddsTable lt, ChangeView ch, DevStatus* st, int gated)
 {
   if (gated ? !marking_complete(st) : ld_relaxed_u32(&st->error) != 0u) return;
+  __shared__ SweepTask queue[8][kSweepQueue];
+  SweepTask* q        = queue[threadIdx.x >> 5];
   const uint32_t nt   = *c.n_touched;
   const int lane      = static_cast<int>(threadIdx.x & 31);
+  const uint32_t lt_m = lanemask_lt();
   const int w         = lane & 7;
   const uint32_t grp  = static_cast<uint32_t>(lane >> 3);
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nw   = (gridDim.x * blockDim.x) >> 5;
   unsigned long long n_upd = 0;
-  for (uint32_t base = warp * 4; base < nt; base += nw * 4)
+  uint32_t head = 0, tail = 0;  // queued planes: [head, tail) modulo kSweepQueue
+  for (uint32_t base = warp * 4;; base += nw * 4)
   {
-    const uint32_t i = base + grp;
-    if (i >= nt) continue;
-    const int slot                 = c.touched[i];
-    // Mark the leaf as part of the map the first time it is swept (every
-    // touched leaf carries at least one update bit).
-    if (w == 0 && ld_ca_u32(flags + slot) == 0u) flags[slot] = 1u;
-    unsigned long long* u          = c.upd + static_cast<size_t>(slot) * 16;
-    const int mp                   = kPerMap ? origin[slot].w : 0;  // loaded beside the masks
-    const unsigned long long hitw  = u[8 + w];
-    const unsigned long long actw  = u[w] | hitw;
-    if (actw == 0ull)
+    const bool more = base < nt;  // warp-uniform
+    if (more)
     {
-      if (kChanges)
+      const uint32_t i             = base + grp;
+      unsigned long long actw      = 0ull, hitw = 0ull;
+      int slot                     = 0;
+      if (i < nt)
       {
-        ch.words[static_cast<size_t>(slot) * 16 + w]     = 0ull;
-        ch.words[static_cast<size_t>(slot) * 16 + 8 + w] = 0ull;
-      }
-      continue;
-    }
-    const LogOdds lo               = kPerMap ? lt.table[mp] : lt.lo0;
-    unsigned long long* aw         = active + static_cast<size_t>(slot) * 8 + w;
-    const unsigned long long on_in = *aw;
-    unsigned long long on          = on_in;
-    float4* vp = reinterpret_cast<float4*>(values + static_cast<size_t>(slot) * 512 + w * 64);
-#pragma unroll
-    for (int half = 0; half < 2; ++half)
-    {
-      float4 v[8];
-#pragma unroll
-      for (int k = 0; k < 8; ++k)
-      {
-        const int qd = half * 8 + k;
-        if ((actw >> (4 * qd)) & 0xfull) v[k] = vp[qd];
-      }
-#pragma unroll
-      for (int k = 0; k < 8; ++k)
-      {
-        const int qd           = half * 8 + k;
-        const uint32_t a4      = static_cast<uint32_t>(actw >> (4 * qd)) & 0xfu;
-        if (!a4) continue;
-        const uint32_t h4      = static_cast<uint32_t>(hitw >> (4 * qd)) & 0xfu;
-        float vv[4]            = {v[k].x, v[k].y, v[k].z, v[k].w};
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
+        slot = c.touched[i];
+        // Mark the leaf as part of the map the first time it is swept (every
+        // touched leaf carries at least one update bit).
+        if (w == 0 && ld_ca_u32(flags + slot) == 0u) flags[slot] = 1u;
+        const unsigned long long* u = c.upd + static_cast<size_t>(slot) * 16;
+        hitw                        = u[8 + w];
+        actw                        = u[w] | hitw;
+        if (kChanges && actw == 0ull)
         {
-          if ((a4 >> j) & 1u)
-          {
-            const int bit = 4 * qd + j;
-            bool o        = (on >> bit) & 1ull;
-            apply_update(vv[j], o, (h4 >> j) & 1u, lo);
-            on = o ? (on | (1ull << bit)) : (on & ~(1ull << bit));
-          }
+          ch.words[static_cast<size_t>(slot) * 16 + w]     = 0ull;
+          ch.words[static_cast<size_t>(slot) * 16 + 8 + w] = 0ull;
         }
-        vp[qd] = make_float4(vv[0], vv[1], vv[2], vv[3]);
       }
+      const bool act    = actw != 0ull;
+      const unsigned am = __ballot_sync(0xffffffffu, act);
+      if (act)
+      {
+        SweepTask& k = q[(tail + static_cast<uint32_t>(__popc(am & lt_m))) % kSweepQueue];
+        k.actw       = actw;
+        k.hitw       = hitw;
+        k.slot       = slot;
+        k.w          = w;
+      }
+      tail += static_cast<uint32_t>(__popc(am));
+      __syncwarp();
     }
-    if (on != on_in) *aw = on;
-    u[w] = 0ull;
-    if (hitw) u[8 + w] = 0ull;
-    n_upd += static_cast<unsigned long long>(__popcll(actw));
-    if (kChanges)
+    while (tail - head >= 32u || (!more && tail != head))
     {
-      // A hit only turns voxels on and a miss only off, so the flipped bits
-      // that are now on are the hits of VDBMapping.hpp:768-772.
-      const unsigned long long flip                   = on ^ on_in;
-      ch.words[static_cast<size_t>(slot) * 16 + w]     = flip;
-      ch.words[static_cast<size_t>(slot) * 16 + 8 + w] = flip & on;
-      if (flip && atomicExch(ch.epoch + slot, ch.cur) != ch.cur) ch.list[atomicAdd(ch.count, 1u)] = slot;
+      const uint32_t n = min(32u, tail - head);
+      if (static_cast<uint32_t>(lane) < n)
+      {
+        const SweepTask k = q[(head + static_cast<uint32_t>(lane)) % kSweepQueue];
+        n_upd += sweep_plane<kPerMap, kChanges>(k, c, values, active, origin, lt, ch);
+      }
+      head += n;
+      __syncwarp();
     }
+    if (!more) break;
   }
   for (int off = 16; off > 0; off >>= 1) n_upd += __shfl_xor_sync(0xffffffffu, n_upd, off);
   if (lane == 0 && n_upd) atomicAdd(&st->updates, n_upd);
