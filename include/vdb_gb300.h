@@ -246,6 +246,39 @@ int vdbg_batch_set_config(vdbg_map* batch, int map, const vdbg_config* config);
 int vdbg_batch_insert(vdbg_map* batch, const float* xyz, const int64_t* counts, int64_t stride_bytes,
                       const double* origins, uint32_t flags, void* stream, vdbg_scan_stats* stats);
 
+/* Map sections. `map` is -1 (or 0) for a single-map handle, the map's index
+ * for a batch. Boxes are index boxes [lo, hi], inclusive: the reference
+ * builds them with createIndexBoundingBox (VDBMapping.hpp:858-870) from a world
+ * box and a transform; the C++ drop-in and the Python package provide that
+ * step. Leaves are in vdbg_export_leaves' layout, sorted by origin.
+ *
+ * getMapSectionGrid / getMapSectionUpdateGrid (VDBMapping.hpp:883-962): the
+ * map's leaves overlapping the box, restricted to the voxels inside it.
+ * full != 0 keeps each inside voxel's value and state (extractFullLeaf,
+ * :972-990). full == 0 gives the active inside voxels value 1 (extractSparseLeaf,
+ * :1001-1012; an update grid reads the values as bool). The others are the
+ * background 0, inactive. A leaf is returned only if a write created it: it
+ * holds an active inside voxel or, full, an inside value other than 0. */
+int vdbg_export_section(vdbg_map* map, int map_index, const int32_t lo[3], const int32_t hi[3], int full,
+                        int64_t capacity, int32_t* origins, float* values, uint64_t* masks, int64_t* n_out);
+
+/* applyMapSectionUpdateGrid without smoothing (VDBMapping.hpp:1058-1085): every
+ * active map voxel inside [lo, hi] (the section's bb_min/bb_max) is set
+ * inactive, then every active voxel of the n section leaves is set active.
+ * Values are kept, and a new leaf starts at 0. */
+int vdbg_apply_section_states(vdbg_map* map, int map_index, const int32_t lo[3], const int32_t hi[3], int64_t n,
+                              const int32_t* origins, const uint64_t* masks);
+
+/* applyMapSectionGrid without smoothing (VDBMapping.hpp:1022-1048). Each
+ * section leaf's 512 values and states overwrite the map leaf, which is
+ * created unless every voxel is inactive 0. The section tree's tiles, the
+ * empty slots of its 128^3 and 4096^3 internal nodes, set the map voxel at
+ * their origin to inactive 0 where a map leaf holds it, as the reference's
+ * cbeginValueAll() does. Smoothing (morphologicalCloseMap, :1095-1100) is not
+ * provided. */
+int vdbg_apply_section_values(vdbg_map* map, int map_index, int64_t n, const int32_t* origins, const float* values,
+                              const uint64_t* masks);
+
 /* CUDA-graph replay of vdbg_batch_insert (batches of two or more maps; on by
  * default). The step is captured once per buffer layout and replayed as one
  * graph launch: prep, endpoint hits, the first DDA pass with its apply,

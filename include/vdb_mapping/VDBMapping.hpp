@@ -16,14 +16,18 @@
 //     openvdb::FloatGrid refreshed on each getGrid() call;
 //   * only the occupancy data type (float log-odds) is implemented, which is
 //     the only specialisation the reference ships (OccupancyVDBMapping.hpp).
-// Parts of the reference outside the insertion path (sections, morphology,
-// artificial areas, file I/O, ray queries, fast mode) are not provided.
+// Map sections are provided (getMapSection*, applyMapSection*, the
+// bounding-box helpers; VDBMapping.hpp:811-1085) without the morphological
+// smoothing option. Other parts of the reference outside the insertion path
+// (morphology, artificial areas, file I/O, ray queries, fast mode) are not.
 #ifndef VDB_MAPPING_GB300_VDB_MAPPING_HPP
 #define VDB_MAPPING_GB300_VDB_MAPPING_HPP
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <iostream>
+#include <limits>
 #include <map>
 #include <tuple>
 #include <memory>
@@ -80,6 +84,15 @@ public:
   Scalar& y() { return m[1]; }
   Scalar& z() { return m[2]; }
   Scalar operator()(int i) const { return m[i]; }
+  // Element (r, c), column-major like Eigen's default storage.
+  Scalar operator()(int r, int c) const { return m[c * Rows + r]; }
+  Scalar& operator()(int r, int c) { return m[c * Rows + r]; }
+  static Matrix Identity()
+  {
+    Matrix e;
+    for (int i = 0; i < Rows && i < Cols; ++i) e(i, i) = Scalar(1);
+    return e;
+  }
 
 private:
   Scalar m[Rows * Cols];
@@ -123,6 +136,29 @@ private:
 };
 } // namespace math
 using Vec3d = math::Vec3<double>;
+// Axis-aligned boxes (openvdb::BBoxd, openvdb::CoordBBox), inclusive.
+struct BBoxd
+{
+  Vec3d mMin, mMax;
+  BBoxd() = default;
+  BBoxd(const Vec3d& lo, const Vec3d& hi) : mMin(lo), mMax(hi) {}
+  const Vec3d& min() const { return mMin; }
+  const Vec3d& max() const { return mMax; }
+};
+struct CoordBBox
+{
+  Coord mMin, mMax;
+  CoordBBox() = default;
+  CoordBBox(const Coord& lo, const Coord& hi) : mMin(lo), mMax(hi) {}
+  const Coord& min() const { return mMin; }
+  const Coord& max() const { return mMax; }
+  bool isInside(const Coord& c) const
+  {
+    for (int a = 0; a < 3; ++a)
+      if (c[a] < mMin[a] || c[a] > mMax[a]) return false;
+    return true;
+  }
+};
 } // namespace openvdb
 #endif
 
@@ -215,6 +251,18 @@ public:
   using ValueType = TData;
 
   explicit LeafGrid(std::shared_ptr<detail::DeviceMap> dev) : m_dev(std::move(dev)) {}
+  /*! A detached grid holding `table` (map sections), with its bb_min / bb_max. */
+  LeafGrid(detail::LeafTable table, const openvdb::Vec3d& bb_min, const openvdb::Vec3d& bb_max)
+    : m_table(std::move(table)), m_bb_min(bb_min), m_bb_max(bb_max)
+  {
+    m_version = 0;
+  }
+  /*! Metadata of a section grid: "bb_min" and "bb_max" (getMapSection, VDBMapping.hpp:957-960). */
+  template <typename T>
+  T metaValue(const std::string& name) const
+  {
+    return name == "bb_min" ? m_bb_min : m_bb_max;
+  }
 
   class Accessor
   {
@@ -286,6 +334,7 @@ private:
   std::shared_ptr<detail::DeviceMap> m_dev;
   mutable detail::LeafTable m_table;
   mutable uint64_t m_version = ~0ull;
+  openvdb::Vec3d m_bb_min, m_bb_max;
 };
 #endif
 
@@ -338,6 +387,27 @@ public:
     }
   }
 
+  /*! Metadata of a section grid: "bb_min" and "bb_max". */
+  template <typename T>
+  T metaValue(const std::string& name) const
+  {
+    return name == "bb_min" ? m_bb_min : m_bb_max;
+  }
+  void setBox(const openvdb::Vec3d& bb_min, const openvdb::Vec3d& bb_max)
+  {
+    m_bb_min = bb_min;
+    m_bb_max = bb_max;
+  }
+  /*! Leaf origins [n][3] and active masks [n][8] (OpenVDB order) of a section or change grid. */
+  const std::vector<int32_t>& leafOrigins() const { return m_change_origins; }
+  std::vector<uint64_t> activeMasks() const
+  {
+    std::vector<uint64_t> out(m_change_origins.size() / 3 * 8);
+    for (size_t i = 0; i < out.size() / 8; ++i)
+      for (int w = 0; w < 8; ++w) out[i * 8 + w] = m_change_words[i * 16 + w];
+    return out;
+  }
+
   // Internal: the hidden source id of this grid inside `map`.
   const std::string& bind(vdbg_map* map)
   {
@@ -364,6 +434,7 @@ private:
   }
   vdbg_map* m_map = nullptr;
   std::string m_id;
+  openvdb::Vec3d m_bb_min, m_bb_max;
   std::vector<int32_t> m_change_origins;
   std::vector<uint64_t> m_change_words;
   std::map<std::tuple<int32_t, int32_t, int32_t>, size_t> m_change_index;
@@ -534,6 +605,118 @@ public:
     return m_vdb_grid;
   }
 
+  /*! VDBMapping.hpp:811-847: the eight corners of the box as float points,
+   * transformed by `map_to_reference_tf` (each coordinate in double as
+   * row . (x, y, z, 1), stored as float, as pcl::transformPointCloud does with
+   * a double matrix), and their float min/max. */
+  openvdb::BBoxd createWorldBoundingBox(const Eigen::Matrix<double, 3, 1>& min_boundary,
+                                        const Eigen::Matrix<double, 3, 1>& max_boundary,
+                                        const Eigen::Matrix<double, 4, 4>& map_to_reference_tf) const
+  {
+    const double xs[2] = {min_boundary.x(), max_boundary.x()};
+    const double ys[2] = {min_boundary.y(), max_boundary.y()};
+    const double zs[2] = {min_boundary.z(), max_boundary.z()};
+    float lo[3] = {std::numeric_limits<float>::max(), std::numeric_limits<float>::max(),
+                   std::numeric_limits<float>::max()};
+    float hi[3] = {-std::numeric_limits<float>::max(), -std::numeric_limits<float>::max(),
+                   -std::numeric_limits<float>::max()};
+    for (int i = 0; i < 8; ++i)
+    {
+      const float p[3] = {static_cast<float>(xs[i >> 2]), static_cast<float>(ys[(i >> 1) & 1]),
+                          static_cast<float>(zs[i & 1])};
+      for (int r = 0; r < 3; ++r)
+      {
+        double acc = map_to_reference_tf(r, 0) * p[0];
+        acc        = acc + map_to_reference_tf(r, 1) * p[1];
+        acc        = acc + map_to_reference_tf(r, 2) * p[2];
+        acc        = acc + map_to_reference_tf(r, 3);
+        const float q = static_cast<float>(acc);
+        lo[r]         = std::min(lo[r], q);
+        hi[r]         = std::max(hi[r], q);
+      }
+    }
+    return openvdb::BBoxd(openvdb::Vec3d(lo[0], lo[1], lo[2]), openvdb::Vec3d(hi[0], hi[1], hi[2]));
+  }
+
+  /*! VDBMapping.hpp:858-870: the world box in index coordinates (w * 1/res), floored. */
+  openvdb::CoordBBox createIndexBoundingBox(const Eigen::Matrix<double, 3, 1>& min_boundary,
+                                            const Eigen::Matrix<double, 3, 1>& max_boundary,
+                                            const Eigen::Matrix<double, 4, 4>& map_to_reference_tf) const
+  {
+    const openvdb::BBoxd w = createWorldBoundingBox(min_boundary, max_boundary, map_to_reference_tf);
+    const double inv       = 1.0 / m_resolution;
+    return openvdb::CoordBBox(openvdb::Coord(static_cast<int32_t>(std::floor(w.min().x() * inv)),
+                                             static_cast<int32_t>(std::floor(w.min().y() * inv)),
+                                             static_cast<int32_t>(std::floor(w.min().z() * inv))),
+                              openvdb::Coord(static_cast<int32_t>(std::floor(w.max().x() * inv)),
+                                             static_cast<int32_t>(std::floor(w.max().y() * inv)),
+                                             static_cast<int32_t>(std::floor(w.max().z() * inv))));
+  }
+
+  /*! VDBMapping.hpp:883-891: the section as an update grid (active voxels;
+   * values read as bool), with bb_min / bb_max. */
+  typename UpdateGridT::Ptr getMapSectionUpdateGrid(const Eigen::Matrix<double, 3, 1>& min_boundary,
+                                                    const Eigen::Matrix<double, 3, 1>& max_boundary,
+                                                    const Eigen::Matrix<double, 4, 4>& map_to_reference_tf,
+                                                    const bool full_grid = false) const
+  {
+    const openvdb::CoordBBox box = createIndexBoundingBox(min_boundary, max_boundary, map_to_reference_tf);
+    detail::LeafTable t          = exportSection(box, full_grid);
+    const size_t n               = t.origins.size() / 3;
+    std::vector<uint64_t> value_bits(n * 8, 0);
+    for (size_t i = 0; i < n; ++i)
+      for (uint32_t off = 0; off < 512; ++off)
+        if (t.values[i * 512 + off] != 0.0f) value_bits[i * 8 + (off >> 6)] |= 1ull << (off & 63);
+    auto g = UpdateGridT::create(false);
+    g->setChanges(std::move(t.origins), t.masks, value_bits);
+    g->setBox(boxCorner(box.min()), boxCorner(box.max()));
+    return g;
+  }
+
+  /*! VDBMapping.hpp:1058-1085 without smoothing. */
+  void applyMapSectionUpdateGrid(const typename UpdateGridT::Ptr section, bool smooth_map = false,
+                                 int /*smoothing_iterations*/ = 2)
+  {
+    if (smooth_map) throw std::runtime_error("applyMapSectionUpdateGrid: smoothing is not provided");
+    const openvdb::Vec3d bmin = section->template metaValue<openvdb::Vec3d>("bb_min");
+    const openvdb::Vec3d bmax = section->template metaValue<openvdb::Vec3d>("bb_max");
+    const int32_t lo[3] = {static_cast<int32_t>(std::floor(bmin.x())), static_cast<int32_t>(std::floor(bmin.y())),
+                           static_cast<int32_t>(std::floor(bmin.z()))};
+    const int32_t hi[3] = {static_cast<int32_t>(std::floor(bmax.x())), static_cast<int32_t>(std::floor(bmax.y())),
+                           static_cast<int32_t>(std::floor(bmax.z()))};
+    const std::vector<int32_t>& o = section->leafOrigins();
+    const std::vector<uint64_t> m = section->activeMasks();
+    std::unique_lock map_lock(*m_map_mutex);
+    check(vdbg_apply_section_states(m_dev->map, -1, lo, hi, static_cast<int64_t>(o.size() / 3), o.data(), m.data()),
+          "vdbg_apply_section_states");
+    ++m_dev->version;
+  }
+
+#if !defined(VDBG_WITH_OPENVDB)
+  /*! VDBMapping.hpp:902-910: the section as a (detached) grid with bb_min / bb_max. */
+  typename GridT::Ptr getMapSectionGrid(const Eigen::Matrix<double, 3, 1>& min_boundary,
+                                        const Eigen::Matrix<double, 3, 1>& max_boundary,
+                                        const Eigen::Matrix<double, 4, 4>& map_to_reference_tf,
+                                        const bool full_grid = false) const
+  {
+    const openvdb::CoordBBox box = createIndexBoundingBox(min_boundary, max_boundary, map_to_reference_tf);
+    return std::make_shared<GridT>(exportSection(box, full_grid), boxCorner(box.min()), boxCorner(box.max()));
+  }
+
+  /*! VDBMapping.hpp:1022-1048 without smoothing (the section tree's tiles included). */
+  void applyMapSectionGrid(const typename GridT::Ptr section, bool smooth_map = false,
+                           int /*smoothing_iterations*/ = 2)
+  {
+    if (smooth_map) throw std::runtime_error("applyMapSectionGrid: smoothing is not provided");
+    const detail::LeafTable& t = section->leaves();
+    std::unique_lock map_lock(*m_map_mutex);
+    check(vdbg_apply_section_values(m_dev->map, -1, static_cast<int64_t>(t.origins.size() / 3), t.origins.data(),
+                                    t.values.data(), t.masks.data()),
+          "vdbg_apply_section_values");
+    ++m_dev->version;
+  }
+#endif
+
   /*! VDBMapping.hpp:1343. */
   std::shared_ptr<std::shared_mutex> getMapMutex() { return m_map_mutex; }
 
@@ -556,6 +739,42 @@ protected:
   static void check(int s, const char* where)
   {
     if (s != VDBG_OK) detail::throw_status(s, where);
+  }
+  static openvdb::Vec3d boxCorner(const openvdb::Coord& c)
+  {
+    return openvdb::Vec3d(static_cast<double>(c.x()), static_cast<double>(c.y()), static_cast<double>(c.z()));
+  }
+  // The map's section over `box` (vdbg_export_section), as a leaf table.
+  detail::LeafTable exportSection(const openvdb::CoordBBox& box, bool full) const
+  {
+    const int32_t lo[3] = {box.min().x(), box.min().y(), box.min().z()};
+    const int32_t hi[3] = {box.max().x(), box.max().y(), box.max().z()};
+    std::shared_lock map_lock(*m_map_mutex);
+    detail::LeafTable t;
+    int64_t n = 0;
+    for (;;)
+    {
+      t.origins.assign(static_cast<size_t>(n) * 3, 0);
+      t.values.assign(static_cast<size_t>(n) * 512, 0.f);
+      t.masks.assign(static_cast<size_t>(n) * 8, 0);
+      int64_t got = 0;
+      const int s = vdbg_export_section(m_dev->map, -1, lo, hi, full ? 1 : 0, n, t.origins.data(), t.values.data(),
+                                        t.masks.data(), &got);
+      if (s == VDBG_ERR_BUFFER_TOO_SMALL)
+      {
+        n = got;
+        continue;
+      }
+      check(s, "vdbg_export_section");
+      n = got;
+      break;
+    }
+    t.origins.resize(static_cast<size_t>(n) * 3);
+    t.values.resize(static_cast<size_t>(n) * 512);
+    t.masks.resize(static_cast<size_t>(n) * 8);
+    for (size_t i = 0; i < static_cast<size_t>(n); ++i)
+      t.index.emplace(std::make_tuple(t.origins[3 * i], t.origins[3 * i + 1], t.origins[3 * i + 2]), i);
+    return t;
   }
   static const float* pointsOf(const typename PointCloudT::ConstPtr& cloud)
   {

@@ -46,6 +46,9 @@ def load():
         "vo_clip_quantise": (None, [P, I64, I64, C.POINTER(D), D, D, P]),
         "vo_clip_quantise_variant": (None, [P, I64, I64, C.POINTER(D), D, D, C.c_int, C.c_int, P]),
         "vo_bench_replicas": (D, [D, C.POINTER(D), P, I64, I64, I64, C.POINTER(D), C.c_int, U64P]),
+        "vo_section": (I64, [P, P, P, C.c_int, I64, P, P, P]),
+        "vo_apply_section_states": (None, [P, P, P, I64, P, P]),
+        "vo_apply_section_values": (None, [P, I64, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -135,6 +138,33 @@ class OracleMap:
         value = np.zeros((n, 8), np.uint64)
         self._l.vo_export_changes(self._h, origins.ctypes.data, active.ctypes.data, value.ctypes.data)
         return origins, active, value
+
+    def getMapSection(self, lo, hi, full=False):
+        """getMapSection over the index box [lo, hi]: (origins, values, masks) sorted by origin."""
+        lo = np.ascontiguousarray(lo, np.int32)
+        hi = np.ascontiguousarray(hi, np.int32)
+        n = self._l.vo_section(self._h, lo.ctypes.data, hi.ctypes.data, 1 if full else 0, 0, None, None, None)
+        origins = np.zeros((n, 3), np.int32)
+        values = np.zeros((n, 512), np.float32)
+        masks = np.zeros((n, 8), np.uint64)
+        self._l.vo_section(self._h, lo.ctypes.data, hi.ctypes.data, 1 if full else 0, n, origins.ctypes.data,
+                           values.ctypes.data, masks.ctypes.data)
+        return origins, values, masks
+
+    def applyMapSectionStates(self, lo, hi, origins, masks):
+        """applyMapSectionUpdateGrid over the index box [lo, hi]."""
+        lo = np.ascontiguousarray(lo, np.int32)
+        hi = np.ascontiguousarray(hi, np.int32)
+        o = np.ascontiguousarray(origins, np.int32)
+        mk = np.ascontiguousarray(masks, np.uint64)
+        self._l.vo_apply_section_states(self._h, lo.ctypes.data, hi.ctypes.data, len(o), o.ctypes.data, mk.ctypes.data)
+
+    def applyMapSectionValues(self, origins, values, masks):
+        """applyMapSectionGrid."""
+        o = np.ascontiguousarray(origins, np.int32)
+        v = np.ascontiguousarray(values, np.float32)
+        mk = np.ascontiguousarray(masks, np.uint64)
+        self._l.vo_apply_section_values(self._h, len(o), o.ctypes.data, v.ctypes.data, mk.ctypes.data)
 
     def getValue(self, xyz) -> float:
         return self._l.vo_get_value(self._h, *[int(c) for c in xyz])

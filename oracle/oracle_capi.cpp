@@ -133,6 +133,53 @@ void vo_export(void* h, int32_t* origins, float* values, uint64_t* masks)
   }
 }
 
+// getMapSection: leaves sorted by origin (OpenVDB order), returns the count;
+// writes at most `cap` leaves.
+int64_t vo_section(void* h, const int32_t* lo, const int32_t* hi, int full, int64_t cap, int32_t* origins,
+                   float* values, uint64_t* masks)
+{
+  const auto sec = static_cast<Handle*>(h)->map.get_map_section(Coord(lo[0], lo[1], lo[2]),
+                                                                Coord(hi[0], hi[1], hi[2]), full != 0);
+  for (size_t i = 0; i < sec.size() && static_cast<int64_t>(i) < cap; ++i)
+  {
+    origins[3 * i + 0] = sec[i].origin.x;
+    origins[3 * i + 1] = sec[i].origin.y;
+    origins[3 * i + 2] = sec[i].origin.z;
+    std::memcpy(values + 512 * i, sec[i].value, 512 * sizeof(float));
+    std::memcpy(masks + 8 * i, sec[i].on, 8 * sizeof(uint64_t));
+  }
+  return static_cast<int64_t>(sec.size());
+}
+
+static std::vector<MapLeaf> section_leaves(int64_t n, const int32_t* origins, const float* values,
+                                           const uint64_t* masks)
+{
+  std::vector<MapLeaf> sec(static_cast<size_t>(n));
+  for (int64_t i = 0; i < n; ++i)
+  {
+    sec[i].origin = Coord(origins[3 * i], origins[3 * i + 1], origins[3 * i + 2]);
+    if (values)
+      std::memcpy(sec[i].value, values + 512 * i, 512 * sizeof(float));
+    else
+      std::fill(sec[i].value, sec[i].value + 512, 0.0f);
+    std::memcpy(sec[i].on, masks + 8 * i, 8 * sizeof(uint64_t));
+  }
+  return sec;
+}
+
+void vo_apply_section_states(void* h, const int32_t* lo, const int32_t* hi, int64_t n, const int32_t* origins,
+                             const uint64_t* masks)
+{
+  static_cast<Handle*>(h)->map.apply_section_states(Coord(lo[0], lo[1], lo[2]), Coord(hi[0], hi[1], hi[2]),
+                                                    section_leaves(n, origins, nullptr, masks));
+}
+
+void vo_apply_section_values(void* h, int64_t n, const int32_t* origins, const float* values,
+                             const uint64_t* masks)
+{
+  static_cast<Handle*>(h)->map.apply_section_values(section_leaves(n, origins, values, masks));
+}
+
 float vo_get_value(void* h, int32_t x, int32_t y, int32_t z)
 {
   return static_cast<Handle*>(h)->map.map().get_value(Coord(x, y, z));

@@ -44,6 +44,7 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <set>
 #include <vector>
 
 namespace vdb_oracle {
@@ -435,6 +436,13 @@ public:
       for (int w = 0; w < 8; ++w) n += static_cast<size_t>(__builtin_popcountll(l->on[w]));
     return n;
   }
+  // Existing leaf with origin `o`, or nullptr.
+  MapLeaf* find_leaf(const Coord& o)
+  {
+    uint32_t idx;
+    return m_index.find(o, idx) ? m_leaves[idx].get() : nullptr;
+  }
+  const std::vector<std::unique_ptr<MapLeaf> >& leaves() const { return m_leaves; }
   // Leaves sorted by origin (x, then y, then z).
   std::vector<const MapLeaf*> sorted_leaves() const
   {
@@ -677,6 +685,126 @@ public:
   }
 
   void set_artificial(const std::vector<Coord>& voxels) { m_artificial = voxels; }
+
+  // getMapSection (VDBMapping.hpp:922-962): the leaves overlapping the index
+  // box [lo, hi] (inclusive, CoordBBox::hasOverlap), restricted to the voxels
+  // inside it. `full` (extractFullLeaf, :972-990) copies every inside voxel
+  // with its value and state; otherwise (extractSparseLeaf, :1001-1012) the
+  // active inside voxels are set on with value true (1.0f). A result leaf
+  // exists only where a write created it: setValueOn always does, setValueOff
+  // only with a value other than the background 0.0f. Sorted by origin.
+  std::vector<MapLeaf> get_map_section(const Coord& lo, const Coord& hi, bool full) const
+  {
+    std::vector<MapLeaf> out;
+    for (const MapLeaf* l : m_map.sorted_leaves())
+    {
+      const Coord& o = l->origin;
+      if (o.x > hi.x || o.x + 7 < lo.x || o.y > hi.y || o.y + 7 < lo.y || o.z > hi.z || o.z + 7 < lo.z) continue;
+      MapLeaf r;
+      r.origin = o;
+      std::fill(r.value, r.value + 512, 0.0f);
+      std::memset(r.on, 0, sizeof(r.on));
+      bool created = false;
+      for (uint32_t off = 0; off < 512; ++off)
+      {
+        const Coord c(o.x + static_cast<int>(off >> 6), o.y + static_cast<int>((off >> 3) & 7),
+                      o.z + static_cast<int>(off & 7));
+        if (c.x < lo.x || c.x > hi.x || c.y < lo.y || c.y > hi.y || c.z < lo.z || c.z > hi.z) continue;
+        const bool on = (l->on[off >> 6] >> (off & 63)) & 1ull;
+        if (on) r.on[off >> 6] |= 1ull << (off & 63);
+        if (full)
+        {
+          r.value[off] = l->value[off];
+          if (on || l->value[off] != 0.0f) created = true;
+        }
+        else if (on)
+        {
+          r.value[off] = 1.0f;
+          created      = true;
+        }
+      }
+      if (created) out.push_back(r);
+    }
+    return out;
+  }
+
+  // applyMapSectionUpdateGrid without smoothing (VDBMapping.hpp:1058-1085):
+  // every active map voxel inside [lo, hi] is set inactive, then every
+  // active voxel of the section is set active (values kept; a new leaf
+  // starts at the background 0.0f).
+  void apply_section_states(const Coord& lo, const Coord& hi, const std::vector<MapLeaf>& section)
+  {
+    for (const auto& lp : m_map.leaves())
+    {
+      MapLeaf& l = *lp;
+      for (uint32_t off = 0; off < 512; ++off)
+      {
+        const Coord c(l.origin.x + static_cast<int>(off >> 6), l.origin.y + static_cast<int>((off >> 3) & 7),
+                      l.origin.z + static_cast<int>(off & 7));
+        if (c.x < lo.x || c.x > hi.x || c.y < lo.y || c.y > hi.y || c.z < lo.z || c.z > hi.z) continue;
+        l.on[off >> 6] &= ~(1ull << (off & 63));
+      }
+    }
+    for (const MapLeaf& sl : section)
+    {
+      for (int w = 0; w < 8; ++w)
+      {
+        if (!sl.on[w]) continue;
+        MapLeaf& l = m_map.touch(sl.origin);
+        l.on[w] |= sl.on[w];
+      }
+    }
+  }
+
+  // applyMapSectionGrid without smoothing (VDBMapping.hpp:1022-1048): the
+  // section's cbeginValueAll() visits every voxel of its leaves and every
+  // tile of its internal nodes, setting each on the map with the section's
+  // value and state. A leaf's 512 voxels overwrite the map leaf, which is
+  // created unless every voxel is inactive background (setValueOff with the
+  // background creates nothing). The tiles are the empty slots of the
+  // section tree's 16^3 (128^3-voxel) and 32^3 (4096^3-voxel) internal nodes:
+  // each sets the map voxel at its origin to the inactive background, which
+  // changes the map only where a map leaf holds that voxel.
+  void apply_section_values(const std::vector<MapLeaf>& section)
+  {
+    std::set<Coord> leaves, n1, n2;
+    for (const MapLeaf& sl : section)
+    {
+      leaves.insert(sl.origin);
+      n1.insert(Coord(sl.origin.x >> 7, sl.origin.y >> 7, sl.origin.z >> 7));
+      n2.insert(Coord(sl.origin.x >> 12, sl.origin.y >> 12, sl.origin.z >> 12));
+      bool any = false;
+      for (int w = 0; w < 8; ++w) any = any || sl.on[w] != 0;
+      for (int i = 0; i < 512 && !any; ++i) any = sl.value[i] != 0.0f;
+      MapLeaf* l = m_map.find_leaf(sl.origin);
+      if (!l && !any) continue;
+      if (!l) l = &m_map.touch(sl.origin);
+      std::memcpy(l->value, sl.value, sizeof(l->value));
+      std::memcpy(l->on, sl.on, sizeof(l->on));
+    }
+    auto clear_voxel = [&](const Coord& c) {
+      MapLeaf* l = m_map.find_leaf(c);  // c is a leaf origin (a multiple of 8)
+      if (!l) return;
+      l->value[0] = 0.0f;
+      l->on[0] &= ~1ull;
+    };
+    for (const Coord& k : n1)
+      for (int i = 0; i < 16; ++i)
+        for (int j = 0; j < 16; ++j)
+          for (int q = 0; q < 16; ++q)
+          {
+            const Coord c((k.x << 7) + 8 * i, (k.y << 7) + 8 * j, (k.z << 7) + 8 * q);
+            if (!leaves.count(c)) clear_voxel(c);
+          }
+    for (const Coord& k : n2)
+      for (int i = 0; i < 32; ++i)
+        for (int j = 0; j < 32; ++j)
+          for (int q = 0; q < 32; ++q)
+          {
+            const Coord c((k.x << 12) + 128 * i, (k.y << 12) + 128 * j, (k.z << 12) + 128 * q);
+            if (!n1.count(Coord(c.x >> 7, c.y >> 7, c.z >> 7))) clear_voxel(c);
+          }
+  }
 
   const FloatMap& map() const { return m_map; }
   float lo_hit() const { return m_lo_hit; }

@@ -152,6 +152,39 @@ TEST(DropIn, UpdateMapReturnsTheChangeGrid)
   EXPECT_FALSE(change3->getAccessor().getValue(openvdb::Coord(5, 0, 0)));
 }
 
+TEST(DropIn, MapSections)
+{
+  // getMapSection* over a world box (VDBMapping.hpp:883-962) and the two
+  // apply calls (:1022-1085) through the reference-style API.
+  OccupancyVDBMapping map(1.0);
+  map.setConfig(test_config(20));
+  map.addInputSource("lidar", 20, 0);
+  Eigen::Matrix<double, 3, 1> origin(0, 0, 0);
+  map.insertPointCloud(cloud_of({{12.f, 0.f, 0.f}, {0.f, 6.f, 0.f}}), origin, "lidar");
+  auto eye = Eigen::Matrix<double, 4, 4>::Identity();
+  Eigen::Matrix<double, 3, 1> lo(9.5, -0.5, -0.5), hi(12.5, 0.5, 0.5);
+  const openvdb::CoordBBox box = map.createIndexBoundingBox(lo, hi, eye);
+  EXPECT_EQ(box.min().x(), 9);
+  EXPECT_EQ(box.max().x(), 12);
+  auto full = map.getMapSectionGrid(lo, hi, eye, true);
+  EXPECT_EQ(full->getAccessor().getValue(openvdb::Coord(12, 0, 0)), logodds(0.9));
+  EXPECT_EQ(full->getAccessor().getValue(openvdb::Coord(10, 0, 0)), logodds(0.1));
+  EXPECT_EQ(full->getAccessor().getValue(openvdb::Coord(5, 0, 0)), 0.0f);  // outside the box
+  EXPECT_EQ(full->metaValue<openvdb::Vec3d>("bb_max").x(), 12.0);
+  auto states = map.getMapSectionUpdateGrid(lo, hi, eye, false);
+  EXPECT_TRUE(states->getAccessor().isValueOn(openvdb::Coord(12, 0, 0)));
+  EXPECT_FALSE(states->getAccessor().isValueOn(openvdb::Coord(10, 0, 0)));
+  // into a second map: the states make the voxel active there (value 0)
+  OccupancyVDBMapping other(1.0);
+  other.applyMapSectionUpdateGrid(states);
+  EXPECT_TRUE(other.getGrid()->getAccessor().isValueOn(openvdb::Coord(12, 0, 0)));
+  EXPECT_EQ(other.getGrid()->getAccessor().getValue(openvdb::Coord(12, 0, 0)), 0.0f);
+  // the full section brings the values
+  other.applyMapSectionGrid(full);
+  EXPECT_EQ(other.getGrid()->getAccessor().getValue(openvdb::Coord(11, 0, 0)), logodds(0.1));
+  EXPECT_EQ(other.getGrid()->getAccessor().getValue(openvdb::Coord(12, 0, 0)), logodds(0.9));
+}
+
 int main(int argc, char** argv)
 {
   ::testing::InitGoogleTest(&argc, argv);

@@ -73,7 +73,7 @@ def test_autotune_returns_a_candidate(vdbg):
     w = W.get("small")
     scans = [w.scan(k) for k in range(2)]
     small = {"rays_per_take": (8, 16), "apply_chunk_runs": (2048,), "length_edges": ((2048, 1024, 512),),
-             "hash_load": (0.5,), "dda_warps_per_sm": (16,)}
+             "hash_load": (0.5,), "dda_warps_per_sm": (autotune.DEFAULT["dda_warps_per_sm"],)}
     best, table = autotune.tune_map(w.resolution, w.config, scans, candidates=small,
                                     initial_leaf_capacity=1 << 18)
     assert best["rays_per_take"] in (8, 16)

@@ -1239,4 +1239,195 @@ __global__ void k_reset_failed_leaves(int* __restrict__ bleaf, size_t cells)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Map sections (VDBMapping.hpp:922-1085): the voxels of an index box taken
+// out of the map, and sections written back. Leaves are z-major here; the
+// host converts to and from OpenVDB's order.
+// ---------------------------------------------------------------------------
+
+// Slot of the existing leaf (lx, ly, lz) of map `map`, or -1 (no insertion;
+// nothing may insert concurrently).
+__device__ __forceinline__ int find_leaf(const MapView& m, int map, int lx, int ly, int lz)
+{
+  const unsigned long long bkey = pack_leaf_key(map, lx >> 3, ly >> 3, lz >> 3);
+  uint32_t h                    = static_cast<uint32_t>(mix64(bkey)) & m.bhmask;
+  for (uint32_t probe = 0; probe < kMaxProbes; ++probe)
+  {
+    const unsigned long long k = m.bkeys[h];
+    if (k == kEmptyKey) return -1;
+    if (k == bkey)
+    {
+      const int b = m.bslots[h];
+      if (b < 0) return -1;
+      const int s = m.bleaf[static_cast<size_t>(b) * 512 + (((lx & 7) << 6) | ((ly & 7) << 3) | (lz & 7))];
+      return s >= 0 ? s : -1;
+    }
+    h = (h + 1) & m.bhmask;
+  }
+  return -1;
+}
+
+// Bits of z-plane word `w` of the leaf at `o` whose voxels lie inside [lo, hi].
+__device__ __forceinline__ unsigned long long box_plane_mask(const int4& o, int w, int3 lo, int3 hi)
+{
+  const int z = o.z + w;
+  if (z < lo.z || z > hi.z) return 0ull;
+  const int x0 = max(lo.x - o.x, 0), x1 = min(hi.x - o.x, 7);
+  const int y0 = max(lo.y - o.y, 0), y1 = min(hi.y - o.y, 7);
+  if (x0 > x1 || y0 > y1) return 0ull;
+  const unsigned long long row = ((1ull << (x1 - x0 + 1)) - 1ull) << x0;
+  unsigned long long mask      = 0ull;
+  for (int y = y0; y <= y1; ++y) mask |= row << (8 * y);
+  return mask;
+}
+
+// Leaves of map `map` in the map (flags set) whose 8^3 box overlaps [lo, hi]
+// (CoordBBox::hasOverlap): their slots into list[*count].
+__global__ void k_section_leaves(const int4* __restrict__ origin, const uint32_t* __restrict__ flags, uint32_t n,
+                                 int map, int3 lo, int3 hi, uint32_t* __restrict__ list, uint32_t* count)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || flags[i] == 0u) return;
+  const int4 o = origin[i];
+  if (o.w != map) return;
+  if (o.x > hi.x || o.x + 7 < lo.x || o.y > hi.y || o.y + 7 < lo.y || o.z > hi.z || o.z + 7 < lo.z) return;
+  list[atomicAdd(count, 1u)] = i;
+}
+
+// getMapSection of the listed leaves, one warp per leaf: the voxels inside the
+// box keep their state and value (full, extractFullLeaf VDBMapping.hpp:972-990)
+// or value 1 where active (extractSparseLeaf :1001-1012), the others are
+// background; keep[j]: the result leaf exists (an inside voxel is active, or,
+// full, holds a value other than the background 0).
+__global__ void k_section_extract(const uint32_t* __restrict__ list, const uint32_t* count,
+                                  const int4* __restrict__ origin, const float* __restrict__ values,
+                                  const unsigned long long* __restrict__ active, int3 lo, int3 hi, int full,
+                                  int4* __restrict__ out_o, float* __restrict__ out_v,
+                                  unsigned long long* __restrict__ out_m, uint32_t* __restrict__ keep)
+{
+  const uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane   = static_cast<int>(threadIdx.x & 31);
+  if (j >= *count) return;
+  const uint32_t slot = list[j];
+  const int4 o        = origin[slot];
+  bool any            = false;
+  unsigned long long lo_bits = 0ull;
+  for (int k = 0; k < 16; ++k)
+  {
+    const int off                  = k * 32 + lane;  // z-major offset
+    const int w                    = off >> 6;
+    const unsigned long long inbox = box_plane_mask(o, w, lo, hi);
+    const bool inside              = (inbox >> (off & 63)) & 1ull;
+    const bool on                  = (active[static_cast<size_t>(slot) * 8 + w] >> (off & 63)) & 1ull;
+    const float v                  = values[static_cast<size_t>(slot) * 512 + off];
+    out_v[static_cast<size_t>(j) * 512 + off] = inside ? (full ? v : (on ? 1.0f : 0.0f)) : 0.0f;
+    any = any || (inside && (on || (full && v != 0.0f)));
+    const unsigned half = __ballot_sync(0xffffffffu, inside && on);
+    if ((k & 1) == 0)
+      lo_bits = half;
+    else if (lane == 0)
+      out_m[static_cast<size_t>(j) * 8 + w] = (static_cast<unsigned long long>(half) << 32) | lo_bits;
+  }
+  const bool kept = __any_sync(0xffffffffu, any);
+  if (lane == 0)
+  {
+    out_o[j] = o;
+    keep[j]  = kept ? 1u : 0u;
+  }
+}
+
+// applyMapSectionUpdateGrid, first loop (VDBMapping.hpp:1071-1077): the listed
+// leaves lose their active voxels inside the box. One thread per (leaf, plane).
+__global__ void k_section_clear(const uint32_t* __restrict__ list, const uint32_t* count,
+                                const int4* __restrict__ origin, unsigned long long* __restrict__ active, int3 lo,
+                                int3 hi)
+{
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= *count * 8u) return;
+  const uint32_t slot = list[t >> 3];
+  const int w         = static_cast<int>(t & 7u);
+  const unsigned long long inbox = box_plane_mask(origin[slot], w, lo, hi);
+  if (inbox) active[static_cast<size_t>(slot) * 8 + w] &= ~inbox;
+}
+
+// applyMapSectionUpdateGrid, second loop (:1078-1081): each section leaf's
+// active voxels are set active in the map, creating the leaf (values at the
+// background 0) where needed. One thread per section leaf.
+__global__ void k_section_set_states(MapView m, const int4* __restrict__ sec_o,
+                                     const unsigned long long* __restrict__ sec_m, uint32_t n, int map,
+                                     uint32_t* __restrict__ flags, unsigned long long* __restrict__ active)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned long long any = 0ull;
+  for (int w = 0; w < 8; ++w) any |= sec_m[static_cast<size_t>(i) * 8 + w];
+  if (!any) return;
+  const int4 o = sec_o[i];
+  const int lx = o.x >> 3, ly = o.y >> 3, lz = o.z >> 3;
+  const int b  = find_or_insert_block(m, map, lx >> 3, ly >> 3, lz >> 3);
+  if (b < 0) return;
+  const int slot = find_or_insert_leaf(m, b, ((lx & 7) << 6) | ((ly & 7) << 3) | (lz & 7), map, lx, ly, lz);
+  if (slot < 0) return;
+  if (flags[slot] == 0u) flags[slot] = 1u;
+  for (int w = 0; w < 8; ++w)
+  {
+    const unsigned long long bits = sec_m[static_cast<size_t>(i) * 8 + w];
+    if (bits) atomicOr(active + static_cast<size_t>(slot) * 8 + w, bits);
+  }
+}
+
+// applyMapSectionGrid for the section's leaves (VDBMapping.hpp:1031-1046), one
+// warp per section leaf: the map leaf takes all 512 values and states; it is
+// created when `create[i]` (a voxel is active or not background), otherwise
+// only an existing map leaf is overwritten.
+__global__ void k_section_set_values(MapView m, const int4* __restrict__ sec_o, const float* __restrict__ sec_v,
+                                     const unsigned long long* __restrict__ sec_m,
+                                     const uint32_t* __restrict__ create, uint32_t n, int map,
+                                     uint32_t* __restrict__ flags, float* __restrict__ values,
+                                     unsigned long long* __restrict__ active)
+{
+  const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane   = static_cast<int>(threadIdx.x & 31);
+  if (i >= n) return;
+  int slot = -1;
+  if (lane == 0)
+  {
+    const int4 o = sec_o[i];
+    const int lx = o.x >> 3, ly = o.y >> 3, lz = o.z >> 3;
+    if (create[i])
+    {
+      const int b = find_or_insert_block(m, map, lx >> 3, ly >> 3, lz >> 3);
+      if (b >= 0) slot = find_or_insert_leaf(m, b, ((lx & 7) << 6) | ((ly & 7) << 3) | (lz & 7), map, lx, ly, lz);
+    }
+    else
+    {
+      slot = find_leaf(m, map, lx, ly, lz);
+      if (slot >= 0 && flags[slot] == 0u) slot = -1;
+    }
+    if (slot >= 0 && flags[slot] == 0u) flags[slot] = 1u;
+  }
+  slot = __shfl_sync(0xffffffffu, slot, 0);
+  if (slot < 0) return;
+  for (int k = 0; k < 16; ++k)
+    values[static_cast<size_t>(slot) * 512 + k * 32 + lane] = sec_v[static_cast<size_t>(i) * 512 + k * 32 + lane];
+  if (lane < 8) active[static_cast<size_t>(slot) * 8 + lane] = sec_m[static_cast<size_t>(i) * 8 + lane];
+}
+
+// The section tree's tiles (VDBMapping.hpp:1035 visits them as values): the map
+// voxel at each point becomes the inactive background where a map leaf holds
+// it. One thread per point.
+__global__ void k_section_clear_voxels(MapView m, const int4* __restrict__ pts, uint32_t n, int map,
+                                       const uint32_t* __restrict__ flags, float* __restrict__ values,
+                                       unsigned long long* __restrict__ active)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int4 p   = pts[i];
+  const int slot = find_leaf(m, map, p.x >> 3, p.y >> 3, p.z >> 3);
+  if (slot < 0 || flags[slot] == 0u) return;
+  const int off = ((p.z & 7) << 6) | ((p.y & 7) << 3) | (p.x & 7);
+  values[static_cast<size_t>(slot) * 512 + off] = 0.0f;
+  atomicAnd(active + static_cast<size_t>(slot) * 8 + (off >> 6), ~(1ull << (off & 63)));
+}
+
 } // namespace vdbg

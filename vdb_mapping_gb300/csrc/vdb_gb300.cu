@@ -14,6 +14,8 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <set>
+#include <tuple>
 #include <vector>
 
 #include "kernels.cuh"
@@ -1982,6 +1984,342 @@ int vdbg_batch_export_leaves(vdbg_map* m, int map, int64_t capacity, int32_t* or
   if (!m || !n_out || capacity < 0 || map < 0 || map >= static_cast<int>(m->conf.size()))
     return VDBG_ERR_INVALID_ARGUMENT;
   return export_impl(m, map, capacity, origins, values, masks, n_out, false);
+}
+
+} // extern "C"
+
+// ---------------------------------------------------------------------------
+// Map sections (VDBMapping.hpp:922-1085).
+// ---------------------------------------------------------------------------
+namespace {
+
+// Map id of `map` for this handle: the one map of a single-map handle (-1 or
+// 0), or a map of a batch.
+bool section_map(const vdbg_map* m, int map, int* out)
+{
+  if (m->batch)
+  {
+    if (map < 0 || map >= static_cast<int>(m->conf.size())) return false;
+    *out = map;
+    return true;
+  }
+  if (map > 0) return false;
+  *out = 0;
+  return true;
+}
+
+bool leaf_origin_ok(const int32_t* o)
+{
+  for (int a = 0; a < 3; ++a)
+  {
+    if ((o[a] & 7) != 0) return false;
+    if (!(o[a] >= kVoxelMin && o[a] + 7 < kVoxelMaxExcl)) return false;
+  }
+  return true;
+}
+
+// Device list of the map's leaves overlapping [lo, hi] (slots), its length on
+// the host. The caller frees list and count.
+int section_list(vdbg_map* m, int mp, int3 lo, int3 hi, uint32_t** list, uint32_t** count, uint32_t* n_host)
+{
+  *list = nullptr;
+  *count = nullptr;
+  *n_host = 0;
+  const uint32_t n = std::min(m->n_leaves, m->capacity);
+  VDBG_TRY(dev_alloc(m, count, 1));
+  if (n == 0) return VDBG_OK;
+  VDBG_TRY(dev_alloc(m, list, n));
+  cudaStream_t s = m->stream;
+  VDBG_CUDA(cudaMemsetAsync(*count, 0, sizeof(uint32_t), s));
+  k_section_leaves<<<(n + 255) / 256, 256, 0, s>>>(m->origin, m->flags, n, mp, lo, hi, *list, *count);
+  VDBG_CUDA(cudaGetLastError());
+  VDBG_CUDA(cudaMemcpyAsync(n_host, *count, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  VDBG_CUDA(cudaStreamSynchronize(s));
+  return VDBG_OK;
+}
+
+// Runs `launch` (which allocates leaves through the map's status counters)
+// until it completes without a pool or hash running out; the pools grow in
+// between. Ends with the status fetched and the leaf and block counts taken.
+template <class F>
+int run_allocating(vdbg_map* m, F&& launch)
+{
+  cudaStream_t s = m->stream;
+  for (int attempt = 0;; ++attempt)
+  {
+    VDBG_TRY(launch());
+    VDBG_TRY(fetch_status(m, s));
+    const uint32_t err = m->h_status->error;
+    m->n_leaves        = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
+    m->n_blocks        = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
+    if (err == 0u) return VDBG_OK;
+    if (err & (kErrSpin | kErrStepBound | kErrCoordRange)) return map_error(err);
+    if (attempt >= 8) return VDBG_ERR_OUT_OF_MEMORY;
+    if (err & kErrPoolFull) VDBG_TRY(grow_for(m, m->h_status->n_leaves));
+    if (err & kErrBlockFull) VDBG_TRY(grow_blocks_for(m, m->h_status->n_blocks));
+    if ((err & kErrHashFull) && !(err & kErrBlockFull)) VDBG_TRY(rebuild_hash(m, m->bhash_size * 2, m->n_blocks));
+    if (m->n_blocks > 0)
+    {
+      k_reset_failed_leaves<<<m->num_sms * 4, 256, 0, s>>>(m->bleaf, static_cast<size_t>(m->n_blocks) * 512);
+      VDBG_CUDA(cudaGetLastError());
+    }
+    VDBG_CUDA(cudaStreamSynchronize(s));
+    clear_error_keep_counters(m);
+    VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+  }
+}
+
+// Room for `n` more leaves and blocks before an allocating section call.
+int reserve_for(vdbg_map* m, int64_t n)
+{
+  if (static_cast<uint64_t>(m->n_leaves) + static_cast<uint64_t>(n) > m->capacity)
+    VDBG_TRY(grow_for(m, static_cast<uint64_t>(m->n_leaves) + static_cast<uint64_t>(n)));
+  if (static_cast<uint64_t>(m->n_blocks) + static_cast<uint64_t>(n) > m->bcapacity)
+    VDBG_TRY(grow_blocks_for(m, static_cast<uint64_t>(m->n_blocks) + static_cast<uint64_t>(n)));
+  return VDBG_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int vdbg_export_section(vdbg_map* m, int map, const int32_t lo[3], const int32_t hi[3], int full, int64_t capacity,
+                        int32_t* origins, float* values, uint64_t* masks, int64_t* n_out)
+{
+  int mp = 0;
+  if (!m || !lo || !hi || !n_out || capacity < 0 || !section_map(m, map, &mp)) return VDBG_ERR_INVALID_ARGUMENT;
+  *n_out = 0;
+  VDBG_TRY(set_device(m));
+  VDBG_CUDA(cudaStreamSynchronize(m->stream));
+  const int3 blo = make_int3(lo[0], lo[1], lo[2]), bhi = make_int3(hi[0], hi[1], hi[2]);
+  uint32_t *list = nullptr, *count = nullptr, *keep = nullptr;
+  int4* out_o      = nullptr;
+  float* out_v     = nullptr;
+  unsigned long long* out_m = nullptr;
+  uint32_t c = 0;
+  std::vector<int4> ho;
+  std::vector<uint32_t> hk;
+  std::vector<float> hv;
+  std::vector<unsigned long long> hm;
+  int st = section_list(m, mp, blo, bhi, &list, &count, &c);
+  if (st == VDBG_OK && c > 0)
+  {
+    cudaStream_t s = m->stream;
+    st = dev_alloc(m, &out_o, c);
+    if (st == VDBG_OK) st = dev_alloc(m, &out_v, static_cast<size_t>(c) * 512);
+    if (st == VDBG_OK) st = dev_alloc(m, &out_m, static_cast<size_t>(c) * 8);
+    if (st == VDBG_OK) st = dev_alloc(m, &keep, c);
+    if (st == VDBG_OK)
+    {
+      k_section_extract<<<static_cast<unsigned>((static_cast<uint64_t>(c) * 32 + 255) / 256), 256, 0, s>>>(
+        list, count, m->origin, m->values, m->active, blo, bhi, full ? 1 : 0, out_o, out_v, out_m, keep);
+      ho.resize(c);
+      hk.resize(c);
+      if (values) hv.resize(static_cast<size_t>(c) * 512);
+      if (masks) hm.resize(static_cast<size_t>(c) * 8);
+      if (cudaGetLastError() != cudaSuccess ||
+          cudaMemcpyAsync(ho.data(), out_o, c * sizeof(int4), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaMemcpyAsync(hk.data(), keep, c * sizeof(uint32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          (values && cudaMemcpyAsync(hv.data(), out_v, hv.size() * sizeof(float), cudaMemcpyDeviceToHost, s) !=
+                       cudaSuccess) ||
+          (masks && cudaMemcpyAsync(hm.data(), out_m, hm.size() * sizeof(unsigned long long),
+                                    cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+          cudaStreamSynchronize(s) != cudaSuccess)
+        st = VDBG_ERR_CUDA;
+    }
+  }
+  dev_free(m, list, std::min(m->n_leaves, m->capacity));
+  dev_free(m, count, 1);
+  dev_free(m, out_o, c);
+  dev_free(m, out_v, static_cast<size_t>(c) * 512);
+  dev_free(m, out_m, static_cast<size_t>(c) * 8);
+  dev_free(m, keep, c);
+  if (st != VDBG_OK) return st;
+  std::vector<uint32_t> idx;
+  for (uint32_t j = 0; j < c; ++j)
+    if (hk[j]) idx.push_back(j);
+  std::sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) {
+    if (ho[a].x != ho[b].x) return ho[a].x < ho[b].x;
+    if (ho[a].y != ho[b].y) return ho[a].y < ho[b].y;
+    return ho[a].z < ho[b].z;
+  });
+  *n_out = static_cast<int64_t>(idx.size());
+  if (static_cast<int64_t>(idx.size()) > capacity) return VDBG_ERR_BUFFER_TOO_SMALL;
+  for (size_t k = 0; k < idx.size(); ++k)
+  {
+    const uint32_t j = idx[k];
+    if (origins)
+    {
+      origins[3 * k + 0] = ho[j].x;
+      origins[3 * k + 1] = ho[j].y;
+      origins[3 * k + 2] = ho[j].z;
+    }
+    if (values) values_to_vdb(hv.data() + static_cast<size_t>(j) * 512, values + 512 * k);
+    if (masks) mask_to_vdb(hm.data() + static_cast<size_t>(j) * 8, masks + 8 * k);
+  }
+  return VDBG_OK;
+}
+
+int vdbg_apply_section_states(vdbg_map* m, int map, const int32_t lo[3], const int32_t hi[3], int64_t n,
+                              const int32_t* origins, const uint64_t* masks)
+{
+  int mp = 0;
+  if (!m || !lo || !hi || n < 0 || (n > 0 && (!origins || !masks)) || n > (int64_t(1) << 30) ||
+      !section_map(m, map, &mp))
+    return VDBG_ERR_INVALID_ARGUMENT;
+  for (int64_t i = 0; i < n; ++i)
+    if (!leaf_origin_ok(origins + 3 * i)) return VDBG_ERR_INVALID_ARGUMENT;
+  VDBG_TRY(set_device(m));
+  VDBG_CUDA(cudaStreamSynchronize(m->stream));
+  VDBG_TRY(reserve_for(m, n));
+  cudaStream_t s = m->stream;
+  const int3 blo = make_int3(lo[0], lo[1], lo[2]), bhi = make_int3(hi[0], hi[1], hi[2]);
+  std::vector<int4> ho(static_cast<size_t>(n));
+  std::vector<unsigned long long> hm(static_cast<size_t>(n) * 8);
+  for (int64_t i = 0; i < n; ++i)
+  {
+    ho[i] = make_int4(origins[3 * i], origins[3 * i + 1], origins[3 * i + 2], mp);
+    mask_to_vdb(reinterpret_cast<const unsigned long long*>(masks + 8 * i), reinterpret_cast<uint64_t*>(&hm[8 * i]));
+  }
+  uint32_t *list = nullptr, *count = nullptr;
+  int4* d_o      = nullptr;
+  unsigned long long* d_m = nullptr;
+  uint32_t c     = 0;
+  const uint32_t n_list = std::min(m->n_leaves, m->capacity);
+  int st = section_list(m, mp, blo, bhi, &list, &count, &c);
+  if (st == VDBG_OK && n > 0) st = dev_alloc(m, &d_o, static_cast<size_t>(n));
+  if (st == VDBG_OK && n > 0) st = dev_alloc(m, &d_m, static_cast<size_t>(n) * 8);
+  if (st == VDBG_OK && n > 0 &&
+      (cudaMemcpyAsync(d_o, ho.data(), ho.size() * sizeof(int4), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+       cudaMemcpyAsync(d_m, hm.data(), hm.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, s) !=
+         cudaSuccess))
+    st = VDBG_ERR_CUDA;
+  if (st == VDBG_OK) st = begin_call(m, s);
+  if (st == VDBG_OK && c > 0)
+  {
+    k_section_clear<<<(c * 8 + 255) / 256, 256, 0, s>>>(list, count, m->origin, m->active, blo, bhi);
+    if (cudaGetLastError() != cudaSuccess) st = VDBG_ERR_CUDA;
+  }
+  if (st == VDBG_OK)
+  {
+    st = run_allocating(m, [&]() -> int {
+      if (n > 0)
+      {
+        k_section_set_states<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(
+          map_view(m), d_o, d_m, static_cast<uint32_t>(n), mp, m->flags, m->active);
+        VDBG_CUDA(cudaGetLastError());
+      }
+      return VDBG_OK;
+    });
+  }
+  dev_free(m, list, n_list);
+  dev_free(m, count, 1);
+  dev_free(m, d_o, static_cast<size_t>(n));
+  dev_free(m, d_m, static_cast<size_t>(n) * 8);
+  if (st != VDBG_OK) return st;
+  return maybe_grow_ahead(m);
+}
+
+int vdbg_apply_section_values(vdbg_map* m, int map, int64_t n, const int32_t* origins, const float* values,
+                              const uint64_t* masks)
+{
+  int mp = 0;
+  if (!m || n < 0 || (n > 0 && (!origins || !values || !masks)) || n > (int64_t(1) << 30) ||
+      !section_map(m, map, &mp))
+    return VDBG_ERR_INVALID_ARGUMENT;
+  for (int64_t i = 0; i < n; ++i)
+    if (!leaf_origin_ok(origins + 3 * i)) return VDBG_ERR_INVALID_ARGUMENT;
+  VDBG_TRY(set_device(m));
+  VDBG_CUDA(cudaStreamSynchronize(m->stream));
+  VDBG_TRY(reserve_for(m, n));
+  cudaStream_t s = m->stream;
+  // Leaves in the device's order, whether each one creates its map leaf, and
+  // the origins of the section tree's tiles: the empty slots of its 128^3
+  // nodes (leaf origins) and of its 4096^3 nodes (128^3 node origins).
+  std::vector<int4> ho(static_cast<size_t>(n));
+  std::vector<float> hv(static_cast<size_t>(n) * 512);
+  std::vector<unsigned long long> hm(static_cast<size_t>(n) * 8);
+  std::vector<uint32_t> hc(static_cast<size_t>(n));
+  std::set<std::tuple<int, int, int>> leaves, n1, n2;
+  for (int64_t i = 0; i < n; ++i)
+  {
+    const int32_t* o = origins + 3 * i;
+    ho[i]            = make_int4(o[0], o[1], o[2], mp);
+    for (int q = 0; q < 512; ++q) hv[512 * i + swap_xz(q)] = values[512 * i + q];
+    mask_to_vdb(reinterpret_cast<const unsigned long long*>(masks + 8 * i), reinterpret_cast<uint64_t*>(&hm[8 * i]));
+    bool any = false;
+    for (int w = 0; w < 8; ++w) any = any || masks[8 * i + w] != 0;
+    for (int q = 0; q < 512 && !any; ++q) any = values[512 * i + q] != 0.0f;
+    hc[i] = any ? 1u : 0u;
+    leaves.insert(std::make_tuple(o[0], o[1], o[2]));
+    n1.insert(std::make_tuple(o[0] >> 7, o[1] >> 7, o[2] >> 7));
+    n2.insert(std::make_tuple(o[0] >> 12, o[1] >> 12, o[2] >> 12));
+  }
+  std::vector<int4> tiles;
+  for (const auto& k : n1)
+    for (int a = 0; a < 16; ++a)
+      for (int b = 0; b < 16; ++b)
+        for (int q = 0; q < 16; ++q)
+        {
+          const int x = (std::get<0>(k) << 7) + 8 * a, y = (std::get<1>(k) << 7) + 8 * b,
+                    z = (std::get<2>(k) << 7) + 8 * q;
+          if (!leaves.count(std::make_tuple(x, y, z))) tiles.push_back(make_int4(x, y, z, mp));
+        }
+  for (const auto& k : n2)
+    for (int a = 0; a < 32; ++a)
+      for (int b = 0; b < 32; ++b)
+        for (int q = 0; q < 32; ++q)
+        {
+          const int x = (std::get<0>(k) << 12) + 128 * a, y = (std::get<1>(k) << 12) + 128 * b,
+                    z = (std::get<2>(k) << 12) + 128 * q;
+          if (!n1.count(std::make_tuple(x >> 7, y >> 7, z >> 7))) tiles.push_back(make_int4(x, y, z, mp));
+        }
+  int4* d_o = nullptr;
+  int4* d_t = nullptr;
+  float* d_v = nullptr;
+  unsigned long long* d_m = nullptr;
+  uint32_t* d_c           = nullptr;
+  int st                  = VDBG_OK;
+  if (n > 0)
+  {
+    st = dev_alloc(m, &d_o, static_cast<size_t>(n));
+    if (st == VDBG_OK) st = dev_alloc(m, &d_v, static_cast<size_t>(n) * 512);
+    if (st == VDBG_OK) st = dev_alloc(m, &d_m, static_cast<size_t>(n) * 8);
+    if (st == VDBG_OK) st = dev_alloc(m, &d_c, static_cast<size_t>(n));
+    if (st == VDBG_OK) st = dev_alloc(m, &d_t, tiles.size());
+    if (st == VDBG_OK &&
+        (cudaMemcpyAsync(d_o, ho.data(), ho.size() * sizeof(int4), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+         cudaMemcpyAsync(d_v, hv.data(), hv.size() * sizeof(float), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+         cudaMemcpyAsync(d_m, hm.data(), hm.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, s) !=
+           cudaSuccess ||
+         cudaMemcpyAsync(d_c, hc.data(), hc.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+         (!tiles.empty() &&
+          cudaMemcpyAsync(d_t, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, s) != cudaSuccess)))
+      st = VDBG_ERR_CUDA;
+    if (st == VDBG_OK) st = begin_call(m, s);
+    if (st == VDBG_OK)
+    {
+      st = run_allocating(m, [&]() -> int {
+        k_section_set_values<<<static_cast<unsigned>((static_cast<uint64_t>(n) * 32 + 255) / 256), 256, 0, s>>>(
+          map_view(m), d_o, d_v, d_m, d_c, static_cast<uint32_t>(n), mp, m->flags, m->values, m->active);
+        VDBG_CUDA(cudaGetLastError());
+        if (!tiles.empty())
+        {
+          k_section_clear_voxels<<<static_cast<unsigned>((tiles.size() + 255) / 256), 256, 0, s>>>(
+            map_view(m), d_t, static_cast<uint32_t>(tiles.size()), mp, m->flags, m->values, m->active);
+          VDBG_CUDA(cudaGetLastError());
+        }
+        return VDBG_OK;
+      });
+    }
+  }
+  dev_free(m, d_o, static_cast<size_t>(n));
+  dev_free(m, d_v, static_cast<size_t>(n) * 512);
+  dev_free(m, d_m, static_cast<size_t>(n) * 8);
+  dev_free(m, d_c, static_cast<size_t>(n));
+  dev_free(m, d_t, tiles.size());
+  if (st != VDBG_OK) return st;
+  return maybe_grow_ahead(m);
 }
 
 } // extern "C"

@@ -150,6 +150,71 @@ class _Accessor:
         return self._g.isValueOn(xyz)
 
 
+def createIndexBoundingBox(min_boundary, max_boundary, map_to_reference_tf, resolution):
+    """createIndexBoundingBox (VDBMapping.hpp:811-870): the eight corners of the
+    world box as float points, transformed by the 4x4 matrix (each coordinate
+    computed in double as row . (x, y, z, 1) and stored as float, as
+    pcl::transformPointCloud does with a double matrix), their float min/max,
+    then worldToIndex (w * (1/res)) and Coord::floor. Returns (lo, hi) int32."""
+    lo_w = np.asarray(min_boundary, np.float64)
+    hi_w = np.asarray(max_boundary, np.float64)
+    tf = np.asarray(map_to_reference_tf, np.float64).reshape(4, 4)
+    corners = []
+    for cx in (lo_w[0], hi_w[0]):
+        for cy in (lo_w[1], hi_w[1]):
+            for cz in (lo_w[2], hi_w[2]):
+                p = [float(np.float32(cx)), float(np.float32(cy)), float(np.float32(cz))]
+                q = []
+                for r in range(3):
+                    acc = tf[r, 0] * p[0]
+                    acc = acc + tf[r, 1] * p[1]
+                    acc = acc + tf[r, 2] * p[2]
+                    acc = acc + tf[r, 3]
+                    q.append(np.float32(acc))
+                corners.append(q)
+    c = np.array(corners, np.float32)
+    inv = 1.0 / float(resolution)
+    lo = np.floor(c.min(axis=0).astype(np.float64) * inv).astype(np.int32)
+    hi = np.floor(c.max(axis=0).astype(np.float64) * inv).astype(np.int32)
+    return lo, hi
+
+
+def _section_export(lib, h, map_index, lo, hi, full, check):
+    lo = np.ascontiguousarray(lo, np.int32)
+    hi = np.ascontiguousarray(hi, np.int32)
+    n = C.c_int64()
+    cap = 0
+    while True:
+        origins = np.zeros((cap, 3), np.int32)
+        values = np.zeros((cap, 512), np.float32)
+        masks = np.zeros((cap, 8), np.uint64)
+        s = lib.vdbg_export_section(h, int(map_index), lo.ctypes.data, hi.ctypes.data, 1 if full else 0, cap,
+                                    origins.ctypes.data, values.ctypes.data, masks.ctypes.data, C.byref(n))
+        if s == _lib.STATUS_CODE["VDBG_ERR_BUFFER_TOO_SMALL"]:
+            cap = n.value
+            continue
+        check(s, "vdbg_export_section")
+        k = n.value
+        return origins[:k], values[:k], masks[:k]
+
+
+def _section_states(lib, h, map_index, lo, hi, origins, masks, check):
+    lo = np.ascontiguousarray(lo, np.int32)
+    hi = np.ascontiguousarray(hi, np.int32)
+    o = np.ascontiguousarray(origins, np.int32).reshape(-1, 3)
+    mk = np.ascontiguousarray(masks, np.uint64).reshape(-1, 8)
+    check(lib.vdbg_apply_section_states(h, int(map_index), lo.ctypes.data, hi.ctypes.data, len(o), o.ctypes.data,
+                                        mk.ctypes.data), "vdbg_apply_section_states")
+
+
+def _section_values(lib, h, map_index, origins, values, masks, check):
+    o = np.ascontiguousarray(origins, np.int32).reshape(-1, 3)
+    v = np.ascontiguousarray(values, np.float32).reshape(-1, 512)
+    mk = np.ascontiguousarray(masks, np.uint64).reshape(-1, 8)
+    check(lib.vdbg_apply_section_values(h, int(map_index), len(o), o.ctypes.data, v.ctypes.data, mk.ctypes.data),
+          "vdbg_apply_section_values")
+
+
 class OccupancyVDBMapping:
     """vdb_mapping::OccupancyVDBMapping (OccupancyVDBMapping.hpp:46-200) on the GPU."""
 
@@ -333,6 +398,20 @@ class OccupancyVDBMapping:
         VDBMapping.hpp:731-792)."""
         self._check(self._lib.vdbg_track_changes(self._h, 1 if enable else 0), "vdbg_track_changes")
 
+    def getMapSection(self, lo, hi, full: bool = False):
+        """getMapSectionGrid over the index box [lo, hi] (see createIndexBoundingBox):
+        (origins, values, masks) sorted by origin; full=False gives value 1 at the
+        active voxels (getMapSectionUpdateGrid reads the same as bool)."""
+        return _section_export(self._lib, self._h, -1, lo, hi, full, self._check)
+
+    def applyMapSectionStates(self, lo, hi, origins, masks) -> None:
+        """applyMapSectionUpdateGrid (no smoothing) with the section's box [lo, hi]."""
+        _section_states(self._lib, self._h, -1, lo, hi, origins, masks, self._check)
+
+    def applyMapSectionValues(self, origins, values, masks) -> None:
+        """applyMapSectionGrid (no smoothing)."""
+        _section_values(self._lib, self._h, -1, origins, values, masks, self._check)
+
     def exportChanges(self):
         """Change set of the last integration: (origins, active, value) per leaf
         with a flip, sorted by origin; `value` marks voxels flipped on by a hit."""
@@ -503,6 +582,15 @@ class MapBatch:
         c, r = C.c_uint64(), C.c_uint64()
         self._check(self._lib.vdbg_graph_stats(self._h, C.byref(c), C.byref(r)), "vdbg_graph_stats")
         return {"captures": c.value, "replays": r.value}
+
+    def getMapSection(self, map_index: int, lo, hi, full: bool = False):
+        return _section_export(self._lib, self._h, map_index, lo, hi, full, self._check)
+
+    def applyMapSectionStates(self, map_index: int, lo, hi, origins, masks) -> None:
+        _section_states(self._lib, self._h, map_index, lo, hi, origins, masks, self._check)
+
+    def applyMapSectionValues(self, map_index: int, origins, values, masks) -> None:
+        _section_values(self._lib, self._h, map_index, origins, values, masks, self._check)
 
     def exportChanges(self, map_index: int):
         """Change set of the last batched insert for one map."""
