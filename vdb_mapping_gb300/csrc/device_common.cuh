@@ -177,6 +177,8 @@ struct RunBuffer
   uint32_t warps;            // segments
   uint32_t take;             // rays a DDA warp takes from the order at a time
   uint32_t apply_chunk;      // runs an apply block merges at a time
+  uint32_t* chunk_prefix;    // [warps + 1] apply chunks of the segments before each (k_apply_prefix)
+  uint32_t* ticket;          // next apply chunk to hand out
 };
 
 // DDA state of a lane whose ray was still in flight when its warp's segment

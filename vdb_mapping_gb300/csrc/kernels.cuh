@@ -676,7 +676,8 @@ struct ApplySmem
   unsigned short list[kTable];     // entries in use
   unsigned long long bar;          // completion of the staged chunk's copies
   unsigned int count;
-  unsigned int next;               // the block's next chunk
+  unsigned int next;               // the block's next chunk ticket
+  unsigned int next_sg, next_start, next_end;  // and its segment and runs
   unsigned int failed;
 };
 
@@ -719,40 +720,56 @@ __device__ __forceinline__ int apply_resolve(const MapView& m, const ChannelView
   return slot;
 }
 
-// Runs [start, end) of work item `item` (segment-major chunks), end <= start
-// when the item is empty.
-__device__ __forceinline__ void apply_item_range(const RunBuffer& rb, uint32_t cps, uint32_t item, uint32_t& sg,
-                                                 uint32_t& start, uint32_t& end)
+// Apply chunks of the segments, for k_apply_runs' tickets: chunk_prefix[w] =
+// chunks of the segments before w, chunk_prefix[warps] = all of them; resets
+// the ticket counter. One block of 1024 threads, run after the DDA pass.
+__global__ void __launch_bounds__(1024) k_apply_prefix(RunBuffer rb)
 {
-  sg              = item / cps;
-  start           = (item % cps) * rb.apply_chunk;
-  const uint32_t c = rb.count[sg];
-  end             = min(start + rb.apply_chunk, c);
-}
-
-// First non-empty item at or after `item` in this block's stride (items when none).
-__device__ __forceinline__ uint32_t apply_next_item(const RunBuffer& rb, uint32_t cps, uint32_t items, uint32_t item)
-{
-  for (; item < items; item += gridDim.x)
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < rb.warps; base += 1024u)
   {
-    uint32_t sg, start, end;
-    apply_item_range(rb, cps, item, sg, start, end);
-    if (start < end) return item;
+    const uint32_t w = base + threadIdx.x;
+    const uint32_t n = w < rb.warps ? (rb.count[w] + rb.apply_chunk - 1u) / rb.apply_chunk : 0u;
+    uint32_t total   = 0;
+    const uint32_t e = block_scan_exclusive(n, &total);
+    if (w < rb.warps) rb.chunk_prefix[w] = carry + e;
+    carry += total;
   }
-  return items;
+  if (threadIdx.x == 0)
+  {
+    rb.chunk_prefix[rb.warps] = carry;
+    *rb.ticket                = 0u;
+  }
 }
 
-// Stages the runs of `item` (thread 0 only). Segments start on 16-run
-// boundaries and chunks are multiples of 256 runs, so every copy starts
+// Segment and runs [start, end) of apply chunk `item` (< all chunks): the
+// segment is the last one whose first chunk is at or before `item`.
+__device__ __forceinline__ void apply_item_range(const RunBuffer& rb, uint32_t item, uint32_t& sg, uint32_t& start,
+                                                 uint32_t& end)
+{
+  uint32_t lo = 0, hi = rb.warps;  // chunk_prefix[lo] <= item < chunk_prefix[hi]
+  while (hi - lo > 1u)
+  {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (rb.chunk_prefix[mid] <= item)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  sg    = lo;
+  start = (item - rb.chunk_prefix[lo]) * rb.apply_chunk;
+  end   = min(start + rb.apply_chunk, rb.count[lo]);
+}
+
+// Stages runs [start, end) of segment `sg` (thread 0 only). Segments start on
+// 16-run boundaries and chunks are multiples of 256 runs, so every copy starts
 // 16-byte aligned; lengths are rounded up to 16 bytes, which stays inside the
 // segment.
 template <int kTable>
-__device__ __forceinline__ void apply_stage(const RunBuffer& rb, uint32_t cps, uint32_t item, ApplySmem<kTable>& t,
-                                            unsigned long long* s_key, unsigned long long* s_bits,
-                                            unsigned char* s_slab)
+__device__ __forceinline__ void apply_stage(const RunBuffer& rb, uint32_t sg, uint32_t start, uint32_t end,
+                                            ApplySmem<kTable>& t, unsigned long long* s_key,
+                                            unsigned long long* s_bits, unsigned char* s_slab)
 {
-  uint32_t sg, start, end;
-  apply_item_range(rb, cps, item, sg, start, end);
   const size_t base  = static_cast<size_t>(sg) * rb.seg + start;
   const uint32_t n   = end - start;
   const uint32_t b8  = (n * 8u + 15u) & ~15u;
@@ -761,6 +778,23 @@ __device__ __forceinline__ void apply_stage(const RunBuffer& rb, uint32_t cps, u
   bulk_copy_g2s(s_key, rb.key + base, b8, &t.bar);
   bulk_copy_g2s(s_bits, rb.bits + base, b8, &t.bar);
   bulk_copy_g2s(s_slab, rb.slab + base, b1, &t.bar);
+}
+
+// Takes the block's next chunk ticket (thread 0 only) and stages its runs.
+template <int kTable>
+__device__ __forceinline__ void apply_take(const RunBuffer& rb, uint32_t items, ApplySmem<kTable>& t,
+                                           unsigned long long* s_key, unsigned long long* s_bits,
+                                           unsigned char* s_slab)
+{
+  const uint32_t item = atomicAdd(rb.ticket, 1u);
+  t.next              = min(item, items);
+  if (item >= items) return;
+  uint32_t sg, start, end;
+  apply_item_range(rb, item, sg, start, end);
+  t.next_sg    = sg;
+  t.next_start = start;
+  t.next_end   = end;
+  apply_stage(rb, sg, start, end, t, s_key, s_bits, s_slab);
 }
 
 template <int kApplyThreads, int kApplyTable>
@@ -772,8 +806,7 @@ __global__ void __launch_bounds__(kApplyThreads) k_apply_runs(RunBuffer rb, MapV
   unsigned long long* s_key  = reinterpret_cast<unsigned long long*>(stage);
   unsigned long long* s_bits = s_key + rb.apply_chunk;
   unsigned char* s_slab      = reinterpret_cast<unsigned char*>(s_bits + rb.apply_chunk);
-  const uint32_t cps         = (rb.seg + rb.apply_chunk - 1) / rb.apply_chunk;
-  const uint32_t items       = rb.warps * cps;
+  const uint32_t items       = rb.chunk_prefix[rb.warps];  // chunks of the pass
   // The error word can be set by other blocks while this one starts: read it
   // once for the whole block, so that either every thread returns or none
   // does (the barriers below need all of them).
@@ -786,8 +819,7 @@ __global__ void __launch_bounds__(kApplyThreads) k_apply_runs(RunBuffer rb, MapV
     {
       mbar_init(&t.bar, 1);
       fence_proxy_async_smem();
-      t.next = apply_next_item(rb, cps, items, blockIdx.x);
-      if (t.next < items) apply_stage(rb, cps, t.next, t, s_key, s_bits, s_slab);
+      apply_take(rb, items, t, s_key, s_bits, s_slab);
     }
   }
   for (int e = threadIdx.x; e < kApplyTable; e += kApplyThreads)
@@ -802,8 +834,7 @@ __global__ void __launch_bounds__(kApplyThreads) k_apply_runs(RunBuffer rb, MapV
   uint32_t parity = 0;
   for (uint32_t item = t.next; item < items;)
   {
-    uint32_t sg, start, end;
-    apply_item_range(rb, cps, item, sg, start, end);
+    const uint32_t start = t.next_start, end = t.next_end;
     const bool staged = mbar_wait_bounded(&t.bar, parity);
     parity ^= 1u;
     if (__syncthreads_or(!staged))
@@ -876,12 +907,8 @@ __global__ void __launch_bounds__(kApplyThreads) k_apply_runs(RunBuffer rb, MapV
     // The staging buffer is free: start copying the block's next chunk.
     if (threadIdx.x == 0)
     {
-      t.next = apply_next_item(rb, cps, items, item + gridDim.x);
-      if (t.next < items)
-      {
-        fence_proxy_async_smem();
-        apply_stage(rb, cps, t.next, t, s_key, s_bits, s_slab);
-      }
+      fence_proxy_async_smem();
+      apply_take(rb, items, t, s_key, s_bits, s_slab);
     }
     const uint32_t n_used = t.count;
     for (uint32_t k = threadIdx.x; k < n_used; k += kApplyThreads)

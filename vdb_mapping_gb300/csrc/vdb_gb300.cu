@@ -113,6 +113,7 @@ struct vdbg_map
   unsigned long long* run_bits = nullptr;
   unsigned char* run_slab      = nullptr;
   uint32_t* run_count   = nullptr;
+  uint32_t* run_prefix  = nullptr;  // [dda_warps + 2]: apply chunk prefix, then the ticket
   LaneState* lstate     = nullptr;
   WarpState* wstate     = nullptr;
   uint32_t passes_last  = 0;
@@ -668,6 +669,7 @@ int ensure_runs(vdbg_map* m, uint32_t seg)
   VDBG_TRY(dev_alloc(m, &m->run_bits, W * seg));
   VDBG_TRY(dev_alloc(m, &m->run_slab, W * seg));
   if (!m->run_count) VDBG_TRY(dev_alloc(m, &m->run_count, W));
+  if (!m->run_prefix) VDBG_TRY(dev_alloc(m, &m->run_prefix, W + 2));
   if (!m->lstate) VDBG_TRY(dev_alloc(m, &m->lstate, W * 32));
   if (!m->wstate) VDBG_TRY(dev_alloc(m, &m->wstate, W));
   m->run_seg = seg;
@@ -675,9 +677,11 @@ int ensure_runs(vdbg_map* m, uint32_t seg)
 }
 
 RunBuffer run_buffer(const vdbg_map* m, unsigned long long* key, unsigned long long* bits, unsigned char* slab,
-                     uint32_t* count, uint32_t seg, uint32_t warps)
+                     uint32_t* count, uint32_t* prefix, uint32_t seg, uint32_t warps)
 {
   RunBuffer rb;
+  rb.chunk_prefix = prefix;
+  rb.ticket       = prefix + warps + 1;
   rb.take        = static_cast<uint32_t>(m->tuning.rays_per_take);
   rb.apply_chunk = static_cast<uint32_t>(m->tuning.apply_chunk_runs);
   rb.key   = key;
@@ -714,6 +718,7 @@ void launch_apply(vdbg_map* m, Channel& c, const RunBuffer& rb, cudaStream_t s)
 {
   const unsigned grid = apply_grid(m, rb.apply_chunk);
   const size_t smem   = apply_stage_bytes(rb.apply_chunk);
+  k_apply_prefix<<<1, 1024, 0, s>>>(rb);
   if (rb.apply_chunk <= kApplySmallChunk)
     k_apply_runs<128, 256><<<grid, 128, smem, s>>>(rb, map_view(m), channel_view(c));
   else
@@ -733,7 +738,7 @@ int launch_dda_pass(vdbg_map* m, Channel& c, const int4* rays, const int* order,
   launch_apply(m, c, rb, s);
   VDBG_CUDA(cudaEventRecordWithFlags(m->ev_a1, s, event_flags));
   VDBG_CUDA(cudaGetLastError());
-  m->timings.launches += 2;
+  m->timings.launches += 3;  // k_dda_mark, k_apply_prefix, k_apply_runs
   return VDBG_OK;
 }
 
@@ -785,7 +790,7 @@ int settle_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* orde
       launch_apply(m, c, rb, s);
       VDBG_CUDA(cudaEventRecord(m->ev_a1, s));
       VDBG_CUDA(cudaGetLastError());
-      m->timings.launches += 2;
+      m->timings.launches += 3;  // k_mark_hits, k_apply_prefix, k_apply_runs
       m->timings.retries += 1;
       VDBG_TRY(fetch_status(m, s));
       add_apply_time(m);
@@ -1051,7 +1056,7 @@ CastPlan plan_single(const vdbg_map* m, int64_t n, const double origin[3], doubl
 }
 
 // Kernel launches of one captured step (memsets excluded).
-constexpr uint32_t kGraphKernels = 9;
+constexpr uint32_t kGraphKernels = 10;
 
 // Queues one batched step for capture: the point count is read on the device
 // from t.first[t.n], the grids cover the scratch capacity `cap`, and every
@@ -1192,7 +1197,7 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
       t.ray_scan = m->d_ray_scan;
     }
     const RunBuffer rb =
-      run_buffer(m, m->run_key, m->run_bits, m->run_slab, m->run_count, m->run_seg, m->dda_warps);
+      run_buffer(m, m->run_key, m->run_bits, m->run_slab, m->run_count, m->run_prefix, m->run_seg, m->dda_warps);
     const bool graphed = m->use_graph && m->batch && t.n > 1 && !m->track_changes && integrate_all &&
                          m->channels.size() == 1 && src == &m->channels[0];
     int d = VDBG_OK;
@@ -1588,6 +1593,7 @@ int vdbg_destroy(vdbg_map* m)
   dev_free(m, m->run_bits, static_cast<size_t>(m->dda_warps) * m->run_seg);
   dev_free(m, m->run_slab, static_cast<size_t>(m->dda_warps) * m->run_seg);
   dev_free(m, m->run_count, m->dda_warps);
+  dev_free(m, m->run_prefix, static_cast<size_t>(m->dda_warps) + 2);
   dev_free(m, m->lstate, static_cast<size_t>(m->dda_warps) * 32);
   dev_free(m, m->wstate, m->dda_warps);
   if (m->h_status) cudaFreeHost(m->h_status);
@@ -1795,6 +1801,7 @@ int vdbg_set_tuning(vdbg_map* m, const vdbg_tuning* t)
     dev_free(m, m->run_bits, W * m->run_seg);
     dev_free(m, m->run_slab, W * m->run_seg);
     dev_free(m, m->run_count, W);
+    dev_free(m, m->run_prefix, W + 2);
     dev_free(m, m->lstate, W * 32);
     dev_free(m, m->wstate, W);
     m->run_seg     = 0;
@@ -2349,10 +2356,12 @@ constexpr size_t kNoAllocRunN       = static_cast<size_t>(kNoAllocWarps) * kNoAl
 constexpr size_t kNoAllocKeyBytes   = align256(kNoAllocRunN * sizeof(unsigned long long));
 constexpr size_t kNoAllocSlabBytes  = align256(kNoAllocRunN);
 constexpr size_t kNoAllocCountBytes = align256(static_cast<size_t>(kNoAllocWarps) * sizeof(uint32_t));
+constexpr size_t kNoAllocPrefixBytes = align256((static_cast<size_t>(kNoAllocWarps) + 2) * sizeof(uint32_t));
 constexpr size_t kNoAllocLaneBytes  = align256(static_cast<size_t>(kNoAllocWarps) * 32 * sizeof(LaneState));
 constexpr size_t kNoAllocWarpBytes  = align256(static_cast<size_t>(kNoAllocWarps) * sizeof(WarpState));
 constexpr size_t kNoAllocBytes = kNoAllocPtsBytes + kNoAllocRaysBytes + kNoAllocOrderBytes + 2 * kNoAllocHistBytes +
-                                 2 * kNoAllocKeyBytes + kNoAllocSlabBytes + kNoAllocCountBytes + kNoAllocLaneBytes +
+                                 2 * kNoAllocKeyBytes + kNoAllocSlabBytes + kNoAllocCountBytes + kNoAllocPrefixBytes +
+                                 kNoAllocLaneBytes +
                                  kNoAllocWarpBytes;
 static_assert(kNoAllocBytes <= static_cast<size_t>(VDBG_NOALLOC_SCRATCH_BYTES), "scratch size and header disagree");
 static_assert(kNoAllocWarps % kDdaWarps == 0, "DDA warps per block");
@@ -2425,6 +2434,8 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
   p += kNoAllocSlabBytes;
   uint32_t* r_count          = reinterpret_cast<uint32_t*>(p);
   p += kNoAllocCountBytes;
+  uint32_t* r_prefix         = reinterpret_cast<uint32_t*>(p);
+  p += kNoAllocPrefixBytes;
   LaneState* ls              = reinterpret_cast<LaneState*>(p);
   p += kNoAllocLaneBytes;
   WarpState* ws              = reinterpret_cast<WarpState*>(p);
@@ -2453,7 +2464,7 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
     {
       VDBG_TRY(launch_prep(m, *src, xyz, n, stride, plan.table, flags, s, d_pts, d_rays, nullptr, d_order, d_hist,
                            d_cursor));
-      const RunBuffer rb = run_buffer(m, r_key, r_bits, r_slab, r_count, kNoAllocSeg, kNoAllocWarps);
+      const RunBuffer rb = run_buffer(m, r_key, r_bits, r_slab, r_count, r_prefix, kNoAllocSeg, kNoAllocWarps);
       dda                = run_dda_passes(m, *src, d_rays, d_order, n, plan.table, rb, ls, ws, false, s);
       if (dda == VDBG_ERR_COORD_RANGE)
       {
