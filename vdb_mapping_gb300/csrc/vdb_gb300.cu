@@ -71,6 +71,8 @@ struct vdbg_map
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t ev_prep = nullptr, ev_dda = nullptr;  // after k_scatter, after k_dda_mark
   cudaEvent_t ev_a0 = nullptr, ev_a1 = nullptr;     // around each k_apply_runs launch
+  cudaStream_t side     = nullptr;  // k_mark_hits beside the first DDA pass
+  cudaEvent_t ev_fork = nullptr, ev_hits = nullptr;
   bool timed_prep       = false;
   vdbg_timings timings{};
 
@@ -727,13 +729,30 @@ void launch_apply(vdbg_map* m, Channel& c, const RunBuffer& rb, cudaStream_t s)
 
 // Queues one DDA pass (a fresh one, or `resume` of the rays left in flight)
 // and its k_apply_runs.
+// The endpoint hits (k_mark_hits) on the map's side stream, forked from `s`:
+// they read the sorted rays and write hit bits and leaves, the first DDA
+// pass only reads the rays, so the two run side by side; the pass's apply
+// joins them (join_hits of launch_dda_pass).
+int launch_hits_forked(vdbg_map* m, Channel& c, const int4* rays, const int* order, const ScanTable& t,
+                       unsigned blocks, cudaStream_t s)
+{
+  VDBG_CUDA(cudaEventRecord(m->ev_fork, s));
+  VDBG_CUDA(cudaStreamWaitEvent(m->side, m->ev_fork, 0));
+  k_mark_hits<<<blocks, 256, 0, m->side>>>(rays, order, t, map_view(m), channel_view(c));
+  VDBG_CUDA(cudaGetLastError());
+  VDBG_CUDA(cudaEventRecord(m->ev_hits, m->side));
+  m->timings.launches += 1;
+  return VDBG_OK;
+}
+
 int launch_dda_pass(vdbg_map* m, Channel& c, const int4* rays, const int* order, const ScanTable& t,
                     const RunBuffer& rb, LaneState* ls, WarpState* ws, bool resume, cudaStream_t s,
-                    unsigned event_flags = cudaEventRecordDefault)
+                    unsigned event_flags = cudaEventRecordDefault, bool join_hits = false)
 {
   VDBG_CUDA(cudaMemsetAsync(&m->d_status->inflight, 0, sizeof(uint32_t), s));
   k_dda_mark<<<rb.warps / kDdaWarps, kDdaWarps * 32, 0, s>>>(rays, order, t, map_view(m), rb, ls, ws,
                                                             resume ? 1 : 0);
+  if (join_hits) VDBG_CUDA(cudaStreamWaitEvent(s, m->ev_hits, 0));
   VDBG_CUDA(cudaEventRecordWithFlags(m->ev_a0, s, event_flags));
   launch_apply(m, c, rb, s);
   VDBG_CUDA(cudaEventRecordWithFlags(m->ev_a1, s, event_flags));
@@ -816,15 +835,41 @@ int settle_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* orde
 // hits (VDBMapping.hpp:533-536), into channel `c`: endpoint hits once, then
 // DDA passes, each followed by k_apply_runs, until no ray is left in flight.
 // One status fetch per pass.
+int reset_changes(vdbg_map* m, cudaStream_t s);
+int launch_sweep(vdbg_map* m, Channel& c, cudaStream_t s, bool gated);
+
+// `eager`: the channel's window is the only one the call integrates, so its
+// compact, sweep and window end go out right behind the first pass, gated on
+// the device on a complete marking (no host round trip in between); *swept
+// tells whether they ran. Otherwise the caller sweeps after the passes.
 int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, int64_t n, const ScanTable& t,
-                   const RunBuffer& rb, LaneState* ls, WarpState* ws, bool may_grow, cudaStream_t s)
+                   const RunBuffer& rb, LaneState* ls, WarpState* ws, bool may_grow, cudaStream_t s,
+                   bool eager = false, bool* swept = nullptr)
 {
-  k_mark_hits<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(rays, order, t, map_view(m),
-                                                                     channel_view(c));
-  m->timings.launches += 1;
-  VDBG_TRY(launch_dda_pass(m, c, rays, order, t, rb, ls, ws, false, s));
+  if (swept) *swept = false;
+  VDBG_TRY(launch_hits_forked(m, c, rays, order, t, static_cast<unsigned>((n + 255) / 256), s));
+  VDBG_TRY(launch_dda_pass(m, c, rays, order, t, rb, ls, ws, false, s, cudaEventRecordDefault, true));
+  if (eager)
+  {
+    VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
+    VDBG_TRY(reset_changes(m, s));
+    VDBG_TRY(launch_sweep(m, c, s, true));
+    k_finish_window<<<1, 1, 0, s>>>(channel_view(c), m->d_status, 1);
+    VDBG_CUDA(cudaGetLastError());
+    m->timings.launches += 1;
+  }
   VDBG_TRY(fetch_status(m, s));
   add_apply_time(m);
+  if (eager && m->h_status->windows > 0u)
+  {
+    m->n_leaves       = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
+    m->n_blocks       = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
+    m->passes_last    = 1;
+    m->timings.passes = 1;
+    c.pending         = false;
+    *swept            = true;
+    return VDBG_OK;
+  }
   return settle_dda_passes(m, c, rays, order, n, t, rb, ls, ws, may_grow, s, 1);
 }
 
@@ -1070,9 +1115,9 @@ int queue_step(vdbg_map* m, Channel& c, int64_t cap, int64_t stride, const ScanT
   launch_scan(m->d_hist, m->d_cursor, static_cast<uint32_t>(kBucketsPerScan * t.n), m->d_status, s);
   k_scatter<<<blocks, 256, 0, s>>>(m->d_rays, cap, t, m->d_cursor, m->d_order);
   VDBG_CUDA(cudaEventRecordWithFlags(m->ev_prep, s, cudaEventRecordExternal));
-  k_mark_hits<<<blocks, 256, 0, s>>>(m->d_rays, m->d_order, t, map_view(m), channel_view(c));
+  VDBG_TRY(launch_hits_forked(m, c, m->d_rays, m->d_order, t, blocks, s));
   VDBG_TRY(launch_dda_pass(m, c, m->d_rays, m->d_order, t, rb, m->lstate, m->wstate, false, s,
-                           cudaEventRecordExternal));
+                           cudaEventRecordExternal, true));
   VDBG_CUDA(cudaEventRecordWithFlags(m->ev_dda, s, cudaEventRecordExternal));
   VDBG_TRY(launch_sweep(m, c, s, true));
   k_finish_window<<<1, 1, 0, s>>>(channel_view(c), m->d_status, 1);
@@ -1217,7 +1262,21 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
     {
       VDBG_TRY(launch_prep(m, *src, xyz, n, stride, t, flags, s, m->d_pts, m->d_rays, m->d_ray_scan, m->d_order,
                            m->d_hist, m->d_cursor));
-      d = run_dda_passes(m, *src, m->d_rays, m->d_order, n, t, rb, m->lstate, m->wstate, true, s);
+      // The sweep follows the marking without a host round trip when this
+      // source's window is the only one the call integrates.
+      bool eager = integrate_all || only == src;
+      if (integrate_all)
+        for (const Channel& c : m->channels)
+          if (&c != src && c.pending) eager = false;
+      bool swept = false;
+      d = run_dda_passes(m, *src, m->d_rays, m->d_order, n, t, rb, m->lstate, m->wstate, true, s, eager, &swept);
+      if (d == VDBG_OK && swept)
+      {
+        record_timings(m);
+        fill_stats(m, leaves_before, stats);
+        VDBG_TRY(maybe_grow_ahead(m));
+        return call_status;
+      }
     }
     if (d == VDBG_ERR_COORD_RANGE)
     {
@@ -1394,7 +1453,11 @@ int create_impl(int n_maps, const double* resolutions, const vdbg_options* optio
       cudaFuncSetAttribute(k_apply_runs<128, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            static_cast<int>(apply_stage_bytes(kApplySmallChunk))) != cudaSuccess)
     return fail(VDBG_ERR_CUDA);
-  if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(VDBG_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&m->ev_hits, cudaEventDisableTiming) != cudaSuccess)
+    return fail(VDBG_ERR_CUDA);
   if (cudaEventCreate(&m->ev0) != cudaSuccess || cudaEventCreate(&m->ev1) != cudaSuccess ||
       cudaEventCreate(&m->ev_prep) != cudaSuccess || cudaEventCreate(&m->ev_dda) != cudaSuccess ||
       cudaEventCreate(&m->ev_a0) != cudaSuccess || cudaEventCreate(&m->ev_a1) != cudaSuccess)
@@ -1603,6 +1666,9 @@ int vdbg_destroy(vdbg_map* m)
   if (m->ev_dda) cudaEventDestroy(m->ev_dda);
   if (m->ev_a0) cudaEventDestroy(m->ev_a0);
   if (m->ev_a1) cudaEventDestroy(m->ev_a1);
+  if (m->ev_fork) cudaEventDestroy(m->ev_fork);
+  if (m->ev_hits) cudaEventDestroy(m->ev_hits);
+  if (m->side) cudaStreamDestroy(m->side);
   if (m->stream) cudaStreamDestroy(m->stream);
   delete m;
   return VDBG_OK;
