@@ -186,7 +186,7 @@ int vdbg_export_changes(vdbg_map* map, int map_index, int64_t capacity, int32_t*
  * on a sample of the caller's scans. */
 typedef struct vdbg_tuning
 {
-  int32_t rays_per_take;     /* rays a DDA warp takes from the sorted order at a time (1-1024; 16) */
+  int32_t rays_per_take;     /* rays a DDA warp takes from the sorted order at a time (1-1024; 32) */
   int32_t apply_chunk_runs;  /* DDA runs an apply block stages and merges at a time (256-4096, a multiple of 256; 2048) */
   int32_t length_edges[3];   /* L1 lengths (voxels) starting the sort's length classes, descending (2048, 1024, 512) */
   float hash_load;           /* block-hash load factor (0.05-0.9; 0.5); a change rebuilds the hash */

@@ -123,7 +123,7 @@ struct vdbg_map
   int64_t bytes         = 0;
   uint64_t run_budget   = 2ull << 30;  // run buffer bytes the map may grow to
   int num_sms           = 152;
-  vdbg_tuning tuning{16, 2048, {2048, 1024, 512}, 0.5f, 16};
+  vdbg_tuning tuning{32, 2048, {2048, 1024, 512}, 0.5f, 16};
   uint32_t apply_grid_chunk = 0;   // apply_chunk the cached grid size is for
   unsigned apply_grid_blocks = 0;
   // Change set of the last integration (vdbg_track_changes).
