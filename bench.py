@@ -42,10 +42,10 @@ STATUS_BYTES = 80  # device status block (DevStatus) read back by every call
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
 # each kernel on a steady-state dense scan, from one ncu capture of the
-# default workload (profiles/dram_traffic_dense_street.md). Only meaningful
+# default workload (profiles/launches_dense_street.md). Only meaningful
 # for the dense workload; other workloads report None.
-NCU_TRAFFIC_BYTES = {"k_dda_mark": 429.6e6, "k_apply_runs": 801.2e6, "k_sweep": 2040.1e6,
-                     "prep (k_prep+k_scan+k_scatter)": 4.2e6}
+NCU_TRAFFIC_BYTES = {"k_dda_mark": 429.5e6, "k_apply_runs": 804.9e6, "k_sweep": 2048.8e6,
+                     "prep (k_prep+k_scan+k_scatter)": 8.4e6}
 
 
 def parse_args():
