@@ -48,7 +48,8 @@ enum vdbg_status
 typedef struct vdbg_config
 {
   double max_range;
-  int32_t fast_mode;
+  int32_t fast_mode;  /* castRayIntoGridFast (VDBMapping.hpp:577-602): single maps only;
+                         vdbg_batch_set_config and the no-allocation insert reject it */
   int32_t reserved0;
   double accumulation_period;
   double prob_hit;
@@ -118,8 +119,8 @@ int vdbg_accumulate_update(vdbg_map* map, const float* xyz, int64_t n, int64_t s
  * grid, in source-id order, then fresh update grids. */
 int vdbg_integrate_update(vdbg_map* map, void* stream, vdbg_scan_stats* stats);
 
-/* VDBMapping::raycastPointCloud VDBMapping.hpp:466-539 with fast_mode off,
- * into the update grid of `source_id` with an explicit raycast range. */
+/* VDBMapping::raycastPointCloud VDBMapping.hpp:466-539 into the update grid
+ * of `source_id` with an explicit raycast range (fast mode as configured). */
 int vdbg_raycast_point_cloud(vdbg_map* map, const float* xyz, int64_t n, int64_t stride_bytes,
                              const double origin[3], double raycast_range, const char* source_id,
                              uint32_t flags, void* stream, vdbg_scan_stats* stats);
@@ -278,6 +279,20 @@ int vdbg_apply_section_states(vdbg_map* map, int map_index, const int32_t lo[3],
  * provided. */
 int vdbg_apply_section_values(vdbg_map* map, int map_index, int64_t n, const int32_t* origins, const float* values,
                               const uint64_t* masks);
+
+/* VDBMapping::raytrace VDBMapping.hpp:675-721 (the single-ray overload,
+ * :646-662, is n = 1) for the map (map_index -1) or map `map_index` of a
+ * batch: n rays with world origins[n][3], directions[n][3] (normalised here)
+ * and max_lengths[n]; successes[n] (1 when the volume ray intersector found a
+ * span of leaves on the ray) and end_points[n][3] (the first active voxel
+ * after the span's start voxel, or the voxel just past the span, or, without
+ * a span, the ray's end) out, all in host memory. The intersector is that of
+ * fast mode (VDBMapping.hpp:1436-1449) on the map as it stands; the reference
+ * has one only in fast mode, this call works in either mode. A ray whose
+ * index-space start or end is NaN or outside +-2^30 fails the call with
+ * VDBG_ERR_COORD_RANGE. */
+int vdbg_raytrace(vdbg_map* map, int map_index, int64_t n, const double* origins, const double* directions,
+                  const double* max_lengths, uint8_t* successes, double* end_points);
 
 /* CUDA-graph replay of vdbg_batch_insert (batches of two or more maps; on by
  * default). The step is captured once per buffer layout and replayed as one

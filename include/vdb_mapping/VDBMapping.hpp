@@ -717,6 +717,52 @@ public:
   }
 #endif
 
+  /*! VDBMapping.hpp:675-721: one raytrace per ray through the map's volume ray
+   * intersector (vdbg_raytrace). The reference builds the intersector only in
+   * fast mode; here it exists in either mode. */
+  void raytrace(const std::vector<openvdb::Vec3d>& ray_origins_world, const std::vector<openvdb::Vec3d>& ray_directions,
+                const std::vector<double>& max_ray_lengths, std::vector<bool>& successes,
+                std::vector<openvdb::Vec3d>& end_points)
+  {
+    const size_t n = ray_origins_world.size();
+    if (ray_directions.size() != n || max_ray_lengths.size() != n)
+      throw std::invalid_argument("raytrace: origins, directions and lengths differ in length");
+    std::vector<double> o(3 * n), d(3 * n), e(3 * n);
+    for (size_t i = 0; i < n; ++i)
+      for (int a = 0; a < 3; ++a)
+      {
+        o[3 * i + a] = ray_origins_world[i][a];
+        d[3 * i + a] = ray_directions[i][a];
+      }
+    std::vector<uint8_t> ok(n, 0);
+    {
+      std::shared_lock map_lock(*m_map_mutex);
+      check(vdbg_raytrace(m_dev->map, -1, static_cast<int64_t>(n), o.data(), d.data(), max_ray_lengths.data(),
+                          ok.data(), e.data()),
+            "vdbg_raytrace");
+    }
+    successes.assign(n, false);
+    end_points.assign(n, openvdb::Vec3d());
+    for (size_t i = 0; i < n; ++i)
+    {
+      successes[i]  = ok[i] != 0;
+      end_points[i] = openvdb::Vec3d(e[3 * i], e[3 * i + 1], e[3 * i + 2]);
+    }
+  }
+
+  /*! VDBMapping.hpp:646-662, one ray (the reference's overload forwards its
+   * length where the batch form wants a vector; here it is that length). */
+  void raytrace(const openvdb::Vec3d& ray_origin_world, const openvdb::Vec3d& ray_direction,
+                const double max_ray_length, bool& success, openvdb::Vec3d& end_point)
+  {
+    std::vector<bool> s;
+    std::vector<openvdb::Vec3d> e;
+    raytrace(std::vector<openvdb::Vec3d>{ray_origin_world}, std::vector<openvdb::Vec3d>{ray_direction},
+             std::vector<double>{max_ray_length}, s, e);
+    success   = s[0];
+    end_point = e[0];
+  }
+
   /*! VDBMapping.hpp:1343. */
   std::shared_ptr<std::shared_mutex> getMapMutex() { return m_map_mutex; }
 

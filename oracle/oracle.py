@@ -49,6 +49,7 @@ def load():
         "vo_section": (I64, [P, P, P, C.c_int, I64, P, P, P]),
         "vo_apply_section_states": (None, [P, P, P, I64, P, P]),
         "vo_apply_section_values": (None, [P, I64, P, P, P]),
+        "vo_raytrace": (C.c_int, [P, I64, P, P, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -165,6 +166,18 @@ class OracleMap:
         v = np.ascontiguousarray(values, np.float32)
         mk = np.ascontiguousarray(masks, np.uint64)
         self._l.vo_apply_section_values(self._h, len(o), o.ctypes.data, v.ctypes.data, mk.ctypes.data)
+
+    def raytrace(self, origins, directions, max_lengths):
+        """raytrace (VDBMapping.hpp:675-721): (status, success bool[n], end points [n][3])."""
+        o = np.ascontiguousarray(np.asarray(origins, np.float64).reshape(-1, 3))
+        d = np.ascontiguousarray(np.asarray(directions, np.float64).reshape(-1, 3))
+        n = o.shape[0]
+        ln = np.ascontiguousarray(np.broadcast_to(np.asarray(max_lengths, np.float64), (n,)))
+        ok = np.zeros(n, np.uint8)
+        ends = np.zeros((n, 3), np.float64)
+        r = self._l.vo_raytrace(self._h, n, o.ctypes.data, d.ctypes.data, ln.ctypes.data, ok.ctypes.data,
+                                ends.ctypes.data)
+        return r, ok.astype(bool), ends
 
     def getValue(self, xyz) -> float:
         return self._l.vo_get_value(self._h, *[int(c) for c in xyz])

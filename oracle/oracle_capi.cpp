@@ -180,6 +180,12 @@ void vo_apply_section_values(void* h, int64_t n, const int32_t* origins, const f
   static_cast<Handle*>(h)->map.apply_section_values(section_leaves(n, origins, values, masks));
 }
 
+int vo_raytrace(void* h, int64_t n, const double* origins, const double* dirs, const double* lengths,
+                uint8_t* success, double* ends)
+{
+  return static_cast<Handle*>(h)->map.raytrace(static_cast<size_t>(n), origins, dirs, lengths, success, ends);
+}
+
 float vo_get_value(void* h, int32_t x, int32_t y, int32_t z)
 {
   return static_cast<Handle*>(h)->map.map().get_value(Coord(x, y, z));

@@ -459,6 +459,227 @@ private:
   std::vector<std::unique_ptr<MapLeaf> > m_leaves;
 };
 
+// ---------------------------------------------------------------------------
+// tools::VolumeRayIntersector<FloatGrid>, as VDBMapping.hpp:1436-1449 builds
+// it for fast mode (castRayIntoGridFast, VDBMapping.hpp:577-602) and the
+// raytrace queries (VDBMapping.hpp:675-721). OpenVDB code, not vendored;
+// restated from its published design (parity with OpenVDB itself is not
+// pinned here: no OpenVDB build exists on these machines):
+//  * the constructor copies the tree's topology and takes the bounding box of
+//    the leaves holding an active voxel (CoordBBox, leaf granularity), its
+//    max corner offset by one; with no active voxel the box stays the empty
+//    CoordBBox (min INT_MAX, max INT_MIN + 1);
+//  * setIndexRay clips the ray to that box (Ray::clip, slab method) and keeps
+//    the ray's times when it misses;
+//  * math::VolumeHDDA<Tree, Ray, 2> marches DDA<Ray, 12> over the cells of the
+//    root's children (4096^3 voxels), descending into the cells that hold a
+//    node with the ray's times set to [entry, DDA::next() = min(t1, next)],
+//    then DDA<Ray, 7> (128^3) and DDA<Ray, 3> (leaves); a span opens at the
+//    first leaf cell holding a leaf and closes at the entry time of the next
+//    cell, at any level, holding nothing; spans of length <= 1e-9
+//    (math::Delta<double>) are dropped; march() stops at the first span,
+//    hits() collects all.
+// The map has no tiles, so a node exists exactly where a leaf below it does.
+// ---------------------------------------------------------------------------
+struct IRay
+{
+  double eye[3], dir[3], inv[3];
+  double t0, t1;
+  IRay(const double e[3], const double d[3], double a, double b) : t0(a), t1(b)
+  {
+    for (int i = 0; i < 3; ++i)
+    {
+      eye[i] = e[i];
+      dir[i] = d[i];
+      inv[i] = 1.0 / d[i];
+    }
+  }
+};
+
+struct ISpan
+{
+  double t0 = -1.0, t1 = -1.0;
+  bool valid(double eps = 1e-9) const { return (t1 - t0) > eps; }
+};
+
+// math::DDA<Ray, Log2Dim> for any cell size.
+struct CellDDA
+{
+  int32_t voxel[3];
+  int32_t step[3];
+  double next[3];
+  double delta[3];
+  double t0, t1;
+
+  CellDDA(const IRay& r, double start, double stop, int log2)
+  {
+    const int32_t dim = 1 << log2;
+    t0                = start;
+    t1                = stop;
+    double pos[3];
+    for (int i = 0; i < 3; ++i)
+    {
+      pos[i]   = r.eye[i] + r.dir[i] * t0;
+      voxel[i] = static_cast<int32_t>(std::floor(pos[i])) & ~(dim - 1);
+    }
+    for (int i = 0; i < 3; ++i)
+    {
+      if (r.dir[i] == 0.0)
+      {
+        step[i]  = 0;
+        next[i]  = std::numeric_limits<double>::max();
+        delta[i] = std::numeric_limits<double>::max();
+      }
+      else if (r.inv[i] > 0)
+      {
+        step[i]  = dim;
+        next[i]  = t0 + (static_cast<double>(voxel[i] + dim) - pos[i]) * r.inv[i];
+        delta[i] = static_cast<double>(step[i]) * r.inv[i];
+      }
+      else
+      {
+        step[i]  = -dim;
+        next[i]  = t0 + (static_cast<double>(voxel[i]) - pos[i]) * r.inv[i];
+        delta[i] = static_cast<double>(step[i]) * r.inv[i];
+      }
+    }
+  }
+  double leave_time() const { return std::min(std::min(t1, next[0]), std::min(next[1], next[2])); }
+  bool advance()
+  {
+    const int a = argmin3_high_ties(next);
+    t0          = next[a];
+    next[a] += delta[a];
+    voxel[a] += step[a];
+    return t0 <= t1;
+  }
+};
+
+class Intersector
+{
+public:
+  explicit Intersector(const FloatMap& map)
+  {
+    for (const auto& lp : map.leaves())
+    {
+      const Coord& o = lp->origin;
+      m_leaf.insert(o);
+      m_node1.insert(Coord(o.x >> 7, o.y >> 7, o.z >> 7));
+      m_node2.insert(Coord(o.x >> 12, o.y >> 12, o.z >> 12));
+      bool on = false;
+      for (int w = 0; w < 8; ++w) on = on || lp->on[w] != 0;
+      if (!on) continue;
+      for (int i = 0; i < 3; ++i)
+      {
+        m_lo[i] = std::min(m_lo[i], o[i]);
+        m_hi[i] = std::max(m_hi[i], o[i] + 7);
+      }
+    }
+    for (int i = 0; i < 3; ++i) m_hi[i] += 1;  // mBBox.max().offset(1)
+  }
+
+  // setIndexRay: the ray clipped to the box, or unchanged when it misses.
+  IRay index_ray(const IRay& in) const
+  {
+    IRay r    = in;
+    double t0 = r.t0, t1 = r.t1;
+    for (int i = 0; i < 3; ++i)
+    {
+      double a = (static_cast<double>(m_lo[i]) - r.eye[i]) * r.inv[i];
+      double b = (static_cast<double>(m_hi[i]) - r.eye[i]) * r.inv[i];
+      if (a > b) std::swap(a, b);
+      if (a > t0) t0 = a;
+      if (b < t1) t1 = b;
+      if (t0 > t1) return r;
+    }
+    r.t0 = t0;
+    r.t1 = t1;
+    return r;
+  }
+
+  // VolumeRayIntersector::march on an index ray: true with the first span.
+  bool march(const IRay& ray, double& t0, double& t1) const
+  {
+    ISpan t;
+    IRay r = ray;
+    if (r.t1 - r.t0 > 1e-9) level(2, r, nullptr, t);
+    t0 = t.t0;
+    t1 = t.t1;
+    return t.valid(0.0);
+  }
+
+  // VolumeRayIntersector::hits on an index ray.
+  std::vector<ISpan> hits(const IRay& ray) const
+  {
+    std::vector<ISpan> out;
+    ISpan t;
+    IRay r = ray;
+    level(2, r, &out, t);
+    if (t.valid()) out.push_back(t);
+    return out;
+  }
+
+private:
+  bool holds(int lvl, const int32_t v[3]) const
+  {
+    if (lvl == 2) return m_node2.count(Coord(v[0] >> 12, v[1] >> 12, v[2] >> 12)) != 0;
+    if (lvl == 1) return m_node1.count(Coord(v[0] >> 7, v[1] >> 7, v[2] >> 7)) != 0;
+    return m_leaf.count(Coord(v[0], v[1], v[2])) != 0;
+  }
+
+  // VolumeHDDA<Tree, Ray, lvl>::march (list == nullptr: stop at the first
+  // span, returning true) or ::hits (collect into *list).
+  bool level(int lvl, IRay& ray, std::vector<ISpan>* list, ISpan& t) const
+  {
+    static const int kLog2[3] = {3, 7, 12};
+    CellDDA d(ray, ray.t0, ray.t1, kLog2[lvl]);
+    do
+    {
+      if (holds(lvl, d.voxel))
+      {
+        if (lvl > 0)
+        {
+          ray.t0 = d.t0;
+          ray.t1 = d.leave_time();
+          if (level(lvl - 1, ray, list, t)) return true;
+        }
+        else if (t.t0 < 0)
+        {
+          t.t0 = d.t0;
+        }
+      }
+      else if (t.t0 >= 0)
+      {
+        t.t1 = d.t0;
+        if (t.valid())
+        {
+          if (!list) return true;
+          list->push_back(t);
+        }
+        t = ISpan();
+      }
+    } while (d.advance());
+    if (t.t0 >= 0) t.t1 = d.t1;
+    return false;
+  }
+
+  std::set<Coord> m_leaf, m_node1, m_node2;
+  int32_t m_lo[3] = {std::numeric_limits<int32_t>::max(), std::numeric_limits<int32_t>::max(),
+                     std::numeric_limits<int32_t>::max()};
+  int32_t m_hi[3] = {std::numeric_limits<int32_t>::min(), std::numeric_limits<int32_t>::min(),
+                     std::numeric_limits<int32_t>::min()};
+};
+
+// Index coordinates a traversal may start from; outside, the call fails with
+// kCoordRange (beyond int32 the reference's Coord::floor is undefined).
+constexpr double kTraceLimit = 1073741824.0;  // 2^30
+inline bool trace_point_ok(const double p[3])
+{
+  for (int i = 0; i < 3; ++i)
+    if (!(p[i] > -kTraceLimit && p[i] < kTraceLimit)) return false;
+  return true;
+}
+
 // Config of OccupancyVDBMapping.hpp:38-44 plus BaseConfig VDBMapping.hpp:64-71
 // (map_directory_path is irrelevant to the path and omitted).
 struct Config
@@ -489,6 +710,7 @@ enum Status : int
   kBadRange          = 3,  // negative max_range (VDBMapping.hpp:1458-1463)
   kBadProbability    = 4,  // OccupancyVDBMapping.hpp:65-76
   kDuplicateSource   = 5,
+  kCoordRange        = 6,  // a raytrace query outside +-2^30 index coordinates (or NaN)
 };
 
 class OccupancyMap
@@ -533,22 +755,32 @@ public:
     return kOk;
   }
 
-  // VDBMapping.hpp:466-539 into `grid` (fast_mode is not part of this path).
+  // VDBMapping.hpp:466-539 into `grid`. In fast mode (VDBMapping.hpp:520-526)
+  // a non-empty map takes castRayIntoGridFast instead of castRayIntoGrid.
   int raycast_point_cloud(const float* xyz, size_t n, size_t stride_floats, const double origin[3],
                           double raycast_range, UpdateGrid& grid, ScanStats* st = nullptr)
   {
     if (!m_config_set) return kNotConfigured;
-    const Coord oi = world_to_index(origin, m_resolution, m_var);
+    const Coord oi        = world_to_index(origin, m_resolution, m_var);
+    const bool grid_empty = m_map.empty();
+    const Intersector* ix = (m_fast_mode && !grid_empty) ? &intersector() : nullptr;
     for (size_t i = 0; i < n; ++i)
     {
       const float* p  = xyz + i * stride_floats;
       const RayEnd re = clip_and_quantise(origin, p[0], p[1], p[2], raycast_range, m_resolution, m_var);
       if (!re.valid) continue;
       if (st) ++st->rays;
-      cast_ray(oi, re.end, [&](const Coord& v) {
-        grid.set_active(v);
-        if (st) ++st->visits;
-      });
+      if (m_fast_mode)
+      {
+        if (ix) cast_ray_fast(*ix, oi, re.end, grid, st);
+      }
+      else
+      {
+        cast_ray(oi, re.end, [&](const Coord& v) {
+          grid.set_active(v);
+          if (st) ++st->visits;
+        });
+      }
       if (!re.clipped)
       {
         grid.set_value_on(re.end);
@@ -560,6 +792,93 @@ public:
       }
     }
     return kOk;
+  }
+
+  // castRayIntoGridFast (VDBMapping.hpp:577-602): the ray of castRayIntoGrid,
+  // clipped by the intersector; along each of its spans the voxel DDA marks the
+  // voxels that are active in the map (no early exit for end == origin).
+  void cast_ray_fast(const Intersector& ix, const Coord& o, const Coord& e, UpdateGrid& grid, ScanStats* st)
+  {
+    double eye[3], dir[3];
+    for (int i = 0; i < 3; ++i)
+    {
+      eye[i] = static_cast<double>(o[i]) + 0.5;
+      dir[i] = static_cast<double>(e[i]) - static_cast<double>(o[i]);
+    }
+    const IRay ray = ix.index_ray(IRay(eye, dir, 0.0, 1.0));
+    for (const ISpan& sp : ix.hits(ray))
+    {
+      CellDDA d(IRay(eye, dir, sp.t0, sp.t1), sp.t0, sp.t1, 0);
+      do
+      {
+        const Coord v(d.voxel[0], d.voxel[1], d.voxel[2]);
+        if (m_map.is_value_on(v))
+        {
+          grid.set_active(v);
+          if (st) ++st->visits;
+        }
+      } while (d.advance());
+    }
+  }
+
+  // raytrace (VDBMapping.hpp:675-721) for n rays: world origins and
+  // directions [n][3], lengths [n]; success[n] and end points [n][3] out.
+  // The single-ray overload (VDBMapping.hpp:646-662) is this with n = 1.
+  // Returns kCoordRange (outputs unspecified) when a ray's index-space start
+  // or end leaves +-2^30 or is NaN.
+  int raytrace(size_t n, const double* origins, const double* dirs, const double* lengths, uint8_t* success,
+               double* ends)
+  {
+    const Intersector& ix = intersector();
+    const double inv_res  = 1.0 / m_resolution;
+    for (size_t i = 0; i < n; ++i)
+    {
+      // Vec3d::normalize (scale by 1/length unless the length is within 1e-7
+      // of 0), then scale to the ray's length.
+      double d[3]     = {dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]};
+      const double ln = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      if (std::fabs(ln - 0.0) > 1e-7)
+      {
+        const double s = 1.0 / ln;
+        for (int k = 0; k < 3; ++k) d[k] *= s;
+      }
+      double oi[3], di[3], tip[3];
+      for (int k = 0; k < 3; ++k)
+      {
+        d[k] *= lengths[i];
+        oi[k]  = m_var.w2i_divide ? origins[3 * i + k] / m_resolution : origins[3 * i + k] * inv_res;
+        di[k]  = m_var.w2i_divide ? d[k] / m_resolution : d[k] * inv_res;
+        tip[k] = oi[k] + di[k] * 1.0;
+      }
+      if (!trace_point_ok(oi) || !trace_point_ok(tip)) return kCoordRange;
+      const IRay ray = ix.index_ray(IRay(oi, di, 0.0, 1.0));
+      double t0, t1;
+      if (ix.march(ray, t0, t1))
+      {
+        CellDDA dda(IRay(oi, di, t0, t1), t0, t1, 0);
+        while (dda.advance() && !m_map.is_value_on(Coord(dda.voxel[0], dda.voxel[1], dda.voxel[2])))
+        {
+        }
+        for (int k = 0; k < 3; ++k) ends[3 * i + k] = static_cast<double>(dda.voxel[k]) * m_resolution;
+        success[i] = 1;
+      }
+      else
+      {
+        for (int k = 0; k < 3; ++k) ends[3 * i + k] = (oi[k] + di[k]) * m_resolution;
+        success[i] = 0;
+      }
+    }
+    return kOk;
+  }
+
+  // The volume ray intersector: refreshed after every integration in fast
+  // mode (updateVolumeRayIntersectors, VDBMapping.hpp:1436-1449). Where the
+  // reference would use a null one (fast mode switched on over a non-empty
+  // map, or raytrace without fast mode) it is built from the map as it is.
+  const Intersector& intersector()
+  {
+    if (!m_intersector) m_intersector.reset(new Intersector(m_map));
+    return *m_intersector;
   }
 
   // VDBMapping.hpp:731-792 with OccupancyVDBMapping.hpp:92-117. Returns the
@@ -663,6 +982,7 @@ public:
       }
       kv.second.grid.clear();
     }
+    if (m_fast_mode && !m_map.empty()) m_intersector.reset(new Intersector(m_map));
   }
 
   const UpdateGrid& last_change() const { return m_last_change; }
@@ -829,6 +1149,7 @@ private:
   float m_lo_min       = 0.0f;
   FloatMap m_map;
   UpdateGrid m_last_change;
+  std::unique_ptr<Intersector> m_intersector;
   std::map<std::string, Source> m_sources;
   std::vector<Coord> m_artificial;
 };

@@ -185,6 +185,48 @@ TEST(DropIn, MapSections)
   EXPECT_EQ(other.getGrid()->getAccessor().getValue(openvdb::Coord(12, 0, 0)), logodds(0.9));
 }
 
+TEST(DropIn, RaytraceAndFastMode)
+{
+  // raytrace (VDBMapping.hpp:646-721) and fast mode (:577-602) through the
+  // reference-style API. One hit at p = 0.9 turns a voxel active, a miss
+  // turns it back to 0 (the two log-odds are exact negatives).
+  OccupancyVDBMapping map(1.0);
+  map.setConfig(test_config(30));
+  map.addInputSource("lidar", 30, 0);
+  Eigen::Matrix<double, 3, 1> origin(0, 0, 0);
+  map.insertPointCloud(cloud_of({{12.f, 0.f, 0.f}}), origin, "lidar");
+  bool ok = false;
+  openvdb::Vec3d end;
+  map.raytrace(openvdb::Vec3d(0.5, 0.5, 0.5), openvdb::Vec3d(1, 0, 0), 20.0, ok, end);
+  EXPECT_TRUE(ok);
+  EXPECT_EQ(end.x(), 12.0);
+  EXPECT_EQ(end.y(), 0.0);
+  std::vector<bool> oks;
+  std::vector<openvdb::Vec3d> ends;
+  map.raytrace({openvdb::Vec3d(0.5, 0.5, 0.5), openvdb::Vec3d(0.5, 30.5, 0.5)},
+               {openvdb::Vec3d(2, 0, 0), openvdb::Vec3d(1, 0, 0)}, {20.0, 20.0}, oks, ends);
+  EXPECT_TRUE(oks[0]);
+  EXPECT_EQ(ends[0].x(), 12.0);
+  EXPECT_FALSE(oks[1]);  // no leaf on the ray: its end
+  EXPECT_EQ(ends[1].x(), 20.5);
+  EXPECT_EQ(ends[1].y(), 30.5);
+
+  OccupancyVDBMapping fast(1.0);
+  Config c    = test_config(30);
+  c.fast_mode = true;
+  fast.setConfig(c);
+  fast.addInputSource("lidar", 30, 0);
+  fast.insertPointCloud(cloud_of({{12.f, 0.f, 0.f}}), origin, "lidar");  // empty map: the hit only
+  auto acc = fast.getGrid()->getAccessor();
+  EXPECT_EQ(acc.getValue(openvdb::Coord(5, 0, 0)), 0.0f);
+  EXPECT_TRUE(acc.isValueOn(openvdb::Coord(12, 0, 0)));
+  fast.insertPointCloud(cloud_of({{14.f, 0.f, 0.f}}), origin, "lidar");  // a miss on the active voxel only
+  EXPECT_EQ(acc.getValue(openvdb::Coord(12, 0, 0)), 0.0f);
+  EXPECT_EQ(acc.getValue(openvdb::Coord(13, 0, 0)), 0.0f);
+  EXPECT_EQ(acc.getValue(openvdb::Coord(5, 0, 0)), 0.0f);
+  EXPECT_EQ(acc.getValue(openvdb::Coord(14, 0, 0)), logodds(0.9));
+}
+
 int main(int argc, char** argv)
 {
   ::testing::InitGoogleTest(&argc, argv);

@@ -17,9 +17,15 @@
 //              OccupancyVDBMapping.hpp:92-117  thresholds, clamp, active mask;
 //                                       clears the update masks
 //   k_rehash   (none)                   rebuilds the block hash after growth
+//   k_topo_build VDBMapping.hpp:1436-1449  the volume ray intersector's view of
+//                                       the map: node sets and active-leaf box
+//   k_fast_mark VDBMapping.hpp:577-602  fast mode: active map voxels along the
+//                                       intersector's spans of each ray
+//   k_raytrace VDBMapping.hpp:675-721   raytrace queries
 #pragma once
 
 #include "device_common.cuh"
+#include "hdda.cuh"
 
 namespace vdbg {
 
@@ -1455,6 +1461,264 @@ __global__ void k_section_clear_voxels(MapView m, const int4* __restrict__ pts, 
   const int off = ((p.z & 7) << 6) | ((p.y & 7) << 3) | (p.x & 7);
   values[static_cast<size_t>(slot) * 512 + off] = 0.0f;
   atomicAnd(active + static_cast<size_t>(slot) * 8 + (off >> 6), ~(1ull << (off & 63)));
+}
+
+// ---------------------------------------------------------------------------
+// Fast mode and raytrace queries: the volume ray intersector
+// (VDBMapping.hpp:1436-1449) over the map's leaves as they are at the call
+// (the integrated ones, flags set). Nodes of 128^3 and 4096^3 voxels hold a
+// leaf exactly when one of the map's leaves lies in them; they go to two
+// open-addressing key sets built per call, leaf cells are looked up in the
+// map's own block hash.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kErrTopoFull = 128u;  // a node set ran out of probes (set size >= 2x the leaves)
+
+struct TopoView
+{
+  unsigned long long* key1;  // 128^3-voxel nodes: pack_leaf_key(map, v >> 7)
+  unsigned long long* key2;  // 4096^3-voxel nodes: pack_leaf_key(map, v >> 12)
+  uint32_t mask;             // set capacity - 1 (both sets)
+  int* box;                  // [6] min xyz, max xyz (inclusive) of the leaves with an active voxel
+  uint32_t* count;           // [0] the map's leaves, [1] nonzero when an insert failed
+  int map;
+};
+
+__device__ __forceinline__ bool topo_insert(unsigned long long* keys, uint32_t mask, unsigned long long key)
+{
+  uint32_t h = static_cast<uint32_t>(mix64(key)) & mask;
+  for (uint32_t probe = 0; probe < kMaxProbes; ++probe)
+  {
+    const unsigned long long k = keys[h];
+    if (k == key) return true;
+    if (k == kEmptyKey)
+    {
+      const unsigned long long prev = atomicCAS(keys + h, kEmptyKey, key);
+      if (prev == kEmptyKey || prev == key) return true;
+    }
+    h = (h + 1) & mask;
+  }
+  return false;
+}
+
+__device__ __forceinline__ bool topo_find(const unsigned long long* keys, uint32_t mask, unsigned long long key)
+{
+  uint32_t h = static_cast<uint32_t>(mix64(key)) & mask;
+  for (uint32_t probe = 0; probe < kMaxProbes; ++probe)
+  {
+    const unsigned long long k = __ldg(keys + h);
+    if (k == key) return true;
+    if (k == kEmptyKey) return false;
+    h = (h + 1) & mask;
+  }
+  return false;
+}
+
+// box = (INT_MAX x3, INT_MIN x3), counts 0: the empty CoordBBox of an
+// intersector on a map without active voxels.
+__global__ void k_topo_init(TopoView tv)
+{
+  if (threadIdx.x < 3) tv.box[threadIdx.x] = 0x7fffffff;
+  if (threadIdx.x >= 3 && threadIdx.x < 6) tv.box[threadIdx.x] = static_cast<int>(0x80000000u);
+  if (threadIdx.x < 2) tv.count[threadIdx.x] = 0u;
+}
+
+// One thread per leaf slot: the integrated leaves of map tv.map enter the node
+// sets; those with an active voxel widen the box.
+__global__ void __launch_bounds__(256) k_topo_build(const int4* __restrict__ origin,
+                                                    const uint32_t* __restrict__ flags,
+                                                    const unsigned long long* __restrict__ active, uint32_t n,
+                                                    TopoView tv)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || flags[i] == 0u) return;
+  const int4 o = origin[i];
+  if (o.w != tv.map) return;
+  atomicAdd(tv.count, 1u);
+  const bool ok = topo_insert(tv.key1, tv.mask, pack_leaf_key(tv.map, o.x >> 7, o.y >> 7, o.z >> 7)) &&
+                  topo_insert(tv.key2, tv.mask, pack_leaf_key(tv.map, o.x >> 12, o.y >> 12, o.z >> 12));
+  if (!ok) atomicOr(tv.count + 1, 1u);
+  unsigned long long any = 0ull;
+  for (int w = 0; w < 8; ++w) any |= active[static_cast<size_t>(i) * 8 + w];
+  if (!any) return;
+  atomicMin(tv.box + 0, o.x);
+  atomicMin(tv.box + 1, o.y);
+  atomicMin(tv.box + 2, o.z);
+  atomicMax(tv.box + 3, o.x + 7);
+  atomicMax(tv.box + 4, o.y + 7);
+  atomicMax(tv.box + 5, o.z + 7);
+}
+
+__device__ __forceinline__ bool voxel_in_map_range(const int v[3])
+{
+  return v[0] >= static_cast<int>(kVoxelMin) && v[0] < static_cast<int>(kVoxelMaxExcl) &&
+         v[1] >= static_cast<int>(kVoxelMin) && v[1] < static_cast<int>(kVoxelMaxExcl) &&
+         v[2] >= static_cast<int>(kVoxelMin) && v[2] < static_cast<int>(kVoxelMaxExcl);
+}
+
+// Block index of (bx, by, bz) of `map`, or -1 (read only).
+__device__ __forceinline__ int find_block(const MapView& m, int map, int bx, int by, int bz)
+{
+  const unsigned long long bkey = pack_leaf_key(map, bx, by, bz);
+  uint32_t h                    = static_cast<uint32_t>(mix64(bkey)) & m.bhmask;
+  for (uint32_t probe = 0; probe < kMaxProbes; ++probe)
+  {
+    const unsigned long long k = m.bkeys[h];
+    if (k == kEmptyKey) return -1;
+    if (k == bkey)
+    {
+      const int b = m.bslots[h];
+      return b >= 0 ? b : -1;
+    }
+    h = (h + 1) & m.bhmask;
+  }
+  return -1;
+}
+
+// The intersector's topology queries for hdda::walk (cell origins at each
+// level; outside the map's coordinate range nothing exists).
+struct DevTopo
+{
+  TopoView tv;
+  MapView m;
+  const uint32_t* flags;
+  __device__ __forceinline__ bool has2(const int v[3]) const
+  {
+    return voxel_in_map_range(v) && topo_find(tv.key2, tv.mask, pack_leaf_key(tv.map, v[0] >> 12, v[1] >> 12, v[2] >> 12));
+  }
+  __device__ __forceinline__ bool has1(const int v[3]) const
+  {
+    return voxel_in_map_range(v) && topo_find(tv.key1, tv.mask, pack_leaf_key(tv.map, v[0] >> 7, v[1] >> 7, v[2] >> 7));
+  }
+  __device__ __forceinline__ bool has0(const int v[3]) const
+  {
+    if (!voxel_in_map_range(v)) return false;
+    const int slot = find_leaf(m, tv.map, v[0] >> 3, v[1] >> 3, v[2] >> 3);
+    return slot >= 0 && flags[slot] != 0u;
+  }
+};
+
+// isValueOn of the map for voxels along one ray, remembering the last leaf
+// (its block and slot, -1 when absent).
+struct ActiveCache
+{
+  const MapView* m;
+  const unsigned long long* active;
+  int map;
+  int lx, ly, lz;
+  int b, slot;
+  __device__ __forceinline__ bool operator()(const int v[3])
+  {
+    const int x = v[0] >> 3, y = v[1] >> 3, z = v[2] >> 3;
+    if (x != lx || y != ly || z != lz)
+    {
+      lx   = x;
+      ly   = y;
+      lz   = z;
+      b    = voxel_in_map_range(v) ? find_block(*m, map, x >> 3, y >> 3, z >> 3) : -1;
+      slot = b >= 0 ? m->bleaf[static_cast<size_t>(b) * 512 + (((x & 7) << 6) | ((y & 7) << 3) | (z & 7))] : -1;
+      if (slot < 0) slot = -1;
+    }
+    if (slot < 0) return false;
+    const int off = ((v[2] & 7) << 6) | ((v[1] & 7) << 3) | (v[0] & 7);
+    return (active[static_cast<size_t>(slot) * 8 + (off >> 6)] >> (off & 63)) & 1ull;
+  }
+};
+
+__device__ __forceinline__ hdda::Box topo_box(const TopoView& tv)
+{
+  hdda::Box b;
+  for (int a = 0; a < 3; ++a)
+  {
+    b.lo[a]      = tv.box[a];
+    b.hi_excl[a] = tv.box[3 + a] + 1;  // mBBox.max().offset(1)
+  }
+  return b;
+}
+
+// Fast mode (castRayIntoGridFast, VDBMapping.hpp:577-602, called by
+// raycastPointCloud VDBMapping.hpp:520-526 when the map is not empty): one
+// thread per valid ray marks, as visited in the update grid, the voxels of the
+// intersector's spans that are active in the map. Those voxels' leaves exist,
+// so nothing is allocated. The prep stage counted the castRayIntoGrid visits
+// of the ray; they are replaced by the marks made here.
+__global__ void __launch_bounds__(128) k_fast_mark(const int4* __restrict__ rays, const int* __restrict__ order,
+                                                   ScanTable t, MapView m, ChannelView c, TopoView tv,
+                                                   const uint32_t* __restrict__ flags,
+                                                   const unsigned long long* __restrict__ active)
+{
+  if (ld_relaxed_u32(&m.st->error) != 0u) return;
+  c.cur_epoch = *c.epoch;
+  const uint32_t nv = m.st->n_valid;
+  const uint32_t j  = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nv) return;
+  if (tv.count[1] != 0u)
+  {
+    atomicOr(&m.st->error, kErrTopoFull);
+    return;
+  }
+  const int ri             = order[j];
+  const int4 r             = rays[ri];
+  const uint32_t l1        = static_cast<uint32_t>(r.w) & kMetaL1Mask;
+  const ScanGeom& g        = scan_geom(t, scan_of_ray(t, static_cast<uint32_t>(ri)));
+  unsigned long long marks = 0ull;
+  if (tv.count[0] != 0u)
+  {
+    const int o[3] = {g.ovx, g.ovy, g.ovz};
+    const int e[3] = {r.x, r.y, r.z};
+    DevTopo topo{tv, m, flags};
+    ActiveCache act{&m, active, tv.map, 0x7fffffff, 0, 0, -1, -1};
+    uint32_t steps = 0;
+    const int st   = hdda::fast_cast_one(o, e, topo_box(tv), topo, act,
+                                         [&](const int v[3]) {
+                                           // act holds v's leaf: active() just found the voxel on.
+                                           const int b    = act.b;
+                                           const int cell = ((act.lx & 7) << 6) | ((act.ly & 7) << 3) | (act.lz & 7);
+                                           touch_block(c, b);
+                                           unsigned long long* bt = c.btouched + static_cast<size_t>(b) * 8 + (cell >> 6);
+                                           if (!((*bt >> (cell & 63)) & 1ull)) atomicOr(bt, 1ull << (cell & 63));
+                                           const int off = ((v[2] & 7) << 6) | ((v[1] & 7) << 3) | (v[0] & 7);
+                                           atomicOr(c.upd + static_cast<size_t>(act.slot) * 16 + (off >> 6),
+                                                    1ull << (off & 63));
+                                           ++marks;
+                                         },
+                                         steps);
+    if (st == hdda::kTraceBound) atomicOr(&m.st->error, kErrStepBound);
+  }
+  const unsigned long long dda_visits = l1 > 0u ? l1 + 1ull : 0ull;
+  if (marks != dda_visits) atomicAdd(&m.st->visits, marks - dda_visits);
+}
+
+// raytrace (VDBMapping.hpp:675-721), one thread per query: q holds the
+// origins [n][3], then the directions [n][3], then the lengths [n]; ok[n] and
+// end[n][3] receive success and end point. A query outside the +-2^30 index
+// box sets kErrCoordRange.
+__global__ void __launch_bounds__(128) k_raytrace(const double* __restrict__ q, uint32_t n, double res,
+                                                  double inv_res, MapView m, TopoView tv,
+                                                  const uint32_t* __restrict__ flags,
+                                                  const unsigned long long* __restrict__ active,
+                                                  unsigned char* __restrict__ ok, double* __restrict__ end)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (tv.count[1] != 0u)
+  {
+    atomicOr(&m.st->error, kErrTopoFull);
+    return;
+  }
+  const double o[3] = {q[3 * static_cast<size_t>(i)], q[3 * static_cast<size_t>(i) + 1], q[3 * static_cast<size_t>(i) + 2]};
+  const double* dq  = q + 3 * static_cast<size_t>(n);
+  const double d[3] = {dq[3 * static_cast<size_t>(i)], dq[3 * static_cast<size_t>(i) + 1], dq[3 * static_cast<size_t>(i) + 2]};
+  const double len  = q[6 * static_cast<size_t>(n) + i];
+  DevTopo topo{tv, m, flags};
+  ActiveCache act{&m, active, tv.map, 0x7fffffff, 0, 0, -1, -1};
+  bool success   = false;
+  double e[3]    = {0.0, 0.0, 0.0};
+  uint32_t steps = 0;
+  const int st   = hdda::raytrace_one(o, d, len, res, inv_res, topo_box(tv), topo, act, success, e, steps);
+  if (st == hdda::kTraceRange) atomicOr(&m.st->error, kErrCoordRange);
+  if (st == hdda::kTraceBound) atomicOr(&m.st->error, kErrStepBound);
+  ok[i] = success ? 1 : 0;
+  for (int a = 0; a < 3; ++a) end[3 * static_cast<size_t>(i) + a] = e[a];
 }
 
 } // namespace vdbg

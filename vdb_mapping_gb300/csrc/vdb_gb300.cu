@@ -145,6 +145,14 @@ struct vdbg_map
   int64_t graph_stride             = 0;
   uint64_t graph_captures          = 0;
   uint64_t graph_replays           = 0;
+  // The volume ray intersector's view of one map (fast mode, raytrace),
+  // rebuilt by every call that uses it: two node sets of topo_cap keys, the
+  // box and counts; and the raytrace queries' device copy.
+  unsigned long long* topo_keys    = nullptr;  // [2 * topo_cap]
+  uint32_t topo_cap                = 0;
+  int* topo_box                    = nullptr;  // [8]: box[6], then two counts
+  char* d_trace                    = nullptr;
+  size_t trace_bytes               = 0;
 };
 
 namespace {
@@ -1074,6 +1082,92 @@ int discard_marking(vdbg_map* m, Channel& c, cudaStream_t s)
 
 // The scans to cast in one call: the table and the status to report when a
 // scan could not be cast at all (an origin outside the index range).
+// The volume ray intersector of map `map` (VDBMapping.hpp:1436-1449) as the
+// map stands: node sets and box from its integrated leaves.
+int build_topology(vdbg_map* m, int map, cudaStream_t s, TopoView* tv)
+{
+  const uint32_t n = std::min(m->n_leaves, m->capacity);
+  uint32_t need    = 1024;
+  while (static_cast<uint64_t>(need) < 2ull * n && need < (1u << 31)) need <<= 1;
+  if (need > m->topo_cap)
+  {
+    dev_free(m, m->topo_keys, 2 * static_cast<size_t>(m->topo_cap));
+    m->topo_cap = 0;
+    VDBG_TRY(dev_alloc(m, &m->topo_keys, 2 * static_cast<size_t>(need)));
+    m->topo_cap = need;
+  }
+  if (!m->topo_box) VDBG_TRY(dev_alloc(m, &m->topo_box, 8));
+  tv->key1  = m->topo_keys;
+  tv->key2  = m->topo_keys + m->topo_cap;
+  tv->mask  = m->topo_cap - 1;
+  tv->box   = m->topo_box;
+  tv->count = reinterpret_cast<uint32_t*>(m->topo_box + 6);
+  tv->map   = map;
+  VDBG_CUDA(cudaMemsetAsync(m->topo_keys, 0xff, 2 * static_cast<size_t>(m->topo_cap) * sizeof(unsigned long long), s));
+  k_topo_init<<<1, 32, 0, s>>>(*tv);
+  if (n > 0) k_topo_build<<<(n + 255) / 256, 256, 0, s>>>(m->origin, m->flags, m->active, n, *tv);
+  VDBG_CUDA(cudaGetLastError());
+  m->timings.launches += n > 0 ? 2 : 1;
+  return VDBG_OK;
+}
+
+// Fast mode (raycastPointCloud VDBMapping.hpp:520-526 with
+// castRayIntoGridFast :577-602) for the rays of the call, into channel `c`:
+// the intersector, the marks of the active voxels along its spans, then the
+// endpoint hits. Only the hits allocate, so a pool or hash that runs out
+// grows and the hits run again (idempotent ORs).
+int run_fast_marking(vdbg_map* m, Channel& c, const int4* rays, const int* order, int64_t n, const ScanTable& t,
+                     cudaStream_t s)
+{
+  TopoView tv;
+  VDBG_TRY(build_topology(m, 0, s, &tv));
+  const unsigned hit_blocks = static_cast<unsigned>((n + 255) / 256);
+  k_fast_mark<<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(rays, order, t, map_view(m), channel_view(c), tv,
+                                                                     m->flags, m->active);
+  k_mark_hits<<<hit_blocks, 256, 0, s>>>(rays, order, t, map_view(m), channel_view(c));
+  VDBG_CUDA(cudaGetLastError());
+  m->timings.launches += 2;
+  VDBG_TRY(fetch_status(m, s));
+  for (int attempt = 0; m->h_status->error != 0u; ++attempt)
+  {
+    const uint32_t err = m->h_status->error;
+    m->n_leaves        = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
+    m->n_blocks        = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
+    if (err & kErrCoordRange)
+    {
+      // Nothing of the cloud was cast (the prep stage flagged it).
+      clear_error_keep_counters(m);
+      VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+      VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
+      VDBG_CUDA(cudaStreamSynchronize(s));
+      return VDBG_ERR_COORD_RANGE;
+    }
+    if (err & (kErrSpin | kErrStepBound | kErrTopoFull)) return map_error(err);
+    if (attempt >= 40) return VDBG_ERR_OUT_OF_MEMORY;
+    if (err & kErrPoolFull) VDBG_TRY(grow_for(m, m->h_status->n_leaves));
+    if (err & kErrBlockFull) VDBG_TRY(grow_blocks_for(m, m->h_status->n_blocks));
+    if ((err & kErrHashFull) && !(err & kErrBlockFull)) VDBG_TRY(rebuild_hash(m, m->bhash_size * 2, m->n_blocks));
+    if (m->n_blocks > 0)
+    {
+      k_reset_failed_leaves<<<m->num_sms * 4, 256, 0, m->stream>>>(m->bleaf, static_cast<size_t>(m->n_blocks) * 512);
+      VDBG_CUDA(cudaGetLastError());
+    }
+    VDBG_CUDA(cudaStreamSynchronize(m->stream));
+    clear_error_keep_counters(m);
+    VDBG_CUDA(cudaMemcpyAsync(m->d_status, m->h_status, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+    k_mark_hits<<<hit_blocks, 256, 0, s>>>(rays, order, t, map_view(m), channel_view(c));
+    VDBG_CUDA(cudaGetLastError());
+    m->timings.launches += 1;
+    m->timings.retries += 1;
+    VDBG_TRY(fetch_status(m, s));
+  }
+  m->n_leaves = std::min<uint32_t>(m->h_status->n_leaves, m->capacity);
+  m->n_blocks = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
+  VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
+  m->timings.passes = 0;
+  return VDBG_OK;
+}
+
 struct CastPlan
 {
   ScanTable table{};
@@ -1243,7 +1337,8 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
     }
     const RunBuffer rb =
       run_buffer(m, m->run_key, m->run_bits, m->run_slab, m->run_count, m->run_prefix, m->run_seg, m->dda_warps);
-    const bool graphed = m->use_graph && m->batch && t.n > 1 && !m->track_changes && integrate_all &&
+    const bool fast    = !m->batch && m->conf[0].fast_mode;
+    const bool graphed = !fast && m->use_graph && m->batch && t.n > 1 && !m->track_changes && integrate_all &&
                          m->channels.size() == 1 && src == &m->channels[0];
     int d = VDBG_OK;
     if (graphed)
@@ -1257,6 +1352,12 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
         VDBG_TRY(maybe_grow_ahead(m));
         return call_status;
       }
+    }
+    else if (fast)
+    {
+      VDBG_TRY(launch_prep(m, *src, xyz, n, stride, t, flags, s, m->d_pts, m->d_rays, m->d_ray_scan, m->d_order,
+                           m->d_hist, m->d_cursor));
+      d = run_fast_marking(m, *src, m->d_rays, m->d_order, n, t, s);
     }
     else
     {
@@ -1659,6 +1760,9 @@ int vdbg_destroy(vdbg_map* m)
   dev_free(m, m->run_prefix, static_cast<size_t>(m->dda_warps) + 2);
   dev_free(m, m->lstate, static_cast<size_t>(m->dda_warps) * 32);
   dev_free(m, m->wstate, m->dda_warps);
+  dev_free(m, m->topo_keys, 2 * static_cast<size_t>(m->topo_cap));
+  dev_free(m, m->topo_box, 8);
+  dev_free(m, m->d_trace, m->trace_bytes);
   if (m->h_status) cudaFreeHost(m->h_status);
   if (m->ev0) cudaEventDestroy(m->ev0);
   if (m->ev1) cudaEventDestroy(m->ev1);
@@ -2036,6 +2140,8 @@ int vdbg_create_batch(int n_maps, const double* resolutions, const vdbg_options*
 int vdbg_batch_set_config(vdbg_map* m, int map, const vdbg_config* c)
 {
   if (!m || !c || !m->batch || map < 0 || map >= static_cast<int>(m->conf.size())) return VDBG_ERR_INVALID_ARGUMENT;
+  // Fast mode is cast per map call (vdbg_insert_point_cloud), not batched.
+  if (c->fast_mode) return VDBG_ERR_INVALID_ARGUMENT;
   return set_config_impl(m, map, c);
 }
 
@@ -2155,6 +2261,48 @@ int reserve_for(vdbg_map* m, int64_t n)
 } // namespace
 
 extern "C" {
+
+int vdbg_raytrace(vdbg_map* m, int map, int64_t n, const double* origins, const double* directions,
+                  const double* max_lengths, uint8_t* successes, double* end_points)
+{
+  int mp = 0;
+  if (!m || n < 0 || !section_map(m, map, &mp) ||
+      (n > 0 && (!origins || !directions || !max_lengths || !successes || !end_points)))
+    return VDBG_ERR_INVALID_ARGUMENT;
+  if (n > (int64_t(1) << 28)) return VDBG_ERR_SIZE_LIMIT;
+  if (n == 0) return VDBG_OK;
+  cudaStream_t s = m->stream;
+  VDBG_TRY(begin_call(m, s));
+  const size_t nn    = static_cast<size_t>(n);
+  const size_t bytes = nn * 10 * sizeof(double) + ((nn + 15) & ~static_cast<size_t>(15));
+  if (bytes > m->trace_bytes)
+  {
+    dev_free(m, m->d_trace, m->trace_bytes);
+    m->trace_bytes = 0;
+    VDBG_TRY(dev_alloc(m, &m->d_trace, bytes));
+    m->trace_bytes = bytes;
+  }
+  double* q         = reinterpret_cast<double*>(m->d_trace);
+  double* end       = q + 7 * nn;
+  unsigned char* ok = reinterpret_cast<unsigned char*>(q + 10 * nn);
+  VDBG_CUDA(cudaMemcpyAsync(q, origins, 3 * nn * sizeof(double), cudaMemcpyHostToDevice, s));
+  VDBG_CUDA(cudaMemcpyAsync(q + 3 * nn, directions, 3 * nn * sizeof(double), cudaMemcpyHostToDevice, s));
+  VDBG_CUDA(cudaMemcpyAsync(q + 6 * nn, max_lengths, nn * sizeof(double), cudaMemcpyHostToDevice, s));
+  TopoView tv;
+  VDBG_TRY(build_topology(m, mp, s, &tv));
+  const MapConf& mc = m->conf[mp];
+  k_raytrace<<<static_cast<unsigned>((nn + 127) / 128), 128, 0, s>>>(q, static_cast<uint32_t>(nn), mc.resolution,
+                                                                     mc.inv_res, map_view(m), tv, m->flags,
+                                                                     m->active, ok, end);
+  VDBG_CUDA(cudaGetLastError());
+  m->timings.launches += 1;
+  VDBG_CUDA(cudaMemcpyAsync(end_points, end, 3 * nn * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VDBG_CUDA(cudaMemcpyAsync(successes, ok, nn, cudaMemcpyDeviceToHost, s));
+  VDBG_TRY(fetch_status(m, s));
+  record_timings(m);
+  if (m->h_status->error != 0u) return map_error(m->h_status->error);
+  return VDBG_OK;
+}
 
 int vdbg_export_section(vdbg_map* m, int map, const int32_t lo[3], const int32_t hi[3], int full, int64_t capacity,
                         int32_t* origins, float* values, uint64_t* masks, int64_t* n_out)
@@ -2475,6 +2623,8 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
                                                void* stream, vdbg_scan_stats* stats)
 {
   if (!m || m->batch || !origin || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
+  // Fast mode builds the intersector's node sets, which allocates.
+  if (m->conf[0].fast_mode) return VDBG_ERR_INVALID_ARGUMENT;
   if (stats) std::memset(stats, 0, sizeof(*stats));
   const bool host_input = (flags & VDBG_POINTS_DEVICE) == 0;
   if (n > kNoAllocMaxPoints || (host_input && stride > 16)) return VDBG_ERR_SIZE_LIMIT;

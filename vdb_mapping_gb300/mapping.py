@@ -215,6 +215,20 @@ def _section_values(lib, h, map_index, origins, values, masks, check):
           "vdbg_apply_section_values")
 
 
+def _raytrace(lib, h, map_index, origins, directions, max_lengths, check):
+    o = np.ascontiguousarray(np.asarray(origins, np.float64).reshape(-1, 3))
+    d = np.ascontiguousarray(np.asarray(directions, np.float64).reshape(-1, 3))
+    n = o.shape[0]
+    if d.shape[0] != n:
+        raise ValueError("origins and directions differ in length")
+    ln = np.ascontiguousarray(np.broadcast_to(np.asarray(max_lengths, np.float64), (n,)))
+    ok = np.zeros(n, np.uint8)
+    ends = np.zeros((n, 3), np.float64)
+    check(lib.vdbg_raytrace(h, int(map_index), n, o.ctypes.data, d.ctypes.data, ln.ctypes.data, ok.ctypes.data,
+                            ends.ctypes.data), "vdbg_raytrace")
+    return ok.astype(bool), ends
+
+
 class OccupancyVDBMapping:
     """vdb_mapping::OccupancyVDBMapping (OccupancyVDBMapping.hpp:46-200) on the GPU."""
 
@@ -412,6 +426,12 @@ class OccupancyVDBMapping:
         """applyMapSectionGrid (no smoothing)."""
         _section_values(self._lib, self._h, -1, origins, values, masks, self._check)
 
+    def raytrace(self, origins, directions, max_lengths):
+        """raytrace (VDBMapping.hpp:675-721) for n rays (world origins and
+        directions (n, 3), lengths (n,) or one length): (successes bool (n,),
+        end points (n, 3)). One ray: raytrace([o], [d], length)."""
+        return _raytrace(self._lib, self._h, -1, origins, directions, max_lengths, self._check)
+
     def exportChanges(self):
         """Change set of the last integration: (origins, active, value) per leaf
         with a flip, sorted by origin; `value` marks voxels flipped on by a hit."""
@@ -591,6 +611,10 @@ class MapBatch:
 
     def applyMapSectionValues(self, map_index: int, origins, values, masks) -> None:
         _section_values(self._lib, self._h, map_index, origins, values, masks, self._check)
+
+    def raytrace(self, map_index: int, origins, directions, max_lengths):
+        """raytrace on one map of the batch (see OccupancyVDBMapping.raytrace)."""
+        return _raytrace(self._lib, self._h, map_index, origins, directions, max_lengths, self._check)
 
     def exportChanges(self, map_index: int):
         """Change set of the last batched insert for one map."""
