@@ -14,6 +14,9 @@
 //   include/vdb_mapping/VDBMapping.hpp:316-406    accumulate / integrate / insert
 //   include/vdb_mapping/VDBMapping.hpp:1352-1375  addInputSource
 //   include/vdb_mapping/VDBMapping.hpp:1456-1469  VDBMapping::setConfig
+//   include/vdb_mapping/VDBMapping.hpp:577-602    castRayIntoGridFast (fast mode)
+//   include/vdb_mapping/VDBMapping.hpp:646-721    raytrace
+//   include/vdb_mapping/VDBMapping.hpp:1436-1449  updateVolumeRayIntersectors
 //   include/vdb_mapping/OccupancyVDBMapping.hpp:59-117  log-odds constants and node updates
 // plus the OpenVDB arithmetic those lines call (OpenVDB is a third-party
 // dependency that is not vendored in the reference; README.md:11 asks for
@@ -27,6 +30,8 @@
 //   Vec3d::length / unit     sqrt((x*x + y*y) + z*z), component-wise division
 //   Tree4<.,5,4,3> leaves    8^3 voxels, offset = (x&7)<<6 | (y&7)<<3 | (z&7),
 //                            background 0.0f, leaves are never pruned here
+//   tools::VolumeRayIntersector, math::VolumeHDDA, Vec3d::normalize: see
+//                            class Intersector and OccupancyMap::raytrace
 //
 // Parity pins: the reference's own tests/mapping.cpp compiles unmodified
 // against oracle/refshim (this header behind the reference class names) and
