@@ -2290,11 +2290,14 @@ int vdbg_raytrace(vdbg_map* m, int map, int64_t n, const double* origins, const 
   VDBG_CUDA(cudaMemcpyAsync(q + 6 * nn, max_lengths, nn * sizeof(double), cudaMemcpyHostToDevice, s));
   TopoView tv;
   VDBG_TRY(build_topology(m, mp, s, &tv));
+  VDBG_CUDA(cudaEventRecord(m->ev_prep, s));  // timings: prep = copies in + intersector, dda = queries
+  m->timed_prep     = true;
   const MapConf& mc = m->conf[mp];
   k_raytrace<<<static_cast<unsigned>((nn + 127) / 128), 128, 0, s>>>(q, static_cast<uint32_t>(nn), mc.resolution,
                                                                      mc.inv_res, map_view(m), tv, m->flags,
                                                                      m->active, ok, end);
   VDBG_CUDA(cudaGetLastError());
+  VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
   m->timings.launches += 1;
   VDBG_CUDA(cudaMemcpyAsync(end_points, end, 3 * nn * sizeof(double), cudaMemcpyDeviceToHost, s));
   VDBG_CUDA(cudaMemcpyAsync(successes, ok, nn, cudaMemcpyDeviceToHost, s));
