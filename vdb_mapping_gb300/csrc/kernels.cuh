@@ -1575,12 +1575,15 @@ __device__ __forceinline__ int find_block(const MapView& m, int map, int bx, int
 }
 
 // The intersector's topology queries for hdda::walk (cell origins at each
-// level; outside the map's coordinate range nothing exists).
+// level; outside the map's coordinate range nothing exists). Leaf cells
+// remember the last 64^3 block looked up: consecutive leaf cells of a ray
+// mostly share one.
 struct DevTopo
 {
   TopoView tv;
   MapView m;
   const uint32_t* flags;
+  mutable int cbx, cby, cbz, cb;  // last block coordinate and its index (-1: none)
   __device__ __forceinline__ bool has2(const int v[3]) const
   {
     return voxel_in_map_range(v) && topo_find(tv.key2, tv.mask, pack_leaf_key(tv.map, v[0] >> 12, v[1] >> 12, v[2] >> 12));
@@ -1592,13 +1595,25 @@ struct DevTopo
   __device__ __forceinline__ bool has0(const int v[3]) const
   {
     if (!voxel_in_map_range(v)) return false;
-    const int slot = find_leaf(m, tv.map, v[0] >> 3, v[1] >> 3, v[2] >> 3);
+    const int bx = v[0] >> 6, by = v[1] >> 6, bz = v[2] >> 6;
+    if (bx != cbx || by != cby || bz != cbz)
+    {
+      cbx = bx;
+      cby = by;
+      cbz = bz;
+      cb  = find_block(m, tv.map, bx, by, bz);
+    }
+    if (cb < 0) return false;
+    const int cell = (((v[0] >> 3) & 7) << 6) | (((v[1] >> 3) & 7) << 3) | ((v[2] >> 3) & 7);
+    const int slot = m.bleaf[static_cast<size_t>(cb) * 512 + cell];
     return slot >= 0 && flags[slot] != 0u;
   }
 };
 
 // isValueOn of the map for voxels along one ray, remembering the last leaf
-// (its block and slot, -1 when absent).
+// (its block and slot, -1 when absent) and the active word of the z-plane
+// last read (a near-horizontal ray stays in one plane of a leaf for many
+// voxels).
 struct ActiveCache
 {
   const MapView* m;
@@ -1606,6 +1621,8 @@ struct ActiveCache
   int map;
   int lx, ly, lz;
   int b, slot;
+  int wz;                   // plane (z & 7) held in `word`, -1 none
+  unsigned long long word;  // active bits of plane wz of leaf `slot`
   __device__ __forceinline__ bool operator()(const int v[3])
   {
     const int x = v[0] >> 3, y = v[1] >> 3, z = v[2] >> 3;
@@ -1617,10 +1634,16 @@ struct ActiveCache
       b    = voxel_in_map_range(v) ? find_block(*m, map, x >> 3, y >> 3, z >> 3) : -1;
       slot = b >= 0 ? m->bleaf[static_cast<size_t>(b) * 512 + (((x & 7) << 6) | ((y & 7) << 3) | (z & 7))] : -1;
       if (slot < 0) slot = -1;
+      wz = -1;
     }
     if (slot < 0) return false;
-    const int off = ((v[2] & 7) << 6) | ((v[1] & 7) << 3) | (v[0] & 7);
-    return (active[static_cast<size_t>(slot) * 8 + (off >> 6)] >> (off & 63)) & 1ull;
+    const int pz = v[2] & 7;
+    if (pz != wz)
+    {
+      word = active[static_cast<size_t>(slot) * 8 + pz];
+      wz   = pz;
+    }
+    return (word >> (((v[1] & 7) << 3) | (v[0] & 7))) & 1ull;
   }
 };
 
@@ -1665,8 +1688,8 @@ __global__ void __launch_bounds__(128) k_fast_mark(const int4* __restrict__ rays
   {
     const int o[3] = {g.ovx, g.ovy, g.ovz};
     const int e[3] = {r.x, r.y, r.z};
-    DevTopo topo{tv, m, flags};
-    ActiveCache act{&m, active, tv.map, 0x7fffffff, 0, 0, -1, -1};
+    DevTopo topo{tv, m, flags, 0x7fffffff, 0, 0, -1};
+    ActiveCache act{&m, active, tv.map, 0x7fffffff, 0, 0, -1, -1, -1, 0ull};
     uint32_t steps = 0;
     const int st   = hdda::fast_cast_one(o, e, topo_box(tv), topo, act,
                                          [&](const int v[3]) {
@@ -1709,8 +1732,8 @@ __global__ void __launch_bounds__(128) k_raytrace(const double* __restrict__ q, 
   const double* dq  = q + 3 * static_cast<size_t>(n);
   const double d[3] = {dq[3 * static_cast<size_t>(i)], dq[3 * static_cast<size_t>(i) + 1], dq[3 * static_cast<size_t>(i) + 2]};
   const double len  = q[6 * static_cast<size_t>(n) + i];
-  DevTopo topo{tv, m, flags};
-  ActiveCache act{&m, active, tv.map, 0x7fffffff, 0, 0, -1, -1};
+  DevTopo topo{tv, m, flags, 0x7fffffff, 0, 0, -1};
+  ActiveCache act{&m, active, tv.map, 0x7fffffff, 0, 0, -1, -1, -1, 0ull};
   bool success   = false;
   double e[3]    = {0.0, 0.0, 0.0};
   uint32_t steps = 0;
