@@ -164,13 +164,12 @@ struct Dda
 };
 
 // Index of the smallest of three values, ties to the higher index
-// (math::MinIndex).
+// (math::MinIndex; the values are never NaN here). Constant indices only, so
+// the DDA state stays in registers.
 VDBG_HD int min_index(const double v[3])
 {
-  int a = 2;
-  if (v[1] < v[a]) a = 1;
-  if (v[0] < v[a]) a = 0;
-  return a;
+  if (v[0] < v[1]) return v[0] < v[2] ? 0 : 2;
+  return v[1] < v[2] ? 1 : 2;
 }
 
 // DDA::init(ray, t0, t1). The caller guarantees |ray(t0)| < 2^30 per axis.
