@@ -18,8 +18,10 @@
 //     the only specialisation the reference ships (OccupancyVDBMapping.hpp).
 // Map sections are provided (getMapSection*, applyMapSection*, the
 // bounding-box helpers; VDBMapping.hpp:811-1085) without the morphological
-// smoothing option. Other parts of the reference outside the insertion path
-// (morphology, artificial areas, file I/O, ray queries, fast mode) are not.
+// smoothing option, and so are fast mode (VDBMapping.hpp:577-602, through
+// Config::fast_mode) and the raytrace queries (VDBMapping.hpp:646-721). Other
+// parts of the reference outside the insertion path (morphology, artificial
+// areas, file I/O, the remote-mapping byte arrays) are not.
 #ifndef VDB_MAPPING_GB300_VDB_MAPPING_HPP
 #define VDB_MAPPING_GB300_VDB_MAPPING_HPP
 
@@ -534,7 +536,8 @@ public:
     return true;
   }
 
-  /*! VDBMapping.hpp:466-539 (fast_mode off) into `update_grid_acc`'s grid. */
+  /*! VDBMapping.hpp:466-539 into `update_grid_acc`'s grid (castRayIntoGridFast
+   * in fast mode, :520-526). */
   bool raycastPointCloud(const typename PointCloudT::ConstPtr& cloud,
                          const Eigen::Matrix<double, 3, 1>& origin,
                          const double raycast_range,
