@@ -280,6 +280,24 @@ int vdbg_apply_section_states(vdbg_map* map, int map_index, const int32_t lo[3],
 int vdbg_apply_section_values(vdbg_map* map, int map_index, int64_t n, const int32_t* origins, const float* values,
                               const uint64_t* masks);
 
+/* Morphology of a map section's active voxels with the 26-neighbourhood:
+ * openvdb::tools::dilateActiveValues / erodeActiveValues with
+ * NN_FACE_EDGE_VERTEX as VDBMapping.hpp:1094-1147 calls them
+ * (morphologicalDilateMap op 0, ErodeMap 1, CloseMap 2 = dilate then erode,
+ * OpenMap 3 = erode then dilate, `iterations` steps each, 0..64). A dilation
+ * step activates every voxel with an active voxel among its 26 neighbours, an
+ * erosion step keeps the active voxels whose 26 neighbours are all active;
+ * voxels outside the leaves are inactive. Input: n leaves (origins multiples
+ * of 8 within +-2^20, masks in vdbg_export_leaves' layout; a repeated origin's
+ * masks are merged). Output: the leaves holding active voxels, sorted by
+ * origin, *n_out of them (VDBG_ERR_BUFFER_TOO_SMALL when capacity is less).
+ * Runs on the map's device and stream; the map is not changed.
+ * applyMapSectionUpdateGrid's smoothing (VDBMapping.hpp:1062-1065) is op 2
+ * before vdbg_apply_section_states. */
+int vdbg_section_morphology(vdbg_map* map, int op, int iterations, int64_t n, const int32_t* origins,
+                            const uint64_t* masks, int64_t capacity, int32_t* out_origins, uint64_t* out_masks,
+                            int64_t* n_out);
+
 /* VDBMapping::raytrace VDBMapping.hpp:675-721 (the single-ray overload,
  * :646-662, is n = 1) for the map (map_index -1) or map `map_index` of a
  * batch: n rays with world origins[n][3], directions[n][3] (normalised here)

@@ -32,6 +32,7 @@
 #include <limits>
 #include <map>
 #include <tuple>
+#include <type_traits>
 #include <memory>
 #include <mutex>
 #include <shared_mutex>
@@ -409,6 +410,14 @@ public:
       for (int w = 0; w < 8; ++w) out[i * 8 + w] = m_change_words[i * 16 + w];
     return out;
   }
+  /*! Value masks [n][8] (the bool values) in the same order. */
+  std::vector<uint64_t> valueMasks() const
+  {
+    std::vector<uint64_t> out(m_change_origins.size() / 3 * 8);
+    for (size_t i = 0; i < out.size() / 8; ++i)
+      for (int w = 0; w < 8; ++w) out[i * 8 + w] = m_change_words[i * 16 + 8 + w];
+    return out;
+  }
 
   // Internal: the hidden source id of this grid inside `map`.
   const std::string& bind(vdbg_map* map)
@@ -676,11 +685,12 @@ public:
     return g;
   }
 
-  /*! VDBMapping.hpp:1058-1085 without smoothing. */
+  /*! VDBMapping.hpp:1058-1085; smoothing closes the section's active voxels
+   * first (in place, as the reference does). */
   void applyMapSectionUpdateGrid(const typename UpdateGridT::Ptr section, bool smooth_map = false,
-                                 int /*smoothing_iterations*/ = 2)
+                                 int smoothing_iterations = 2)
   {
-    if (smooth_map) throw std::runtime_error("applyMapSectionUpdateGrid: smoothing is not provided");
+    if (smooth_map) morphologicalCloseMap<UpdateGridT>(section, smoothing_iterations);
     const openvdb::Vec3d bmin = section->template metaValue<openvdb::Vec3d>("bb_min");
     const openvdb::Vec3d bmax = section->template metaValue<openvdb::Vec3d>("bb_max");
     const int32_t lo[3] = {static_cast<int32_t>(std::floor(bmin.x())), static_cast<int32_t>(std::floor(bmin.y())),
@@ -766,6 +776,31 @@ public:
     end_point = e[0];
   }
 
+  /*! VDBMapping.hpp:1094-1147 on a section update grid, on the GPU
+   * (vdbg_section_morphology): the active voxels dilated / eroded with the
+   * 26-neighbourhood, values kept; leaves left without an active voxel are
+   * dropped. Value grids (GridT) are not supported. */
+  template <typename TGrid>
+  void morphologicalCloseMap(typename TGrid::Ptr grid, int iterations)
+  {
+    morphology<TGrid>(grid, 2, iterations);
+  }
+  template <typename TGrid>
+  void morphologicalOpenMap(typename TGrid::Ptr grid, int iterations)
+  {
+    morphology<TGrid>(grid, 3, iterations);
+  }
+  template <typename TGrid>
+  void morphologicalDilateMap(typename TGrid::Ptr grid, int iterations)
+  {
+    morphology<TGrid>(grid, 0, iterations);
+  }
+  template <typename TGrid>
+  void morphologicalErodeMap(typename TGrid::Ptr grid, int iterations)
+  {
+    morphology<TGrid>(grid, 1, iterations);
+  }
+
   /*! VDBMapping.hpp:1343. */
   std::shared_ptr<std::shared_mutex> getMapMutex() { return m_map_mutex; }
 
@@ -788,6 +823,34 @@ protected:
   static void check(int s, const char* where)
   {
     if (s != VDBG_OK) detail::throw_status(s, where);
+  }
+  template <typename TGrid>
+  void morphology(const typename TGrid::Ptr& grid, int op, int iterations)
+  {
+    static_assert(std::is_same<TGrid, UpdateGridT>::value,
+                  "morphology is provided for section update grids (UpdateGridT) only");
+    const std::vector<int32_t> o = grid->leafOrigins();
+    const std::vector<uint64_t> m = grid->activeMasks();
+    const std::vector<uint64_t> v = grid->valueMasks();
+    int64_t n = 0;
+    int s = vdbg_section_morphology(m_dev->map, op, iterations, static_cast<int64_t>(o.size() / 3), o.data(),
+                                    m.data(), 0, nullptr, nullptr, &n);
+    if (s != VDBG_OK && s != VDBG_ERR_BUFFER_TOO_SMALL) check(s, "vdbg_section_morphology");
+    std::vector<int32_t> ro(static_cast<size_t>(n) * 3);
+    std::vector<uint64_t> rm(static_cast<size_t>(n) * 8), rv(static_cast<size_t>(n) * 8, 0);
+    if (n > 0)
+      check(vdbg_section_morphology(m_dev->map, op, iterations, static_cast<int64_t>(o.size() / 3), o.data(),
+                                    m.data(), n, ro.data(), rm.data(), &n),
+            "vdbg_section_morphology");
+    std::map<std::tuple<int32_t, int32_t, int32_t>, size_t> old;
+    for (size_t i = 0; i < o.size() / 3; ++i) old[std::make_tuple(o[3 * i], o[3 * i + 1], o[3 * i + 2])] = i;
+    for (size_t i = 0; i < static_cast<size_t>(n); ++i)
+    {
+      const auto it = old.find(std::make_tuple(ro[3 * i], ro[3 * i + 1], ro[3 * i + 2]));
+      if (it != old.end())
+        for (int w = 0; w < 8; ++w) rv[i * 8 + w] = v[it->second * 8 + w];
+    }
+    grid->setChanges(std::move(ro), rm, rv);
   }
   static openvdb::Vec3d boxCorner(const openvdb::Coord& c)
   {

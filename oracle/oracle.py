@@ -50,6 +50,7 @@ def load():
         "vo_apply_section_states": (None, [P, P, P, I64, P, P]),
         "vo_apply_section_values": (None, [P, I64, P, P, P]),
         "vo_raytrace": (C.c_int, [P, I64, P, P, P, P, P]),
+        "vo_morphology": (I64, [I64, P, P, C.c_int, C.c_int, I64, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -228,6 +229,23 @@ def clip_quantise_variant(cloud, origin, max_range, res, w2i_divide=False, unit_
     lib.vo_clip_quantise_variant(arr.ctypes.data, n, stride, _d3(origin), float(max_range), float(res),
                                  int(w2i_divide), int(unit_reciprocal), rec.ctypes.data)
     return rec
+
+
+MORPH_OPS = {"dilate": 0, "erode": 1, "close": 2, "open": 3}
+
+
+def morphology(origins, masks, op, iterations):
+    """dilate / erode / close / open with the 26-neighbourhood (VDBMapping.hpp:1094-1147)
+    of leaves (origins (n,3), OpenVDB-order masks (n,8)): (origins, masks) sorted by origin."""
+    lib = load()
+    o = np.ascontiguousarray(np.asarray(origins, np.int32).reshape(-1, 3))
+    m = np.ascontiguousarray(np.asarray(masks, np.uint64).reshape(-1, 8))
+    n = lib.vo_morphology(len(o), o.ctypes.data, m.ctypes.data, MORPH_OPS[op], int(iterations), 0, None, None)
+    oo = np.zeros((n, 3), np.int32)
+    om = np.zeros((n, 8), np.uint64)
+    lib.vo_morphology(len(o), o.ctypes.data, m.ctypes.data, MORPH_OPS[op], int(iterations), n, oo.ctypes.data,
+                      om.ctypes.data)
+    return oo, om
 
 
 def bench_replicas(res, cfg, scans, origins, threads):

@@ -675,6 +675,78 @@ private:
                      std::numeric_limits<int32_t>::min()};
 };
 
+// openvdb::tools::dilateActiveValues / erodeActiveValues with
+// NN_FACE_EDGE_VERTEX (VDBMapping.hpp:1094-1147: morphologicalDilateMap,
+// ErodeMap, CloseMap = dilate then erode, OpenMap = erode then dilate), on the
+// active voxels of a set of leaves (OpenVDB is not vendored; restated from its
+// published definition): a dilation step activates every voxel with an active
+// voxel among its 26 neighbours, an erosion step keeps the active voxels whose
+// 26 neighbours are all active; voxels outside the set are inactive. Returns
+// the leaves holding active voxels (values left at the background), sorted by
+// origin.
+enum MorphOp : int
+{
+  kMorphDilate = 0,
+  kMorphErode  = 1,
+  kMorphClose  = 2,
+  kMorphOpen   = 3,
+};
+
+inline std::vector<MapLeaf> morphology(const std::vector<MapLeaf>& in, int op, int iterations)
+{
+  std::set<Coord> on;
+  for (const MapLeaf& l : in)
+    for (uint32_t off = 0; off < 512; ++off)
+      if ((l.on[off >> 6] >> (off & 63)) & 1ull)
+        on.insert(Coord(l.origin.x + static_cast<int32_t>(off >> 6), l.origin.y + static_cast<int32_t>((off >> 3) & 7),
+                        l.origin.z + static_cast<int32_t>(off & 7)));
+  auto dilate = [&]() {
+    std::set<Coord> out;
+    for (const Coord& v : on)
+      for (int dx = -1; dx <= 1; ++dx)
+        for (int dy = -1; dy <= 1; ++dy)
+          for (int dz = -1; dz <= 1; ++dz) out.insert(Coord(v.x + dx, v.y + dy, v.z + dz));
+    on.swap(out);
+  };
+  auto erode = [&]() {
+    std::set<Coord> out;
+    for (const Coord& v : on)
+    {
+      bool all = true;
+      for (int dx = -1; dx <= 1 && all; ++dx)
+        for (int dy = -1; dy <= 1 && all; ++dy)
+          for (int dz = -1; dz <= 1 && all; ++dz) all = on.count(Coord(v.x + dx, v.y + dy, v.z + dz)) != 0;
+      if (all) out.insert(v);
+    }
+    on.swap(out);
+  };
+  const bool dilate_first = op == kMorphDilate || op == kMorphClose;
+  const bool both         = op == kMorphClose || op == kMorphOpen;
+  for (int i = 0; i < iterations; ++i) dilate_first ? dilate() : erode();
+  if (both)
+    for (int i = 0; i < iterations; ++i) dilate_first ? erode() : dilate();
+  std::map<Coord, MapLeaf> leaves;
+  for (const Coord& v : on)
+  {
+    const Coord o = leaf_origin(v);
+    auto it       = leaves.find(o);
+    if (it == leaves.end())
+    {
+      MapLeaf l;
+      l.origin = o;
+      std::fill(l.value, l.value + 512, 0.0f);
+      std::memset(l.on, 0, sizeof(l.on));
+      it = leaves.emplace(o, l).first;
+    }
+    const uint32_t off = leaf_offset(v);
+    it->second.on[off >> 6] |= 1ull << (off & 63);
+  }
+  std::vector<MapLeaf> out;
+  out.reserve(leaves.size());
+  for (auto& kv : leaves) out.push_back(kv.second);
+  return out;
+}
+
 // Index coordinates a traversal may start from; outside, the call fails with
 // kCoordRange (beyond int32 the reference's Coord::floor is undefined).
 constexpr double kTraceLimit = 1073741824.0;  // 2^30

@@ -185,6 +185,31 @@ TEST(DropIn, MapSections)
   EXPECT_EQ(other.getGrid()->getAccessor().getValue(openvdb::Coord(12, 0, 0)), logodds(0.9));
 }
 
+TEST(DropIn, SmoothedSectionStates)
+{
+  // applyMapSectionUpdateGrid with smoothing (VDBMapping.hpp:1062-1065): the
+  // section is closed in place, so the gap between two active voxels fills.
+  OccupancyVDBMapping map(1.0);
+  map.setConfig(test_config(20));
+  map.addInputSource("lidar", 20, 0);
+  Eigen::Matrix<double, 3, 1> origin(0, 0, 0);
+  map.insertPointCloud(cloud_of({{12.f, 0.f, 0.f}, {14.f, 0.f, 0.f}}), origin, "lidar");
+  auto eye = Eigen::Matrix<double, 4, 4>::Identity();
+  Eigen::Matrix<double, 3, 1> lo(9.5, -0.5, -0.5), hi(15.5, 0.5, 0.5);
+  auto states = map.getMapSectionUpdateGrid(lo, hi, eye, false);
+  EXPECT_TRUE(states->getAccessor().isValueOn(openvdb::Coord(12, 0, 0)));
+  EXPECT_FALSE(states->getAccessor().isValueOn(openvdb::Coord(13, 0, 0)));
+  OccupancyVDBMapping other(1.0);
+  other.applyMapSectionUpdateGrid(states, true, 1);
+  EXPECT_TRUE(states->getAccessor().isValueOn(openvdb::Coord(13, 0, 0)));
+  auto acc = other.getGrid()->getAccessor();
+  EXPECT_TRUE(acc.isValueOn(openvdb::Coord(12, 0, 0)));
+  EXPECT_TRUE(acc.isValueOn(openvdb::Coord(13, 0, 0)));
+  EXPECT_TRUE(acc.isValueOn(openvdb::Coord(14, 0, 0)));
+  EXPECT_FALSE(acc.isValueOn(openvdb::Coord(13, 1, 0)));
+  EXPECT_FALSE(acc.isValueOn(openvdb::Coord(11, 0, 0)));
+}
+
 TEST(DropIn, RaytraceAndFastMode)
 {
   // raytrace (VDBMapping.hpp:646-721) and fast mode (:577-602) through the

@@ -22,10 +22,12 @@
 //   k_fast_mark VDBMapping.hpp:577-602  fast mode: active map voxels along the
 //                                       intersector's spans of each ray
 //   k_raytrace VDBMapping.hpp:675-721   raytrace queries
+//   k_morph_*  VDBMapping.hpp:1094-1147 dilation / erosion of section leaves
 #pragma once
 
 #include "device_common.cuh"
 #include "hdda.cuh"
+#include "morph.cuh"
 
 namespace vdbg {
 
@@ -1742,6 +1744,154 @@ __global__ void __launch_bounds__(128) k_raytrace(const double* __restrict__ q, 
   if (st == hdda::kTraceBound) atomicOr(&m.st->error, kErrStepBound);
   ok[i] = success ? 1 : 0;
   for (int a = 0; a < 3; ++a) end[3 * static_cast<size_t>(i) + a] = e[a];
+}
+
+// ---------------------------------------------------------------------------
+// Morphology of section leaves (VDBMapping.hpp:1094-1147): one dilation or
+// erosion step with the 26-neighbourhood over a set of leaves (origins and
+// OpenVDB-order masks), per vdbg::morph. A set carries an open-addressing
+// hash from leaf key to index, so the 27 neighbours of a leaf are found by
+// lookup. A dilation step's leaves are the input leaves' neighbours that
+// receive bits (morph::feeds), an erosion step's are the input leaves; the
+// steps' empty leaves are dropped by a compaction.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kMorphHashFull = 1u;  // MorphSet::flags: a hash insert ran out of probes
+constexpr uint32_t kMorphSetFull  = 2u;  //                  more leaves than the set holds
+
+struct MorphSet
+{
+  int4* origin;               // [cap] leaf origins (.w unused)
+  unsigned long long* mask;   // [cap][8]
+  uint32_t* count;            // device scalar
+  uint32_t cap;
+  unsigned long long* keys;   // [hmask + 1] leaf keys, kEmptyKey when free
+  int* vals;                  // [hmask + 1] leaf index of the key
+  uint32_t hmask;
+  uint32_t* flags;            // device scalar, kMorph* bits
+};
+
+__device__ __forceinline__ unsigned long long morph_key(int x, int y, int z)
+{
+  return pack_leaf_key(0, x >> 3, y >> 3, z >> 3);
+}
+
+__device__ __forceinline__ int morph_find(const MorphSet& s, unsigned long long key)
+{
+  uint32_t h = static_cast<uint32_t>(mix64(key)) & s.hmask;
+  for (uint32_t probe = 0; probe < kMaxProbes; ++probe)
+  {
+    const unsigned long long k = s.keys[h];
+    if (k == key) return s.vals[h];
+    if (k == kEmptyKey) return -1;
+    h = (h + 1) & s.hmask;
+  }
+  return -1;
+}
+
+// Inserts `key`; the thread that adds it takes the next index of the set,
+// writes the origin and publishes the index (read by later kernels only).
+// Returns false when the hash or the set is full (flag set).
+__device__ __forceinline__ bool morph_insert(const MorphSet& s, unsigned long long key, int4 o)
+{
+  uint32_t h = static_cast<uint32_t>(mix64(key)) & s.hmask;
+  for (uint32_t probe = 0; probe < kMaxProbes; ++probe)
+  {
+    const unsigned long long k = s.keys[h];
+    if (k == key) return true;
+    if (k == kEmptyKey)
+    {
+      const unsigned long long prev = atomicCAS(s.keys + h, kEmptyKey, key);
+      if (prev == kEmptyKey)
+      {
+        const uint32_t i = atomicAdd(s.count, 1u);
+        if (i >= s.cap)
+        {
+          atomicOr(s.flags, kMorphSetFull);
+          s.vals[h] = -1;
+          return false;
+        }
+        s.origin[i] = o;
+        s.vals[h]   = static_cast<int>(i);
+        return true;
+      }
+      if (prev == key) return true;
+    }
+    h = (h + 1) & s.hmask;
+  }
+  atomicOr(s.flags, kMorphHashFull);
+  return false;
+}
+
+// The leaves of `in` (n of them, with their masks) into the empty set `out`
+// (hash and origins; the masks are copied by index).
+__global__ void k_morph_load(const int4* __restrict__ origin, const unsigned long long* __restrict__ mask, uint32_t n,
+                             MorphSet out)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int4 o = origin[i];
+  if (!morph_insert(out, morph_key(o.x, o.y, o.z), o)) return;
+  const int j = morph_find(out, morph_key(o.x, o.y, o.z));
+  if (j < 0) return;
+  for (int w = 0; w < 8; ++w) out.mask[static_cast<size_t>(j) * 8 + w] = mask[static_cast<size_t>(i) * 8 + w];
+}
+
+// Dilation: one thread per (leaf of `in`, direction); the neighbours that
+// receive bits become the leaves of `out` (deduplicated by its hash).
+// Erosion (dilate == 0): the leaves of `in` themselves.
+__global__ void k_morph_candidates(MorphSet in, uint32_t n_in, MorphSet out, int dilate)
+{
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_in * 27u) return;
+  const uint32_t i = t / 27u;
+  const int d      = static_cast<int>(t % 27u);
+  const int dx = d / 9 - 1, dy = (d / 3) % 3 - 1, dz = d % 3 - 1;
+  if (!dilate && d != 13) return;
+  if (dilate && !morph::feeds(reinterpret_cast<const uint64_t*>(in.mask + static_cast<size_t>(i) * 8), dx, dy, dz))
+    return;
+  const int4 o = in.origin[i];
+  const int4 c = make_int4(o.x + 8 * dx, o.y + 8 * dy, o.z + 8 * dz, 0);
+  morph_insert(out, morph_key(c.x, c.y, c.z), c);
+}
+
+// The 27 neighbour leaves of one leaf of a step's output, looked up in the
+// step's input set.
+struct MorphNeighbours
+{
+  const MorphSet* in;
+  int cx, cy, cz;
+  __device__ __forceinline__ const uint64_t* operator()(int d) const
+  {
+    const int j = morph_find(*in, morph_key(cx + 8 * (d / 9 - 1), cy + 8 * ((d / 3) % 3 - 1), cz + 8 * (d % 3 - 1)));
+    return j < 0 ? nullptr : reinterpret_cast<const uint64_t*>(in->mask + static_cast<size_t>(j) * 8);
+  }
+};
+
+// One thread per (leaf of `out`, word): the word after the step.
+__global__ void k_morph_words(MorphSet in, MorphSet out, uint32_t n_out, int dilate)
+{
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_out * 8u) return;
+  const uint32_t j = t >> 3;
+  const int a      = static_cast<int>(t & 7u);
+  const int4 o     = out.origin[j];
+  const MorphNeighbours nb{&in, o.x, o.y, o.z};
+  out.mask[static_cast<size_t>(j) * 8 + a] = dilate ? morph::dilate_word(nb, a) : morph::erode_word(nb, a);
+}
+
+// The leaves of `in` with an active voxel, into the empty set `out`.
+__global__ void k_morph_compact(MorphSet in, uint32_t n_in, MorphSet out)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_in) return;
+  unsigned long long any = 0ull;
+  for (int w = 0; w < 8; ++w) any |= in.mask[static_cast<size_t>(i) * 8 + w];
+  if (!any) return;
+  const int4 o = in.origin[i];
+  if (!morph_insert(out, morph_key(o.x, o.y, o.z), o)) return;
+  const int j = morph_find(out, morph_key(o.x, o.y, o.z));
+  if (j < 0) return;
+  for (int w = 0; w < 8; ++w) out.mask[static_cast<size_t>(j) * 8 + w] = in.mask[static_cast<size_t>(i) * 8 + w];
 }
 
 } // namespace vdbg

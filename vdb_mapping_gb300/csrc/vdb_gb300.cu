@@ -2258,6 +2258,164 @@ int reserve_for(vdbg_map* m, int64_t n)
   return VDBG_OK;
 }
 
+// Device buffers of one leaf set of the morphology (MorphSet) with room for
+// `cap` leaves and a hash of at least twice that.
+struct MorphBuf
+{
+  int4* origin              = nullptr;
+  unsigned long long* mask  = nullptr;
+  unsigned long long* keys  = nullptr;
+  int* vals                 = nullptr;
+  uint32_t cap              = 0;
+  uint32_t hsize            = 0;
+};
+
+void morph_free(vdbg_map* m, MorphBuf& b)
+{
+  dev_free(m, b.origin, b.cap);
+  dev_free(m, b.mask, static_cast<size_t>(b.cap) * 8);
+  dev_free(m, b.keys, b.hsize);
+  dev_free(m, b.vals, b.hsize);
+  b.cap = b.hsize = 0;
+}
+
+// Allocates `b` for `cap` leaves and empties it (count 0, hash free).
+int morph_alloc(vdbg_map* m, MorphBuf& b, uint32_t cap, uint32_t* count, cudaStream_t s)
+{
+  cap = std::max<uint32_t>(cap, 1u);
+  uint32_t hs = 1024;
+  while (hs < 2ull * cap) hs <<= 1;
+  VDBG_TRY(dev_alloc(m, &b.origin, cap));
+  b.cap = cap;
+  VDBG_TRY(dev_alloc(m, &b.mask, static_cast<size_t>(cap) * 8));
+  VDBG_TRY(dev_alloc(m, &b.keys, hs));
+  VDBG_TRY(dev_alloc(m, &b.vals, hs));
+  b.hsize = hs;
+  VDBG_CUDA(cudaMemsetAsync(b.keys, 0xff, static_cast<size_t>(hs) * sizeof(unsigned long long), s));
+  VDBG_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t), s));
+  return VDBG_OK;
+}
+
+MorphSet morph_view(const MorphBuf& b, uint32_t* count, uint32_t* flags)
+{
+  MorphSet v;
+  v.origin = b.origin;
+  v.mask   = b.mask;
+  v.count  = count;
+  v.cap    = b.cap;
+  v.keys   = b.keys;
+  v.vals   = b.vals;
+  v.hmask  = b.hsize - 1;
+  v.flags  = flags;
+  return v;
+}
+
+// Reads the four counters (count A, flags, count B, unused) after the queued
+// work; a set or hash that ran out fails the call.
+int morph_counters(const uint32_t* d, uint32_t* h, cudaStream_t s)
+{
+  VDBG_CUDA(cudaMemcpyAsync(h, d, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  VDBG_CUDA(cudaStreamSynchronize(s));
+  if (h[1] != 0u) return VDBG_ERR_OUT_OF_MEMORY;
+  return VDBG_OK;
+}
+
+// The morphology of n leaves (unique origins, OpenVDB-order masks) on the
+// device: the steps of `op`, each a candidate pass, a word pass and a
+// compaction. The result leaves (unsorted) come back in out_o / out_m.
+int morph_run(vdbg_map* m, int op, int iterations, const std::vector<int32_t>& origins,
+              const std::vector<uint64_t>& masks, std::vector<int32_t>& out_o, std::vector<uint64_t>& out_m)
+{
+  cudaStream_t s = m->stream;
+  const uint32_t n = static_cast<uint32_t>(origins.size() / 3);
+  std::vector<int4> h_o(n);
+  for (uint32_t i = 0; i < n; ++i) h_o[i] = make_int4(origins[3 * i], origins[3 * i + 1], origins[3 * i + 2], 0);
+  std::vector<bool> steps;  // true: dilation
+  const bool dilate_first = op == 0 || op == 2;
+  for (int i = 0; i < iterations; ++i) steps.push_back(dilate_first);
+  if (op >= 2)
+    for (int i = 0; i < iterations; ++i) steps.push_back(!dilate_first);
+  int4* d_o                = nullptr;
+  unsigned long long* d_m  = nullptr;
+  uint32_t* ctr            = nullptr;  // [0] count A, [1] flags, [2] count B, [3] flags (unused)
+  MorphBuf A, B, C;
+  uint32_t hc[4]           = {0u, 0u, 0u, 0u};
+  int st                   = VDBG_OK;
+  auto run = [&]() -> int {
+    VDBG_TRY(dev_alloc(m, &ctr, 4));
+    VDBG_CUDA(cudaMemsetAsync(ctr, 0, 4 * sizeof(uint32_t), s));
+    VDBG_TRY(dev_alloc(m, &d_o, std::max<uint32_t>(n, 1u)));
+    VDBG_TRY(dev_alloc(m, &d_m, std::max<uint32_t>(n, 1u) * 8ull));
+    if (n > 0)
+    {
+      VDBG_CUDA(cudaMemcpyAsync(d_o, h_o.data(), n * sizeof(int4), cudaMemcpyHostToDevice, s));
+      VDBG_CUDA(cudaMemcpyAsync(d_m, masks.data(), n * 8 * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    }
+    // The input, with its empty leaves dropped.
+    VDBG_TRY(morph_alloc(m, A, n, ctr, s));
+    if (n > 0)
+    {
+      VDBG_TRY(morph_alloc(m, B, n, ctr + 2, s));
+      k_morph_load<<<(n + 255) / 256, 256, 0, s>>>(d_o, d_m, n, morph_view(B, ctr + 2, ctr + 1));
+      k_morph_compact<<<(n + 255) / 256, 256, 0, s>>>(morph_view(B, ctr + 2, ctr + 1), n,
+                                                      morph_view(A, ctr, ctr + 1));
+      VDBG_CUDA(cudaGetLastError());
+      m->timings.launches += 2;
+      morph_free(m, B);
+    }
+    VDBG_TRY(morph_counters(ctr, hc, s));
+    uint32_t n_a = hc[0];
+    for (bool dil : steps)
+    {
+      if (n_a == 0) break;
+      const uint64_t cap_b = dil ? 27ull * n_a : n_a;
+      if (cap_b > (1ull << 28)) return VDBG_ERR_SIZE_LIMIT;
+      VDBG_TRY(morph_alloc(m, B, static_cast<uint32_t>(cap_b), ctr + 2, s));
+      const MorphSet va = morph_view(A, ctr, ctr + 1);
+      const MorphSet vb = morph_view(B, ctr + 2, ctr + 1);
+      k_morph_candidates<<<static_cast<unsigned>((27ull * n_a + 255) / 256), 256, 0, s>>>(va, n_a, vb, dil ? 1 : 0);
+      VDBG_CUDA(cudaGetLastError());
+      VDBG_TRY(morph_counters(ctr, hc, s));
+      const uint32_t n_b = hc[2];
+      if (n_b > 0) k_morph_words<<<(n_b * 8u + 255) / 256, 256, 0, s>>>(va, vb, n_b, dil ? 1 : 0);
+      VDBG_TRY(morph_alloc(m, C, n_b, ctr, s));
+      if (n_b > 0) k_morph_compact<<<(n_b + 255) / 256, 256, 0, s>>>(vb, n_b, morph_view(C, ctr, ctr + 1));
+      VDBG_CUDA(cudaGetLastError());
+      m->timings.launches += 3;
+      VDBG_TRY(morph_counters(ctr, hc, s));
+      morph_free(m, A);
+      morph_free(m, B);
+      A   = C;
+      C   = MorphBuf();
+      n_a = hc[0];
+    }
+    out_o.assign(static_cast<size_t>(n_a) * 3, 0);
+    out_m.assign(static_cast<size_t>(n_a) * 8, 0);
+    if (n_a > 0)
+    {
+      std::vector<int4> ro(n_a);
+      VDBG_CUDA(cudaMemcpyAsync(ro.data(), A.origin, n_a * sizeof(int4), cudaMemcpyDeviceToHost, s));
+      VDBG_CUDA(cudaMemcpyAsync(out_m.data(), A.mask, n_a * 8 * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+      VDBG_CUDA(cudaStreamSynchronize(s));
+      for (uint32_t i = 0; i < n_a; ++i)
+      {
+        out_o[3 * i]     = ro[i].x;
+        out_o[3 * i + 1] = ro[i].y;
+        out_o[3 * i + 2] = ro[i].z;
+      }
+    }
+    return VDBG_OK;
+  };
+  st = run();
+  morph_free(m, A);
+  morph_free(m, B);
+  morph_free(m, C);
+  dev_free(m, d_o, std::max<uint32_t>(n, 1u));
+  dev_free(m, d_m, std::max<uint32_t>(n, 1u) * 8ull);
+  dev_free(m, ctr, 4);
+  return st;
+}
+
 } // namespace
 
 extern "C" {
@@ -2304,6 +2462,60 @@ int vdbg_raytrace(vdbg_map* m, int map, int64_t n, const double* origins, const 
   VDBG_TRY(fetch_status(m, s));
   record_timings(m);
   if (m->h_status->error != 0u) return map_error(m->h_status->error);
+  return VDBG_OK;
+}
+
+int vdbg_section_morphology(vdbg_map* m, int op, int iterations, int64_t n, const int32_t* origins,
+                            const uint64_t* masks, int64_t capacity, int32_t* out_origins, uint64_t* out_masks,
+                            int64_t* n_out)
+{
+  if (!m || !n_out || op < 0 || op > 3 || iterations < 0 || iterations > 64 || n < 0 || capacity < 0 ||
+      (n > 0 && (!origins || !masks)) || (capacity > 0 && (!out_origins || !out_masks)))
+    return VDBG_ERR_INVALID_ARGUMENT;
+  *n_out = 0;
+  if (n > (int64_t(1) << 24)) return VDBG_ERR_SIZE_LIMIT;
+  // Unique leaves (masks of a repeated origin are merged); origins within
+  // +-2^20, so the steps' leaves stay inside the key range.
+  std::map<std::tuple<int32_t, int32_t, int32_t>, size_t> index;
+  std::vector<int32_t> uo;
+  std::vector<uint64_t> um;
+  for (int64_t i = 0; i < n; ++i)
+  {
+    const int32_t* o = origins + 3 * i;
+    for (int a = 0; a < 3; ++a)
+    {
+      if ((o[a] & 7) != 0) return VDBG_ERR_INVALID_ARGUMENT;
+      if (!(o[a] >= -(1 << 20) && o[a] < (1 << 20))) return VDBG_ERR_COORD_RANGE;
+    }
+    const auto key = std::make_tuple(o[0], o[1], o[2]);
+    auto it        = index.find(key);
+    if (it == index.end())
+    {
+      it = index.emplace(key, uo.size() / 3).first;
+      uo.insert(uo.end(), o, o + 3);
+      um.insert(um.end(), 8, 0ull);
+    }
+    for (int w = 0; w < 8; ++w) um[it->second * 8 + w] |= masks[8 * i + w];
+  }
+  VDBG_TRY(set_device(m));
+  VDBG_CUDA(cudaStreamSynchronize(m->stream));
+  std::vector<int32_t> ro;
+  std::vector<uint64_t> rm;
+  VDBG_TRY(morph_run(m, op, iterations, uo, um, ro, rm));
+  const size_t k = ro.size() / 3;
+  std::vector<size_t> order(k);
+  std::iota(order.begin(), order.end(), size_t(0));
+  std::sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+    return std::make_tuple(ro[3 * a], ro[3 * a + 1], ro[3 * a + 2]) <
+           std::make_tuple(ro[3 * b], ro[3 * b + 1], ro[3 * b + 2]);
+  });
+  *n_out = static_cast<int64_t>(k);
+  if (static_cast<int64_t>(k) > capacity) return VDBG_ERR_BUFFER_TOO_SMALL;
+  for (size_t j = 0; j < k; ++j)
+  {
+    std::memcpy(out_origins + 3 * j, ro.data() + 3 * order[j], 3 * sizeof(int32_t));
+    std::memcpy(out_masks + 8 * j, rm.data() + 8 * order[j], 8 * sizeof(uint64_t));
+  }
   return VDBG_OK;
 }
 

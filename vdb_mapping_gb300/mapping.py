@@ -215,6 +215,26 @@ def _section_values(lib, h, map_index, origins, values, masks, check):
           "vdbg_apply_section_values")
 
 
+MORPH_OPS = {"dilate": 0, "erode": 1, "close": 2, "open": 3}
+
+
+def _morphology(lib, h, origins, masks, op, iterations, check):
+    o = np.ascontiguousarray(np.asarray(origins, np.int32).reshape(-1, 3))
+    mk = np.ascontiguousarray(np.asarray(masks, np.uint64).reshape(-1, 8))
+    n = C.c_int64()
+    cap = 0
+    while True:
+        oo = np.zeros((cap, 3), np.int32)
+        om = np.zeros((cap, 8), np.uint64)
+        s = lib.vdbg_section_morphology(h, MORPH_OPS[op], int(iterations), len(o), o.ctypes.data, mk.ctypes.data, cap,
+                                        oo.ctypes.data, om.ctypes.data, C.byref(n))
+        if s == _lib.STATUS_CODE["VDBG_ERR_BUFFER_TOO_SMALL"]:
+            cap = n.value
+            continue
+        check(s, "vdbg_section_morphology")
+        return oo[: n.value], om[: n.value]
+
+
 def _raytrace(lib, h, map_index, origins, directions, max_lengths, check):
     o = np.ascontiguousarray(np.asarray(origins, np.float64).reshape(-1, 3))
     d = np.ascontiguousarray(np.asarray(directions, np.float64).reshape(-1, 3))
@@ -418,9 +438,18 @@ class OccupancyVDBMapping:
         active voxels (getMapSectionUpdateGrid reads the same as bool)."""
         return _section_export(self._lib, self._h, -1, lo, hi, full, self._check)
 
-    def applyMapSectionStates(self, lo, hi, origins, masks) -> None:
-        """applyMapSectionUpdateGrid (no smoothing) with the section's box [lo, hi]."""
+    def applyMapSectionStates(self, lo, hi, origins, masks, smooth: bool = False, iterations: int = 2) -> None:
+        """applyMapSectionUpdateGrid with the section's box [lo, hi]; smooth closes
+        the section's active voxels first (VDBMapping.hpp:1062-1065)."""
+        if smooth:
+            origins, masks = self.sectionMorphology(origins, masks, "close", iterations)
         _section_states(self._lib, self._h, -1, lo, hi, origins, masks, self._check)
+
+    def sectionMorphology(self, origins, masks, op: str = "close", iterations: int = 2):
+        """morphologicalDilateMap / ErodeMap / CloseMap / OpenMap (VDBMapping.hpp:1094-1147)
+        of a section's active voxels on the GPU: op in dilate, erode, close, open.
+        Returns (origins, masks) of the leaves with active voxels, sorted by origin."""
+        return _morphology(self._lib, self._h, origins, masks, op, iterations, self._check)
 
     def applyMapSectionValues(self, origins, values, masks) -> None:
         """applyMapSectionGrid (no smoothing)."""
@@ -606,8 +635,15 @@ class MapBatch:
     def getMapSection(self, map_index: int, lo, hi, full: bool = False):
         return _section_export(self._lib, self._h, map_index, lo, hi, full, self._check)
 
-    def applyMapSectionStates(self, map_index: int, lo, hi, origins, masks) -> None:
+    def applyMapSectionStates(self, map_index: int, lo, hi, origins, masks, smooth: bool = False,
+                              iterations: int = 2) -> None:
+        if smooth:
+            origins, masks = self.sectionMorphology(origins, masks, "close", iterations)
         _section_states(self._lib, self._h, map_index, lo, hi, origins, masks, self._check)
+
+    def sectionMorphology(self, origins, masks, op: str = "close", iterations: int = 2):
+        """See OccupancyVDBMapping.sectionMorphology."""
+        return _morphology(self._lib, self._h, origins, masks, op, iterations, self._check)
 
     def applyMapSectionValues(self, map_index: int, origins, values, masks) -> None:
         _section_values(self._lib, self._h, map_index, origins, values, masks, self._check)
