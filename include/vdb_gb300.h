@@ -263,10 +263,11 @@ int vdbg_batch_insert(vdbg_map* batch, const float* xyz, const int64_t* counts, 
 int vdbg_export_section(vdbg_map* map, int map_index, const int32_t lo[3], const int32_t hi[3], int full,
                         int64_t capacity, int32_t* origins, float* values, uint64_t* masks, int64_t* n_out);
 
-/* applyMapSectionUpdateGrid without smoothing (VDBMapping.hpp:1058-1085): every
- * active map voxel inside [lo, hi] (the section's bb_min/bb_max) is set
- * inactive, then every active voxel of the n section leaves is set active.
- * Values are kept, and a new leaf starts at 0. */
+/* applyMapSectionUpdateGrid (VDBMapping.hpp:1058-1085): every active map
+ * voxel inside [lo, hi] (the section's bb_min/bb_max) is set inactive, then
+ * every active voxel of the n section leaves is set active. Values are kept,
+ * and a new leaf starts at 0. With smoothing, the caller closes the section
+ * first with vdbg_section_morphology (op 2). */
 int vdbg_apply_section_states(vdbg_map* map, int map_index, const int32_t lo[3], const int32_t hi[3], int64_t n,
                               const int32_t* origins, const uint64_t* masks);
 
@@ -275,8 +276,8 @@ int vdbg_apply_section_states(vdbg_map* map, int map_index, const int32_t lo[3],
  * created unless every voxel is inactive 0. The section tree's tiles, the
  * empty slots of its 128^3 and 4096^3 internal nodes, set the map voxel at
  * their origin to inactive 0 where a map leaf holds it, as the reference's
- * cbeginValueAll() does. Smoothing (morphologicalCloseMap, :1095-1100) is not
- * provided. */
+ * cbeginValueAll() does. Smoothing of value sections (morphologicalCloseMap,
+ * :1026-1029) is not provided. */
 int vdbg_apply_section_values(vdbg_map* map, int map_index, int64_t n, const int32_t* origins, const float* values,
                               const uint64_t* masks);
 
