@@ -17,6 +17,7 @@
 //   include/vdb_mapping/VDBMapping.hpp:577-602    castRayIntoGridFast (fast mode)
 //   include/vdb_mapping/VDBMapping.hpp:646-721    raytrace
 //   include/vdb_mapping/VDBMapping.hpp:1436-1449  updateVolumeRayIntersectors
+//   include/vdb_mapping/VDBMapping.hpp:1094-1147  morphological Dilate/Erode/Close/OpenMap
 //   include/vdb_mapping/OccupancyVDBMapping.hpp:59-117  log-odds constants and node updates
 // plus the OpenVDB arithmetic those lines call (OpenVDB is a third-party
 // dependency that is not vendored in the reference; README.md:11 asks for
