@@ -73,3 +73,30 @@ def test_build_targets_sm_103a_only():
     assert "arch=compute_103a,code=sm_103a" in flags
     assert flags.count("-gencode") == 1
     assert "-fmad=false" in flags
+
+
+def test_new_entry_points_reject_bad_arguments_before_device_work(lib_path):
+    """Argument checks of the raytrace and morphology entry points run before
+    any CUDA call, so they hold without a GPU."""
+    from vdb_mapping_gb300 import _lib
+
+    lib = _lib.load()
+    bad = _lib.STATUS_CODE["VDBG_ERR_INVALID_ARGUMENT"]
+    n = C.c_int64(7)
+    d3 = (C.c_double * 3)()
+    ok = (C.c_uint8 * 1)()
+    # no map
+    assert lib.vdbg_raytrace(None, -1, 1, d3, d3, d3, ok, d3) == bad
+    assert lib.vdbg_section_morphology(None, 2, 1, 0, None, None, 0, None, None, C.byref(n)) == bad
+    # unknown op, iterations out of range, missing outputs: checked before the map is used
+    fake = C.c_void_p(1)
+    assert lib.vdbg_section_morphology(fake, 4, 1, 0, None, None, 0, None, None, C.byref(n)) == bad
+    assert lib.vdbg_section_morphology(fake, 2, 65, 0, None, None, 0, None, None, C.byref(n)) == bad
+    assert lib.vdbg_section_morphology(fake, 2, 1, 1, None, None, 0, None, None, C.byref(n)) == bad
+    assert lib.vdbg_section_morphology(fake, 2, 1, 0, None, None, 0, None, None, None) == bad
+    o = (C.c_int32 * 3)(3, 0, 0)  # not a multiple of 8
+    m = (C.c_uint64 * 8)()
+    assert lib.vdbg_section_morphology(fake, 2, 1, 1, o, m, 0, None, None, C.byref(n)) == bad
+    o = (C.c_int32 * 3)(1 << 21, 0, 0)  # beyond +-2^20
+    assert lib.vdbg_section_morphology(fake, 2, 1, 1, o, m, 0, None, None, C.byref(n)) == \
+        _lib.STATUS_CODE["VDBG_ERR_COORD_RANGE"]
