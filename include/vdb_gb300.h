@@ -281,6 +281,25 @@ int vdbg_apply_section_states(vdbg_map* map, int map_index, const int32_t lo[3],
 int vdbg_apply_section_values(vdbg_map* map, int map_index, int64_t n, const int32_t* origins, const float* values,
                               const uint64_t* masks);
 
+/* Artificial areas (VDBMapping.hpp:1152-1236), single maps only.
+ * vdbg_add_artificial_walls is addArtificialWall (:1210-1236) for n walls
+ * (world start and end points [n][3]): both ends go through worldToIndex,
+ * and for every layer i in [(int)(negative_height / res),
+ * (int)(positive_height / res)) the voxels castRayIntoGrid visits from
+ * start + (0,0,i) to end + (0,0,i) join the artificial set. After every
+ * update of the map that integrates a non-empty update grid, each artificial
+ * voxel is set active, its leaf created at the background when absent
+ * (updateMap, :785-789). addArtificialPolygon is the walls between
+ * consecutive corners, closing back to the first; addArtificialAreas is
+ * vdbg_restore_map_integrity, then its polygons.
+ * vdbg_restore_map_integrity is restoreMapIntegrity (:1153-1166): every
+ * artificial voxel's state becomes value > the log-odds of prob_thres_max
+ * (setNodeState), then the set is emptied. The no-allocation insert rejects
+ * a map with artificial areas. */
+int vdbg_add_artificial_walls(vdbg_map* map, int64_t n, const double* starts, const double* ends,
+                              double negative_height, double positive_height);
+int vdbg_restore_map_integrity(vdbg_map* map);
+
 /* Morphology of a map section's active voxels with the 26-neighbourhood:
  * openvdb::tools::dilateActiveValues / erodeActiveValues with
  * NN_FACE_EDGE_VERTEX as VDBMapping.hpp:1094-1147 calls them

@@ -801,6 +801,41 @@ public:
     morphology<TGrid>(grid, 1, iterations);
   }
 
+  /*! VDBMapping.hpp:1153-1166. */
+  void restoreMapIntegrity()
+  {
+    std::unique_lock map_lock(*m_map_mutex);
+    check(vdbg_restore_map_integrity(m_dev->map), "vdbg_restore_map_integrity");
+    ++m_dev->version;
+  }
+
+  /*! VDBMapping.hpp:1175-1189. */
+  void addArtificialAreas(const std::vector<std::vector<Eigen::Matrix<double, 4, 1> > >& artificial_areas,
+                          const double negative_height, const double positive_height)
+  {
+    restoreMapIntegrity();
+    for (const auto& area : artificial_areas) addArtificialPolygon(area, negative_height, positive_height);
+  }
+
+  /*! VDBMapping.hpp:1198-1207. */
+  void addArtificialPolygon(const std::vector<Eigen::Matrix<double, 4, 1> >& polygon, const double negative_height,
+                            const double positive_height)
+  {
+    for (size_t i = 0; i < polygon.size(); ++i)
+      addArtificialWall(polygon[i], polygon[(i + 1) % polygon.size()], negative_height, positive_height);
+  }
+
+  /*! VDBMapping.hpp:1210-1236: the wall's voxels are set active after every
+   * update of the map. */
+  void addArtificialWall(const Eigen::Matrix<double, 4, 1>& start, const Eigen::Matrix<double, 4, 1>& end,
+                         const double negative_height, const double positive_height)
+  {
+    const double s[3] = {start.x(), start.y(), start.z()};
+    const double e[3] = {end.x(), end.y(), end.z()};
+    check(vdbg_add_artificial_walls(m_dev->map, 1, s, e, negative_height, positive_height),
+          "vdbg_add_artificial_walls");
+  }
+
   /*! VDBMapping.hpp:1343. */
   std::shared_ptr<std::shared_mutex> getMapMutex() { return m_map_mutex; }
 

@@ -51,6 +51,8 @@ def load():
         "vo_apply_section_values": (None, [P, I64, P, P, P]),
         "vo_raytrace": (C.c_int, [P, I64, P, P, P, P, P]),
         "vo_morphology": (I64, [I64, P, P, C.c_int, C.c_int, I64, P, P]),
+        "vo_add_artificial_wall": (None, [P, C.POINTER(D), C.POINTER(D), D, D]),
+        "vo_restore_map_integrity": (None, [P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -167,6 +169,26 @@ class OracleMap:
         v = np.ascontiguousarray(values, np.float32)
         mk = np.ascontiguousarray(masks, np.uint64)
         self._l.vo_apply_section_values(self._h, len(o), o.ctypes.data, v.ctypes.data, mk.ctypes.data)
+
+    def addArtificialWall(self, start, end, negative_height, positive_height):
+        """addArtificialWall (VDBMapping.hpp:1210-1236)."""
+        self._l.vo_add_artificial_wall(self._h, _d3(start[:3]), _d3(end[:3]), float(negative_height),
+                                       float(positive_height))
+
+    def addArtificialPolygon(self, polygon, negative_height, positive_height):
+        """addArtificialPolygon (VDBMapping.hpp:1198-1207): walls between consecutive corners, closed."""
+        for i in range(len(polygon)):
+            self.addArtificialWall(polygon[i], polygon[(i + 1) % len(polygon)], negative_height, positive_height)
+
+    def addArtificialAreas(self, areas, negative_height, positive_height):
+        """addArtificialAreas (VDBMapping.hpp:1175-1189): restore, then every polygon."""
+        self.restoreMapIntegrity()
+        for poly in areas:
+            self.addArtificialPolygon(poly, negative_height, positive_height)
+
+    def restoreMapIntegrity(self):
+        """restoreMapIntegrity (VDBMapping.hpp:1153-1166)."""
+        self._l.vo_restore_map_integrity(self._h)
 
     def raytrace(self, origins, directions, max_lengths):
         """raytrace (VDBMapping.hpp:675-721): (status, success bool[n], end points [n][3])."""

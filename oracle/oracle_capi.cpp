@@ -194,6 +194,14 @@ int64_t vo_morphology(int64_t n, const int32_t* origins, const uint64_t* masks, 
   return static_cast<int64_t>(r.size());
 }
 
+void vo_add_artificial_wall(void* h, const double* start, const double* end, double negative_height,
+                            double positive_height)
+{
+  static_cast<Handle*>(h)->map.add_artificial_wall(start, end, negative_height, positive_height);
+}
+
+void vo_restore_map_integrity(void* h) { static_cast<Handle*>(h)->map.restore_map_integrity(); }
+
 int vo_raytrace(void* h, int64_t n, const double* origins, const double* dirs, const double* lengths,
                 uint8_t* success, double* ends)
 {

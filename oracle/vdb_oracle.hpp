@@ -1084,6 +1084,45 @@ public:
 
   void set_artificial(const std::vector<Coord>& voxels) { m_artificial = voxels; }
 
+  // addArtificialWall (VDBMapping.hpp:1210-1236): worldToIndex of both ends;
+  // for every layer i in [(int)(neg / res), (int)(pos / res)) the voxels
+  // castRayIntoGrid visits from start + (0,0,i) to end + (0,0,i) join the
+  // artificial set (re-activated by every update_map).
+  void add_artificial_wall(const double start[3], const double end[3], double negative_height,
+                           double positive_height)
+  {
+    const Coord s = world_to_index(start, m_resolution, m_var);
+    const Coord e = world_to_index(end, m_resolution, m_var);
+    const int lo  = static_cast<int>(negative_height / m_resolution);
+    const int hi  = static_cast<int>(positive_height / m_resolution);
+    for (int i = lo; i < hi; ++i)
+      cast_ray(Coord(s.x, s.y, s.z + i), Coord(e.x, e.y, e.z + i), [&](const Coord& v) { m_artificial.push_back(v); });
+  }
+
+  // restoreMapIntegrity (VDBMapping.hpp:1153-1166): each artificial voxel's
+  // state becomes value > thres_max (setNodeState, OccupancyVDBMapping.hpp:
+  // 130-134); a voxel outside the map is a background tile, which becomes a
+  // leaf only if that changes its state (0 > thres_max). Then the set is
+  // emptied.
+  void restore_map_integrity()
+  {
+    for (const Coord& c : m_artificial)
+    {
+      MapLeaf* l = m_map.find_leaf(leaf_origin(c));
+      if (!l)
+      {
+        if (!(0.0f > m_lo_thres_max)) continue;
+        l = &m_map.touch(c);
+      }
+      const uint32_t off = leaf_offset(c);
+      if (l->value[off] > m_lo_thres_max)
+        l->on[off >> 6] |= 1ull << (off & 63);
+      else
+        l->on[off >> 6] &= ~(1ull << (off & 63));
+    }
+    m_artificial.clear();
+  }
+
   // getMapSection (VDBMapping.hpp:922-962): the leaves overlapping the index
   // box [lo, hi] (inclusive, CoordBBox::hasOverlap), restricted to the voxels
   // inside it. `full` (extractFullLeaf, :972-990) copies every inside voxel

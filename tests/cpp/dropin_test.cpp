@@ -210,6 +210,27 @@ TEST(DropIn, SmoothedSectionStates)
   EXPECT_FALSE(acc.isValueOn(openvdb::Coord(11, 0, 0)));
 }
 
+TEST(DropIn, ArtificialWall)
+{
+  // addArtificialWall (VDBMapping.hpp:1210-1236): the wall turns active with
+  // the next update of the map; restoreMapIntegrity (:1153-1166) undoes it.
+  OccupancyVDBMapping map(1.0);
+  map.setConfig(test_config(20));
+  map.addInputSource("lidar", 20, 0);
+  Eigen::Matrix<double, 4, 1> a, b;
+  a(0, 0) = 2.0; a(1, 0) = 5.0; a(2, 0) = 0.0; a(3, 0) = 1.0;
+  b(0, 0) = 6.0; b(1, 0) = 5.0; b(2, 0) = 0.0; b(3, 0) = 1.0;
+  map.addArtificialWall(a, b, 0.0, 1.0);
+  EXPECT_EQ(map.getGrid()->leafCount(), static_cast<size_t>(0));
+  map.insertPointCloud(cloud_of({{0.f, 0.f, 3.f}}), Eigen::Matrix<double, 3, 1>(0, 0, 0), "lidar");
+  auto acc = map.getGrid()->getAccessor();
+  EXPECT_TRUE(acc.isValueOn(openvdb::Coord(2, 5, 0)));
+  EXPECT_TRUE(acc.isValueOn(openvdb::Coord(6, 5, 0)));
+  EXPECT_FALSE(acc.isValueOn(openvdb::Coord(7, 5, 0)));
+  map.restoreMapIntegrity();
+  EXPECT_FALSE(map.getGrid()->getAccessor().isValueOn(openvdb::Coord(4, 5, 0)));
+}
+
 TEST(DropIn, RaytraceAndFastMode)
 {
   // raytrace (VDBMapping.hpp:646-721) and fast mode (:577-602) through the

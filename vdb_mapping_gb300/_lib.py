@@ -197,6 +197,8 @@ SIGNATURES = [
     ("vdbg_apply_section_states", C.c_int, [_P, C.c_int, _P, _P, C.c_int64, _P, _P]),
     ("vdbg_apply_section_values", C.c_int, [_P, C.c_int, C.c_int64, _P, _P, _P]),
     ("vdbg_raytrace", C.c_int, [_P, C.c_int, C.c_int64, _P, _P, _P, _P, _P]),
+    ("vdbg_add_artificial_walls", C.c_int, [_P, C.c_int64, _P, _P, C.c_double, C.c_double]),
+    ("vdbg_restore_map_integrity", C.c_int, [_P]),
     ("vdbg_section_morphology", C.c_int, [_P, C.c_int, C.c_int, C.c_int64, _P, _P, C.c_int64, _P, _P,
                                           C.POINTER(C.c_int64)]),
     ("vdbg_batch_use_graph", C.c_int, [_P, C.c_int]),

@@ -23,6 +23,8 @@
 //                                       intersector's spans of each ray
 //   k_raytrace VDBMapping.hpp:675-721   raytrace queries
 //   k_morph_*  VDBMapping.hpp:1094-1147 dilation / erosion of section leaves
+//   k_wall_voxels VDBMapping.hpp:1210-1236  artificial walls, castRayIntoGrid per layer
+//   k_artificial_restore VDBMapping.hpp:1153-1166  restoreMapIntegrity
 #pragma once
 
 #include "device_common.cuh"
@@ -1892,6 +1894,77 @@ __global__ void k_morph_compact(MorphSet in, uint32_t n_in, MorphSet out)
   const int j = morph_find(out, morph_key(o.x, o.y, o.z));
   if (j < 0) return;
   for (int w = 0; w < 8; ++w) out.mask[static_cast<size_t>(j) * 8 + w] = in.mask[static_cast<size_t>(i) * 8 + w];
+}
+
+// ---------------------------------------------------------------------------
+// Artificial areas (VDBMapping.hpp:1152-1236). Their voxels are re-activated
+// after every update of the map by k_section_set_states (VDBMapping.hpp:
+// 785-789 does setActiveState(v, true)); walls are rasterised here and the
+// states restored when the areas are replaced.
+// ---------------------------------------------------------------------------
+
+// addArtificialWall (VDBMapping.hpp:1210-1236): layer i is castRayIntoGrid
+// (VDBMapping.hpp:550-566) from voxel a[i] to b[i]: the voxel DDA of the ray
+// a + 0.5 -> b + 0.5 over t in [0, 1], nothing when a == b. Its 1 + L1
+// voxels go to out[first[i], first[i + 1]); a count that disagrees sets *bad.
+__global__ void k_wall_voxels(const int4* __restrict__ a, const int4* __restrict__ b,
+                              const uint32_t* __restrict__ first, uint32_t n, int4* __restrict__ out,
+                              uint32_t* bad)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t base = first[i], cnt = first[i + 1] - base;
+  if (cnt == 0u) return;
+  const int4 s = a[i], e = b[i];
+  const double eye[3] = {hdda::add(static_cast<double>(s.x), 0.5), hdda::add(static_cast<double>(s.y), 0.5),
+                         hdda::add(static_cast<double>(s.z), 0.5)};
+  const double dir[3] = {hdda::sub(static_cast<double>(e.x), static_cast<double>(s.x)),
+                         hdda::sub(static_cast<double>(e.y), static_cast<double>(s.y)),
+                         hdda::sub(static_cast<double>(e.z), static_cast<double>(s.z))};
+  const hdda::Ray r = hdda::make_ray(eye, dir, 0.0, 1.0);
+  hdda::Dda d;
+  hdda::dda_init(d, r, 0.0, 1.0, 0);
+  uint32_t k = 0;
+  do
+  {
+    if (k >= cnt)
+    {
+      atomicOr(bad, 1u);
+      return;
+    }
+    out[base + k] = make_int4(d.voxel[0], d.voxel[1], d.voxel[2], 0);
+    ++k;
+  } while (hdda::dda_step(d));
+  if (k != cnt) atomicOr(bad, 1u);
+}
+
+// restoreMapIntegrity (VDBMapping.hpp:1153-1166) on the integrated map
+// leaves holding artificial voxels: each such voxel's state becomes
+// value > thres_max (setNodeState, OccupancyVDBMapping.hpp:130-134). One
+// thread per (artificial leaf, plane word); the leaves are distinct, so no
+// word has two writers.
+__global__ void k_artificial_restore(MapView m, const int4* __restrict__ art_o,
+                                     const unsigned long long* __restrict__ art_m, uint32_t n,
+                                     const uint32_t* __restrict__ flags, const float* __restrict__ values,
+                                     unsigned long long* __restrict__ active, float thres_max)
+{
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * 8u) return;
+  const uint32_t i              = t >> 3;
+  const int w                   = static_cast<int>(t & 7u);
+  const unsigned long long bits = art_m[static_cast<size_t>(i) * 8 + w];
+  if (!bits) return;
+  const int4 o   = art_o[i];
+  const int slot = find_leaf(m, o.w, o.x >> 3, o.y >> 3, o.z >> 3);
+  if (slot < 0 || flags[slot] == 0u) return;
+  unsigned long long on = 0ull;
+  for (unsigned long long z = bits; z; z &= z - 1ull)
+  {
+    const int k = __ffsll(static_cast<long long>(z)) - 1;
+    if (values[static_cast<size_t>(slot) * 512 + w * 64 + k] > thres_max) on |= 1ull << k;
+  }
+  unsigned long long* a = active + static_cast<size_t>(slot) * 8 + w;
+  *a                    = (*a & ~bits) | on;
 }
 
 } // namespace vdbg

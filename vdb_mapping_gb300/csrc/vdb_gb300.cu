@@ -8,6 +8,7 @@
 // the calls have the reference's synchronous semantics.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -153,6 +154,14 @@ struct vdbg_map
   int* topo_box                    = nullptr;  // [8]: box[6], then two counts
   char* d_trace                    = nullptr;
   size_t trace_bytes               = 0;
+  // Artificial areas (VDBMapping.hpp:1152-1236): their voxels as leaves
+  // (origins, device-order masks) on the host, and the device copy that
+  // k_section_set_states re-activates after every update of the map.
+  std::vector<int4> art_o;
+  std::vector<unsigned long long> art_m;
+  int4* d_art_o                    = nullptr;
+  unsigned long long* d_art_m      = nullptr;
+  uint32_t art_n                   = 0;  // leaves in the device copy
 };
 
 namespace {
@@ -1301,6 +1310,27 @@ int graph_step(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t str
   return settle_dda_passes(m, c, m->d_rays, m->d_order, n, t, rb, m->lstate, m->wstate, true, s, 1);
 }
 
+template <class F>
+int run_allocating(vdbg_map* m, F&& launch);
+
+// VDBMapping.hpp:785-789 after the sweep of channel `c`: every artificial
+// voxel is set active (its leaf created at the background when absent), unless
+// the update grid was empty (updateMap returns before, VDBMapping.hpp:735-738).
+int reactivate_artificial(vdbg_map* m, Channel& c, cudaStream_t s)
+{
+  uint32_t touched = 0;
+  VDBG_CUDA(cudaMemcpyAsync(&touched, c.n_touched, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  VDBG_CUDA(cudaStreamSynchronize(s));
+  if (touched == 0u) return VDBG_OK;
+  return run_allocating(m, [&]() -> int {
+    k_section_set_states<<<(m->art_n + 255) / 256, 256, 0, s>>>(map_view(m), m->d_art_o, m->d_art_m, m->art_n, 0,
+                                                                m->flags, m->active);
+    VDBG_CUDA(cudaGetLastError());
+    m->timings.launches += 1;
+    return VDBG_OK;
+  });
+}
+
 int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t stride, const CastPlan& plan,
                              Channel* src, uint32_t flags, cudaStream_t s, bool integrate_all, Channel* only,
                              vdbg_scan_stats* stats)
@@ -1365,7 +1395,7 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
                            m->d_hist, m->d_cursor));
       // The sweep follows the marking without a host round trip when this
       // source's window is the only one the call integrates.
-      bool eager = integrate_all || only == src;
+      bool eager = (integrate_all || only == src) && m->art_n == 0;
       if (integrate_all)
         for (const Channel& c : m->channels)
           if (&c != src && c.pending) eager = false;
@@ -1401,7 +1431,11 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
     todo.push_back(only);
   }
   if (integrate_all || only) VDBG_TRY(reset_changes(m, s));
-  for (Channel* c : todo) VDBG_TRY(launch_sweep(m, *c, s));
+  for (Channel* c : todo)
+  {
+    VDBG_TRY(launch_sweep(m, *c, s));
+    if (m->art_n > 0) VDBG_TRY(reactivate_artificial(m, *c, s));
+  }
   VDBG_TRY(fetch_status(m, s));
   if (m->h_status->error != 0u) return map_error(m->h_status->error);
   record_timings(m);
@@ -1763,6 +1797,8 @@ int vdbg_destroy(vdbg_map* m)
   dev_free(m, m->topo_keys, 2 * static_cast<size_t>(m->topo_cap));
   dev_free(m, m->topo_box, 8);
   dev_free(m, m->d_trace, m->trace_bytes);
+  dev_free(m, m->d_art_o, m->art_n);
+  dev_free(m, m->d_art_m, static_cast<size_t>(m->art_n) * 8);
   if (m->h_status) cudaFreeHost(m->h_status);
   if (m->ev0) cudaEventDestroy(m->ev0);
   if (m->ev1) cudaEventDestroy(m->ev1);
@@ -2416,9 +2452,149 @@ int morph_run(vdbg_map* m, int op, int iterations, const std::vector<int32_t>& o
   return st;
 }
 
+// Replaces the device copy of the artificial leaves with the host's.
+int upload_artificial(vdbg_map* m)
+{
+  dev_free(m, m->d_art_o, m->art_n);
+  dev_free(m, m->d_art_m, static_cast<size_t>(m->art_n) * 8);
+  m->art_n = 0;
+  const size_t n = m->art_o.size();
+  if (n == 0) return VDBG_OK;
+  VDBG_TRY(dev_alloc(m, &m->d_art_o, n));
+  VDBG_TRY(dev_alloc(m, &m->d_art_m, n * 8));
+  cudaStream_t s = m->stream;
+  VDBG_CUDA(cudaMemcpyAsync(m->d_art_o, m->art_o.data(), n * sizeof(int4), cudaMemcpyHostToDevice, s));
+  VDBG_CUDA(cudaMemcpyAsync(m->d_art_m, m->art_m.data(), n * 8 * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                            s));
+  VDBG_CUDA(cudaStreamSynchronize(s));
+  m->art_n = static_cast<uint32_t>(n);
+  return VDBG_OK;
+}
+
 } // namespace
 
 extern "C" {
+
+int vdbg_add_artificial_walls(vdbg_map* m, int64_t n, const double* starts, const double* ends,
+                              double negative_height, double positive_height)
+{
+  if (!m || m->batch || n < 0 || (n > 0 && (!starts || !ends)) || !std::isfinite(negative_height) ||
+      !std::isfinite(positive_height))
+    return VDBG_ERR_INVALID_ARGUMENT;
+  if (n == 0) return VDBG_OK;
+  const MapConf& mc = m->conf[0];
+  // VDBMapping.hpp:1223-1233: worldToIndex of both ends, the layer range
+  // truncated toward 0, one castRayIntoGrid per layer.
+  const double nh = negative_height / mc.resolution, ph = positive_height / mc.resolution;
+  if (!(nh > -kVoxelMaxExcl && nh < kVoxelMaxExcl && ph > -kVoxelMaxExcl && ph < kVoxelMaxExcl))
+    return VDBG_ERR_COORD_RANGE;
+  const int lo_i = static_cast<int>(nh), hi_i = static_cast<int>(ph);
+  std::vector<int4> a, b;
+  std::vector<uint32_t> first(1, 0u);
+  for (int64_t w = 0; w < n; ++w)
+  {
+    int s3[3], e3[3];
+    if (!origin_to_index(mc, starts + 3 * w, s3) || !origin_to_index(mc, ends + 3 * w, e3))
+      return VDBG_ERR_COORD_RANGE;
+    for (int i = lo_i; i < hi_i; ++i)
+    {
+      const int64_t sz = static_cast<int64_t>(s3[2]) + i, ez = static_cast<int64_t>(e3[2]) + i;
+      if (sz < static_cast<int64_t>(kVoxelMin) || sz >= static_cast<int64_t>(kVoxelMaxExcl) ||
+          ez < static_cast<int64_t>(kVoxelMin) || ez >= static_cast<int64_t>(kVoxelMaxExcl))
+        return VDBG_ERR_COORD_RANGE;
+      a.push_back(make_int4(s3[0], s3[1], static_cast<int>(sz), 0));
+      b.push_back(make_int4(e3[0], e3[1], static_cast<int>(ez), 0));
+      const uint64_t l1 = static_cast<uint64_t>(std::llabs(static_cast<long long>(e3[0]) - s3[0])) +
+                          static_cast<uint64_t>(std::llabs(static_cast<long long>(e3[1]) - s3[1])) +
+                          static_cast<uint64_t>(std::llabs(ez - sz));
+      const uint64_t next = first.back() + (l1 == 0 ? 0 : l1 + 1);
+      if (next > (1ull << 28)) return VDBG_ERR_SIZE_LIMIT;
+      first.push_back(static_cast<uint32_t>(next));
+    }
+  }
+  const uint32_t layers = static_cast<uint32_t>(a.size());
+  const uint32_t total  = first.back();
+  if (total == 0) return VDBG_OK;
+  VDBG_TRY(set_device(m));
+  cudaStream_t s = m->stream;
+  VDBG_CUDA(cudaStreamSynchronize(s));
+  int4 *d_a = nullptr, *d_b = nullptr, *d_v = nullptr;
+  uint32_t *d_first = nullptr, *d_bad = nullptr;
+  std::vector<int4> vox(total);
+  uint32_t bad = 0;
+  int st       = dev_alloc(m, &d_a, layers);
+  if (st == VDBG_OK) st = dev_alloc(m, &d_b, layers);
+  if (st == VDBG_OK) st = dev_alloc(m, &d_first, layers + 1u);
+  if (st == VDBG_OK) st = dev_alloc(m, &d_v, total);
+  if (st == VDBG_OK) st = dev_alloc(m, &d_bad, 1);
+  if (st == VDBG_OK &&
+      (cudaMemcpyAsync(d_a, a.data(), layers * sizeof(int4), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+       cudaMemcpyAsync(d_b, b.data(), layers * sizeof(int4), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+       cudaMemcpyAsync(d_first, first.data(), (layers + 1u) * sizeof(uint32_t), cudaMemcpyHostToDevice, s) !=
+         cudaSuccess ||
+       cudaMemsetAsync(d_bad, 0, sizeof(uint32_t), s) != cudaSuccess))
+    st = VDBG_ERR_CUDA;
+  if (st == VDBG_OK)
+  {
+    k_wall_voxels<<<(layers + 127) / 128, 128, 0, s>>>(d_a, d_b, d_first, layers, d_v, d_bad);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(vox.data(), d_v, total * sizeof(int4), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(&bad, d_bad, sizeof(uint32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      st = VDBG_ERR_CUDA;
+  }
+  dev_free(m, d_a, layers);
+  dev_free(m, d_b, layers);
+  dev_free(m, d_first, layers + 1u);
+  dev_free(m, d_v, total);
+  dev_free(m, d_bad, 1);
+  if (st != VDBG_OK) return st;
+  if (bad) return VDBG_ERR_CUDA;
+  // Into the artificial leaves (device order: bit (z & 7) << 6 | (y & 7) << 3 | (x & 7)).
+  std::map<std::tuple<int, int, int>, size_t> index;
+  for (size_t i = 0; i < m->art_o.size(); ++i) index[std::make_tuple(m->art_o[i].x, m->art_o[i].y, m->art_o[i].z)] = i;
+  for (const int4& v : vox)
+  {
+    const auto key = std::make_tuple(v.x & ~7, v.y & ~7, v.z & ~7);
+    auto it        = index.find(key);
+    if (it == index.end())
+    {
+      it = index.emplace(key, m->art_o.size()).first;
+      m->art_o.push_back(make_int4(v.x & ~7, v.y & ~7, v.z & ~7, 0));
+      m->art_m.insert(m->art_m.end(), 8, 0ull);
+    }
+    const int off = ((v.z & 7) << 6) | ((v.y & 7) << 3) | (v.x & 7);
+    m->art_m[it->second * 8 + (off >> 6)] |= 1ull << (off & 63);
+  }
+  return upload_artificial(m);
+}
+
+int vdbg_restore_map_integrity(vdbg_map* m)
+{
+  if (!m || m->batch) return VDBG_ERR_INVALID_ARGUMENT;
+  if (m->art_n > 0)
+  {
+    cudaStream_t s = m->stream;
+    VDBG_TRY(begin_call(m, s));
+    const float thres_max = m->conf[0].lo.thres_max;
+    // setNodeState on a voxel outside the map turns it on only when the
+    // background 0 exceeds the threshold; then its leaf is created first.
+    if (0.0f > thres_max)
+      VDBG_TRY(run_allocating(m, [&]() -> int {
+        k_section_set_states<<<(m->art_n + 255) / 256, 256, 0, s>>>(map_view(m), m->d_art_o, m->d_art_m, m->art_n,
+                                                                    0, m->flags, m->active);
+        VDBG_CUDA(cudaGetLastError());
+        return VDBG_OK;
+      }));
+    k_artificial_restore<<<(m->art_n * 8u + 255) / 256, 256, 0, s>>>(map_view(m), m->d_art_o, m->d_art_m, m->art_n,
+                                                                     m->flags, m->values, m->active, thres_max);
+    VDBG_CUDA(cudaGetLastError());
+    VDBG_CUDA(cudaStreamSynchronize(s));
+  }
+  m->art_o.clear();
+  m->art_m.clear();
+  return upload_artificial(m);
+}
 
 int vdbg_raytrace(vdbg_map* m, int map, int64_t n, const double* origins, const double* directions,
                   const double* max_lengths, uint8_t* successes, double* end_points)
@@ -2838,8 +3014,9 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
                                                void* stream, vdbg_scan_stats* stats)
 {
   if (!m || m->batch || !origin || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
-  // Fast mode builds the intersector's node sets, which allocates.
-  if (m->conf[0].fast_mode) return VDBG_ERR_INVALID_ARGUMENT;
+  // Fast mode builds the intersector's node sets and artificial areas may
+  // create leaves after the sweep: both allocate.
+  if (m->conf[0].fast_mode || m->art_n > 0) return VDBG_ERR_INVALID_ARGUMENT;
   if (stats) std::memset(stats, 0, sizeof(*stats));
   const bool host_input = (flags & VDBG_POINTS_DEVICE) == 0;
   if (n > kNoAllocMaxPoints || (host_input && stride > 16)) return VDBG_ERR_SIZE_LIMIT;
@@ -2916,7 +3093,11 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
     if (c.pending) todo.push_back(&c);
   if (m->track_changes && !m->chg_words) return VDBG_ERR_SIZE_LIMIT;  // would allocate
   if (m->track_changes) VDBG_CUDA(cudaMemsetAsync(m->chg_count, 0, sizeof(uint32_t), s));
-  for (Channel* c : todo) VDBG_TRY(launch_sweep(m, *c, s));
+  for (Channel* c : todo)
+  {
+    VDBG_TRY(launch_sweep(m, *c, s));
+    if (m->art_n > 0) VDBG_TRY(reactivate_artificial(m, *c, s));
+  }
   VDBG_TRY(fetch_status(m, s));
   if (m->h_status->error != 0u) return map_error(m->h_status->error);
   record_timings(m);

@@ -445,6 +445,37 @@ class OccupancyVDBMapping:
             origins, masks = self.sectionMorphology(origins, masks, "close", iterations)
         _section_states(self._lib, self._h, -1, lo, hi, origins, masks, self._check)
 
+    def addArtificialWall(self, start, end, negative_height: float, positive_height: float) -> None:
+        """addArtificialWall (VDBMapping.hpp:1210-1236): the wall's voxels are set
+        active after every update of the map (x, y, z of start and end are used)."""
+        st = np.ascontiguousarray(np.asarray(start, np.float64)[:3])
+        en = np.ascontiguousarray(np.asarray(end, np.float64)[:3])
+        self._check(self._lib.vdbg_add_artificial_walls(self._h, 1, st.ctypes.data, en.ctypes.data,
+                                                        float(negative_height), float(positive_height)),
+                    "vdbg_add_artificial_walls")
+
+    def addArtificialPolygon(self, polygon, negative_height: float, positive_height: float) -> None:
+        """addArtificialPolygon (VDBMapping.hpp:1198-1207): walls between consecutive corners, closed."""
+        pts = np.asarray(polygon, np.float64).reshape(len(polygon), -1)[:, :3]
+        if len(pts) == 0:
+            return
+        st = np.ascontiguousarray(pts)
+        en = np.ascontiguousarray(np.roll(pts, -1, axis=0))
+        self._check(self._lib.vdbg_add_artificial_walls(self._h, len(pts), st.ctypes.data, en.ctypes.data,
+                                                        float(negative_height), float(positive_height)),
+                    "vdbg_add_artificial_walls")
+
+    def addArtificialAreas(self, areas, negative_height: float, positive_height: float) -> None:
+        """addArtificialAreas (VDBMapping.hpp:1175-1189): restoreMapIntegrity, then every polygon."""
+        self.restoreMapIntegrity()
+        for poly in areas:
+            self.addArtificialPolygon(poly, negative_height, positive_height)
+
+    def restoreMapIntegrity(self) -> None:
+        """restoreMapIntegrity (VDBMapping.hpp:1153-1166)."""
+        self._check(self._lib.vdbg_restore_map_integrity(self._h), "vdbg_restore_map_integrity")
+        self._version += 1
+
     def sectionMorphology(self, origins, masks, op: str = "close", iterations: int = 2):
         """morphologicalDilateMap / ErodeMap / CloseMap / OpenMap (VDBMapping.hpp:1094-1147)
         of a section's active voxels on the GPU: op in dilate, erode, close, open.
