@@ -16,12 +16,14 @@
 //     openvdb::FloatGrid refreshed on each getGrid() call;
 //   * only the occupancy data type (float log-odds) is implemented, which is
 //     the only specialisation the reference ships (OccupancyVDBMapping.hpp).
-// Map sections are provided (getMapSection*, applyMapSection*, the
-// bounding-box helpers; VDBMapping.hpp:811-1085) without the morphological
-// smoothing option, and so are fast mode (VDBMapping.hpp:577-602, through
-// Config::fast_mode) and the raytrace queries (VDBMapping.hpp:646-721). Other
-// parts of the reference outside the insertion path (morphology, artificial
-// areas, file I/O, the remote-mapping byte arrays) are not.
+// Also provided:
+//   * map sections (getMapSection*, applyMapSection*, the bounding-box
+//     helpers; VDBMapping.hpp:811-1085), with smoothing of update-grid
+//     sections (morphological*Map, :1094-1147);
+//   * fast mode (VDBMapping.hpp:577-602, through Config::fast_mode);
+//   * the raytrace queries (:646-721);
+//   * artificial areas (:1152-1236).
+// File I/O and the remote-mapping byte arrays are not.
 #ifndef VDB_MAPPING_GB300_VDB_MAPPING_HPP
 #define VDB_MAPPING_GB300_VDB_MAPPING_HPP
 
