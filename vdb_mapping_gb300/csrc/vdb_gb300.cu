@@ -5,7 +5,9 @@
 // or (vdbg_create_batch) a batch of independent maps sharing one pool, each
 // with its own resolution and log-odds, integrated one scan per map per call.
 // Every entry point launches its kernels on one stream and waits for them, so
-// the calls have the reference's synchronous semantics.
+// the calls have the reference's synchronous semantics. Beside insertion:
+// change sets, map sections and their morphology, the volume ray
+// intersector (fast mode, raytrace queries) and artificial areas.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
