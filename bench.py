@@ -76,6 +76,8 @@ def parse_args():
                     help="dense mode: timed inserts in fast mode (castRayIntoGridFast) after normal warm-up inserts")
     ap.add_argument("--queries", type=int, default=1 << 20, help="--workload raytrace: queries per step")
     ap.add_argument("--map-scans", type=int, default=6, help="--workload raytrace: dense scans forming the map")
+    ap.add_argument("--no-trajectory", action="store_true",
+                    help="dense mode: skip timing the whole 100-scan trajectory into one map")
     return ap.parse_args()
 
 
@@ -265,6 +267,38 @@ def cpu_baseline_single(wl, scans, n, fast_after=0):
             "sample": f"{what}, one thread, C++ oracle restating the reference path (-O2, no FMA contraction)"}
 
 
+def time_trajectory(wl, scans, new_map, flush, stream, sh):
+    """Every scan of the trajectory inserted into one fresh map, each timed
+    with CUDA events on the map's stream (device-resident points, L2 flushed
+    before each): the latency distribution over the map's whole growth,
+    including the pool extensions it needs on the way."""
+    import numpy as np
+    import torch
+
+    dev = [torch.from_numpy(p).cuda() for p, _ in scans]
+    m = new_map()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in scans]
+    updates = 0
+    torch.cuda.synchronize()
+    for k, (_, org) in enumerate(scans):
+        flush.zero_()
+        ev[k][0].record(stream)
+        m.insertPointCloud(dev[k], org, "lidar", stream=sh)
+        ev[k][1].record(stream)
+        updates += m.last_stats["updates"]
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    n_rays = sum(p.shape[0] for p, _ in scans)
+    out = {"scans": len(scans), "ms_per_insert": statistics.mean(ms),
+           "rays_per_s": n_rays / (sum(ms) / 1000.0), "voxel_updates_per_s": updates / (sum(ms) / 1000.0),
+           "latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99)),
+                          "max": max(ms), "argmax": int(np.argmax(ms))},
+           "map_leaves": m.leafCount(), "pool": m.poolInfo(), "device_bytes": m.deviceBytes()}
+    del m, dev
+    torch.cuda.synchronize()
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -282,7 +316,13 @@ def run_ours(args):
 
     wl = W.get(args.workload)
     n_scans = args.warmup + args.steps
-    scans = [wl.scan(k % wl.n_scans) for k in range(n_scans)]
+    want_traj = wl.name == "dense" and not args.no_trajectory and not args.points and not args.fast_mode
+    n_gen = max(n_scans, wl.n_scans) if want_traj else n_scans
+    from concurrent.futures import ThreadPoolExecutor
+
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
+        all_scans = list(ex.map(lambda k: wl.scan(k % wl.n_scans), range(n_gen)))
+    scans = all_scans[:n_scans]
     if args.points:
         # an evenly strided subset keeps the scan's geometry (all elevations)
         scans = [(np.ascontiguousarray(p[::max(1, p.shape[0] // args.points)][:args.points]), o) for p, o in scans]
@@ -397,6 +437,7 @@ def run_ours(args):
         "gpu_launches": launches,
         "wall_s_timed_region": wall,
         "map_leaves": m.leafCount(),
+        "pool": m.poolInfo(),
     }
     if clk:
         line["clocks"] = clk
@@ -429,6 +470,9 @@ def run_ours(args):
                        "latency_ms": {"p50": 1000 * float(np.percentile(e2e_t, 50)),
                                       "p99": 1000 * float(np.percentile(e2e_t, 99))}}
         del m2
+
+    if want_traj:
+        line["trajectory"] = time_trajectory(wl, all_scans[:wl.n_scans], new_map, flush, stream, sh)
 
     if rank == 0 and not args.no_cpu_baseline:
         fa = min(args.warmup, len(scans) - 1) if args.fast_mode else 0

@@ -166,6 +166,28 @@ int vdbg_get_timings(const vdbg_map* map, vdbg_timings* out);
 /* Device bytes held by the map. */
 int vdbg_device_bytes(const vdbg_map* map, int64_t* out);
 
+/* The map's pools (no counterpart in the reference, whose OpenVDB tree
+ * allocates node by node). Leaf and block slots live in address ranges
+ * reserved when the map is created and are backed by device memory as they
+ * are needed, so a slot never moves and growing a pool copies nothing. While
+ * a call's kernels run, the library backs and initialises the next stretch
+ * of slots when the pool is about to run short ("ahead"); a call that still
+ * runs out grows the pool on the spot ("sync") and retries its marking. */
+typedef struct vdbg_pool_info
+{
+  int64_t leaf_capacity;   /* leaf slots the kernels may use */
+  int64_t leaf_backed;     /* leaf slots backed and initialised (>= leaf_capacity) */
+  int64_t leaf_reserved;   /* leaf slots the address range can hold */
+  int64_t leaves;          /* leaves in use */
+  int64_t block_capacity;  /* 64^3-voxel block slots the kernels may use */
+  int64_t blocks;          /* blocks in use */
+  int64_t hash_entries;    /* block hash size */
+  uint64_t grow_ahead;     /* extensions prepared while kernels ran */
+  uint64_t grow_sync;      /* extensions made because a call ran out */
+} vdbg_pool_info;
+
+int vdbg_get_pool_info(const vdbg_map* map, vdbg_pool_info* out);
+
 /* Change set (the grid updateMap returns, VDBMapping.hpp:731-792): with
  * tracking on, every call that integrates (insert, integrate_update,
  * update_map, batch insert) replaces the change set with the voxels whose

@@ -81,12 +81,17 @@ def test_graph_device_inputs_at_new_addresses(vdbg):
         torch.cuda.synchronize()
         if k == 1 and len(keep) == 4:
             before = pair[0].graphStats()["captures"]
+            grown = pair[0].poolInfo()
         for b in pair:
             b.insert_packed(keep[-1], counts, [o for _, o in scans])
     assert_pair_equal(pair, wl.n_maps)
     gs = pair[0].graphStats()
     assert gs["replays"] == 5
-    assert gs["captures"] == before  # new input addresses replay the same graph
+    # New input addresses replay the same graph; only a pool extension (new
+    # capacities in the kernels' parameters) updates it.
+    after = pair[0].poolInfo()
+    extensions = (after["grow_ahead"] - grown["grow_ahead"]) + (after["grow_sync"] - grown["grow_sync"])
+    assert gs["captures"] - before <= extensions
 
 
 def test_graph_coord_range_leaves_maps_unchanged(vdbg):

@@ -159,6 +159,23 @@ class vdbg_server_stats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class vdbg_pool_info(C.Structure):
+    _fields_ = [
+        ("leaf_capacity", C.c_int64),
+        ("leaf_backed", C.c_int64),
+        ("leaf_reserved", C.c_int64),
+        ("leaves", C.c_int64),
+        ("block_capacity", C.c_int64),
+        ("blocks", C.c_int64),
+        ("hash_entries", C.c_int64),
+        ("grow_ahead", C.c_uint64),
+        ("grow_sync", C.c_uint64),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 # (name, restype, argtypes) of every exported entry point.
 _P = C.c_void_p
 _D3 = C.POINTER(C.c_double)
@@ -182,6 +199,7 @@ SIGNATURES = [
     ("vdbg_export_leaves", C.c_int, [_P, C.c_int64, _P, _P, _P, C.POINTER(C.c_int64)]),
     ("vdbg_device_bytes", C.c_int, [_P, C.POINTER(C.c_int64)]),
     ("vdbg_get_timings", C.c_int, [_P, C.POINTER(vdbg_timings)]),
+    ("vdbg_get_pool_info", C.c_int, [_P, C.POINTER(vdbg_pool_info)]),
     ("vdbg_insert_point_cloud_noalloc", C.c_int,
      [_P, _P, C.c_int64, C.c_int64, _D3, C.c_char_p, C.c_uint32, _P, C.POINTER(vdbg_scan_stats)]),
     ("vdbg_track_changes", C.c_int, [_P, C.c_int]),

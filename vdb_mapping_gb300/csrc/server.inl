@@ -149,7 +149,10 @@ void server_loop(vdbg_server* sv)
         if (sv->pending[i].empty()) continue;
         const int64_t need = static_cast<int64_t>(sv->new_leaves_est[i] * 1.25) + 1;
         int64_t grow       = 0;
-        if (need > slots_free) grow = static_cast<int64_t>(m->capacity) * kLeafSlotBytes;  // a doubling
+        // The pool grows in place by at least a quarter (grow_for).
+        int64_t grow_slots = 0;
+        if (need > slots_free) grow_slots = std::max<int64_t>(need - slots_free, static_cast<int64_t>(m->capacity) / 4);
+        grow = grow_slots * kLeafSlotBytes;
         if (budget > 0 && projected + grow > budget && !step.empty()) continue;  // wait for a later step
         if (budget > 0 && projected + grow > budget)
         {
@@ -164,7 +167,7 @@ void server_loop(vdbg_server* sv)
           continue;
         }
         projected += grow;
-        slots_free = (grow ? slots_free + static_cast<int64_t>(m->capacity) : slots_free) - need;
+        slots_free = slots_free + grow_slots - need;
         step.push_back(sv->pending[i].front());
         sv->pending[i].pop_front();
         --sv->queued;

@@ -23,6 +23,7 @@
 
 #include "kernels.cuh"
 #include "vdb_gb300.h"
+#include "vmem.h"
 
 using namespace vdbg;
 
@@ -40,6 +41,9 @@ struct Channel
   int* blist                        = nullptr;  // [PB]
   uint32_t* n_blist                 = nullptr;  // device scalar
   bool pending                      = false;    // marked since its last integration
+  // Address ranges behind upd, touched (leaf slots) and btouched, bepoch,
+  // blist (block slots), grown in place with the pools.
+  vmem::Array vm_upd, vm_touched, vm_btouched, vm_bepoch, vm_blist;
 };
 
 // Configuration of one map (OccupancyVDBMapping::setConfig).
@@ -79,16 +83,25 @@ struct vdbg_map
   bool timed_prep       = false;
   vdbg_timings timings{};
 
-  // Leaf pool.
+  // Leaf pool. `capacity` is what the kernels may allocate up to; the arrays
+  // are backed and initialised up to `cap_ready` >= capacity (the slots in
+  // between were prepared ahead on `grow` and are published by
+  // publish_growth). Slot numbers and addresses never move.
   uint32_t capacity     = 0;
+  uint32_t cap_ready    = 0;
+  uint32_t max_slots    = 0;  // address range reserved per leaf array, in slots
   float* values         = nullptr;
   unsigned long long* active = nullptr;
   int4* origin          = nullptr;
   uint32_t* flags       = nullptr;
   uint32_t n_leaves     = 0;  // host copy after the last call
-  // Block pool and block hash.
+  // Block pool and block hash (same scheme as the leaf pool).
   uint32_t bcapacity    = 0;
+  uint32_t bcap_ready   = 0;
+  uint32_t max_blocks   = 0;
   uint32_t bhash_size   = 0;
+  uint32_t hash_ready   = 0;  // entries backed; a rebuild to this size is due when > bhash_size
+  uint32_t max_hash     = 0;
   int* bleaf            = nullptr;
   int4* borigin         = nullptr;
   unsigned long long* bkeys = nullptr;
@@ -96,6 +109,20 @@ struct vdbg_map
   uint32_t n_blocks     = 0;  // host copy after the last call
   uint32_t call_leaves  = 0;  // n_leaves / n_blocks when the current call began
   uint32_t call_blocks  = 0;
+  vmem::Array vm_values, vm_active, vm_origin, vm_flags, vm_bleaf, vm_borigin, vm_bkeys, vm_bslots;
+  size_t page           = 0;  // physical page size of the device
+  // Growth ahead of need: while a call's kernels run, the pools are extended
+  // on `grow` (map + fill) when the expected demand of the next calls comes
+  // close to capacity; the extension is published once the call completed.
+  cudaStream_t grow     = nullptr;
+  cudaEvent_t ev_grow   = nullptr;
+  bool grow_pending     = false;
+  bool grow_checked     = false;  // this call has considered growing ahead
+  bool no_grow          = false;  // the current call must not allocate (no-allocation insert)
+  double leaf_hint      = 0.0;    // new leaves per call to plan for (decaying maximum)
+  double block_hint     = 0.0;
+  uint64_t grow_events  = 0;      // extensions prepared ahead
+  uint64_t grow_sync    = 0;      // extensions made inside a call that ran out
 
   DevStatus* d_status   = nullptr;
   DevStatus* h_status   = nullptr;  // pinned
@@ -131,7 +158,8 @@ struct vdbg_map
   unsigned apply_grid_blocks = 0;
   // Change set of the last integration (vdbg_track_changes).
   bool track_changes               = false;
-  uint32_t chg_cap                 = 0;  // leaf slots the arrays cover
+  uint32_t chg_cap                 = 0;  // leaf slots the arrays cover (cap_ready while tracking)
+  vmem::Array vm_chg_words, vm_chg_list, vm_chg_epoch;
   unsigned long long* chg_words    = nullptr;
   int* chg_list                    = nullptr;
   uint32_t* chg_epoch              = nullptr;
@@ -193,6 +221,24 @@ uint32_t next_pow2(uint64_t v)
   return static_cast<uint32_t>(p);
 }
 
+// VDBG_TRACE=1 in the environment: every out-of-memory decision of the host
+// code prints where it was taken (a diagnostic for users sizing pools).
+bool trace_on()
+{
+  static const bool on = [] {
+    const char* e = std::getenv("VDBG_TRACE");
+    return e && *e && *e != '0';
+  }();
+  return on;
+}
+
+int oom(const char* where, uint64_t a = 0, uint64_t b = 0)
+{
+  if (trace_on()) std::fprintf(stderr, "vdb_gb300: out of memory at %s (%llu, %llu)\n", where,
+                               static_cast<unsigned long long>(a), static_cast<unsigned long long>(b));
+  return VDBG_ERR_OUT_OF_MEMORY;
+}
+
 int set_device(const vdbg_map* m)
 {
   VDBG_CUDA(cudaSetDevice(m->device));
@@ -205,7 +251,7 @@ int dev_alloc(vdbg_map* m, T** p, size_t count)
   *p = nullptr;
   if (count == 0) return VDBG_OK;
   const size_t b = count * sizeof(T);
-  if (m->max_bytes > 0 && m->bytes + static_cast<int64_t>(b) > m->max_bytes) return VDBG_ERR_OUT_OF_MEMORY;
+  if (m->max_bytes > 0 && m->bytes + static_cast<int64_t>(b) > m->max_bytes) return oom("dev_alloc budget", b);
   VDBG_CUDA(cudaMalloc(reinterpret_cast<void**>(p), b));
   m->bytes += static_cast<int64_t>(b);
   m->layout += 1;
@@ -261,132 +307,149 @@ ChannelView channel_view(const Channel& c)
   return v;
 }
 
-// Leaf-indexed arrays of an update grid.
-int alloc_channel_leaves(vdbg_map* m, Channel& c, uint32_t cap)
-{
-  VDBG_TRY(dev_alloc(m, &c.upd, static_cast<size_t>(cap) * 16));
-  VDBG_TRY(dev_alloc(m, &c.touched, cap));
-  VDBG_CUDA(cudaMemsetAsync(c.upd, 0, static_cast<size_t>(cap) * 16 * sizeof(unsigned long long), m->stream));
-  return VDBG_OK;
-}
+// ---- pools in reserved address ranges --------------------------------------
 
-void free_channel_leaves(vdbg_map* m, Channel& c, uint32_t cap)
+int vm_error(vmem::Status st)
 {
-  dev_free(m, c.upd, static_cast<size_t>(cap) * 16);
-  dev_free(m, c.touched, cap);
-}
-
-// Block-indexed arrays of an update grid.
-int alloc_channel_blocks(vdbg_map* m, Channel& c, uint32_t bcap)
-{
-  VDBG_TRY(dev_alloc(m, &c.btouched, static_cast<size_t>(bcap) * 8));
-  VDBG_TRY(dev_alloc(m, &c.bepoch, bcap));
-  VDBG_TRY(dev_alloc(m, &c.blist, bcap));
-  VDBG_CUDA(cudaMemsetAsync(c.btouched, 0, static_cast<size_t>(bcap) * 8 * sizeof(unsigned long long), m->stream));
-  VDBG_CUDA(cudaMemsetAsync(c.bepoch, 0, static_cast<size_t>(bcap) * sizeof(uint32_t), m->stream));
-  return VDBG_OK;
-}
-
-void free_channel_blocks(vdbg_map* m, Channel& c, uint32_t bcap)
-{
-  dev_free(m, c.btouched, static_cast<size_t>(bcap) * 8);
-  dev_free(m, c.bepoch, bcap);
-  dev_free(m, c.blist, bcap);
-}
-
-// Builds the block hash of blocks [0, n) into a fresh table of `hsize` entries.
-int rebuild_hash(vdbg_map* m, uint32_t hsize, uint32_t n)
-{
-  unsigned long long* keys = nullptr;
-  int* slots               = nullptr;
-  int st                   = dev_alloc(m, &keys, hsize);
-  if (st == VDBG_OK) st = dev_alloc(m, &slots, hsize);
-  if (st != VDBG_OK)
+  switch (st)
   {
-    dev_free(m, keys, hsize);
-    dev_free(m, slots, hsize);
-    return st;
+    case vmem::Status::ok: return VDBG_OK;
+    case vmem::Status::out_of_memory: return oom("vmem");
+    case vmem::Status::no_driver:
+      std::fprintf(stderr, "vdb_gb300: CUDA virtual memory management is unavailable\n");
+      return VDBG_ERR_CUDA;
+    default: return VDBG_ERR_CUDA;
   }
-  dev_free(m, m->bkeys, m->bhash_size);
-  dev_free(m, m->bslots, m->bhash_size);
-  m->bkeys      = keys;
-  m->bslots     = slots;
+}
+
+// Reserves the address range of one pool array: `per` bytes for each of up to
+// `max_n` slots (at least `need` slots).
+int vm_reserve(vdbg_map* m, vmem::Array& a, size_t per, uint64_t need, uint64_t max_n)
+{
+  return vm_error(vmem::reserve(a, per * need, per * max_n, m->page));
+}
+
+// Backs the first `n` slots of an array of `per` bytes a slot, within the
+// map's device-memory budget.
+int vm_commit(vdbg_map* m, vmem::Array& a, size_t per, uint64_t n)
+{
+  const size_t want = vmem::round_up(per * n, m->page);
+  if (want <= a.mapped) return VDBG_OK;
+  if (m->max_bytes > 0 && m->bytes + static_cast<int64_t>(want - a.mapped) > m->max_bytes)
+    return oom("vm_commit budget", want, a.mapped);
+  size_t added = 0;
+  const int st = vm_error(vmem::commit(a, want, m->page, m->device, &added));
+  m->bytes += static_cast<int64_t>(added);
+  return st;
+}
+
+void vm_free(vdbg_map* m, vmem::Array& a)
+{
+  m->bytes -= static_cast<int64_t>(a.mapped);
+  vmem::release(a);
+}
+
+// One array of a pool: its range, bytes per slot, and the byte new slots are
+// filled with (-1: none, its slots are written before they are read).
+struct SlotArray
+{
+  vmem::Array* a;
+  size_t per;
+  int fill;
+};
+
+std::vector<SlotArray> leaf_arrays(vdbg_map* m)
+{
+  std::vector<SlotArray> v{{&m->vm_values, 512 * sizeof(float), 0},
+                           {&m->vm_active, 8 * sizeof(unsigned long long), 0},
+                           {&m->vm_origin, sizeof(int4), -1},
+                           {&m->vm_flags, sizeof(uint32_t), 0}};
+  for (Channel& c : m->channels)
+  {
+    v.push_back({&c.vm_upd, 16 * sizeof(unsigned long long), 0});
+    v.push_back({&c.vm_touched, sizeof(int), -1});
+  }
+  if (m->chg_words)
+  {
+    v.push_back({&m->vm_chg_words, 16 * sizeof(unsigned long long), -1});
+    v.push_back({&m->vm_chg_list, sizeof(int), -1});
+    v.push_back({&m->vm_chg_epoch, sizeof(uint32_t), 0});
+  }
+  return v;
+}
+
+std::vector<SlotArray> block_arrays(vdbg_map* m)
+{
+  std::vector<SlotArray> v{{&m->vm_bleaf, 512 * sizeof(int), 0xff}, {&m->vm_borigin, sizeof(int4), -1}};
+  for (Channel& c : m->channels)
+  {
+    v.push_back({&c.vm_btouched, 8 * sizeof(unsigned long long), 0});
+    v.push_back({&c.vm_bepoch, sizeof(uint32_t), 0});
+    v.push_back({&c.vm_blist, sizeof(int), -1});
+  }
+  return v;
+}
+
+// Backs slots [from, to) of every array and queues their fill on `s`.
+int extend_slots(vdbg_map* m, const std::vector<SlotArray>& arrays, uint32_t from, uint32_t to, cudaStream_t s)
+{
+  for (const SlotArray& x : arrays) VDBG_TRY(vm_commit(m, *x.a, x.per, to));
+  if (to <= from) return VDBG_OK;
+  for (const SlotArray& x : arrays)
+    if (x.fill >= 0)
+      VDBG_CUDA(cudaMemsetAsync(x.a->base + x.per * from, x.fill, x.per * (to - from), s));
+  return VDBG_OK;
+}
+
+// Reserves and backs a new update grid's arrays for the pools as they are
+// (its masks and block epochs start at zero).
+int alloc_channel(vdbg_map* m, Channel& c)
+{
+  VDBG_TRY(vm_reserve(m, c.vm_upd, 16 * sizeof(unsigned long long), m->cap_ready, m->max_slots));
+  VDBG_TRY(vm_reserve(m, c.vm_touched, sizeof(int), m->cap_ready, m->max_slots));
+  VDBG_TRY(vm_reserve(m, c.vm_btouched, 8 * sizeof(unsigned long long), m->bcap_ready, m->max_blocks));
+  VDBG_TRY(vm_reserve(m, c.vm_bepoch, sizeof(uint32_t), m->bcap_ready, m->max_blocks));
+  VDBG_TRY(vm_reserve(m, c.vm_blist, sizeof(int), m->bcap_ready, m->max_blocks));
+  c.upd      = reinterpret_cast<unsigned long long*>(c.vm_upd.base);
+  c.touched  = reinterpret_cast<int*>(c.vm_touched.base);
+  c.btouched = reinterpret_cast<unsigned long long*>(c.vm_btouched.base);
+  c.bepoch   = reinterpret_cast<uint32_t*>(c.vm_bepoch.base);
+  c.blist    = reinterpret_cast<int*>(c.vm_blist.base);
+  const std::vector<SlotArray> leaves{{&c.vm_upd, 16 * sizeof(unsigned long long), 0}, {&c.vm_touched, sizeof(int), -1}};
+  const std::vector<SlotArray> blocks{{&c.vm_btouched, 8 * sizeof(unsigned long long), 0},
+                                      {&c.vm_bepoch, sizeof(uint32_t), 0},
+                                      {&c.vm_blist, sizeof(int), -1}};
+  VDBG_TRY(extend_slots(m, leaves, 0, m->cap_ready, m->stream));
+  VDBG_TRY(extend_slots(m, blocks, 0, m->bcap_ready, m->stream));
+  return VDBG_OK;
+}
+
+void free_channel(vdbg_map* m, Channel& c)
+{
+  for (vmem::Array* a : {&c.vm_upd, &c.vm_touched, &c.vm_btouched, &c.vm_bepoch, &c.vm_blist}) vm_free(m, *a);
+  c.upd = nullptr, c.touched = nullptr, c.btouched = nullptr, c.bepoch = nullptr, c.blist = nullptr;
+}
+
+// Rebuilds the block hash in place with `hsize` entries from blocks [0, n),
+// queued on `s`.
+int rebuild_hash(vdbg_map* m, uint32_t hsize, uint32_t n, cudaStream_t s)
+{
+  if (hsize > m->max_hash) return oom("rebuild_hash", hsize, m->max_hash);
+  VDBG_TRY(vm_commit(m, m->vm_bkeys, sizeof(unsigned long long), hsize));
+  VDBG_TRY(vm_commit(m, m->vm_bslots, sizeof(int), hsize));
+  m->hash_ready = std::max(m->hash_ready, hsize);
   m->bhash_size = hsize;
-  VDBG_CUDA(cudaMemsetAsync(m->bkeys, 0xff, static_cast<size_t>(hsize) * sizeof(unsigned long long), m->stream));
-  VDBG_CUDA(cudaMemsetAsync(m->bslots, 0xff, static_cast<size_t>(hsize) * sizeof(int), m->stream));
+  m->layout += 1;
+  VDBG_CUDA(cudaMemsetAsync(m->bkeys, 0xff, static_cast<size_t>(hsize) * sizeof(unsigned long long), s));
+  VDBG_CUDA(cudaMemsetAsync(m->bslots, 0xff, static_cast<size_t>(hsize) * sizeof(int), s));
   if (n > 0)
   {
-    k_rehash<<<(n + 255) / 256, 256, 0, m->stream>>>(map_view(m), n);
+    k_rehash<<<(n + 255) / 256, 256, 0, s>>>(map_view(m), n);
     VDBG_CUDA(cudaGetLastError());
   }
   return VDBG_OK;
 }
-
-// Allocates the leaf pool with `cap` slots, keeping leaves [0, keep). The
-// block tables keep their slot numbers, so nothing else moves.
-int resize_pool(vdbg_map* m, uint32_t cap, uint32_t keep)
-{
-  float* values              = nullptr;
-  unsigned long long* active = nullptr;
-  int4* origin               = nullptr;
-  uint32_t* flags            = nullptr;
-  std::vector<Channel> fresh(m->channels.size());
-  int st = dev_alloc(m, &values, static_cast<size_t>(cap) * 512);
-  if (st == VDBG_OK) st = dev_alloc(m, &active, static_cast<size_t>(cap) * 8);
-  if (st == VDBG_OK) st = dev_alloc(m, &origin, cap);
-  if (st == VDBG_OK) st = dev_alloc(m, &flags, cap);
-  for (size_t i = 0; i < fresh.size() && st == VDBG_OK; ++i) st = alloc_channel_leaves(m, fresh[i], cap);
-  if (st != VDBG_OK)
-  {
-    // Leave the map as it was.
-    dev_free(m, values, static_cast<size_t>(cap) * 512);
-    dev_free(m, active, static_cast<size_t>(cap) * 8);
-    dev_free(m, origin, cap);
-    dev_free(m, flags, cap);
-    for (Channel& c : fresh) free_channel_leaves(m, c, cap);
-    return st;
-  }
-  cudaStream_t s = m->stream;
-  VDBG_CUDA(cudaMemsetAsync(values, 0, static_cast<size_t>(cap) * 512 * sizeof(float), s));
-  VDBG_CUDA(cudaMemsetAsync(active, 0, static_cast<size_t>(cap) * 8 * sizeof(unsigned long long), s));
-  VDBG_CUDA(cudaMemsetAsync(flags, 0, static_cast<size_t>(cap) * sizeof(uint32_t), s));
-  if (keep > 0)
-  {
-    VDBG_CUDA(cudaMemcpyAsync(values, m->values, static_cast<size_t>(keep) * 512 * sizeof(float),
-                              cudaMemcpyDeviceToDevice, s));
-    VDBG_CUDA(cudaMemcpyAsync(active, m->active, static_cast<size_t>(keep) * 8 * sizeof(unsigned long long),
-                              cudaMemcpyDeviceToDevice, s));
-    VDBG_CUDA(cudaMemcpyAsync(origin, m->origin, static_cast<size_t>(keep) * sizeof(int4),
-                              cudaMemcpyDeviceToDevice, s));
-    VDBG_CUDA(cudaMemcpyAsync(flags, m->flags, static_cast<size_t>(keep) * sizeof(uint32_t),
-                              cudaMemcpyDeviceToDevice, s));
-  }
-  for (size_t i = 0; i < m->channels.size(); ++i)
-  {
-    Channel& c  = m->channels[i];
-    Channel& nc = fresh[i];
-    if (keep > 0)
-    {
-      VDBG_CUDA(cudaMemcpyAsync(nc.upd, c.upd, static_cast<size_t>(keep) * 16 * sizeof(unsigned long long),
-                                cudaMemcpyDeviceToDevice, s));
-    }
-    VDBG_CUDA(cudaStreamSynchronize(s));
-    free_channel_leaves(m, c, m->capacity);
-    c.upd     = nc.upd;
-    c.touched = nc.touched;
-  }
-  VDBG_CUDA(cudaStreamSynchronize(s));
-  dev_free(m, m->values, static_cast<size_t>(m->capacity) * 512);
-  dev_free(m, m->active, static_cast<size_t>(m->capacity) * 8);
-  dev_free(m, m->origin, m->capacity);
-  dev_free(m, m->flags, m->capacity);
-  m->values   = values;
-  m->active   = active;
-  m->origin   = origin;
-  m->flags    = flags;
-  m->capacity = cap;
-  return VDBG_OK;
-}
+int rebuild_hash(vdbg_map* m, uint32_t hsize, uint32_t n) { return rebuild_hash(m, hsize, n, m->stream); }
 
 // Block hash entries for `bcap` blocks at the tuned load factor (power of two).
 uint32_t hash_size_for(const vdbg_map* m, uint32_t bcap)
@@ -395,61 +458,108 @@ uint32_t hash_size_for(const vdbg_map* m, uint32_t bcap)
   return next_pow2(static_cast<uint64_t>(std::ceil(static_cast<double>(bcap) / load)));
 }
 
-// Allocates the block pool with `bcap` blocks, keeping blocks [0, keep), and
-// rebuilds the block hash.
-int resize_blocks(vdbg_map* m, uint32_t bcap, uint32_t keep)
+// Makes growth prepared ahead visible to the kernels: waits for its fills
+// (normally long complete) and rebuilds the block hash when it was sized up.
+int publish_growth(vdbg_map* m, cudaStream_t s)
 {
-  int* bleaf    = nullptr;
-  int4* borigin = nullptr;
-  std::vector<Channel> fresh(m->channels.size());
-  int st = dev_alloc(m, &bleaf, static_cast<size_t>(bcap) * 512);
-  if (st == VDBG_OK) st = dev_alloc(m, &borigin, bcap);
-  for (size_t i = 0; i < fresh.size() && st == VDBG_OK; ++i) st = alloc_channel_blocks(m, fresh[i], bcap);
-  if (st != VDBG_OK)
+  if (!m->grow_pending) return VDBG_OK;
+  m->grow_pending = false;
+  VDBG_CUDA(cudaEventSynchronize(m->ev_grow));
+  m->capacity  = std::max(m->capacity, m->cap_ready);
+  m->bcapacity = std::max(m->bcapacity, m->bcap_ready);
+  m->layout += 1;  // MapView of a captured step changes
+  if (m->hash_ready > m->bhash_size)
   {
-    dev_free(m, bleaf, static_cast<size_t>(bcap) * 512);
-    dev_free(m, borigin, bcap);
-    for (Channel& c : fresh) free_channel_blocks(m, c, bcap);
-    return st;
-  }
-  cudaStream_t s = m->stream;
-  VDBG_CUDA(cudaMemsetAsync(bleaf, 0xff, static_cast<size_t>(bcap) * 512 * sizeof(int), s));
-  if (keep > 0)
-  {
-    VDBG_CUDA(cudaMemcpyAsync(bleaf, m->bleaf, static_cast<size_t>(keep) * 512 * sizeof(int),
-                              cudaMemcpyDeviceToDevice, s));
-    VDBG_CUDA(cudaMemcpyAsync(borigin, m->borigin, static_cast<size_t>(keep) * sizeof(int4),
-                              cudaMemcpyDeviceToDevice, s));
-  }
-  for (size_t i = 0; i < m->channels.size(); ++i)
-  {
-    Channel& c  = m->channels[i];
-    Channel& nc = fresh[i];
-    if (keep > 0)
-    {
-      VDBG_CUDA(cudaMemcpyAsync(nc.btouched, c.btouched, static_cast<size_t>(keep) * 8 * sizeof(unsigned long long),
-                                cudaMemcpyDeviceToDevice, s));
-      VDBG_CUDA(cudaMemcpyAsync(nc.bepoch, c.bepoch, static_cast<size_t>(keep) * sizeof(uint32_t),
-                                cudaMemcpyDeviceToDevice, s));
-      VDBG_CUDA(cudaMemcpyAsync(nc.blist, c.blist, static_cast<size_t>(keep) * sizeof(int),
-                                cudaMemcpyDeviceToDevice, s));
-    }
+    VDBG_TRY(rebuild_hash(m, m->hash_ready, m->n_blocks, s));
+    // Later work may be queued on another stream.
     VDBG_CUDA(cudaStreamSynchronize(s));
-    free_channel_blocks(m, c, m->bcapacity);
-    c.btouched = nc.btouched;
-    c.bepoch   = nc.bepoch;
-    c.blist    = nc.blist;
   }
-  VDBG_CUDA(cudaStreamSynchronize(s));
-  dev_free(m, m->bleaf, static_cast<size_t>(m->bcapacity) * 512);
-  dev_free(m, m->borigin, m->bcapacity);
-  m->bleaf     = bleaf;
-  m->borigin   = borigin;
-  m->bcapacity = bcap;
-  VDBG_TRY(rebuild_hash(m, hash_size_for(m, bcap), keep));
-  // Work queued by the caller on another stream must see the new tables.
-  VDBG_CUDA(cudaStreamSynchronize(s));
   return VDBG_OK;
+}
+
+// Grows the leaf pool to `cap` slots now (published at once), on `s`.
+int grow_leaves_now(vdbg_map* m, uint32_t cap, cudaStream_t s)
+{
+  VDBG_TRY(publish_growth(m, s));
+  if (cap <= m->capacity) return VDBG_OK;
+  if (cap > m->max_slots) return oom("grow_leaves_now", cap, m->max_slots);
+  if (cap > m->cap_ready)
+  {
+    VDBG_TRY(extend_slots(m, leaf_arrays(m), m->cap_ready, cap, s));
+    m->cap_ready = cap;
+    if (m->chg_words) m->chg_cap = cap;
+  }
+  m->capacity = cap;
+  m->layout += 1;
+  return VDBG_OK;
+}
+
+// Grows the block pool to `bcap` blocks now, with the hash sized for it.
+// The hash is rebuilt when it grows; `rehash` rebuilds it in any case, which
+// drops the entries of block allocations that failed (a marking that ran out
+// of blocks leaves them behind, and they would fail again).
+int grow_blocks_now(vdbg_map* m, uint32_t bcap, cudaStream_t s, bool rehash = false)
+{
+  VDBG_TRY(publish_growth(m, s));
+  if (bcap > m->max_blocks) return oom("grow_blocks_now", bcap, m->max_blocks);
+  if (bcap > m->bcapacity)
+  {
+    if (bcap > m->bcap_ready)
+    {
+      VDBG_TRY(extend_slots(m, block_arrays(m), m->bcap_ready, bcap, s));
+      m->bcap_ready = bcap;
+    }
+    m->bcapacity = bcap;
+    m->layout += 1;
+  }
+  const uint32_t h = hash_size_for(m, m->bcapacity);
+  if (h > m->bhash_size || rehash) VDBG_TRY(rebuild_hash(m, std::max(h, m->bhash_size), m->n_blocks, s));
+  return VDBG_OK;
+}
+
+// Reserves the pools' address ranges and backs `cap` leaf and `bcap` block
+// slots (a new map).
+int create_pools(vdbg_map* m, uint32_t cap, uint32_t bcap)
+{
+  if (!vmem::api()) return vm_error(vmem::Status::no_driver);
+  m->page = vmem::granularity(m->device);
+  if (m->page == 0) return VDBG_ERR_CUDA;
+  size_t free_b = 0, total_b = 0;
+  VDBG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const uint64_t budget = m->max_bytes > 0 ? std::min<uint64_t>(m->max_bytes, total_b) : total_b;
+  // Address space for every slot the device (or the budget) could hold.
+  uint64_t slots = std::max<uint64_t>(cap, budget / (512 * sizeof(float)));
+  slots          = std::min<uint64_t>((slots + 1023) & ~uint64_t(1023), uint64_t(1) << 30);
+  m->max_slots   = static_cast<uint32_t>(slots);
+  m->max_blocks  = static_cast<uint32_t>(std::min<uint64_t>(std::max<uint64_t>(bcap, slots / 4), uint64_t(1) << 28));
+  m->max_hash    = next_pow2(std::min<uint64_t>(static_cast<uint64_t>(m->max_blocks) * 20, uint64_t(1) << 31));
+  for (const SlotArray& x : leaf_arrays(m)) VDBG_TRY(vm_reserve(m, *x.a, x.per, cap, m->max_slots));
+  for (const SlotArray& x : block_arrays(m)) VDBG_TRY(vm_reserve(m, *x.a, x.per, bcap, m->max_blocks));
+  const uint32_t h = hash_size_for(m, bcap);
+  VDBG_TRY(vm_reserve(m, m->vm_bkeys, sizeof(unsigned long long), h, m->max_hash));
+  VDBG_TRY(vm_reserve(m, m->vm_bslots, sizeof(int), h, m->max_hash));
+  m->values  = reinterpret_cast<float*>(m->vm_values.base);
+  m->active  = reinterpret_cast<unsigned long long*>(m->vm_active.base);
+  m->origin  = reinterpret_cast<int4*>(m->vm_origin.base);
+  m->flags   = reinterpret_cast<uint32_t*>(m->vm_flags.base);
+  m->bleaf   = reinterpret_cast<int*>(m->vm_bleaf.base);
+  m->borigin = reinterpret_cast<int4*>(m->vm_borigin.base);
+  m->bkeys   = reinterpret_cast<unsigned long long*>(m->vm_bkeys.base);
+  m->bslots  = reinterpret_cast<int*>(m->vm_bslots.base);
+  VDBG_TRY(grow_leaves_now(m, cap, m->stream));
+  VDBG_TRY(grow_blocks_now(m, bcap, m->stream));
+  return VDBG_OK;
+}
+
+void free_pools(vdbg_map* m)
+{
+  for (const SlotArray& x : leaf_arrays(m)) vm_free(m, *x.a);
+  for (const SlotArray& x : block_arrays(m)) vm_free(m, *x.a);
+  vm_free(m, m->vm_bkeys);
+  vm_free(m, m->vm_bslots);
+  m->values = nullptr, m->active = nullptr, m->origin = nullptr, m->flags = nullptr;
+  m->bleaf = nullptr, m->borigin = nullptr, m->bkeys = nullptr, m->bslots = nullptr;
+  m->capacity = m->cap_ready = m->bcapacity = m->bcap_ready = m->bhash_size = m->hash_ready = 0;
 }
 
 int ensure_scratch(vdbg_map* m, int64_t n, int64_t stride, bool host_input)
@@ -506,9 +616,14 @@ bool origin_to_index(const MapConf& mc, const double o[3], int out[3])
 
 void clear_status(DevStatus* h) { std::memset(h, 0, sizeof(DevStatus)); }
 
+void grow_ahead(vdbg_map* m);
+int publish_growth(vdbg_map* m, cudaStream_t s);
+
 int begin_call(vdbg_map* m, cudaStream_t s)
 {
   VDBG_TRY(set_device(m));
+  VDBG_TRY(publish_growth(m, s));
+  m->grow_checked = false;
   m->timings.launches_total += m->timings.launches;
   const uint64_t total = m->timings.launches_total;
   m->timings           = vdbg_timings{};
@@ -528,6 +643,7 @@ int fetch_status(vdbg_map* m, cudaStream_t s)
 {
   VDBG_CUDA(cudaEventRecord(m->ev1, s));
   VDBG_CUDA(cudaMemcpyAsync(m->h_status, m->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+  grow_ahead(m);  // while the device works through the call
   VDBG_CUDA(cudaStreamSynchronize(s));
   return VDBG_OK;
 }
@@ -809,7 +925,7 @@ int settle_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* orde
         return VDBG_ERR_COORD_RANGE;
       }
       if (err & (kErrSpin | kErrStepBound)) return map_error(err);
-      if (!may_grow || attempt >= 40) return VDBG_ERR_OUT_OF_MEMORY;
+      if (!may_grow || attempt >= 40) return oom("settle_dda_passes", attempt, err);
       if (err & kErrPoolFull) VDBG_TRY(grow_for(m, m->h_status->n_leaves));
       if (err & kErrBlockFull) VDBG_TRY(grow_blocks_for(m, m->h_status->n_blocks));
       if ((err & kErrHashFull) && !(err & kErrBlockFull))
@@ -896,25 +1012,39 @@ int run_dda_passes(vdbg_map* m, Channel& c, const int4* rays, const int* order, 
 // of touched leaves, then sweep them.
 void free_changes(vdbg_map* m)
 {
-  dev_free(m, m->chg_words, static_cast<size_t>(m->chg_cap) * 16);
-  dev_free(m, m->chg_list, m->chg_cap);
-  dev_free(m, m->chg_epoch, m->chg_cap);
+  vm_free(m, m->vm_chg_words);
+  vm_free(m, m->vm_chg_list);
+  vm_free(m, m->vm_chg_epoch);
   dev_free(m, m->chg_count, 1);
-  m->chg_cap = 0;
+  m->chg_words = nullptr;
+  m->chg_list  = nullptr;
+  m->chg_epoch = nullptr;
+  m->chg_cap   = 0;
 }
 
-// Change-set arrays for the current leaf capacity (their contents only live
-// for one integration, so a resize starts them empty).
+// Change-set arrays for every backed leaf slot (their contents only live for
+// one integration; the epochs start at zero). Once they exist they grow with
+// the leaf pool.
 int ensure_changes(vdbg_map* m, cudaStream_t s)
 {
-  if (m->chg_cap == m->capacity && m->chg_words) return VDBG_OK;
-  free_changes(m);
-  const uint32_t cap = m->capacity;
-  VDBG_TRY(dev_alloc(m, &m->chg_words, static_cast<size_t>(cap) * 16));
-  VDBG_TRY(dev_alloc(m, &m->chg_list, cap));
-  VDBG_TRY(dev_alloc(m, &m->chg_epoch, cap));
-  VDBG_TRY(dev_alloc(m, &m->chg_count, 1));
-  VDBG_CUDA(cudaMemsetAsync(m->chg_epoch, 0, static_cast<size_t>(cap) * sizeof(uint32_t), s));
+  if (m->chg_words) return VDBG_OK;
+  const uint32_t cap = m->cap_ready;
+  int st             = vm_reserve(m, m->vm_chg_words, 16 * sizeof(unsigned long long), cap, m->max_slots);
+  if (st == VDBG_OK) st = vm_reserve(m, m->vm_chg_list, sizeof(int), cap, m->max_slots);
+  if (st == VDBG_OK) st = vm_reserve(m, m->vm_chg_epoch, sizeof(uint32_t), cap, m->max_slots);
+  if (st == VDBG_OK) st = dev_alloc(m, &m->chg_count, 1);
+  const std::vector<SlotArray> arrays{{&m->vm_chg_words, 16 * sizeof(unsigned long long), -1},
+                                      {&m->vm_chg_list, sizeof(int), -1},
+                                      {&m->vm_chg_epoch, sizeof(uint32_t), 0}};
+  if (st == VDBG_OK) st = extend_slots(m, arrays, 0, cap, s);
+  if (st != VDBG_OK)
+  {
+    free_changes(m);
+    return st;
+  }
+  m->chg_words = reinterpret_cast<unsigned long long*>(m->vm_chg_words.base);
+  m->chg_list  = reinterpret_cast<int*>(m->vm_chg_list.base);
+  m->chg_epoch = reinterpret_cast<uint32_t*>(m->vm_chg_epoch.base);
   VDBG_CUDA(cudaMemsetAsync(m->chg_count, 0, sizeof(uint32_t), s));
   m->chg_cap = cap;
   return VDBG_OK;
@@ -978,26 +1108,37 @@ int finish_sweep(vdbg_map* m, Channel& c, cudaStream_t s, bool gated = false)
   return VDBG_OK;
 }
 
-// Grows the leaf pool after an allocation failure (or when it is getting
-// full). `requested` is the bump counter, which counts every allocation
-// attempt of the failed pass.
+// Grows the leaf pool after an allocation failure. `requested` is the bump
+// counter, which counts every allocation attempt of the failed pass. The pool
+// grows in place (no copy), by at least a quarter.
 int grow_for(vdbg_map* m, uint64_t requested)
 {
-  const uint32_t keep = std::min<uint32_t>(m->n_leaves, m->capacity);
-  uint64_t want       = std::max<uint64_t>(static_cast<uint64_t>(m->capacity) * 2, requested + requested / 2);
-  if (want > (1ull << 30)) want = 1ull << 30;
-  if (want <= m->capacity) return VDBG_ERR_OUT_OF_MEMORY;
-  return resize_pool(m, static_cast<uint32_t>(want), keep);
+  VDBG_TRY(publish_growth(m, m->stream));
+  if (requested <= m->capacity) return VDBG_OK;  // what was prepared ahead covers it
+  uint64_t want = std::max<uint64_t>(static_cast<uint64_t>(m->capacity) * 5 / 4, requested + requested / 4);
+  want          = std::min<uint64_t>((want + 1023) & ~uint64_t(1023), m->max_slots);
+  if (want <= m->capacity) return oom("grow_for", want, m->capacity);
+  m->grow_sync += 1;
+  VDBG_TRY(grow_leaves_now(m, static_cast<uint32_t>(want), m->stream));
+  VDBG_CUDA(cudaStreamSynchronize(m->stream));
+  return VDBG_OK;
 }
 
-// Same for the block pool (which also rebuilds the block hash).
+// Same for the block pool (and its hash).
 int grow_blocks_for(vdbg_map* m, uint64_t requested)
 {
-  const uint32_t keep = std::min<uint32_t>(m->n_blocks, m->bcapacity);
-  uint64_t want       = std::max<uint64_t>(static_cast<uint64_t>(m->bcapacity) * 2, requested + requested / 2);
-  if (want > (1ull << 28)) want = 1ull << 28;
-  if (want <= m->bcapacity) return VDBG_ERR_OUT_OF_MEMORY;
-  return resize_blocks(m, static_cast<uint32_t>(want), keep);
+  VDBG_TRY(publish_growth(m, m->stream));
+  uint64_t want = std::max<uint64_t>(static_cast<uint64_t>(m->bcapacity) * 3 / 2, requested + requested / 2);
+  want          = std::min<uint64_t>(want, m->max_blocks);
+  if (requested <= m->bcapacity)
+    want = m->bcapacity;  // what was prepared ahead covers it: only the failed entries go
+  else if (want <= m->bcapacity)
+    return oom("grow_blocks_for", want, m->bcapacity);
+  else
+    m->grow_sync += 1;
+  VDBG_TRY(grow_blocks_now(m, static_cast<uint32_t>(want), m->stream, true));
+  VDBG_CUDA(cudaStreamSynchronize(m->stream));
+  return VDBG_OK;
 }
 
 int map_error(uint32_t err)
@@ -1005,20 +1146,81 @@ int map_error(uint32_t err)
   if (err & kErrCoordRange) return VDBG_ERR_COORD_RANGE;
   if (err & kErrSpin) return VDBG_ERR_TIMEOUT;
   if (err & kErrStepBound) return VDBG_ERR_CUDA;
-  return VDBG_ERR_OUT_OF_MEMORY;
+  return oom("device error word", err);
 }
 
-int maybe_grow_ahead(vdbg_map* m)
+// Slots a pool of `cap` slots holding `n` is extended to ahead of need, for
+// calls that add about `hint` slots each: nothing while four calls' worth is
+// free; otherwise room for eight calls, but at least an eighth and at most a
+// half more than now (unless two calls need more).
+uint64_t ahead_target(uint64_t cap, uint64_t n, double hint, uint64_t max_n)
 {
-  if (static_cast<uint64_t>(m->n_leaves) * 10 > static_cast<uint64_t>(m->capacity) * 7)
+  if (static_cast<double>(cap) - static_cast<double>(n) >= 4.0 * hint) return cap;
+  const uint64_t want = n + static_cast<uint64_t>(8.0 * hint);
+  const uint64_t lo   = cap + cap / 8;
+  const uint64_t hi   = std::max<uint64_t>(cap + cap / 2, n + static_cast<uint64_t>(2.0 * hint));
+  return std::min<uint64_t>(std::min(std::max(want, lo), hi), max_n);
+}
+
+// (whole 1024-slot steps: 2 MiB of values)
+uint32_t leaf_target(const vdbg_map* m, uint64_t n_leaves)
+{
+  uint64_t t = ahead_target(m->capacity, n_leaves, std::max(m->leaf_hint, 4096.0), m->max_slots);
+  t          = std::min<uint64_t>((t + 1023) & ~uint64_t(1023), m->max_slots);
+  return static_cast<uint32_t>(std::max<uint64_t>(t, m->capacity));
+}
+
+uint32_t block_target(const vdbg_map* m, uint64_t n_blocks)
+{
+  const uint64_t t = ahead_target(m->bcapacity, n_blocks, std::max(m->block_hint, 256.0), m->max_blocks);
+  return static_cast<uint32_t>(std::max<uint64_t>(t, m->bcapacity));
+}
+
+// Called while the current call's kernels run (before its first status
+// wait): when the pools are about to run short, backs and fills the next
+// stretch of slots on the `grow` stream. The kernels in flight only use slots
+// below the published capacities, so the fills overlap them safely; the new
+// slots are published when the call ends (publish_growth). Failures are left
+// to the synchronous path, which reports them if the slots are really needed.
+void grow_ahead(vdbg_map* m)
+{
+  if (m->no_grow || m->grow_checked || m->grow_pending) return;
+  m->grow_checked    = true;
+  const uint32_t lt  = leaf_target(m, m->call_leaves);
+  const uint32_t bt  = block_target(m, m->call_blocks);
+  bool any           = false;
+  if (lt > m->cap_ready && extend_slots(m, leaf_arrays(m), m->cap_ready, lt, m->grow) == VDBG_OK)
   {
-    VDBG_TRY(grow_for(m, static_cast<uint64_t>(m->capacity) * 2));
+    m->cap_ready = lt;
+    if (m->chg_words) m->chg_cap = lt;
+    any = true;
   }
-  if (static_cast<uint64_t>(m->n_blocks) * 10 > static_cast<uint64_t>(m->bcapacity) * 7)
+  if (bt > m->bcap_ready && extend_slots(m, block_arrays(m), m->bcap_ready, bt, m->grow) == VDBG_OK)
   {
-    VDBG_TRY(grow_blocks_for(m, static_cast<uint64_t>(m->bcapacity) * 2));
+    m->bcap_ready    = bt;
+    const uint32_t h = hash_size_for(m, bt);
+    if (h > m->hash_ready && h <= m->max_hash && vm_commit(m, m->vm_bkeys, sizeof(unsigned long long), h) == VDBG_OK &&
+        vm_commit(m, m->vm_bslots, sizeof(int), h) == VDBG_OK)
+      m->hash_ready = h;
+    any = true;
   }
-  return VDBG_OK;
+  if (any && cudaEventRecord(m->ev_grow, m->grow) == cudaSuccess)
+  {
+    m->grow_pending = true;
+    m->grow_events += 1;
+  }
+  cudaGetLastError();
+}
+
+// The end of a call that completed: learns the demand of a call for the
+// growth ahead, and publishes what was prepared during it.
+int end_call(vdbg_map* m, cudaStream_t s)
+{
+  const double dl = static_cast<double>(m->n_leaves) - static_cast<double>(m->call_leaves);
+  const double db = static_cast<double>(m->n_blocks) - static_cast<double>(m->call_blocks);
+  m->leaf_hint    = std::max(dl, 0.5 * m->leaf_hint);
+  m->block_hint   = std::max(db, 0.5 * m->block_hint);
+  return publish_growth(m, s);
 }
 
 cudaStream_t pick_stream(vdbg_map* m, void* stream)
@@ -1154,7 +1356,7 @@ int run_fast_marking(vdbg_map* m, Channel& c, const int4* rays, const int* order
       return VDBG_ERR_COORD_RANGE;
     }
     if (err & (kErrSpin | kErrStepBound | kErrTopoFull)) return map_error(err);
-    if (attempt >= 40) return VDBG_ERR_OUT_OF_MEMORY;
+    if (attempt >= 40) return oom("fast marking", attempt, err);
     if (err & kErrPoolFull) VDBG_TRY(grow_for(m, m->h_status->n_leaves));
     if (err & kErrBlockFull) VDBG_TRY(grow_blocks_for(m, m->h_status->n_blocks));
     if ((err & kErrHashFull) && !(err & kErrBlockFull)) VDBG_TRY(rebuild_hash(m, m->bhash_size * 2, m->n_blocks));
@@ -1263,7 +1465,7 @@ int capture_step(vdbg_map* m, Channel& c, int64_t stride, const ScanTable& t, co
   if (ei != cudaSuccess)
   {
     m->graph = nullptr;
-    return ei == cudaErrorMemoryAllocation ? VDBG_ERR_OUT_OF_MEMORY : VDBG_ERR_CUDA;
+    return ei == cudaErrorMemoryAllocation ? oom("cudaGraphInstantiate") : VDBG_ERR_CUDA;
   }
   m->graph_layout = m->layout;
   m->graph_stride = stride;
@@ -1381,7 +1583,7 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
       {
         record_timings(m);
         fill_stats(m, leaves_before, stats);
-        VDBG_TRY(maybe_grow_ahead(m));
+        VDBG_TRY(end_call(m, s));
         return call_status;
       }
     }
@@ -1407,7 +1609,7 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
       {
         record_timings(m);
         fill_stats(m, leaves_before, stats);
-        VDBG_TRY(maybe_grow_ahead(m));
+        VDBG_TRY(end_call(m, s));
         return call_status;
       }
     }
@@ -1444,7 +1646,7 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
   for (Channel* c : todo) VDBG_TRY(finish_sweep(m, *c, s));
   if (!todo.empty()) VDBG_CUDA(cudaStreamSynchronize(s));
   fill_stats(m, leaves_before, stats);
-  VDBG_TRY(maybe_grow_ahead(m));
+  VDBG_TRY(end_call(m, s));
   return call_status;
 }
 
@@ -1592,6 +1794,8 @@ int create_impl(int n_maps, const double* resolutions, const vdbg_options* optio
     return fail(VDBG_ERR_CUDA);
   if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&m->grow, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&m->ev_grow, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&m->ev_hits, cudaEventDisableTiming) != cudaSuccess)
     return fail(VDBG_ERR_CUDA);
@@ -1628,11 +1832,9 @@ int create_impl(int n_maps, const double* resolutions, const vdbg_options* optio
       return fail(VDBG_ERR_OUT_OF_MEMORY);
     if (cudaMemsetAsync(m->d_lo, 0, sizeof(LogOdds) * n_maps, m->stream) != cudaSuccess) return fail(VDBG_ERR_CUDA);
   }
-  s = resize_pool(m, cap, 0);
-  if (s != VDBG_OK) return fail(s);
-  // A block holds up to 512 leaves; maps fill blocks partly, so reserve one
+  // A block holds up to 512 leaves; maps fill blocks partly, so back one
   // block per 32 leaf slots and grow on demand.
-  s = resize_blocks(m, bcap ? bcap : std::max<uint32_t>(kMinBlocks, cap / 32), 0);
+  s = create_pools(m, cap, bcap ? bcap : std::max<uint32_t>(kMinBlocks, cap / 32));
   if (s != VDBG_OK) return fail(s);
   if (cudaStreamSynchronize(m->stream) != cudaSuccess) return fail(VDBG_ERR_CUDA);
   *out = m;
@@ -1759,22 +1961,15 @@ int vdbg_destroy(vdbg_map* m)
   if (m->stream) cudaStreamSynchronize(m->stream);
   if (m->graph) cudaGraphExecDestroy(m->graph);
   m->graph = nullptr;
+  if (m->grow) cudaStreamSynchronize(m->grow);
+  free_changes(m);
   for (Channel& c : m->channels)
   {
-    free_channel_leaves(m, c, m->capacity);
-    free_channel_blocks(m, c, m->bcapacity);
+    free_channel(m, c);
     dev_free(m, c.n_touched, 4);
     dev_free(m, c.n_blist, 1);
   }
-  dev_free(m, m->values, static_cast<size_t>(m->capacity) * 512);
-  dev_free(m, m->active, static_cast<size_t>(m->capacity) * 8);
-  dev_free(m, m->origin, m->capacity);
-  dev_free(m, m->flags, m->capacity);
-  dev_free(m, m->bleaf, static_cast<size_t>(m->bcapacity) * 512);
-  dev_free(m, m->borigin, m->bcapacity);
-  dev_free(m, m->bkeys, m->bhash_size);
-  dev_free(m, m->bslots, m->bhash_size);
-  free_changes(m);
+  free_pools(m);
   dev_free(m, m->d_status, 1);
   dev_free(m, m->d_hist, m->buckets);
   dev_free(m, m->d_cursor, m->buckets + kScanMaxTiles);
@@ -1810,6 +2005,8 @@ int vdbg_destroy(vdbg_map* m)
   if (m->ev_a1) cudaEventDestroy(m->ev_a1);
   if (m->ev_fork) cudaEventDestroy(m->ev_fork);
   if (m->ev_hits) cudaEventDestroy(m->ev_hits);
+  if (m->ev_grow) cudaEventDestroy(m->ev_grow);
+  if (m->grow) cudaStreamDestroy(m->grow);
   if (m->side) cudaStreamDestroy(m->side);
   if (m->stream) cudaStreamDestroy(m->stream);
   delete m;
@@ -1844,14 +2041,13 @@ int vdbg_add_input_source(vdbg_map* m, const char* id, double max_range, double 
   Channel c;
   c.id        = id;
   c.max_range = (max_range == 0) ? m->conf[0].max_range : max_range;
-  int st      = alloc_channel_leaves(m, c, m->capacity);
-  if (st == VDBG_OK) st = alloc_channel_blocks(m, c, m->bcapacity);
+  VDBG_TRY(publish_growth(m, m->stream));
+  int st = alloc_channel(m, c);
   if (st == VDBG_OK) st = dev_alloc(m, &c.n_touched, 4);
   if (st == VDBG_OK) st = dev_alloc(m, &c.n_blist, 1);
   if (st != VDBG_OK)
   {
-    free_channel_leaves(m, c, m->capacity);
-    free_channel_blocks(m, c, m->bcapacity);
+    free_channel(m, c);
     dev_free(m, c.n_touched, 4);
     dev_free(m, c.n_blist, 1);
     return st;
@@ -1932,6 +2128,7 @@ int vdbg_reset_map(vdbg_map* m)
   if (!m) return VDBG_ERR_INVALID_ARGUMENT;
   VDBG_TRY(set_device(m));
   cudaStream_t s      = m->stream;
+  VDBG_TRY(publish_growth(m, s));
   const uint32_t cap  = m->capacity;
   const uint32_t bcap = m->bcapacity;
   VDBG_CUDA(cudaMemsetAsync(m->values, 0, static_cast<size_t>(cap) * 512 * sizeof(float), s));
@@ -1984,6 +2181,21 @@ int vdbg_device_bytes(const vdbg_map* m, int64_t* out)
   return VDBG_OK;
 }
 
+int vdbg_get_pool_info(const vdbg_map* m, vdbg_pool_info* out)
+{
+  if (!m || !out) return VDBG_ERR_INVALID_ARGUMENT;
+  out->leaf_capacity  = m->capacity;
+  out->leaf_backed    = m->cap_ready;
+  out->leaf_reserved  = m->max_slots;
+  out->leaves         = m->n_leaves;
+  out->block_capacity = m->bcapacity;
+  out->blocks         = m->n_blocks;
+  out->hash_entries   = m->bhash_size;
+  out->grow_ahead     = m->grow_events;
+  out->grow_sync      = m->grow_sync;
+  return VDBG_OK;
+}
+
 int vdbg_set_tuning(vdbg_map* m, const vdbg_tuning* t)
 {
   if (!m || !t) return VDBG_ERR_INVALID_ARGUMENT;
@@ -1999,6 +2211,7 @@ int vdbg_set_tuning(vdbg_map* m, const vdbg_tuning* t)
     return VDBG_ERR_INVALID_ARGUMENT;
   VDBG_TRY(set_device(m));
   VDBG_CUDA(cudaStreamSynchronize(m->stream));
+  VDBG_TRY(publish_growth(m, m->stream));
   const bool rehash = t->hash_load != m->tuning.hash_load;
   if (t->dda_warps_per_sm != m->tuning.dda_warps_per_sm)
   {
@@ -2157,8 +2370,7 @@ int vdbg_create_batch(int n_maps, const double* resolutions, const vdbg_options*
   vdbg_map* m = *out;
   Channel c;
   c.id   = "";
-  int st = alloc_channel_leaves(m, c, m->capacity);
-  if (st == VDBG_OK) st = alloc_channel_blocks(m, c, m->bcapacity);
+  int st = alloc_channel(m, c);
   if (st == VDBG_OK) st = dev_alloc(m, &c.n_touched, 4);
   if (st == VDBG_OK) st = dev_alloc(m, &c.n_blist, 1);
   if (st == VDBG_OK)
@@ -2271,7 +2483,7 @@ int run_allocating(vdbg_map* m, F&& launch)
     m->n_blocks        = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
     if (err == 0u) return VDBG_OK;
     if (err & (kErrSpin | kErrStepBound | kErrCoordRange)) return map_error(err);
-    if (attempt >= 8) return VDBG_ERR_OUT_OF_MEMORY;
+    if (attempt >= 8) return oom("run_allocating", attempt, err);
     if (err & kErrPoolFull) VDBG_TRY(grow_for(m, m->h_status->n_leaves));
     if (err & kErrBlockFull) VDBG_TRY(grow_blocks_for(m, m->h_status->n_blocks));
     if ((err & kErrHashFull) && !(err & kErrBlockFull)) VDBG_TRY(rebuild_hash(m, m->bhash_size * 2, m->n_blocks));
@@ -2831,7 +3043,7 @@ int vdbg_apply_section_states(vdbg_map* m, int map, const int32_t lo[3], const i
   dev_free(m, d_o, static_cast<size_t>(n));
   dev_free(m, d_m, static_cast<size_t>(n) * 8);
   if (st != VDBG_OK) return st;
-  return maybe_grow_ahead(m);
+  return end_call(m, s);
 }
 
 int vdbg_apply_section_values(vdbg_map* m, int map, int64_t n, const int32_t* origins, const float* values,
@@ -2933,7 +3145,7 @@ int vdbg_apply_section_values(vdbg_map* m, int map, int64_t n, const int32_t* or
   dev_free(m, d_c, static_cast<size_t>(n));
   dev_free(m, d_t, tiles.size());
   if (st != VDBG_OK) return st;
-  return maybe_grow_ahead(m);
+  return end_call(m, s);
 }
 
 } // extern "C"
@@ -3022,9 +3234,21 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
   if (stats) std::memset(stats, 0, sizeof(*stats));
   const bool host_input = (flags & VDBG_POINTS_DEVICE) == 0;
   if (n > kNoAllocMaxPoints || (host_input && stride > 16)) return VDBG_ERR_SIZE_LIMIT;
+  // Change tracking needs its arrays over every backed leaf slot before
+  // anything is queued (they grow with the pool once they exist): sizing them
+  // here would allocate, and refusing after the marking would leave a
+  // half-applied scan pending.
+  if (m->track_changes && (!m->chg_words || m->chg_cap < m->cap_ready)) return VDBG_ERR_SIZE_LIMIT;
   VDBG_TRY(set_device(m));
   char* base = nullptr;
   VDBG_TRY(noalloc_scratch(m->device, &base));
+  // Nothing in this call extends the pools, not even ahead of need.
+  struct NoGrow
+  {
+    vdbg_map* m;
+    explicit NoGrow(vdbg_map* x) : m(x) { m->no_grow = true; }
+    ~NoGrow() { m->no_grow = false; }
+  } no_grow(m);
   char* p            = base;
   char* d_pts        = p;
   p += kNoAllocPtsBytes;
@@ -3093,7 +3317,8 @@ extern "C" int vdbg_insert_point_cloud_noalloc(vdbg_map* m, const float* xyz, in
   std::vector<Channel*> todo;
   for (Channel& c : m->channels)
     if (c.pending) todo.push_back(&c);
-  if (m->track_changes && !m->chg_words) return VDBG_ERR_SIZE_LIMIT;  // would allocate
+  // (The change arrays cover the pool, checked on entry, so the sweep's
+  // reset_changes finds them sized and allocates nothing.)
   if (m->track_changes) VDBG_CUDA(cudaMemsetAsync(m->chg_count, 0, sizeof(uint32_t), s));
   for (Channel* c : todo)
   {

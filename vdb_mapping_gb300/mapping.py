@@ -417,6 +417,12 @@ class OccupancyVDBMapping:
         self._check(self._lib.vdbg_device_bytes(self._h, C.byref(n)), "vdbg_device_bytes")
         return n.value
 
+    def poolInfo(self) -> dict:
+        """Leaf and block pool sizes and how often they grew (ahead / on demand)."""
+        p = _lib.vdbg_pool_info()
+        self._check(self._lib.vdbg_get_pool_info(self._h, C.byref(p)), "vdbg_get_pool_info")
+        return p.as_dict()
+
     def setTuning(self, tuning: dict) -> None:
         """Kernel launch/layout parameters (speed only; results never change)."""
         t = _lib.vdbg_tuning.from_dict(tuning)
@@ -713,6 +719,12 @@ class MapBatch:
         n = C.c_int64()
         self._check(self._lib.vdbg_device_bytes(self._h, C.byref(n)), "vdbg_device_bytes")
         return n.value
+
+    def poolInfo(self) -> dict:
+        """Leaf and block pool sizes and how often they grew (ahead / on demand)."""
+        p = _lib.vdbg_pool_info()
+        self._check(self._lib.vdbg_get_pool_info(self._h, C.byref(p)), "vdbg_get_pool_info")
+        return p.as_dict()
 
 
 class MapServer:

@@ -84,6 +84,77 @@ def _hit_cylinders(o, d, cyls, t_best):
         t_best[ok] = np.minimum(t_best[ok], t[ok])
 
 
+def _azimuth_columns(o, ax, ay, half, cols):
+    """Columns of a spinning-LiDAR grid (azimuth j * 2*pi/cols) within `half`
+    radians (plus one column) of the direction (ax, ay) seen from o."""
+    centre = np.arctan2(ay - o[1], ax - o[0])
+    step = 2 * np.pi / cols
+    j0 = int(np.floor((centre - half) / step)) - 1
+    j1 = int(np.ceil((centre + half) / step)) + 1
+    if j1 - j0 + 1 >= cols:
+        return None
+    return np.arange(j0, j1 + 1) % cols
+
+
+def _lidar_subset(cols_idx, rows, cols):
+    """Flat ray indices (row-major rows x cols grid) of the given columns."""
+    return (np.arange(rows)[:, None] * cols + cols_idx[None, :]).reshape(-1)
+
+
+def _hit_boxes_lidar(o, d, inv, boxes, t_best, rows, cols):
+    """_hit_boxes for a rows x cols LiDAR grid, testing only the columns whose
+    azimuth can reach each box (the same arithmetic per tested ray)."""
+    for lo, hi in boxes:
+        cx, cy = 0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1])
+        rad = 0.5 * np.hypot(hi[0] - lo[0], hi[1] - lo[1])
+        dist = np.hypot(cx - o[0], cy - o[1])
+        idx = None
+        if dist > rad * 1.01 + 1e-6:
+            idx = _azimuth_columns(o, cx, cy, np.arcsin(min(1.0, rad / dist)) + 1e-3, cols)
+        if idx is None:
+            sub, isub = d, inv
+        else:
+            idx = _lidar_subset(idx, rows, cols)
+            sub, isub = d[idx], inv[idx]
+        t1 = (lo - o) * isub
+        t2 = (hi - o) * isub
+        tmin = np.nanmax(np.minimum(t1, t2), axis=1)
+        tmax = np.nanmin(np.maximum(t1, t2), axis=1)
+        ok = (tmax >= tmin) & (tmax > 0) & (tmin > 1e-6)
+        if idx is None:
+            t_best[ok] = np.minimum(t_best[ok], tmin[ok])
+        else:
+            sel = idx[ok]
+            t_best[sel] = np.minimum(t_best[sel], tmin[ok])
+
+
+def _hit_cylinders_lidar(o, d, cyls, t_best, rows, cols):
+    """_hit_cylinders for a rows x cols LiDAR grid, column-culled likewise."""
+    for cx, cy, r, z0, z1 in cyls:
+        dist = np.hypot(cx - o[0], cy - o[1])
+        idx = None
+        if dist > r * 1.01 + 1e-6:
+            idx = _azimuth_columns(o, cx, cy, np.arcsin(min(1.0, r / dist)) + 1e-3, cols)
+        if idx is not None:
+            idx = _lidar_subset(idx, rows, cols)
+        sub = d if idx is None else d[idx]
+        a = sub[:, 0] ** 2 + sub[:, 1] ** 2
+        ox, oy = o[0] - cx, o[1] - cy
+        b = 2 * (ox * sub[:, 0] + oy * sub[:, 1])
+        c = ox * ox + oy * oy - r * r
+        disc = b * b - 4 * a * c
+        ok = (disc >= 0) & (a > 1e-12)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            t = (-b - np.sqrt(np.where(ok, disc, 0))) / (2 * a)
+        z = o[2] + t * sub[:, 2]
+        ok &= (t > 1e-6) & (z >= z0) & (z <= z1)
+        if idx is None:
+            t_best[ok] = np.minimum(t_best[ok], t[ok])
+        else:
+            sel = idx[ok]
+            t_best[sel] = np.minimum(t_best[sel], t[ok])
+
+
 def _hit_ground(o, d, t_best, z=0.0):
     with np.errstate(divide="ignore", invalid="ignore"):
         t = (z - o[2]) / d[:, 2]
@@ -201,6 +272,9 @@ class StreetWorkload(Workload):
             cyls.append((cx, cy, r, 0.0, rng.uniform(3, 9)))
         self.boxes, self.cyls = boxes, cyls
         self.dirs = lidar_directions(rows, cols)
+        self.rows, self.cols = rows, cols
+        with np.errstate(divide="ignore"):
+            self.inv_dirs = 1.0 / self.dirs
         self.sigma, self.no_return = sigma, no_return
         self.bounds_lo, self.bounds_hi = np.array([-100.0, -100.0, 0.0]), np.array([100.0, 100.0, 20.0])
 
@@ -217,8 +291,9 @@ class StreetWorkload(Workload):
         near_boxes = [b for b in self.boxes
                       if (b[0][0] - o[0] < reach) and (o[0] - b[1][0] < reach)]
         near_cyls = [c for c in self.cyls if abs(c[0] - o[0]) < reach]
-        _hit_boxes(o, d, near_boxes, t)
-        _hit_cylinders(o, d, near_cyls, t)
+        # Each primitive is tested against the beams whose azimuth reaches it.
+        _hit_boxes_lidar(o, d, self.inv_dirs, near_boxes, t, self.rows, self.cols)
+        _hit_cylinders_lidar(o, d, near_cyls, t, self.rows, self.cols)
         # The scene ends at its 200x200x20 m bounds: no return beyond.
         exit_t = np.full(d.shape[0], np.inf)
         _hit_room_inside(o, d, self.bounds_lo, self.bounds_hi, exit_t)
