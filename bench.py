@@ -78,6 +78,10 @@ def parse_args():
     ap.add_argument("--map-scans", type=int, default=6, help="--workload raytrace: dense scans forming the map")
     ap.add_argument("--no-trajectory", action="store_true",
                     help="dense mode: skip timing the whole 100-scan trajectory into one map")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="dense mode: skip the short batched and serving runs whose figures join the line")
+    ap.add_argument("--extras-serve-seconds", type=float, default=4.0,
+                    help="seconds of simulated traffic of the serving figures in the dense line")
     return ap.parse_args()
 
 
@@ -154,6 +158,25 @@ def max_over_ranks(seconds, dist):
     return float(t.item())
 
 
+def host_cpu():
+    """The host's CPU model and logical core count."""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware") and ":" in line:
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    if not model:
+        import platform
+
+        model = platform.processor() or platform.machine()
+    return {"model": model, "logical_cores": os.cpu_count()}
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -217,13 +240,17 @@ def run_reference(args):
             rays += threads * slice_rays
     total = sum(times)
     value = rays / total
+    config = config_block(wl, args, world)
+    config["parallelism"] = (f"{threads} CPU replicas (one map per host thread), each inserting a "
+                             f"{slice_rays}-ray slice of the step's scan into a fresh map per step")
+    config["host_cpu"] = host_cpu()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded street scene, no dataset)",
-        "config": config_block(wl, args, world),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+        "config": config,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "host_cpu": host_cpu(),
                          "sample": f"{threads} independent CPU maps (one per thread), each inserting a "
                                    f"{slice_rays}-ray slice of a {wl.name} scan per step; the C++ oracle "
                                    f"restating raycastPointCloud+updateMap, -O2, single-threaded per map like "
@@ -263,7 +290,7 @@ def cpu_baseline_single(wl, scans, n, fast_after=0):
     sec = time.perf_counter() - t0
     what = (f"{wl.name} scans {fast_after}-{fast_after + len(timed) - 1} ({rays} rays) in fast mode into a map of "
             f"scans 0-{fast_after - 1}") if fast_after else f"{wl.name} scans 0-{n - 1} ({rays} rays) into a fresh map"
-    return {"value": rays / sec, "unit": UNIT, "cores": 1, "kind": "port",
+    return {"value": rays / sec, "unit": UNIT, "cores": 1, "kind": "port", "host_cpu": host_cpu(),
             "sample": f"{what}, one thread, C++ oracle restating the reference path (-O2, no FMA contraction)"}
 
 
@@ -474,6 +501,28 @@ def run_ours(args):
     if want_traj:
         line["trajectory"] = time_trajectory(wl, all_scans[:wl.n_scans], new_map, flush, stream, sh)
 
+    # The rest of the metric (batched vs plain GPU, serving latency), from
+    # short runs of those workloads on the same GPU; `value` stays the dense
+    # insertion rate.
+    if wl.name == "dense" and world == 1 and not args.no_extras and not args.points and not args.fast_mode:
+        del flush
+        torch.cuda.synchronize()
+        bl = measure_batched(local, steps_timed=5, warmup=2, n_distinct=2, autotune=True)
+        sv = measure_serving(local, args.extras_serve_seconds, args.serve_budget_gb)
+        line["batched_over_plain"] = bl["batched_over_plain"]
+        line["batched_voxel_updates_per_s"] = bl["batched"]["voxel_updates_per_s"]
+        line["plain_per_map_voxel_updates_per_s"] = bl["plain_per_map"]["voxel_updates_per_s"]
+        line["batched_maps_bit_identical"] = bl["maps_bit_identical"]
+        line["serving_p50_ms"] = sv["latency_ms_all"]["p50"]
+        line["serving_p99_ms"] = sv["latency_ms_all"]["p99"]
+        line["extras"] = {
+            "batched": {k: bl[k] for k in ("config", "batched", "plain_per_map", "tuning", "gpu_launches_per_step",
+                                           "steps", "warmup")},
+            "serving": {k: sv[k] for k in ("config", "latency_ms", "latency_ms_all", "rays_per_s",
+                                           "voxel_updates_per_s", "mean_scans_per_step", "gpu_busy_frac",
+                                           "statuses")},
+        }
+
     if rank == 0 and not args.no_cpu_baseline:
         fa = min(args.warmup, len(scans) - 1) if args.fast_mode else 0
         line["cpu_baseline"] = cpu_baseline_single(wl, scans, min(args.cpu_scans, len(scans) - fa), fast_after=fa)
@@ -489,21 +538,20 @@ def run_ours(args):
 # Batched maps: one call per step for all maps vs one call per map
 # --------------------------------------------------------------------------
 
-def run_batched(args):
+def measure_batched(local, steps_timed, warmup, n_distinct, autotune=True, use_graph=True):
     """32 independent maps, one scan each per step: the batched entry point
     (one pass of the kernels for all maps) against the plain per-map path on
     the same scans, both on device-resident points with CUDA events, plus a
-    bit-exact comparison of every map between the two."""
+    comparison of every map between the two (map digests, vdbg_map_digest:
+    every leaf, value bit pattern and active bit). Returns the line."""
     import numpy as np
     import torch
 
     from vdb_mapping_gb300 import MapBatch, OccupancyVDBMapping
     from vdb_mapping_gb300 import workloads as W
 
-    world, rank, local = dist_env()
-    torch.cuda.set_device(local)
     wl = W.get("batched")
-    n_distinct = max(1, min(args.warmup + args.steps, args.batch_steps))
+    n_distinct = max(1, min(warmup + steps_timed, n_distinct))
     steps = [wl.step(k) for k in range(n_distinct)]
     counts = [p.shape[0] for p, _ in steps[0]]
     packed = [torch.from_numpy(np.concatenate([p for p, _ in st])).cuda() for st in steps]
@@ -514,7 +562,7 @@ def run_batched(args):
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
     tuned = None
-    if not args.no_autotune:
+    if autotune:
         # Autotuned launch parameters on the first sample steps (speed only;
         # both arms use them).
         from vdb_mapping_gb300 import autotune
@@ -523,7 +571,7 @@ def run_batched(args):
     b = MapBatch(wl.resolutions, initial_leaf_capacity=1 << 22, device=local)
     if tuned:
         b.setTuning(tuned)
-    b.useGraph(not args.no_graph)
+    b.useGraph(use_graph)
     for i, c in enumerate(wl.configs):
         b.setConfig(i, c)
     plain = []
@@ -550,13 +598,13 @@ def run_batched(args):
     phase = []
 
     def timed(fn):
-        for k in range(args.warmup):
+        for k in range(warmup):
             fn(k)
         torch.cuda.synchronize()
         phase.clear()
         ms, upd, rays = [], 0, 0
-        for i in range(args.steps):
-            k = args.warmup + i
+        for i in range(steps_timed):
+            k = warmup + i
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
@@ -576,18 +624,17 @@ def run_batched(args):
     b_phase = {k: float(np.mean([p[k] for p in phase])) for k in ("prep_ms", "dda_ms", "sweep_ms", "total_ms")}
     p_ms, p_upd, p_rays = timed(plain_step)
     clk = clocks.stop()
-    same = all(all(np.array_equal(x, y) for x, y in zip(b.exportLeaves(i), plain[i].exportLeaves()))
-               for i in range(len(plain)))
+    same = all(b.mapDigest(i) == plain[i].mapDigest() for i in range(len(plain)))
     b_s, p_s = sum(b_ms) / 1000.0, sum(p_ms) / 1000.0
     line = {
         "metric": "voxel-updates/s, 32 independent maps per step: batched call vs one call per map",
-        "value": b_upd / b_s, "unit": "voxel-updates/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1000.0 * b_s / args.steps, "higher_is_better": True,
+        "value": b_upd / b_s, "unit": "voxel-updates/s", "n_gpus": 1, "steps": steps_timed,
+        "warmup": warmup, "ms_per_step": 1000.0 * b_s / steps_timed, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 DDA / f32 log-odds",
         "data": f"synthetic (seeded batched workload, {n_distinct} distinct steps cycled)",
         "config": {**wl.describe(), "l2": "flushed between steps (256 MiB write)"},
         "batched": {"voxel_updates_per_s": b_upd / b_s, "rays_per_s": b_rays / b_s, "phases_ms": b_phase,
-                    "updates_per_step": b_upd / args.steps,
+                    "updates_per_step": b_upd / steps_timed,
                     "ms_per_step": {"p50": float(np.percentile(b_ms, 50)), "p99": float(np.percentile(b_ms, 99))}},
         "plain_per_map": {"voxel_updates_per_s": p_upd / p_s, "rays_per_s": p_rays / p_s,
                           "ms_per_step": {"p50": float(np.percentile(p_ms, 50)),
@@ -597,11 +644,25 @@ def run_batched(args):
         "tuning": tuned or "library defaults",
         "gpu_launches_per_step": {"batched": b.timings()["launches"],
                                   "plain": sum(g.timings()["launches"] for g in plain)},
-        "cuda_graph": {**b.graphStats(), "enabled": not args.no_graph,
-                       "steps": args.warmup + args.steps},
+        "cuda_graph": {**b.graphStats(), "enabled": use_graph,
+                       "steps": warmup + steps_timed},
     }
     if clk:
         line["clocks"] = clk
+    b.close()
+    for g in plain:
+        g.close()
+    torch.cuda.synchronize()
+    return line
+
+
+def run_batched(args):
+    import torch
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    line = measure_batched(local, args.steps, args.warmup, args.batch_steps, autotune=not args.no_autotune,
+                           use_graph=not args.no_graph)
     print(json.dumps(line))
     return 0
 
@@ -610,11 +671,12 @@ def run_batched(args):
 # Serving: Poisson sensor streams through the continuous-batching loop
 # --------------------------------------------------------------------------
 
-def run_serving(args):
-    """16 sensor streams with Poisson arrivals in real time for --serve-seconds
-    through MapServer; reports p50/p99 latency (submit to done) per sensor
+def measure_serving(local, seconds, budget_gb, use_graph=True):
+    """16 sensor streams with Poisson arrivals in real time for `seconds`
+    through MapServer; returns p50/p99 latency (submit to done) per sensor
     class next to rays/s and voxel-updates/s."""
     import threading
+    from concurrent.futures import ThreadPoolExecutor
 
     import numpy as np
     import torch
@@ -622,21 +684,21 @@ def run_serving(args):
     from vdb_mapping_gb300 import MapBatch, MapServer
     from vdb_mapping_gb300 import workloads as W
 
-    world, rank, local = dist_env()
-    torch.cuda.set_device(local)
     wl = W.get("serving")
     K = wl.distinct_scans
-    scans = {(i, k): wl.scan(i, k) for i in range(len(wl.streams)) for k in range(K)}
+    keys = [(i, k) for i in range(len(wl.streams)) for k in range(K)]
+    with ThreadPoolExecutor(max_workers=8) as ex:
+        scans = dict(zip(keys, ex.map(lambda ik: wl.scan(*ik), keys)))
     batch = MapBatch(wl.resolutions, initial_leaf_capacity=1 << 23, device=local)
-    batch.useGraph(not args.no_graph)
+    batch.useGraph(use_graph)
     for i, c in enumerate(wl.configs):
         batch.setConfig(i, c)
     # Warm the scratch and run buffers with one scan per map (not timed).
     batch.insert([scans[(i, 0)][0] for i in range(len(wl.streams))],
                  [scans[(i, 0)][1] for i in range(len(wl.streams))])
-    budget = int(args.serve_budget_gb * (1 << 30))
+    budget = int(budget_gb * (1 << 30))
     server = MapServer(batch, memory_budget_bytes=budget)
-    arrivals = wl.arrivals(args.serve_seconds)
+    arrivals = wl.arrivals(seconds)
     results, busy = [], 0
     counter = [0] * len(wl.streams)
     t_start = time.perf_counter()
@@ -679,7 +741,9 @@ def run_serving(args):
         "steps": st["steps"], "warmup": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 DDA / f32 log-odds",
         "data": f"synthetic (seeded rooms; {K} distinct scans per stream cycled, sensor moving)",
-        "config": {**wl.describe(), "seconds": args.serve_seconds, "memory_budget_gb": args.serve_budget_gb},
+        "config": {**wl.describe(), "seconds": seconds, "memory_budget_gb": budget_gb},
+        "latency_ms_all": {"p50": float(np.percentile(allv, 50)), "p99": float(np.percentile(allv, 99)),
+                           "max": float(max(allv)), "n": len(allv)},
         "latency_ms": {c: {"p50": float(np.percentile(v, 50)), "p99": float(np.percentile(v, 99)),
                            "max": float(max(v)), "n": len(v),
                            "sensor_period_ms": 1000.0 / (wl.streams[-1]["hz"] if c == "depth" else wl.streams[0]["hz"])}
@@ -691,12 +755,21 @@ def run_serving(args):
         "rejected": st["rejected"], "max_queued": st["max_queued"], "submit_retries_busy": busy,
         "device_bytes": st["device_bytes"],
         "statuses": sorted({r["status"] for r in results}),
-        "cuda_graph": {**batch.graphStats(), "enabled": not args.no_graph},
+        "cuda_graph": {**batch.graphStats(), "enabled": use_graph},
     }
     if clk:
         line["clocks"] = clk
-    print(json.dumps(line))
     batch.close()
+    torch.cuda.synchronize()
+    return line
+
+
+def run_serving(args):
+    import torch
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    print(json.dumps(measure_serving(local, args.serve_seconds, args.serve_budget_gb, use_graph=not args.no_graph)))
     return 0
 
 
@@ -799,6 +872,111 @@ def run_raytrace(args):
     return 0
 
 
+# --------------------------------------------------------------------------
+# Precision stress: long rays far from the world origin at 0.02 m
+# --------------------------------------------------------------------------
+
+def run_stress(args):
+    """The 20 stress scans (65,536 rays each, log-uniform 0.5-200 m from
+    (5000,-3000,40) m, 0.02 m voxels, 1% of the endpoints on voxel faces and
+    DDA tie directions), each inserted into the map after a resetMap (one scan
+    makes about 16.5M leaves, so the 20 do not fit one GPU together): rays/s
+    and voxel-updates/s from CUDA events around each insert, and the voxel
+    mismatch count of the traversal against the oracle's FP64 DDA over every
+    ray of the config (per-ray path digests)."""
+    import numpy as np
+    import torch
+
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle as O
+
+    from vdb_mapping_gb300 import OccupancyVDBMapping
+    from vdb_mapping_gb300 import workloads as W
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    wl = W.get("stress")
+    scans = [wl.scan(k) for k in range(wl.n_scans)]
+    dev = [torch.from_numpy(p).cuda() for p, _ in scans]
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    m = OccupancyVDBMapping(wl.resolution, initial_leaf_capacity=args.leaf_capacity or (1 << 25), device=local)
+    m.setConfig(wl.config)
+    m.addInputSource("s", wl.max_range, 0)
+    order = [k % wl.n_scans for k in range(args.warmup + args.steps)]
+    ms, updates, rays, visits, leaves, launches = [], 0, 0, 0, [], 0
+    clocks = ClockSampler(local)
+    clocks.start()
+    for j, k in enumerate(order):
+        m.resetMap()
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        m.insertPointCloud(dev[k], scans[k][1], "s", stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if j >= args.warmup:
+            ms.append(e0.elapsed_time(e1))
+            st = m.last_stats
+            updates += st["updates"]
+            rays += st["rays"]
+            visits += st["visits"]
+            leaves.append(m.leafCount())
+            launches += m.timings()["launches"]
+    clk = clocks.stop()
+    # Traversal parity over the whole config: every ray of every scan.
+    mismatched, checked = 0, 0
+    t0 = time.perf_counter()
+    for k in range(wl.n_scans):
+        pts, org = scans[k]
+        dg = m.rayDigests(dev[k], org, wl.max_range)
+        do = O.ray_digests(pts, org, wl.max_range, wl.resolution)
+        mismatched += int(np.any(dg != do, axis=1).sum())
+        checked += pts.shape[0]
+    parity_s = time.perf_counter() - t0
+    total_s = sum(ms) / 1000.0
+    line = {
+        "metric": "precision stress: rays/s and voxel mismatch count of the FP64 traversal against the oracle",
+        "value": rays / total_s, "unit": "rays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 DDA / f32 log-odds",
+        "data": "synthetic (seeded random rays, no dataset)",
+        "config": {"workload": "stress: 20 scans x 65,536 rays, log-uniform 0.5-200 m from (5000,-3000,40) m, "
+                               "voxel 0.02 m, max_range 250 m, 1% of endpoints on voxel faces and DDA ties",
+                   "map": "resetMap before every scan (one scan is ~16.5M leaves)",
+                   "l2": "flushed between steps (256 MiB write)"},
+        "voxel_updates_per_s": updates / total_s,
+        "latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99)), "max": max(ms)},
+        "per_scan": {"rays": rays / len(ms), "visits": visits / len(ms), "updates": updates / len(ms),
+                     "leaves": float(np.mean(leaves))},
+        "voxel_mismatch_count": mismatched,
+        "parity": {"rays_checked": checked, "rays_with_a_different_path": mismatched,
+                   "method": "per-ray path digests (visit count, voxel sequence hash, end voxel, clip flag): "
+                             "vdbg_ray_digests against the oracle's FP64 DDA, every ray of the 20 scans",
+                   "seconds": parity_s},
+        "traversal": "FP64 (no FP32 variant is shipped; the mismatch count is of the FP64 path)",
+        "gpu_launches": launches,
+    }
+    if clk:
+        line["clocks"] = clk
+    if not args.no_cpu_baseline:
+        om = O.OracleMap(wl.resolution)
+        om.setConfig(wl.config)
+        om.addInputSource("s", wl.max_range, 0)
+        pts, org = scans[0]
+        sample = np.ascontiguousarray(pts[:4096])
+        t0 = time.perf_counter()
+        om.insertPointCloud(sample, org, "s")
+        sec = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": sample.shape[0] / sec, "unit": "rays/s", "cores": 1, "kind": "port",
+                                "sample": "the first 4096 rays of stress scan 0 into a fresh map, one thread, "
+                                          "C++ oracle (-O2, no FMA contraction)"}
+    print(json.dumps(line))
+    m.close()
+    return 0
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
@@ -809,6 +987,8 @@ def main():
         return run_batched(args)
     if args.workload == "serving":
         return run_serving(args)
+    if args.workload == "stress":
+        return run_stress(args)
     return run_ours(args)
 
 

@@ -188,6 +188,31 @@ typedef struct vdbg_pool_info
 
 int vdbg_get_pool_info(const vdbg_map* map, vdbg_pool_info* out);
 
+/* Verification digests (no counterpart in the reference): numbers that
+ * summarise a traversal or a map exactly, for comparisons at sizes where
+ * exporting everything is impractical (the oracle computes the same).
+ *
+ * vdbg_ray_digests: castRayIntoGrid (VDBMapping.hpp:550-566) of every point
+ * of the cloud, as raycastPointCloud (VDBMapping.hpp:499-530) sets it up for
+ * this map with `raycast_range`, walked by the insertion's own DDA but marking
+ * nothing. out: uint64[n][2], per point: word 0 = visited voxels | clipped <<
+ * 40 | valid << 41 (NaN and infinite points are not valid), word 1 = a hash
+ * chain over the visited voxels in order and the end voxel:
+ *   k(x,y,z) = u32(x)*0x9E3779B97F4A7C15 ^ u32(y)*0xC2B2AE3D27D4EB4F
+ *              ^ u32(z)*0x165667B19E3779F9
+ *   h = 0x243F6A8885A308D3; h = fmix64(h ^ k(v)) per visited voxel v;
+ *   h = fmix64(h ^ k(end) ^ 0x5851F42D4C957F2D)
+ * (fmix64: MurmurHash3's 64-bit finaliser). The map is not changed.
+ *
+ * vdbg_map_digest: out[4] = {leaves, voxels, leaf sum, voxel sum} of map
+ * `map_index` (-1: every map of a batch), the sums mod 2^64 of fmix64(k(leaf
+ * origin)) over its leaves and of fmix64(k(x,y,z) ^ (bits << 1 | active) *
+ * 0xD6E8FEB86659FD93) over its voxels whose FP32 value bits are non-zero or
+ * that are active. */
+int vdbg_ray_digests(vdbg_map* map, const float* xyz, int64_t n, int64_t stride_bytes, const double origin[3],
+                     double raycast_range, uint32_t flags, uint64_t* out);
+int vdbg_map_digest(vdbg_map* map, int map_index, uint64_t out[4]);
+
 /* Change set (the grid updateMap returns, VDBMapping.hpp:731-792): with
  * tracking on, every call that integrates (insert, integrate_update,
  * update_map, batch insert) replaces the change set with the voxels whose

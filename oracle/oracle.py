@@ -53,6 +53,8 @@ def load():
         "vo_morphology": (I64, [I64, P, P, C.c_int, C.c_int, I64, P, P]),
         "vo_add_artificial_wall": (None, [P, C.POINTER(D), C.POINTER(D), D, D]),
         "vo_restore_map_integrity": (None, [P]),
+        "vo_ray_digests": (None, [P, I64, I64, C.POINTER(D), D, D, C.c_int, P]),
+        "vo_map_digest": (None, [P, U64P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -125,6 +127,13 @@ class OracleMap:
 
     def activeVoxelCount(self) -> int:
         return self._l.vo_active_count(self._h)
+
+    def mapDigest(self):
+        """(leaves, voxels, leaf sum, voxel sum), the map digest the library's
+        vdbg_map_digest computes."""
+        out = (C.c_uint64 * 4)()
+        self._l.vo_map_digest(self._h, out)
+        return tuple(int(v) for v in out)
 
     def exportLeaves(self):
         n = self.leafCount()
@@ -224,6 +233,18 @@ def cast_ray(o, e, cap=1 << 20):
     if n > cap:
         return cast_ray(o, e, cap=int(n))
     return out[:n].copy()
+
+
+def ray_digests(cloud, origin, max_range, res, threads=None):
+    """uint64 (N, 2) per-point traversal digests (the definition of the
+    library's vdbg_ray_digests), from the oracle's clip, quantiser and DDA."""
+    import os
+
+    arr, n, stride = _cloud(cloud)
+    out = np.zeros((n, 2), np.uint64)
+    load().vo_ray_digests(arr.ctypes.data, n, stride, _d3(origin), float(max_range), float(res),
+                          int(threads or os.cpu_count() or 1), out.ctypes.data)
+    return out
 
 
 def world_to_index(res, w, divide=False):

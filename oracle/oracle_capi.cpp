@@ -4,6 +4,7 @@
 #include "vdb_oracle.hpp"
 
 #include <algorithm>
+#include <cstring>
 
 #include <chrono>
 #include <thread>
@@ -325,6 +326,90 @@ double vo_bench_replicas(double res, const double* cfg7, const float* xyz, int64
   const auto t1 = std::chrono::steady_clock::now();
   put_stats(st[0], stats);
   return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// Verification digests (restating the definitions the library documents for
+// vdbg_ray_digests and vdbg_map_digest; computed here from the oracle's own
+// traversal and map).
+static inline uint64_t fmix64(uint64_t k)
+{
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ull;
+  k ^= k >> 33;
+  return k;
+}
+
+static inline uint64_t digest_key(int32_t x, int32_t y, int32_t z)
+{
+  return static_cast<uint64_t>(static_cast<uint32_t>(x)) * 0x9E3779B97F4A7C15ull ^
+         static_cast<uint64_t>(static_cast<uint32_t>(y)) * 0xC2B2AE3D27D4EB4Full ^
+         static_cast<uint64_t>(static_cast<uint32_t>(z)) * 0x165667B19E3779F9ull;
+}
+
+// Per point of the cloud: castRayIntoGrid's visits from the origin voxel to
+// the clipped and quantised end voxel (VDBMapping.hpp:499-566), hashed. out is
+// uint64[n][2]; the points are split over `threads` threads.
+void vo_ray_digests(const float* xyz, int64_t n, int64_t stride_floats, const double* origin, double range,
+                    double res, int threads, uint64_t* out)
+{
+  const Coord o = world_to_index(origin, res);
+  auto work     = [&](int64_t a, int64_t b) {
+    for (int64_t i = a; i < b; ++i)
+    {
+      const float* p  = xyz + i * stride_floats;
+      const RayEnd re = clip_and_quantise(origin, p[0], p[1], p[2], range, res);
+      uint64_t h = 0x243F6A8885A308D3ull, cnt = 0;
+      if (re.valid)
+      {
+        cast_ray(o, re.end, [&](const Coord& v) {
+          h = fmix64(h ^ digest_key(v.x, v.y, v.z));
+          ++cnt;
+        });
+        h = fmix64(h ^ digest_key(re.end.x, re.end.y, re.end.z) ^ 0x5851F42D4C957F2Dull);
+      }
+      out[2 * i]     = cnt | (re.clipped ? 1ull << 40 : 0ull) | (re.valid ? 1ull << 41 : 0ull);
+      out[2 * i + 1] = re.valid ? h : 0ull;
+    }
+  };
+  if (threads < 1) threads = 1;
+  std::vector<std::thread> pool;
+  const int64_t chunk = (n + threads - 1) / threads;
+  for (int t = 0; t < threads; ++t)
+  {
+    const int64_t a = t * chunk, b = std::min<int64_t>(n, a + chunk);
+    if (a < b) pool.emplace_back(work, a, b);
+  }
+  for (auto& th : pool) th.join();
+}
+
+// {leaves, voxels, leaf sum, voxel sum} of the map (OpenVDB leaf order:
+// offset = x << 6 | y << 3 | z).
+void vo_map_digest(void* h, uint64_t* out)
+{
+  uint64_t leaves = 0, voxels = 0, lsum = 0, vsum = 0;
+  for (const auto& l : static_cast<Handle*>(h)->map.map().leaves())
+  {
+    ++leaves;
+    lsum += fmix64(digest_key(l->origin.x, l->origin.y, l->origin.z));
+    for (uint32_t off = 0; off < 512; ++off)
+    {
+      uint32_t bits;
+      std::memcpy(&bits, &l->value[off], sizeof(bits));
+      const uint64_t on = (l->on[off >> 6] >> (off & 63)) & 1ull;
+      if (bits == 0u && !on) continue;
+      const int32_t x = l->origin.x + static_cast<int32_t>(off >> 6);
+      const int32_t y = l->origin.y + static_cast<int32_t>((off >> 3) & 7);
+      const int32_t z = l->origin.z + static_cast<int32_t>(off & 7);
+      ++voxels;
+      vsum += fmix64(digest_key(x, y, z) ^ ((static_cast<uint64_t>(bits) << 1) | on) * 0xD6E8FEB86659FD93ull);
+    }
+  }
+  out[0] = leaves;
+  out[1] = voxels;
+  out[2] = lsum;
+  out[3] = vsum;
 }
 
 } // extern "C"

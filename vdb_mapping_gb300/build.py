@@ -77,13 +77,15 @@ def build_oracle() -> None:
 
 
 def build_reference_tests() -> bool:
-    """The reference's own tests/mapping.cpp compiled against the oracle, when
-    the reference tree is present on this machine (oracle/_ref/)."""
-    ref = os.environ.get("VDB_MAPPING_REFERENCE", "/root/reference")
-    if not os.path.exists(os.path.join(ref, "tests", "mapping.cpp")):
-        return False
-    res = subprocess.run(["make", "-s", "-C", os.path.join(REPO_DIR, "oracle"), "ref", f"REF={ref}"],
-                         capture_output=True, text=True)
+    """The reference's own tests/mapping.cpp compiled against the oracle
+    (outputs in oracle/_ref/), where the reference tree is present: the one
+    the environment names (VDB_MAPPING_REFERENCE), else the oracle recipe's
+    default location. Elsewhere nothing is built."""
+    cmd = ["make", "-s", "-C", os.path.join(REPO_DIR, "oracle"), "ref-if-present"]
+    ref = os.environ.get("VDB_MAPPING_REFERENCE")
+    if ref:
+        cmd.append(f"REF={ref}")
+    res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         sys.stderr.write(res.stdout + res.stderr)
         raise RuntimeError("building the reference tests against the oracle failed")

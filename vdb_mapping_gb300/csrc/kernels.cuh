@@ -424,6 +424,81 @@ __device__ __forceinline__ void dda_emit(DdaWarpSmem& q, bool close, uint32_t lt
   n += static_cast<uint32_t>(__popc(em));
 }
 
+// OpenVDB's DDA<Ray<double>,0> (VDBMapping.hpp:554-558) for one ray from
+// the origin voxel o to the end voxel e: eye = o + 0.5, dir = e - o, t in
+// [0, 1]. tMax is kept as the bit pattern of a non-negative double, so the
+// argmin is an integer compare.
+struct DdaRay
+{
+  int vx, vy, vz;        // current voxel
+  int sx, sy, sz;        // steps
+  long long nx, ny, nz;  // tMax (bits)
+  double dx, dy, dz;     // tDelta
+};
+
+constexpr long long kDdaOne = 0x3ff0000000000000ll;  // bits of 1.0
+constexpr long long kDdaMax = 0x7fefffffffffffffll;  // bits of DBL_MAX
+
+__device__ __forceinline__ void dda_setup(const int o[3], const int e[3], DdaRay& r)
+{
+  int vox[3], stp[3];
+  long long nxt[3];
+  double dlt[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+  {
+    const double eye = __dadd_rn(static_cast<double>(o[a]), 0.5);
+    const double dir = __dsub_rn(static_cast<double>(e[a]), static_cast<double>(o[a]));
+    const double pos = __dadd_rn(eye, __dmul_rn(dir, 0.0));
+    vox[a]           = static_cast<int>(floor(pos));
+    if (dir == 0.0)
+    {
+      stp[a] = 0;
+      nxt[a] = kDdaMax;
+      dlt[a] = 1.7976931348623157e308;
+    }
+    else
+    {
+      const double inv = __ddiv_rn(1.0, dir);
+      if (inv > 0.0)
+      {
+        stp[a] = 1;
+        nxt[a] = __double_as_longlong(
+          __dadd_rn(0.0, __dmul_rn(__dsub_rn(static_cast<double>(vox[a] + 1), pos), inv)));
+      }
+      else
+      {
+        stp[a] = -1;
+        nxt[a] = __double_as_longlong(__dadd_rn(0.0, __dmul_rn(__dsub_rn(static_cast<double>(vox[a]), pos), inv)));
+      }
+      dlt[a] = __dmul_rn(static_cast<double>(stp[a]), inv);
+    }
+  }
+  r.vx = vox[0]; r.vy = vox[1]; r.vz = vox[2];
+  r.sx = stp[0]; r.sy = stp[1]; r.sz = stp[2];
+  r.nx = nxt[0]; r.ny = nxt[1]; r.nz = nxt[2];
+  r.dx = dlt[0]; r.dy = dlt[1]; r.dz = dlt[2];
+}
+
+// DDA::step(): argmin of tMax with ties to the higher axis, branch-free; the
+// sequential tMax += tDelta in FP64. Returns the bits of the t it stepped at
+// (the ray goes on while that is <= 1.0).
+__device__ __forceinline__ long long dda_advance(DdaRay& r)
+{
+  const bool ax      = (r.nx < r.ny) && (r.nx < r.nz);
+  const bool ay      = !ax && (r.ny < r.nz);
+  const long long t0 = ax ? r.nx : (ay ? r.ny : r.nz);
+  const double d     = ax ? r.dx : (ay ? r.dy : r.dz);
+  const long long tn = __double_as_longlong(__dadd_rn(__longlong_as_double(t0), d));
+  r.nx               = ax ? tn : r.nx;
+  r.ny               = ay ? tn : r.ny;
+  r.nz               = (!ax && !ay) ? tn : r.nz;
+  r.vx += ax ? r.sx : 0;
+  r.vy += ay ? r.sy : 0;
+  r.vz += (!ax && !ay) ? r.sz : 0;
+  return t0;
+}
+
 __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __restrict__ rays,
                                                                const int* __restrict__ order, ScanTable t,
                                                                MapView m, RunBuffer rb,
@@ -468,8 +543,7 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
     budget = l.budget;
     map    = static_cast<int>(l.map);
   }
-  const long long kOne = __double_as_longlong(1.0);
-  const long long kMax = __double_as_longlong(1.7976931348623157e308);
+  const long long kOne = kDdaOne;
   bool paused          = false;
 
   for (;;)
@@ -512,45 +586,13 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
           const ScanGeom& g = scan_geom(t, scan_of_ray(t, static_cast<uint32_t>(ri)));
           map               = g.map;
           const int o[3]    = {g.ovx, g.ovy, g.ovz};
-          const int e[3] = {r.x, r.y, r.z};
-          int vox[3], stp[3];
-          long long nxt[3];
-          double dlt[3];
-#pragma unroll
-          for (int a = 0; a < 3; ++a)
-          {
-            const double eye = __dadd_rn(static_cast<double>(o[a]), 0.5);
-            const double dir = __dsub_rn(static_cast<double>(e[a]), static_cast<double>(o[a]));
-            const double pos = __dadd_rn(eye, __dmul_rn(dir, 0.0));
-            vox[a]           = static_cast<int>(floor(pos));
-            if (dir == 0.0)
-            {
-              stp[a] = 0;
-              nxt[a] = kMax;
-              dlt[a] = 1.7976931348623157e308;
-            }
-            else
-            {
-              const double inv = __ddiv_rn(1.0, dir);
-              if (inv > 0.0)
-              {
-                stp[a] = 1;
-                nxt[a] = __double_as_longlong(
-                  __dadd_rn(0.0, __dmul_rn(__dsub_rn(static_cast<double>(vox[a] + 1), pos), inv)));
-              }
-              else
-              {
-                stp[a] = -1;
-                nxt[a] = __double_as_longlong(
-                  __dadd_rn(0.0, __dmul_rn(__dsub_rn(static_cast<double>(vox[a]), pos), inv)));
-              }
-              dlt[a] = __dmul_rn(static_cast<double>(stp[a]), inv);
-            }
-          }
-          vx = vox[0]; vy = vox[1]; vz = vox[2];
-          sx = stp[0]; sy = stp[1]; sz = stp[2];
-          nx = nxt[0]; ny = nxt[1]; nz = nxt[2];
-          dx = dlt[0]; dy = dlt[1]; dz = dlt[2];
+          const int e[3]    = {r.x, r.y, r.z};
+          DdaRay d;
+          dda_setup(o, e, d);
+          vx = d.vx; vy = d.vy; vz = d.vz;
+          sx = d.sx; sy = d.sy; sz = d.sz;
+          nx = d.nx; ny = d.ny; nz = d.nz;
+          dx = d.dx; dy = d.dy; dz = d.dz;
           budget   = l1 + 1;
           has_ray  = true;
           run_open = false;
@@ -582,18 +624,10 @@ __global__ void __launch_bounds__(kDdaWarps * 32, 10) k_dda_mark(const int4* __r
         rz       = vz;
         run_open = true;
         run |= 1ull << (((vy & 7) << 3) | (vx & 7));
-        // DDA::step(): argmin of tMax (ties to the higher axis), branch-free.
-        const bool ax      = (nx < ny) && (nx < nz);
-        const bool ay      = !ax && (ny < nz);
-        const long long t0 = ax ? nx : (ay ? ny : nz);
-        const double d     = ax ? dx : (ay ? dy : dz);
-        const long long tn = __double_as_longlong(__dadd_rn(__longlong_as_double(t0), d));
-        nx                 = ax ? tn : nx;
-        ny                 = ay ? tn : ny;
-        nz                 = (!ax && !ay) ? tn : nz;
-        vx += ax ? sx : 0;
-        vy += ay ? sy : 0;
-        vz += (!ax && !ay) ? sz : 0;
+        DdaRay d{vx, vy, vz, sx, sy, sz, nx, ny, nz, dx, dy, dz};
+        const long long t0 = dda_advance(d);
+        vx = d.vx; vy = d.vy; vz = d.vz;
+        nx = d.nx; ny = d.ny; nz = d.nz;
         budget -= 1;
         bool fin = t0 > kOne;
         if (!fin && budget == 0)
@@ -1965,6 +1999,107 @@ __global__ void k_artificial_restore(MapView m, const int4* __restrict__ art_o,
   }
   unsigned long long* a = active + static_cast<size_t>(slot) * 8 + w;
   *a                    = (*a & ~bits) | on;
+}
+
+// ---------------------------------------------------------------------------
+// Digests for verification at sizes where exporting a map is impractical.
+// Both are restated in the oracle (oracle_capi.cpp), which computes the same
+// numbers from its own traversal and map.
+//   voxel key  k(x,y,z) = u32(x)*0x9E3779B97F4A7C15 ^ u32(y)*0xC2B2AE3D27D4EB4F
+//                         ^ u32(z)*0x165667B19E3779F9
+//   ray digest: h = 0x243F6A8885A308D3, then h = mix64(h ^ k(v)) for every
+//               voxel castRayIntoGrid visits, in order; finally
+//               h = mix64(h ^ k(end) ^ 0x5851F42D4C957F2D)
+//               word 0: visits | clipped << 40 | valid << 41; word 1: h
+//   map digest: over the map's leaves, sums (mod 2^64) of mix64(k(origin))
+//               and, over its voxels whose value bits are non-zero or that
+//               are active, of mix64(k(x,y,z) ^ (bits << 1 | active) *
+//               0xD6E8FEB86659FD93); plus the counts of both.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long digest_key(int x, int y, int z)
+{
+  return static_cast<unsigned long long>(static_cast<uint32_t>(x)) * 0x9E3779B97F4A7C15ull ^
+         static_cast<unsigned long long>(static_cast<uint32_t>(y)) * 0xC2B2AE3D27D4EB4Full ^
+         static_cast<unsigned long long>(static_cast<uint32_t>(z)) * 0x165667B19E3779F9ull;
+}
+
+// One thread per ray record (k_prep's output, point order): the DDA of
+// k_dda_mark (dda_setup / dda_advance) walked alone, hashed as above.
+__global__ void __launch_bounds__(256) k_ray_digest(const int4* __restrict__ rays, int64_t n, ScanTable t,
+                                                    unsigned long long* __restrict__ out, DevStatus* st)
+{
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int4 r            = rays[i];
+  const uint32_t meta     = static_cast<uint32_t>(r.w);
+  const bool valid        = (meta & kMetaValid) != 0u;
+  const bool clipped      = (meta & kMetaClipped) != 0u;
+  const uint32_t l1       = meta & kMetaL1Mask;
+  unsigned long long h    = 0x243F6A8885A308D3ull;
+  unsigned long long cnt  = 0;
+  if (valid && l1 > 0)
+  {
+    const ScanGeom& g = scan_geom(t, scan_of_point(t, static_cast<uint32_t>(i)));
+    const int o[3]    = {g.ovx, g.ovy, g.ovz};
+    const int e[3]    = {r.x, r.y, r.z};
+    DdaRay d;
+    dda_setup(o, e, d);
+    for (uint32_t budget = l1 + 1;; --budget)
+    {
+      h = mix64(h ^ digest_key(d.vx, d.vy, d.vz));
+      ++cnt;
+      if (dda_advance(d) > kDdaOne) break;
+      if (budget == 1u)
+      {
+        atomicOr(&st->error, kErrStepBound);
+        break;
+      }
+    }
+  }
+  if (valid) h = mix64(h ^ digest_key(r.x, r.y, r.z) ^ 0x5851F42D4C957F2Dull);
+  out[2 * i]     = cnt | (clipped ? 1ull << 40 : 0ull) | (valid ? 1ull << 41 : 0ull);
+  out[2 * i + 1] = valid ? h : 0ull;
+}
+
+// One warp per leaf slot below `n`: the map digest of map `map` (-1: all),
+// added into out[4] = {leaves, voxels, leaf sum, voxel sum}.
+__global__ void __launch_bounds__(256) k_map_digest(const int4* __restrict__ origin,
+                                                    const uint32_t* __restrict__ flags,
+                                                    const float* __restrict__ values,
+                                                    const unsigned long long* __restrict__ active, uint32_t n,
+                                                    int map, unsigned long long* __restrict__ out)
+{
+  const uint32_t slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane      = static_cast<int>(threadIdx.x & 31);
+  if (slot >= n) return;  // (whole warps)
+  const int4 o = origin[slot];
+  if (flags[slot] == 0u || (map >= 0 && o.w != map)) return;
+  unsigned long long cnt = 0, sum = 0;
+  for (int k = lane; k < 512; k += 32)
+  {
+    // device leaf order: offset = z << 6 | y << 3 | x, mask word = z
+    const int z = k >> 6, y = (k >> 3) & 7, x = k & 7;
+    const uint32_t bits = __float_as_uint(values[static_cast<size_t>(slot) * 512 + k]);
+    const uint32_t on   = static_cast<uint32_t>((active[static_cast<size_t>(slot) * 8 + z] >> (k & 63)) & 1ull);
+    if (bits != 0u || on)
+    {
+      ++cnt;
+      sum += mix64(digest_key(o.x + x, o.y + y, o.z + z) ^
+                   ((static_cast<unsigned long long>(bits) << 1) | on) * 0xD6E8FEB86659FD93ull);
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1)
+  {
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+    sum += __shfl_xor_sync(0xffffffffu, sum, off);
+  }
+  if (lane == 0)
+  {
+    atomicAdd(out + 0, 1ull);
+    atomicAdd(out + 1, cnt);
+    atomicAdd(out + 2, mix64(digest_key(o.x, o.y, o.z)));
+    atomicAdd(out + 3, sum);
+  }
 }
 
 } // namespace vdbg

@@ -2181,6 +2181,73 @@ int vdbg_device_bytes(const vdbg_map* m, int64_t* out)
   return VDBG_OK;
 }
 
+int vdbg_ray_digests(vdbg_map* m, const float* xyz, int64_t n, int64_t stride, const double origin[3],
+                     double raycast_range, uint32_t flags, uint64_t* out)
+{
+  if (!m || m->batch || !origin || !out || bad_points(xyz, n, stride)) return VDBG_ERR_INVALID_ARGUMENT;
+  if (n == 0) return VDBG_OK;
+  std::memset(out, 0, static_cast<size_t>(n) * 2 * sizeof(uint64_t));
+  cudaStream_t s = m->stream;
+  VDBG_TRY(begin_call(m, s));
+  CastPlan plan = plan_single(m, n, origin, raycast_range);
+  if (plan.status != VDBG_OK) return plan.status;
+  if (!plan.any) return VDBG_OK;  // a NaN origin: nothing is cast
+  set_edges(m, plan.table);
+  const bool host_input = (flags & VDBG_POINTS_DEVICE) == 0;
+  VDBG_TRY(ensure_scratch(m, n, stride, host_input));
+  const char* pts = reinterpret_cast<const char*>(xyz);
+  if (host_input)
+  {
+    VDBG_CUDA(cudaMemcpyAsync(m->d_pts, xyz, static_cast<size_t>(n) * static_cast<size_t>(stride),
+                              cudaMemcpyHostToDevice, s));
+    pts = m->d_pts;
+  }
+  unsigned long long* d_out = nullptr;
+  VDBG_TRY(dev_alloc(m, &d_out, static_cast<size_t>(n) * 2));
+  const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
+  k_prep<<<blocks, 256, 0, s>>>(pts, nullptr, n, stride, plan.table, m->d_rays, nullptr, m->d_hist, m->d_status);
+  k_ray_digest<<<blocks, 256, 0, s>>>(m->d_rays, n, plan.table, d_out, m->d_status);
+  int st = cudaGetLastError() == cudaSuccess ? VDBG_OK : VDBG_ERR_CUDA;
+  // (k_prep counted the rays into the sort histogram, which must start the
+  // next insertion at zero)
+  if (st == VDBG_OK && cudaMemsetAsync(m->d_hist, 0, m->buckets * sizeof(uint32_t), s) != cudaSuccess)
+    st = VDBG_ERR_CUDA;
+  if (st == VDBG_OK && cudaMemcpyAsync(out, d_out, static_cast<size_t>(n) * 2 * sizeof(uint64_t),
+                                       cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    st = VDBG_ERR_CUDA;
+  if (st == VDBG_OK) st = fetch_status(m, s);
+  dev_free(m, d_out, static_cast<size_t>(n) * 2);
+  if (st != VDBG_OK) return st;
+  if (m->h_status->error != 0u) return map_error(m->h_status->error);
+  return VDBG_OK;
+}
+
+int vdbg_map_digest(vdbg_map* m, int map, uint64_t out[4])
+{
+  if (!m || !out || map < -1 || map >= static_cast<int>(m->conf.size())) return VDBG_ERR_INVALID_ARGUMENT;
+  VDBG_TRY(set_device(m));
+  cudaStream_t s = m->stream;
+  VDBG_CUDA(cudaStreamSynchronize(s));
+  const uint32_t n          = std::min(m->n_leaves, m->capacity);
+  unsigned long long* d_out = nullptr;
+  VDBG_TRY(dev_alloc(m, &d_out, 4));
+  int st = cudaMemsetAsync(d_out, 0, 4 * sizeof(unsigned long long), s) == cudaSuccess ? VDBG_OK : VDBG_ERR_CUDA;
+  if (st == VDBG_OK && n > 0)
+  {
+    const uint64_t threads = static_cast<uint64_t>(n) * 32;
+    k_map_digest<<<static_cast<unsigned>((threads + 255) / 256), 256, 0, s>>>(m->origin, m->flags, m->values,
+                                                                               m->active, n, map, d_out);
+    if (cudaGetLastError() != cudaSuccess) st = VDBG_ERR_CUDA;
+  }
+  unsigned long long h[4] = {0, 0, 0, 0};
+  if (st == VDBG_OK && (cudaMemcpyAsync(h, d_out, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                        cudaStreamSynchronize(s) != cudaSuccess))
+    st = VDBG_ERR_CUDA;
+  dev_free(m, d_out, 4);
+  for (int k = 0; k < 4; ++k) out[k] = h[k];
+  return st;
+}
+
 int vdbg_get_pool_info(const vdbg_map* m, vdbg_pool_info* out)
 {
   if (!m || !out) return VDBG_ERR_INVALID_ARGUMENT;

@@ -423,6 +423,24 @@ class OccupancyVDBMapping:
         self._check(self._lib.vdbg_get_pool_info(self._h, C.byref(p)), "vdbg_get_pool_info")
         return p.as_dict()
 
+    def rayDigests(self, cloud, origin, raycast_range: float) -> np.ndarray:
+        """uint64 (N, 2): per point, castRayIntoGrid's visit count with the
+        clipped and valid flags, and a hash chain over the visited voxels
+        (vdbg_ray_digests). The map is not changed."""
+        ptr, n, stride, flags, keep = _cloud_args(cloud)
+        out = np.zeros((n, 2), np.uint64)
+        s = self._lib.vdbg_ray_digests(self._h, C.c_void_p(ptr), n, stride, _origin(origin), float(raycast_range),
+                                       flags, out.ctypes.data)
+        del keep
+        self._check(s, "vdbg_ray_digests")
+        return out
+
+    def mapDigest(self) -> tuple:
+        """(leaves, voxels, leaf sum, voxel sum) of the map (vdbg_map_digest)."""
+        out = (C.c_uint64 * 4)()
+        self._check(self._lib.vdbg_map_digest(self._h, 0, out), "vdbg_map_digest")
+        return tuple(int(v) for v in out)
+
     def setTuning(self, tuning: dict) -> None:
         """Kernel launch/layout parameters (speed only; results never change)."""
         t = _lib.vdbg_tuning.from_dict(tuning)
@@ -725,6 +743,12 @@ class MapBatch:
         p = _lib.vdbg_pool_info()
         self._check(self._lib.vdbg_get_pool_info(self._h, C.byref(p)), "vdbg_get_pool_info")
         return p.as_dict()
+
+    def mapDigest(self, map_index: int) -> tuple:
+        """(leaves, voxels, leaf sum, voxel sum) of one map (vdbg_map_digest)."""
+        out = (C.c_uint64 * 4)()
+        self._check(self._lib.vdbg_map_digest(self._h, int(map_index), out), "vdbg_map_digest")
+        return tuple(int(v) for v in out)
 
 
 class MapServer:

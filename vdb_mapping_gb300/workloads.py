@@ -413,8 +413,12 @@ class BatchedWorkload:
         return _to_pcl(o, d, r), o
 
     def step(self, k):
-        """[(points, origin)] of every map at step k."""
-        return [self.scan(i, k) for i in range(self.n_maps)]
+        """[(points, origin)] of every map at step k (maps generated on
+        several threads; numpy releases the interpreter lock)."""
+        from concurrent.futures import ThreadPoolExecutor
+
+        with ThreadPoolExecutor(max_workers=8) as ex:
+            return list(ex.map(lambda i: self.scan(i, k), range(self.n_maps)))
 
     def describe(self) -> dict:
         return {"workload": self.name, "maps": self.n_maps, "steps": self.n_steps,
