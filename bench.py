@@ -78,11 +78,29 @@ def parse_args():
     ap.add_argument("--map-scans", type=int, default=6, help="--workload raytrace: dense scans forming the map")
     ap.add_argument("--no-trajectory", action="store_true",
                     help="dense mode: skip timing the whole 100-scan trajectory into one map")
+    ap.add_argument("--peaks", action="store_true",
+                    help="print the roofline denominators of this GPU (HBM copy rate and measured L2 atomic rates)")
     ap.add_argument("--no-extras", action="store_true",
                     help="dense mode: skip the short batched and serving runs whose figures join the line")
     ap.add_argument("--extras-serve-seconds", type=float, default=4.0,
                     help="seconds of simulated traffic of the serving figures in the dense line")
     return ap.parse_args()
+
+
+def l2_atomic_rates(device):
+    """Measured L2 reduction rates of this GPU (ops/s), or None."""
+    import ctypes as C
+
+    from vdb_mapping_gb300 import _lib
+
+    lib = _lib.load()
+    out = {}
+    for name, pattern in (("coalesced", 0), ("random", 1)):
+        r = C.c_double()
+        if lib.vdbg_l2_atomic_rate(int(device), pattern, C.byref(r)) != 0 or r.value <= 0:
+            return None
+        out[name] = r.value
+    return out
 
 
 def measured_peaks():
@@ -405,7 +423,18 @@ def run_ours(args):
     value = rays / total_s
     launches = sum(p["launches"] for p in phases)
 
-    # ---- roofline of the dominant kernel (live event times) -------------------
+    # ---- roofline (live event times) ------------------------------------------
+    # Algorithmic work per scan of N points, U updated voxels, Lt touched
+    # leaves and V visits:
+    #   HBM bytes of the window = 12 N (points) + 8.25 U (FP32 read+write and
+    #     the active bit per updated voxel) + 128 Lt (visited and hit masks
+    #     read once per touched leaf), over the whole insertion's kernels;
+    #   atomics of the marking = V (one visited-bit OR per DDA visit and one
+    #     hit-bit OR per unclipped ray, before any merging), over the marking
+    #     kernels (k_mark_hits, k_dda_mark, k_apply_runs), against the L2
+    #     atomic rate measured on this GPU (vdbg_l2_atomic_rate).
+    # Intermediates this design chose (ray records, the DDA run buffer) are
+    # not algorithmic: they show up in `traffic` (ncu DRAM bytes).
     hbm_peak, peak_kind = measured_peaks()
     mean = lambda key: statistics.mean(p[key] for p in phases)  # noqa: E731
     dda = mean("dda_ms")
@@ -414,29 +443,37 @@ def run_ours(args):
     prep = mean("prep_ms")
     mean_u = statistics.mean(s["updates"] for s in stats)
     mean_lt = statistics.mean(s["touched_leaves"] for s in stats)
+    mean_v = statistics.mean(s["visits"] for s in stats)
     mean_runs = mean("runs")
-    # Algorithmic bytes per launch: sweep = FP32 read+write per updated voxel
-    # + active bit r/w + visited/hit masks per touched leaf; apply = the slab
-    # runs it reads (17 B) + one 64 B visited-mask line per touched leaf;
-    # traversal = ray record + order index per ray + the runs it writes;
-    # prep = point read + ray record write.
-    alg = {
-        "k_sweep": (8.25 * mean_u + 128.0 * mean_lt, sweep),
-        "k_apply_runs": (17.0 * mean_runs + 64.0 * mean_lt, apply_ms),
-        "k_dda_mark": (20.0 * n_pts + 17.0 * mean_runs, dda - apply_ms),
-        "prep (k_prep+k_scan+k_scatter)": (36.0 * n_pts, prep),
-    }
-    if args.fast_mode:
-        # fast marking: ray record + order index per ray, one leaf slot's
-        # origin, flag and mask words per map leaf for the intersector
-        del alg["k_apply_runs"], alg["k_dda_mark"]
-        alg["fast marking (k_topo_build+k_fast_mark+k_mark_hits)"] = (20.0 * n_pts + 84.0 * m.leafCount(), dda)
-    dom = max(alg, key=lambda k: alg[k][1])
-    dom_bytes, dom_ms = alg[dom]
-    traffic = NCU_TRAFFIC_BYTES if (wl.name == "dense" and not args.points and not args.fast_mode) else {}
-    achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
-    window_bytes = 12.0 * n_pts + 8.25 * mean_u + 128.0 * mean_lt
     mean_total_ms = mean("total_ms")
+    window_bytes = 12.0 * n_pts + 8.25 * mean_u + 128.0 * mean_lt
+    traffic = NCU_TRAFFIC_BYTES if (wl.name == "dense" and not args.points and not args.fast_mode) else {}
+    hbm_achieved = window_bytes / (mean_total_ms / 1000.0) / 1e9
+    hbm = {"achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_achieved / hbm_peak,
+           "peak_kind": peak_kind, "algorithmic_bytes_per_launch": window_bytes, "launch_ms": mean_total_ms,
+           "scope": "the whole insertion (prep, marking, sweep)",
+           "traffic": sum(traffic.values()) if traffic else None}
+    atomic_rate = l2_atomic_rates(local)
+    atomic = None
+    if atomic_rate and not args.fast_mode:
+        a_achieved = mean_v / (dda / 1000.0) / 1e9
+        atomic = {"achieved": a_achieved, "peak": atomic_rate["random"] / 1e9, "unit": "G atomics/s",
+                  "frac": a_achieved / (atomic_rate["random"] / 1e9), "peak_kind": "measured (vdbg_l2_atomic_rate)",
+                  "peak_coalesced": atomic_rate["coalesced"] / 1e9, "algorithmic_atomics_per_launch": mean_v,
+                  "launch_ms": dda, "scope": "the marking (k_mark_hits, k_dda_mark, k_apply_runs)",
+                  "note": "the marking merges visits into z-plane runs and leaf masks before its ORs reach L2, so "
+                          "it issues far fewer atomics than V"}
+    top = atomic if atomic and atomic["frac"] > hbm["frac"] else hbm
+    per_kernel = {
+        "prep (k_prep+k_scan+k_scatter)": {"ms": prep, "algorithmic_bytes": 12.0 * n_pts,
+                                           "traffic": traffic.get("prep (k_prep+k_scan+k_scatter)")},
+        "marking (k_mark_hits+k_dda_mark+k_apply_runs)": {
+            "ms": dda, "algorithmic_atomics": mean_v,
+            "traffic": (traffic["k_dda_mark"] + traffic["k_apply_runs"]) if traffic else None},
+        "sweep (k_compact+k_sweep)": {"ms": sweep, "algorithmic_bytes": 8.25 * mean_u + 128.0 * mean_lt,
+                                      "GBps": (8.25 * mean_u + 128.0 * mean_lt) / (sweep / 1000.0) / 1e9,
+                                      "traffic": traffic.get("k_sweep")},
+    }
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -453,14 +490,11 @@ def run_ours(args):
                      "runs": mean_runs, "updates": mean_u, "touched_leaves": mean_lt,
                      "new_leaves": statistics.mean(s["new_leaves"] for s in stats),
                      "dda_passes": [p["passes"] for p in phases], "warmup_dda_passes": warmup_passes},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "peak_kind": peak_kind,
-                     "traffic": traffic.get(dom),
-                     "algorithmic_bytes_per_launch": dom_bytes, "launch_ms": dom_ms,
-                     "per_kernel": {k: {"GBps": b_ / (t_ / 1000.0) / 1e9 if t_ > 0 else None, "ms": t_,
-                                        "algorithmic_bytes": b_, "traffic": traffic.get(k)}
-                                    for k, (b_, t_) in alg.items()},
-                     "window_GBps": window_bytes / (mean_total_ms / 1000.0) / 1e9},
+        "roofline": {"bound": "l2_atomic" if top is atomic else "hbm",
+                     "kernel": "marking (k_mark_hits+k_dda_mark+k_apply_runs)" if top is atomic else
+                               "the whole insertion",
+                     "achieved": top["achieved"], "peak": top["peak"], "unit": top["unit"], "frac": top["frac"],
+                     "traffic": hbm["traffic"], "hbm": hbm, "atomic": atomic, "per_kernel": per_kernel},
         "gpu_launches": launches,
         "wall_s_timed_region": wall,
         "map_leaves": m.leafCount(),
@@ -977,8 +1011,25 @@ def run_stress(args):
     return 0
 
 
+def run_peaks(args):
+    import torch
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    hbm, kind = measured_peaks()
+    rates = l2_atomic_rates(local)
+    line = {"metric": "roofline denominators", "hbm_gbs": hbm, "hbm_kind": kind,
+            "l2_atomic_ops_per_s": rates, "device": torch.cuda.get_device_name(local),
+            "how": "vdbg_l2_atomic_rate: 64-bit ORs with unused results on a 32 MiB buffer, best of 3 launches "
+                   "of (SMs x 8) blocks x 256 threads x 512 ops, CUDA events"}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse_args()
+    if args.peaks:
+        return run_peaks(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "raytrace":

@@ -213,6 +213,14 @@ int vdbg_ray_digests(vdbg_map* map, const float* xyz, int64_t n, int64_t stride_
                      double raycast_range, uint32_t flags, uint64_t* out);
 int vdbg_map_digest(vdbg_map* map, int map_index, uint64_t out[4]);
 
+/* L2 atomic throughput of `device` (no counterpart in the reference): the
+ * rate of 64-bit ORs with unused results (reductions) on an L2-resident
+ * buffer, in operations per second, best of three timed launches. pattern 0:
+ * a warp ORs 32 consecutive words per request (the shape of the update-mask
+ * merges); 1: every lane a pseudo-random word (the endpoint hits). It is the
+ * denominator of the atomic half of the insertion's roofline. */
+int vdbg_l2_atomic_rate(int device, int pattern, double* ops_per_s);
+
 /* Change set (the grid updateMap returns, VDBMapping.hpp:731-792): with
  * tracking on, every call that integrates (insert, integrate_update,
  * update_map, batch insert) replaces the change set with the voxels whose

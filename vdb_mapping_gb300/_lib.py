@@ -202,6 +202,7 @@ SIGNATURES = [
     ("vdbg_get_pool_info", C.c_int, [_P, C.POINTER(vdbg_pool_info)]),
     ("vdbg_ray_digests", C.c_int, [_P, _P, C.c_int64, C.c_int64, _D3, C.c_double, C.c_uint32, _P]),
     ("vdbg_map_digest", C.c_int, [_P, C.c_int, C.POINTER(C.c_uint64)]),
+    ("vdbg_l2_atomic_rate", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("vdbg_insert_point_cloud_noalloc", C.c_int,
      [_P, _P, C.c_int64, C.c_int64, _D3, C.c_char_p, C.c_uint32, _P, C.POINTER(vdbg_scan_stats)]),
     ("vdbg_track_changes", C.c_int, [_P, C.c_int]),

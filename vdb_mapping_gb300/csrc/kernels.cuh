@@ -2102,4 +2102,38 @@ __global__ void __launch_bounds__(256) k_map_digest(const int4* __restrict__ ori
   }
 }
 
+// ---------------------------------------------------------------------------
+// L2 atomic throughput probe (the atomic half of the roofline): every thread
+// issues `iters` 64-bit ORs whose results are unused (RED) to words of an
+// L2-resident buffer of mask + 1 words. pattern 0: each warp ORs 32
+// consecutive words (one 256-byte request, as the apply's leaf-mask ORs
+// are); pattern 1: every lane a pseudo-random word (as the endpoint hits
+// are).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_atomic_probe(unsigned long long* __restrict__ buf, uint32_t mask,
+                                                      uint32_t iters, int pattern)
+{
+  const uint32_t tid  = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t x          = tid * 2654435761u + 12345u;
+  uint32_t base       = (tid >> 5) * 32u * 97u;
+  for (uint32_t i = 0; i < iters; ++i)
+  {
+    uint32_t idx;
+    if (pattern == 0)
+    {
+      base += 32u * 131u;
+      idx = (base + lane) & mask;
+    }
+    else
+    {
+      x ^= x << 13;
+      x ^= x >> 17;
+      x ^= x << 5;
+      idx = x & mask;
+    }
+    atomicOr(buf + idx, 1ull << (i & 63u));
+  }
+}
+
 } // namespace vdbg

@@ -2248,6 +2248,48 @@ int vdbg_map_digest(vdbg_map* m, int map, uint64_t out[4])
   return st;
 }
 
+int vdbg_l2_atomic_rate(int device, int pattern, double* ops_per_s)
+{
+  if (!ops_per_s || pattern < 0 || pattern > 1) return VDBG_ERR_INVALID_ARGUMENT;
+  *ops_per_s = 0.0;
+  VDBG_CUDA(cudaSetDevice(device));
+  int sms = 0;
+  VDBG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  const uint32_t words = 1u << 22;  // 32 MiB: resident in L2
+  const uint32_t iters = 512;
+  const unsigned grid  = static_cast<unsigned>(sms) * 8u;
+  unsigned long long* buf = nullptr;
+  cudaStream_t s          = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int st = VDBG_OK;
+  if (cudaMalloc(reinterpret_cast<void**>(&buf), static_cast<size_t>(words) * sizeof(unsigned long long)) !=
+        cudaSuccess ||
+      cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+      cudaEventCreate(&e1) != cudaSuccess)
+    st = VDBG_ERR_CUDA;
+  float best = 0.f;
+  if (st == VDBG_OK && cudaMemsetAsync(buf, 0, static_cast<size_t>(words) * 8, s) != cudaSuccess) st = VDBG_ERR_CUDA;
+  for (int rep = 0; rep < 4 && st == VDBG_OK; ++rep)
+  {
+    cudaEventRecord(e0, s);
+    k_atomic_probe<<<grid, 256, 0, s>>>(buf, words - 1u, iters, pattern);
+    cudaEventRecord(e1, s);
+    float ms = 0.f;
+    if (cudaGetLastError() != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+      st = VDBG_ERR_CUDA;
+    else if (rep > 0 && (best == 0.f || ms < best))
+      best = ms;  // (the first launch is the warm-up)
+  }
+  if (st == VDBG_OK && best > 0.f)
+    *ops_per_s = static_cast<double>(grid) * 256.0 * iters / (static_cast<double>(best) * 1e-3);
+  if (buf) cudaFree(buf);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (s) cudaStreamDestroy(s);
+  return st;
+}
+
 int vdbg_get_pool_info(const vdbg_map* m, vdbg_pool_info* out)
 {
   if (!m || !out) return VDBG_ERR_INVALID_ARGUMENT;
