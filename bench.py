@@ -63,6 +63,9 @@ def parse_args():
                     help="use an evenly strided subset of N points of each scan (small profiling cases)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="simulated traffic for --workload serving")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="device-memory admission budget")
+    ap.add_argument("--serve-drift", default="",
+                    help="serving: metres per scan that LiDAR and depth scans move along their heading, 'L,D' "
+                         "(maps keep growing); empty: scans cycle in place")
     ap.add_argument("--no-autotune", action="store_true", help="batched mode: keep the library's default tuning")
     ap.add_argument("--tuning", default=None,
                     help='dense mode: kernel tuning as JSON, e.g. \'{"apply_chunk_runs": 1024}\' (speed only)')
@@ -553,7 +556,7 @@ def run_ours(args):
             "batched": {k: bl[k] for k in ("config", "batched", "plain_per_map", "tuning", "gpu_launches_per_step",
                                            "steps", "warmup")},
             "serving": {k: sv[k] for k in ("config", "latency_ms", "latency_ms_all", "rays_per_s",
-                                           "voxel_updates_per_s", "mean_scans_per_step", "gpu_busy_frac",
+                                           "voxel_updates_per_s", "mean_scans_per_step", "gpu_busy_frac", "overlapped_steps",
                                            "statuses")},
         }
 
@@ -705,10 +708,14 @@ def run_batched(args):
 # Serving: Poisson sensor streams through the continuous-batching loop
 # --------------------------------------------------------------------------
 
-def measure_serving(local, seconds, budget_gb, use_graph=True):
+def measure_serving(local, seconds, budget_gb, use_graph=True, drift=None):
     """16 sensor streams with Poisson arrivals in real time for `seconds`
     through MapServer; returns p50/p99 latency (submit to done) per sensor
-    class next to rays/s and voxel-updates/s."""
+    class next to rays/s and voxel-updates/s. With `drift` (metres per scan,
+    LiDAR and depth) every scan is the stream's base scan carried along the
+    stream's heading by drift x its scan number, scene and sensor together,
+    so the maps keep growing as on a long trajectory; the line reports the
+    maps' sizes."""
     import threading
     from concurrent.futures import ThreadPoolExecutor
 
@@ -746,6 +753,13 @@ def measure_serving(local, seconds, budget_gb, use_graph=True):
             k = counter[i]
             counter[i] += 1
             pts, org = scans[(i, k % K)]
+            if drift:
+                s_ = wl.streams[i]
+                d = (drift[1] if s_["depth"] else drift[0]) * k
+                off = np.array([d * np.cos(s_["heading"]), d * np.sin(s_["heading"]), 0.0])
+                pts = pts.copy()
+                pts[:, :3] += off.astype(np.float32)
+                org = org + off
             while server.submit(i, pts, org, tag=j) != 0:
                 busy += 1
                 time.sleep(0.0005)
@@ -764,6 +778,8 @@ def measure_serving(local, seconds, budget_gb, use_graph=True):
     clk = clocks.stop()
     st = server.stats()
     server.close()
+    leaf_bytes = 512 * 4 + 8 * 8 + 16 + 4 + 16 * 8 + 4
+    map_gb = [batch.leafCount(i) * leaf_bytes / 1e9 for i in range(len(wl.streams))]
     lat = {"lidar": [], "depth": []}
     for r in results:
         lat["depth" if wl.streams[r["map"]]["depth"] else "lidar"].append((r["done_ns"] - r["submit_ns"]) / 1e6)
@@ -774,8 +790,14 @@ def measure_serving(local, seconds, budget_gb, use_graph=True):
         "value": float(np.percentile(allv, 99)), "unit": "ms (p99 latency)", "n_gpus": 1,
         "steps": st["steps"], "warmup": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 DDA / f32 log-odds",
-        "data": f"synthetic (seeded rooms; {K} distinct scans per stream cycled, sensor moving)",
-        "config": {**wl.describe(), "seconds": seconds, "memory_budget_gb": budget_gb},
+        "data": f"synthetic (seeded rooms; {K} distinct scans per stream cycled, sensor moving"
+                + (", carried along the heading" if drift else "") + ")",
+        "config": {**wl.describe(), "seconds": seconds, "memory_budget_gb": budget_gb,
+                   "arrivals": "Poisson, real time (not compressed)",
+                   "drift_m_per_scan": {"lidar": drift[0], "depth": drift[1]} if drift else None},
+        "map_gb": {"lidar": [round(g, 3) for i, g in enumerate(map_gb) if not wl.streams[i]["depth"]],
+                   "depth": [round(g, 3) for i, g in enumerate(map_gb) if wl.streams[i]["depth"]],
+                   "device_gb": st["device_bytes"] / 1e9},
         "latency_ms_all": {"p50": float(np.percentile(allv, 50)), "p99": float(np.percentile(allv, 99)),
                            "max": float(max(allv)), "n": len(allv)},
         "latency_ms": {c: {"p50": float(np.percentile(v, 50)), "p99": float(np.percentile(v, 99)),
@@ -786,6 +808,9 @@ def measure_serving(local, seconds, budget_gb, use_graph=True):
         "offered_points_per_s": sum(s["n"] * s["hz"] for s in wl.streams),
         "steps": st["steps"], "mean_scans_per_step": st["requests_done"] / max(1, st["steps"]),
         "max_scans_per_step": st["max_step_maps"], "gpu_busy_frac": st["busy_ns"] / 1e9 / span_s,
+        "overlapped_steps": st["overlapped_steps"],
+        "overlap": "the next step's upload and ray preparation run on a second stream while a step is marked "
+                   "and swept",
         "rejected": st["rejected"], "max_queued": st["max_queued"], "submit_retries_busy": busy,
         "device_bytes": st["device_bytes"],
         "statuses": sorted({r["status"] for r in results}),
@@ -803,7 +828,9 @@ def run_serving(args):
 
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
-    print(json.dumps(measure_serving(local, args.serve_seconds, args.serve_budget_gb, use_graph=not args.no_graph)))
+    drift = tuple(float(v) for v in args.serve_drift.split(",")) if args.serve_drift else None
+    print(json.dumps(measure_serving(local, args.serve_seconds, args.serve_budget_gb, use_graph=not args.no_graph,
+                                     drift=drift)))
     return 0
 
 

@@ -416,7 +416,10 @@ int vdbg_batch_export_leaves(vdbg_map* batch, int map, int64_t capacity, int32_t
  * need the pool to grow past the budget waits for a step of its own, and is
  * completed with VDBG_ERR_OUT_OF_MEMORY if even then it does not fit), and
  * inserts them with one batched call; scans arriving meanwhile join the next
- * step. A scan's result is the same whatever it shares a step with. While a
+ * step. Steps are pipelined: while the device marks and sweeps one step, the
+ * next is formed from what has arrived and its upload and ray preparation run
+ * on a second stream beside it; its marking starts when the step before ends.
+ * A scan's result is the same whatever it shares a step with. While a
  * server runs, only the server calls may touch its batch; destroy the server
  * before using the batch directly again. */
 typedef struct vdbg_server vdbg_server;
@@ -454,6 +457,7 @@ typedef struct vdbg_server_stats
   uint64_t updates;
   int64_t busy_ns;       /* time spent in batched calls */
   int64_t device_bytes;
+  int64_t overlapped_steps; /* steps during which the next step's upload and ray preparation were queued */
 } vdbg_server_stats;
 
 int vdbg_server_create(vdbg_map* batch, const vdbg_server_options* options, vdbg_server** out);

@@ -100,3 +100,35 @@ def test_serving_queue_backpressure(vdbg):
     done = server.poll(64)
     assert len(done) == codes.count(0)
     server.close()
+
+
+def test_serving_pipelined_steps_equal_alone(vdbg):
+    """Scans queued faster than the device drains them: while one step is
+    marked and swept, the next is formed and its upload and ray preparation
+    run on the second stream (overlapped_steps counts those steps). Every map
+    still equals the same scans inserted alone, in order."""
+    wl = W.BatchedWorkload(seed=57, n_maps=4, n_steps=6, n_min=20000, n_max=120000)
+    scans = {(i, k): wl.scan(i, k) for i in range(wl.n_maps) for k in range(6)}
+    batch = vdbg.MapBatch(wl.resolutions)
+    for i, c in enumerate(wl.configs):
+        batch.setConfig(i, c)
+    server = vdbg.MapServer(batch)
+    j = 0
+    for k in range(6):
+        for i in range(wl.n_maps):
+            pts, org = scans[(i, k)]
+            assert server.submit(i, pts, org, tag=j) == 0
+            j += 1
+    server.drain()
+    results = server.poll(256)
+    st = server.stats()
+    server.close()
+    assert len(results) == j and all(r["status"] == 0 for r in results)
+    assert st["overlapped_steps"] >= 1, st
+    for i in range(wl.n_maps):
+        g = vdbg.OccupancyVDBMapping(wl.resolutions[i])
+        g.setConfig(wl.configs[i])
+        g.addInputSource("s", wl.configs[i].max_range, 0)
+        for k in range(6):
+            g.insertPointCloud(*scans[(i, k)], "s")
+        assert_same_map(batch.exportLeaves(i), g.exportLeaves(), f"map {i}")

@@ -153,6 +153,7 @@ class vdbg_server_stats(C.Structure):
         ("updates", C.c_uint64),
         ("busy_ns", C.c_int64),
         ("device_bytes", C.c_int64),
+        ("overlapped_steps", C.c_int64),
     ]
 
     def as_dict(self):

@@ -12,11 +12,17 @@
 //   borigin int4[PB]     block coordinate (voxel >> 6), .w = map
 //   bleaf   i32[PB][512] leaf slot of each leaf cell of the block, -1 none
 //   origin  int4[P]      leaf origin (voxel coordinates, multiples of 8), .w = map
-//   values  f32[P][512]  log-odds, z-major leaf order (z&7)<<6 | (y&7)<<3 | (x&7)
-//                        (OpenVDB's order with x and z swapped: a mask word is
-//                        one z-plane, which a near-horizontal ray crosses in
-//                        one run; the export swaps them back)
-//   active  u64[P][8]    value (active) mask, bit i of word w = offset 64w+i
+//   values  f32[P][512]  log-odds by z-plane: plane z&7 holds floats 64(z&7)..
+//                        +63 (OpenVDB's order has x outermost; z-planes make a
+//                        mask word one plane, which a near-horizontal ray
+//                        crosses in one run). Within a plane, voxel bit
+//                        k = (y&7)<<3 | (x&7) sits at plane_float(k): runs of
+//                        4 x stay contiguous, each 64-byte chunk holds a 4 x 4
+//                        tile (x by y) and each 32-byte sector a 4 x 2 tile,
+//                        so rays in any horizontal direction update more
+//                        voxels per chunk than with rows of 8 x. The export
+//                        maps both back.
+//   active  u64[P][8]    value (active) mask, bit i of word w = voxel bit i of plane w
 //   flags   u32[P]       1 once the leaf belongs to the map (first integration)
 // Per update grid (one per input source):
 //   upd      u64[P][16]  words 0-7 visited, 8-15 hit, same bit order as active
@@ -30,6 +36,14 @@
 #include <cuda_runtime.h>
 
 namespace vdbg {
+
+// Float position within a z-plane of the quad (4 consecutive x) q = k >> 2 of
+// voxel bit k, y = q >> 1: 64-byte chunk (y >> 2) * 2 + (q & 1) (a 4 x 4 tile
+// of the plane), then row y & 3 of it (so each 32-byte sector is a 4 x 2 tile).
+__host__ __device__ constexpr int plane_quad(int q) { return (((q >> 3) * 2 + (q & 1)) * 4 + ((q >> 1) & 3)); }
+__host__ __device__ constexpr int plane_float(int k) { return plane_quad(k >> 2) * 4 + (k & 3); }
+// Float index within a leaf of z-major offset o = (z&7)<<6 | (y&7)<<3 | (x&7).
+__host__ __device__ constexpr int leaf_float(int o) { return (o & ~63) | plane_float(o & 63); }
 
 constexpr unsigned long long kEmptyKey = ~0ull;
 constexpr int kSlotPending             = -1;  // block hash: being published

@@ -1025,7 +1025,8 @@ struct SweepTask
 {
   unsigned long long actw, hitw;  // visited-or-hit and hit bits of the plane
   int slot;                       // leaf slot
-  int w;                          // plane
+  short w;                        // plane
+  short map;                      // the leaf's map (a pool of several maps)
 };
 constexpr int kSweepQueue = 64;  // per-warp ring: up to 31 left over + 32 found
 
@@ -1036,7 +1037,7 @@ __device__ __forceinline__ unsigned long long sweep_plane(const SweepTask& k, Ch
 {
   const unsigned long long actw = k.actw, hitw = k.hitw;
   const int slot = k.slot, w = k.w;
-  const LogOdds lo               = kPerMap ? lt.table[origin[slot].w] : lt.lo0;
+  const LogOdds lo               = kPerMap ? lt.table[k.map] : lt.lo0;
   unsigned long long* aw         = active + static_cast<size_t>(slot) * 8 + w;
   const unsigned long long on_in = *aw;
   unsigned long long on          = on_in;
@@ -1049,7 +1050,7 @@ __device__ __forceinline__ unsigned long long sweep_plane(const SweepTask& k, Ch
     for (int k4 = 0; k4 < 8; ++k4)
     {
       const int qd = half * 8 + k4;
-      if ((actw >> (4 * qd)) & 0xfull) v[k4] = vp[qd];
+      if ((actw >> (4 * qd)) & 0xfull) v[k4] = vp[plane_quad(qd)];
     }
 #pragma unroll
     for (int k4 = 0; k4 < 8; ++k4)
@@ -1070,7 +1071,7 @@ __device__ __forceinline__ unsigned long long sweep_plane(const SweepTask& k, Ch
           on = o ? (on | (1ull << bit)) : (on & ~(1ull << bit));
         }
       }
-      vp[qd] = make_float4(vv[0], vv[1], vv[2], vv[3]);
+      vp[plane_quad(qd)] = make_float4(vv[0], vv[1], vv[2], vv[3]);
     }
   }
   if (on != on_in) *aw = on;
@@ -1115,9 +1116,11 @@ __global__ void __launch_bounds__(256, 4) k_sweep(ChannelView c, float* __restri
       const uint32_t i             = base + grp;
       unsigned long long actw      = 0ull, hitw = 0ull;
       int slot                     = 0;
+      int map                      = 0;
       if (i < nt)
       {
         slot = c.touched[i];
+        if (kPerMap && w == 0) map = origin[slot].w;  // once per leaf
         // Mark the leaf as part of the map the first time it is swept (every
         // touched leaf carries at least one update bit).
         if (w == 0 && ld_ca_u32(flags + slot) == 0u) flags[slot] = 1u;
@@ -1130,6 +1133,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep(ChannelView c, float* __restri
           ch.words[static_cast<size_t>(slot) * 16 + 8 + w] = 0ull;
         }
       }
+      if (kPerMap) map = __shfl_sync(0xffffffffu, map, lane & ~7);
       const bool act    = actw != 0ull;
       const unsigned am = __ballot_sync(0xffffffffu, act);
       if (act)
@@ -1138,7 +1142,8 @@ __global__ void __launch_bounds__(256, 4) k_sweep(ChannelView c, float* __restri
         k.actw       = actw;
         k.hitw       = hitw;
         k.slot       = slot;
-        k.w          = w;
+        k.w          = static_cast<short>(w);
+        k.map        = static_cast<short>(map);
       }
       tail += static_cast<uint32_t>(__popc(am));
       __syncwarp();
@@ -1227,6 +1232,19 @@ __global__ void k_window_init(ChannelView c)
 // After a sweep (or a dropped marking): a fresh window for the channel.
 // `gated` (a captured step) skips it when the marking did not complete, so
 // the window is left to the host's continuation of the step.
+// A step whose rays were prepared ahead on another stream into their own
+// status block: its counters and the quantiser's error bit join the call's
+// status before the marking reads them (k_dda_mark reads n_valid).
+__global__ void k_absorb_prep(DevStatus* st, const DevStatus* __restrict__ prep)
+{
+  st->rays += prep->rays;
+  st->visits += prep->visits;
+  st->hits += prep->hits;
+  st->nonfinite += prep->nonfinite;
+  st->n_valid = prep->n_valid;
+  st->error |= prep->error;
+}
+
 __global__ void k_finish_window(ChannelView c, DevStatus* st, int gated)
 {
   if (gated && !marking_complete(st)) return;
@@ -1390,7 +1408,7 @@ __global__ void k_section_extract(const uint32_t* __restrict__ list, const uint3
     const unsigned long long inbox = box_plane_mask(o, w, lo, hi);
     const bool inside              = (inbox >> (off & 63)) & 1ull;
     const bool on                  = (active[static_cast<size_t>(slot) * 8 + w] >> (off & 63)) & 1ull;
-    const float v                  = values[static_cast<size_t>(slot) * 512 + off];
+    const float v                  = values[static_cast<size_t>(slot) * 512 + leaf_float(off)];
     out_v[static_cast<size_t>(j) * 512 + off] = inside ? (full ? v : (on ? 1.0f : 0.0f)) : 0.0f;
     any = any || (inside && (on || (full && v != 0.0f)));
     const unsigned half = __ballot_sync(0xffffffffu, inside && on);
@@ -1480,7 +1498,8 @@ __global__ void k_section_set_values(MapView m, const int4* __restrict__ sec_o, 
   slot = __shfl_sync(0xffffffffu, slot, 0);
   if (slot < 0) return;
   for (int k = 0; k < 16; ++k)
-    values[static_cast<size_t>(slot) * 512 + k * 32 + lane] = sec_v[static_cast<size_t>(i) * 512 + k * 32 + lane];
+    values[static_cast<size_t>(slot) * 512 + leaf_float(k * 32 + lane)] =
+      sec_v[static_cast<size_t>(i) * 512 + k * 32 + lane];
   if (lane < 8) active[static_cast<size_t>(slot) * 8 + lane] = sec_m[static_cast<size_t>(i) * 8 + lane];
 }
 
@@ -1497,7 +1516,7 @@ __global__ void k_section_clear_voxels(MapView m, const int4* __restrict__ pts, 
   const int slot = find_leaf(m, map, p.x >> 3, p.y >> 3, p.z >> 3);
   if (slot < 0 || flags[slot] == 0u) return;
   const int off = ((p.z & 7) << 6) | ((p.y & 7) << 3) | (p.x & 7);
-  values[static_cast<size_t>(slot) * 512 + off] = 0.0f;
+  values[static_cast<size_t>(slot) * 512 + leaf_float(off)] = 0.0f;
   atomicAnd(active + static_cast<size_t>(slot) * 8 + (off >> 6), ~(1ull << (off & 63)));
 }
 
@@ -1995,7 +2014,7 @@ __global__ void k_artificial_restore(MapView m, const int4* __restrict__ art_o,
   for (unsigned long long z = bits; z; z &= z - 1ull)
   {
     const int k = __ffsll(static_cast<long long>(z)) - 1;
-    if (values[static_cast<size_t>(slot) * 512 + w * 64 + k] > thres_max) on |= 1ull << k;
+    if (values[static_cast<size_t>(slot) * 512 + w * 64 + plane_float(k)] > thres_max) on |= 1ull << k;
   }
   unsigned long long* a = active + static_cast<size_t>(slot) * 8 + w;
   *a                    = (*a & ~bits) | on;
@@ -2079,7 +2098,7 @@ __global__ void __launch_bounds__(256) k_map_digest(const int4* __restrict__ ori
   {
     // device leaf order: offset = z << 6 | y << 3 | x, mask word = z
     const int z = k >> 6, y = (k >> 3) & 7, x = k & 7;
-    const uint32_t bits = __float_as_uint(values[static_cast<size_t>(slot) * 512 + k]);
+    const uint32_t bits = __float_as_uint(values[static_cast<size_t>(slot) * 512 + leaf_float(k)]);
     const uint32_t on   = static_cast<uint32_t>((active[static_cast<size_t>(slot) * 8 + z] >> (k & 63)) & 1ull);
     if (bits != 0u || on)
     {

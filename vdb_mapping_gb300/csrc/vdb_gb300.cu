@@ -10,6 +10,7 @@
 // intersector (fast mode, raytrace queries) and artificial areas.
 #include <algorithm>
 #include <cmath>
+#include <functional>
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
@@ -123,6 +124,10 @@ struct vdbg_map
   double block_hint     = 0.0;
   uint64_t grow_events  = 0;      // extensions prepared ahead
   uint64_t grow_sync    = 0;      // extensions made inside a call that ran out
+  // Host work to do while the device runs the current call (the serving loop
+  // queues its next step's upload and ray preparation here); run once, at
+  // the call's first wait for its status.
+  std::function<void()> pre_wait;
 
   DevStatus* d_status   = nullptr;
   DevStatus* h_status   = nullptr;  // pinned
@@ -643,7 +648,14 @@ int fetch_status(vdbg_map* m, cudaStream_t s)
 {
   VDBG_CUDA(cudaEventRecord(m->ev1, s));
   VDBG_CUDA(cudaMemcpyAsync(m->h_status, m->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
-  grow_ahead(m);  // while the device works through the call
+  // While the device works through the call:
+  if (m->pre_wait)
+  {
+    std::function<void()> f = std::move(m->pre_wait);
+    m->pre_wait             = nullptr;
+    f();
+  }
+  grow_ahead(m);
   VDBG_CUDA(cudaStreamSynchronize(s));
   return VDBG_OK;
 }
@@ -1872,8 +1884,16 @@ int set_config_impl(vdbg_map* m, int i, const vdbg_config* c)
 // to the other.
 inline int swap_xz(int o) { return ((o & 7) << 6) | (o & 0x38) | (o >> 6); }
 
-// One leaf's 512 values into OpenVDB's order.
+// One leaf's 512 values as the pool stores them (z-planes of 4 x 2 tiles)
+// into OpenVDB's order.
 void values_to_vdb(const float* in, float* out)
+{
+  for (int o = 0; o < 512; ++o) out[swap_xz(o)] = in[leaf_float(o)];
+}
+
+// The same from plain z-major order (offset z << 6 | y << 3 | x), the order
+// the section extraction writes.
+void zmajor_to_vdb(const float* in, float* out)
 {
   for (int o = 0; o < 512; ++o) out[swap_xz(o)] = in[o];
 }
@@ -3089,7 +3109,7 @@ int vdbg_export_section(vdbg_map* m, int map, const int32_t lo[3], const int32_t
       origins[3 * k + 1] = ho[j].y;
       origins[3 * k + 2] = ho[j].z;
     }
-    if (values) values_to_vdb(hv.data() + static_cast<size_t>(j) * 512, values + 512 * k);
+    if (values) zmajor_to_vdb(hv.data() + static_cast<size_t>(j) * 512, values + 512 * k);
     if (masks) mask_to_vdb(hm.data() + static_cast<size_t>(j) * 8, masks + 8 * k);
   }
   return VDBG_OK;
