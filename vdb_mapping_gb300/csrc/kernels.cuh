@@ -19,8 +19,9 @@
 //   k_rehash   (none)                   rebuilds the block hash after growth
 //   k_topo_build VDBMapping.hpp:1436-1449  the volume ray intersector's view of
 //                                       the map: node sets and active-leaf box
-//   k_fast_mark VDBMapping.hpp:577-602  fast mode: active map voxels along the
-//                                       intersector's spans of each ray
+//   k_fast_spans, k_fast_walk VDBMapping.hpp:577-602  fast mode: the
+//                                       intersector's spans of each ray, then
+//                                       the active map voxels along each span
 //   k_raytrace VDBMapping.hpp:675-721   raytrace queries
 //   k_morph_*  VDBMapping.hpp:1094-1147 dilation / erosion of section leaves
 //   k_wall_voxels VDBMapping.hpp:1210-1236  artificial walls, castRayIntoGrid per layer
@@ -1716,57 +1717,132 @@ __device__ __forceinline__ hdda::Box topo_box(const TopoView& tv)
 }
 
 // Fast mode (castRayIntoGridFast, VDBMapping.hpp:577-602, called by
-// raycastPointCloud VDBMapping.hpp:520-526 when the map is not empty): one
-// thread per valid ray marks, as visited in the update grid, the voxels of the
-// intersector's spans that are active in the map. Those voxels' leaves exist,
-// so nothing is allocated. The prep stage counted the castRayIntoGrid visits
-// of the ray; they are replaced by the marks made here.
-__global__ void __launch_bounds__(128) k_fast_mark(const int4* __restrict__ rays, const int* __restrict__ order,
-                                                   ScanTable t, MapView m, ChannelView c, TopoView tv,
-                                                   const uint32_t* __restrict__ flags,
-                                                   const unsigned long long* __restrict__ active)
+// raycastPointCloud VDBMapping.hpp:520-526 when the map is not empty): the
+// voxels of the intersector's spans that are active in the map are marked
+// visited in the update grid. Those voxels' leaves exist, so nothing is
+// allocated. The prep stage counted the castRayIntoGrid visits of the rays;
+// they are replaced by the marks made here (k_fast_visits).
+// Two phases, so that the lanes of a warp run the same loop: k_fast_spans
+// walks the intersector's three coarse levels for every ray and writes its
+// spans; k_fast_walk then walks the voxel DDA over one span per thread, in
+// the order the spans were written (neighbouring rays' spans together). The
+// spans and their fine walks are those of hdda::fast_cast_one.
+struct SpanRec
 {
-  if (ld_relaxed_u32(&m.st->error) != 0u) return;
-  c.cur_epoch = *c.epoch;
+  double t0, t1;
+  int ray;  // index into the ray records
+  int pad;
+};
+
+struct SpanBuf
+{
+  SpanRec* rec;
+  uint32_t cap;
+  uint32_t* count;                 // spans written (may exceed cap: the host grows and repeats)
+  unsigned long long* dda_visits;  // castRayIntoGrid visits the prep counted for these rays
+};
+
+__device__ __forceinline__ void fast_ray(const int4& r, const ScanGeom& g, double eye[3], double dir[3])
+{
+  const int o[3] = {g.ovx, g.ovy, g.ovz};
+  const int e[3] = {r.x, r.y, r.z};
+  for (int a = 0; a < 3; ++a)
+  {
+    eye[a] = hdda::add(static_cast<double>(o[a]), 0.5);
+    dir[a] = hdda::sub(static_cast<double>(e[a]), static_cast<double>(o[a]));
+  }
+}
+
+__global__ void __launch_bounds__(128) k_fast_spans(const int4* __restrict__ rays, const int* __restrict__ order,
+                                                    ScanTable t, MapView m, TopoView tv,
+                                                    const uint32_t* __restrict__ flags, SpanBuf sb)
+{
+  // (read once per warp: the warp reduces below)
+  const int lane = static_cast<int>(threadIdx.x & 31);
+  if (__shfl_sync(0xffffffffu, lane == 0 ? ld_relaxed_u32(&m.st->error) : 0u, 0) != 0u) return;
   const uint32_t nv = m.st->n_valid;
   const uint32_t j  = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nv) return;
-  if (tv.count[1] != 0u)
+  unsigned long long dv = 0;
+  if (j < nv && tv.count[1] == 0u)
+  {
+    const int ri      = order[j];
+    const int4 r      = rays[ri];
+    const uint32_t l1 = static_cast<uint32_t>(r.w) & kMetaL1Mask;
+    dv                = l1 > 0u ? l1 + 1ull : 0ull;
+    if (tv.count[0] != 0u)
+    {
+      const ScanGeom& g = scan_geom(t, scan_of_ray(t, static_cast<uint32_t>(ri)));
+      double eye[3], dir[3];
+      fast_ray(r, g, eye, dir);
+      hdda::Ray ray = hdda::make_ray(eye, dir, 0.0, 1.0);
+      hdda::clip(ray, topo_box(tv).lo, topo_box(tv).hi_excl);
+      DevTopo topo{tv, m, flags, 0x7fffffff, 0, 0, -1};
+      uint32_t steps = 0;
+      const int w    = hdda::all_spans(ray, topo, steps, [&](const hdda::Span& sp) {
+        const uint32_t k = atomicAdd(sb.count, 1u);
+        if (k < sb.cap) sb.rec[k] = SpanRec{sp.t0, sp.t1, ri, 0};
+      });
+      if (w == hdda::kWalkBound) atomicOr(&m.st->error, kErrStepBound);
+    }
+  }
+  else if (j < nv)
   {
     atomicOr(&m.st->error, kErrTopoFull);
-    return;
   }
-  const int ri             = order[j];
-  const int4 r             = rays[ri];
-  const uint32_t l1        = static_cast<uint32_t>(r.w) & kMetaL1Mask;
-  const ScanGeom& g        = scan_geom(t, scan_of_ray(t, static_cast<uint32_t>(ri)));
+  for (int off = 16; off > 0; off >>= 1) dv += __shfl_xor_sync(0xffffffffu, dv, off);
+  if ((threadIdx.x & 31) == 0 && dv) atomicAdd(sb.dda_visits, dv);
+}
+
+__global__ void __launch_bounds__(128) k_fast_walk(const int4* __restrict__ rays, ScanTable t, MapView m,
+                                                   ChannelView c, TopoView tv,
+                                                   const unsigned long long* __restrict__ active, SpanBuf sb,
+                                                   uint32_t n)
+{
+  const int lane = static_cast<int>(threadIdx.x & 31);
+  if (__shfl_sync(0xffffffffu, lane == 0 ? ld_relaxed_u32(&m.st->error) : 0u, 0) != 0u) return;
+  c.cur_epoch       = *c.epoch;
+  const uint32_t i  = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long marks = 0ull;
-  if (tv.count[0] != 0u)
+  if (i < n)
   {
-    const int o[3] = {g.ovx, g.ovy, g.ovz};
-    const int e[3] = {r.x, r.y, r.z};
-    DevTopo topo{tv, m, flags, 0x7fffffff, 0, 0, -1};
+    const SpanRec sp  = sb.rec[i];
+    const int4 r      = rays[sp.ray];
+    const ScanGeom& g = scan_geom(t, scan_of_ray(t, static_cast<uint32_t>(sp.ray)));
+    double eye[3], dir[3];
+    fast_ray(r, g, eye, dir);
+    const hdda::Ray fine = hdda::make_ray(eye, dir, sp.t0, sp.t1);
+    hdda::Dda dda;
+    hdda::dda_init(dda, fine, sp.t0, sp.t1, 0);
     ActiveCache act{&m, active, tv.map, 0x7fffffff, 0, 0, -1, -1, -1, 0ull};
     uint32_t steps = 0;
-    const int st   = hdda::fast_cast_one(o, e, topo_box(tv), topo, act,
-                                         [&](const int v[3]) {
-                                           // act holds v's leaf: active() just found the voxel on.
-                                           const int b    = act.b;
-                                           const int cell = ((act.lx & 7) << 6) | ((act.ly & 7) << 3) | (act.lz & 7);
-                                           touch_block(c, b);
-                                           unsigned long long* bt = c.btouched + static_cast<size_t>(b) * 8 + (cell >> 6);
-                                           if (!((*bt >> (cell & 63)) & 1ull)) atomicOr(bt, 1ull << (cell & 63));
-                                           const int off = ((v[2] & 7) << 6) | ((v[1] & 7) << 3) | (v[0] & 7);
-                                           atomicOr(c.upd + static_cast<size_t>(act.slot) * 16 + (off >> 6),
-                                                    1ull << (off & 63));
-                                           ++marks;
-                                         },
-                                         steps);
-    if (st == hdda::kTraceBound) atomicOr(&m.st->error, kErrStepBound);
+    do
+    {
+      if (++steps > hdda::kStepLimit)
+      {
+        atomicOr(&m.st->error, kErrStepBound);
+        break;
+      }
+      if (act(dda.voxel))
+      {
+        // act holds the voxel's leaf: mark it visited in the update grid.
+        const int b    = act.b;
+        const int cell = ((act.lx & 7) << 6) | ((act.ly & 7) << 3) | (act.lz & 7);
+        touch_block(c, b);
+        unsigned long long* bt = c.btouched + static_cast<size_t>(b) * 8 + (cell >> 6);
+        if (!((*bt >> (cell & 63)) & 1ull)) atomicOr(bt, 1ull << (cell & 63));
+        const int off = ((dda.voxel[2] & 7) << 6) | ((dda.voxel[1] & 7) << 3) | (dda.voxel[0] & 7);
+        atomicOr(c.upd + static_cast<size_t>(act.slot) * 16 + (off >> 6), 1ull << (off & 63));
+        ++marks;
+      }
+    } while (hdda::dda_step(dda));
   }
-  const unsigned long long dda_visits = l1 > 0u ? l1 + 1ull : 0ull;
-  if (marks != dda_visits) atomicAdd(&m.st->visits, marks - dda_visits);
+  for (int off = 16; off > 0; off >>= 1) marks += __shfl_xor_sync(0xffffffffu, marks, off);
+  if ((threadIdx.x & 31) == 0 && marks) atomicAdd(&m.st->visits, marks);
 }
+
+// The fast marking's visits replace the castRayIntoGrid visits the prep
+// counted (one thread).
+__global__ void k_fast_visits(DevStatus* st, const unsigned long long* dda_visits) { st->visits -= *dda_visits; }
 
 // raytrace (VDBMapping.hpp:675-721), one thread per query: q holds the
 // origins [n][3], then the directions [n][3], then the lengths [n]; ok[n] and

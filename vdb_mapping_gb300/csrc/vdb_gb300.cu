@@ -189,6 +189,10 @@ struct vdbg_map
   int* topo_box                    = nullptr;  // [8]: box[6], then two counts
   char* d_trace                    = nullptr;
   size_t trace_bytes               = 0;
+  // Fast mode's span records (k_fast_spans -> k_fast_walk) and their counters.
+  SpanRec* fast_spans              = nullptr;
+  uint32_t fast_cap                = 0;
+  unsigned long long* fast_ctr     = nullptr;  // [2]: span count (low 32 bits), castRayIntoGrid visits
   // Artificial areas (VDBMapping.hpp:1152-1236): their voxels as leaves
   // (origins, device-order masks) on the host, and the device copy that
   // k_section_set_states re-activates after every update of the map.
@@ -1347,11 +1351,46 @@ int run_fast_marking(vdbg_map* m, Channel& c, const int4* rays, const int* order
   TopoView tv;
   VDBG_TRY(build_topology(m, 0, s, &tv));
   const unsigned hit_blocks = static_cast<unsigned>((n + 255) / 256);
-  k_fast_mark<<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(rays, order, t, map_view(m), channel_view(c), tv,
-                                                                     m->flags, m->active);
   k_mark_hits<<<hit_blocks, 256, 0, s>>>(rays, order, t, map_view(m), channel_view(c));
   VDBG_CUDA(cudaGetLastError());
-  m->timings.launches += 2;
+  m->timings.launches += 1;
+  // Phase 1: the spans of every ray (repeated with a larger buffer if they
+  // did not fit; the walk writes nothing but the records and counters).
+  if (!m->fast_ctr) VDBG_TRY(dev_alloc(m, &m->fast_ctr, 2));
+  uint32_t want = std::max<uint32_t>(m->fast_cap, static_cast<uint32_t>(std::min<int64_t>(4 * n, 1 << 30)));
+  uint32_t spans = 0;
+  for (int round = 0; round < 3; ++round)
+  {
+    if (want > m->fast_cap)
+    {
+      dev_free(m, m->fast_spans, m->fast_cap);
+      m->fast_cap = 0;
+      VDBG_TRY(dev_alloc(m, &m->fast_spans, want));
+      m->fast_cap = want;
+    }
+    VDBG_CUDA(cudaMemsetAsync(m->fast_ctr, 0, 2 * sizeof(unsigned long long), s));
+    SpanBuf sb{m->fast_spans, m->fast_cap, reinterpret_cast<uint32_t*>(m->fast_ctr), m->fast_ctr + 1};
+    k_fast_spans<<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(rays, order, t, map_view(m), tv, m->flags,
+                                                                         sb);
+    VDBG_CUDA(cudaGetLastError());
+    m->timings.launches += 1;
+    VDBG_CUDA(cudaMemcpyAsync(&spans, m->fast_ctr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    VDBG_CUDA(cudaStreamSynchronize(s));
+    if (spans <= m->fast_cap) break;
+    want = spans + spans / 4;
+  }
+  if (spans > m->fast_cap) return oom("fast spans", spans, m->fast_cap);
+  // Phase 2: the voxel walks over the spans.
+  if (spans > 0)
+  {
+    SpanBuf sb{m->fast_spans, m->fast_cap, reinterpret_cast<uint32_t*>(m->fast_ctr), m->fast_ctr + 1};
+    k_fast_walk<<<(spans + 127) / 128, 128, 0, s>>>(rays, t, map_view(m), channel_view(c), tv, m->active, sb,
+                                                    spans);
+    m->timings.launches += 1;
+  }
+  k_fast_visits<<<1, 1, 0, s>>>(m->d_status, m->fast_ctr + 1);
+  VDBG_CUDA(cudaGetLastError());
+  m->timings.launches += 1;
   VDBG_TRY(fetch_status(m, s));
   for (int attempt = 0; m->h_status->error != 0u; ++attempt)
   {
@@ -2014,6 +2053,8 @@ int vdbg_destroy(vdbg_map* m)
   dev_free(m, m->topo_keys, 2 * static_cast<size_t>(m->topo_cap));
   dev_free(m, m->topo_box, 8);
   dev_free(m, m->d_trace, m->trace_bytes);
+  dev_free(m, m->fast_spans, m->fast_cap);
+  dev_free(m, m->fast_ctr, 2);
   dev_free(m, m->d_art_o, m->art_n);
   dev_free(m, m->d_art_m, static_cast<size_t>(m->art_n) * 8);
   if (m->h_status) cudaFreeHost(m->h_status);
@@ -2955,6 +2996,8 @@ int vdbg_raytrace(vdbg_map* m, int map, int64_t n, const double* origins, const 
   if (bytes > m->trace_bytes)
   {
     dev_free(m, m->d_trace, m->trace_bytes);
+  dev_free(m, m->fast_spans, m->fast_cap);
+  dev_free(m, m->fast_ctr, 2);
     m->trace_bytes = 0;
     VDBG_TRY(dev_alloc(m, &m->d_trace, bytes));
     m->trace_bytes = bytes;
