@@ -43,9 +43,10 @@ STATUS_BYTES = 80  # device status block (DevStatus) read back by every call
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
 # each kernel on a steady-state dense scan, from one ncu capture of the
-# default workload (profiles/launches_dense_street.md). Only meaningful
-# for the dense workload; other workloads report None.
-NCU_TRAFFIC_BYTES = {"k_dda_mark": 429.5e6, "k_apply_runs": 804.9e6, "k_sweep": 2048.8e6,
+# default workload's launch list (the last of three inserts; prep = k_prep +
+# k_scatter). Only meaningful for the dense workload; other workloads report
+# None.
+NCU_TRAFFIC_BYTES = {"k_dda_mark": 429.4e6, "k_apply_runs": 804.0e6, "k_sweep": 1986.8e6,
                      "prep (k_prep+k_scan+k_scatter)": 8.4e6}
 
 
@@ -71,6 +72,9 @@ def parse_args():
                     help='dense mode: kernel tuning as JSON, e.g. \'{"apply_chunk_runs": 1024}\' (speed only)')
     ap.add_argument("--no-graph", action="store_true",
                     help="batched and serving modes: separate launches instead of the captured step")
+    ap.add_argument("--batch-maps", type=int, default=32,
+                    help="--workload batched: maps per step (the first N maps of the 32-map workload; smaller "
+                         "cases for profiling)")
     ap.add_argument("--batch-steps", type=int, default=4,
                     help="distinct steps generated for --workload batched (cycled)")
     ap.add_argument("--leaf-capacity", type=int, default=0,
@@ -81,6 +85,9 @@ def parse_args():
     ap.add_argument("--map-scans", type=int, default=6, help="--workload raytrace: dense scans forming the map")
     ap.add_argument("--no-trajectory", action="store_true",
                     help="dense mode: skip timing the whole 100-scan trajectory into one map")
+    ap.add_argument("--profile-range", action="store_true",
+                    help="bracket the timed steps (batched: the batched arm's) with cudaProfilerStart/Stop, for "
+                         "ncu --profile-from-start off")
     ap.add_argument("--peaks", action="store_true",
                     help="print the roofline denominators of this GPU (HBM copy rate and measured L2 atomic rates)")
     ap.add_argument("--no-extras", action="store_true",
@@ -88,6 +95,29 @@ def parse_args():
     ap.add_argument("--extras-serve-seconds", type=float, default=4.0,
                     help="seconds of simulated traffic of the serving figures in the dense line")
     return ap.parse_args()
+
+
+class ProfileRange:
+    """cudaProfilerStart/Stop around a region when enabled (ncu
+    --profile-from-start off then captures only that region)."""
+
+    def __init__(self, enabled):
+        self.enabled = enabled
+
+    def __enter__(self):
+        if self.enabled:
+            import torch
+
+            torch.cuda.synchronize()
+            torch.cuda.cudart().cudaProfilerStart()
+        return self
+
+    def __exit__(self, *exc):
+        if self.enabled:
+            import torch
+
+            torch.cuda.synchronize()
+            torch.cuda.cudart().cudaProfilerStop()
 
 
 def l2_atomic_rates(device):
@@ -407,15 +437,16 @@ def run_ours(args):
     torch.cuda.synchronize()
     clocks.start()
     wall0 = time.perf_counter()
-    for i in range(args.steps):
-        k = args.warmup + i
-        flush.zero_()
-        ev[i][0].record(stream)
-        m.insertPointCloud(dev_pts[k], scans[k][1], "lidar", stream=sh)
-        ev[i][1].record(stream)
-        stats.append(dict(m.last_stats))
-        phases.append(m.timings())
-    torch.cuda.synchronize()
+    with ProfileRange(args.profile_range):
+        for i in range(args.steps):
+            k = args.warmup + i
+            flush.zero_()
+            ev[i][0].record(stream)
+            m.insertPointCloud(dev_pts[k], scans[k][1], "lidar", stream=sh)
+            ev[i][1].record(stream)
+            stats.append(dict(m.last_stats))
+            phases.append(m.timings())
+        torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
@@ -575,7 +606,8 @@ def run_ours(args):
 # Batched maps: one call per step for all maps vs one call per map
 # --------------------------------------------------------------------------
 
-def measure_batched(local, steps_timed, warmup, n_distinct, autotune=True, use_graph=True):
+def measure_batched(local, steps_timed, warmup, n_distinct, autotune=True, use_graph=True, profile=False,
+                    n_maps=32, leaf_capacity=1 << 22):
     """32 independent maps, one scan each per step: the batched entry point
     (one pass of the kernels for all maps) against the plain per-map path on
     the same scans, both on device-resident points with CUDA events, plus a
@@ -587,7 +619,7 @@ def measure_batched(local, steps_timed, warmup, n_distinct, autotune=True, use_g
     from vdb_mapping_gb300 import MapBatch, OccupancyVDBMapping
     from vdb_mapping_gb300 import workloads as W
 
-    wl = W.get("batched")
+    wl = W.get("batched") if n_maps == 32 else W.BatchedWorkload(n_maps=n_maps)
     n_distinct = max(1, min(warmup + steps_timed, n_distinct))
     steps = [wl.step(k) for k in range(n_distinct)]
     counts = [p.shape[0] for p, _ in steps[0]]
@@ -605,7 +637,7 @@ def measure_batched(local, steps_timed, warmup, n_distinct, autotune=True, use_g
         from vdb_mapping_gb300 import autotune
 
         tuned, _ = autotune.tune_batch(wl.resolutions, wl.configs, steps[:min(3, n_distinct)], warmup=1)
-    b = MapBatch(wl.resolutions, initial_leaf_capacity=1 << 22, device=local)
+    b = MapBatch(wl.resolutions, initial_leaf_capacity=leaf_capacity, device=local)
     if tuned:
         b.setTuning(tuned)
     b.useGraph(use_graph)
@@ -640,19 +672,20 @@ def measure_batched(local, steps_timed, warmup, n_distinct, autotune=True, use_g
         torch.cuda.synchronize()
         phase.clear()
         ms, upd, rays = [], 0, 0
-        for i in range(steps_timed):
-            k = warmup + i
-            flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            st = fn(k)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ms.append(e0.elapsed_time(e1))
-            upd += st["updates"]
-            rays += st["rays"]
-            if fn is batched_step:
-                phase.append(b.timings())
+        with ProfileRange(profile and fn is batched_step):
+            for i in range(steps_timed):
+                k = warmup + i
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                st = fn(k)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+                upd += st["updates"]
+                rays += st["rays"]
+                if fn is batched_step:
+                    phase.append(b.timings())
         return ms, upd, rays
 
     clocks = ClockSampler(local)
@@ -699,7 +732,8 @@ def run_batched(args):
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
     line = measure_batched(local, args.steps, args.warmup, args.batch_steps, autotune=not args.no_autotune,
-                           use_graph=not args.no_graph)
+                           use_graph=not args.no_graph, profile=args.profile_range, n_maps=args.batch_maps,
+                           leaf_capacity=args.leaf_capacity or (1 << 22))
     print(json.dumps(line))
     return 0
 
