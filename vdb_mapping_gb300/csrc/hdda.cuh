@@ -30,6 +30,7 @@
 
 #include <cstdint>
 #include <cmath>
+#include <cstring>
 
 #ifdef __CUDACC__
 #define VDBG_HD __host__ __device__ __forceinline__
@@ -163,13 +164,32 @@ struct Dda
   double t0, t1;
 };
 
+// Order key of a DDA time. Every time a walk compares is >= 0 (the clipped
+// ray starts at t0 >= 0, each cell's exit time is at least its entry time,
+// the steps are positive) or DBL_MAX, never negative or NaN; for such values
+// the bit pattern read as an integer orders as the doubles do, once -0.0 is
+// folded onto +0.0 (they compare equal). Integer compares keep the walks off
+// the FP64 pipe, which is narrow on this GPU; the results are those of the
+// double compares.
+VDBG_HD long long tkey(double t)
+{
+#ifdef __CUDA_ARCH__
+  const long long b = __double_as_longlong(t);
+#else
+  long long b;
+  std::memcpy(&b, &t, sizeof(b));
+#endif
+  return b == static_cast<long long>(0x8000000000000000ull) ? 0ll : b;
+}
+
 // Index of the smallest of three values, ties to the higher index
-// (math::MinIndex; the values are never NaN here). Constant indices only, so
-// the DDA state stays in registers.
+// (math::MinIndex). Constant indices only, so the DDA state stays in
+// registers.
 VDBG_HD int min_index(const double v[3])
 {
-  if (v[0] < v[1]) return v[0] < v[2] ? 0 : 2;
-  return v[1] < v[2] ? 1 : 2;
+  const long long a = tkey(v[0]), b = tkey(v[1]), c = tkey(v[2]);
+  if (a < b) return a < c ? 0 : 2;
+  return b < c ? 1 : 2;
 }
 
 // DDA::init(ray, t0, t1). The caller guarantees |ray(t0)| < 2^30 per axis.
@@ -230,7 +250,7 @@ VDBG_HD bool dda_step(Dda& d)
     d.next[2] = add(d.next[2], d.delta[2]);
     d.voxel[2] += d.step[2];
   }
-  return d.t0 <= d.t1;
+  return tkey(d.t0) <= tkey(d.t1);
 }
 
 // DDA::next(): the time the current cell is left, at most t1.
@@ -238,7 +258,7 @@ VDBG_HD double dda_exit(const Dda& d)
 {
   double m = d.t1;
   for (int a = 0; a < 3; ++a)
-    if (d.next[a] < m) m = d.next[a];
+    if (tkey(d.next[a]) < tkey(m)) m = d.next[a];
   return m;
 }
 
@@ -268,7 +288,10 @@ enum Walk : int
 template <class Topo, class OnSpan>
 VDBG_HD int walk(Ray r, const Topo& topo, bool first_only, Span& t, uint32_t& steps, OnSpan&& on_span)
 {
-  // A span ends at a cell without a node: report it (march stops there).
+  // `open`: a span has started (t.t0 holds its start; closed spans are reset
+  // to t = {-1, -1}). A span ends at a cell without a node: report it (march
+  // stops there).
+  bool open = t.t0 >= 0.0;
 #define VDBG_HDDA_CLOSE(time)                       \
   do                                                \
   {                                                 \
@@ -280,6 +303,7 @@ VDBG_HD int walk(Ray r, const Topo& topo, bool first_only, Span& t, uint32_t& st
     }                                               \
     t.t0 = -1.0;                                    \
     t.t1 = -1.0;                                    \
+    open = false;                                   \
   } while (0)
 
   Dda d2;
@@ -307,28 +331,32 @@ VDBG_HD int walk(Ray r, const Topo& topo, bool first_only, Span& t, uint32_t& st
             if (++steps > kStepLimit) return kWalkBound;
             if (topo.has0(d0.voxel))
             {
-              if (t.t0 < 0.0) t.t0 = d0.t0;
+              if (!open)
+              {
+                t.t0 = d0.t0;
+                open = true;
+              }
             }
-            else if (t.t0 >= 0.0)
+            else if (open)
             {
               VDBG_HDDA_CLOSE(d0.t0);
             }
           } while (dda_step(d0));
-          if (t.t0 >= 0.0) t.t1 = d0.t1;
+          if (open) t.t1 = d0.t1;
         }
-        else if (t.t0 >= 0.0)
+        else if (open)
         {
           VDBG_HDDA_CLOSE(d1.t0);
         }
       } while (dda_step(d1));
-      if (t.t0 >= 0.0) t.t1 = d1.t1;
+      if (open) t.t1 = d1.t1;
     }
-    else if (t.t0 >= 0.0)
+    else if (open)
     {
       VDBG_HDDA_CLOSE(d2.t0);
     }
   } while (dda_step(d2));
-  if (t.t0 >= 0.0) t.t1 = d2.t1;
+  if (open) t.t1 = d2.t1;
   return kWalkDone;
 #undef VDBG_HDDA_CLOSE
 }

@@ -1731,8 +1731,9 @@ struct SpanRec
 {
   double t0, t1;
   int ray;  // index into the ray records
-  int pad;
+  int cls;  // length class: floor(log2) of the span's estimated voxel steps
 };
+constexpr int kSpanClasses = 32;
 
 struct SpanBuf
 {
@@ -1778,9 +1779,13 @@ __global__ void __launch_bounds__(128) k_fast_spans(const int4* __restrict__ ray
       hdda::clip(ray, topo_box(tv).lo, topo_box(tv).hi_excl);
       DevTopo topo{tv, m, flags, 0x7fffffff, 0, 0, -1};
       uint32_t steps = 0;
-      const int w    = hdda::all_spans(ray, topo, steps, [&](const hdda::Span& sp) {
+      const double l1 = fabs(dir[0]) + fabs(dir[1]) + fabs(dir[2]);  // voxels per unit t
+      const int w     = hdda::all_spans(ray, topo, steps, [&](const hdda::Span& sp) {
         const uint32_t k = atomicAdd(sb.count, 1u);
-        if (k < sb.cap) sb.rec[k] = SpanRec{sp.t0, sp.t1, ri, 0};
+        // (an estimate, for ordering only)
+        const double est = fmin((sp.t1 - sp.t0) * l1 + 2.0, 2147483647.0);
+        const int cls    = 31 - __clz(max(1, static_cast<int>(est)));
+        if (k < sb.cap) sb.rec[k] = SpanRec{sp.t0, sp.t1, ri, cls};
       });
       if (w == hdda::kWalkBound) atomicOr(&m.st->error, kErrStepBound);
     }
@@ -1838,6 +1843,51 @@ __global__ void __launch_bounds__(128) k_fast_walk(const int4* __restrict__ rays
   }
   for (int off = 16; off > 0; off >>= 1) marks += __shfl_xor_sync(0xffffffffu, marks, off);
   if ((threadIdx.x & 31) == 0 && marks) atomicAdd(&m.st->visits, marks);
+}
+
+// Span records by length class, longest first (a counting sort, so that the
+// spans a warp walks together take about as many steps each).
+__global__ void __launch_bounds__(256) k_span_hist(const SpanRec* __restrict__ rec, uint32_t n,
+                                                   uint32_t* __restrict__ hist)
+{
+  __shared__ uint32_t h[kSpanClasses];
+  if (threadIdx.x < kSpanClasses) h[threadIdx.x] = 0u;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    atomicAdd(h + rec[i].cls, 1u);
+  __syncthreads();
+  if (threadIdx.x < kSpanClasses && h[threadIdx.x]) atomicAdd(hist + threadIdx.x, h[threadIdx.x]);
+}
+
+// One warp: hist[c] becomes the first position of class c, classes in
+// descending order.
+__global__ void k_span_offsets(uint32_t* hist)
+{
+  const int lane   = static_cast<int>(threadIdx.x);
+  const int c      = kSpanClasses - 1 - lane;  // lane 0: the longest class
+  const uint32_t v = hist[c];
+  uint32_t incl    = v;
+  for (int off = 1; off < 32; off <<= 1)
+  {
+    const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += o;
+  }
+  hist[c] = incl - v;
+}
+
+__global__ void __launch_bounds__(256) k_span_scatter(const SpanRec* __restrict__ rec, uint32_t n,
+                                                      uint32_t* __restrict__ cursor, SpanRec* __restrict__ out)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool in    = i < n;
+  const int cls    = in ? rec[i].cls : -1;
+  // one atomic per class present in the warp, ranks within it by lane order
+  const unsigned peers = __match_any_sync(0xffffffffu, cls);
+  const int leader     = __ffs(peers) - 1;
+  uint32_t base        = 0;
+  if (in && static_cast<int>(threadIdx.x & 31) == leader) base = atomicAdd(cursor + cls, static_cast<uint32_t>(__popc(peers)));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (in) out[base + static_cast<uint32_t>(__popc(peers & lanemask_lt()))] = rec[i];
 }
 
 // The fast marking's visits replace the castRayIntoGrid visits the prep

@@ -190,7 +190,9 @@ struct vdbg_map
   char* d_trace                    = nullptr;
   size_t trace_bytes               = 0;
   // Fast mode's span records (k_fast_spans -> k_fast_walk) and their counters.
-  SpanRec* fast_spans              = nullptr;
+  SpanRec* fast_spans              = nullptr;  // [fast_cap] as written, then
+  SpanRec* fast_sorted             = nullptr;  // [fast_cap] by length class
+  uint32_t* fast_hist              = nullptr;  // [kSpanClasses]
   uint32_t fast_cap                = 0;
   unsigned long long* fast_ctr     = nullptr;  // [2]: span count (low 32 bits), castRayIntoGrid visits
   // Artificial areas (VDBMapping.hpp:1152-1236): their voxels as leaves
@@ -1364,8 +1366,10 @@ int run_fast_marking(vdbg_map* m, Channel& c, const int4* rays, const int* order
     if (want > m->fast_cap)
     {
       dev_free(m, m->fast_spans, m->fast_cap);
+      dev_free(m, m->fast_sorted, m->fast_cap);
       m->fast_cap = 0;
       VDBG_TRY(dev_alloc(m, &m->fast_spans, want));
+      VDBG_TRY(dev_alloc(m, &m->fast_sorted, want));
       m->fast_cap = want;
     }
     VDBG_CUDA(cudaMemsetAsync(m->fast_ctr, 0, 2 * sizeof(unsigned long long), s));
@@ -1380,10 +1384,18 @@ int run_fast_marking(vdbg_map* m, Channel& c, const int4* rays, const int* order
     want = spans + spans / 4;
   }
   if (spans > m->fast_cap) return oom("fast spans", spans, m->fast_cap);
-  // Phase 2: the voxel walks over the spans.
+  // Phase 2: the voxel walks over the spans, longest first.
   if (spans > 0)
   {
-    SpanBuf sb{m->fast_spans, m->fast_cap, reinterpret_cast<uint32_t*>(m->fast_ctr), m->fast_ctr + 1};
+    if (!m->fast_hist) VDBG_TRY(dev_alloc(m, &m->fast_hist, kSpanClasses));
+    VDBG_CUDA(cudaMemsetAsync(m->fast_hist, 0, kSpanClasses * sizeof(uint32_t), s));
+    const unsigned sblocks = (spans + 255) / 256;
+    k_span_hist<<<std::min<unsigned>(sblocks, static_cast<unsigned>(m->num_sms) * 4u), 256, 0, s>>>(
+      m->fast_spans, spans, m->fast_hist);
+    k_span_offsets<<<1, 32, 0, s>>>(m->fast_hist);
+    k_span_scatter<<<sblocks, 256, 0, s>>>(m->fast_spans, spans, m->fast_hist, m->fast_sorted);
+    m->timings.launches += 3;
+    SpanBuf sb{m->fast_sorted, m->fast_cap, reinterpret_cast<uint32_t*>(m->fast_ctr), m->fast_ctr + 1};
     k_fast_walk<<<(spans + 127) / 128, 128, 0, s>>>(rays, t, map_view(m), channel_view(c), tv, m->active, sb,
                                                     spans);
     m->timings.launches += 1;
@@ -2054,6 +2066,8 @@ int vdbg_destroy(vdbg_map* m)
   dev_free(m, m->topo_box, 8);
   dev_free(m, m->d_trace, m->trace_bytes);
   dev_free(m, m->fast_spans, m->fast_cap);
+  dev_free(m, m->fast_sorted, m->fast_cap);
+  dev_free(m, m->fast_hist, kSpanClasses);
   dev_free(m, m->fast_ctr, 2);
   dev_free(m, m->d_art_o, m->art_n);
   dev_free(m, m->d_art_m, static_cast<size_t>(m->art_n) * 8);
@@ -2997,6 +3011,8 @@ int vdbg_raytrace(vdbg_map* m, int map, int64_t n, const double* origins, const 
   {
     dev_free(m, m->d_trace, m->trace_bytes);
   dev_free(m, m->fast_spans, m->fast_cap);
+  dev_free(m, m->fast_sorted, m->fast_cap);
+  dev_free(m, m->fast_hist, kSpanClasses);
   dev_free(m, m->fast_ctr, 2);
     m->trace_bytes = 0;
     VDBG_TRY(dev_alloc(m, &m->d_trace, bytes));
