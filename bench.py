@@ -213,12 +213,21 @@ def host_cpu():
     """The host's CPU model and logical core count."""
     model = None
     try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip().lower() == "model name" and ":" in line:
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    try:
         with open("/proc/cpuinfo") as f:
             for line in f:
+                if model:
+                    break
                 key = line.split(":")[0].strip().lower()
                 if key in ("model name", "cpu model", "hardware") and ":" in line:
                     model = line.split(":", 1)[1].strip()
-                    break
     except OSError:
         pass
     if not model:
