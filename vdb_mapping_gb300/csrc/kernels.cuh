@@ -1681,15 +1681,24 @@ struct ActiveCache
   int b, slot;
   int wz;                   // plane (z & 7) held in `word`, -1 none
   unsigned long long word;  // active bits of plane wz of leaf `slot`
+  int bx = 0x7fffffff, by = 0, bz = 0;  // block coordinate `b` was found for
   __device__ __forceinline__ bool operator()(const int v[3])
   {
     const int x = v[0] >> 3, y = v[1] >> 3, z = v[2] >> 3;
     if (x != lx || y != ly || z != lz)
     {
-      lx   = x;
-      ly   = y;
-      lz   = z;
-      b    = voxel_in_map_range(v) ? find_block(*m, map, x >> 3, y >> 3, z >> 3) : -1;
+      lx = x;
+      ly = y;
+      lz = z;
+      // A ray crosses several leaves of a block (8^3 leaves) in a row: probe
+      // the block hash only when the block changes.
+      if ((x >> 3) != bx || (y >> 3) != by || (z >> 3) != bz)
+      {
+        bx = x >> 3;
+        by = y >> 3;
+        bz = z >> 3;
+        b  = voxel_in_map_range(v) ? find_block(*m, map, bx, by, bz) : -1;
+      }
       slot = b >= 0 ? m->bleaf[static_cast<size_t>(b) * 512 + (((x & 7) << 6) | ((y & 7) << 3) | (z & 7))] : -1;
       if (slot < 0) slot = -1;
       wz = -1;
@@ -1818,6 +1827,13 @@ __global__ void __launch_bounds__(128) k_fast_walk(const int4* __restrict__ rays
     const hdda::Ray fine = hdda::make_ray(eye, dir, sp.t0, sp.t1);
     hdda::Dda dda;
     hdda::dda_init(dda, fine, sp.t0, sp.t1, 0);
+    // The voxel steps of hdda::dda_step on the insertion DDA's state: the
+    // times held as their order keys (hdda::tkey), the argmin and the FP64
+    // tMax += tDelta as dda_advance does them (same tie rule, same sums).
+    DdaRay d{dda.voxel[0], dda.voxel[1], dda.voxel[2], dda.step[0], dda.step[1], dda.step[2],
+             hdda::tkey(dda.next[0]), hdda::tkey(dda.next[1]), hdda::tkey(dda.next[2]),
+             dda.delta[0], dda.delta[1], dda.delta[2]};
+    const long long t1 = hdda::tkey(sp.t1);
     ActiveCache act{&m, active, tv.map, 0x7fffffff, 0, 0, -1, -1, -1, 0ull};
     uint32_t steps = 0;
     do
@@ -1827,7 +1843,8 @@ __global__ void __launch_bounds__(128) k_fast_walk(const int4* __restrict__ rays
         atomicOr(&m.st->error, kErrStepBound);
         break;
       }
-      if (act(dda.voxel))
+      const int v[3] = {d.vx, d.vy, d.vz};
+      if (act(v))
       {
         // act holds the voxel's leaf: mark it visited in the update grid.
         const int b    = act.b;
@@ -1835,11 +1852,11 @@ __global__ void __launch_bounds__(128) k_fast_walk(const int4* __restrict__ rays
         touch_block(c, b);
         unsigned long long* bt = c.btouched + static_cast<size_t>(b) * 8 + (cell >> 6);
         if (!((*bt >> (cell & 63)) & 1ull)) atomicOr(bt, 1ull << (cell & 63));
-        const int off = ((dda.voxel[2] & 7) << 6) | ((dda.voxel[1] & 7) << 3) | (dda.voxel[0] & 7);
+        const int off = ((v[2] & 7) << 6) | ((v[1] & 7) << 3) | (v[0] & 7);
         atomicOr(c.upd + static_cast<size_t>(act.slot) * 16 + (off >> 6), 1ull << (off & 63));
         ++marks;
       }
-    } while (hdda::dda_step(dda));
+    } while (dda_advance(d) <= t1);
   }
   for (int off = 16; off > 0; off >>= 1) marks += __shfl_xor_sync(0xffffffffu, marks, off);
   if ((threadIdx.x & 31) == 0 && marks) atomicAdd(&m.st->visits, marks);
