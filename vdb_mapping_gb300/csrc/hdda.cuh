@@ -253,6 +253,60 @@ VDBG_HD bool dda_step(Dda& d)
   return tkey(d.t0) <= tkey(d.t1);
 }
 
+// A voxel-level DDA (log2 = 0) continued on integer-keyed state: the times
+// held as their order keys (tkey), the argmin with ties to the higher axis,
+// and the FP64 tMax += tDelta; fine_step enters the next voxel exactly as
+// dda_step does, with fewer instructions per step.
+struct FineDda
+{
+  int voxel[3];
+  int step[3];
+  long long next[3];  // tkey of the times
+  double delta[3];
+  long long t1;
+};
+
+VDBG_HD FineDda fine_from(const Dda& d)
+{
+  FineDda f;
+  for (int a = 0; a < 3; ++a)
+  {
+    f.voxel[a] = d.voxel[a];
+    f.step[a]  = d.step[a];
+    f.next[a]  = tkey(d.next[a]);
+    f.delta[a] = d.delta[a];
+  }
+  f.t1 = tkey(d.t1);
+  return f;
+}
+
+VDBG_HD double key_time(long long k)
+{
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(k);
+#else
+  double t;
+  std::memcpy(&t, &k, sizeof(t));
+  return t;
+#endif
+}
+
+VDBG_HD bool fine_step(FineDda& f)
+{
+  const bool ax      = (f.next[0] < f.next[1]) && (f.next[0] < f.next[2]);
+  const bool ay      = !ax && (f.next[1] < f.next[2]);
+  const long long t0 = ax ? f.next[0] : (ay ? f.next[1] : f.next[2]);
+  const double d     = ax ? f.delta[0] : (ay ? f.delta[1] : f.delta[2]);
+  const long long tn = tkey(add(key_time(t0), d));
+  f.next[0]          = ax ? tn : f.next[0];
+  f.next[1]          = ay ? tn : f.next[1];
+  f.next[2]          = (!ax && !ay) ? tn : f.next[2];
+  f.voxel[0] += ax ? f.step[0] : 0;
+  f.voxel[1] += ay ? f.step[1] : 0;
+  f.voxel[2] += (!ax && !ay) ? f.step[2] : 0;
+  return t0 <= f.t1;
+}
+
 // DDA::next(): the time the current cell is left, at most t1.
 VDBG_HD double dda_exit(const Dda& d)
 {
@@ -440,11 +494,12 @@ VDBG_HD int raytrace_one(const double o[3], const double dir[3], double len, dou
     const Ray fine = make_ray(oi, di, sp.t0, sp.t1);
     Dda dda;
     dda_init(dda, fine, sp.t0, sp.t1, 0);
-    while (dda_step(dda) && !active(dda.voxel))
+    FineDda f = fine_from(dda);
+    while (fine_step(f) && !active(f.voxel))
     {
       if (++steps > kStepLimit) return kTraceBound;
     }
-    for (int a = 0; a < 3; ++a) end[a] = mul(static_cast<double>(dda.voxel[a]), res);
+    for (int a = 0; a < 3; ++a) end[a] = mul(static_cast<double>(f.voxel[a]), res);
     success = true;
   }
   else
