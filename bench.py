@@ -674,12 +674,14 @@ def measure_batched(local, steps_timed, warmup, n_distinct, autotune=True, use_g
         return {"updates": upd, "rays": int(sum(counts))}
 
     phase = []
+    passes = []
 
     def timed(fn):
         for k in range(warmup):
             fn(k)
         torch.cuda.synchronize()
         phase.clear()
+        passes.clear()
         ms, upd, rays = [], 0, 0
         with ProfileRange(profile and fn is batched_step):
             for i in range(steps_timed):
@@ -695,12 +697,14 @@ def measure_batched(local, steps_timed, warmup, n_distinct, autotune=True, use_g
                 rays += st["rays"]
                 if fn is batched_step:
                     phase.append(b.timings())
+                    passes.append(b.timings()["passes"])
         return ms, upd, rays
 
     clocks = ClockSampler(local)
     clocks.start()
     b_ms, b_upd, b_rays = timed(batched_step)
     b_phase = {k: float(np.mean([p[k] for p in phase])) for k in ("prep_ms", "dda_ms", "sweep_ms", "total_ms")}
+    b_passes = list(passes)
     p_ms, p_upd, p_rays = timed(plain_step)
     clk = clocks.stop()
     same = all(b.mapDigest(i) == plain[i].mapDigest() for i in range(len(plain)))
@@ -713,6 +717,7 @@ def measure_batched(local, steps_timed, warmup, n_distinct, autotune=True, use_g
         "data": f"synthetic (seeded batched workload, {n_distinct} distinct steps cycled)",
         "config": {**wl.describe(), "l2": "flushed between steps (256 MiB write)"},
         "batched": {"voxel_updates_per_s": b_upd / b_s, "rays_per_s": b_rays / b_s, "phases_ms": b_phase,
+                    "dda_passes": b_passes,
                     "updates_per_step": b_upd / steps_timed,
                     "ms_per_step": {"p50": float(np.percentile(b_ms, 50)), "p99": float(np.percentile(b_ms, 99))}},
         "plain_per_map": {"voxel_updates_per_s": p_upd / p_s, "rays_per_s": p_rays / p_s,

@@ -340,7 +340,7 @@ int run_prepped(vdbg_map* m, PrepSet& p, vdbg_scan_stats* stats)
   uint32_t seg = std::max<uint32_t>(m->run_seg, kMinRunSeg);
   if (m->passes_last > 1)
   {
-    const uint64_t want  = static_cast<uint64_t>(m->run_seg) * m->passes_last * 5 / 4;
+    const uint64_t want  = static_cast<uint64_t>(m->run_seg) * m->passes_last * 2;
     const uint64_t limit = m->run_budget / (17ull * m->dda_warps);
     seg                  = static_cast<uint32_t>(std::min<uint64_t>(want, limit));
   }

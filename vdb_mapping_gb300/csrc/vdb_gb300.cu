@@ -1610,11 +1610,12 @@ int accumulate_and_integrate(vdbg_map* m, const float* xyz, int64_t n, int64_t s
     const bool host_input = (flags & VDBG_POINTS_DEVICE) == 0;
     VDBG_TRY(ensure_scratch(m, n, stride, host_input));
     // One pass for a scan like the last one: segments sized from the previous
-    // call's pass count (bounded by the run-buffer budget).
+    // call's pass count, with room to spare (a warp's runs vary from call to
+    // call with the long rays it takes), bounded by the run-buffer budget.
     uint32_t seg = std::max<uint32_t>(m->run_seg, kMinRunSeg);
     if (m->passes_last > 1)
     {
-      const uint64_t want  = static_cast<uint64_t>(m->run_seg) * m->passes_last * 5 / 4;
+      const uint64_t want  = static_cast<uint64_t>(m->run_seg) * m->passes_last * 2;
       const uint64_t limit = m->run_budget / (17ull * m->dda_warps);
       seg                  = static_cast<uint32_t>(std::min<uint64_t>(want, limit));
     }
