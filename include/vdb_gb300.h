@@ -331,8 +331,8 @@ int vdbg_apply_section_states(vdbg_map* map, int map_index, const int32_t lo[3],
  * created unless every voxel is inactive 0. The section tree's tiles, the
  * empty slots of its 128^3 and 4096^3 internal nodes, set the map voxel at
  * their origin to inactive 0 where a map leaf holds it, as the reference's
- * cbeginValueAll() does. Smoothing of value sections (morphologicalCloseMap,
- * :1026-1029) is not provided. */
+ * cbeginValueAll() does. Smoothing (morphologicalCloseMap, :1026-1029) is
+ * vdbg_section_morphology with VDBG_MORPH_KEEP_LEAVES first. */
 int vdbg_apply_section_values(vdbg_map* map, int map_index, int64_t n, const int32_t* origins, const float* values,
                               const uint64_t* masks);
 
@@ -368,7 +368,14 @@ int vdbg_restore_map_integrity(vdbg_map* map);
  * origin, *n_out of them (VDBG_ERR_BUFFER_TOO_SMALL when capacity is less).
  * Runs on the map's device and stream; the map is not changed.
  * applyMapSectionUpdateGrid's smoothing (VDBMapping.hpp:1062-1065) is op 2
- * before vdbg_apply_section_states. */
+ * before vdbg_apply_section_states.
+ * op | VDBG_MORPH_KEEP_LEAVES keeps the leaf topology as OpenVDB's morphology
+ * leaves a tree it does not prune: the output holds every input leaf and
+ * every leaf a dilation step set bits in, empty or not (erosion removes no
+ * leaf). applyMapSectionGrid's smoothing (VDBMapping.hpp:1026-1029) is op 2
+ * with this flag; the leaves it adds take the value 0, the others keep
+ * theirs, before vdbg_apply_section_values. */
+#define VDBG_MORPH_KEEP_LEAVES 16
 int vdbg_section_morphology(vdbg_map* map, int op, int iterations, int64_t n, const int32_t* origins,
                             const uint64_t* masks, int64_t capacity, int32_t* out_origins, uint64_t* out_masks,
                             int64_t* n_out);

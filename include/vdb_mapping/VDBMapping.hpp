@@ -18,8 +18,8 @@
 //     the only specialisation the reference ships (OccupancyVDBMapping.hpp).
 // Also provided:
 //   * map sections (getMapSection*, applyMapSection*, the bounding-box
-//     helpers; VDBMapping.hpp:811-1085), with smoothing of update-grid
-//     sections (morphological*Map, :1094-1147);
+//     helpers; VDBMapping.hpp:811-1085), with their smoothing
+//     (morphological*Map, :1094-1147);
 //   * fast mode (VDBMapping.hpp:577-602, through Config::fast_mode);
 //   * the raytrace queries (:646-721);
 //   * artificial areas (:1152-1236).
@@ -317,6 +317,13 @@ public:
   {
     sync();
     return m_table;
+  }
+  /*! Replaces the leaves of a detached (section) grid; the map's own grid
+   * follows the map and cannot be assigned. */
+  void assignLeaves(detail::LeafTable table)
+  {
+    if (m_dev) throw std::runtime_error("LeafGrid::assignLeaves: the grid follows the map");
+    m_table = std::move(table);
   }
 
 private:
@@ -718,11 +725,12 @@ public:
     return std::make_shared<GridT>(exportSection(box, full_grid), boxCorner(box.min()), boxCorner(box.max()));
   }
 
-  /*! VDBMapping.hpp:1022-1048 without smoothing (the section tree's tiles included). */
+  /*! VDBMapping.hpp:1022-1048 (the section tree's tiles included);
+   * smoothing closes the section in place first, as the reference does. */
   void applyMapSectionGrid(const typename GridT::Ptr section, bool smooth_map = false,
-                           int /*smoothing_iterations*/ = 2)
+                           int smoothing_iterations = 2)
   {
-    if (smooth_map) throw std::runtime_error("applyMapSectionGrid: smoothing is not provided");
+    if (smooth_map) morphologicalCloseMap<GridT>(section, smoothing_iterations);
     const detail::LeafTable& t = section->leaves();
     std::unique_lock map_lock(*m_map_mutex);
     check(vdbg_apply_section_values(m_dev->map, -1, static_cast<int64_t>(t.origins.size() / 3), t.origins.data(),
@@ -778,10 +786,13 @@ public:
     end_point = e[0];
   }
 
-  /*! VDBMapping.hpp:1094-1147 on a section update grid, on the GPU
+  /*! VDBMapping.hpp:1094-1147 on a section grid, on the GPU
    * (vdbg_section_morphology): the active voxels dilated / eroded with the
-   * 26-neighbourhood, values kept; leaves left without an active voxel are
-   * dropped. Value grids (GridT) are not supported. */
+   * 26-neighbourhood, values kept. On an update grid (UpdateGridT) leaves
+   * left without an active voxel are dropped (only its active voxels are
+   * ever read); on a value section (GridT from getMapSectionGrid) every leaf
+   * stays and the leaves a dilation adds hold 0, as OpenVDB leaves the tree
+   * when it does not prune (VDBG_MORPH_KEEP_LEAVES). */
   template <typename TGrid>
   void morphologicalCloseMap(typename TGrid::Ptr grid, int iterations)
   {
@@ -864,8 +875,48 @@ protected:
   template <typename TGrid>
   void morphology(const typename TGrid::Ptr& grid, int op, int iterations)
   {
-    static_assert(std::is_same<TGrid, UpdateGridT>::value,
-                  "morphology is provided for section update grids (UpdateGridT) only");
+    if constexpr (std::is_same<TGrid, UpdateGridT>::value)
+      morphologyStates(grid, op, iterations);
+    else
+      morphologyValues<TGrid>(grid, op, iterations);
+  }
+  template <typename TGrid>
+  void morphologyValues(const typename TGrid::Ptr& grid, int op, int iterations)
+  {
+#if defined(VDBG_WITH_OPENVDB)
+    static_assert(sizeof(TGrid) == 0, "morphology of an OpenVDB grid: call openvdb::tools on it");
+#else
+    static_assert(std::is_same<TGrid, GridT>::value, "morphology is provided for section grids");
+    const detail::LeafTable& t = grid->leaves();
+    const int64_t n_in          = static_cast<int64_t>(t.origins.size() / 3);
+    const int code              = op | VDBG_MORPH_KEEP_LEAVES;
+    int64_t n                   = 0;
+    int s = vdbg_section_morphology(m_dev->map, code, iterations, n_in, t.origins.data(), t.masks.data(), 0, nullptr,
+                                    nullptr, &n);
+    if (s != VDBG_OK && s != VDBG_ERR_BUFFER_TOO_SMALL) check(s, "vdbg_section_morphology");
+    detail::LeafTable r;
+    r.origins.assign(static_cast<size_t>(n) * 3, 0);
+    r.masks.assign(static_cast<size_t>(n) * 8, 0);
+    r.values.assign(static_cast<size_t>(n) * 512, 0.f);
+    if (n > 0)
+      check(vdbg_section_morphology(m_dev->map, code, iterations, n_in, t.origins.data(), t.masks.data(), n,
+                                    r.origins.data(), r.masks.data(), &n),
+            "vdbg_section_morphology");
+    for (size_t i = 0; i < static_cast<size_t>(n); ++i)
+    {
+      const auto key = std::make_tuple(r.origins[3 * i], r.origins[3 * i + 1], r.origins[3 * i + 2]);
+      const auto it  = t.index.find(key);
+      if (it != t.index.end())
+        std::copy(t.values.begin() + static_cast<std::ptrdiff_t>(it->second * 512),
+                  t.values.begin() + static_cast<std::ptrdiff_t>(it->second * 512 + 512),
+                  r.values.begin() + static_cast<std::ptrdiff_t>(i * 512));
+      r.index.emplace(key, i);
+    }
+    grid->assignLeaves(std::move(r));
+#endif
+  }
+  void morphologyStates(const typename UpdateGridT::Ptr& grid, int op, int iterations)
+  {
     const std::vector<int32_t> o = grid->leafOrigins();
     const std::vector<uint64_t> m = grid->activeMasks();
     const std::vector<uint64_t> v = grid->valueMasks();

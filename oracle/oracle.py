@@ -51,6 +51,7 @@ def load():
         "vo_apply_section_values": (None, [P, I64, P, P, P]),
         "vo_raytrace": (C.c_int, [P, I64, P, P, P, P, P]),
         "vo_morphology": (I64, [I64, P, P, C.c_int, C.c_int, I64, P, P]),
+        "vo_close_value_section": (I64, [I64, P, P, P, C.c_int, I64, P, P, P]),
         "vo_add_artificial_wall": (None, [P, C.POINTER(D), C.POINTER(D), D, D]),
         "vo_restore_map_integrity": (None, [P]),
         "vo_ray_digests": (None, [P, I64, I64, C.POINTER(D), D, D, C.c_int, P]),
@@ -172,8 +173,10 @@ class OracleMap:
         mk = np.ascontiguousarray(masks, np.uint64)
         self._l.vo_apply_section_states(self._h, lo.ctypes.data, hi.ctypes.data, len(o), o.ctypes.data, mk.ctypes.data)
 
-    def applyMapSectionValues(self, origins, values, masks):
-        """applyMapSectionGrid."""
+    def applyMapSectionValues(self, origins, values, masks, smooth=False, iterations=2):
+        """applyMapSectionGrid; smooth closes the section first (VDBMapping.hpp:1026-1029)."""
+        if smooth:
+            origins, values, masks = close_value_section(origins, values, masks, iterations)
         o = np.ascontiguousarray(origins, np.int32)
         v = np.ascontiguousarray(values, np.float32)
         mk = np.ascontiguousarray(masks, np.uint64)
@@ -277,18 +280,37 @@ def clip_quantise_variant(cloud, origin, max_range, res, w2i_divide=False, unit_
 MORPH_OPS = {"dilate": 0, "erode": 1, "close": 2, "open": 3}
 
 
-def morphology(origins, masks, op, iterations):
+def morphology(origins, masks, op, iterations, keep_leaves=False):
     """dilate / erode / close / open with the 26-neighbourhood (VDBMapping.hpp:1094-1147)
-    of leaves (origins (n,3), OpenVDB-order masks (n,8)): (origins, masks) sorted by origin."""
+    of leaves (origins (n,3), OpenVDB-order masks (n,8)): (origins, masks) sorted by origin.
+    keep_leaves: every input leaf and every leaf a dilation step reached stays, empty or not."""
     lib = load()
     o = np.ascontiguousarray(np.asarray(origins, np.int32).reshape(-1, 3))
     m = np.ascontiguousarray(np.asarray(masks, np.uint64).reshape(-1, 8))
-    n = lib.vo_morphology(len(o), o.ctypes.data, m.ctypes.data, MORPH_OPS[op], int(iterations), 0, None, None)
+    code = MORPH_OPS[op] | (16 if keep_leaves else 0)
+    n = lib.vo_morphology(len(o), o.ctypes.data, m.ctypes.data, code, int(iterations), 0, None, None)
     oo = np.zeros((n, 3), np.int32)
     om = np.zeros((n, 8), np.uint64)
-    lib.vo_morphology(len(o), o.ctypes.data, m.ctypes.data, MORPH_OPS[op], int(iterations), n, oo.ctypes.data,
+    lib.vo_morphology(len(o), o.ctypes.data, m.ctypes.data, code, int(iterations), n, oo.ctypes.data,
                       om.ctypes.data)
     return oo, om
+
+
+def close_value_section(origins, values, masks, iterations):
+    """morphologicalCloseMap of a value section (applyMapSectionGrid with smoothing,
+    VDBMapping.hpp:1026-1029): (origins, values, masks) sorted by origin."""
+    lib = load()
+    o = np.ascontiguousarray(np.asarray(origins, np.int32).reshape(-1, 3))
+    v = np.ascontiguousarray(np.asarray(values, np.float32).reshape(-1, 512))
+    m = np.ascontiguousarray(np.asarray(masks, np.uint64).reshape(-1, 8))
+    n = lib.vo_close_value_section(len(o), o.ctypes.data, v.ctypes.data, m.ctypes.data, int(iterations), 0, None,
+                                   None, None)
+    oo = np.zeros((n, 3), np.int32)
+    ov = np.zeros((n, 512), np.float32)
+    om = np.zeros((n, 8), np.uint64)
+    lib.vo_close_value_section(len(o), o.ctypes.data, v.ctypes.data, m.ctypes.data, int(iterations), n,
+                               oo.ctypes.data, ov.ctypes.data, om.ctypes.data)
+    return oo, ov, om
 
 
 def bench_replicas(res, cfg, scans, origins, threads):

@@ -181,15 +181,33 @@ void vo_apply_section_values(void* h, int64_t n, const int32_t* origins, const f
   static_cast<Handle*>(h)->map.apply_section_values(section_leaves(n, origins, values, masks));
 }
 
-// morphology (dilate 0, erode 1, close 2, open 3) of n leaves; returns the
-// result's leaf count and writes at most `cap` leaves (origins, masks).
+// morphology (dilate 0, erode 1, close 2, open 3; plus 16: keep the leaf
+// topology) of n leaves; returns the result's leaf count and writes at most
+// `cap` leaves (origins, masks).
 int64_t vo_morphology(int64_t n, const int32_t* origins, const uint64_t* masks, int op, int iterations, int64_t cap,
                       int32_t* out_origins, uint64_t* out_masks)
 {
-  const std::vector<MapLeaf> r = morphology(section_leaves(n, origins, nullptr, masks), op, iterations);
+  const std::vector<MapLeaf> r =
+    morphology(section_leaves(n, origins, nullptr, masks), op & 15, iterations, (op & 16) != 0);
   for (size_t i = 0; i < r.size() && static_cast<int64_t>(i) < cap; ++i)
   {
     for (int a = 0; a < 3; ++a) out_origins[3 * i + a] = r[i].origin[a];
+    std::memcpy(out_masks + 8 * i, r[i].on, sizeof(r[i].on));
+  }
+  return static_cast<int64_t>(r.size());
+}
+
+// close_value_section of n section leaves (origins, values, masks): returns
+// the result's leaf count and writes at most `cap` leaves.
+int64_t vo_close_value_section(int64_t n, const int32_t* origins, const float* values, const uint64_t* masks,
+                               int iterations, int64_t cap, int32_t* out_origins, float* out_values,
+                               uint64_t* out_masks)
+{
+  const std::vector<MapLeaf> r = close_value_section(section_leaves(n, origins, values, masks), iterations);
+  for (size_t i = 0; i < r.size() && static_cast<int64_t>(i) < cap; ++i)
+  {
+    for (int a = 0; a < 3; ++a) out_origins[3 * i + a] = r[i].origin[a];
+    std::memcpy(out_values + 512 * i, r[i].value, sizeof(r[i].value));
     std::memcpy(out_masks + 8 * i, r[i].on, sizeof(r[i].on));
   }
   return static_cast<int64_t>(r.size());

@@ -685,6 +685,10 @@ private:
 // 26 neighbours are all active; voxels outside the set are inactive. Returns
 // the leaves holding active voxels (values left at the background), sorted by
 // origin.
+// keep_leaves: the tree's topology as OpenVDB's morphology leaves it when it
+// does not prune: every input leaf stays, and a dilation step adds the leaves
+// it sets bits in; erosion removes none. The result then holds all of these
+// leaves, empty ones included.
 enum MorphOp : int
 {
   kMorphDilate = 0,
@@ -693,14 +697,18 @@ enum MorphOp : int
   kMorphOpen   = 3,
 };
 
-inline std::vector<MapLeaf> morphology(const std::vector<MapLeaf>& in, int op, int iterations)
+inline std::vector<MapLeaf> morphology(const std::vector<MapLeaf>& in, int op, int iterations,
+                                       bool keep_leaves = false)
 {
-  std::set<Coord> on;
+  std::set<Coord> on, topology;
   for (const MapLeaf& l : in)
+  {
+    if (keep_leaves) topology.insert(l.origin);
     for (uint32_t off = 0; off < 512; ++off)
       if ((l.on[off >> 6] >> (off & 63)) & 1ull)
         on.insert(Coord(l.origin.x + static_cast<int32_t>(off >> 6), l.origin.y + static_cast<int32_t>((off >> 3) & 7),
                         l.origin.z + static_cast<int32_t>(off & 7)));
+  }
   auto dilate = [&]() {
     std::set<Coord> out;
     for (const Coord& v : on)
@@ -708,6 +716,8 @@ inline std::vector<MapLeaf> morphology(const std::vector<MapLeaf>& in, int op, i
         for (int dy = -1; dy <= 1; ++dy)
           for (int dz = -1; dz <= 1; ++dz) out.insert(Coord(v.x + dx, v.y + dy, v.z + dz));
     on.swap(out);
+    if (keep_leaves)
+      for (const Coord& v : on) topology.insert(leaf_origin(v));
   };
   auto erode = [&]() {
     std::set<Coord> out;
@@ -727,6 +737,14 @@ inline std::vector<MapLeaf> morphology(const std::vector<MapLeaf>& in, int op, i
   if (both)
     for (int i = 0; i < iterations; ++i) dilate_first ? erode() : dilate();
   std::map<Coord, MapLeaf> leaves;
+  for (const Coord& o : topology)
+  {
+    MapLeaf l;
+    l.origin = o;
+    std::fill(l.value, l.value + 512, 0.0f);
+    std::memset(l.on, 0, sizeof(l.on));
+    leaves.emplace(o, l);
+  }
   for (const Coord& v : on)
   {
     const Coord o = leaf_origin(v);
@@ -745,6 +763,23 @@ inline std::vector<MapLeaf> morphology(const std::vector<MapLeaf>& in, int op, i
   std::vector<MapLeaf> out;
   out.reserve(leaves.size());
   for (auto& kv : leaves) out.push_back(kv.second);
+  return out;
+}
+
+// morphologicalCloseMap<GridT> of a value section (applyMapSectionGrid with
+// smooth_map, VDBMapping.hpp:1026-1029, 1094-1099): the active voxels closed
+// with the leaf topology kept (see morphology), values untouched; leaves the
+// dilation added hold the background 0. Sorted by origin.
+inline std::vector<MapLeaf> close_value_section(const std::vector<MapLeaf>& section, int iterations)
+{
+  std::vector<MapLeaf> out = morphology(section, kMorphClose, iterations, true);
+  std::map<Coord, const MapLeaf*> by_origin;
+  for (const MapLeaf& l : section) by_origin[l.origin] = &l;
+  for (MapLeaf& l : out)
+  {
+    auto it = by_origin.find(l.origin);
+    if (it != by_origin.end()) std::memcpy(l.value, it->second->value, sizeof(l.value));
+  }
   return out;
 }
 

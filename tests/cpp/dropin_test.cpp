@@ -210,6 +210,33 @@ TEST(DropIn, SmoothedSectionStates)
   EXPECT_FALSE(acc.isValueOn(openvdb::Coord(11, 0, 0)));
 }
 
+TEST(DropIn, SmoothedValueSection)
+{
+  // applyMapSectionGrid with smoothing (VDBMapping.hpp:1026-1029): the section
+  // is closed in place; the gap voxel turns active with the section's value
+  // there (a miss), and the leaves the dilation reached join the section.
+  OccupancyVDBMapping map(1.0);
+  map.setConfig(test_config(20));
+  map.addInputSource("lidar", 20, 0);
+  Eigen::Matrix<double, 3, 1> origin(0, 0, 0);
+  map.insertPointCloud(cloud_of({{12.f, 0.f, 0.f}, {14.f, 0.f, 0.f}}), origin, "lidar");
+  auto eye = Eigen::Matrix<double, 4, 4>::Identity();
+  Eigen::Matrix<double, 3, 1> lo(9.5, -0.5, -0.5), hi(15.5, 0.5, 0.5);
+  auto full = map.getMapSectionGrid(lo, hi, eye, true);
+  const size_t leaves_before = full->leafCount();
+  EXPECT_FALSE(full->getAccessor().isValueOn(openvdb::Coord(13, 0, 0)));
+  OccupancyVDBMapping other(1.0);
+  other.applyMapSectionGrid(full, true, 1);
+  EXPECT_TRUE(full->getAccessor().isValueOn(openvdb::Coord(13, 0, 0)));
+  EXPECT_TRUE(full->leafCount() > leaves_before);
+  auto acc = other.getGrid()->getAccessor();
+  EXPECT_TRUE(acc.isValueOn(openvdb::Coord(12, 0, 0)));
+  EXPECT_TRUE(acc.isValueOn(openvdb::Coord(13, 0, 0)));
+  EXPECT_EQ(acc.getValue(openvdb::Coord(13, 0, 0)), logodds(0.1));
+  EXPECT_EQ(acc.getValue(openvdb::Coord(12, 0, 0)), logodds(0.9));
+  EXPECT_FALSE(acc.isValueOn(openvdb::Coord(11, 0, 0)));
+}
+
 TEST(DropIn, ArtificialWall)
 {
   // addArtificialWall (VDBMapping.hpp:1210-1236): the wall turns active with

@@ -1,7 +1,8 @@
 """GPU parity of the section morphology (VDBMapping.hpp:1094-1147,
-vdbg_section_morphology) against the oracle's voxel-set restatement, and of
-applyMapSectionUpdateGrid with smoothing (VDBMapping.hpp:1062-1065). Bit-exact:
-leaf origins and masks."""
+vdbg_section_morphology, with and without the kept leaf topology) against the
+oracle's voxel-set restatement, and of applyMapSectionUpdateGrid and
+applyMapSectionGrid with smoothing (VDBMapping.hpp:1062-1065, 1026-1029).
+Bit-exact: leaf origins, masks and values."""
 import numpy as np
 import pytest
 
@@ -49,3 +50,30 @@ def test_smoothed_section_states_match_oracle(vdbg, oracle):
     o.applyMapSectionStates(lo, hi, co, cm)
     assert_same_map(g.exportLeaves(), o.exportLeaves(), "smoothed states")
     assert len(co) >= len(so)
+
+
+@pytest.mark.parametrize("op", ["dilate", "erode", "close", "open"])
+def test_morphology_keeping_leaves_matches_oracle(vdbg, oracle, op):
+    g = vdbg.OccupancyVDBMapping(0.1)
+    for seed in range(4):
+        for density in (0.0, 0.02, 0.5):
+            o, m = random_section(100 + seed, 30, density)
+            it = 1 + seed % 3
+            go, gm = g.sectionMorphology(o, m, op, it, keep_leaves=True)
+            oo, om = oracle.morphology(o, m, op, it, keep_leaves=True)
+            assert np.array_equal(go, oo), (op, seed, density, len(go), len(oo))
+            assert np.array_equal(gm, om), (op, seed, density)
+            assert len(go) >= len(o)
+
+
+@pytest.mark.parametrize("iterations", [1, 2])
+def test_smoothed_value_section_matches_oracle(vdbg, oracle, iterations):
+    g, o = built_pair(vdbg, oracle)
+    _, src_o = built_pair(vdbg, oracle)
+    lo, hi = np.array([-60, -60, -8]), np.array([60, 60, 16])
+    so, sv, sm = src_o.getMapSection(lo, hi, full=True)
+    g.applyMapSectionValues(so, sv, sm, smooth=True, iterations=iterations)
+    o.applyMapSectionValues(so, sv, sm, smooth=True, iterations=iterations)
+    assert_same_map(g.exportLeaves(), o.exportLeaves(), "smoothed values")
+    co, _, _ = oracle.close_value_section(so, sv, sm, iterations)
+    assert len(co) > len(so)

@@ -61,3 +61,30 @@ def test_result_is_sorted_and_without_empty_leaves(oracle):
     keys = [tuple(x) for x in o]
     assert keys == sorted(keys)
     assert all(int(np.bitwise_or.reduce(row)) != 0 for row in m)
+
+
+def test_keep_leaves_holds_every_leaf_a_dilation_reached(oracle):
+    # A voxel at a leaf corner: the dilation reaches the seven leaves around
+    # it, the erosion empties them again; with the topology kept they stay.
+    vox = [(0, 0, 0), (0, 0, 2)]
+    o, m = oracle.morphology(*leaves_of(vox), "close", 1, keep_leaves=True)
+    assert sorted(map(tuple, o)) == sorted(itertools.product((-8, 0), repeat=3))
+    assert voxels_of(o, m) == {(0, 0, 0), (0, 0, 1), (0, 0, 2)}
+    assert sum(int(np.bitwise_or.reduce(row)) == 0 for row in m) == 7
+    # an empty input leaf stays; erosion alone removes no leaf
+    eo = np.array([[64, 64, 64], [0, 0, 0]], np.int32)
+    em = np.zeros((2, 8), np.uint64)
+    em[1][0] = np.uint64(1)  # voxel (0, 0, 0)
+    ko, km = oracle.morphology(eo, em, "erode", 2, keep_leaves=True)
+    assert sorted(map(tuple, ko)) == [(0, 0, 0), (64, 64, 64)] and not km.any()
+    assert len(oracle.morphology(eo, em, "erode", 2)[0]) == 0
+
+
+def test_close_value_section_keeps_values_and_zero_fills_new_leaves(oracle):
+    o, m = leaves_of([(0, 0, 0), (2, 0, 0)])
+    v = np.full((1, 512), 0.25, np.float32)
+    co, cv, cm = oracle.close_value_section(o, v, m, 1)
+    assert len(co) == 8
+    for org, vals in zip(co, cv):
+        assert np.all(vals == (0.25 if tuple(org) == (0, 0, 0) else 0.0))
+    assert voxels_of(co, cm) == {(0, 0, 0), (1, 0, 0), (2, 0, 0)}

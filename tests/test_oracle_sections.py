@@ -125,3 +125,31 @@ def test_create_index_bounding_box():
     rot = np.array([[0, -1, 0, 1.0], [1, 0, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1]], np.float64)  # 90 deg about z, +1 m x
     lo, hi = createIndexBoundingBox((0.0, 0.0, 0.0), (1.0, 2.0, 1.0), rot, 0.5)
     assert tuple(lo) == (-2, 0, 0) and tuple(hi) == (2, 2, 2)
+
+
+def test_apply_smoothed_value_section(oracle):
+    """applyMapSectionGrid with smoothing (VDBMapping.hpp:1026-1029): the
+    closing fills the gap between two active voxels with the section's stored
+    value there, and the leaves its dilation reached are written as well: a
+    leaf the erosion emptied again overwrites the map leaf there with
+    inactive zeros (the morphology does not prune it)."""
+    m = small_map(oracle)
+    assert m.getValue((-1, 0, 0)) == 0.0
+    # a map leaf at (-8, 0, 0) with values: a ray towards -x
+    m.insertPointCloud(np.array([[-0.75, 0.05, 0.05]], np.float32), (0.0, 0.0, 0.0), "s")
+    assert m.getValue((-3, 0, 0)) != 0.0
+    org = np.array([[0, 0, 0]], np.int32)
+    vals = np.full((1, 512), 0.5, np.float32)
+    masks = np.zeros((1, 8), np.uint64)
+    for x in (0, 2):
+        masks[0][vdb_off(x, 0, 0) >> 6] |= np.uint64(1) << np.uint64(vdb_off(x, 0, 0) & 63)
+    unsmoothed = small_map(oracle)
+    unsmoothed.insertPointCloud(np.array([[-0.75, 0.05, 0.05]], np.float32), (0.0, 0.0, 0.0), "s")
+    unsmoothed.applyMapSectionValues(org, vals, masks)
+    assert not unsmoothed.isValueOn((1, 0, 0))
+    assert unsmoothed.getValue((-3, 0, 0)) == m.getValue((-3, 0, 0))
+    m.applyMapSectionValues(org, vals, masks, smooth=True, iterations=1)
+    assert m.isValueOn((1, 0, 0)) and m.getValue((1, 0, 0)) == 0.5
+    assert m.isValueOn((0, 0, 0)) and m.isValueOn((2, 0, 0))
+    # the dilated, then emptied, leaf (-8, 0, 0) of the section
+    assert m.getValue((-3, 0, 0)) == 0.0 and not m.isValueOn((-3, 0, 0))

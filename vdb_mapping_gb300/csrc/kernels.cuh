@@ -2036,8 +2036,9 @@ __global__ void k_morph_load(const int4* __restrict__ origin, const unsigned lon
 
 // Dilation: one thread per (leaf of `in`, direction); the neighbours that
 // receive bits become the leaves of `out` (deduplicated by its hash).
-// Erosion (dilate == 0): the leaves of `in` themselves.
-__global__ void k_morph_candidates(MorphSet in, uint32_t n_in, MorphSet out, int dilate)
+// Erosion (dilate == 0): the leaves of `in` themselves. `keep`: every leaf of
+// `in` is also a leaf of `out`, empty or not (the topology is never pruned).
+__global__ void k_morph_candidates(MorphSet in, uint32_t n_in, MorphSet out, int dilate, int keep)
 {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_in * 27u) return;
@@ -2045,7 +2046,8 @@ __global__ void k_morph_candidates(MorphSet in, uint32_t n_in, MorphSet out, int
   const int d      = static_cast<int>(t % 27u);
   const int dx = d / 9 - 1, dy = (d / 3) % 3 - 1, dz = d % 3 - 1;
   if (!dilate && d != 13) return;
-  if (dilate && !morph::feeds(reinterpret_cast<const uint64_t*>(in.mask + static_cast<size_t>(i) * 8), dx, dy, dz))
+  if (dilate && !(keep && d == 13) &&
+      !morph::feeds(reinterpret_cast<const uint64_t*>(in.mask + static_cast<size_t>(i) * 8), dx, dy, dz))
     return;
   const int4 o = in.origin[i];
   const int4 c = make_int4(o.x + 8 * dx, o.y + 8 * dy, o.z + 8 * dz, 0);
@@ -2077,12 +2079,13 @@ __global__ void k_morph_words(MorphSet in, MorphSet out, uint32_t n_out, int dil
   out.mask[static_cast<size_t>(j) * 8 + a] = dilate ? morph::dilate_word(nb, a) : morph::erode_word(nb, a);
 }
 
-// The leaves of `in` with an active voxel, into the empty set `out`.
-__global__ void k_morph_compact(MorphSet in, uint32_t n_in, MorphSet out)
+// The leaves of `in` with an active voxel (`keep`: all of them), into the
+// empty set `out`.
+__global__ void k_morph_compact(MorphSet in, uint32_t n_in, MorphSet out, int keep)
 {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_in) return;
-  unsigned long long any = 0ull;
+  unsigned long long any = keep ? 1ull : 0ull;
   for (int w = 0; w < 8; ++w) any |= in.mask[static_cast<size_t>(i) * 8 + w];
   if (!any) return;
   const int4 o = in.origin[i];

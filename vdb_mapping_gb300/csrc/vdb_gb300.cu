@@ -2758,7 +2758,9 @@ int morph_counters(const uint32_t* d, uint32_t* h, cudaStream_t s)
 // The morphology of n leaves (unique origins, OpenVDB-order masks) on the
 // device: the steps of `op`, each a candidate pass, a word pass and a
 // compaction. The result leaves (unsorted) come back in out_o / out_m.
-int morph_run(vdbg_map* m, int op, int iterations, const std::vector<int32_t>& origins,
+// `keep`: no leaf is dropped (the input's empty leaves, and those a dilation
+// step reached and a later erosion emptied, stay).
+int morph_run(vdbg_map* m, int op, int iterations, bool keep, const std::vector<int32_t>& origins,
               const std::vector<uint64_t>& masks, std::vector<int32_t>& out_o, std::vector<uint64_t>& out_m)
 {
   cudaStream_t s = m->stream;
@@ -2793,7 +2795,7 @@ int morph_run(vdbg_map* m, int op, int iterations, const std::vector<int32_t>& o
       VDBG_TRY(morph_alloc(m, B, n, ctr + 2, s));
       k_morph_load<<<(n + 255) / 256, 256, 0, s>>>(d_o, d_m, n, morph_view(B, ctr + 2, ctr + 1));
       k_morph_compact<<<(n + 255) / 256, 256, 0, s>>>(morph_view(B, ctr + 2, ctr + 1), n,
-                                                      morph_view(A, ctr, ctr + 1));
+                                                      morph_view(A, ctr, ctr + 1), keep ? 1 : 0);
       VDBG_CUDA(cudaGetLastError());
       m->timings.launches += 2;
       morph_free(m, B);
@@ -2808,13 +2810,15 @@ int morph_run(vdbg_map* m, int op, int iterations, const std::vector<int32_t>& o
       VDBG_TRY(morph_alloc(m, B, static_cast<uint32_t>(cap_b), ctr + 2, s));
       const MorphSet va = morph_view(A, ctr, ctr + 1);
       const MorphSet vb = morph_view(B, ctr + 2, ctr + 1);
-      k_morph_candidates<<<static_cast<unsigned>((27ull * n_a + 255) / 256), 256, 0, s>>>(va, n_a, vb, dil ? 1 : 0);
+      k_morph_candidates<<<static_cast<unsigned>((27ull * n_a + 255) / 256), 256, 0, s>>>(va, n_a, vb, dil ? 1 : 0,
+                                                                                         keep ? 1 : 0);
       VDBG_CUDA(cudaGetLastError());
       VDBG_TRY(morph_counters(ctr, hc, s));
       const uint32_t n_b = hc[2];
       if (n_b > 0) k_morph_words<<<(n_b * 8u + 255) / 256, 256, 0, s>>>(va, vb, n_b, dil ? 1 : 0);
       VDBG_TRY(morph_alloc(m, C, n_b, ctr, s));
-      if (n_b > 0) k_morph_compact<<<(n_b + 255) / 256, 256, 0, s>>>(vb, n_b, morph_view(C, ctr, ctr + 1));
+      if (n_b > 0)
+        k_morph_compact<<<(n_b + 255) / 256, 256, 0, s>>>(vb, n_b, morph_view(C, ctr, ctr + 1), keep ? 1 : 0);
       VDBG_CUDA(cudaGetLastError());
       m->timings.launches += 3;
       VDBG_TRY(morph_counters(ctr, hc, s));
@@ -3048,6 +3052,8 @@ int vdbg_section_morphology(vdbg_map* m, int op, int iterations, int64_t n, cons
                             const uint64_t* masks, int64_t capacity, int32_t* out_origins, uint64_t* out_masks,
                             int64_t* n_out)
 {
+  const bool keep = (op & VDBG_MORPH_KEEP_LEAVES) != 0;
+  op &= ~VDBG_MORPH_KEEP_LEAVES;
   if (!m || !n_out || op < 0 || op > 3 || iterations < 0 || iterations > 64 || n < 0 || capacity < 0 ||
       (n > 0 && (!origins || !masks)) || (capacity > 0 && (!out_origins || !out_masks)))
     return VDBG_ERR_INVALID_ARGUMENT;
@@ -3080,7 +3086,7 @@ int vdbg_section_morphology(vdbg_map* m, int op, int iterations, int64_t n, cons
   VDBG_CUDA(cudaStreamSynchronize(m->stream));
   std::vector<int32_t> ro;
   std::vector<uint64_t> rm;
-  VDBG_TRY(morph_run(m, op, iterations, uo, um, ro, rm));
+  VDBG_TRY(morph_run(m, op, iterations, keep, uo, um, ro, rm));
   const size_t k = ro.size() / 3;
   std::vector<size_t> order(k);
   std::iota(order.begin(), order.end(), size_t(0));

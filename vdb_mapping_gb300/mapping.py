@@ -218,21 +218,40 @@ def _section_values(lib, h, map_index, origins, values, masks, check):
 MORPH_OPS = {"dilate": 0, "erode": 1, "close": 2, "open": 3}
 
 
-def _morphology(lib, h, origins, masks, op, iterations, check):
+MORPH_KEEP_LEAVES = 16  # VDBG_MORPH_KEEP_LEAVES
+
+
+def _morphology(lib, h, origins, masks, op, iterations, check, keep_leaves=False):
     o = np.ascontiguousarray(np.asarray(origins, np.int32).reshape(-1, 3))
     mk = np.ascontiguousarray(np.asarray(masks, np.uint64).reshape(-1, 8))
+    code = MORPH_OPS[op] | (MORPH_KEEP_LEAVES if keep_leaves else 0)
     n = C.c_int64()
     cap = 0
     while True:
         oo = np.zeros((cap, 3), np.int32)
         om = np.zeros((cap, 8), np.uint64)
-        s = lib.vdbg_section_morphology(h, MORPH_OPS[op], int(iterations), len(o), o.ctypes.data, mk.ctypes.data, cap,
+        s = lib.vdbg_section_morphology(h, code, int(iterations), len(o), o.ctypes.data, mk.ctypes.data, cap,
                                         oo.ctypes.data, om.ctypes.data, C.byref(n))
         if s == _lib.STATUS_CODE["VDBG_ERR_BUFFER_TOO_SMALL"]:
             cap = n.value
             continue
         check(s, "vdbg_section_morphology")
         return oo[: n.value], om[: n.value]
+
+
+def _close_value_section(lib, h, origins, values, masks, iterations, check):
+    """morphologicalCloseMap of a value section (VDBMapping.hpp:1026-1029, 1094-1099):
+    the active voxels closed with every leaf kept; the leaves the dilation adds hold 0."""
+    o = np.asarray(origins, np.int32).reshape(-1, 3)
+    v = np.asarray(values, np.float32).reshape(-1, 512)
+    ro, rm = _morphology(lib, h, o, masks, "close", iterations, check, keep_leaves=True)
+    rv = np.zeros((len(ro), 512), np.float32)
+    where = {tuple(int(c) for c in org): i for i, org in enumerate(o)}
+    for j, org in enumerate(ro):
+        i = where.get(tuple(int(c) for c in org))
+        if i is not None:
+            rv[j] = v[i]
+    return ro, rv, rm
 
 
 def _raytrace(lib, h, map_index, origins, directions, max_lengths, check):
@@ -500,14 +519,18 @@ class OccupancyVDBMapping:
         self._check(self._lib.vdbg_restore_map_integrity(self._h), "vdbg_restore_map_integrity")
         self._version += 1
 
-    def sectionMorphology(self, origins, masks, op: str = "close", iterations: int = 2):
+    def sectionMorphology(self, origins, masks, op: str = "close", iterations: int = 2, keep_leaves: bool = False):
         """morphologicalDilateMap / ErodeMap / CloseMap / OpenMap (VDBMapping.hpp:1094-1147)
         of a section's active voxels on the GPU: op in dilate, erode, close, open.
-        Returns (origins, masks) of the leaves with active voxels, sorted by origin."""
-        return _morphology(self._lib, self._h, origins, masks, op, iterations, self._check)
+        Returns (origins, masks) of the leaves with active voxels, sorted by origin;
+        keep_leaves: every input leaf and every leaf a dilation reached, empty or not."""
+        return _morphology(self._lib, self._h, origins, masks, op, iterations, self._check, keep_leaves)
 
-    def applyMapSectionValues(self, origins, values, masks) -> None:
-        """applyMapSectionGrid (no smoothing)."""
+    def applyMapSectionValues(self, origins, values, masks, smooth: bool = False, iterations: int = 2) -> None:
+        """applyMapSectionGrid; smooth closes the section first (VDBMapping.hpp:1026-1029)."""
+        if smooth:
+            origins, values, masks = _close_value_section(self._lib, self._h, origins, values, masks, iterations,
+                                                          self._check)
         _section_values(self._lib, self._h, -1, origins, values, masks, self._check)
 
     def raytrace(self, origins, directions, max_lengths):
@@ -696,11 +719,15 @@ class MapBatch:
             origins, masks = self.sectionMorphology(origins, masks, "close", iterations)
         _section_states(self._lib, self._h, map_index, lo, hi, origins, masks, self._check)
 
-    def sectionMorphology(self, origins, masks, op: str = "close", iterations: int = 2):
+    def sectionMorphology(self, origins, masks, op: str = "close", iterations: int = 2, keep_leaves: bool = False):
         """See OccupancyVDBMapping.sectionMorphology."""
-        return _morphology(self._lib, self._h, origins, masks, op, iterations, self._check)
+        return _morphology(self._lib, self._h, origins, masks, op, iterations, self._check, keep_leaves)
 
-    def applyMapSectionValues(self, map_index: int, origins, values, masks) -> None:
+    def applyMapSectionValues(self, map_index: int, origins, values, masks, smooth: bool = False,
+                              iterations: int = 2) -> None:
+        if smooth:
+            origins, values, masks = _close_value_section(self._lib, self._h, origins, values, masks, iterations,
+                                                          self._check)
         _section_values(self._lib, self._h, map_index, origins, values, masks, self._check)
 
     def raytrace(self, map_index: int, origins, directions, max_lengths):
