@@ -274,15 +274,21 @@ __device__ __forceinline__ uint32_t ld_ca_u32(const uint32_t* p)
   asm volatile("ld.global.ca.u32 %0, [%1];" : "=r"(v) : "l"(p));
   return v;
 }
-__device__ __forceinline__ int ld_acquire_s32(const int* p)
+// Relaxed (coherent, unordered) load and store at device scope: for a value
+// that is itself the whole message, with nothing else to order behind it.
+// The pools publish slots this way: within a kernel the threads that wait
+// for a slot use only the slot number, and the slot's origin record is read
+// by later kernels only (a release would make every allocating thread wait
+// for all of its earlier memory operations).
+__device__ __forceinline__ int ld_relaxed_s32(const int* p)
 {
   int v;
-  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release_s32(int* p, int v)
+__device__ __forceinline__ void st_relaxed_s32(int* p, int v)
 {
-  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+  asm volatile("st.relaxed.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 // ---- bulk asynchronous copies (global -> shared) completed on an mbarrier ----
@@ -419,7 +425,7 @@ __device__ __forceinline__ int find_or_insert_block(const MapView& m, int map, i
           m.borigin[s] = make_int4(bx, by, bz, map);
           slot         = static_cast<int>(s);
         }
-        st_release_s32(m.bslots + h, slot);
+        st_relaxed_s32(m.bslots + h, slot);
         return slot;
       }
       k = prev;
@@ -427,7 +433,7 @@ __device__ __forceinline__ int find_or_insert_block(const MapView& m, int map, i
     if (k == key)
     {
       int s = ld_ca_s32(m.bslots + h);
-      if (s == kSlotPending) s = ld_acquire_s32(m.bslots + h);
+      if (s == kSlotPending) s = ld_relaxed_s32(m.bslots + h);
       uint32_t spins = 0;
       while (s == kSlotPending)
       {
@@ -437,7 +443,7 @@ __device__ __forceinline__ int find_or_insert_block(const MapView& m, int map, i
           return kSlotFailed;
         }
         __nanosleep(64);
-        s = ld_acquire_s32(m.bslots + h);
+        s = ld_relaxed_s32(m.bslots + h);
       }
       if (s < 0)
       {
@@ -471,11 +477,11 @@ __device__ __forceinline__ int find_or_insert_leaf(const MapView& m, int b, int 
       if (t >= m.capacity)
       {
         atomicOr(&m.st->error, kErrPoolFull);
-        st_release_s32(e, kLeafFailed);
+        st_relaxed_s32(e, kLeafFailed);
         return kSlotFailed;
       }
       m.origin[t] = make_int4(lx * 8, ly * 8, lz * 8, map);
-      st_release_s32(e, static_cast<int>(t));
+      st_relaxed_s32(e, static_cast<int>(t));
       return static_cast<int>(t);
     }
     s = prev;
@@ -489,7 +495,7 @@ __device__ __forceinline__ int find_or_insert_leaf(const MapView& m, int b, int 
       return kSlotFailed;
     }
     __nanosleep(64);
-    s = ld_acquire_s32(e);
+    s = ld_relaxed_s32(e);
   }
   if (s < 0)
   {
