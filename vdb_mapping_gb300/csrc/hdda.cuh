@@ -464,10 +464,13 @@ enum TraceStatus : int
 // finds a span, the voxel DDA from its start steps until it enters an active
 // voxel or passes the span's end (the start voxel is not tested), and the
 // end point is that voxel in world space; otherwise the ray's end.
-template <class Topo, class Active>
-VDBG_HD int raytrace_one(const double o[3], const double dir[3], double len, double res, double inv_res,
-                         const Box& box, const Topo& topo, Active&& active, bool& success, double end[3],
-                         uint32_t& steps)
+// In three parts, so that a caller can run them apart (the device finds all
+// queries' spans first, then walks them): trace_ray, trace_span, trace_walk.
+
+// The query's ray in index space, origin oi and direction di (t in [0, 1]);
+// false when its start or end leaves the +-2^30 index box (or is NaN).
+VDBG_HD bool trace_ray(const double o[3], const double dir[3], double len, double inv_res, double oi[3],
+                       double di[3])
 {
   double d[3]     = {dir[0], dir[1], dir[2]};
   const double ln = root(add(add(mul(d[0], d[0]), mul(d[1], d[1])), mul(d[2], d[2])));
@@ -476,35 +479,71 @@ VDBG_HD int raytrace_one(const double o[3], const double dir[3], double len, dou
     const double s = dvd(1.0, ln);
     for (int a = 0; a < 3; ++a) d[a] = mul(d[a], s);
   }
-  double oi[3], di[3];
   for (int a = 0; a < 3; ++a)
   {
     d[a]  = mul(d[a], len);
     oi[a] = mul(o[a], inv_res);
     di[a] = mul(d[a], inv_res);
   }
+  const Ray r = make_ray(oi, di, 0.0, 1.0);
+  return start_ok(r, 0.0) && start_ok(r, 1.0);
+}
+
+// The first span of the query's ray clipped by the box (march).
+template <class Topo>
+VDBG_HD int trace_span(const double oi[3], const double di[3], const Box& box, const Topo& topo, Span& sp,
+                       bool& found, uint32_t& steps)
+{
   Ray r = make_ray(oi, di, 0.0, 1.0);
-  if (!start_ok(r, 0.0) || !start_ok(r, 1.0)) return kTraceRange;
   clip(r, box.lo, box.hi_excl);
+  sp    = Span{-1.0, -1.0};
+  found = false;
+  if (march_first(r, topo, sp, found, steps) == kWalkBound) return kTraceBound;
+  return kTraceOk;
+}
+
+// The voxel walk over span `sp`: end = the first active voxel after the
+// start voxel, or the voxel just past the span, in world space.
+template <class Active>
+VDBG_HD int trace_walk(const double oi[3], const double di[3], const Span& sp, double res, Active&& active,
+                       double end[3], uint32_t& steps)
+{
+  const Ray fine = make_ray(oi, di, sp.t0, sp.t1);
+  Dda dda;
+  dda_init(dda, fine, sp.t0, sp.t1, 0);
+  FineDda f = fine_from(dda);
+  while (fine_step(f) && !active(f.voxel))
+  {
+    if (++steps > kStepLimit) return kTraceBound;
+  }
+  for (int a = 0; a < 3; ++a) end[a] = mul(static_cast<double>(f.voxel[a]), res);
+  return kTraceOk;
+}
+
+// The end point of a query without a span: the ray's end.
+VDBG_HD void trace_miss(const double oi[3], const double di[3], double res, double end[3])
+{
+  for (int a = 0; a < 3; ++a) end[a] = mul(add(oi[a], di[a]), res);
+}
+
+template <class Topo, class Active>
+VDBG_HD int raytrace_one(const double o[3], const double dir[3], double len, double res, double inv_res,
+                         const Box& box, const Topo& topo, Active&& active, bool& success, double end[3],
+                         uint32_t& steps)
+{
+  double oi[3], di[3];
+  if (!trace_ray(o, dir, len, inv_res, oi, di)) return kTraceRange;
   Span sp{-1.0, -1.0};
   bool found = false;
-  if (march_first(r, topo, sp, found, steps) == kWalkBound) return kTraceBound;
+  if (trace_span(oi, di, box, topo, sp, found, steps) == kTraceBound) return kTraceBound;
   if (found)
   {
-    const Ray fine = make_ray(oi, di, sp.t0, sp.t1);
-    Dda dda;
-    dda_init(dda, fine, sp.t0, sp.t1, 0);
-    FineDda f = fine_from(dda);
-    while (fine_step(f) && !active(f.voxel))
-    {
-      if (++steps > kStepLimit) return kTraceBound;
-    }
-    for (int a = 0; a < 3; ++a) end[a] = mul(static_cast<double>(f.voxel[a]), res);
+    if (trace_walk(oi, di, sp, res, active, end, steps) == kTraceBound) return kTraceBound;
     success = true;
   }
   else
   {
-    for (int a = 0; a < 3; ++a) end[a] = mul(add(oi[a], di[a]), res);
+    trace_miss(oi, di, res, end);
     success = false;
   }
   return kTraceOk;

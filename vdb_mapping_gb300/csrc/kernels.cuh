@@ -22,7 +22,8 @@
 //   k_fast_spans, k_fast_walk VDBMapping.hpp:577-602  fast mode: the
 //                                       intersector's spans of each ray, then
 //                                       the active map voxels along each span
-//   k_raytrace VDBMapping.hpp:675-721   raytrace queries
+//   k_trace_spans, k_trace_walk VDBMapping.hpp:675-721  raytrace queries:
+//                                       first spans, then the voxel walks
 //   k_morph_*  VDBMapping.hpp:1094-1147 dilation / erosion of section leaves
 //   k_wall_voxels VDBMapping.hpp:1210-1236  artificial walls, castRayIntoGrid per layer
 //   k_artificial_restore VDBMapping.hpp:1153-1166  restoreMapIntegrity
@@ -1739,8 +1740,10 @@ __device__ __forceinline__ hdda::Box topo_box(const TopoView& tv)
 struct SpanRec
 {
   double t0, t1;
-  int ray;  // index into the ray records
-  int cls;  // length class: floor(log2) of the span's estimated voxel steps
+  int ray;         // index into the ray records (raytrace: the query)
+  int cls;         // length class: floor(log2) of the span's estimated voxel steps
+  uint32_t steps;  // raytrace: the steps its coarse walk took (one bound for the query)
+  uint32_t pad;
 };
 constexpr int kSpanClasses = 32;
 
@@ -1911,15 +1914,40 @@ __global__ void __launch_bounds__(256) k_span_scatter(const SpanRec* __restrict_
 // counted (one thread).
 __global__ void k_fast_visits(DevStatus* st, const unsigned long long* dda_visits) { st->visits -= *dda_visits; }
 
-// raytrace (VDBMapping.hpp:675-721), one thread per query: q holds the
-// origins [n][3], then the directions [n][3], then the lengths [n]; ok[n] and
-// end[n][3] receive success and end point. A query outside the +-2^30 index
-// box sets kErrCoordRange.
-__global__ void __launch_bounds__(128) k_raytrace(const double* __restrict__ q, uint32_t n, double res,
-                                                  double inv_res, MapView m, TopoView tv,
-                                                  const uint32_t* __restrict__ flags,
-                                                  const unsigned long long* __restrict__ active,
-                                                  unsigned char* __restrict__ ok, double* __restrict__ end)
+// raytrace (VDBMapping.hpp:675-721) in two phases, as fast mode walks its
+// spans: k_trace_spans finds every query's first span (hdda::trace_span) and
+// answers the queries without one; the spans are sorted by length (longest
+// first, k_span_hist / k_span_scatter), and k_trace_walk walks one span per
+// thread to its first active voxel (hdda::trace_walk). The coarse walk needs
+// many registers and the voxel walk few, so apart each runs at its own
+// occupancy, and the walks of a warp take about as many steps each. q holds
+// the origins [n][3], then the directions [n][3], then the lengths [n]; ok[n]
+// and end[n][3] receive success and end point. A query outside the +-2^30
+// index box sets kErrCoordRange.
+__device__ __forceinline__ void trace_query(const double* __restrict__ q, uint32_t n, uint32_t i, double o[3],
+                                            double d[3], double& len)
+{
+  const double* dq = q + 3 * static_cast<size_t>(n);
+  for (int a = 0; a < 3; ++a)
+  {
+    o[a] = q[3 * static_cast<size_t>(i) + a];
+    d[a] = dq[3 * static_cast<size_t>(i) + a];
+  }
+  len = q[6 * static_cast<size_t>(n) + i];
+}
+
+__device__ __forceinline__ void trace_answer(unsigned char* ok, double* end, uint32_t i, bool success,
+                                             const double e[3])
+{
+  ok[i] = success ? 1 : 0;
+  for (int a = 0; a < 3; ++a) end[3 * static_cast<size_t>(i) + a] = e[a];
+}
+
+__global__ void __launch_bounds__(128) k_trace_spans(const double* __restrict__ q, uint32_t n, double res,
+                                                     double inv_res, MapView m, TopoView tv,
+                                                     const uint32_t* __restrict__ flags,
+                                                     unsigned char* __restrict__ ok, double* __restrict__ end,
+                                                     SpanBuf sb)
 {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -1928,20 +1956,65 @@ __global__ void __launch_bounds__(128) k_raytrace(const double* __restrict__ q, 
     atomicOr(&m.st->error, kErrTopoFull);
     return;
   }
-  const double o[3] = {q[3 * static_cast<size_t>(i)], q[3 * static_cast<size_t>(i) + 1], q[3 * static_cast<size_t>(i) + 2]};
-  const double* dq  = q + 3 * static_cast<size_t>(n);
-  const double d[3] = {dq[3 * static_cast<size_t>(i)], dq[3 * static_cast<size_t>(i) + 1], dq[3 * static_cast<size_t>(i) + 2]};
-  const double len  = q[6 * static_cast<size_t>(n) + i];
+  double o[3], d[3], len;
+  trace_query(q, n, i, o, d, len);
+  const double zero[3] = {0.0, 0.0, 0.0};
+  double oi[3], di[3];
+  if (!hdda::trace_ray(o, d, len, inv_res, oi, di))
+  {
+    atomicOr(&m.st->error, kErrCoordRange);
+    trace_answer(ok, end, i, false, zero);
+    return;
+  }
   DevTopo topo{tv, m, flags, 0x7fffffff, 0, 0, -1};
-  ActiveCache act{&m, active, tv.map, 0x7fffffff, 0, 0, -1, -1, -1, 0ull};
-  bool success   = false;
-  double e[3]    = {0.0, 0.0, 0.0};
+  hdda::Span sp{-1.0, -1.0};
+  bool found     = false;
   uint32_t steps = 0;
-  const int st   = hdda::raytrace_one(o, d, len, res, inv_res, topo_box(tv), topo, act, success, e, steps);
-  if (st == hdda::kTraceRange) atomicOr(&m.st->error, kErrCoordRange);
-  if (st == hdda::kTraceBound) atomicOr(&m.st->error, kErrStepBound);
-  ok[i] = success ? 1 : 0;
-  for (int a = 0; a < 3; ++a) end[3 * static_cast<size_t>(i) + a] = e[a];
+  if (hdda::trace_span(oi, di, topo_box(tv), topo, sp, found, steps) == hdda::kTraceBound)
+  {
+    atomicOr(&m.st->error, kErrStepBound);
+    trace_answer(ok, end, i, false, zero);
+    return;
+  }
+  if (!found)
+  {
+    double e[3];
+    hdda::trace_miss(oi, di, res, e);
+    trace_answer(ok, end, i, false, e);
+    return;
+  }
+  // (an estimate, for ordering only)
+  const double l1  = fabs(di[0]) + fabs(di[1]) + fabs(di[2]);
+  const double est = fmin((sp.t1 - sp.t0) * l1 + 2.0, 2147483647.0);
+  const int cls    = 31 - __clz(max(1, static_cast<int>(est)));
+  const uint32_t k = atomicAdd(sb.count, 1u);
+  if (k < sb.cap) sb.rec[k] = SpanRec{sp.t0, sp.t1, static_cast<int>(i), cls, steps, 0u};
+}
+
+__global__ void __launch_bounds__(128) k_trace_walk(const double* __restrict__ q, uint32_t n, double res,
+                                                    double inv_res, MapView m, TopoView tv,
+                                                    const unsigned long long* __restrict__ active,
+                                                    unsigned char* __restrict__ ok, double* __restrict__ end,
+                                                    const SpanRec* __restrict__ rec, uint32_t n_spans)
+{
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_spans) return;
+  const SpanRec r  = rec[j];
+  const uint32_t i = static_cast<uint32_t>(r.ray);
+  double o[3], d[3], len;
+  trace_query(q, n, i, o, d, len);
+  double oi[3], di[3];
+  hdda::trace_ray(o, d, len, inv_res, oi, di);  // in range: its span was found
+  ActiveCache act{&m, active, tv.map, 0x7fffffff, 0, 0, -1, -1, -1, 0ull};
+  uint32_t steps = r.steps;
+  double e[3]    = {0.0, 0.0, 0.0};
+  const bool done = hdda::trace_walk(oi, di, hdda::Span{r.t0, r.t1}, res, act, e, steps) == hdda::kTraceOk;
+  if (!done)
+  {
+    atomicOr(&m.st->error, kErrStepBound);
+    e[0] = e[1] = e[2] = 0.0;
+  }
+  trace_answer(ok, end, i, done, e);
 }
 
 // ---------------------------------------------------------------------------

@@ -1342,6 +1342,22 @@ int build_topology(vdbg_map* m, int map, cudaStream_t s, TopoView* tv)
   return VDBG_OK;
 }
 
+// Span records of fast mode and raytrace (with their sort's histogram and
+// the two counters) for at least `want` spans.
+int ensure_span_buffers(vdbg_map* m, uint32_t want)
+{
+  if (!m->fast_ctr) VDBG_TRY(dev_alloc(m, &m->fast_ctr, 2));
+  if (!m->fast_hist) VDBG_TRY(dev_alloc(m, &m->fast_hist, kSpanClasses));
+  if (want <= m->fast_cap) return VDBG_OK;
+  dev_free(m, m->fast_spans, m->fast_cap);
+  dev_free(m, m->fast_sorted, m->fast_cap);
+  m->fast_cap = 0;
+  VDBG_TRY(dev_alloc(m, &m->fast_spans, want));
+  VDBG_TRY(dev_alloc(m, &m->fast_sorted, want));
+  m->fast_cap = want;
+  return VDBG_OK;
+}
+
 // Fast mode (raycastPointCloud VDBMapping.hpp:520-526 with
 // castRayIntoGridFast :577-602) for the rays of the call, into channel `c`:
 // the intersector, the marks of the active voxels along its spans, then the
@@ -1358,20 +1374,11 @@ int run_fast_marking(vdbg_map* m, Channel& c, const int4* rays, const int* order
   m->timings.launches += 1;
   // Phase 1: the spans of every ray (repeated with a larger buffer if they
   // did not fit; the walk writes nothing but the records and counters).
-  if (!m->fast_ctr) VDBG_TRY(dev_alloc(m, &m->fast_ctr, 2));
   uint32_t want = std::max<uint32_t>(m->fast_cap, static_cast<uint32_t>(std::min<int64_t>(4 * n, 1 << 30)));
   uint32_t spans = 0;
   for (int round = 0; round < 3; ++round)
   {
-    if (want > m->fast_cap)
-    {
-      dev_free(m, m->fast_spans, m->fast_cap);
-      dev_free(m, m->fast_sorted, m->fast_cap);
-      m->fast_cap = 0;
-      VDBG_TRY(dev_alloc(m, &m->fast_spans, want));
-      VDBG_TRY(dev_alloc(m, &m->fast_sorted, want));
-      m->fast_cap = want;
-    }
+    VDBG_TRY(ensure_span_buffers(m, want));
     VDBG_CUDA(cudaMemsetAsync(m->fast_ctr, 0, 2 * sizeof(unsigned long long), s));
     SpanBuf sb{m->fast_spans, m->fast_cap, reinterpret_cast<uint32_t*>(m->fast_ctr), m->fast_ctr + 1};
     k_fast_spans<<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(rays, order, t, map_view(m), tv, m->flags,
@@ -1387,7 +1394,6 @@ int run_fast_marking(vdbg_map* m, Channel& c, const int4* rays, const int* order
   // Phase 2: the voxel walks over the spans, longest first.
   if (spans > 0)
   {
-    if (!m->fast_hist) VDBG_TRY(dev_alloc(m, &m->fast_hist, kSpanClasses));
     VDBG_CUDA(cudaMemsetAsync(m->fast_hist, 0, kSpanClasses * sizeof(uint32_t), s));
     const unsigned sblocks = (spans + 255) / 256;
     k_span_hist<<<std::min<unsigned>(sblocks, static_cast<unsigned>(m->num_sms) * 4u), 256, 0, s>>>(
@@ -3015,14 +3021,12 @@ int vdbg_raytrace(vdbg_map* m, int map, int64_t n, const double* origins, const 
   if (bytes > m->trace_bytes)
   {
     dev_free(m, m->d_trace, m->trace_bytes);
-  dev_free(m, m->fast_spans, m->fast_cap);
-  dev_free(m, m->fast_sorted, m->fast_cap);
-  dev_free(m, m->fast_hist, kSpanClasses);
-  dev_free(m, m->fast_ctr, 2);
     m->trace_bytes = 0;
     VDBG_TRY(dev_alloc(m, &m->d_trace, bytes));
     m->trace_bytes = bytes;
   }
+  // Span records (shared with fast mode): one per query at most.
+  VDBG_TRY(ensure_span_buffers(m, static_cast<uint32_t>(nn)));
   double* q         = reinterpret_cast<double*>(m->d_trace);
   double* end       = q + 7 * nn;
   unsigned char* ok = reinterpret_cast<unsigned char*>(q + 10 * nn);
@@ -3034,12 +3038,31 @@ int vdbg_raytrace(vdbg_map* m, int map, int64_t n, const double* origins, const 
   VDBG_CUDA(cudaEventRecord(m->ev_prep, s));  // timings: prep = copies in + intersector, dda = queries
   m->timed_prep     = true;
   const MapConf& mc = m->conf[mp];
-  k_raytrace<<<static_cast<unsigned>((nn + 127) / 128), 128, 0, s>>>(q, static_cast<uint32_t>(nn), mc.resolution,
-                                                                     mc.inv_res, map_view(m), tv, m->flags,
-                                                                     m->active, ok, end);
+  const uint32_t n32 = static_cast<uint32_t>(nn);
+  VDBG_CUDA(cudaMemsetAsync(m->fast_ctr, 0, 2 * sizeof(unsigned long long), s));
+  const SpanBuf sb{m->fast_spans, m->fast_cap, reinterpret_cast<uint32_t*>(m->fast_ctr), m->fast_ctr + 1};
+  k_trace_spans<<<(n32 + 127) / 128, 128, 0, s>>>(q, n32, mc.resolution, mc.inv_res, map_view(m), tv, m->flags, ok,
+                                                 end, sb);
   VDBG_CUDA(cudaGetLastError());
-  VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
+  uint32_t spans = 0;
+  VDBG_CUDA(cudaMemcpyAsync(&spans, m->fast_ctr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  VDBG_CUDA(cudaStreamSynchronize(s));
   m->timings.launches += 1;
+  if (spans > 0)
+  {
+    spans = std::min(spans, m->fast_cap);
+    VDBG_CUDA(cudaMemsetAsync(m->fast_hist, 0, kSpanClasses * sizeof(uint32_t), s));
+    const unsigned sblocks = (spans + 255) / 256;
+    k_span_hist<<<std::min<unsigned>(sblocks, static_cast<unsigned>(m->num_sms) * 4u), 256, 0, s>>>(
+      m->fast_spans, spans, m->fast_hist);
+    k_span_offsets<<<1, 32, 0, s>>>(m->fast_hist);
+    k_span_scatter<<<sblocks, 256, 0, s>>>(m->fast_spans, spans, m->fast_hist, m->fast_sorted);
+    k_trace_walk<<<(spans + 127) / 128, 128, 0, s>>>(q, n32, mc.resolution, mc.inv_res, map_view(m), tv, m->active,
+                                                    ok, end, m->fast_sorted, spans);
+    VDBG_CUDA(cudaGetLastError());
+    m->timings.launches += 4;
+  }
+  VDBG_CUDA(cudaEventRecord(m->ev_dda, s));
   VDBG_CUDA(cudaMemcpyAsync(end_points, end, 3 * nn * sizeof(double), cudaMemcpyDeviceToHost, s));
   VDBG_CUDA(cudaMemcpyAsync(successes, ok, nn, cudaMemcpyDeviceToHost, s));
   VDBG_TRY(fetch_status(m, s));
