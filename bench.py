@@ -924,16 +924,17 @@ def run_raytrace(args):
     wall, kern, intersector = [], [], []
     launches = 0
     ok = None
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ok, ends = m.raytrace(org, d, ln)
-        wall.append(time.perf_counter() - t0)
-        t = m.timings()
-        kern.append(t["dda_ms"] / 1000.0)
-        intersector.append(t["prep_ms"] / 1000.0)
-        launches += t["launches"]
+    with ProfileRange(args.profile_range):
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ok, ends = m.raytrace(org, d, ln)
+            wall.append(time.perf_counter() - t0)
+            t = m.timings()
+            kern.append(t["dda_ms"] / 1000.0)
+            intersector.append(t["prep_ms"] / 1000.0)
+            launches += t["launches"]
     clk = clocks.stop()
     hbm_peak, peak_kind = measured_peaks()
     per_query = 7 * 8 + 3 * 8 + 1  # query in, end point and flag out

@@ -135,6 +135,29 @@ def test_fast_mode_matches_oracle(vdbg, oracle):
             assert sg[key] == o.last_stats[key], (k, key, sg[key], o.last_stats[key])
 
 
+def test_raytrace_and_fast_mode_share_span_buffers(vdbg, oracle):
+    """Fast mode and raytrace keep their span records in the same device
+    buffers: fast inserts, raytraces that grow the query buffer and the span
+    buffers, then fast inserts again, all equal to the oracle."""
+    wl, g, o = built_pair(vdbg, oracle)
+    cfg = fast_config(wl)
+    g.setConfig(cfg)
+    o.setConfig(cfg)
+    step = 0
+    for n in (256, 16384, 65536):
+        pts, org = wl.scan(3 + step % 3)
+        g.insertPointCloud(pts[::8], org, "s")
+        o.insertPointCloud(pts[::8], org, "s")
+        assert_same_map(g.exportLeaves(), o.exportLeaves(), f"fast insert before {n} queries")
+        q_org, d, ln = queries(wl, n, 11 + step)
+        same_trace(g.raytrace(q_org, d, ln), o.raytrace(q_org, d, ln), f"{n} queries")
+        step += 1
+    pts, org = wl.scan(1)
+    g.insertPointCloud(pts, org, "s")
+    o.insertPointCloud(pts, org, "s")
+    assert_same_map(g.exportLeaves(), o.exportLeaves(), "fast insert after the queries")
+
+
 def test_fast_mode_from_an_empty_map(vdbg, oracle):
     wl = W.get("small")
     cfg = fast_config(wl)

@@ -1540,6 +1540,7 @@ struct TopoView
   int* box;                  // [6] min xyz, max xyz (inclusive) of the leaves with an active voxel
   uint32_t* count;           // [0] the map's leaves, [1] nonzero when an insert failed
   int map;
+  unsigned long long* leafbits;  // [blocks][8]: bit `cell` of block b set when the leaf there is in the map
 };
 
 __device__ __forceinline__ bool topo_insert(unsigned long long* keys, uint32_t mask, unsigned long long key)
@@ -1581,12 +1582,15 @@ __global__ void k_topo_init(TopoView tv)
   if (threadIdx.x < 2) tv.count[threadIdx.x] = 0u;
 }
 
+__device__ __forceinline__ int find_block(const MapView& m, int map, int bx, int by, int bz);
+
 // One thread per leaf slot: the integrated leaves of map tv.map enter the node
-// sets; those with an active voxel widen the box.
+// sets and their block's leaf bitmap; those with an active voxel widen the
+// box.
 __global__ void __launch_bounds__(256) k_topo_build(const int4* __restrict__ origin,
                                                     const uint32_t* __restrict__ flags,
                                                     const unsigned long long* __restrict__ active, uint32_t n,
-                                                    TopoView tv)
+                                                    MapView m, TopoView tv)
 {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || flags[i] == 0u) return;
@@ -1595,7 +1599,13 @@ __global__ void __launch_bounds__(256) k_topo_build(const int4* __restrict__ ori
   atomicAdd(tv.count, 1u);
   const bool ok = topo_insert(tv.key1, tv.mask, pack_leaf_key(tv.map, o.x >> 7, o.y >> 7, o.z >> 7)) &&
                   topo_insert(tv.key2, tv.mask, pack_leaf_key(tv.map, o.x >> 12, o.y >> 12, o.z >> 12));
-  if (!ok) atomicOr(tv.count + 1, 1u);
+  const int b = find_block(m, tv.map, o.x >> 6, o.y >> 6, o.z >> 6);
+  if (!ok || b < 0) atomicOr(tv.count + 1, 1u);
+  if (b >= 0)
+  {
+    const int cell = (((o.x >> 3) & 7) << 6) | (((o.y >> 3) & 7) << 3) | ((o.z >> 3) & 7);
+    atomicOr(tv.leafbits + static_cast<size_t>(b) * 8 + (cell >> 6), 1ull << (cell & 63));
+  }
   unsigned long long any = 0ull;
   for (int w = 0; w < 8; ++w) any |= active[static_cast<size_t>(i) * 8 + w];
   if (!any) return;
@@ -1643,6 +1653,8 @@ struct DevTopo
   MapView m;
   const uint32_t* flags;
   mutable int cbx, cby, cbz, cb;  // last block coordinate and its index (-1: none)
+  mutable int cw = -1;            // word of cb's leaf bitmap held in `bits` (-1: none)
+  mutable unsigned long long bits = 0ull;
   __device__ __forceinline__ bool has2(const int v[3]) const
   {
     return voxel_in_map_range(v) && topo_find(tv.key2, tv.mask, pack_leaf_key(tv.map, v[0] >> 12, v[1] >> 12, v[2] >> 12));
@@ -1661,11 +1673,16 @@ struct DevTopo
       cby = by;
       cbz = bz;
       cb  = find_block(m, tv.map, bx, by, bz);
+      cw  = -1;
     }
     if (cb < 0) return false;
     const int cell = (((v[0] >> 3) & 7) << 6) | (((v[1] >> 3) & 7) << 3) | ((v[2] >> 3) & 7);
-    const int slot = m.bleaf[static_cast<size_t>(cb) * 512 + cell];
-    return slot >= 0 && flags[slot] != 0u;
+    if ((cell >> 6) != cw)
+    {
+      cw   = cell >> 6;
+      bits = tv.leafbits[static_cast<size_t>(cb) * 8 + cw];
+    }
+    return (bits >> (cell & 63)) & 1ull;
   }
 };
 
