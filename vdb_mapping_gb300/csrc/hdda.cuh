@@ -316,12 +316,12 @@ VDBG_HD double dda_exit(const Dda& d)
   return m;
 }
 
-// True when ray(t) lies inside the +-2^30 index box (NaN fails).
-VDBG_HD bool start_ok(const Ray& r, double t)
+// True when eye + dir * t lies inside the +-2^30 index box (NaN fails).
+VDBG_HD bool point_ok(const double eye[3], const double dir[3], double t)
 {
   for (int a = 0; a < 3; ++a)
   {
-    const double p = add(r.eye[a], mul(r.dir[a], t));
+    const double p = add(eye[a], mul(dir[a], t));
     if (!(p > -kCoordLimit && p < kCoordLimit)) return false;
   }
   return true;
@@ -485,8 +485,7 @@ VDBG_HD bool trace_ray(const double o[3], const double dir[3], double len, doubl
     oi[a] = mul(o[a], inv_res);
     di[a] = mul(d[a], inv_res);
   }
-  const Ray r = make_ray(oi, di, 0.0, 1.0);
-  return start_ok(r, 0.0) && start_ok(r, 1.0);
+  return point_ok(oi, di, 0.0) && point_ok(oi, di, 1.0);
 }
 
 // The first span of the query's ray clipped by the box (march).

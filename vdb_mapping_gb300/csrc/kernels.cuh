@@ -1960,14 +1960,115 @@ __device__ __forceinline__ void trace_answer(unsigned char* ok, double* end, uin
   for (int a = 0; a < 3; ++a) end[3 * static_cast<size_t>(i) + a] = e[a];
 }
 
+// The queries' order for the span phase: by a coarse origin region and the
+// direction cell of ray_bucket's cube map (face, 13 x 13), so that the lanes
+// of a warp walk neighbouring rays through the same nodes, and take about as
+// many steps (the answers do not depend on the order). A counting sort: bin
+// histogram, exclusive scan, scatter.
+constexpr int kTraceRegions = 8;
+constexpr int kTraceBins    = kTraceRegions * kDirCells;
+
+__device__ __forceinline__ int trace_bin(const double* __restrict__ q, uint32_t n, uint32_t i, double inv_res)
+{
+  const double* dq = q + 3 * static_cast<size_t>(n);
+  const float dx = static_cast<float>(dq[3 * static_cast<size_t>(i)]);
+  const float dy = static_cast<float>(dq[3 * static_cast<size_t>(i) + 1]);
+  const float dz = static_cast<float>(dq[3 * static_cast<size_t>(i) + 2]);
+  const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+  int face;
+  float u, v, mx;
+  if (ax >= ay && ax >= az)
+  {
+    face = dx >= 0.f ? 0 : 1;
+    u    = dy;
+    v    = dz;
+    mx   = ax;
+  }
+  else if (ay >= az)
+  {
+    face = dy >= 0.f ? 2 : 3;
+    u    = dx;
+    v    = dz;
+    mx   = ay;
+  }
+  else
+  {
+    face = dz >= 0.f ? 4 : 5;
+    u    = dx;
+    v    = dy;
+    mx   = az;
+  }
+  int cell = 0;
+  if (mx > 0.f)  // (a zero or NaN direction takes cell 0)
+  {
+    const int iu = min(12, max(0, static_cast<int>((u / mx + 1.f) * 6.5f)));
+    const int iv = min(12, max(0, static_cast<int>((v / mx + 1.f) * 6.5f)));
+    cell         = face * 169 + iv * 13 + iu;
+  }
+  // origin region: 256-voxel cells, hashed
+  long long c[3];
+  for (int a = 0; a < 3; ++a)
+  {
+    const double x = q[3 * static_cast<size_t>(i) + a] * inv_res;
+    c[a]           = (x > -1e15 && x < 1e15) ? static_cast<long long>(floor(x)) >> 8 : 0;
+  }
+  const unsigned long long h = mix64(static_cast<unsigned long long>(c[0]) * 73856093ull ^
+                                     static_cast<unsigned long long>(c[1]) * 19349663ull ^
+                                     static_cast<unsigned long long>(c[2]) * 83492791ull);
+  return static_cast<int>(h % kTraceRegions) * kDirCells + cell;
+}
+
+__global__ void __launch_bounds__(256) k_trace_bin(const double* __restrict__ q, uint32_t n, double inv_res,
+                                                   unsigned short* __restrict__ bin, uint32_t* __restrict__ hist)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b      = i < n ? trace_bin(q, n, i, inv_res) : -1;
+  const unsigned peers = __match_any_sync(0xffffffffu, b);
+  if (i < n)
+  {
+    bin[i] = static_cast<unsigned short>(b);
+    if ((__ffs(peers) - 1) == static_cast<int>(threadIdx.x & 31)) atomicAdd(hist + b, static_cast<uint32_t>(__popc(peers)));
+  }
+}
+
+// One block of 1024 threads: hist[] (kTraceBins) becomes the first position of each bin.
+__global__ void __launch_bounds__(1024) k_trace_offsets(uint32_t* __restrict__ hist)
+{
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < static_cast<uint32_t>(kTraceBins); base += 1024u)
+  {
+    const uint32_t b = base + threadIdx.x;
+    const uint32_t v = b < static_cast<uint32_t>(kTraceBins) ? hist[b] : 0u;
+    uint32_t total   = 0;
+    const uint32_t e = block_scan_exclusive(v, &total);
+    if (b < static_cast<uint32_t>(kTraceBins)) hist[b] = carry + e;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_trace_scatter(const unsigned short* __restrict__ bin, uint32_t n,
+                                                       uint32_t* __restrict__ cursor, uint32_t* __restrict__ order)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b      = i < n ? static_cast<int>(bin[i]) : -1;
+  const unsigned peers = __match_any_sync(0xffffffffu, b);
+  const int leader     = __ffs(peers) - 1;
+  uint32_t base        = 0;
+  if (i < n && static_cast<int>(threadIdx.x & 31) == leader) base = atomicAdd(cursor + b, static_cast<uint32_t>(__popc(peers)));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (i < n) order[base + static_cast<uint32_t>(__popc(peers & lanemask_lt()))] = i;
+}
+
 __global__ void __launch_bounds__(128) k_trace_spans(const double* __restrict__ q, uint32_t n, double res,
                                                      double inv_res, MapView m, TopoView tv,
                                                      const uint32_t* __restrict__ flags,
+                                                     const uint32_t* __restrict__ order,
                                                      unsigned char* __restrict__ ok, double* __restrict__ end,
                                                      SpanBuf sb)
 {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const uint32_t i = order[j];
   if (tv.count[1] != 0u)
   {
     atomicOr(&m.st->error, kErrTopoFull);

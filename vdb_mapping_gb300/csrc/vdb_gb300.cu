@@ -3026,7 +3026,11 @@ int vdbg_raytrace(vdbg_map* m, int map, int64_t n, const double* origins, const 
   cudaStream_t s = m->stream;
   VDBG_TRY(begin_call(m, s));
   const size_t nn    = static_cast<size_t>(n);
-  const size_t bytes = nn * 10 * sizeof(double) + ((nn + 15) & ~static_cast<size_t>(15));
+  // queries (7 doubles) and end points (3), then the order (u32), the bins
+  // (u16), the bin offsets and the success flags
+  const size_t n16   = (nn + 15) & ~static_cast<size_t>(15);
+  const size_t bytes = nn * 10 * sizeof(double) + n16 * (sizeof(uint32_t) + sizeof(unsigned short)) +
+                       kTraceBins * sizeof(uint32_t) + n16;
   if (bytes > m->trace_bytes)
   {
     dev_free(m, m->d_trace, m->trace_bytes);
@@ -3036,9 +3040,12 @@ int vdbg_raytrace(vdbg_map* m, int map, int64_t n, const double* origins, const 
   }
   // Span records (shared with fast mode): one per query at most.
   VDBG_TRY(ensure_span_buffers(m, static_cast<uint32_t>(nn)));
-  double* q         = reinterpret_cast<double*>(m->d_trace);
-  double* end       = q + 7 * nn;
-  unsigned char* ok = reinterpret_cast<unsigned char*>(q + 10 * nn);
+  double* q              = reinterpret_cast<double*>(m->d_trace);
+  double* end            = q + 7 * nn;
+  uint32_t* order        = reinterpret_cast<uint32_t*>(q + 10 * nn);
+  unsigned short* bins   = reinterpret_cast<unsigned short*>(order + n16);
+  uint32_t* bin_hist     = reinterpret_cast<uint32_t*>(bins + n16);
+  unsigned char* ok      = reinterpret_cast<unsigned char*>(bin_hist + kTraceBins);
   VDBG_CUDA(cudaMemcpyAsync(q, origins, 3 * nn * sizeof(double), cudaMemcpyHostToDevice, s));
   VDBG_CUDA(cudaMemcpyAsync(q + 3 * nn, directions, 3 * nn * sizeof(double), cudaMemcpyHostToDevice, s));
   VDBG_CUDA(cudaMemcpyAsync(q + 6 * nn, max_lengths, nn * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -3049,14 +3056,18 @@ int vdbg_raytrace(vdbg_map* m, int map, int64_t n, const double* origins, const 
   const MapConf& mc = m->conf[mp];
   const uint32_t n32 = static_cast<uint32_t>(nn);
   VDBG_CUDA(cudaMemsetAsync(m->fast_ctr, 0, 2 * sizeof(unsigned long long), s));
+  VDBG_CUDA(cudaMemsetAsync(bin_hist, 0, kTraceBins * sizeof(uint32_t), s));
+  k_trace_bin<<<(n32 + 255) / 256, 256, 0, s>>>(q, n32, mc.inv_res, bins, bin_hist);
+  k_trace_offsets<<<1, 1024, 0, s>>>(bin_hist);
+  k_trace_scatter<<<(n32 + 255) / 256, 256, 0, s>>>(bins, n32, bin_hist, order);
   const SpanBuf sb{m->fast_spans, m->fast_cap, reinterpret_cast<uint32_t*>(m->fast_ctr), m->fast_ctr + 1};
-  k_trace_spans<<<(n32 + 127) / 128, 128, 0, s>>>(q, n32, mc.resolution, mc.inv_res, map_view(m), tv, m->flags, ok,
-                                                 end, sb);
+  k_trace_spans<<<(n32 + 127) / 128, 128, 0, s>>>(q, n32, mc.resolution, mc.inv_res, map_view(m), tv, m->flags,
+                                                 order, ok, end, sb);
   VDBG_CUDA(cudaGetLastError());
   uint32_t spans = 0;
   VDBG_CUDA(cudaMemcpyAsync(&spans, m->fast_ctr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   VDBG_CUDA(cudaStreamSynchronize(s));
-  m->timings.launches += 1;
+  m->timings.launches += 4;
   if (spans > 0)
   {
     spans = std::min(spans, m->fast_cap);
