@@ -123,6 +123,48 @@ VDBG_HD Ray make_ray(const double eye[3], const double dir[3], double t0, double
   return r;
 }
 
+VDBG_HD long long dbits(double x)
+{
+#ifdef __CUDA_ARCH__
+  return __double_as_longlong(x);
+#else
+  long long b;
+  std::memcpy(&b, &x, sizeof(b));
+  return b;
+#endif
+}
+VDBG_HD double bits_double(long long b)
+{
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(b);
+#else
+  double x;
+  std::memcpy(&x, &b, sizeof(x));
+  return x;
+#endif
+}
+
+// The tests DDA::init makes of an axis, on the bit patterns (integer
+// compares, off the narrow FP64 pipe): dir == 0.0 (either zero), and
+// inv > 0.0 (sign clear, not zero, not NaN).
+VDBG_HD bool is_zero(double x) { return (dbits(x) & 0x7fffffffffffffffll) == 0; }
+VDBG_HD bool is_positive(double x)
+{
+  const long long b = dbits(x);
+  return b > 0 && b <= 0x7ff0000000000000ll;
+}
+
+// step * inv for step = +-2^log2 of inv's sign: |inv| * 2^log2, which is
+// exact, formed on the exponent field (off the narrow FP64 pipe) when |inv|
+// is a normal number that stays finite; otherwise the product itself.
+VDBG_HD double pow2_delta(double inv, int step, int log2)
+{
+  const long long b = dbits(inv) & 0x7fffffffffffffffll;
+  const long long e = b >> 52;
+  if (e > 0 && e + log2 < 2047) return bits_double(b + (static_cast<long long>(log2) << 52));
+  return mul(static_cast<double>(step), inv);
+}
+
 struct Span
 {
   double t0, t1;
@@ -206,23 +248,23 @@ VDBG_HD void dda_init(Dda& d, const Ray& r, double t0, double t1, int log2)
   }
   for (int a = 0; a < 3; ++a)
   {
-    if (r.dir[a] == 0.0)
+    if (is_zero(r.dir[a]))
     {
       d.step[a]  = 0;
       d.next[a]  = kDblMax;
       d.delta[a] = kDblMax;
     }
-    else if (r.inv[a] > 0.0)
+    else if (is_positive(r.inv[a]))
     {
       d.step[a]  = dim;
       d.next[a]  = add(t0, mul(sub(static_cast<double>(d.voxel[a] + dim), pos[a]), r.inv[a]));
-      d.delta[a] = mul(static_cast<double>(d.step[a]), r.inv[a]);
+      d.delta[a] = pow2_delta(r.inv[a], d.step[a], log2);
     }
     else
     {
       d.step[a]  = -dim;
       d.next[a]  = add(t0, mul(sub(static_cast<double>(d.voxel[a]), pos[a]), r.inv[a]));
-      d.delta[a] = mul(static_cast<double>(d.step[a]), r.inv[a]);
+      d.delta[a] = pow2_delta(r.inv[a], d.step[a], log2);
     }
   }
 }
