@@ -355,6 +355,16 @@ int vdbg_add_artificial_walls(vdbg_map* map, int64_t n, const double* starts, co
                               double negative_height, double positive_height);
 int vdbg_restore_map_integrity(vdbg_map* map);
 
+/* Test hook for the bounded device waits (no counterpart in the reference).
+ * Leaves the empty cell of leaf (lx, ly, lz) (voxel coordinates / 8) of the
+ * map (map_index -1) or map `map_index` of a batch pending, as if a thread
+ * had claimed it and never published its slot. The next call whose rays
+ * reach that leaf waits for the slot up to the wait's bound (about a
+ * second), then returns VDBG_ERR_TIMEOUT with its marking discarded; the
+ * map and the context stay usable, and vdbg_reset_map clears the cell.
+ * VDBG_ERR_INVALID_ARGUMENT when the leaf exists. */
+int vdbg_test_stall_leaf(vdbg_map* map, int map_index, int32_t lx, int32_t ly, int32_t lz);
+
 /* Morphology of a map section's active voxels with the 26-neighbourhood:
  * openvdb::tools::dilateActiveValues / erodeActiveValues with
  * NN_FACE_EDGE_VERTEX as VDBMapping.hpp:1094-1147 calls them

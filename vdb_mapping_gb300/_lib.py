@@ -221,6 +221,7 @@ SIGNATURES = [
     ("vdbg_raytrace", C.c_int, [_P, C.c_int, C.c_int64, _P, _P, _P, _P, _P]),
     ("vdbg_add_artificial_walls", C.c_int, [_P, C.c_int64, _P, _P, C.c_double, C.c_double]),
     ("vdbg_restore_map_integrity", C.c_int, [_P]),
+    ("vdbg_test_stall_leaf", C.c_int, [_P, C.c_int, C.c_int32, C.c_int32, C.c_int32]),
     ("vdbg_section_morphology", C.c_int, [_P, C.c_int, C.c_int, C.c_int64, _P, _P, C.c_int64, _P, _P,
                                           C.POINTER(C.c_int64)]),
     ("vdbg_batch_use_graph", C.c_int, [_P, C.c_int]),

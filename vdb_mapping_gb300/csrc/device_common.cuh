@@ -437,7 +437,8 @@ __device__ __forceinline__ int find_or_insert_block(const MapView& m, int map, i
       uint32_t spins = 0;
       while (s == kSlotPending)
       {
-        if (++spins > kSpinLimit)
+        // (a wait that another thread already gave up on ends here too)
+        if (++spins > kSpinLimit || ((spins & 1023u) == 0u && (ld_relaxed_u32(&m.st->error) & kErrSpin)))
         {
           atomicOr(&m.st->error, kErrSpin);
           return kSlotFailed;
@@ -489,7 +490,8 @@ __device__ __forceinline__ int find_or_insert_leaf(const MapView& m, int b, int 
   uint32_t spins = 0;
   while (s == kLeafPending)
   {
-    if (++spins > kSpinLimit)
+    // (a wait that another thread already gave up on ends here too)
+    if (++spins > kSpinLimit || ((spins & 1023u) == 0u && (ld_relaxed_u32(&m.st->error) & kErrSpin)))
     {
       atomicOr(&m.st->error, kErrSpin);
       return kSlotFailed;

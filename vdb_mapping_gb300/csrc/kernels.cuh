@@ -1223,6 +1223,22 @@ __global__ void __launch_bounds__(256) k_compact(MapView m, ChannelView c, DevSt
   }
 }
 
+// Test hook for the bounded waits: the empty cell of leaf (lx, ly, lz) of
+// `map` is left pending, as if a thread had claimed it and never published
+// its slot. *out: 0 planted, 1 the cell was not empty, 2 no block.
+__global__ void k_test_stall_leaf(MapView m, int map, int lx, int ly, int lz, int* out)
+{
+  const int b = find_or_insert_block(m, map, lx >> 3, ly >> 3, lz >> 3);
+  if (b < 0)
+  {
+    *out = 2;
+    return;
+  }
+  const int cell = ((lx & 7) << 6) | ((ly & 7) << 3) | (lz & 7);
+  const int prev = atomicCAS(m.bleaf + static_cast<size_t>(b) * 512 + cell, kLeafEmpty, kLeafPending);
+  *out           = prev == kLeafEmpty ? 0 : 1;
+}
+
 // Starts a channel's first window: empty lists, epoch 1.
 __global__ void k_window_init(ChannelView c)
 {

@@ -3224,6 +3224,37 @@ int vdbg_export_section(vdbg_map* m, int map, const int32_t lo[3], const int32_t
   return VDBG_OK;
 }
 
+int vdbg_test_stall_leaf(vdbg_map* m, int map, int32_t lx, int32_t ly, int32_t lz)
+{
+  int mp = 0;
+  if (!m || !section_map(m, map, &mp)) return VDBG_ERR_INVALID_ARGUMENT;
+  const int32_t lim = static_cast<int32_t>(kVoxelMaxExcl) / 8;
+  if (lx < -lim || lx >= lim || ly < -lim || ly >= lim || lz < -lim || lz >= lim) return VDBG_ERR_COORD_RANGE;
+  VDBG_TRY(set_device(m));
+  VDBG_CUDA(cudaStreamSynchronize(m->stream));
+  VDBG_TRY(reserve_for(m, 1));
+  cudaStream_t s = m->stream;
+  int* d_out     = nullptr;
+  VDBG_TRY(dev_alloc(m, &d_out, 1));
+  int st = begin_call(m, s);
+  if (st == VDBG_OK)
+  {
+    k_test_stall_leaf<<<1, 1, 0, s>>>(map_view(m), mp, lx, ly, lz, d_out);
+    if (cudaGetLastError() != cudaSuccess) st = VDBG_ERR_CUDA;
+  }
+  int out = 2;
+  if (st == VDBG_OK && cudaMemcpyAsync(&out, d_out, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    st = VDBG_ERR_CUDA;
+  if (st == VDBG_OK) st = fetch_status(m, s);
+  dev_free(m, d_out, 1);
+  VDBG_TRY(st);
+  m->n_blocks = std::min<uint32_t>(m->h_status->n_blocks, m->bcapacity);
+  if (m->h_status->error != 0u) return map_error(m->h_status->error);
+  if (out == 1) return VDBG_ERR_INVALID_ARGUMENT;
+  if (out != 0) return VDBG_ERR_OUT_OF_MEMORY;
+  return VDBG_OK;
+}
+
 int vdbg_apply_section_states(vdbg_map* m, int map, const int32_t lo[3], const int32_t hi[3], int64_t n,
                               const int32_t* origins, const uint64_t* masks)
 {
