@@ -1556,7 +1556,9 @@ struct TopoView
   int* box;                  // [6] min xyz, max xyz (inclusive) of the leaves with an active voxel
   uint32_t* count;           // [0] the map's leaves, [1] nonzero when an insert failed
   int map;
-  unsigned long long* leafbits;  // [blocks][8]: bit `cell` of block b set when the leaf there is in the map
+  // [blocks][16]: words 0-7, bit `cell` set when the leaf in that cell of the
+  // block is in the map; words 8-15, when it also holds an active voxel.
+  unsigned long long* leafbits;
 };
 
 __device__ __forceinline__ bool topo_insert(unsigned long long* keys, uint32_t mask, unsigned long long key)
@@ -1617,14 +1619,12 @@ __global__ void __launch_bounds__(256) k_topo_build(const int4* __restrict__ ori
                   topo_insert(tv.key2, tv.mask, pack_leaf_key(tv.map, o.x >> 12, o.y >> 12, o.z >> 12));
   const int b = find_block(m, tv.map, o.x >> 6, o.y >> 6, o.z >> 6);
   if (!ok || b < 0) atomicOr(tv.count + 1, 1u);
-  if (b >= 0)
-  {
-    const int cell = (((o.x >> 3) & 7) << 6) | (((o.y >> 3) & 7) << 3) | ((o.z >> 3) & 7);
-    atomicOr(tv.leafbits + static_cast<size_t>(b) * 8 + (cell >> 6), 1ull << (cell & 63));
-  }
+  const int cell = (((o.x >> 3) & 7) << 6) | (((o.y >> 3) & 7) << 3) | ((o.z >> 3) & 7);
+  if (b >= 0) atomicOr(tv.leafbits + static_cast<size_t>(b) * 16 + (cell >> 6), 1ull << (cell & 63));
   unsigned long long any = 0ull;
   for (int w = 0; w < 8; ++w) any |= active[static_cast<size_t>(i) * 8 + w];
   if (!any) return;
+  if (b >= 0) atomicOr(tv.leafbits + static_cast<size_t>(b) * 16 + 8 + (cell >> 6), 1ull << (cell & 63));
   atomicMin(tv.box + 0, o.x);
   atomicMin(tv.box + 1, o.y);
   atomicMin(tv.box + 2, o.z);
@@ -1696,7 +1696,7 @@ struct DevTopo
     if ((cell >> 6) != cw)
     {
       cw   = cell >> 6;
-      bits = tv.leafbits[static_cast<size_t>(cb) * 8 + cw];
+      bits = tv.leafbits[static_cast<size_t>(cb) * 16 + cw];
     }
     return (bits >> (cell & 63)) & 1ull;
   }
@@ -1705,7 +1705,11 @@ struct DevTopo
 // isValueOn of the map for voxels along one ray, remembering the last leaf
 // (its block and slot, -1 when absent) and the active word of the z-plane
 // last read (a near-horizontal ray stays in one plane of a leaf for many
-// voxels).
+// voxels). With the intersector's per-block bitmaps (`bits`, TopoView
+// leafbits), a leaf without an active voxel is known from one cached bitmap
+// word, and its slot and active words are not read: a walk through free
+// space does one load per 8 x 8 leaves of a block instead of two dependent
+// ones per leaf.
 struct ActiveCache
 {
   const MapView* m;
@@ -1716,6 +1720,9 @@ struct ActiveCache
   int wz;                   // plane (z & 7) held in `word`, -1 none
   unsigned long long word;  // active bits of plane wz of leaf `slot`
   int bx = 0x7fffffff, by = 0, bz = 0;  // block coordinate `b` was found for
+  const unsigned long long* bits = nullptr;  // TopoView leafbits, or none
+  int aw = -1;                               // word of b's active-leaf bitmap held in `abits`
+  unsigned long long abits = 0ull;
   __device__ __forceinline__ bool operator()(const int v[3])
   {
     const int x = v[0] >> 3, y = v[1] >> 3, z = v[2] >> 3;
@@ -1732,8 +1739,20 @@ struct ActiveCache
         by = y >> 3;
         bz = z >> 3;
         b  = voxel_in_map_range(v) ? find_block(*m, map, bx, by, bz) : -1;
+        aw = -1;
       }
-      slot = b >= 0 ? m->bleaf[static_cast<size_t>(b) * 512 + (((x & 7) << 6) | ((y & 7) << 3) | (z & 7))] : -1;
+      const int cell = ((x & 7) << 6) | ((y & 7) << 3) | (z & 7);
+      bool maybe     = b >= 0;
+      if (maybe && bits)
+      {
+        if ((cell >> 6) != aw)
+        {
+          aw    = cell >> 6;
+          abits = bits[static_cast<size_t>(b) * 16 + 8 + aw];
+        }
+        maybe = (abits >> (cell & 63)) & 1ull;
+      }
+      slot = maybe ? m->bleaf[static_cast<size_t>(b) * 512 + cell] : -1;
       if (slot < 0) slot = -1;
       wz = -1;
     }
@@ -1871,6 +1890,7 @@ __global__ void __launch_bounds__(128) k_fast_walk(const int4* __restrict__ rays
              dda.delta[0], dda.delta[1], dda.delta[2]};
     const long long t1 = hdda::tkey(sp.t1);
     ActiveCache act{&m, active, tv.map, 0x7fffffff, 0, 0, -1, -1, -1, 0ull};
+    act.bits = tv.leafbits;
     uint32_t steps = 0;
     do
     {
@@ -2140,6 +2160,7 @@ __global__ void __launch_bounds__(128) k_trace_walk(const double* __restrict__ q
   double oi[3], di[3];
   hdda::trace_ray(o, d, len, inv_res, oi, di);  // in range: its span was found
   ActiveCache act{&m, active, tv.map, 0x7fffffff, 0, 0, -1, -1, -1, 0ull};
+  act.bits = tv.leafbits;
   uint32_t steps = r.steps;
   double e[3]    = {0.0, 0.0, 0.0};
   const bool done = hdda::trace_walk(oi, di, hdda::Span{r.t0, r.t1}, res, act, e, steps) == hdda::kTraceOk;

@@ -111,9 +111,10 @@ struct vdbg_map
   uint32_t call_leaves  = 0;  // n_leaves / n_blocks when the current call began
   uint32_t call_blocks  = 0;
   vmem::Array vm_values, vm_active, vm_origin, vm_flags, vm_bleaf, vm_borigin, vm_bkeys, vm_bslots;
-  // Per block, which of its 512 leaf cells hold a leaf of the map (8 words),
-  // rebuilt by every intersector call; a block array, so it grows with the
-  // block pool in place.
+  // Per block, which of its 512 leaf cells hold a leaf of the map (8 words)
+  // and which of those hold an active voxel (8 more), rebuilt by every
+  // intersector call; a block array, so it grows with the block pool in
+  // place.
   vmem::Array vm_tbits;
   size_t page           = 0;  // physical page size of the device
   // Growth ahead of need: while a call's kernels run, the pools are extended
@@ -397,7 +398,7 @@ std::vector<SlotArray> block_arrays(vdbg_map* m)
 {
   std::vector<SlotArray> v{{&m->vm_bleaf, 512 * sizeof(int), 0xff},
                            {&m->vm_borigin, sizeof(int4), -1},
-                           {&m->vm_tbits, 8 * sizeof(unsigned long long), -1}};
+                           {&m->vm_tbits, 16 * sizeof(unsigned long long), -1}};
   for (Channel& c : m->channels)
   {
     v.push_back({&c.vm_btouched, 8 * sizeof(unsigned long long), 0});
@@ -1336,7 +1337,7 @@ int build_topology(vdbg_map* m, int map, cudaStream_t s, TopoView* tv)
   if (!m->topo_box) VDBG_TRY(dev_alloc(m, &m->topo_box, 8));
   const size_t blocks = std::min(m->n_blocks, m->bcapacity);
   tv->leafbits        = reinterpret_cast<unsigned long long*>(m->vm_tbits.base);
-  if (blocks > 0) VDBG_CUDA(cudaMemsetAsync(tv->leafbits, 0, blocks * 8 * sizeof(unsigned long long), s));
+  if (blocks > 0) VDBG_CUDA(cudaMemsetAsync(tv->leafbits, 0, blocks * 16 * sizeof(unsigned long long), s));
   tv->key1  = m->topo_keys;
   tv->key2  = m->topo_keys + m->topo_cap;
   tv->mask  = m->topo_cap - 1;
