@@ -1610,27 +1610,52 @@ __global__ void __launch_bounds__(256) k_topo_build(const int4* __restrict__ ori
                                                     const unsigned long long* __restrict__ active, uint32_t n,
                                                     MapView m, TopoView tv)
 {
+  // Whole warps run to the end: the count and the box are reduced over the
+  // warp first, so each warp makes one atomic per counter instead of one per
+  // leaf (the same few words take them from every leaf of the map).
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n || flags[i] == 0u) return;
-  const int4 o = origin[i];
-  if (o.w != tv.map) return;
-  atomicAdd(tv.count, 1u);
-  const bool ok = topo_insert(tv.key1, tv.mask, pack_leaf_key(tv.map, o.x >> 7, o.y >> 7, o.z >> 7)) &&
-                  topo_insert(tv.key2, tv.mask, pack_leaf_key(tv.map, o.x >> 12, o.y >> 12, o.z >> 12));
-  const int b = find_block(m, tv.map, o.x >> 6, o.y >> 6, o.z >> 6);
-  if (!ok || b < 0) atomicOr(tv.count + 1, 1u);
-  const int cell = (((o.x >> 3) & 7) << 6) | (((o.y >> 3) & 7) << 3) | ((o.z >> 3) & 7);
-  if (b >= 0) atomicOr(tv.leafbits + static_cast<size_t>(b) * 16 + (cell >> 6), 1ull << (cell & 63));
-  unsigned long long any = 0ull;
-  for (int w = 0; w < 8; ++w) any |= active[static_cast<size_t>(i) * 8 + w];
-  if (!any) return;
-  if (b >= 0) atomicOr(tv.leafbits + static_cast<size_t>(b) * 16 + 8 + (cell >> 6), 1ull << (cell & 63));
-  atomicMin(tv.box + 0, o.x);
-  atomicMin(tv.box + 1, o.y);
-  atomicMin(tv.box + 2, o.z);
-  atomicMax(tv.box + 3, o.x + 7);
-  atomicMax(tv.box + 4, o.y + 7);
-  atomicMax(tv.box + 5, o.z + 7);
+  const int lane   = static_cast<int>(threadIdx.x & 31);
+  int4 o           = make_int4(0, 0, 0, -1);
+  bool in          = i < n && flags[i] != 0u;
+  if (in)
+  {
+    o  = origin[i];
+    in = o.w == tv.map;
+  }
+  bool act = false;
+  if (in)
+  {
+    const bool ok = topo_insert(tv.key1, tv.mask, pack_leaf_key(tv.map, o.x >> 7, o.y >> 7, o.z >> 7)) &&
+                    topo_insert(tv.key2, tv.mask, pack_leaf_key(tv.map, o.x >> 12, o.y >> 12, o.z >> 12));
+    const int b = find_block(m, tv.map, o.x >> 6, o.y >> 6, o.z >> 6);
+    if (!ok || b < 0) atomicOr(tv.count + 1, 1u);
+    const int cell = (((o.x >> 3) & 7) << 6) | (((o.y >> 3) & 7) << 3) | ((o.z >> 3) & 7);
+    if (b >= 0) atomicOr(tv.leafbits + static_cast<size_t>(b) * 16 + (cell >> 6), 1ull << (cell & 63));
+    unsigned long long any = 0ull;
+    for (int w = 0; w < 8; ++w) any |= active[static_cast<size_t>(i) * 8 + w];
+    act = any != 0ull;
+    if (act && b >= 0) atomicOr(tv.leafbits + static_cast<size_t>(b) * 16 + 8 + (cell >> 6), 1ull << (cell & 63));
+  }
+  const unsigned in_w = __ballot_sync(0xffffffffu, in);
+  if (lane == 0 && in_w) atomicAdd(tv.count, static_cast<uint32_t>(__popc(in_w)));
+  const unsigned act_w = __ballot_sync(0xffffffffu, act);
+  if (!act_w) return;
+  const int big = 0x7fffffff, small = static_cast<int>(0x80000000u);
+  const int x0 = __reduce_min_sync(0xffffffffu, act ? o.x : big);
+  const int y0 = __reduce_min_sync(0xffffffffu, act ? o.y : big);
+  const int z0 = __reduce_min_sync(0xffffffffu, act ? o.z : big);
+  const int x1 = __reduce_max_sync(0xffffffffu, act ? o.x + 7 : small);
+  const int y1 = __reduce_max_sync(0xffffffffu, act ? o.y + 7 : small);
+  const int z1 = __reduce_max_sync(0xffffffffu, act ? o.z + 7 : small);
+  if (lane == 0)
+  {
+    atomicMin(tv.box + 0, x0);
+    atomicMin(tv.box + 1, y0);
+    atomicMin(tv.box + 2, z0);
+    atomicMax(tv.box + 3, x1);
+    atomicMax(tv.box + 4, y1);
+    atomicMax(tv.box + 5, z1);
+  }
 }
 
 __device__ __forceinline__ bool voxel_in_map_range(const int v[3])
