@@ -82,12 +82,13 @@ VDBG_HD double root(double a)
   return std::sqrt(a);
 #endif
 }
-VDBG_HD double flr(double a)
+// (int)floor(a) for |a| < 2^31, in one conversion with rounding down.
+VDBG_HD int flr_int(double a)
 {
 #ifdef __CUDA_ARCH__
-  return ::floor(a);
+  return __double2int_rd(a);
 #else
-  return std::floor(a);
+  return static_cast<int>(std::floor(a));
 #endif
 }
 
@@ -244,7 +245,7 @@ VDBG_HD void dda_init(Dda& d, const Ray& r, double t0, double t1, int log2)
   for (int a = 0; a < 3; ++a)
   {
     pos[a]     = add(r.eye[a], mul(r.dir[a], t0));
-    d.voxel[a] = static_cast<int>(flr(pos[a])) & ~(dim - 1);
+    d.voxel[a] = flr_int(pos[a]) & ~(dim - 1);
   }
   for (int a = 0; a < 3; ++a)
   {

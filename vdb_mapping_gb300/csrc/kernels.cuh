@@ -2024,8 +2024,8 @@ __device__ __forceinline__ void trace_answer(unsigned char* ok, double* end, uin
 // The queries' order for the span phase: by a coarse origin region and the
 // direction cell of ray_bucket's cube map (face, 13 x 13), so that the lanes
 // of a warp walk neighbouring rays through the same nodes, and take about as
-// many steps (the answers do not depend on the order). A counting sort: bin
-// histogram, exclusive scan, scatter.
+// many steps (the answers do not depend on the order, nor on the order within
+// a bin). A counting sort: bin histogram, exclusive scan, scatter.
 constexpr int kTraceRegions = 8;
 constexpr int kTraceBins    = kTraceRegions * kDirCells;
 
@@ -2066,16 +2066,17 @@ __device__ __forceinline__ int trace_bin(const double* __restrict__ q, uint32_t 
     const int iv = min(12, max(0, static_cast<int>((v / mx + 1.f) * 6.5f)));
     cell         = face * 169 + iv * 13 + iu;
   }
-  // origin region: 256-voxel cells, hashed
-  long long c[3];
+  // origin region: 256-voxel cells, hashed (single precision: an ordering key only)
+  int c[3];
+  const float inv = static_cast<float>(inv_res) * (1.f / 256.f);
   for (int a = 0; a < 3; ++a)
   {
-    const double x = q[3 * static_cast<size_t>(i) + a] * inv_res;
-    c[a]           = (x > -1e15 && x < 1e15) ? static_cast<long long>(floor(x)) >> 8 : 0;
+    const float x = static_cast<float>(q[3 * static_cast<size_t>(i) + a]) * inv;
+    c[a]          = (x > -1e9f && x < 1e9f) ? __float2int_rd(x) : 0;
   }
-  const unsigned long long h = mix64(static_cast<unsigned long long>(c[0]) * 73856093ull ^
-                                     static_cast<unsigned long long>(c[1]) * 19349663ull ^
-                                     static_cast<unsigned long long>(c[2]) * 83492791ull);
+  const unsigned long long h = mix64(static_cast<unsigned long long>(static_cast<unsigned>(c[0])) * 73856093ull ^
+                                     static_cast<unsigned long long>(static_cast<unsigned>(c[1])) * 19349663ull ^
+                                     static_cast<unsigned long long>(static_cast<unsigned>(c[2])) * 83492791ull);
   return static_cast<int>(h % kTraceRegions) * kDirCells + cell;
 }
 
@@ -2083,13 +2084,10 @@ __global__ void __launch_bounds__(256) k_trace_bin(const double* __restrict__ q,
                                                    unsigned short* __restrict__ bin, uint32_t* __restrict__ hist)
 {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int b      = i < n ? trace_bin(q, n, i, inv_res) : -1;
-  const unsigned peers = __match_any_sync(0xffffffffu, b);
-  if (i < n)
-  {
-    bin[i] = static_cast<unsigned short>(b);
-    if ((__ffs(peers) - 1) == static_cast<int>(threadIdx.x & 31)) atomicAdd(hist + b, static_cast<uint32_t>(__popc(peers)));
-  }
+  if (i >= n) return;
+  const int b = trace_bin(q, n, i, inv_res);
+  bin[i]      = static_cast<unsigned short>(b);
+  atomicAdd(hist + b, 1u);
 }
 
 // One block of 1024 threads: hist[] (kTraceBins) becomes the first position of each bin.
@@ -2111,13 +2109,8 @@ __global__ void __launch_bounds__(256) k_trace_scatter(const unsigned short* __r
                                                        uint32_t* __restrict__ cursor, uint32_t* __restrict__ order)
 {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int b      = i < n ? static_cast<int>(bin[i]) : -1;
-  const unsigned peers = __match_any_sync(0xffffffffu, b);
-  const int leader     = __ffs(peers) - 1;
-  uint32_t base        = 0;
-  if (i < n && static_cast<int>(threadIdx.x & 31) == leader) base = atomicAdd(cursor + b, static_cast<uint32_t>(__popc(peers)));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (i < n) order[base + static_cast<uint32_t>(__popc(peers & lanemask_lt()))] = i;
+  if (i >= n) return;
+  order[atomicAdd(cursor + bin[i], 1u)] = i;
 }
 
 __global__ void __launch_bounds__(128) k_trace_spans(const double* __restrict__ q, uint32_t n, double res,
