@@ -950,8 +950,10 @@ __global__ void __launch_bounds__(kApplyThreads) k_apply_runs(RunBuffer rb, MapV
       }
     }
     __syncthreads();
-    // The staging buffer is free: start copying the block's next chunk.
-    if (threadIdx.x == 0)
+    // The staging buffer is free: start copying the block's next chunk. The
+    // last thread takes the ticket: it has the fewest (mostly no) leaves to
+    // resolve below, so the ticket's round trips stay off the slowest path.
+    if (threadIdx.x == kApplyThreads - 1)
     {
       fence_proxy_async_smem();
       apply_take(rb, items, t, s_key, s_bits, s_slab);
