@@ -1170,6 +1170,177 @@ __global__ void __launch_bounds__(256, 4) k_sweep(ChannelView c, float* __restri
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&st->touched, nt);
 }
 
+// Grouped sweep, for maps whose touched planes hold few updates: the same
+// finding stage and per-voxel rules as k_sweep, but eight lanes apply one
+// plane: lane `sub` of the group holds the 16-byte groups at positions sub
+// and sub + 8 of the plane (two planes per group at a time), so a warp's
+// loads and stores of four planes are four contiguous 128-byte runs
+// instead of 32 scattered groups. The new active word is the OR of the
+// group's lanes. On the batched workload's sparse planes (about 20 updates
+// per touched leaf) it takes 10% less time than k_sweep; on dense planes
+// (about 40) k_sweep, which keeps twice the loads in flight, is faster, and
+// the host picks by the update density of the previous sweep.
+__device__ __forceinline__ int quad_at(int pos)  // inverse of plane_quad
+{
+  return (pos & 8) | (((pos >> 1) & 1) << 2) | ((pos & 1) << 1) | ((pos >> 2) & 1);
+}
+
+template <bool kPerMap, bool kChanges>
+__global__ void __launch_bounds__(256, 3) k_sweep_grouped(ChannelView c, float* __restrict__ values,
+                                                          unsigned long long* __restrict__ active,
+                                                          uint32_t* __restrict__ flags,
+                                                          const int4* __restrict__ origin, LogOddsTable lt,
+                                                          ChangeView ch, DevStatus* st, int gated)
+{
+  constexpr int kUnroll = 2;
+  if (gated ? !marking_complete(st) : ld_relaxed_u32(&st->error) != 0u) return;
+  __shared__ SweepTask queue[8][kSweepQueue];
+  SweepTask* q        = queue[threadIdx.x >> 5];
+  const uint32_t nt   = *c.n_touched;
+  const int lane      = static_cast<int>(threadIdx.x & 31);
+  const uint32_t lt_m = lanemask_lt();
+  const int w         = lane & 7;
+  const uint32_t grp  = static_cast<uint32_t>(lane >> 3);
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nw   = (gridDim.x * blockDim.x) >> 5;
+  const int sub       = lane & 7;
+  const int qa = quad_at(sub), qb = quad_at(sub + 8);
+  constexpr uint32_t kTake = 4u * kUnroll;
+  unsigned long long n_upd = 0;
+  uint32_t head = 0, tail = 0;  // queued planes: [head, tail) modulo kSweepQueue
+  for (uint32_t base = warp * 4;; base += nw * 4)
+  {
+    const bool more = base < nt;  // warp-uniform
+    if (more)
+    {
+      const uint32_t i        = base + grp;
+      unsigned long long actw = 0ull, hitw = 0ull;
+      int slot                = 0;
+      int map                 = 0;
+      if (i < nt)
+      {
+        slot = c.touched[i];
+        if (kPerMap && w == 0) map = origin[slot].w;  // once per leaf
+        if (w == 0 && ld_ca_u32(flags + slot) == 0u) flags[slot] = 1u;
+        const unsigned long long* u = c.upd + static_cast<size_t>(slot) * 16;
+        hitw                        = u[8 + w];
+        actw                        = u[w] | hitw;
+        if (kChanges && actw == 0ull)
+        {
+          ch.words[static_cast<size_t>(slot) * 16 + w]     = 0ull;
+          ch.words[static_cast<size_t>(slot) * 16 + 8 + w] = 0ull;
+        }
+      }
+      if (kPerMap) map = __shfl_sync(0xffffffffu, map, lane & ~7);
+      const bool act    = actw != 0ull;
+      const unsigned am = __ballot_sync(0xffffffffu, act);
+      if (act)
+      {
+        SweepTask& k = q[(tail + static_cast<uint32_t>(__popc(am & lt_m))) % kSweepQueue];
+        k.actw       = actw;
+        k.hitw       = hitw;
+        k.slot       = slot;
+        k.w          = static_cast<short>(w);
+        k.map        = static_cast<short>(map);
+      }
+      tail += static_cast<uint32_t>(__popc(am));
+      __syncwarp();
+    }
+    while (tail - head >= kTake || (!more && tail != head))
+    {
+      const uint32_t n = min(kTake, tail - head);
+      SweepTask k[kUnroll];
+      float4 va[kUnroll], vb[kUnroll];
+      unsigned long long on_in[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u)
+      {
+        const uint32_t idx = static_cast<uint32_t>(u) * 4u + grp;
+        if (idx < n)
+        {
+          k[u] = q[(head + idx) % kSweepQueue];
+        }
+        else
+        {
+          k[u].actw = 0ull;
+          k[u].hitw = 0ull;
+          k[u].slot = 0;
+          k[u].w    = 0;
+          k[u].map  = 0;
+        }
+        const float4* vp =
+          reinterpret_cast<const float4*>(values + static_cast<size_t>(k[u].slot) * 512 + k[u].w * 64);
+        if ((k[u].actw >> (4 * qa)) & 0xfull) va[u] = vp[sub];
+        if ((k[u].actw >> (4 * qb)) & 0xfull) vb[u] = vp[sub + 8];
+        on_in[u] = idx < n ? active[static_cast<size_t>(k[u].slot) * 8 + k[u].w] : 0ull;
+      }
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u)
+      {
+        const uint32_t idx            = static_cast<uint32_t>(u) * 4u + grp;
+        const LogOdds lo              = kPerMap ? lt.table[k[u].map] : lt.lo0;
+        const unsigned long long actw = k[u].actw, hitw = k[u].hitw;
+        unsigned long long mine       = 0ull;
+        float4* vp = reinterpret_cast<float4*>(values + static_cast<size_t>(k[u].slot) * 512 + k[u].w * 64);
+#pragma unroll
+        for (int half = 0; half < 2; ++half)
+        {
+          const int qd      = half ? qb : qa;
+          const uint32_t a4 = static_cast<uint32_t>(actw >> (4 * qd)) & 0xfu;
+          if (!a4) continue;
+          const uint32_t h4 = static_cast<uint32_t>(hitw >> (4 * qd)) & 0xfu;
+          const float4 v4   = half ? vb[u] : va[u];
+          float vv[4]       = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+          {
+            if ((a4 >> j) & 1u)
+            {
+              const int bit = 4 * qd + j;
+              bool o        = (on_in[u] >> bit) & 1ull;
+              apply_update(vv[j], o, (h4 >> j) & 1u, lo);
+              if (o) mine |= 1ull << bit;
+            }
+          }
+          vp[half ? sub + 8 : sub] = make_float4(vv[0], vv[1], vv[2], vv[3]);
+        }
+        // The group's new bits (each lane holds its own eight voxels).
+        uint32_t mlo = static_cast<uint32_t>(mine), mhi = static_cast<uint32_t>(mine >> 32);
+#pragma unroll
+        for (int off = 1; off < 8; off <<= 1)
+        {
+          mlo |= __shfl_xor_sync(0xffffffffu, mlo, off);
+          mhi |= __shfl_xor_sync(0xffffffffu, mhi, off);
+        }
+        if (sub == 0 && idx < n)
+        {
+          const int slot = k[u].slot, pw = k[u].w;
+          const unsigned long long on =
+            (on_in[u] & ~actw) | ((static_cast<unsigned long long>(mhi) << 32) | mlo);
+          if (on != on_in[u]) active[static_cast<size_t>(slot) * 8 + pw] = on;
+          unsigned long long* up = c.upd + static_cast<size_t>(slot) * 16;
+          up[pw]                 = 0ull;
+          if (hitw) up[8 + pw] = 0ull;
+          if (kChanges)
+          {
+            const unsigned long long flip                    = on ^ on_in[u];
+            ch.words[static_cast<size_t>(slot) * 16 + pw]     = flip;
+            ch.words[static_cast<size_t>(slot) * 16 + 8 + pw] = flip & on;
+            if (flip && atomicExch(ch.epoch + slot, ch.cur) != ch.cur) ch.list[atomicAdd(ch.count, 1u)] = slot;
+          }
+          n_upd += static_cast<unsigned long long>(__popcll(actw));
+        }
+      }
+      head += n;
+      __syncwarp();
+    }
+    if (!more) break;
+  }
+  for (int off = 16; off > 0; off >>= 1) n_upd += __shfl_xor_sync(0xffffffffu, n_upd, off);
+  if (lane == 0 && n_upd) atomicAdd(&st->updates, n_upd);
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&st->touched, nt);
+}
+
 // Gathers the listed change leaves of map `map` (-1: all): origin and the 16
 // change words per leaf, one thread per word; out_n counts what was kept.
 __global__ void k_gather_changes(ChangeView ch, const int4* __restrict__ origin, int map, int4* __restrict__ out_o,

@@ -181,6 +181,12 @@ struct vdbg_map
   bool use_graph                   = true;
   cudaGraphExec_t graph            = nullptr;
   uint64_t graph_layout            = 0;
+  bool graph_grouped               = false;  // the sweep kernel the captured step holds
+  // Sweep kernel choice by the update density (updated voxels per touched
+  // leaf) of the previous sweep: k_sweep_grouped below kGroupedBelow, back
+  // to k_sweep above kGroupedAbove (a gap, so the choice does not flip
+  // between steps of similar scans).
+  bool sweep_grouped               = false;
   const char** d_pts_ref           = nullptr;  // the step's points address (batch), read by k_prep
   const char** h_pts_ref           = nullptr;  // pinned staging
   int64_t graph_stride             = 0;
@@ -687,9 +693,18 @@ void fill_stats(vdbg_map* m, uint32_t leaves_before, vdbg_scan_stats* st)
   st->device_ms = m->timings.total_ms;
 }
 
+constexpr double kGroupedBelow = 30.0;
+constexpr double kGroupedAbove = 36.0;
+
 void record_timings(vdbg_map* m)
 {
   m->timings.runs = m->h_status->runs;
+  if (m->h_status->touched > 0u && m->h_status->updates > 0u)
+  {
+    const double density = static_cast<double>(m->h_status->updates) / static_cast<double>(m->h_status->touched);
+    if (!m->sweep_grouped && density < kGroupedBelow) m->sweep_grouped = true;
+    if (m->sweep_grouped && density > kGroupedAbove) m->sweep_grouped = false;
+  }
   float ms = 0.f;
   cudaEventElapsedTime(&ms, m->ev0, m->ev1);
   m->timings.total_ms = ms;
@@ -1107,7 +1122,22 @@ int launch_sweep(vdbg_map* m, Channel& c, cudaStream_t s, bool gated = false)
     ch.cur   = m->chg_cur;
   }
   const ChannelView cv = channel_view(c);
-  if (m->batch && m->track_changes)
+  if (m->sweep_grouped)
+  {
+    if (m->batch && m->track_changes)
+      k_sweep_grouped<true, true><<<kSweepBlocks, kSweepThreads, 0, s>>>(cv, m->values, m->active, m->flags,
+                                                                         m->origin, lt, ch, m->d_status, g);
+    else if (m->batch)
+      k_sweep_grouped<true, false><<<kSweepBlocks, kSweepThreads, 0, s>>>(cv, m->values, m->active, m->flags,
+                                                                          m->origin, lt, ch, m->d_status, g);
+    else if (m->track_changes)
+      k_sweep_grouped<false, true><<<kSweepBlocks, kSweepThreads, 0, s>>>(cv, m->values, m->active, m->flags,
+                                                                          m->origin, lt, ch, m->d_status, g);
+    else
+      k_sweep_grouped<false, false><<<kSweepBlocks, kSweepThreads, 0, s>>>(cv, m->values, m->active, m->flags,
+                                                                           m->origin, lt, ch, m->d_status, g);
+  }
+  else if (m->batch && m->track_changes)
     k_sweep<true, true><<<kSweepBlocks, kSweepThreads, 0, s>>>(cv, m->values, m->active, m->flags, m->origin, lt, ch,
                                                                m->d_status, g);
   else if (m->batch)
@@ -1546,7 +1576,8 @@ int capture_step(vdbg_map* m, Channel& c, int64_t stride, const ScanTable& t, co
     m->graph = nullptr;
     return ei == cudaErrorMemoryAllocation ? oom("cudaGraphInstantiate") : VDBG_ERR_CUDA;
   }
-  m->graph_layout = m->layout;
+  m->graph_layout  = m->layout;
+  m->graph_grouped = m->sweep_grouped;
   m->graph_stride = stride;
   m->graph_captures += 1;
   return VDBG_OK;
@@ -1572,7 +1603,7 @@ int graph_step(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t str
   *m->h_pts_ref = pts;
   VDBG_CUDA(cudaMemcpyAsync(m->d_pts_ref, m->h_pts_ref, sizeof(const char*), cudaMemcpyHostToDevice, s));
   c.pending = true;
-  if (!m->graph || m->graph_layout != m->layout || m->graph_stride != stride)
+  if (!m->graph || m->graph_layout != m->layout || m->graph_stride != stride || m->graph_grouped != m->sweep_grouped)
     VDBG_TRY(capture_step(m, c, stride, t, rb, s));
   VDBG_CUDA(cudaGraphLaunch(m->graph, s));
   m->graph_replays += 1;
