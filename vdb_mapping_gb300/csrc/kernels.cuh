@@ -1865,7 +1865,6 @@ struct DevTopo
 {
   TopoView tv;
   MapView m;
-  const uint32_t* flags;
   mutable int cbx, cby, cbz, cb;  // last block coordinate and its index (-1: none)
   mutable int cw = -1;            // word of cb's leaf bitmap held in `bits` (-1: none)
   mutable unsigned long long bits = 0ull;
@@ -2017,8 +2016,7 @@ __device__ __forceinline__ void fast_ray(const int4& r, const ScanGeom& g, doubl
 }
 
 __global__ void __launch_bounds__(128) k_fast_spans(const int4* __restrict__ rays, const int* __restrict__ order,
-                                                    ScanTable t, MapView m, TopoView tv,
-                                                    const uint32_t* __restrict__ flags, SpanBuf sb)
+                                                    ScanTable t, MapView m, TopoView tv, SpanBuf sb)
 {
   // (read once per warp: the warp reduces below)
   const int lane = static_cast<int>(threadIdx.x & 31);
@@ -2039,7 +2037,7 @@ __global__ void __launch_bounds__(128) k_fast_spans(const int4* __restrict__ ray
       fast_ray(r, g, eye, dir);
       hdda::Ray ray = hdda::make_ray(eye, dir, 0.0, 1.0);
       hdda::clip(ray, topo_box(tv).lo, topo_box(tv).hi_excl);
-      DevTopo topo{tv, m, flags, 0x7fffffff, 0, 0, -1};
+      DevTopo topo{tv, m, 0x7fffffff, 0, 0, -1};
       uint32_t steps = 0;
       const double l1 = fabs(dir[0]) + fabs(dir[1]) + fabs(dir[2]);  // voxels per unit t
       const int w     = hdda::all_spans(ray, topo, steps, [&](const hdda::Span& sp) {
@@ -2288,7 +2286,6 @@ __global__ void __launch_bounds__(256) k_trace_scatter(const unsigned short* __r
 
 __global__ void __launch_bounds__(128) k_trace_spans(const double* __restrict__ q, uint32_t n, double res,
                                                      double inv_res, MapView m, TopoView tv,
-                                                     const uint32_t* __restrict__ flags,
                                                      const uint32_t* __restrict__ order,
                                                      unsigned char* __restrict__ ok, double* __restrict__ end,
                                                      SpanBuf sb)
@@ -2311,7 +2308,7 @@ __global__ void __launch_bounds__(128) k_trace_spans(const double* __restrict__ 
     trace_answer(ok, end, i, false, zero);
     return;
   }
-  DevTopo topo{tv, m, flags, 0x7fffffff, 0, 0, -1};
+  DevTopo topo{tv, m, 0x7fffffff, 0, 0, -1};
   hdda::Span sp{-1.0, -1.0};
   bool found     = false;
   uint32_t steps = 0;

@@ -1421,8 +1421,7 @@ int run_fast_marking(vdbg_map* m, Channel& c, const int4* rays, const int* order
     VDBG_TRY(ensure_span_buffers(m, want));
     VDBG_CUDA(cudaMemsetAsync(m->fast_ctr, 0, 2 * sizeof(unsigned long long), s));
     SpanBuf sb{m->fast_spans, m->fast_cap, reinterpret_cast<uint32_t*>(m->fast_ctr), m->fast_ctr + 1};
-    k_fast_spans<<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(rays, order, t, map_view(m), tv, m->flags,
-                                                                         sb);
+    k_fast_spans<<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(rays, order, t, map_view(m), tv, sb);
     VDBG_CUDA(cudaGetLastError());
     m->timings.launches += 1;
     VDBG_CUDA(cudaMemcpyAsync(&spans, m->fast_ctr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -3093,8 +3092,8 @@ int vdbg_raytrace(vdbg_map* m, int map, int64_t n, const double* origins, const 
   k_trace_offsets<<<1, 1024, 0, s>>>(bin_hist);
   k_trace_scatter<<<(n32 + 255) / 256, 256, 0, s>>>(bins, n32, bin_hist, order);
   const SpanBuf sb{m->fast_spans, m->fast_cap, reinterpret_cast<uint32_t*>(m->fast_ctr), m->fast_ctr + 1};
-  k_trace_spans<<<(n32 + 127) / 128, 128, 0, s>>>(q, n32, mc.resolution, mc.inv_res, map_view(m), tv, m->flags,
-                                                 order, ok, end, sb);
+  k_trace_spans<<<(n32 + 127) / 128, 128, 0, s>>>(q, n32, mc.resolution, mc.inv_res, map_view(m), tv, order, ok,
+                                                 end, sb);
   VDBG_CUDA(cudaGetLastError());
   uint32_t spans = 0;
   VDBG_CUDA(cudaMemcpyAsync(&spans, m->fast_ctr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
