@@ -1176,10 +1176,11 @@ __global__ void __launch_bounds__(256, 4) k_sweep(ChannelView c, float* __restri
 // and sub + 8 of the plane (two planes per group at a time), so a warp's
 // loads and stores of four planes are four contiguous 128-byte runs
 // instead of 32 scattered groups. The new active word is the OR of the
-// group's lanes. On the batched workload's sparse planes (about 20 updates
-// per touched leaf) it takes 10% less time than k_sweep; on dense planes
-// (about 40) k_sweep, which keeps twice the loads in flight, is faster, and
-// the host picks by the update density of the previous sweep.
+// group's lanes. On the batched workload's planes (about 20 updates per
+// touched leaf) it takes 10% less time than k_sweep; on dense planes (about
+// 40) k_sweep, which keeps twice the loads in flight, is faster, and on very
+// sparse ones (about 9, one update per plane) its per-plane overhead makes
+// it slower too. The host picks by the update density of the previous sweep.
 __device__ __forceinline__ int quad_at(int pos)  // inverse of plane_quad
 {
   return (pos & 8) | (((pos >> 1) & 1) << 2) | ((pos & 1) << 1) | ((pos >> 2) & 1);

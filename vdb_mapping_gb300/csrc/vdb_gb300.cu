@@ -183,9 +183,9 @@ struct vdbg_map
   uint64_t graph_layout            = 0;
   bool graph_grouped               = false;  // the sweep kernel the captured step holds
   // Sweep kernel choice by the update density (updated voxels per touched
-  // leaf) of the previous sweep: k_sweep_grouped below kGroupedBelow, back
-  // to k_sweep above kGroupedAbove (a gap, so the choice does not flip
-  // between steps of similar scans).
+  // leaf) of the previous sweep: k_sweep_grouped inside a band of medium
+  // densities, k_sweep outside it (the band's edges have gaps, so the
+  // choice does not flip between steps of similar scans).
   bool sweep_grouped               = false;
   const char** d_pts_ref           = nullptr;  // the step's points address (batch), read by k_prep
   const char** h_pts_ref           = nullptr;  // pinned staging
@@ -693,8 +693,16 @@ void fill_stats(vdbg_map* m, uint32_t leaves_before, vdbg_scan_stats* st)
   st->device_ms = m->timings.total_ms;
 }
 
-constexpr double kGroupedBelow = 30.0;
-constexpr double kGroupedAbove = 36.0;
+// The grouped sweep's band, in updated voxels per touched leaf. Measured on
+// one GB300: the grouped sweep takes 10% less time at 20-25 (the batched
+// workload's maps), 27% more at 42 (dense street scans) and also more at 9
+// (precision-stress scans into an empty map, about one update per plane,
+// where its per-plane overhead dominates). Entered inside [16, 30), left
+// outside [13, 36).
+constexpr double kGroupedEnterLo = 16.0;
+constexpr double kGroupedEnterHi = 30.0;
+constexpr double kGroupedLeaveLo = 13.0;
+constexpr double kGroupedLeaveHi = 36.0;
 
 void record_timings(vdbg_map* m)
 {
@@ -702,8 +710,8 @@ void record_timings(vdbg_map* m)
   if (m->h_status->touched > 0u && m->h_status->updates > 0u)
   {
     const double density = static_cast<double>(m->h_status->updates) / static_cast<double>(m->h_status->touched);
-    if (!m->sweep_grouped && density < kGroupedBelow) m->sweep_grouped = true;
-    if (m->sweep_grouped && density > kGroupedAbove) m->sweep_grouped = false;
+    if (!m->sweep_grouped && density >= kGroupedEnterLo && density < kGroupedEnterHi) m->sweep_grouped = true;
+    if (m->sweep_grouped && (density < kGroupedLeaveLo || density > kGroupedLeaveHi)) m->sweep_grouped = false;
   }
   float ms = 0.f;
   cudaEventElapsedTime(&ms, m->ev0, m->ev1);
