@@ -1,6 +1,6 @@
 """The kernels' tuning parameters change speed only: maps inserted under
-different tunings are bit-identical, and the autotuner returns a valid
-tuning from its candidate set."""
+different tunings (both sweep kernels forced among them) are bit-identical,
+and the autotuner returns a valid tuning from its candidate set."""
 import numpy as np
 import pytest
 
@@ -17,6 +17,8 @@ TUNINGS = [
      "dda_warps_per_sm": 2},
     {"rays_per_take": 32, "apply_chunk_runs": 4096, "length_edges": (4096, 64, 8), "hash_load": 0.1,
      "dda_warps_per_sm": 8},
+    dict(autotune.DEFAULT, sweep_kernel=1),  # one z-plane per lane
+    dict(autotune.DEFAULT, sweep_kernel=2),  # eight lanes per z-plane
 ]
 
 
@@ -62,7 +64,8 @@ def test_invalid_tunings_rejected(vdbg):
            dict(autotune.DEFAULT, apply_chunk_runs=100), dict(autotune.DEFAULT, apply_chunk_runs=8192),
            dict(autotune.DEFAULT, apply_chunk_runs=1000), dict(autotune.DEFAULT, dda_warps_per_sm=7),
            dict(autotune.DEFAULT, dda_warps_per_sm=22),
-           dict(autotune.DEFAULT, length_edges=(256, 512, 1024)), dict(autotune.DEFAULT, hash_load=0.95)]
+           dict(autotune.DEFAULT, length_edges=(256, 512, 1024)), dict(autotune.DEFAULT, hash_load=0.95),
+           dict(autotune.DEFAULT, sweep_kernel=3)]
     for t in bad:
         with pytest.raises(VdbgError):
             m.setTuning(t)

@@ -96,12 +96,13 @@ class vdbg_tuning(C.Structure):
         ("length_edges", C.c_int32 * 3),
         ("hash_load", C.c_float),
         ("dda_warps_per_sm", C.c_int32),
+        ("sweep_kernel", C.c_int32),
     ]
 
     def as_dict(self):
         return {"rays_per_take": self.rays_per_take, "apply_chunk_runs": self.apply_chunk_runs,
                 "length_edges": tuple(self.length_edges), "hash_load": round(float(self.hash_load), 4),
-                "dda_warps_per_sm": self.dda_warps_per_sm}
+                "dda_warps_per_sm": self.dda_warps_per_sm, "sweep_kernel": self.sweep_kernel}
 
     @classmethod
     def from_dict(cls, d):
@@ -112,6 +113,7 @@ class vdbg_tuning(C.Structure):
             t.length_edges[k] = int(d["length_edges"][k])
         t.hash_load = float(d["hash_load"])
         t.dda_warps_per_sm = int(d.get("dda_warps_per_sm", 16))
+        t.sweep_kernel = int(d.get("sweep_kernel", 0))
         return t
 
 

@@ -14,7 +14,7 @@ from __future__ import annotations
 import statistics
 
 DEFAULT = {"rays_per_take": 32, "apply_chunk_runs": 2048, "length_edges": (2048, 1024, 512), "hash_load": 0.5,
-           "dda_warps_per_sm": 16}
+           "dda_warps_per_sm": 16, "sweep_kernel": 0}
 
 CANDIDATES = {
     "rays_per_take": (8, 16, 32),

@@ -163,7 +163,7 @@ struct vdbg_map
   int64_t bytes         = 0;
   uint64_t run_budget   = 2ull << 30;  // run buffer bytes the map may grow to
   int num_sms           = 152;
-  vdbg_tuning tuning{32, 2048, {2048, 1024, 512}, 0.5f, 16};
+  vdbg_tuning tuning{32, 2048, {2048, 1024, 512}, 0.5f, 16, 0};
   uint32_t apply_grid_chunk = 0;   // apply_chunk the cached grid size is for
   unsigned apply_grid_blocks = 0;
   // Change set of the last integration (vdbg_track_changes).
@@ -693,6 +693,14 @@ void fill_stats(vdbg_map* m, uint32_t leaves_before, vdbg_scan_stats* st)
   st->device_ms = m->timings.total_ms;
 }
 
+// The sweep kernel of the map's next sweep (the tuning may fix it).
+bool use_grouped_sweep(const vdbg_map* m)
+{
+  if (m->tuning.sweep_kernel == 1) return false;
+  if (m->tuning.sweep_kernel == 2) return true;
+  return m->sweep_grouped;
+}
+
 // The grouped sweep's band, in updated voxels per touched leaf. Measured on
 // one GB300: the grouped sweep takes 10% less time at 20-25 (the batched
 // workload's maps), 27% more at 42 (dense street scans) and also more at 9
@@ -1130,7 +1138,7 @@ int launch_sweep(vdbg_map* m, Channel& c, cudaStream_t s, bool gated = false)
     ch.cur   = m->chg_cur;
   }
   const ChannelView cv = channel_view(c);
-  if (m->sweep_grouped)
+  if (use_grouped_sweep(m))
   {
     if (m->batch && m->track_changes)
       k_sweep_grouped<true, true><<<kSweepBlocks, kSweepThreads, 0, s>>>(cv, m->values, m->active, m->flags,
@@ -1584,7 +1592,7 @@ int capture_step(vdbg_map* m, Channel& c, int64_t stride, const ScanTable& t, co
     return ei == cudaErrorMemoryAllocation ? oom("cudaGraphInstantiate") : VDBG_ERR_CUDA;
   }
   m->graph_layout  = m->layout;
-  m->graph_grouped = m->sweep_grouped;
+  m->graph_grouped = use_grouped_sweep(m);
   m->graph_stride = stride;
   m->graph_captures += 1;
   return VDBG_OK;
@@ -1610,7 +1618,7 @@ int graph_step(vdbg_map* m, Channel& c, const float* xyz, int64_t n, int64_t str
   *m->h_pts_ref = pts;
   VDBG_CUDA(cudaMemcpyAsync(m->d_pts_ref, m->h_pts_ref, sizeof(const char*), cudaMemcpyHostToDevice, s));
   c.pending = true;
-  if (!m->graph || m->graph_layout != m->layout || m->graph_stride != stride || m->graph_grouped != m->sweep_grouped)
+  if (!m->graph || m->graph_layout != m->layout || m->graph_stride != stride || m->graph_grouped != use_grouped_sweep(m))
     VDBG_TRY(capture_step(m, c, stride, t, rb, s));
   VDBG_CUDA(cudaGraphLaunch(m->graph, s));
   m->graph_replays += 1;
@@ -2448,6 +2456,7 @@ int vdbg_set_tuning(vdbg_map* m, const vdbg_tuning* t)
   if (!(t->hash_load > 0.05f && t->hash_load <= 0.9f)) return VDBG_ERR_INVALID_ARGUMENT;
   if (t->dda_warps_per_sm < kDdaWarps || t->dda_warps_per_sm > 10 * kDdaWarps || (t->dda_warps_per_sm % kDdaWarps))
     return VDBG_ERR_INVALID_ARGUMENT;
+  if (t->sweep_kernel < 0 || t->sweep_kernel > 2) return VDBG_ERR_INVALID_ARGUMENT;
   VDBG_TRY(set_device(m));
   VDBG_CUDA(cudaStreamSynchronize(m->stream));
   VDBG_TRY(publish_growth(m, m->stream));
