@@ -66,6 +66,41 @@ def test_struct_layouts_match_header():
     assert C.sizeof(_lib.vdbg_scan_stats) == 64
 
 
+STRUCTS = ("vdbg_config", "vdbg_options", "vdbg_scan_stats", "vdbg_timings", "vdbg_pool_info", "vdbg_tuning",
+           "vdbg_server_options", "vdbg_server_result", "vdbg_server_stats")
+
+
+def test_ctypes_mirrors_match_the_compiled_header(tmp_path):
+    """Every struct of include/vdb_gb300.h, compiled by the C compiler: its
+    size and every field's offset equal the ctypes mirror's."""
+    from vdb_mapping_gb300 import _lib
+
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "vdb_gb300.h"', "int main(void) {"]
+    for name in STRUCTS:
+        cls = getattr(_lib, name)
+        lines.append(f'  printf("{name} size %zu\\n", sizeof({name}));')
+        for field, _ in cls._fields_:
+            lines.append(f'  printf("{name} {field} %zu\\n", offsetof({name}, {field}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layouts.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layouts"
+    include = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    res = subprocess.run(["gcc", "-std=c11", "-I", include, str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {}
+    for line in out:
+        if line:
+            *key, value = line.split()
+            got[tuple(key)] = int(value)
+    for name in STRUCTS:
+        cls = getattr(_lib, name)
+        assert got[(name, "size")] == C.sizeof(cls), name
+        for field, _ in cls._fields_:
+            assert got[(name, field)] == getattr(cls, field).offset, (name, field)
+
+
 def test_build_targets_sm_103a_only():
     from vdb_mapping_gb300 import build
 
