@@ -247,8 +247,9 @@ typedef struct vdbg_tuning
   int32_t length_edges[3];   /* L1 lengths (voxels) starting the sort's length classes, descending (2048, 1024, 512) */
   float hash_load;           /* block-hash load factor (0.05-0.9; 0.5); a change rebuilds the hash */
   int32_t dda_warps_per_sm;  /* resident DDA warps per SM (2-20, even; 16) */
-  int32_t sweep_kernel;      /* 0: picked by the previous sweep's updates per touched leaf (default);
-                                1: one z-plane per lane; 2: eight lanes per z-plane */
+  int32_t sweep_kernel;      /* 0 (default): one z-plane per lane, or for a batch of maps eight lanes
+                                per z-plane when its previous sweep updated 16-30 voxels per touched
+                                leaf; 1: one z-plane per lane; 2: eight lanes per z-plane */
 } vdbg_tuning;
 
 int vdbg_set_tuning(vdbg_map* map, const vdbg_tuning* tuning);

@@ -693,12 +693,17 @@ void fill_stats(vdbg_map* m, uint32_t leaves_before, vdbg_scan_stats* st)
   st->device_ms = m->timings.total_ms;
 }
 
-// The sweep kernel of the map's next sweep (the tuning may fix it).
+// The sweep kernel of the map's next sweep (the tuning may fix it). By
+// default the grouped sweep is picked for batches of maps only, where it was
+// measured faster inside the density band; on single maps it was measured
+// slower at 26 updates per touched leaf (a dense street scan at a quarter of
+// its rays: 384 against 255 us under ncu), so updates per leaf do not
+// predict it there.
 bool use_grouped_sweep(const vdbg_map* m)
 {
   if (m->tuning.sweep_kernel == 1) return false;
   if (m->tuning.sweep_kernel == 2) return true;
-  return m->sweep_grouped;
+  return m->batch && m->sweep_grouped;
 }
 
 // The grouped sweep's band, in updated voxels per touched leaf. Measured on
